@@ -1,0 +1,335 @@
+"""Benchmark: DOF x Newton-steps per second of the implicit time step on one GB300.
+
+Workload (the configuration the headline metric is quoted on): seeded Gray-Scott,
+2 species, unit square 512 x 512 P1 triangles (526,338 DOF), Alexander2 DIRK dt = 1,
+Newton relative tolerance 1e-10 (squared l2, as the reference), direct-solve semantics
+(the reference's default UMFPack is replaced by BiCGSTAB converged to 1e-13).
+
+A "step" is one Alexander2 time step (2 stages x Newton iterations).  Timed per step with
+CUDA events on the engine's stream (dc_step_info.device_ms); the L2 cache is flushed
+between timed steps (a 256 MiB write).  value = DOF x Newton iterations of all timed
+steps / sum of device step times.  e2e = the same through the public C ABI with host
+buffers: state upload (pinned->device), step, state download, host-timed.
+
+--impl reference times the CPU restatement of the reference algorithm (numpy assembly +
+SuperLU direct solve, the oracle) on the host cores, one Newton iteration of the full
+workload per step.
+
+Multi-GPU: independent replicas (one model per rank), no collective; scaling "weak".
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "dune-copasi_gb300")
+for p in (ROOT, PKG):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+METRIC = "DOF·Newton-steps/s"
+WORKLOAD = "gray_scott_512x512_p1_alexander2_dt1"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=512)
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_setup(args):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        # one GPU per rank: restrict the rank's view before any CUDA initialisation
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    return rank, world
+
+
+def make_workload(n):
+    import workloads as W
+    return W.gray_scott(n=n, steps=100000, dt=1.0)
+
+
+def initial_vector(ini, init):
+    """Seeded initial state in the reference DOF order (built with the oracle's layout rules,
+    which the engine shares: compartment-major, vertex-major, species interleaved)."""
+    import numpy as np
+    from oracle.mesh import Mesh
+    from oracle.ini import ParameterTree
+    cfg = ParameterTree.from_text(ini)
+    mesh = Mesh.from_config(cfg.sub("grid"))
+    nv = mesh.nv
+    x = np.empty(2 * nv)
+    x[0::2] = init("u", mesh.coords)
+    x[1::2] = init("v", mesh.coords)
+    return x
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.QUERY, "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": []}
+        if self.proc is None:
+            return out
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if sm:
+            out = {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                   "samples": len(sm)}
+        return out
+
+
+def cpu_baseline(ini, init, newton_steps=1):
+    """Oracle (numpy assembly + SuperLU) on the host: one Newton iteration of the full workload."""
+    import numpy as np
+    from oracle.model import OracleModel
+    om = OracleModel(ini)
+    x0 = initial_vector(ini, init)
+    a = 1.0 - 0.5 * 2 ** 0.5
+    t0 = time.perf_counter()
+    for _ in range(newton_steps):
+        r = om.residual(x0, a, "mass") + a * om.residual(x0, a, "stiffness")
+        J = om.jacobian(x0, a, "mass") + a * om.jacobian(x0, a, "stiffness")
+        z = om._solve(J, r)
+        x0 = x0 - z
+    dt = time.perf_counter() - t0
+    return {"value": om.ndof * newton_steps / dt, "unit": METRIC, "cores": 1, "kind": "port",
+            "sample": "%d Newton iteration(s) (residual + Jacobian assembly + SuperLU solve) of the "
+                      "%d-DOF Gray-Scott stage system, first Alexander2 stage" % (newton_steps, om.ndof),
+            "seconds": dt}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    ini, init = make_workload(args.n)
+    from oracle.model import OracleModel
+    om = OracleModel(ini)
+    x = initial_vector(ini, init)
+    a = 1.0 - 0.5 * 2 ** 0.5
+    times = []
+    for k in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        r = om.residual(x, a, "mass") + a * om.residual(x, a, "stiffness")
+        J = om.jacobian(x, a, "mass") + a * om.jacobian(x, a, "stiffness")
+        z = om._solve(J, r)
+        x = x - z
+        t1 = time.perf_counter()
+        if k >= args.warmup:
+            times.append(t1 - t0)
+    total = sum(times)
+    value = om.ndof * len(times) / total
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded Gray-Scott initial perturbation)",
+            "config": {"workload": WORKLOAD, "dof": om.ndof, "step": "one Newton iteration (assembly + SuperLU)"},
+            "cpu_baseline": {"value": value, "unit": METRIC, "cores": 1, "kind": "port",
+                             "sample": "one Newton iteration of the full workload per step"},
+            "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def spmv_bytes(ndof, nnzb, bs, nrows, vbytes):
+    """Algorithmic bytes of one BSR SpMV: values + block column indices + row pointers +
+    x read once + y written once."""
+    return nnzb * (bs * bs * vbytes + 4) + (nrows + 1) * 4 + 2 * ndof * vbytes
+
+
+def assembly_bytes(ne, nl, ns, ndof, nnz, jac):
+    """Algorithmic bytes of one residual (+ Jacobian) assembly pass: cell vertex and node
+    indices, vertex coordinates and coefficients gathered once per cell, residual written
+    once, Jacobian values written once (colour-ordered, no read-back)."""
+    b = ne * (nl * 4 * 2 + nl * ns * 8) + ndof * 8
+    if jac:
+        b += nnz * 8 + ne * nl * nl * 4
+    return b
+
+
+def main():
+    args = parse()
+    rank, world = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    import numpy as np
+    import torch
+    import __graft_entry__ as g
+    g.build()
+    import dcgpu
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+
+    ini, init = make_workload(args.n)
+    model = dcgpu.Model(ini)
+    if args.precision == "mixed":
+        model.set_mixed_precision(True)
+    x0 = initial_vector(ini, init)
+    ndof = model.ndof
+    model.set_state(x0, 0.0)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+
+    dt = 1.0
+    for _ in range(args.warmup):
+        dt = model.step(dt)["dt_next"]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+
+    model.profile(True)
+    clocks = ClockSampler()
+    clocks.start()
+    launches0 = dcgpu.launch_count()
+    dev_ms = []
+    newton = 0
+    linear = 0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        info = model.step(dt)
+        dt = info["dt_next"]
+        dev_ms.append(info["device_ms"])
+        newton += info["newton_iterations"]
+        linear += info["linear_iterations"]
+    launches = dcgpu.launch_count() - launches0
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    kt = model.kernel_times()
+    model.profile(False)
+    total_ms = sum(dev_ms)
+    if dist:
+        t = torch.tensor([total_ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * ndof * newton / (total_ms * 1e-3)
+
+    # end to end through the C ABI with host buffers (upload, step, download)
+    xs = model.state()
+    e2e_t = 0.0
+    e2e_newton = 0
+    nrep = max(2, min(args.steps, 5))
+    for _ in range(nrep):
+        t0 = time.perf_counter()
+        model.set_state(xs, model.time())
+        info = model.step(dt)
+        xs = model.state()
+        e2e_t += time.perf_counter() - t0
+        e2e_newton += info["newton_iterations"]
+        dt = info["dt_next"]
+    e2e = {"value": world * ndof * e2e_newton / e2e_t, "unit": METRIC,
+           "h2d_bytes_per_step": ndof * 8, "d2h_bytes_per_step": ndof * 8}
+
+    # roofline of the dominant kernel category
+    import json as _j
+    peaks = {}
+    try:
+        peaks = _j.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        peak_gbs = float(peaks["hbm_gbs"])
+        peak_src = "measured"
+    except Exception:
+        peak_gbs = 6800.0
+        peak_src = "fallback"
+    info_m = model.info
+    bs = info_m["block_size"]
+    nrows = info_m["n_block_rows"]
+    nnzb = info_m["n_blocks"]
+    ne = info_m["n_elements"]
+    vbytes = 4 if args.precision == "mixed" else 8
+    cats = {}
+    for name, (ms, calls) in kt.items():
+        if calls:
+            cats[name] = (ms, calls)
+    dom = max(cats, key=lambda k: cats[k][0]) if cats else "spmv"
+    ms, calls = cats.get(dom, (0.0, 1))
+    avg_s = ms * 1e-3 / max(calls, 1)
+    if dom == "spmv":
+        alg = spmv_bytes(ndof, nnzb, bs, nrows, vbytes)
+    elif dom == "assembly":
+        alg = assembly_bytes(ne, 3, 2, ndof, nnzb * bs * bs, jac=True)
+    else:
+        alg = nrows * bs * bs * vbytes + 2 * ndof * vbytes
+    achieved = alg / avg_s / 1e9 if avg_s > 0 else 0.0
+    roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak_gbs, "unit": "GB/s",
+            "frac": achieved / peak_gbs, "peak_source": peak_src, "traffic": None,
+            "algorithmic_bytes_per_launch": alg, "avg_launch_us": avg_s * 1e6, "launches": calls,
+            "category_ms": {k: v[0] for k, v in cats.items()},
+            "category_launches": {k: v[1] for k, v in cats.items()}}
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(ini, init)
+    line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f64+f32",
+            "data": "synthetic (seeded Gray-Scott initial perturbation, no dataset)",
+            "config": {"workload": WORKLOAD, "mesh": "%dx%d P1 triangles" % (args.n, args.n), "dof": ndof,
+                       "species": 2, "scheme": "Alexander2", "dt": 1.0, "precision": args.precision,
+                       "linear_solver": "BiCGSTAB+block-Jacobi to 1e-13 (direct-solve semantics)",
+                       "newton_rel_tol_sq": 1e-10, "l2_flush": "256 MiB write between timed steps",
+                       "newton_iterations": newton, "krylov_iterations": linear},
+            "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    model.close()
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

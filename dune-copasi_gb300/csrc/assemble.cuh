@@ -1,0 +1,27 @@
+// P1 residual / Jacobian assembly kernels (sm_103a).
+//
+// One thread per element of one colour class: the element gathers its vertex
+// coordinates and coefficients, evaluates the compiled expression program at each
+// quadrature point, accumulates its local residual and Jacobian coefficients, and adds
+// them into the global residual / BSR values.  Elements of one colour share no vertex,
+// so the read-modify-write scatter is race-free without atomics; the colour classes run
+// as consecutive launches.  Restates local_operator.hh:417-491 (residual) and :541-707
+// (analytic Jacobian); the face kernel restates :777-971 and :973-1203.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "device.cuh"
+
+namespace dcgpu {
+
+// mode bit 1: residual, bit 2: Jacobian
+void launch_volume(int dim, int ns, const VolumeParams& p, int begin, int end, int mode,
+                   cudaStream_t stream);
+void launch_faces(int dim, const FaceParams& p, int begin, int end, int mode, cudaStream_t stream);
+// J[diag[i]] block gets identity in the padded slots s >= ns_of_row (rows of compartments
+// with fewer species than the block size)
+void launch_pad_identity(const int32_t* diag, const int8_t* row_ns, int nrows, int bs, double* J,
+                         double value, cudaStream_t stream);
+
+}  // namespace dcgpu

@@ -1,0 +1,254 @@
+// Interface / boundary outflow assembly (local_operator.hh:777-971 residual,
+// :973-1203 analytic Jacobian, :1398-1436 boundary).
+//
+// One thread per face of one colour class.  On a conforming P1 face the basis functions
+// of both neighbouring cells restrict to the face barycentric coordinates, so the
+// coefficients of the face vertices of each side's compartment give the values at the
+// face quadrature points; gradients (only loaded when a program reads them) come from
+// the full neighbouring cells.  Values of species living on the other side are taken at
+// the same physical point through the other side's own cell.
+#include <stdexcept>
+
+#include "assemble.cuh"
+#include "interp.cuh"
+#include "linalg.cuh"
+
+namespace dcgpu {
+
+namespace {
+
+constexpr int kFaceMaxSpecies = 8;
+
+template <int DIM> struct FaceRule;
+template <> struct FaceRule<2> {
+  static constexpr int NQ = 2;
+  __device__ static double lam(int q, int k) {
+    const double s = (q == 0) ? 0.5 - 0.28867513459481288225 : 0.5 + 0.28867513459481288225;
+    return k == 0 ? 1.0 - s : s;
+  }
+  __device__ static constexpr double w(int) { return 0.5; }
+};
+template <> struct FaceRule<3> {
+  static constexpr int NQ = 3;
+  __device__ static double lam(int q, int k) {
+    const double x0 = (q == 0) ? 2.0 / 3.0 : 1.0 / 6.0;
+    const double x1 = (q == 1) ? 2.0 / 3.0 : 1.0 / 6.0;
+    return k == 0 ? 1.0 - x0 - x1 : (k == 1 ? x0 : x1);
+  }
+  __device__ static constexpr double w(int) { return 1.0 / 6.0; }
+};
+
+// gradient of the species of one side inside cell e (P1, affine)
+template <int DIM>
+__device__ void cell_gradients(const FaceParams& P, int side, int e, int ns, double (*grad)[3]) {
+  constexpr int NL = DIM + 1;
+  double X[NL][DIM];
+  int nd[NL];
+  for (int a = 0; a < NL; ++a) {
+    const int v = P.cells[static_cast<int64_t>(e) * NL + a];
+    nd[a] = P.vnode[side][v];
+    for (int d = 0; d < DIM; ++d) X[a][d] = P.coords[static_cast<int64_t>(v) * DIM + d];
+  }
+  double Bm[DIM][DIM], Bi[DIM][DIM];
+  for (int i = 0; i < DIM; ++i)
+    for (int j = 0; j < DIM; ++j) Bm[i][j] = X[j + 1][i] - X[0][i];
+  if constexpr (DIM == 2) {
+    const double det = Bm[0][0] * Bm[1][1] - Bm[0][1] * Bm[1][0];
+    Bi[0][0] = Bm[1][1] / det;  Bi[0][1] = -Bm[0][1] / det;
+    Bi[1][0] = -Bm[1][0] / det; Bi[1][1] = Bm[0][0] / det;
+  } else {
+    const double c00 = Bm[1][1] * Bm[2][2] - Bm[1][2] * Bm[2][1];
+    const double c01 = Bm[1][2] * Bm[2][0] - Bm[1][0] * Bm[2][2];
+    const double c02 = Bm[1][0] * Bm[2][1] - Bm[1][1] * Bm[2][0];
+    const double det = Bm[0][0] * c00 + Bm[0][1] * c01 + Bm[0][2] * c02;
+    Bi[0][0] = c00 / det; Bi[1][0] = c01 / det; Bi[2][0] = c02 / det;
+    Bi[0][1] = (Bm[0][2] * Bm[2][1] - Bm[0][1] * Bm[2][2]) / det;
+    Bi[1][1] = (Bm[0][0] * Bm[2][2] - Bm[0][2] * Bm[2][0]) / det;
+    Bi[2][1] = (Bm[0][1] * Bm[2][0] - Bm[0][0] * Bm[2][1]) / det;
+    Bi[0][2] = (Bm[0][1] * Bm[1][2] - Bm[0][2] * Bm[1][1]) / det;
+    Bi[1][2] = (Bm[0][2] * Bm[1][0] - Bm[0][0] * Bm[1][2]) / det;
+    Bi[2][2] = (Bm[0][0] * Bm[1][1] - Bm[0][1] * Bm[1][0]) / det;
+  }
+  double G[NL][DIM];
+  for (int j = 0; j < DIM; ++j) {
+    double s = 0.0;
+    for (int k = 0; k < DIM; ++k) { G[k + 1][j] = Bi[k][j]; s += Bi[k][j]; }
+    G[0][j] = -s;
+  }
+  for (int s = 0; s < ns; ++s)
+    for (int j = 0; j < 3; ++j) {
+      double acc = 0.0;
+      if (j < DIM)
+        for (int a = 0; a < NL; ++a)
+          acc += P.x[static_cast<int64_t>(nd[a]) * P.bs + s] * G[a][j];
+      grad[s][j] = acc;
+    }
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(128) k_faces(const FaceParams P, const int begin, const int end,
+                                               const int mode) {
+  constexpr int NF = DIM;
+  constexpr int NQ = FaceRule<DIM>::NQ;
+  const int f = begin + blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= end) return;
+  const bool has_out = P.elem_out[f] >= 0;
+  const int bs = P.bs, bs2 = bs * bs;
+  int fv[NF], node[2][NF];
+  double Xf[NF][DIM];
+  for (int k = 0; k < NF; ++k) {
+    fv[k] = P.fverts[static_cast<int64_t>(f) * NF + k];
+    node[0][k] = P.node_in[static_cast<int64_t>(f) * NF + k];
+    node[1][k] = P.node_out[static_cast<int64_t>(f) * NF + k];
+    for (int d = 0; d < DIM; ++d) Xf[k][d] = P.coords[static_cast<int64_t>(fv[k]) * DIM + d];
+  }
+  double nrm[DIM];
+  for (int d = 0; d < DIM; ++d) nrm[d] = P.normal[static_cast<int64_t>(f) * DIM + d];
+  const double ielem = P.ielem[f];
+  const double fvol = P.fvolume[f];
+  const bool do_res = (mode & 1) && P.r;
+  const bool do_jac = (mode & 2) && P.J;
+
+  // coefficients of both sides at the face vertices
+  double cf[2][NF][kFaceMaxSpecies];
+  for (int sd = 0; sd < 2; ++sd)
+    for (int k = 0; k < NF; ++k)
+      for (int s = 0; s < kFaceMaxSpecies; ++s)
+        cf[sd][k][s] = (s < P.ns[sd] && node[sd][k] >= 0)
+                           ? P.x[static_cast<int64_t>(node[sd][k]) * bs + s] : 0.0;
+
+  double R[kMaxDevRegisters];
+  for (int side = 0; side < 2; ++side) {
+    if (P.n_terms[side] == 0) continue;
+    if (side == 1 && !has_out) continue;
+    const int other = 1 - side;
+    // gradients, only if the program reads one
+    bool need_grad = false;
+    for (int i = 0; i < P.prog[side].ninputs; ++i) {
+      const uint16_t id = P.prog[side].inputs[i];
+      need_grad |= (id >= IN_GRAD && id < IN_POSITION);
+    }
+    double grad[2][kFaceMaxSpecies][3];
+    for (int sd = 0; sd < 2; ++sd)
+      for (int s = 0; s < kFaceMaxSpecies; ++s)
+        for (int j = 0; j < 3; ++j) grad[sd][s][j] = 0.0;
+    if (need_grad) {
+      const int e_side = side == 0 ? P.elem_in[f] : P.elem_out[f];
+      const int e_other = side == 0 ? P.elem_out[f] : P.elem_in[f];
+      if (P.ns[side] > 0) cell_gradients<DIM>(P, side, e_side, P.ns[side], grad[side]);
+      if (has_out && P.ns[other] > 0) cell_gradients<DIM>(P, other, e_other, P.ns[other], grad[other]);
+    }
+    const double sgn = side == 0 ? 1.0 : -1.0;
+    double rl[NF][kFaceMaxSpecies];
+    for (int k = 0; k < NF; ++k)
+      for (int s = 0; s < kFaceMaxSpecies; ++s) rl[k][s] = 0.0;
+    double coef[kMaxCoefficients];
+    const int nt = P.n_terms[side];
+    const Term* terms = P.terms[side];
+    for (int q = 0; q < NQ; ++q) {
+      double lam[NF];
+      for (int k = 0; k < NF; ++k) lam[k] = FaceRule<DIM>::lam(q, k);
+      double xq[3] = {0.0, 0.0, 0.0};
+      for (int d = 0; d < DIM; ++d)
+        for (int k = 0; k < NF; ++k) xq[d] += lam[k] * Xf[k][d];
+      const double fq = FaceRule<DIM>::w(q) * ielem;
+      for (int i = 0; i < P.prog[side].ninputs; ++i) {
+        const uint16_t id = P.prog[side].inputs[i];
+        double v = 0.0;
+        if (id < IN_GRAD || (id >= IN_GRAD && id < IN_POSITION)) {
+          const bool is_grad = id >= IN_GRAD;
+          const int gi = is_grad ? (id - IN_GRAD) / 3 : id;
+          const int ax = is_grad ? (id - IN_GRAD) % 3 : 0;
+          for (int sd = 0; sd < 2; ++sd) {
+            const int ls = gi - P.species_offset[sd];
+            if (ls >= 0 && ls < P.ns[sd] && (sd == 0 || has_out)) {
+              if (is_grad) {
+                v = grad[sd][ls][ax];
+              } else {
+                double acc = 0.0;
+                for (int k = 0; k < NF; ++k) acc += cf[sd][k][ls] * lam[k];
+                v = acc;
+              }
+            }
+          }
+        } else if (id < IN_NORMAL) {
+          v = xq[id - IN_POSITION];
+        } else if (id < IN_TIME) {
+          const int ax = id - IN_NORMAL;
+          v = ax < DIM ? sgn * nrm[ax] : 0.0;
+        } else if (id == IN_TIME) {
+          v = P.t;
+        } else if (id == IN_ENTITY_VOLUME) {
+          v = fvol;
+        } else if (id == IN_IN_BOUNDARY) {
+          v = has_out ? 0.0 : 1.0;
+        } else if (id == IN_IN_SKELETON) {
+          v = has_out ? 1.0 : 0.0;
+        }
+        R[i] = v;
+      }
+      run_program(P.prog[side], P.tables, R);
+      const uint8_t* out = P.prog[side].outputs;
+      for (int t = 0; t < nt; ++t) {
+        const Term T = terms[t];
+        const double o = R[out[T.out]] * P.ca * fq;
+        if (T.kind == F_OUTFLOW) {
+          if (do_res)
+            for (int k = 0; k < NF; ++k) rl[k][T.test] += o * lam[k];
+        } else if (T.kind == F_OUTFLOW_JAC) {
+          if (do_jac) coef[T.coef + q] = o;
+        }
+      }
+    }
+    if (do_res)
+      for (int k = 0; k < NF; ++k)
+        for (int s = 0; s < P.ns[side]; ++s)
+          P.r[static_cast<int64_t>(node[side][k]) * bs + s] += rl[k][s];
+    if (do_jac) {
+      for (int t = 0; t < nt; ++t) {
+        const Term T = terms[t];
+        if (T.kind != F_OUTFLOW_JAC) continue;
+        const int col_side = T.side ? other : side;
+        const int pair = side * 2 + col_side;
+        const int32_t* bp = P.bpos + (static_cast<int64_t>(f) * 4 + pair) * NF * NF;
+        for (int k = 0; k < NF; ++k)
+          for (int l = 0; l < NF; ++l) {
+            double v = 0.0;
+            for (int q = 0; q < NQ; ++q)
+              v += coef[T.coef + q] * FaceRule<DIM>::lam(q, k) * FaceRule<DIM>::lam(q, l);
+            P.J[static_cast<int64_t>(bp[k * NF + l]) * bs2 + T.test * bs + T.trial] += v;
+          }
+      }
+    }
+  }
+}
+
+__global__ void k_pad_identity(const int32_t* diag, const int8_t* row_ns, int nrows, int bs, double* J,
+                               double value) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nrows) return;
+  const int64_t base = static_cast<int64_t>(diag[i]) * bs * bs;
+  for (int s = row_ns[i]; s < bs; ++s) J[base + s * bs + s] += value;
+}
+
+}  // namespace
+
+void launch_faces(int dim, const FaceParams& p, int begin, int end, int mode, cudaStream_t stream) {
+  const int n = end - begin;
+  if (n <= 0) return;
+  const int threads = 128;
+  const int blocks = (n + threads - 1) / threads;
+  count_launches(1);
+  if (dim == 2) k_faces<2><<<blocks, threads, 0, stream>>>(p, begin, end, mode);
+  else if (dim == 3) k_faces<3><<<blocks, threads, 0, stream>>>(p, begin, end, mode);
+  else throw std::runtime_error("faces: unsupported dimension");
+}
+
+void launch_pad_identity(const int32_t* diag, const int8_t* row_ns, int nrows, int bs, double* J,
+                         double value, cudaStream_t stream) {
+  if (nrows <= 0) return;
+  count_launches(1);
+  k_pad_identity<<<(nrows + 255) / 256, 256, 0, stream>>>(diag, row_ns, nrows, bs, J, value);
+}
+
+}  // namespace dcgpu

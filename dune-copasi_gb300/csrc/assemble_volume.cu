@@ -1,0 +1,426 @@
+// Volume assembly kernels: residual and analytic Jacobian of the mass and stiffness
+// forms (dune/copasi/model/diffusion_reaction/local_operator.hh:417-491, 541-707).
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+
+#include "assemble.cuh"
+#include "interp.cuh"
+#include "linalg.cuh"
+
+namespace dcgpu {
+
+namespace {
+
+// order-2 simplex rules (the same tables as the CPU oracle)
+template <int DIM> struct Rule;
+template <> struct Rule<2> {
+  static constexpr int NQ = 3;
+  __device__ static constexpr double xi(int q, int k) {
+    return (q == 0) ? (k == 0 ? 2.0 / 3.0 : 1.0 / 6.0)
+         : (q == 1) ? (k == 0 ? 1.0 / 6.0 : 2.0 / 3.0)
+                    : 1.0 / 6.0;
+  }
+  __device__ static constexpr double w(int) { return 1.0 / 6.0; }
+};
+template <> struct Rule<3> {
+  static constexpr int NQ = 4;
+  __device__ static constexpr double xi(int q, int k) {
+    // q = 0: (b,b,b); q = 1..3: a in coordinate q-1
+    return (q == k + 1) ? 0.5854101966249685 : 0.1381966011250105;
+  }
+  __device__ static constexpr double w(int) { return 1.0 / 24.0; }
+};
+
+template <int DIM>
+__device__ __forceinline__ double phi(int q, int a) {
+  if (a == 0) {
+    double s = 1.0;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) s -= Rule<DIM>::xi(q, k);
+    return s;
+  }
+  return Rule<DIM>::xi(q, a - 1);
+}
+
+template <int DIM, int NS>
+__device__ __forceinline__ double volume_input(uint16_t id, const double (&u)[NS],
+                                               const double (&g)[NS][DIM], const double (&xq)[DIM],
+                                               double t, double vol, int soff) {
+  if (id < IN_GRAD) {
+    const int s = static_cast<int>(id) - soff;
+    double v = 0.0;
+#pragma unroll
+    for (int i = 0; i < NS; ++i)
+      if (i == s) v = u[i];
+    return v;
+  }
+  if (id < IN_POSITION) {
+    const int gi = static_cast<int>(id) - IN_GRAD;
+    const int s = gi / 3 - soff, ax = gi % 3;
+    double v = 0.0;
+#pragma unroll
+    for (int i = 0; i < NS; ++i)
+#pragma unroll
+      for (int d = 0; d < DIM; ++d)
+        if (i == s && d == ax) v = g[i][d];
+    return v;
+  }
+  if (id < IN_NORMAL) {
+    const int ax = static_cast<int>(id) - IN_POSITION;
+    double v = 0.0;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d)
+      if (d == ax) v = xq[d];
+    return v;
+  }
+  switch (id) {
+    case IN_TIME: return t;
+    case IN_ENTITY_VOLUME: return vol;
+    case IN_IN_VOLUME: return 1.0;
+    default: return 0.0;
+  }
+}
+
+template <int DIM, int NS>
+__global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int begin, const int end,
+                                                const int mode) {
+  constexpr int NL = DIM + 1;
+  constexpr int NQ = Rule<DIM>::NQ;
+  const int k = begin + blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= end) return;
+
+  int nd[NL];
+  double X[NL][DIM];
+#pragma unroll
+  for (int a = 0; a < NL; ++a) {
+    const int v = P.verts[static_cast<int64_t>(k) * NL + a];
+    nd[a] = P.nodes[static_cast<int64_t>(k) * NL + a];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) X[a][d] = P.coords[static_cast<int64_t>(v) * DIM + d];
+  }
+  // affine map x = X0 + Bm xi ; gradients of the P1 basis: rows of B^{-1} (local_operator.hh:461-464)
+  double Bm[DIM][DIM];
+#pragma unroll
+  for (int i = 0; i < DIM; ++i)
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) Bm[i][j] = X[j + 1][i] - X[0][i];
+  double Bi[DIM][DIM];
+  double det;
+  if constexpr (DIM == 2) {
+    det = Bm[0][0] * Bm[1][1] - Bm[0][1] * Bm[1][0];
+    const double id = 1.0 / det;
+    Bi[0][0] = Bm[1][1] * id;  Bi[0][1] = -Bm[0][1] * id;
+    Bi[1][0] = -Bm[1][0] * id; Bi[1][1] = Bm[0][0] * id;
+  } else {
+    const double c00 = Bm[1][1] * Bm[2][2] - Bm[1][2] * Bm[2][1];
+    const double c01 = Bm[1][2] * Bm[2][0] - Bm[1][0] * Bm[2][2];
+    const double c02 = Bm[1][0] * Bm[2][1] - Bm[1][1] * Bm[2][0];
+    det = Bm[0][0] * c00 + Bm[0][1] * c01 + Bm[0][2] * c02;
+    const double id = 1.0 / det;
+    Bi[0][0] = c00 * id;
+    Bi[1][0] = c01 * id;
+    Bi[2][0] = c02 * id;
+    Bi[0][1] = (Bm[0][2] * Bm[2][1] - Bm[0][1] * Bm[2][2]) * id;
+    Bi[1][1] = (Bm[0][0] * Bm[2][2] - Bm[0][2] * Bm[2][0]) * id;
+    Bi[2][1] = (Bm[0][1] * Bm[2][0] - Bm[0][0] * Bm[2][1]) * id;
+    Bi[0][2] = (Bm[0][1] * Bm[1][2] - Bm[0][2] * Bm[1][1]) * id;
+    Bi[1][2] = (Bm[0][2] * Bm[1][0] - Bm[0][0] * Bm[1][2]) * id;
+    Bi[2][2] = (Bm[0][0] * Bm[1][1] - Bm[0][1] * Bm[1][0]) * id;
+  }
+  const double adet = fabs(det);
+  const double vol = adet / (DIM == 2 ? 2.0 : 6.0);
+  double G[NL][DIM];
+#pragma unroll
+  for (int j = 0; j < DIM; ++j) {
+    double s = 0.0;
+#pragma unroll
+    for (int kk = 0; kk < DIM; ++kk) {
+      G[kk + 1][j] = Bi[kk][j];
+      s += Bi[kk][j];
+    }
+    G[0][j] = -s;
+  }
+
+  const int bs = P.bs;
+  double c[NL][NS];
+#pragma unroll
+  for (int a = 0; a < NL; ++a)
+#pragma unroll
+    for (int s = 0; s < NS; ++s) c[a][s] = P.x[static_cast<int64_t>(nd[a]) * bs + s];
+  double g[NS][DIM];
+#pragma unroll
+  for (int s = 0; s < NS; ++s)
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) {
+      double acc = 0.0;
+#pragma unroll
+      for (int a = 0; a < NL; ++a) acc += c[a][s] * G[a][j];
+      g[s][j] = acc;
+    }
+
+  const bool do_res = (mode & 1) && P.r;
+  const bool do_jac = (mode & 2) && P.J;
+  double rl[NL][NS];
+#pragma unroll
+  for (int a = 0; a < NL; ++a)
+#pragma unroll
+    for (int s = 0; s < NS; ++s) rl[a][s] = 0.0;
+  double coef[kMaxCoefficients];
+  if (do_jac) {
+    int ncoef = 0;
+    for (int t = 0; t < P.n_jac_terms; ++t) {
+      const Term T = P.jac_terms[t];
+      int sz = (T.kind == J_MASS || T.kind == J_MASS_U || T.kind == J_STORAGE_SELF) ? NQ
+             : (T.kind == J_DIFF_SCALAR) ? 1
+             : (T.kind == J_DIFF_TENSOR) ? DIM * DIM
+                                         : NL * DIM;
+      ncoef = max(ncoef, T.coef + sz);
+    }
+    for (int i = 0; i < ncoef; ++i) coef[i] = 0.0;
+  }
+  double R[kMaxDevRegisters];
+
+#pragma unroll 1
+  for (int q = 0; q < NQ; ++q) {
+    double u[NS];
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+      double acc = 0.0;
+#pragma unroll
+      for (int a = 0; a < NL; ++a) acc += c[a][s] * phi<DIM>(q, a);
+      u[s] = acc;
+    }
+    double xq[DIM];
+#pragma unroll
+    for (int i = 0; i < DIM; ++i) {
+      double acc = X[0][i];
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) acc += Bm[i][j] * Rule<DIM>::xi(q, j);
+      xq[i] = acc;
+    }
+    const double fq = Rule<DIM>::w(q) * adet;
+    for (int i = 0; i < P.prog.ninputs; ++i)
+      R[i] = volume_input<DIM, NS>(P.prog.inputs[i], u, g, xq, P.t, vol, P.species_offset);
+    run_program(P.prog, P.tables, R);
+    const uint8_t* out = P.prog.outputs;
+
+    if (do_res) {
+      double scal[NS], flux[NS][DIM];
+#pragma unroll
+      for (int s = 0; s < NS; ++s) {
+        scal[s] = 0.0;
+#pragma unroll
+        for (int j = 0; j < DIM; ++j) flux[s][j] = 0.0;
+      }
+      for (int t = 0; t < P.n_res_terms; ++t) {
+        const Term T = P.res_terms[t];
+        const double sc = T.form ? P.ca : P.cm;
+        const double o = R[out[T.out]];
+        double ds = 0.0, df[DIM];
+#pragma unroll
+        for (int j = 0; j < DIM; ++j) df[j] = 0.0;
+        double ut = 0.0;
+#pragma unroll
+        for (int s = 0; s < NS; ++s)
+          if (s == T.test) ut = u[s];
+        double gw[DIM];
+#pragma unroll
+        for (int j = 0; j < DIM; ++j) {
+          gw[j] = 0.0;
+#pragma unroll
+          for (int s = 0; s < NS; ++s)
+            if (s == T.trial) gw[j] = g[s][j];
+        }
+        switch (T.kind) {
+          case R_REACTION: ds = -o; break;
+          case R_STORAGE: ds = ut * o; break;
+          case R_VELOCITY:
+#pragma unroll
+            for (int j = 0; j < DIM; ++j) df[j] = R[out[T.out + j]] * ut;
+            break;
+          case R_DIFF_SCALAR:
+#pragma unroll
+            for (int j = 0; j < DIM; ++j) df[j] = -o * gw[j];
+            break;
+          case R_DIFF_TENSOR:
+#pragma unroll
+            for (int i = 0; i < DIM; ++i) {
+              double acc = 0.0;
+#pragma unroll
+              for (int j = 0; j < DIM; ++j) acc += R[out[T.out + i * DIM + j]] * gw[j];
+              df[i] = -acc;
+            }
+            break;
+          default: break;
+        }
+#pragma unroll
+        for (int s = 0; s < NS; ++s) {
+          if (s == T.test) {
+            scal[s] += sc * ds;
+#pragma unroll
+            for (int j = 0; j < DIM; ++j) flux[s][j] += sc * df[j];
+          }
+        }
+      }
+#pragma unroll
+      for (int a = 0; a < NL; ++a) {
+        const double pa = phi<DIM>(q, a);
+#pragma unroll
+        for (int s = 0; s < NS; ++s) {
+          double fg = 0.0;
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) fg += flux[s][j] * G[a][j];
+          rl[a][s] += (scal[s] * pa - fg) * fq;
+        }
+      }
+    }
+
+    if (do_jac) {
+      for (int t = 0; t < P.n_jac_terms; ++t) {
+        const Term T = P.jac_terms[t];
+        const double sc = (T.form ? P.ca : P.cm) * fq;
+        const double o = R[out[T.out]];
+        double ut = 0.0;
+#pragma unroll
+        for (int s = 0; s < NS; ++s)
+          if (s == T.test) ut = u[s];
+        switch (T.kind) {
+          case J_MASS:
+          case J_STORAGE_SELF: coef[T.coef + q] += sc * o; break;
+          case J_MASS_U: coef[T.coef + q] += sc * o * ut; break;
+          case J_DIFF_SCALAR: coef[T.coef] += sc * o; break;
+          case J_DIFF_TENSOR:
+#pragma unroll
+            for (int i = 0; i < DIM * DIM; ++i) coef[T.coef + i] += sc * R[out[T.out + i]];
+            break;
+          case J_VELOCITY:
+          case J_VELOCITY_JAC:
+          case J_DIFFJAC_SCALAR:
+          case J_DIFFJAC_TENSOR: {
+            double vec[DIM];
+            if (T.kind == J_VELOCITY) {
+#pragma unroll
+              for (int j = 0; j < DIM; ++j) vec[j] = -R[out[T.out + j]];
+            } else if (T.kind == J_VELOCITY_JAC) {
+#pragma unroll
+              for (int j = 0; j < DIM; ++j) vec[j] = -R[out[T.out + j]] * ut;
+            } else {
+              double gw[DIM];
+#pragma unroll
+              for (int j = 0; j < DIM; ++j) {
+                gw[j] = 0.0;
+#pragma unroll
+                for (int s = 0; s < NS; ++s)
+                  if (s == T.trial) gw[j] = g[s][j];
+              }
+              if (T.kind == J_DIFFJAC_SCALAR) {
+#pragma unroll
+                for (int j = 0; j < DIM; ++j) vec[j] = o * gw[j];
+              } else {
+#pragma unroll
+                for (int i = 0; i < DIM; ++i) {
+                  double acc = 0.0;
+#pragma unroll
+                  for (int j = 0; j < DIM; ++j) acc += R[out[T.out + i * DIM + j]] * gw[j];
+                  vec[i] = acc;
+                }
+              }
+            }
+#pragma unroll
+            for (int a = 0; a < NL; ++a) {
+              const double pa = phi<DIM>(q, a) * sc;
+#pragma unroll
+              for (int j = 0; j < DIM; ++j) coef[T.coef + a * DIM + j] += pa * vec[j];
+            }
+            break;
+          }
+          default: break;
+        }
+      }
+    }
+  }
+
+  if (do_res) {
+#pragma unroll
+    for (int a = 0; a < NL; ++a)
+#pragma unroll
+      for (int s = 0; s < NS; ++s) P.r[static_cast<int64_t>(nd[a]) * bs + s] += rl[a][s];
+  }
+  if (do_jac) {
+    const int bs2 = bs * bs;
+    const int32_t* bp = P.bpos + static_cast<int64_t>(k) * NL * NL;
+    int blk[NL][NL];
+#pragma unroll
+    for (int a = 0; a < NL; ++a)
+#pragma unroll
+      for (int b = 0; b < NL; ++b) blk[a][b] = bp[a * NL + b];
+    for (int t = 0; t < P.n_jac_terms; ++t) {
+      const Term T = P.jac_terms[t];
+      const int te = T.test;
+      const int tr = (T.kind == J_STORAGE_SELF || T.kind == J_VELOCITY) ? T.test : T.trial;
+#pragma unroll
+      for (int a = 0; a < NL; ++a) {
+#pragma unroll
+        for (int b = 0; b < NL; ++b) {
+          double v = 0.0;
+          switch (T.kind) {
+            case J_MASS:
+            case J_MASS_U:
+            case J_STORAGE_SELF:
+#pragma unroll
+              for (int q = 0; q < NQ; ++q) v += coef[T.coef + q] * (phi<DIM>(q, a) * phi<DIM>(q, b));
+              break;
+            case J_DIFF_SCALAR: {
+              double gg = 0.0;
+#pragma unroll
+              for (int j = 0; j < DIM; ++j) gg += G[a][j] * G[b][j];
+              v = coef[T.coef] * gg;
+              break;
+            }
+            case J_DIFF_TENSOR:
+              // (T G_a) . G_b
+#pragma unroll
+              for (int i = 0; i < DIM; ++i) {
+                double tg = 0.0;
+#pragma unroll
+                for (int j = 0; j < DIM; ++j) tg += coef[T.coef + i * DIM + j] * G[a][j];
+                v += tg * G[b][i];
+              }
+              break;
+            default:
+              // phi_a-weighted vector . G_b
+#pragma unroll
+              for (int j = 0; j < DIM; ++j) v += coef[T.coef + a * DIM + j] * G[b][j];
+              break;
+          }
+          P.J[static_cast<int64_t>(blk[a][b]) * bs2 + te * bs + tr] += v;
+        }
+      }
+    }
+  }
+}
+
+template <int DIM, int NS>
+void launch_t(const VolumeParams& p, int begin, int end, int mode, cudaStream_t stream) {
+  const int n = end - begin;
+  if (n <= 0) return;
+  const int threads = 128;
+  count_launches(1);
+  k_volume<DIM, NS><<<(n + threads - 1) / threads, threads, 0, stream>>>(p, begin, end, mode);
+}
+
+}  // namespace
+
+void launch_volume(int dim, int ns, const VolumeParams& p, int begin, int end, int mode,
+                   cudaStream_t stream) {
+#define DC_CASE(D, S) \
+  if (dim == D && ns == S) return launch_t<D, S>(p, begin, end, mode, stream);
+  DC_CASE(2, 1) DC_CASE(2, 2) DC_CASE(2, 3) DC_CASE(2, 4) DC_CASE(2, 5) DC_CASE(2, 6) DC_CASE(2, 7) DC_CASE(2, 8)
+  DC_CASE(3, 1) DC_CASE(3, 2) DC_CASE(3, 3) DC_CASE(3, 4) DC_CASE(3, 5) DC_CASE(3, 6) DC_CASE(3, 7) DC_CASE(3, 8)
+#undef DC_CASE
+  throw std::runtime_error("volume assembly supports dimension 2/3 and 1..8 species per compartment, got dim=" +
+                           std::to_string(dim) + " species=" + std::to_string(ns));
+}
+
+}  // namespace dcgpu

@@ -1,0 +1,373 @@
+// extern "C" boundary (include/dcgpu.h).  Exceptions are caught here and turned into
+// status codes; the message is kept per thread for dc_last_error().
+#include <cstring>
+#include <memory>
+#include <string>
+
+#include "../../include/dcgpu.h"
+#include "model.hpp"
+#include "solver.hpp"
+
+struct dc_model {
+  std::unique_ptr<dcgpu::Model> model;
+  std::unique_ptr<dcgpu::Solver> solver;
+  cudaStream_t stream = nullptr;
+  dcgpu::DeviceBuffer<double> scratch_x, scratch_r, scratch_j;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+template <class F>
+int guarded(F&& f) {
+  try {
+    g_last_error.clear();
+    return f();
+  } catch (const dcgpu::ConfigError& e) {
+    g_last_error = e.what();
+    return DC_ERR_CONFIG;
+  } catch (const dcgpu::CudaError& e) {
+    g_last_error = e.what();
+    return DC_ERR_CUDA;
+  } catch (const dcgpu::StepFailure& e) {
+    g_last_error = e.what();
+    return e.code;
+  } catch (const std::invalid_argument& e) {
+    g_last_error = e.what();
+    return DC_ERR_ARGUMENT;
+  } catch (const std::exception& e) {
+    g_last_error = e.what();
+    return DC_ERR_INTERNAL;
+  } catch (...) {
+    g_last_error = "unknown error";
+    return DC_ERR_INTERNAL;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* dc_last_error(void) { return g_last_error.c_str(); }
+
+int dc_model_create(const char* ini_text, const char* overrides, dc_model** out) {
+  return guarded([&] {
+    if (!ini_text || !out) throw std::invalid_argument("null argument");
+    *out = nullptr;
+    int dev_count = 0;
+    dcgpu::cuda_check(cudaGetDeviceCount(&dev_count), "cudaGetDeviceCount");
+    if (dev_count == 0) throw dcgpu::CudaError("no CUDA device");
+    auto m = std::make_unique<dc_model>();
+    dcgpu::cuda_check(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    m->model = std::make_unique<dcgpu::Model>(ini_text, overrides ? overrides : "");
+    m->solver = std::make_unique<dcgpu::Solver>(*m->model, m->stream);
+    *out = m.release();
+    return DC_OK;
+  });
+}
+
+int dc_model_destroy(dc_model* model) {
+  return guarded([&] {
+    if (!model) return DC_OK;
+    cudaStream_t s = model->stream;
+    if (s) cudaStreamSynchronize(s);
+    model->solver.reset();
+    model->model.reset();
+    if (s) cudaStreamDestroy(s);
+    delete model;
+    return DC_OK;
+  });
+}
+
+int dc_model_info_get(const dc_model* model, dc_model_info* info) {
+  return guarded([&] {
+    if (!model || !info) throw std::invalid_argument("null argument");
+    const auto& m = *model->model;
+    info->dim = m.dim;
+    info->n_species = static_cast<int32_t>(m.species.size());
+    info->n_compartments = static_cast<int32_t>(m.comp_names.size());
+    info->block_size = m.bs;
+    info->n_vertices = m.mesh.nv;
+    info->n_elements = m.mesh.ne;
+    info->n_dof = m.ndof;
+    info->n_block_rows = m.nnodes;
+    info->n_blocks = m.nnzb();
+    return DC_OK;
+  });
+}
+
+int dc_species_name(const dc_model* model, int32_t species, char* buf, size_t len) {
+  return guarded([&] {
+    if (!model || !buf) throw std::invalid_argument("null argument");
+    const auto& sp = model->model->species;
+    if (species < 0 || species >= static_cast<int32_t>(sp.size())) throw std::invalid_argument("species index out of range");
+    const std::string& n = sp[species].name;
+    if (len < n.size() + 1) throw std::invalid_argument("buffer too small");
+    std::memcpy(buf, n.c_str(), n.size() + 1);
+    return DC_OK;
+  });
+}
+
+int dc_species_size(const dc_model* model, int32_t species, int64_t* n_vertices) {
+  return guarded([&] {
+    if (!model || !n_vertices) throw std::invalid_argument("null argument");
+    const auto& m = *model->model;
+    if (species < 0 || species >= static_cast<int32_t>(m.species.size())) throw std::invalid_argument("species index out of range");
+    *n_vertices = static_cast<int64_t>(m.comp_vertices[m.species[species].comp].size());
+    return DC_OK;
+  });
+}
+
+int dc_species_vertices(const dc_model* model, int32_t species, int64_t* vertex_ids, size_t n) {
+  return guarded([&] {
+    if (!model || !vertex_ids) throw std::invalid_argument("null argument");
+    const auto& m = *model->model;
+    if (species < 0 || species >= static_cast<int32_t>(m.species.size())) throw std::invalid_argument("species index out of range");
+    const auto& v = m.comp_vertices[m.species[species].comp];
+    if (n != v.size()) throw std::invalid_argument("size mismatch");
+    for (size_t k = 0; k < n; ++k) vertex_ids[k] = v[k];
+    return DC_OK;
+  });
+}
+
+int dc_state_set_initial(dc_model* model) {
+  return guarded([&] {
+    if (!model) throw std::invalid_argument("null argument");
+    auto& m = *model->model;
+    model->solver->set_state(m.initial_state(), m.cfg.sub("model").get_double("time_step_operator.time_begin", 0.0));
+    return DC_OK;
+  });
+}
+
+int dc_state_get(const dc_model* model, double* host_out, size_t n) {
+  return guarded([&] {
+    if (!model || !host_out) throw std::invalid_argument("null argument");
+    if (static_cast<int64_t>(n) != model->model->ndof) throw std::invalid_argument("size mismatch");
+    auto v = model->solver->get_state();
+    std::memcpy(host_out, v.data(), n * sizeof(double));
+    return DC_OK;
+  });
+}
+
+int dc_state_set(dc_model* model, const double* host_in, size_t n, double time) {
+  return guarded([&] {
+    if (!model || !host_in) throw std::invalid_argument("null argument");
+    if (static_cast<int64_t>(n) != model->model->ndof) throw std::invalid_argument("size mismatch");
+    model->solver->set_state(std::vector<double>(host_in, host_in + n), time);
+    return DC_OK;
+  });
+}
+
+int dc_state_get_species(const dc_model* model, int32_t species, double* host_out, size_t n) {
+  return guarded([&] {
+    if (!model || !host_out) throw std::invalid_argument("null argument");
+    const auto& m = *model->model;
+    if (species < 0 || species >= static_cast<int32_t>(m.species.size())) throw std::invalid_argument("species index out of range");
+    const auto& sp = m.species[species];
+    const auto& verts = m.comp_vertices[sp.comp];
+    if (n != verts.size()) throw std::invalid_argument("size mismatch");
+    auto v = model->solver->get_state();
+    for (size_t k = 0; k < n; ++k) host_out[k] = v[m.ref_dof(sp.comp, static_cast<int32_t>(k), sp.local)];
+    return DC_OK;
+  });
+}
+
+int dc_state_time(const dc_model* model, double* time) {
+  return guarded([&] {
+    if (!model || !time) throw std::invalid_argument("null argument");
+    *time = model->solver->time();
+    return DC_OK;
+  });
+}
+
+int dc_step(dc_model* model, double* dt, dc_step_info* info) {
+  return guarded([&] {
+    if (!model || !dt) throw std::invalid_argument("null argument");
+    auto& s = *model->solver;
+    const auto before = s.stats;
+    double used = 0.0;
+    cudaEvent_t e0, e1;
+    dcgpu::cuda_check(cudaEventCreate(&e0), "cudaEventCreate");
+    dcgpu::cuda_check(cudaEventCreate(&e1), "cudaEventCreate");
+    dcgpu::cuda_check(cudaEventRecord(e0, model->stream), "cudaEventRecord");
+    int st = s.do_step(*dt, &used);
+    dcgpu::cuda_check(cudaEventRecord(e1, model->stream), "cudaEventRecord");
+    dcgpu::cuda_check(cudaEventSynchronize(e1), "cudaEventSynchronize");
+    float ms = 0.0f;
+    dcgpu::cuda_check(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (info) {
+      info->device_ms = ms;
+      info->time = s.time();
+      info->dt_used = used;
+      info->newton_iterations = static_cast<int32_t>(s.stats.newton_iterations - before.newton_iterations);
+      info->linear_iterations = static_cast<int32_t>(s.stats.linear_iterations - before.linear_iterations);
+      info->failed_attempts = static_cast<int32_t>(s.stats.failed_steps - before.failed_steps);
+      info->status = st;
+    }
+    if (st != DC_OK) g_last_error = "time step failed";
+    return st;
+  });
+}
+
+int dc_evolve(dc_model* model, double t_end, double* dt, dc_callback cb, void* user) {
+  return guarded([&] {
+    if (!model || !dt) throw std::invalid_argument("null argument");
+    int st = model->solver->evolve(t_end, *dt, [&](double t) {
+      if (cb) cb(model, t, user);
+    });
+    if (st != DC_OK) g_last_error = "evolve failed";
+    return st;
+  });
+}
+
+int dc_assemble(dc_model* model, const double* x, double t, double cm, double ca, double* r, double* jac_values,
+                size_t n_jac_values) {
+  return guarded([&] {
+    if (!model || !x) throw std::invalid_argument("null argument");
+    auto& m = *model->model;
+    const int64_t n = m.nnodes * m.bs;
+    const int64_t nj = m.nnzb() * m.bs * m.bs;
+    if (jac_values && static_cast<int64_t>(n_jac_values) != nj) throw std::invalid_argument("jacobian size mismatch");
+    std::vector<double> blk;
+    m.to_blocked(std::vector<double>(x, x + m.ndof), blk);
+    if (model->scratch_x.size() != static_cast<size_t>(n)) model->scratch_x.resize(n);
+    if (model->scratch_r.size() != static_cast<size_t>(n)) model->scratch_r.resize(n);
+    if (jac_values && model->scratch_j.size() != static_cast<size_t>(nj)) model->scratch_j.resize(nj);
+    cudaStream_t s = model->stream;
+    dcgpu::cuda_check(cudaMemcpyAsync(model->scratch_x.get(), blk.data(), n * sizeof(double), cudaMemcpyHostToDevice, s), "copy");
+    dcgpu::cuda_check(cudaMemsetAsync(model->scratch_r.get(), 0, n * sizeof(double), s), "memset");
+    if (jac_values) dcgpu::cuda_check(cudaMemsetAsync(model->scratch_j.get(), 0, nj * sizeof(double), s), "memset");
+    int mode = (r ? 1 : 0) | (jac_values ? 2 : 0);
+    if (mode) m.assemble(model->scratch_x.get(), t, cm, ca, r ? model->scratch_r.get() : nullptr,
+                         jac_values ? model->scratch_j.get() : nullptr, mode, s);
+    dcgpu::cuda_check(cudaStreamSynchronize(s), "assemble");
+    dcgpu::cuda_check(cudaGetLastError(), "assemble");
+    if (r) {
+      std::vector<double> rb(n), rr;
+      dcgpu::cuda_check(cudaMemcpy(rb.data(), model->scratch_r.get(), n * sizeof(double), cudaMemcpyDeviceToHost), "copy");
+      m.from_blocked(rb, rr);
+      std::memcpy(r, rr.data(), m.ndof * sizeof(double));
+    }
+    if (jac_values)
+      dcgpu::cuda_check(cudaMemcpy(jac_values, model->scratch_j.get(), nj * sizeof(double), cudaMemcpyDeviceToHost), "copy");
+    return DC_OK;
+  });
+}
+
+int dc_pattern(const dc_model* model, int32_t* rowptr, size_t n_rowptr, int32_t* colidx, size_t n_colidx) {
+  return guarded([&] {
+    if (!model || !rowptr || !colidx) throw std::invalid_argument("null argument");
+    const auto& m = *model->model;
+    if (n_rowptr != m.rowptr.size() || n_colidx != m.colidx.size()) throw std::invalid_argument("size mismatch");
+    std::memcpy(rowptr, m.rowptr.data(), n_rowptr * sizeof(int32_t));
+    std::memcpy(colidx, m.colidx.data(), n_colidx * sizeof(int32_t));
+    return DC_OK;
+  });
+}
+
+int dc_dof_map(const dc_model* model, int64_t* ref_to_dev, size_t n) {
+  return guarded([&] {
+    if (!model || !ref_to_dev) throw std::invalid_argument("null argument");
+    const auto& m = *model->model;
+    if (static_cast<int64_t>(n) != m.ndof) throw std::invalid_argument("size mismatch");
+    int64_t off = 0;
+    for (size_t c = 0; c < m.comp_names.size(); ++c) {
+      const int64_t nvc = static_cast<int64_t>(m.comp_vertices[c].size());
+      for (int64_t k = 0; k < nvc; ++k)
+        for (int s = 0; s < m.ns[c]; ++s) ref_to_dev[off + k * m.ns[c] + s] = (m.comp_node_offset[c] + k) * m.bs + s;
+      off += nvc * m.ns[c];
+    }
+    return DC_OK;
+  });
+}
+
+int dc_stats(const dc_model* model, int64_t* newton_iterations, int64_t* linear_iterations, int64_t* assemblies,
+             int64_t* failed_steps) {
+  return guarded([&] {
+    if (!model) throw std::invalid_argument("null argument");
+    const auto& st = model->solver->stats;
+    if (newton_iterations) *newton_iterations = st.newton_iterations;
+    if (linear_iterations) *linear_iterations = st.linear_iterations;
+    if (assemblies) *assemblies = st.assemblies;
+    if (failed_steps) *failed_steps = st.failed_steps;
+    return DC_OK;
+  });
+}
+
+int dc_expr_eval(const char* expression, const char* context_ini, const char* const* names, const double* values,
+                 int32_t n, double* out) {
+  return guarded([&] {
+    if (!expression || !out || (n > 0 && (!names || !values))) throw std::invalid_argument("null argument");
+    dcgpu::ParserContext ctx;
+    if (context_ini) {
+      dcgpu::Ini ini = dcgpu::Ini::parse(context_ini);
+      if (ini.has_sub("parser_context")) ctx = dcgpu::ParserContext(ini.sub("parser_context"));
+    }
+    dcgpu::ProgramBuilder pb(ctx);
+    dcgpu::Resolver res = [&](const std::string& nm) -> std::optional<dcgpu::Symbol> {
+      for (int32_t i = 0; i < n; ++i)
+        if (nm == names[i]) {
+          dcgpu::Symbol s;
+          s.is_input = true;
+          s.input = static_cast<uint16_t>(i);
+          return s;
+        }
+      if (nm == "no_value") {
+        dcgpu::Symbol s;
+        s.value = 1.7976931348623157e308;
+        return s;
+      }
+      return std::nullopt;
+    };
+    pb.add_output(pb.compile_text(expression, res));
+    dcgpu::Program p = pb.finish();
+    std::vector<double> in(p.inputs.size());
+    for (size_t i = 0; i < p.inputs.size(); ++i) in[i] = values[p.inputs[i]];
+    *out = dcgpu::run_program_host(p, ctx, in.data());
+    return DC_OK;
+  });
+}
+
+int dc_stream_handle(const dc_model* model, void** stream) {
+  return guarded([&] {
+    if (!model || !stream) throw std::invalid_argument("null argument");
+    *stream = reinterpret_cast<void*>(model->stream);
+    return DC_OK;
+  });
+}
+
+int64_t dc_launch_count(void) { return dcgpu::launch_count(); }
+
+int dc_profile_enable(dc_model* model, int enabled) {
+  return guarded([&] {
+    if (!model) throw std::invalid_argument("null argument");
+    model->solver->enable_profiling(enabled != 0);
+    return DC_OK;
+  });
+}
+
+int dc_profile_get(const dc_model* model, double* ms, int64_t* calls, int32_t n_categories) {
+  return guarded([&] {
+    if (!model || !ms || !calls) throw std::invalid_argument("null argument");
+    const auto& kt = model->solver->kernel_times;
+    for (int32_t c = 0; c < n_categories; ++c) {
+      const bool ok = c < dcgpu::Solver::kTimerCategories;
+      ms[c] = ok ? kt.ms[c] : 0.0;
+      calls[c] = ok ? kt.calls[c] : 0;
+    }
+    return DC_OK;
+  });
+}
+
+int dc_set_mixed_precision(dc_model* model, int enabled) {
+  return guarded([&] {
+    if (!model) throw std::invalid_argument("null argument");
+    model->solver->enable_mixed(enabled != 0);
+    return DC_OK;
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,110 @@
+// Device-side data structures shared by the assembly kernels and the host driver.
+#pragma once
+
+#include <cstdint>
+
+#include "bytecode.hpp"
+
+namespace dcgpu {
+
+// One compiled expression program resident in device memory.
+struct DevProgram {
+  const Instr* code = nullptr;
+  const double* consts = nullptr;
+  const uint16_t* inputs = nullptr;
+  const uint8_t* outputs = nullptr;
+  int ncode = 0, ninputs = 0, noutputs = 0, nregs = 0;
+};
+
+// 1-D interpolation tables of the parser context
+struct DevTables {
+  const double* x = nullptr;
+  const double* y = nullptr;
+  const int* off = nullptr;
+  const int* len = nullptr;
+};
+
+// Volume term kinds (residual and Jacobian of local_operator.hh:417-707).
+enum TermKind : uint8_t {
+  // residual
+  R_REACTION = 0,     // scalar -= out
+  R_STORAGE,          // scalar += u_test * out
+  R_VELOCITY,         // flux += out[0..dim) * u_test
+  R_DIFF_SCALAR,      // flux -= out * grad u_trial
+  R_DIFF_TENSOR,      // flux -= T(out[0..dim^2)) grad u_trial
+  // Jacobian
+  J_MASS,             // J[a,test][b,trial] += out * phi_a phi_b
+  J_MASS_U,           // J[a,test][b,trial] += out * u_test * phi_a phi_b
+  J_STORAGE_SELF,     // J[a,test][b,test]  += out * phi_a phi_b
+  J_VELOCITY,         // J[a,test][b,test]  -= phi_a (v . G_b)
+  J_VELOCITY_JAC,     // J[a,test][b,trial] -= phi_a ((out * u_test) . G_b)
+  J_DIFF_SCALAR,      // J[a,test][b,trial] += out (G_a . G_b)
+  J_DIFF_TENSOR,      // J[a,test][b,trial] += (T G_a) . G_b
+  J_DIFFJAC_SCALAR,   // J[a,test][b,trial] += phi_a (out grad u_trial) . G_b
+  J_DIFFJAC_TENSOR,   // J[a,test][b,trial] += phi_a (T grad u_trial) . G_b
+  // faces
+  F_OUTFLOW,          // r[k,test] += out * psi_k
+  F_OUTFLOW_JAC,      // J[k,test][l,trial@side] += out * psi_k psi_l
+};
+
+struct Term {
+  uint8_t kind;
+  uint8_t form;     // 0 = mass form (scaled by cm), 1 = stiffness form (scaled by ca)
+  uint8_t test;     // local species index (compartment of the element / face side)
+  uint8_t trial;    // local species index of the trial / gradient species
+  uint8_t side;     // faces: 0 = trial lives on this side, 1 = on the other side
+  uint8_t pad;
+  uint16_t out;     // first program output
+  uint16_t coef;    // Jacobian terms: offset into the per-thread coefficient array
+  uint16_t pad2;
+};
+
+constexpr int kMaxDevRegisters = 64;   // register file of the device interpreter
+constexpr int kMaxCoefficients = 192;  // per-element Jacobian coefficient storage
+
+// Launch parameters for the volume assembly of one compartment.
+struct VolumeParams {
+  const double* coords;      // nv * dim
+  const int32_t* verts;      // ne * nl (coloured order)
+  const int32_t* nodes;      // ne * nl block-row index of each local vertex
+  const int32_t* bpos;       // ne * nl * nl block index in the BSR pattern
+  const Term* res_terms;
+  const Term* jac_terms;
+  int n_res_terms, n_jac_terms;
+  DevProgram prog;           // outputs for residual (and Jacobian when assembling it)
+  DevTables tables;
+  const double* x;           // state, node-major with block size bs
+  double* r;                 // residual accumulator (may be null)
+  double* J;                 // BSR values accumulator (may be null)
+  int bs;                    // block size
+  int species_offset;        // model-global index of local species 0
+  double t, cm, ca;          // time, mass-form scale, stiffness-form scale
+};
+
+struct FaceParams {
+  const double* coords;
+  const int32_t* fverts;     // nf * dim face vertices
+  const int32_t* node_in;    // nf * dim block rows of the face vertices, side 0 compartment
+  const int32_t* node_out;   // nf * dim block rows, side 1 compartment (or -1)
+  const int32_t* bpos;       // nf * 4 * dim * dim : (in,in) (in,out) (out,in) (out,out)
+  const double* normal;      // nf * dim unit normal pointing from side 0 to side 1
+  const double* ielem;       // nf integration element (edge length / twice the triangle area)
+  const double* fvolume;     // nf face measure (entity_volume)
+  const int32_t* elem_in;    // nf elements (for gradients)
+  const int32_t* elem_out;
+  const int32_t* cells;      // mesh cells (nl per element)
+  const int32_t* vnode[2];   // vertex -> block row of each side's compartment (-1 if absent)
+  const Term* terms[2];      // per side
+  int n_terms[2];
+  DevProgram prog[2];        // per side
+  DevTables tables;
+  const double* x;
+  double* r;
+  double* J;
+  int bs;
+  int species_offset[2];     // model-global species index of local species 0, per side
+  int ns[2];
+  double t, ca;
+};
+
+}  // namespace dcgpu

@@ -1,0 +1,112 @@
+// Device interpreter for the expression bytecode (see bytecode.hpp).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "device.cuh"
+
+namespace dcgpu {
+
+__device__ __forceinline__ double interp_table(const DevTables& T, int tab, double x) {
+  const double* X = T.x + T.off[tab];
+  const double* Y = T.y + T.off[tab];
+  const int n = T.len[tab];
+  if (x <= X[0]) return Y[0];
+  if (x > X[n - 1]) return Y[n - 1];
+  int lo = 0, hi = n - 1;  // X[lo] < x <= X[hi]
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (X[mid] < x) lo = mid; else hi = mid;
+  }
+  double s = (x - X[lo]) / (X[hi] - X[lo]);
+  return Y[lo] + s * (Y[hi] - Y[lo]);
+}
+
+__device__ __forceinline__ double apply_op(const Instr ins, double a, double b, double c,
+                                           const DevTables& T) {
+  switch (ins.op) {
+    case OP_ADD: return a + b;
+    case OP_SUB: return a - b;
+    case OP_MUL: return a * b;
+    case OP_DIV: return a / b;
+    case OP_POW: return pow(a, b);
+    case OP_FMOD: return fmod(a, b);
+    case OP_ATAN2: return atan2(a, b);
+    case OP_HYPOT: return hypot(a, b);
+    case OP_MIN: return fmin(a, b);
+    case OP_MAX: return fmax(a, b);
+    case OP_LT: return a < b ? 1.0 : 0.0;
+    case OP_LE: return a <= b ? 1.0 : 0.0;
+    case OP_GT: return a > b ? 1.0 : 0.0;
+    case OP_GE: return a >= b ? 1.0 : 0.0;
+    case OP_EQ: return a == b ? 1.0 : 0.0;
+    case OP_NE: return a != b ? 1.0 : 0.0;
+    case OP_AND: return (a != 0.0 && b != 0.0) ? 1.0 : 0.0;
+    case OP_OR: return (a != 0.0 || b != 0.0) ? 1.0 : 0.0;
+    case OP_NEG: return -a;
+    case OP_NOT: return a != 0.0 ? 0.0 : 1.0;
+    case OP_SQR: return a * a;
+    case OP_CUBE: return a * a * a;
+    case OP_RECIP: return 1.0 / a;
+    case OP_EXP: return exp(a);
+    case OP_LOG: return log(a);
+    case OP_LOG2: return log2(a);
+    case OP_LOG10: return log10(a);
+    case OP_SQRT: return sqrt(a);
+    case OP_SIN: return sin(a);
+    case OP_COS: return cos(a);
+    case OP_TAN: return tan(a);
+    case OP_ASIN: return asin(a);
+    case OP_ACOS: return acos(a);
+    case OP_ATAN: return atan(a);
+    case OP_SINH: return sinh(a);
+    case OP_COSH: return cosh(a);
+    case OP_TANH: return tanh(a);
+    case OP_ASINH: return asinh(a);
+    case OP_ACOSH: return acosh(a);
+    case OP_ATANH: return atanh(a);
+    case OP_ABS: return fabs(a);
+    case OP_SIGN: return a < 0.0 ? -1.0 : (a > 0.0 ? 1.0 : 0.0);
+    case OP_RINT: return rint(a);
+    case OP_FLOOR: return floor(a);
+    case OP_CEIL: return ceil(a);
+    case OP_ROUND: return round(a);
+    case OP_TRUNC: return trunc(a);
+    case OP_ERF: return erf(a);
+    case OP_ERFC: return erfc(a);
+    case OP_SEL: return a != 0.0 ? b : c;
+    case OP_POWI: {
+      int e = static_cast<int8_t>(ins.c);
+      int n = e < 0 ? -e : e;
+      double r = 1.0, x = a;
+      while (n) {
+        if (n & 1) r *= x;
+        x *= x;
+        n >>= 1;
+      }
+      return e < 0 ? 1.0 / r : r;
+    }
+    case OP_INTERP: return interp_table(T, ins.b, a);
+    default: return __longlong_as_double(0x7ff8000000000000ULL);
+  }
+}
+
+// Run a program; inputs must already be in R[0..ninputs).  All threads of a warp run the
+// same instruction stream, so the dispatch is uniform.
+__device__ __forceinline__ void run_program(const DevProgram& P, const DevTables& T, double* R) {
+  for (int pc = 0; pc < P.ncode; ++pc) {
+    const Instr ins = P.code[pc];
+    double v;
+    if (ins.op == OP_CONST) {
+      v = P.consts[ins.a | (ins.b << 8)];
+    } else {
+      const double a = R[ins.a];
+      const double b = (ins.op == OP_POWI || ins.op == OP_INTERP) ? 0.0 : R[ins.b];
+      const double c = (ins.op == OP_SEL) ? R[ins.c] : 0.0;
+      v = apply_op(ins, a, b, c, T);
+    }
+    R[ins.dst] = v;
+  }
+}
+
+}  // namespace dcgpu

@@ -1,0 +1,95 @@
+// Sparse linear algebra on the device: BSR SpMV, fused Krylov vector updates with
+// deterministic reductions, block-Jacobi preconditioning.
+//
+// Replaces the dune-istl operators the reference's LinearSolver drives
+// (dune/copasi/model/make_step_operator.hh:102-146, solver/istl/factory/*.hh).
+#pragma once
+
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace dcgpu {
+
+struct Bsr {
+  int nrows = 0;          // block rows
+  int bs = 1;             // block size
+  int64_t nnzb = 0;       // stored blocks
+  const int32_t* rowptr = nullptr;
+  const int32_t* colidx = nullptr;
+  double* val = nullptr;  // nnzb * bs * bs, row-major blocks
+  float* val32 = nullptr; // single-precision copy (mixed-precision Krylov)
+};
+
+// Reduction scratch: per-block partial sums and a completion counter.
+struct ReduceScratch {
+  double* partial = nullptr;    // kReduceBlocks * 4
+  unsigned int* counter = nullptr;
+  double* result = nullptr;     // device scalars written by the last block
+};
+constexpr int kReduceBlocks = 608;    // 4 x 152 SMs
+constexpr int kReduceThreads = 256;
+
+// y = A x   (fp64)
+void spmv(const Bsr& A, const double* x, double* y, cudaStream_t s);
+// y = A x   (fp32 values, fp32 vectors)
+void spmv32(const Bsr& A, const float* x, float* y, cudaStream_t s);
+// r = b - A x (fp64)
+void residual(const Bsr& A, const double* x, const double* b, double* r, cudaStream_t s);
+
+// result[slot] = <x, y>  (deterministic; fixed grid and order)
+void dot(const double* x, const double* y, int64_t n, ReduceScratch rs, int slot, cudaStream_t s);
+
+// block Jacobi: dinv = inverse of the diagonal blocks; returns via status[0] != 0 on a
+// singular block
+void block_jacobi_setup(const Bsr& A, const int32_t* diag, double* dinv, int* status, cudaStream_t s);
+void block_jacobi_apply(int nrows, int bs, const double* dinv, const double* x, double* y, cudaStream_t s);
+void block_jacobi_apply32(int nrows, int bs, const float* dinv, const float* x, float* y, cudaStream_t s);
+
+// BiCGSTAB fused steps; scalars live in sc[] on the device:
+//   sc[0]=rho  sc[1]=alpha  sc[2]=omega  sc[3]=rho_new  sc[4]=<rhat,v>  sc[5]=<t,s>
+//   sc[6]=<t,t> sc[7]=||r||^2  sc[8]=||s||^2  sc[9]=beta  sc[10]=breakdown flag
+void bicg_init(const double* r, double* rhat, double* p, double* v, int64_t n, ReduceScratch rs,
+               double* sc, cudaStream_t s);
+void bicg_update_p(double* p, const double* r, const double* v, int64_t n, const double* sc,
+                   cudaStream_t s);
+void bicg_alpha(const double* rhat, const double* v, int64_t n, ReduceScratch rs, double* sc,
+                cudaStream_t s);
+void bicg_s(double* s_, const double* r, const double* v, int64_t n, ReduceScratch rs, double* sc,
+            cudaStream_t s);
+void bicg_omega(const double* t, const double* s_, int64_t n, ReduceScratch rs, double* sc,
+                cudaStream_t s);
+void bicg_xr(double* x, double* r, const double* phat, const double* shat, const double* s_,
+             const double* t, const double* rhat, int64_t n, ReduceScratch rs, double* sc,
+             cudaStream_t s);
+
+// float variants for the mixed-precision inner solve (reductions stay in fp64)
+void bicg_init32(const float* r, float* rhat, float* p, float* v, int64_t n, ReduceScratch rs,
+                 double* sc, cudaStream_t s);
+void bicg_update_p32(float* p, const float* r, const float* v, int64_t n, const double* sc,
+                     cudaStream_t s);
+void bicg_alpha32(const float* rhat, const float* v, int64_t n, ReduceScratch rs, double* sc,
+                  cudaStream_t s);
+void bicg_s32(float* s_, const float* r, const float* v, int64_t n, ReduceScratch rs, double* sc,
+              cudaStream_t s);
+void bicg_omega32(const float* t, const float* s_, int64_t n, ReduceScratch rs, double* sc,
+                  cudaStream_t s);
+void bicg_xr32(float* x, float* r, const float* phat, const float* shat, const float* s_,
+               const float* t, const float* rhat, int64_t n, ReduceScratch rs, double* sc,
+               cudaStream_t s);
+
+// number of kernels this library has launched (all threads, all models)
+long long launch_count();
+void count_launches(long long n);
+
+// elementwise helpers
+void axpy(int64_t n, double a, const double* x, double* y, cudaStream_t s);          // y += a x
+void axpby(int64_t n, double a, const double* x, double b, double* y, cudaStream_t s); // y = a x + b y
+void scale_copy(int64_t n, double a, const double* x, double* y, cudaStream_t s);     // y = a x
+void to_float(int64_t n, const double* x, float* y, cudaStream_t s);
+void add_float(int64_t n, const float* x, double* y, cudaStream_t s);                 // y += x
+void to_float_scaled(int64_t n, const double* x, double scale, float* y, cudaStream_t s);
+void add_float_scaled(int64_t n, const float* x, double scale, double* y, cudaStream_t s);
+void fill(int64_t n, double v, double* y, cudaStream_t s);
+
+}  // namespace dcgpu

@@ -1,0 +1,184 @@
+// Model setup: configuration -> mesh, compartments, species, DOF blocks, BSR pattern,
+// colour classes, compiled expression programs and term tables, all resident on the
+// device.
+//
+// Mirrors DiffusionReaction::make_model / ModelMultiCompartment (dune/copasi/model/
+// diffusion_reaction/factory.hh:46-136, model_multi_compartment.impl.hh:55-92) and the
+// functor tree of local_equations.hh:617-700 built through
+// functor_factory_parser.impl.hh:25-182.  DOF layout (model_multi_compartment_traits.hh:
+// 16-23): compartment-major, vertices ascending inside a compartment, the species of the
+// compartment interleaved per vertex.  On the device every (compartment, vertex) pair is
+// one block row of size bs = max species per compartment (padded slots carry an identity
+// diagonal and a zero residual).
+#pragma once
+
+#include <cstdint>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "device.cuh"
+#include "expr.hpp"
+#include "ini.hpp"
+#include "linalg.cuh"
+#include "mesh.hpp"
+
+namespace dcgpu {
+
+class CudaError : public std::runtime_error {
+ public:
+  using std::runtime_error::runtime_error;
+};
+void cuda_check(cudaError_t e, const char* what);
+
+template <class T>
+class DeviceBuffer {
+ public:
+  DeviceBuffer() = default;
+  explicit DeviceBuffer(size_t n) { resize(n); }
+  DeviceBuffer(const DeviceBuffer&) = delete;
+  DeviceBuffer& operator=(const DeviceBuffer&) = delete;
+  DeviceBuffer(DeviceBuffer&& o) noexcept : p_(o.p_), n_(o.n_) { o.p_ = nullptr; o.n_ = 0; }
+  DeviceBuffer& operator=(DeviceBuffer&& o) noexcept {
+    if (this != &o) { release(); p_ = o.p_; n_ = o.n_; o.p_ = nullptr; o.n_ = 0; }
+    return *this;
+  }
+  ~DeviceBuffer() { release(); }
+  void resize(size_t n) {
+    release();
+    if (n) cuda_check(cudaMalloc(&p_, n * sizeof(T)), "cudaMalloc");
+    n_ = n;
+  }
+  void upload(const std::vector<T>& h) {
+    resize(h.size());
+    if (n_) cuda_check(cudaMemcpy(p_, h.data(), n_ * sizeof(T), cudaMemcpyHostToDevice), "upload");
+  }
+  std::vector<T> download() const {
+    std::vector<T> h(n_);
+    if (n_) cuda_check(cudaMemcpy(h.data(), p_, n_ * sizeof(T), cudaMemcpyDeviceToHost), "download");
+    return h;
+  }
+  T* get() const { return p_; }
+  size_t size() const { return n_; }
+
+ private:
+  void release() {
+    if (p_) cudaFree(p_);
+    p_ = nullptr;
+    n_ = 0;
+  }
+  T* p_ = nullptr;
+  size_t n_ = 0;
+};
+
+struct SpeciesInfo {
+  std::string name;
+  int comp = 0;   // compartment index
+  int local = 0;  // index inside the compartment
+  int global = 0; // model-wide index
+};
+
+// one compiled program + its device copy
+struct ProgramBundle {
+  Program host;
+  DeviceBuffer<Instr> code;
+  DeviceBuffer<double> consts;
+  DeviceBuffer<uint16_t> inputs;
+  DeviceBuffer<uint8_t> outputs;
+  DevProgram view() const;
+  void upload();
+};
+
+struct VolumeGroup {
+  int comp = 0, ns = 0;
+  int64_t ne = 0;
+  std::vector<int> color_offsets;  // colour c: [off[c], off[c+1])
+  DeviceBuffer<int32_t> verts, nodes, bpos;
+  ProgramBundle prog_res, prog_all;
+  std::vector<Term> res_terms_r, res_terms_a, jac_terms;  // for prog_res / prog_all
+  DeviceBuffer<Term> d_res_r, d_res_a, d_jac;
+  bool has_mass = false, has_stiffness = false;
+};
+
+struct FaceGroup {
+  int comp[2] = {-1, -1};
+  bool boundary = false;
+  int64_t nf = 0;
+  std::vector<int> color_offsets;
+  DeviceBuffer<int32_t> fverts, node_in, node_out, bpos, elem_in, elem_out;
+  DeviceBuffer<double> normal, ielem, fvolume;
+  ProgramBundle prog[2];
+  std::vector<Term> terms[2];
+  DeviceBuffer<Term> d_terms[2];
+};
+
+class Model {
+ public:
+  Model(const std::string& ini_text, const std::string& overrides);
+  ~Model() = default;
+
+  // configuration
+  Ini cfg;
+  ParserContext ctx;
+  Mesh mesh;
+  int dim = 2;
+  std::vector<std::string> comp_names;
+  std::vector<int32_t> elem_comp;              // compartment of each element (-1: none)
+  std::vector<SpeciesInfo> species;
+  std::vector<int> ns;                          // species per compartment
+  std::vector<int> species_offset;              // global index of the first species of each compartment
+  bool is_linear = false;
+  bool numerical_jacobian = false;
+  int bs = 1;
+
+  // block rows
+  int64_t nnodes = 0;
+  int64_t ndof = 0;                             // reference DOF count (no padding)
+  std::vector<int64_t> comp_node_offset;
+  std::vector<std::vector<int32_t>> comp_vertices;  // ascending global vertex ids per compartment
+  std::vector<std::vector<int32_t>> comp_vnode;     // vertex -> block row (-1 if absent)
+  std::vector<int8_t> row_ns;                   // species count of each block row
+
+  // BSR pattern
+  std::vector<int32_t> rowptr, colidx, diag;
+  DeviceBuffer<int32_t> d_rowptr, d_colidx, d_diag;
+  DeviceBuffer<int8_t> d_row_ns;
+  bool padded = false;
+
+  // geometry on the device
+  DeviceBuffer<double> d_coords;
+  DeviceBuffer<int32_t> d_cells;
+  std::vector<DeviceBuffer<int32_t>> d_comp_vnode;
+  DeviceBuffer<double> d_tab_x, d_tab_y;
+  DeviceBuffer<int> d_tab_off, d_tab_len;
+  DevTables tables{};
+
+  std::vector<VolumeGroup> vgroups;
+  std::vector<FaceGroup> fgroups;
+
+  // host-side helpers
+  std::vector<double> initial_state() const;        // reference DOF order
+  void to_blocked(const std::vector<double>& ref, std::vector<double>& blk) const;
+  void from_blocked(const std::vector<double>& blk, std::vector<double>& ref) const;
+  int64_t ref_dof(int comp, int32_t vloc, int local) const;
+
+  // assemble into r (residual, may be null) and J (BSR values, may be null):
+  //   r += cm * M(x, t) + ca * A(x, t),  J += cm * dM/dx + ca * dA/dx
+  // mode bit 1: residual, bit 2: Jacobian.
+  void assemble(const double* x, double t, double cm, double ca, double* r, double* J, int mode,
+                cudaStream_t s) const;
+  Bsr bsr(double* val, float* val32) const;
+  int64_t nnzb() const { return static_cast<int64_t>(colidx.size()); }
+
+ private:
+  void build_species();
+  void build_nodes();
+  void build_volume_groups();
+  void build_face_groups();
+  void build_pattern();
+  void upload_geometry();
+};
+
+}  // namespace dcgpu

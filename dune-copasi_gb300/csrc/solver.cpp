@@ -1,0 +1,528 @@
+#include "solver.hpp"
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <limits>
+
+#include "assemble.cuh"
+#include "linalg.cuh"
+
+namespace dcgpu {
+
+// ------------------------------------------------------------------ Runge-Kutta tables
+// PDELab one-step parameter form: stage i (1-based) solves
+//   sum_{j<=i} A[i-1][j] M(u_j, t + D[j] dt) + B[i-1][j] dt A(u_j, t + D[j] dt) = 0
+
+RKTable RKTable::make(const std::string& name) {
+  RKTable t;
+  if (name == "ImplicitEuler") {
+    t.A = {{-1.0, 1.0}};
+    t.B = {{0.0, 1.0}};
+    t.D = {0.0, 1.0};
+  } else if (name == "ExplicitEuler") {
+    t.A = {{-1.0, 1.0}};
+    t.B = {{1.0, 0.0}};
+    t.D = {0.0, 1.0};
+  } else if (name == "Alexander2") {
+    const double a = 1.0 - 0.5 * std::sqrt(2.0);
+    t.A = {{-1.0, 1.0, 0.0}, {-1.0, 0.0, 1.0}};
+    t.B = {{0.0, a, 0.0}, {0.0, 1.0 - a, a}};
+    t.D = {0.0, a, 1.0};
+  } else if (name == "Heun") {
+    t.A = {{-1.0, 1.0, 0.0}, {-0.5, -0.5, 1.0}};
+    t.B = {{1.0, 0.0, 0.0}, {0.0, 0.5, 0.0}};
+    t.D = {0.0, 1.0, 1.0};
+  } else if (name == "Shu3") {
+    t.A = {{-1.0, 1.0, 0.0, 0.0}, {-0.75, -0.25, 1.0, 0.0}, {-1.0 / 3.0, 0.0, -2.0 / 3.0, 1.0}};
+    t.B = {{1.0, 0.0, 0.0, 0.0}, {0.0, 0.25, 0.0, 0.0}, {0.0, 0.0, 2.0 / 3.0, 0.0}};
+    t.D = {0.0, 1.0, 0.5, 1.0};
+  } else if (name == "RungeKutta4") {
+    t.A = {{-1.0, 1.0, 0.0, 0.0, 0.0}, {-1.0, 0.0, 1.0, 0.0, 0.0}, {-1.0, 0.0, 0.0, 1.0, 0.0},
+           {-1.0, 0.0, 0.0, 0.0, 1.0}};
+    t.B = {{0.5, 0.0, 0.0, 0.0, 0.0}, {0.0, 0.5, 0.0, 0.0, 0.0}, {0.0, 0.0, 1.0, 0.0, 0.0},
+           {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0, 0.0}};
+    t.D = {0.0, 0.5, 0.5, 1.0, 1.0};
+  } else if (name == "FractionalStepTheta") {
+    const double th = 1.0 - 0.5 * std::sqrt(2.0), thp = 1.0 - 2.0 * th, al = 2.0 - std::sqrt(2.0),
+                 be = 1.0 - al;
+    t.A = {{-1.0, 1.0, 0.0, 0.0}, {0.0, -1.0, 1.0, 0.0}, {0.0, 0.0, -1.0, 1.0}};
+    t.B = {{th * be, th * al, 0.0, 0.0}, {0.0, thp * al, thp * be, 0.0}, {0.0, 0.0, th * be, th * al}};
+    t.D = {0.0, th, 1.0 - th, 1.0};
+  } else if (name == "Alexander3") {
+    const double al = 0.4358665215084590, tau2 = (1.0 + al) / 2.0;
+    const double b1 = -(6.0 * al * al - 16.0 * al + 1.0) / 4.0, b2 = (6.0 * al * al - 20.0 * al + 5.0) / 4.0;
+    t.A = {{-1.0, 1.0, 0.0, 0.0}, {-1.0, 0.0, 1.0, 0.0}, {-1.0, 0.0, 0.0, 1.0}};
+    t.B = {{0.0, al, 0.0, 0.0}, {0.0, tau2 - al, al, 0.0}, {0.0, b1, b2, al}};
+    t.D = {0.0, al, tau2, 1.0};
+  } else {
+    throw ConfigError("Not known time stepping type '" + name + "'");
+  }
+  return t;
+}
+
+// dune FloatCmp, relativeWeak with epsilon = 8 * DBL_EPSILON
+static bool f_eq(double a, double b) { return std::fabs(a - b) <= 8.0 * DBL_EPSILON * std::max(std::fabs(a), std::fabs(b)); }
+static bool f_le(double a, double b) { return a < b || f_eq(a, b); }
+static bool f_lt(double a, double b) { return a < b && !f_eq(a, b); }
+static bool f_gt(double a, double b) { return a > b && !f_eq(a, b); }
+
+Solver::Solver(Model& m, cudaStream_t s) : model(m), stream(s) {
+  n_ = m.nnodes * m.bs;
+  x_.resize(n_);
+  r_.resize(n_);
+  stage_.resize(n_);
+  const_.resize(n_);
+  z_.resize(n_);
+  J_.resize(static_cast<size_t>(m.nnzb()) * m.bs * m.bs);
+  kr_.resize(n_); krhat_.resize(n_); kp_.resize(n_); kv_.resize(n_); ks_.resize(n_); kt_.resize(n_);
+  kphat_.resize(n_); kshat_.resize(n_); kx_.resize(n_);
+  dinv_.resize(static_cast<size_t>(m.nnodes) * m.bs * m.bs);
+  partial_.resize(kReduceBlocks * 4);
+  scal_.resize(32);
+  counter_.resize(1);
+  status_.resize(1);
+  cuda_check(cudaMemset(counter_.get(), 0, sizeof(unsigned int)), "memset");
+  cuda_check(cudaMemset(scal_.get(), 0, 32 * sizeof(double)), "memset");
+  cuda_check(cudaMallocHost(&pinned_, 32 * sizeof(double)), "cudaMallocHost");
+  rs_.partial = partial_.get();
+  rs_.counter = counter_.get();
+  rs_.result = scal_.get() + 16;
+
+  Ini tso = m.cfg.sub("model").sub("time_step_operator");
+  scheme_ = tso.get("type", "Alexander2");
+  RKTable::make(scheme_);  // validate
+  Ini ns = tso.sub("nonlinear_solver");
+  newton_rel_ = ns.get_double("convergence_condition.relative_tolerance", 1e-4);
+  auto range = ns.get_doubles("convergence_condition.iteration_range", {0.0, 40.0});
+  if (range.size() != 2) throw ConfigError("convergence_condition.iteration_range needs two values");
+  it_min_ = static_cast<int>(range[0]);
+  it_max_ = static_cast<int>(range[1]);
+  newton_abs_ = ns.get_double("convergence_condition.absolute_tolerance", 0.0);
+  lin_threshold_ = ns.get_double("linearization_threshold", 0.0);
+  dx_fixed_ = ns.get_bool("dx_inverse_fixed_tolerance", false);
+  dx_min_rel_ = ns.get_double("dx_inverse_min_relative_tolerance", 0.1);
+  norm_ = ns.get("norm", "l_2");
+  if (norm_ != "l_2" && norm_ != "l_inf" && norm_ != "l_1") throw ConfigError("Not known nonlinear norm '" + norm_ + "'");
+  Ini ls = tso.sub("linear_solver");
+  std::string lt = ls.get("type", "UMFPack");
+  // direct solvers of the reference (UMFPack default, SuperLU, DenseInverse) are replaced
+  // by a BiCGSTAB solve converged to near machine precision
+  lin_direct_ = (lt == "UMFPack" || lt == "SuperLU" || lt == "DenseInverse");
+  lin_rel_ = ls.get_double("convergence_condition.relative_tolerance", 1e-4);
+  lin_max_it_ = 500;
+  if (ls.has_key("convergence_condition.iteration_range")) {
+    auto r = ls.get_doubles("convergence_condition.iteration_range", {1.0, 500.0});
+    lin_max_it_ = static_cast<int>(r.back());
+  }
+  if (lin_direct_) lin_max_it_ = std::max(lin_max_it_, 5000);
+  precond_ = ls.get("preconditioner.type", "Jacobi");
+  const bool want_mixed = ls.get("precision", "double") == "mixed";
+  dec_ = tso.get_double("time_step_decrease_factor", 0.5);
+  inc_ = tso.get_double("time_step_increase_factor", 1.1);
+  has_min_ = tso.has_key("time_step_min");
+  has_max_ = tso.has_key("time_step_max");
+  dt_min_ = tso.get_double("time_step_min", 0.0);
+  dt_max_ = tso.get_double("time_step_max", 0.0);
+  if (f_gt(dec_, 1.0) || f_lt(dec_, 0.0)) throw ConfigError("Decrease factor must be in the range of (0,1]");
+  if (f_lt(inc_, 1.0)) throw ConfigError("Increase factor must be in the range of (1,inf)");
+  enable_mixed(want_mixed);
+  std::vector<double> init = m.initial_state();
+  set_state(init, tso.get_double("time_begin", 0.0));
+}
+
+void Solver::enable_mixed(bool on) {
+  mixed_precision = on;
+  if (on && fr_.size() != static_cast<size_t>(n_)) {
+    fr_.resize(n_); frhat_.resize(n_); fp_.resize(n_); fv_.resize(n_); fs_.resize(n_); ft_.resize(n_);
+    fphat_.resize(n_); fshat_.resize(n_); fx_.resize(n_); fb_.resize(n_);
+    fdinv_.resize(static_cast<size_t>(model.nnodes) * model.bs * model.bs);
+    J32_.resize(static_cast<size_t>(model.nnzb()) * model.bs * model.bs);
+  }
+}
+
+Solver::~Solver() {
+  if (pinned_) cudaFreeHost(pinned_);
+  for (auto& p : pending_) {
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.b);
+  }
+  for (cudaEvent_t e : event_pool_) cudaEventDestroy(e);
+}
+
+void Solver::set_state(const std::vector<double>& ref, double t) {
+  if (static_cast<int64_t>(ref.size()) != model.ndof) throw std::invalid_argument("state size mismatch");
+  std::vector<double> blk;
+  model.to_blocked(ref, blk);
+  cuda_check(cudaMemcpyAsync(x_.get(), blk.data(), blk.size() * sizeof(double), cudaMemcpyHostToDevice, stream),
+             "set_state");
+  cuda_check(cudaStreamSynchronize(stream), "set_state");
+  t_ = t;
+}
+
+std::vector<double> Solver::get_state() const {
+  std::vector<double> blk(n_);
+  cuda_check(cudaMemcpyAsync(blk.data(), x_.get(), n_ * sizeof(double), cudaMemcpyDeviceToHost, stream), "get_state");
+  cuda_check(cudaStreamSynchronize(stream), "get_state");
+  std::vector<double> ref;
+  model.from_blocked(blk, ref);
+  return ref;
+}
+
+double Solver::read_scalar(int slot) {
+  double v;
+  read_scalars(&v, slot, 1);
+  return v;
+}
+
+void Solver::read_scalars(double* out, int first, int count) {
+  cuda_check(cudaMemcpyAsync(pinned_, scal_.get() + first, count * sizeof(double), cudaMemcpyDeviceToHost, stream),
+             "read scalars");
+  cuda_check(cudaStreamSynchronize(stream), "read scalars");
+  for (int i = 0; i < count; ++i) out[i] = pinned_[i];
+  tflush();
+}
+
+void Solver::enable_profiling(bool on) {
+  profiling_ = on;
+  kernel_times = KernelTimes{};
+}
+
+void Solver::tbegin(int cat) {
+  if (!profiling_) return;
+  PendingTiming p{cat, nullptr, nullptr};
+  for (cudaEvent_t* e : {&p.a, &p.b}) {
+    if (!event_pool_.empty()) {
+      *e = event_pool_.back();
+      event_pool_.pop_back();
+    } else {
+      cuda_check(cudaEventCreate(e), "cudaEventCreate");
+    }
+  }
+  cuda_check(cudaEventRecord(p.a, stream), "cudaEventRecord");
+  pending_.push_back(p);
+}
+
+void Solver::tend() {
+  if (!profiling_ || pending_.empty()) return;
+  cuda_check(cudaEventRecord(pending_.back().b, stream), "cudaEventRecord");
+}
+
+void Solver::tflush() {
+  if (pending_.empty()) return;
+  for (auto& p : pending_) {
+    float ms = 0.0f;
+    cuda_check(cudaEventElapsedTime(&ms, p.a, p.b), "cudaEventElapsedTime");
+    kernel_times.ms[p.cat] += ms;
+    kernel_times.calls[p.cat] += 1;
+    event_pool_.push_back(p.a);
+    event_pool_.push_back(p.b);
+  }
+  pending_.clear();
+}
+
+double Solver::norm2(const double* v) {
+  dot(v, v, n_, rs_, 0, stream);
+  return read_scalar(16);
+}
+
+void Solver::setup_preconditioner() {
+  cuda_check(cudaMemsetAsync(status_.get(), 0, sizeof(int), stream), "memset");
+  Bsr A = model.bsr(J_.get(), nullptr);
+  block_jacobi_setup(A, model.d_diag.get(), dinv_.get(), status_.get(), stream);
+  int st = 0;
+  cuda_check(cudaMemcpyAsync(&st, status_.get(), sizeof(int), cudaMemcpyDeviceToHost, stream), "status");
+  cuda_check(cudaStreamSynchronize(stream), "status");
+  if (st) throw StepFailure("singular diagonal block in the Jacobian");
+  if (mixed_precision) {
+    to_float(static_cast<int64_t>(model.nnzb()) * model.bs * model.bs, J_.get(), J32_.get(), stream);
+    to_float(static_cast<int64_t>(model.nnodes) * model.bs * model.bs, dinv_.get(), fdinv_.get(), stream);
+  }
+}
+
+int Solver::bicgstab(const double* b, double* z, double rel_tol, int max_it, int* iters) {
+  // z = 0 start: r = b
+  Bsr A = model.bsr(J_.get(), nullptr);
+  const int64_t n = n_;
+  cuda_check(cudaMemsetAsync(z, 0, n * sizeof(double), stream), "memset");
+  cuda_check(cudaMemcpyAsync(kr_.get(), b, n * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");
+  double* sc = scal_.get();
+  bicg_init(kr_.get(), krhat_.get(), kp_.get(), kv_.get(), n, rs_, sc, stream);
+  double h[11];
+  read_scalars(h, 0, 11);
+  const double r0 = std::sqrt(h[7]);
+  *iters = 0;
+  if (r0 == 0.0) return DC_OK;
+  if (!std::isfinite(r0)) return DC_ERR_DIVERGED;
+  const double target = rel_tol * r0;
+  for (int it = 1; it <= max_it; ++it) {
+    bicg_update_p(kp_.get(), kr_.get(), kv_.get(), n, sc, stream);
+    tbegin(2);
+    block_jacobi_apply(A.nrows, A.bs, dinv_.get(), kp_.get(), kphat_.get(), stream);
+    tend();
+    tbegin(1);
+    spmv(A, kphat_.get(), kv_.get(), stream);
+    tend();
+    bicg_alpha(krhat_.get(), kv_.get(), n, rs_, sc, stream);
+    bicg_s(ks_.get(), kr_.get(), kv_.get(), n, rs_, sc, stream);
+    tbegin(2);
+    block_jacobi_apply(A.nrows, A.bs, dinv_.get(), ks_.get(), kshat_.get(), stream);
+    tend();
+    tbegin(1);
+    spmv(A, kshat_.get(), kt_.get(), stream);
+    tend();
+    bicg_omega(kt_.get(), ks_.get(), n, rs_, sc, stream);
+    bicg_xr(z, kr_.get(), kphat_.get(), kshat_.get(), ks_.get(), kt_.get(), krhat_.get(), n, rs_, sc, stream);
+    read_scalars(h, 0, 11);
+    *iters = it;
+    const double rn = std::sqrt(h[7]);
+    if (!std::isfinite(rn)) return DC_ERR_DIVERGED;
+    if (rn <= target) return DC_OK;
+    if (h[10] != 0.0) {
+      // breakdown: accept if already good enough, otherwise report failure
+      return rn <= target ? DC_OK : DC_ERR_DIVERGED;
+    }
+  }
+  return DC_ERR_TIMEOUT;
+}
+
+// fp32 BiCGSTAB on the correction equation inside fp64 iterative refinement:
+//   r = b - J z (fp64);  solve J d = r in fp32 to a modest reduction;  z += d
+int Solver::bicgstab_mixed(const double* b, double* z, double rel_tol, int max_it, int* iters) {
+  Bsr A = model.bsr(J_.get(), J32_.get());
+  const int64_t n = n_;
+  double* sc = scal_.get();
+  cuda_check(cudaMemsetAsync(z, 0, n * sizeof(double), stream), "memset");
+  const double b0 = std::sqrt(norm2(b));
+  *iters = 0;
+  if (b0 == 0.0) return DC_OK;
+  if (!std::isfinite(b0)) return DC_ERR_DIVERGED;
+  const double target = rel_tol * b0;
+  const double inner_red = 1e-4;
+  double rn = b0;
+  int total = 0;
+  for (int ref = 0; ref < 50 && total < max_it; ++ref) {
+    // fp64 refinement residual r = b - J z (skip the SpMV for z = 0)
+    if (ref == 0) cuda_check(cudaMemcpyAsync(kr_.get(), b, n * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");
+    else residual(A, z, b, kr_.get(), stream);
+    if (ref > 0) {
+      rn = std::sqrt(norm2(kr_.get()));
+      if (!std::isfinite(rn)) return DC_ERR_DIVERGED;
+      if (rn <= target) { *iters = total; return DC_OK; }
+    }
+    ++stats.refinements;
+    // scale into fp32 range
+    const double scale = 1.0 / rn;
+    to_float_scaled(n, kr_.get(), scale, fr_.get(), stream);
+    cuda_check(cudaMemsetAsync(fx_.get(), 0, n * sizeof(float), stream), "memset");
+    bicg_init32(fr_.get(), frhat_.get(), fp_.get(), fv_.get(), n, rs_, sc, stream);
+    double h[11];
+    read_scalars(h, 0, 11);
+    const double f0 = std::sqrt(h[7]);
+    const double ftarget = std::max(inner_red, 0.5 * target / rn) * f0;
+    for (int it = 1; it <= max_it - total; ++it) {
+      bicg_update_p32(fp_.get(), fr_.get(), fv_.get(), n, sc, stream);
+      tbegin(2);
+      block_jacobi_apply32(A.nrows, A.bs, fdinv_.get(), fp_.get(), fphat_.get(), stream);
+      tend();
+      tbegin(1);
+      spmv32(A, fphat_.get(), fv_.get(), stream);
+      tend();
+      bicg_alpha32(frhat_.get(), fv_.get(), n, rs_, sc, stream);
+      bicg_s32(fs_.get(), fr_.get(), fv_.get(), n, rs_, sc, stream);
+      tbegin(2);
+      block_jacobi_apply32(A.nrows, A.bs, fdinv_.get(), fs_.get(), fshat_.get(), stream);
+      tend();
+      tbegin(1);
+      spmv32(A, fshat_.get(), ft_.get(), stream);
+      tend();
+      bicg_omega32(ft_.get(), fs_.get(), n, rs_, sc, stream);
+      bicg_xr32(fx_.get(), fr_.get(), fphat_.get(), fshat_.get(), fs_.get(), ft_.get(), frhat_.get(), n, rs_, sc, stream);
+      read_scalars(h, 0, 11);
+      ++total;
+      const double fn = std::sqrt(h[7]);
+      if (!std::isfinite(fn)) return DC_ERR_DIVERGED;
+      if (fn <= ftarget || h[10] != 0.0) break;
+    }
+    add_float_scaled(n, fx_.get(), rn, z, stream);
+  }
+  residual(A, z, b, kr_.get(), stream);
+  rn = std::sqrt(norm2(kr_.get()));
+  *iters = total;
+  return rn <= target ? DC_OK : DC_ERR_TIMEOUT;
+}
+
+int Solver::linear_solve(const double* b, double* z, double rel_tol, int* iters) {
+  setup_preconditioner();
+  int it = 0;
+  int st = mixed_precision ? bicgstab_mixed(b, z, rel_tol, lin_max_it_, &it) : bicgstab(b, z, rel_tol, lin_max_it_, &it);
+  if (iters) *iters = it;
+  stats.linear_iterations += it;
+  ++stats.linear_solves;
+  return st;
+}
+
+void Solver::linear_step(double* x, const std::function<void(const double*, double*)>& res,
+                         const std::function<void(const double*)>& jac) {
+  // make_step_operator.hh:210-245: b = F(x); solve J z = b; x -= z
+  res(x, r_.get());
+  jac(x);
+  int it = 0;
+  const double tol = lin_direct_ ? 1e-13 : lin_rel_;
+  int st = linear_solve(r_.get(), z_.get(), tol, &it);
+  if (st != DC_OK) throw StepFailure("linear solver did not converge");
+  axpy(n_, -1.0, z_.get(), x, stream);
+}
+
+void Solver::newton(double* x, const std::function<void(const double*, double*)>& res,
+                    const std::function<void(const double*)>& jac) {
+  auto norm = [&](const double* v) -> double {
+    if (norm_ == "l_2") return norm2(v);  // two_norm2: the SQUARED norm (make_step_operator.hh:274-276)
+    std::vector<double> h(n_);
+    cuda_check(cudaMemcpyAsync(h.data(), v, n_ * sizeof(double), cudaMemcpyDeviceToHost, stream), "norm");
+    cuda_check(cudaStreamSynchronize(stream), "norm");
+    double acc = 0.0;
+    for (double e : h) acc = (norm_ == "l_inf") ? std::max(acc, std::fabs(e)) : acc + std::fabs(e);
+    return acc;
+  };
+  res(x, r_.get());
+  double defect = norm(r_.get());
+  const double first = defect;
+  double prev = defect;
+  int it = 0;
+  bool have_jac = false;
+  while (true) {
+    if (!std::isfinite(defect)) throw StepFailure("Newton defect is not finite");
+    if (it >= it_min_ && (defect <= newton_abs_ || defect < first * newton_rel_ || defect == 0.0)) break;
+    if (it >= it_max_) throw StepFailure("Newton did not converge within the iteration range", DC_ERR_DIVERGED);
+    if (!have_jac || lin_threshold_ <= 0.0 || !(prev > 0.0 && defect / prev < lin_threshold_)) {
+      jac(x);
+      have_jac = true;
+    }
+    double red;
+    if (lin_direct_) {
+      red = 1e-13;
+    } else if (dx_fixed_) {
+      red = dx_min_rel_;
+    } else {
+      const double stop = std::max(first * newton_rel_, newton_abs_);
+      const double q = (prev > 0.0) ? (defect * defect) / (prev * prev) : 1.0;
+      if (stop / (10.0 * defect) > q) red = stop / (10.0 * defect);
+      else red = std::min(dx_min_rel_, q);
+    }
+    int lit = 0;
+    int st = linear_solve(r_.get(), z_.get(), red, &lit);
+    if (st != DC_OK) throw StepFailure("linear solver did not converge");
+    axpy(n_, -1.0, z_.get(), x, stream);
+    prev = defect;
+    res(x, r_.get());
+    defect = norm(r_.get());
+    ++it;
+  }
+  stats.newton_iterations += it;
+  stats.last_newton = it;
+}
+
+void Solver::one_step(double dt) {
+  const RKTable tab = RKTable::make(scheme_);
+  const int s = static_cast<int>(tab.A.size());
+  if (static_cast<int>(us_.size()) < s + 1) {
+    us_.resize(s + 1);
+    for (auto& u : us_) if (u.size() != static_cast<size_t>(n_)) u.resize(n_);
+  }
+  const double t = t_;
+  std::vector<double> ts(s + 1);
+  for (int j = 0; j <= s; ++j) ts[j] = t + tab.D[j] * dt;
+  cuda_check(cudaMemcpyAsync(us_[0].get(), x_.get(), n_ * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");
+  cuda_check(cudaMemcpyAsync(stage_.get(), x_.get(), n_ * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");
+  const int64_t nj = static_cast<int64_t>(model.nnzb()) * model.bs * model.bs;
+  for (int i = 1; i <= s; ++i) {
+    const auto& a = tab.A[i - 1];
+    const auto& b = tab.B[i - 1];
+    // explicit part of the stage residual, fixed during the Newton solve
+    cuda_check(cudaMemsetAsync(const_.get(), 0, n_ * sizeof(double), stream), "memset");
+    for (int j = 0; j < i; ++j) {
+      if (a[j] == 0.0 && b[j] == 0.0) continue;
+      tbegin(0);
+      model.assemble(us_[j].get(), ts[j], a[j], b[j] * dt, const_.get(), nullptr, 1, stream);
+      tend();
+      ++stats.assemblies;
+    }
+    const double ai = a[i], bi = b[i] * dt, ti = ts[i];
+    auto res = [&](const double* y, double* r) {
+      cuda_check(cudaMemcpyAsync(r, const_.get(), n_ * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");
+      tbegin(0);
+      model.assemble(y, ti, ai, bi, r, nullptr, 1, stream);
+      tend();
+      ++stats.assemblies;
+    };
+    auto jac = [&](const double* y) {
+      cuda_check(cudaMemsetAsync(J_.get(), 0, nj * sizeof(double), stream), "memset");
+      tbegin(0);
+      model.assemble(y, ti, ai, bi, nullptr, J_.get(), 2, stream);
+      tend();
+      if (model.padded)
+        launch_pad_identity(model.d_diag.get(), model.d_row_ns.get(), static_cast<int>(model.nnodes), model.bs,
+                            J_.get(), 1.0, stream);
+      ++stats.assemblies;
+    };
+    if (model.is_linear) linear_step(stage_.get(), res, jac);
+    else newton(stage_.get(), res, jac);
+    cuda_check(cudaMemcpyAsync(us_[i].get(), stage_.get(), n_ * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");
+  }
+  cuda_check(cudaMemcpyAsync(x_.get(), stage_.get(), n_ * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");
+  cuda_check(cudaStreamSynchronize(stream), "step");
+  tflush();
+}
+
+int Solver::do_step(double& dt, double* dt_used) {
+  auto check = [&](double d) {
+    if (has_min_ && f_lt(std::fabs(d), std::fabs(dt_min_))) return false;
+    if (has_max_ && f_gt(std::fabs(d), std::fabs(dt_max_))) return false;
+    return true;
+  };
+  if (!check(dt)) return DC_ERR_DT_MIN;
+  while (true) {
+    try {
+      one_step(dt);
+      break;
+    } catch (const StepFailure&) {
+      ++stats.failed_steps;
+      // restore the state of the step's start (x_ is only overwritten on success)
+      dt = dt * dec_;
+      if (!check(dt)) return DC_ERR_DT_MIN;
+    }
+  }
+  if (dt_used) *dt_used = dt;
+  t_ = t_ + dt;
+  ++stats.steps;
+  double nd = dt * inc_;
+  if (has_max_) nd = std::clamp(nd, -std::fabs(dt_max_), std::fabs(dt_max_));
+  dt = nd;
+  return DC_OK;
+}
+
+int Solver::evolve(double t_end, double& dt, const std::function<void(double)>& cb) {
+  while (f_le(t_ + 2.0 * dt, t_end)) {
+    int st = do_step(dt);
+    if (st != DC_OK) return st;
+    if (cb) cb(t_);
+  }
+  int snap = 0;
+  while (f_lt(t_, t_end)) {
+    const int k = static_cast<int>(std::ceil((t_end - t_) / dt));
+    if (k <= 0) return DC_ERR_INTERNAL;
+    dt = (t_end - t_) / k;
+    int st = do_step(dt);
+    if (st == DC_OK) {
+      if (cb) cb(t_);
+    } else {
+      if (snap == 100) return st;
+      ++snap;
+      dt *= 0.5;
+    }
+  }
+  return DC_OK;
+}
+
+}  // namespace dcgpu

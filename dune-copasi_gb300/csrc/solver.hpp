@@ -1,0 +1,154 @@
+// Time stepping on the device: Runge-Kutta stages, Newton, preconditioned BiCGSTAB.
+//
+// Restates, for the GPU:
+//   * the Runge-Kutta one-step operator of dune/copasi/model/make_step_operator.hh:408-443
+//     (PDELab one-step parameter tables: ImplicitEuler, Alexander2 (default), ...);
+//   * the Newton configuration of make_step_operator.hh:246-288 (relative tolerance on the
+//     SQUARED l2 norm by default, iteration range {0,40}, linearization threshold, adaptive
+//     linear tolerance) and the linear defect-correction branch :210-245;
+//   * the LinearSolver of make_step_operator.hh:102-146, with the dune-istl Krylov solve
+//     replaced by a device BiCGSTAB (block-Jacobi preconditioned; fp64, or fp32 inside
+//     fp64 iterative refinement);
+//   * SimpleAdaptiveStepper::do_step and TimeStepper::evolve / snap_to_time
+//     (dune/copasi/common/stepper.hh:95-239, 337-368).
+#pragma once
+
+#include <functional>
+#include <string>
+#include <vector>
+
+#include "model.hpp"
+
+namespace dcgpu {
+
+enum Status : int {
+  DC_OK = 0,
+  DC_ERR_DIVERGED = 1,     // Newton / linear solve did not converge
+  DC_ERR_DT_MIN = 2,       // time step reached its lower limit
+  DC_ERR_TIMEOUT = 3,      // iteration cap hit
+  DC_ERR_CONFIG = 4,
+  DC_ERR_CUDA = 5,
+  DC_ERR_ARGUMENT = 6,
+  DC_ERR_INTERNAL = 7,
+};
+
+struct RKTable {
+  std::vector<std::vector<double>> A, B;
+  std::vector<double> D;
+  static RKTable make(const std::string& name);
+};
+
+struct SolverStats {
+  long newton_iterations = 0;
+  long linear_iterations = 0;
+  long linear_solves = 0;
+  long assemblies = 0;
+  long failed_steps = 0;
+  long steps = 0;
+  long refinements = 0;
+  int last_newton = 0;
+};
+
+class StepFailure : public std::runtime_error {
+ public:
+  explicit StepFailure(const std::string& w, int code = DC_ERR_DIVERGED) : std::runtime_error(w), code(code) {}
+  int code;
+};
+
+class Solver {
+ public:
+  explicit Solver(Model& m, cudaStream_t stream = nullptr);
+  ~Solver();
+  Solver(const Solver&) = delete;
+  Solver& operator=(const Solver&) = delete;
+
+  // state (reference DOF order on the host)
+  void set_state(const std::vector<double>& ref, double t);
+  std::vector<double> get_state() const;
+  double time() const { return t_; }
+  const double* device_state() const { return x_.get(); }
+  double* device_state() { return x_.get(); }
+
+  // one Runge-Kutta step from (x, t) with dt, result in x on success; throws StepFailure
+  void one_step(double dt);
+  // SimpleAdaptiveStepper::do_step; returns status, updates dt to the suggested next dt
+  int do_step(double& dt, double* dt_used = nullptr);
+  // TimeStepper::evolve (snap to end time); callback after each successful step
+  int evolve(double t_end, double& dt, const std::function<void(double)>& cb);
+
+  // linear algebra entry points for tests
+  int linear_solve(const double* b, double* z, double rel_tol, int* iters);
+  double* jacobian_values() { return J_.get(); }
+  double* residual_buffer() { return r_.get(); }
+
+  void enable_mixed(bool on);
+
+  // per-category device time of the hot launches, measured with CUDA events on the
+  // solver's stream: 0 = assembly (all colour launches of one operator evaluation),
+  // 1 = SpMV (fp64 and fp32), 2 = preconditioner apply
+  static constexpr int kTimerCategories = 3;
+  struct KernelTimes {
+    double ms[kTimerCategories] = {0, 0, 0};
+    long long calls[kTimerCategories] = {0, 0, 0};
+  };
+  void enable_profiling(bool on);
+  KernelTimes kernel_times;
+
+  SolverStats stats;
+  Model& model;
+  bool mixed_precision = false;
+  cudaStream_t stream;
+
+ private:
+  void newton(double* x, const std::function<void(const double*, double*)>& res,
+              const std::function<void(const double*)>& jac);
+  void linear_step(double* x, const std::function<void(const double*, double*)>& res,
+                   const std::function<void(const double*)>& jac);
+  void setup_preconditioner();
+  int bicgstab(const double* b, double* z, double rel_tol, int max_it, int* iters);
+  int bicgstab_mixed(const double* b, double* z, double rel_tol, int max_it, int* iters);
+  double norm2(const double* v);
+  double read_scalar(int slot);
+  void read_scalars(double* out, int first, int count);
+
+  struct PendingTiming {
+    int cat;
+    cudaEvent_t a, b;
+  };
+  bool profiling_ = false;
+  std::vector<cudaEvent_t> event_pool_;
+  std::vector<PendingTiming> pending_;
+  void tbegin(int cat);
+  void tend();
+  void tflush();  // call after the stream has been synchronised
+
+  int64_t n_ = 0;          // padded vector length
+  double t_ = 0.0;
+  DeviceBuffer<double> x_, r_, J_, stage_, const_, z_;
+  std::vector<DeviceBuffer<double>> us_;
+  // Krylov workspace
+  DeviceBuffer<double> kr_, krhat_, kp_, kv_, ks_, kt_, kphat_, kshat_, kx_, dinv_;
+  DeviceBuffer<float> fr_, frhat_, fp_, fv_, fs_, ft_, fphat_, fshat_, fx_, fdinv_, fb_;
+  DeviceBuffer<float> J32_;
+  DeviceBuffer<double> partial_, scal_;
+  DeviceBuffer<unsigned int> counter_;
+  DeviceBuffer<int> status_;
+  double* pinned_ = nullptr;
+  ReduceScratch rs_{};
+
+  // configuration
+  std::string scheme_;
+  double newton_rel_ = 1e-4, newton_abs_ = 0.0, lin_threshold_ = 0.0, dx_min_rel_ = 0.1;
+  bool dx_fixed_ = false;
+  int it_min_ = 0, it_max_ = 40;
+  std::string norm_ = "l_2";
+  double lin_rel_ = 1e-4;
+  bool lin_direct_ = true;
+  int lin_max_it_ = 500;
+  std::string precond_ = "Jacobi";
+  double dec_ = 0.5, inc_ = 1.1;
+  bool has_min_ = false, has_max_ = false;
+  double dt_min_ = 0.0, dt_max_ = 0.0;
+};
+
+}  // namespace dcgpu

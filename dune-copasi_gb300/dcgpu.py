@@ -1,0 +1,311 @@
+"""ctypes binding of libdcgpu (include/dcgpu.h), mirroring the reference's model / stepper API.
+
+The reference drives a simulation as (src/dune_copasi.cc:381-437):
+    model = DiffusionReaction::make_model<Model>(config, functor_factory)
+    state = model->make_state(grid, config); model->interpolate(state, model->make_initial(...))
+    step_operator = model->make_step_operator(state, config)
+    stepper.evolve(step_operator, state, state, dt, end_time, callback)
+``Model`` below bundles make_model + make_state + interpolate + make_step_operator (the
+state lives on the GPU), ``Model.step`` is SimpleAdaptiveStepper::do_step and
+``Model.evolve`` is TimeStepper::evolve.  Errors raise ``DcError`` with the library's
+message, as the reference raises format_exception(...).
+
+There is no CPU fallback: constructing a model without the compiled library or without
+a CUDA device raises.
+"""
+
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libdcgpu.so")
+
+DC_OK = 0
+STATUS_NAMES = {0: "DC_OK", 1: "DC_ERR_DIVERGED", 2: "DC_ERR_DT_MIN", 3: "DC_ERR_TIMEOUT",
+                4: "DC_ERR_CONFIG", 5: "DC_ERR_CUDA", 6: "DC_ERR_ARGUMENT", 7: "DC_ERR_INTERNAL"}
+
+EXPORTED = [
+    "dc_model_create", "dc_model_destroy", "dc_model_info_get", "dc_species_name",
+    "dc_species_size", "dc_species_vertices", "dc_state_set_initial", "dc_state_get",
+    "dc_state_set", "dc_state_get_species", "dc_state_time", "dc_step", "dc_evolve",
+    "dc_assemble", "dc_pattern", "dc_dof_map", "dc_stats", "dc_set_mixed_precision",
+    "dc_expr_eval", "dc_stream_handle", "dc_launch_count", "dc_profile_enable", "dc_profile_get",
+    "dc_last_error",
+]
+
+
+class DcError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__("%s: %s" % (STATUS_NAMES.get(status, status), message))
+        self.status = status
+
+
+class ModelInfo(ctypes.Structure):
+    _fields_ = [("dim", ctypes.c_int32), ("n_species", ctypes.c_int32),
+                ("n_compartments", ctypes.c_int32), ("block_size", ctypes.c_int32),
+                ("n_vertices", ctypes.c_int64), ("n_elements", ctypes.c_int64),
+                ("n_dof", ctypes.c_int64), ("n_block_rows", ctypes.c_int64),
+                ("n_blocks", ctypes.c_int64)]
+
+
+class StepInfo(ctypes.Structure):
+    _fields_ = [("time", ctypes.c_double), ("dt_used", ctypes.c_double),
+                ("newton_iterations", ctypes.c_int32), ("linear_iterations", ctypes.c_int32),
+                ("failed_attempts", ctypes.c_int32), ("status", ctypes.c_int32),
+                ("device_ms", ctypes.c_double)]
+
+
+CALLBACK = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p)
+
+_lib = None
+
+
+def load_library(path=LIB_PATH):
+    """Load libdcgpu.so and declare every exported entry point (raises if missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError("libdcgpu.so not built (run __graft_entry__.build()): %s" % path)
+    lib = ctypes.CDLL(path)
+    for name in EXPORTED:
+        if not hasattr(lib, name):
+            raise ImportError("libdcgpu.so lacks symbol %s" % name)
+    P = ctypes.POINTER
+    vp = ctypes.c_void_p
+    d = ctypes.c_double
+    i32 = ctypes.c_int32
+    sz = ctypes.c_size_t
+    pd = P(ctypes.c_double)
+    lib.dc_model_create.argtypes = [ctypes.c_char_p, ctypes.c_char_p, P(vp)]
+    lib.dc_model_destroy.argtypes = [vp]
+    lib.dc_model_info_get.argtypes = [vp, P(ModelInfo)]
+    lib.dc_species_name.argtypes = [vp, i32, ctypes.c_char_p, sz]
+    lib.dc_species_size.argtypes = [vp, i32, P(ctypes.c_int64)]
+    lib.dc_species_vertices.argtypes = [vp, i32, P(ctypes.c_int64), sz]
+    lib.dc_state_set_initial.argtypes = [vp]
+    lib.dc_state_get.argtypes = [vp, pd, sz]
+    lib.dc_state_set.argtypes = [vp, pd, sz, d]
+    lib.dc_state_get_species.argtypes = [vp, i32, pd, sz]
+    lib.dc_state_time.argtypes = [vp, pd]
+    lib.dc_step.argtypes = [vp, pd, P(StepInfo)]
+    lib.dc_evolve.argtypes = [vp, d, pd, CALLBACK, vp]
+    lib.dc_assemble.argtypes = [vp, pd, d, d, d, pd, pd, sz]
+    lib.dc_pattern.argtypes = [vp, P(ctypes.c_int32), sz, P(ctypes.c_int32), sz]
+    lib.dc_dof_map.argtypes = [vp, P(ctypes.c_int64), sz]
+    lib.dc_stats.argtypes = [vp, P(ctypes.c_int64), P(ctypes.c_int64), P(ctypes.c_int64), P(ctypes.c_int64)]
+    lib.dc_set_mixed_precision.argtypes = [vp, ctypes.c_int]
+    lib.dc_expr_eval.argtypes = [ctypes.c_char_p, ctypes.c_char_p, P(ctypes.c_char_p), pd, i32, pd]
+    lib.dc_stream_handle.argtypes = [vp, P(vp)]
+    lib.dc_launch_count.argtypes = []
+    lib.dc_profile_enable.argtypes = [vp, ctypes.c_int]
+    lib.dc_profile_get.argtypes = [vp, pd, P(ctypes.c_int64), i32]
+    lib.dc_last_error.argtypes = []
+    lib.dc_last_error.restype = ctypes.c_char_p
+    for name in EXPORTED:
+        if name not in ("dc_last_error", "dc_launch_count"):
+            getattr(lib, name).restype = ctypes.c_int
+    lib.dc_launch_count.restype = ctypes.c_int64
+    _lib = lib
+    return lib
+
+
+def _check(status):
+    if status != DC_OK:
+        msg = _lib.dc_last_error().decode(errors="replace")
+        raise DcError(status, msg)
+
+
+def expr_eval(expression, variables=None, context_ini=None):
+    """Evaluate one expression on the host with the engine's compiler (no GPU needed)."""
+    lib = load_library()
+    variables = variables or {}
+    names = list(variables)
+    arr_n = (ctypes.c_char_p * max(len(names), 1))(*[n.encode() for n in names])
+    vals = np.array([float(variables[n]) for n in names] or [0.0])
+    out = ctypes.c_double()
+    _check(lib.dc_expr_eval(expression.encode(), context_ini.encode() if context_ini else None, arr_n,
+                            vals.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), len(names),
+                            ctypes.byref(out)))
+    return out.value
+
+
+def _ptr(a, ctype=ctypes.c_double):
+    return a.ctypes.data_as(ctypes.POINTER(ctype))
+
+
+class Model:
+    """A DuneCopasi diffusion-reaction model resident on the GPU.
+
+    ``ini`` is the configuration text; ``overrides`` maps keys to values (the CLI's
+    ``--key=value``).
+    """
+
+    def __init__(self, ini, overrides=None):
+        lib = load_library()
+        self._lib = lib
+        ov = None
+        if overrides:
+            ov = "\n".join("%s=%s" % (k, v) for k, v in overrides.items()).encode()
+        h = ctypes.c_void_p()
+        _check(lib.dc_model_create(ini.encode(), ov, ctypes.byref(h)))
+        self._h = h
+        info = ModelInfo()
+        _check(lib.dc_model_info_get(h, ctypes.byref(info)))
+        self.info = {f: getattr(info, f) for f, _ in ModelInfo._fields_}
+        self.species = []
+        buf = ctypes.create_string_buffer(256)
+        for s in range(info.n_species):
+            _check(lib.dc_species_name(h, s, buf, 256))
+            self.species.append(buf.value.decode())
+
+    # -- lifetime
+    def close(self):
+        if getattr(self, "_h", None):
+            _check(self._lib.dc_model_destroy(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- state
+    @property
+    def ndof(self):
+        return self.info["n_dof"]
+
+    def state(self):
+        out = np.empty(self.ndof)
+        _check(self._lib.dc_state_get(self._h, _ptr(out), out.size))
+        return out
+
+    def set_state(self, x, time):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        _check(self._lib.dc_state_set(self._h, _ptr(x), x.size, float(time)))
+
+    def set_initial(self):
+        _check(self._lib.dc_state_set_initial(self._h))
+
+    def time(self):
+        t = ctypes.c_double()
+        _check(self._lib.dc_state_time(self._h, ctypes.byref(t)))
+        return t.value
+
+    def species_index(self, name):
+        return self.species.index(name)
+
+    def species_vertices(self, name):
+        s = self.species_index(name)
+        n = ctypes.c_int64()
+        _check(self._lib.dc_species_size(self._h, s, ctypes.byref(n)))
+        out = np.empty(n.value, np.int64)
+        _check(self._lib.dc_species_vertices(self._h, s, _ptr(out, ctypes.c_int64), out.size))
+        return out
+
+    def species_values(self, name):
+        s = self.species_index(name)
+        n = ctypes.c_int64()
+        _check(self._lib.dc_species_size(self._h, s, ctypes.byref(n)))
+        out = np.empty(n.value)
+        _check(self._lib.dc_state_get_species(self._h, s, _ptr(out), out.size))
+        return out
+
+    # -- stepping (SimpleAdaptiveStepper / TimeStepper)
+    def step(self, dt):
+        """One adaptive step; returns a dict with the step statistics and the next dt."""
+        d = ctypes.c_double(dt)
+        info = StepInfo()
+        st = self._lib.dc_step(self._h, ctypes.byref(d), ctypes.byref(info))
+        _check(st)
+        out = {f: getattr(info, f) for f, _ in StepInfo._fields_}
+        out["dt_next"] = d.value
+        return out
+
+    def evolve(self, t_end, dt, callback=None):
+        d = ctypes.c_double(dt)
+
+        def _cb(_m, t, _u):
+            if callback is not None:
+                callback(t)
+
+        cb = CALLBACK(_cb)
+        _check(self._lib.dc_evolve(self._h, float(t_end), ctypes.byref(d), cb, None))
+        return d.value
+
+    # -- operator access
+    def assemble(self, x, t, cm, ca, residual=True, jacobian=True):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        r = np.empty(self.ndof) if residual else None
+        bs = self.info["block_size"]
+        nj = self.info["n_blocks"] * bs * bs
+        J = np.empty(nj) if jacobian else None
+        _check(self._lib.dc_assemble(self._h, _ptr(x), float(t), float(cm), float(ca),
+                                     _ptr(r) if r is not None else None,
+                                     _ptr(J) if J is not None else None, nj if J is not None else 0))
+        return r, J
+
+    def pattern(self):
+        nr = self.info["n_block_rows"]
+        rowptr = np.empty(nr + 1, np.int32)
+        colidx = np.empty(self.info["n_blocks"], np.int32)
+        _check(self._lib.dc_pattern(self._h, _ptr(rowptr, ctypes.c_int32), rowptr.size,
+                                    _ptr(colidx, ctypes.c_int32), colidx.size))
+        return rowptr, colidx
+
+    def dof_map(self):
+        out = np.empty(self.ndof, np.int64)
+        _check(self._lib.dc_dof_map(self._h, _ptr(out, ctypes.c_int64), out.size))
+        return out
+
+    def jacobian_csr(self, J):
+        """Expand BSR values into a scipy CSR matrix in the reference DOF order."""
+        import scipy.sparse as sp
+        rowptr, colidx = self.pattern()
+        bs = self.info["block_size"]
+        nr = self.info["n_block_rows"]
+        blocks = J.reshape(-1, bs, bs)
+        brow = np.repeat(np.arange(nr), np.diff(rowptr))
+        rows = (brow[:, None, None] * bs + np.arange(bs)[None, :, None]).repeat(bs, axis=2)
+        cols = (colidx[:, None, None] * bs + np.arange(bs)[None, None, :]).repeat(bs, axis=1)
+        A = sp.csr_matrix((blocks.ravel(), (rows.ravel(), cols.ravel())), shape=(nr * bs, nr * bs))
+        m = self.dof_map()
+        return A[m][:, m]
+
+    def stats(self):
+        v = [ctypes.c_int64() for _ in range(4)]
+        _check(self._lib.dc_stats(self._h, *[ctypes.byref(x) for x in v]))
+        return dict(zip(("newton_iterations", "linear_iterations", "assemblies", "failed_steps"),
+                        [x.value for x in v]))
+
+    def set_mixed_precision(self, enabled):
+        _check(self._lib.dc_set_mixed_precision(self._h, 1 if enabled else 0))
+
+    # -- instrumentation
+    def stream_handle(self):
+        s = ctypes.c_void_p()
+        _check(self._lib.dc_stream_handle(self._h, ctypes.byref(s)))
+        return s.value or 0
+
+    def profile(self, enabled=True):
+        _check(self._lib.dc_profile_enable(self._h, 1 if enabled else 0))
+
+    def kernel_times(self):
+        """{category: (total ms, launches)} for assembly, spmv, precond."""
+        ms = np.zeros(3)
+        calls = np.zeros(3, np.int64)
+        _check(self._lib.dc_profile_get(self._h, _ptr(ms), _ptr(calls, ctypes.c_int64), 3))
+        return {k: (float(ms[i]), int(calls[i])) for i, k in enumerate(("assembly", "spmv", "precond"))}
+
+
+def launch_count():
+    return int(load_library().dc_launch_count())

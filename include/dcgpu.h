@@ -1,0 +1,132 @@
+/* dcgpu: GB300-native implicit-step engine for DuneCopasi diffusion-reaction models.
+ *
+ * C ABI of the drop-in boundary.  Every entry point returns an int status (DC_OK = 0);
+ * no C++ exception crosses this boundary.  dc_last_error() gives the message of the
+ * last failure on the calling thread.  One host thread per model handle.
+ *
+ * Each entry point names the reference interface it replaces (paths inside the
+ * dune-copasi source tree).
+ */
+#ifndef DCGPU_H
+#define DCGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  DC_OK = 0,
+  DC_ERR_DIVERGED = 1, /* Newton or linear solve did not converge (PDELab::ErrorCondition) */
+  DC_ERR_DT_MIN = 2,   /* time step reached time_step_min (stepper.hh:371-382) */
+  DC_ERR_TIMEOUT = 3,  /* iteration cap reached */
+  DC_ERR_CONFIG = 4,   /* configuration error (format_exception(IOError...)) */
+  DC_ERR_CUDA = 5,
+  DC_ERR_ARGUMENT = 6,
+  DC_ERR_INTERNAL = 7
+};
+
+typedef struct dc_model dc_model;
+
+typedef struct dc_model_info {
+  int32_t dim;          /* grid dimension */
+  int32_t n_species;    /* scalar fields over all compartments */
+  int32_t n_compartments;
+  int32_t block_size;   /* species per block row on the device */
+  int64_t n_vertices;
+  int64_t n_elements;
+  int64_t n_dof;        /* reference DOF count */
+  int64_t n_block_rows;
+  int64_t n_blocks;     /* stored BSR blocks */
+} dc_model_info;
+
+typedef struct dc_step_info {
+  double time;          /* time after the step */
+  double dt_used;       /* step size that succeeded */
+  int32_t newton_iterations;  /* Newton iterations in this step, all stages */
+  int32_t linear_iterations;  /* Krylov iterations in this step */
+  int32_t failed_attempts;    /* attempts rejected before success */
+  int32_t status;
+  double device_ms;           /* CUDA-event time of the step on the model's stream */
+} dc_step_info;
+
+typedef void (*dc_callback)(const dc_model* model, double time, void* user);
+
+/* Replaces DiffusionReaction::make_model + Model::make_state + make_step_operator
+ * (dune/copasi/model/diffusion_reaction/factory.hh:46-136, model/model.hh:24-101,
+ * model_single_compartment.impl.hh:195-232).  `ini_text` is the configuration file
+ * content; `overrides` holds "key=value" lines (the CLI's --key=value, src/dune_copasi.cc:
+ * 270-288) or is NULL.  The state is initialised from the initial conditions. */
+int dc_model_create(const char* ini_text, const char* overrides, dc_model** out);
+int dc_model_destroy(dc_model* model);
+int dc_model_info_get(const dc_model* model, dc_model_info* info);
+
+/* species metadata (names in configuration order, compartment-major) */
+int dc_species_name(const dc_model* model, int32_t species, char* buf, size_t len);
+int dc_species_size(const dc_model* model, int32_t species, int64_t* n_vertices);
+int dc_species_vertices(const dc_model* model, int32_t species, int64_t* vertex_ids, size_t n);
+
+/* Replaces make_initial + interpolate (dune/copasi/model/make_initial.hh:24-90,
+ * interpolate.hh:21-78): nodal interpolation of initial.expression at time_begin. */
+int dc_state_set_initial(dc_model* model);
+/* full coefficient vector in the reference DOF order (State::coefficients,
+ * model/model.hh:36-42): compartment-major, vertex-major, species interleaved */
+int dc_state_get(const dc_model* model, double* host_out, size_t n);
+int dc_state_set(dc_model* model, const double* host_in, size_t n, double time);
+int dc_state_get_species(const dc_model* model, int32_t species, double* host_out, size_t n);
+int dc_state_time(const dc_model* model, double* time);
+
+/* Replaces SimpleAdaptiveStepper::do_step (dune/copasi/common/stepper.hh:337-368):
+ * one step with dt, halving on failure down to time_step_min; on success *dt becomes
+ * the suggested next step (x increase factor, clamped to time_step_max). */
+int dc_step(dc_model* model, double* dt, dc_step_info* info);
+/* Replaces TimeStepper::evolve + snap_to_time (stepper.hh:144-239): steps until t_end,
+ * calling `cb` after every successful step. */
+int dc_evolve(dc_model* model, double t_end, double* dt, dc_callback cb, void* user);
+
+/* Operator entry points (the local-operator boundary, local_operator.hh:417-707 and
+ * :777-1203, as driven by PDELab's instationary assembler): at state x (reference
+ * order) and time t, r = cm * M(x) + ca * A(x) and the BSR values of
+ * cm * dM/dx + ca * dA/dx.  r and jac_values may be NULL. */
+int dc_assemble(dc_model* model, const double* x, double t, double cm, double ca, double* r, double* jac_values,
+                size_t n_jac_values);
+/* BSR pattern of the Jacobian (block rows = (compartment, vertex) pairs) */
+int dc_pattern(const dc_model* model, int32_t* rowptr, size_t n_rowptr, int32_t* colidx, size_t n_colidx);
+/* map from reference DOF index to padded device index (node * block_size + species) */
+int dc_dof_map(const dc_model* model, int64_t* ref_to_dev, size_t n);
+
+/* solver statistics accumulated since creation */
+int dc_stats(const dc_model* model, int64_t* newton_iterations, int64_t* linear_iterations, int64_t* assemblies,
+             int64_t* failed_steps);
+
+/* set the linear-solve precision: 0 = fp64 BiCGSTAB, 1 = fp32 BiCGSTAB inside fp64 iterative refinement */
+int dc_set_mixed_precision(dc_model* model, int enabled);
+
+/* Replaces the parser interface (dune/copasi/parser/parser.hh:15-62: define_variable,
+ * set_expression, compile, operator()) for host-side checks: compiles `expression` with
+ * the parser_context section of `context_ini` (may be NULL) and the n variables
+ * names[i] = values[i], evaluates it on the host and writes the value to *out.  No GPU
+ * is needed. */
+int dc_expr_eval(const char* expression, const char* context_ini, const char* const* names, const double* values,
+                 int32_t n, double* out);
+
+/* Instrumentation (no reference counterpart; replaces the reference's perfetto trace
+ * counters of LinearSolver / TimeStep, model/make_step_operator.hh:104-139):
+ * the CUDA stream the model launches on (cudaStream_t as void*), the number of kernels
+ * this library has launched, and per-category device times measured with CUDA events
+ * (0 = assembly, 1 = SpMV, 2 = preconditioner apply) while profiling is enabled. */
+int dc_stream_handle(const dc_model* model, void** stream);
+int64_t dc_launch_count(void);
+int dc_profile_enable(dc_model* model, int enabled);
+int dc_profile_get(const dc_model* model, double* ms, int64_t* calls, int32_t n_categories);
+
+/* message of the last failure on this thread ("" if none) */
+const char* dc_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DCGPU_H */

@@ -1,0 +1,139 @@
+"""Small model configurations shared by the parity tests (seeded, CPU-oracle sized)."""
+
+import numpy as np
+
+import workloads as W
+
+
+def small_heat(n=24, steps=6):
+    return W.heat(n=n, steps=steps, dt=0.01)
+
+
+def small_gray_scott(n=24, steps=4):
+    return W.gray_scott(n=n, steps=steps, dt=1.0)
+
+
+def small_two_compartment(n=24, steps=4):
+    return W.two_compartment(n=n, steps=steps, dt=0.05)
+
+
+def small_3d(n=5, steps=3):
+    return W.cross_diffusion_3d(n=n, steps=steps, dt=0.01)
+
+
+FEATURES_INI = """
+[grid]
+dimension = 2
+cells = 10 8
+extensions = 1.5 1
+origin = -0.25 0
+
+[compartments.domain]
+expression = 1
+
+[parser_context.rate]
+type = constant
+value = 0.7
+
+[parser_context.pulse]
+type = function
+expression = t, x: exp(-t) * (1 + 0.5*sin(3*x))
+
+[parser_context.profile]
+type = interpolation
+domain = -1 0 1 2
+range = 0.5 1 2 1
+
+[model.scalar_field.u]
+compartment = domain
+initial.expression = 0.5 + 0.25*cos(2*position_x)*sin(3*position_y)
+storage.expression = 1 + 0.1*u
+storage.jacobian.u.expression = 0.1
+reaction.expression = -rate*u*w + pulse(time, position_x)
+reaction.jacobian.u.expression = -rate*w
+reaction.jacobian.w.expression = -rate*u
+velocity.x.expression = 0.3*profile(position_y)
+velocity.y.expression = -0.2
+cross_diffusion.u.type = tensor
+cross_diffusion.u.xx.expression = 0.02*(1 + u^2)
+cross_diffusion.u.xy.expression = 0.005
+cross_diffusion.u.yx.expression = 0.002
+cross_diffusion.u.yy.expression = 0.01
+cross_diffusion.u.jacobian.u.type = tensor
+cross_diffusion.u.jacobian.u.xx.expression = 0.04*u
+cross_diffusion.w.expression = 0.003
+outflow.domain.expression = 0.2*u*(position_x > 0.5 ? 1 : 0.5) + 0.1*normal_x
+outflow.domain.jacobian.u.expression = 0.2*(position_x > 0.5 ? 1 : 0.5)
+
+[model.scalar_field.w]
+compartment = domain
+initial.expression = 0.3 + 0.1*position_x*position_y
+storage.expression = 1
+reaction.expression = rate*u*w - 0.1*w + entity_volume*0
+reaction.jacobian.u.expression = rate*w
+reaction.jacobian.w.expression = rate*u - 0.1
+cross_diffusion.w.expression = 0.01 + 0.002*(time > 0.05)
+velocity.x.expression = 0.1*w
+velocity.jacobian.w.x.expression = 0.1
+
+[model.time_step_operator]
+type = Alexander2
+time_begin = 0
+time_end = 0.1
+time_step_initial = 0.02
+time_step_max = 0.02
+
+[model.time_step_operator.nonlinear_solver]
+convergence_condition.relative_tolerance = 1e-16
+"""
+
+FEATURES_3D_INI = """
+[grid]
+dimension = 3
+cells = 3 4 3
+
+[compartments]
+lower.expression = position_z < 0.5
+upper.expression = position_z >= 0.5
+
+[model.scalar_field.p]
+compartment = lower
+initial.expression = 1 + position_x
+storage.expression = 1
+cross_diffusion.p.expression = 0.05
+reaction.expression = -0.3*p^2
+reaction.jacobian.p.expression = -0.6*p
+outflow.upper.expression = 0.4*(p - q) + 0.05*normal_z
+outflow.upper.jacobian.p.expression = 0.4
+outflow.upper.jacobian.q.expression = -0.4
+
+[model.scalar_field.q]
+compartment = upper
+initial.expression = 0.2*position_y
+storage.expression = 1
+cross_diffusion.q.type = tensor
+cross_diffusion.q.xx.expression = 0.02
+cross_diffusion.q.yy.expression = 0.03
+cross_diffusion.q.zz.expression = 0.04
+cross_diffusion.q.xz.expression = 0.005
+outflow.lower.expression = 0.4*(q - p)
+outflow.lower.jacobian.q.expression = 0.4
+outflow.lower.jacobian.p.expression = -0.4
+
+[model.scalar_field.r]
+compartment = upper
+initial.expression = 0.5
+storage.expression = 1
+reaction.expression = 0.1*q - 0.2*r
+reaction.jacobian.q.expression = 0.1
+reaction.jacobian.r.expression = -0.2
+cross_diffusion.r.expression = 0.01
+
+[model.time_step_operator]
+type = ImplicitEuler
+time_end = 0.3
+time_step_max = 0.1
+
+[model.time_step_operator.nonlinear_solver]
+convergence_condition.relative_tolerance = 1e-16
+"""

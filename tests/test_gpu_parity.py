@@ -1,0 +1,265 @@
+"""GPU parity tests: the CUDA engine (through the C ABI) against the CPU oracle.
+
+Tolerances: assembly (residual and Jacobian) relative 1e-12 of the operator's scale;
+time stepping: per-species relative L2 <= 1e-8 after every step, Newton iteration
+counts equal to within +-1 per stage.
+"""
+
+import numpy as np
+import pytest
+
+import cases
+from oracle.model import OracleModel
+
+pytestmark = pytest.mark.gpu
+
+STEP_TOL = 1e-8
+ASM_TOL = 1e-12
+
+
+def _init_state(om, init):
+    x = om.initial_state()
+    if init is not None:
+        for sp in om.species:
+            verts = om.comp_vertices[sp.comp]
+            x[om.dof(sp, verts)] = init(sp.name, om.mesh.coords[verts])
+    return x
+
+
+def _rel(a, b):
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
+
+
+def _species_errors(om, gm, xo, xg):
+    out = {}
+    for sp in om.species:
+        out[sp.name] = _rel(gm_species(gm, om, xg, sp), xo[om.dof(sp, om.comp_vertices[sp.comp])])
+    return out
+
+
+def gm_species(gm, om, xg, sp):
+    return xg[om.dof(sp, om.comp_vertices[sp.comp])]
+
+
+ALL_CASES = {
+    "heat": cases.small_heat,
+    "gray_scott": cases.small_gray_scott,
+    "two_compartment": cases.small_two_compartment,
+    "cross_diffusion_3d": cases.small_3d,
+    "features_2d": lambda: (cases.FEATURES_INI, None),
+    "features_3d_padded": lambda: (cases.FEATURES_3D_INI, None),
+}
+
+
+@pytest.mark.parametrize("case", sorted(ALL_CASES))
+def test_layout_matches_oracle(dcgpu_lib, case):
+    ini, _ = ALL_CASES[case]()
+    om = OracleModel(ini)
+    gm = dcgpu_lib.Model(ini)
+    assert gm.ndof == om.ndof
+    assert gm.species == [s.name for s in om.species]
+    for sp in om.species:
+        assert np.array_equal(gm.species_vertices(sp.name), om.comp_vertices[sp.comp])
+    np.testing.assert_allclose(gm.state(), om.initial_state(), rtol=1e-14, atol=1e-14)
+    gm.close()
+
+
+@pytest.mark.parametrize("case", sorted(ALL_CASES))
+@pytest.mark.parametrize("form", ["mass", "stiffness"])
+def test_assembly_matches_oracle(dcgpu_lib, case, form):
+    ini, init = ALL_CASES[case]()
+    om = OracleModel(ini)
+    rng = np.random.default_rng(11)
+    x = _init_state(om, init) + 0.05 * rng.uniform(-1, 1, om.ndof)
+    t = 0.0375
+    gm = dcgpu_lib.Model(ini)
+    cm, ca = (1.0, 0.0) if form == "mass" else (0.0, 1.0)
+    r, J = gm.assemble(x, t, cm, ca)
+    r_ref = om.residual(x, t, form)
+    scale = max(np.abs(r_ref).max(), 1e-300)
+    assert np.abs(r - r_ref).max() <= ASM_TOL * scale + 1e-300, case
+    Jg = gm.jacobian_csr(J)
+    Jo = om.jacobian(x, t, form)
+    D = (Jg - Jo).tocoo()
+    jscale = max(abs(Jo).max(), 1e-300)
+    assert (np.abs(D.data).max() if D.nnz else 0.0) <= ASM_TOL * jscale, case
+    # combined stage operator: cm M + ca A in one pass
+    r2, J2 = gm.assemble(x, t, 0.7, -1.3)
+    r2_ref = 0.7 * om.residual(x, t, "mass") - 1.3 * om.residual(x, t, "stiffness")
+    assert np.abs(r2 - r2_ref).max() <= 1e-11 * max(np.abs(r2_ref).max(), 1e-300)
+    gm.close()
+
+
+def _run_both(dcgpu_lib, ini, init, mixed=False, overrides=None):
+    om = OracleModel(ini, overrides)
+    gm = dcgpu_lib.Model(ini, overrides)
+    if mixed:
+        gm.set_mixed_precision(True)
+    x = _init_state(om, init)
+    _dec, _inc, t0, t1, _mn, _mx, dt0 = om.stepper_params()
+    gm.set_state(x, t0)
+    dt_o = dt0
+    dt_g = dt0
+    t = t0
+    records = []
+    while t < t1 - 1e-12:
+        st = {}
+        x, t_new, dt_o, used_o = om.do_step(x, t, dt_o, st)
+        info = gm.step(dt_g)
+        dt_g = info["dt_next"]
+        assert info["time"] == pytest.approx(t_new, rel=0, abs=1e-14)
+        assert info["dt_used"] == pytest.approx(used_o, rel=0, abs=1e-15)
+        xg = gm.state()
+        errs = {sp.name: _rel(xg[om.dof(sp, om.comp_vertices[sp.comp])],
+                              x[om.dof(sp, om.comp_vertices[sp.comp])]) for sp in om.species}
+        records.append((t_new, errs, st.get("newton_iterations", 0), info["newton_iterations"],
+                        len(st.get("newton_per_stage", []))))
+        t = t_new
+    gm.close()
+    return records
+
+
+@pytest.mark.parametrize("case", sorted(ALL_CASES))
+def test_time_stepping_matches_oracle(dcgpu_lib, case):
+    ini, init = ALL_CASES[case]()
+    records = _run_both(dcgpu_lib, ini, init)
+    assert records
+    for t, errs, n_o, n_g, stages in records:
+        for name, e in errs.items():
+            assert e <= STEP_TOL, (case, t, name, e)
+        assert abs(n_o - n_g) <= max(1, stages), (case, t, n_o, n_g)
+
+
+@pytest.mark.parametrize("case", ["gray_scott", "two_compartment", "cross_diffusion_3d", "features_3d_padded"])
+def test_mixed_precision_matches_oracle(dcgpu_lib, case):
+    """fp32 BiCGSTAB inside fp64 iterative refinement: same tolerance against the fp64 oracle."""
+    ini, init = ALL_CASES[case]()
+    records = _run_both(dcgpu_lib, ini, init, mixed=True)
+    for t, errs, n_o, n_g, stages in records:
+        for name, e in errs.items():
+            assert e <= STEP_TOL, (case, t, name, e)
+        assert abs(n_o - n_g) <= max(1, stages)
+
+
+def test_linear_model_defect_correction(dcgpu_lib):
+    """is_linear = true: one defect-correction solve per stage (make_step_operator.hh:210-245)."""
+    import test_oracle as T
+    ini = T.GAUSS_INI.replace("refinement_level = 5", "refinement_level = 3")
+    records = _run_both(dcgpu_lib, ini, None)
+    assert records
+    for t, errs, *_ in records:
+        assert errs["u"] <= STEP_TOL
+
+
+def test_iterative_solver_configuration(dcgpu_lib):
+    """linear_solver.type = BiCGSTAB with the adaptive Newton linear tolerance still converges
+    to the oracle's solution within the Newton tolerance."""
+    ini, init = cases.small_gray_scott()
+    ov = {"model.time_step_operator.linear_solver.type": "BiCGSTAB",
+          "model.time_step_operator.nonlinear_solver.convergence_condition.relative_tolerance": "1e-24"}
+    records = _run_both(dcgpu_lib, ini, init, overrides=ov)
+    for t, errs, n_o, n_g, stages in records:
+        for e in errs.values():
+            assert e <= STEP_TOL
+
+
+def test_deterministic_bitwise(dcgpu_lib):
+    ini, init = cases.small_two_compartment(steps=2)
+    om = OracleModel(ini)
+    x0 = _init_state(om, init)
+    outs = []
+    for _ in range(2):
+        gm = dcgpu_lib.Model(ini)
+        gm.set_state(x0, 0.0)
+        dt = 0.05
+        for _s in range(2):
+            dt = gm.step(dt)["dt_next"]
+        outs.append(gm.state())
+        gm.close()
+    assert np.array_equal(outs[0], outs[1])
+
+
+def test_evolve_matches_oracle_times(dcgpu_lib):
+    ini, _ = cases.small_heat(n=12, steps=5)
+    ini = ini.replace("time_end = 0.05", "time_end = 0.047")
+    om = OracleModel(ini)
+    times_o = []
+    om.run(callback=lambda x, t: times_o.append(t))
+    gm = dcgpu_lib.Model(ini)
+    times_g = []
+    gm.evolve(0.047, 0.01, callback=lambda t: times_g.append(t))
+    assert len(times_g) == len(times_o)
+    np.testing.assert_allclose(times_g, times_o, rtol=0, atol=1e-15)
+    gm.close()
+
+
+def test_step_failure_halves_dt_and_reports_dt_min(dcgpu_lib):
+    """A stage whose expressions go non-finite fails; the stepper halves dt down to
+    time_step_min and reports DC_ERR_DT_MIN, leaving the state untouched (stepper.hh:337-382)."""
+    ini = """
+[grid]
+cells = 4 4
+[compartments.domain]
+expression = 1
+[model.scalar_field.u]
+compartment = domain
+initial.expression = 1
+storage.expression = 1
+reaction.expression = log(u - 2)
+reaction.jacobian.u.expression = 1/(u - 2)
+cross_diffusion.u.expression = 0.1
+[model.time_step_operator]
+type = ImplicitEuler
+time_end = 1
+time_step_initial = 0.1
+time_step_min = 0.02
+time_step_max = 0.1
+"""
+    gm = dcgpu_lib.Model(ini)
+    before = gm.state()
+    with pytest.raises(dcgpu_lib.DcError) as ei:
+        gm.step(0.1)
+    assert ei.value.status == 2
+    assert np.array_equal(gm.state(), before)
+    assert gm.time() == 0.0
+    assert gm.stats()["failed_steps"] >= 3
+    gm.close()
+
+
+def test_config_errors_are_reported(dcgpu_lib):
+    with pytest.raises(dcgpu_lib.DcError) as ei:
+        dcgpu_lib.Model("[grid]\ncells = 2 2\n[compartments.d]\nexpression = 1\n"
+                        "[model.scalar_field.u]\ncompartment = d\nreaction.expression = u +\n")
+    assert ei.value.status == 4
+    with pytest.raises(dcgpu_lib.DcError) as ei:
+        dcgpu_lib.Model("[grid]\ncells = 2 2\n[compartments.d]\nexpression = 1\n")
+    assert ei.value.status == 4
+
+
+def test_single_cell_and_empty_compartment(dcgpu_lib):
+    """Edge cases: a one-cell grid, and a compartment that contains no cell."""
+    ini = """
+[grid]
+cells = 1 1
+[compartments]
+a.expression = 1
+b.expression = 0
+[model.scalar_field.u]
+compartment = a
+initial.expression = position_x + 2*position_y
+storage.expression = 1
+cross_diffusion.u.expression = 1
+reaction.expression = -u
+reaction.jacobian.u.expression = -1
+[model.scalar_field.v]
+compartment = b
+initial.expression = 1
+[model.time_step_operator]
+type = ImplicitEuler
+time_end = 0.2
+time_step_max = 0.1
+"""
+    records = _run_both(dcgpu_lib, ini, None)
+    for t, errs, *_ in records:
+        assert errs["u"] <= STEP_TOL

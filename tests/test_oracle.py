@@ -1,0 +1,312 @@
+"""CPU tests of the oracle against the reference's own known answers.
+
+The reference's system tests pin this path only through analytic-error thresholds
+(test/exp.ini, test/gauss.ini); their configuration text is restated below (it is data,
+not code).  Closed-form P1 identities on the Kuhn grid pin the assembly.
+"""
+
+import math
+
+import numpy as np
+import pytest
+
+from oracle import expr as E
+from oracle.ini import ParameterTree
+from oracle.mesh import Mesh, structured_simplex
+from oracle.model import OracleModel, f_le, rk_scheme
+
+EXP_INI = """
+[grid]
+dimension = 2
+refinement_level = 1
+
+[compartments.domain]
+type = expression
+expression = 1
+
+[parser_context.grow_rate]
+type = constant
+value = -2.
+
+[model.scalar_field.u]
+compartment = domain
+initial.expression = 1
+storage.expression = 1
+reaction.expression = grow_rate*u
+reaction.jacobian.u.expression = grow_rate
+
+[model.time_step_operator]
+time_step_max = 0.1
+time_end = 10
+"""
+
+GAUSS_INI = """
+[grid]
+extensions = 2 2
+origin = -1 -1
+refinement_level = 5
+
+[compartments.domain]
+type = expression
+expression = 1
+
+[parser_context.diffusion]
+type = constant
+value = 0.005
+
+[parser_context.gauss]
+type = function
+expression = x, y, z, t: exp(-(x^2+y^2+z^2)/(4*t*diffusion)) / (4*3.14159265359*t*diffusion)
+
+[model]
+is_linear = true
+
+[model.scalar_field.u]
+compartment = domain
+
+[model.scalar_field.u.cross_diffusion.u]
+expression = diffusion
+
+[model.scalar_field.u.initial]
+expression = gauss(position_x, position_y, position_z, time)
+
+[model.scalar_field.u.storage]
+expression = 1
+
+[model.time_step_operator]
+time_begin = 1
+time_end = 1.2
+"""
+
+
+def _l2_error(m, x, t, exact):
+    env, _g, _c = m._volume_env(np.arange(m.mesh.ne), m.species, x, t)
+    xq = m.xq
+    ex = exact(xq[..., 0], xq[..., 1], t)
+    return math.sqrt(float(((env["u"] - ex) ** 2 * m.factor).sum()))
+
+
+def test_exp_ini_known_answer():
+    """test/exp.ini: ||u - exp(-2t)||_L2 <= 5e-3 at every step (test/exp.ini:32-35)."""
+    m = OracleModel(EXP_INI)
+    errs = []
+    m.run(callback=lambda x, t: errs.append(_l2_error(m, x, t, lambda X, Y, T: np.exp(-2.0 * T) + 0 * X)))
+    assert len(errs) >= 100
+    assert max(errs) <= 5e-3
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_exp_ini_dimensions(dim):
+    """exp-{dim}D runs of test/CMakeLists.txt:111-116 (grid.dimension override)."""
+    ini = EXP_INI.replace("time_end = 10", "time_end = 1")
+    m = OracleModel(ini, {"grid.dimension": dim})
+    x, t, _ = m.run()
+    assert abs(t - 1.0) < 1e-12
+    assert np.all(np.abs(x - math.exp(-2.0)) < 5e-3)
+
+
+def test_gauss_ini_known_answer():
+    """test/gauss.ini: L2 error <= 0.5, max <= 1/(4 pi D), min >= -1e-2 (gauss.ini:38-55)."""
+    m = OracleModel(GAUSS_INI)
+    D = 0.005
+
+    def gauss(X, Y, T):
+        return np.exp(-(X ** 2 + Y ** 2) / (4 * T * D)) / (4 * 3.14159265359 * T * D)
+
+    rec = []
+    m.run(callback=lambda x, t: rec.append((_l2_error(m, x, t, gauss), x.max(), x.min())))
+    assert rec
+    for err, mx, mn in rec:
+        assert err <= 0.5
+        assert mx <= 1.0 / (4 * 3.14159265359 * D)
+        assert mn >= -1e-2
+
+
+def test_p1_stiffness_is_five_point_stencil():
+    """On the Kuhn triangulation the P1 Laplacian is the 5-point stencil (h-independent in 2D)."""
+    n = 6
+    ini = """
+[grid]
+cells = {n} {n}
+[compartments.domain]
+expression = 1
+[model.scalar_field.u]
+compartment = domain
+cross_diffusion.u.expression = 1
+""".format(n=n)
+    m = OracleModel(ini)
+    K = m.jacobian(np.zeros(m.ndof), 0.0, "stiffness").toarray()
+    # interior vertex (i, j) = (3, 3)
+    v = 3 + 3 * (n + 1)
+    row = K[v]
+    assert row[v] == pytest.approx(4.0)
+    for nb in (v - 1, v + 1, v - (n + 1), v + (n + 1)):
+        assert row[nb] == pytest.approx(-1.0)
+    assert abs(row.sum()) < 1e-12
+    assert np.count_nonzero(np.abs(row) > 1e-14) == 5
+    assert np.allclose(K, K.T)
+
+
+def test_p1_mass_matrix_known_answer():
+    """Consistent P1 mass matrix: total mass = area, diagonal at an interior vertex = h^2/2."""
+    n = 8
+    ini = """
+[grid]
+cells = {n} {n}
+[compartments.domain]
+expression = 1
+[model.scalar_field.u]
+compartment = domain
+storage.expression = 1
+""".format(n=n)
+    m = OracleModel(ini)
+    M = m.jacobian(np.zeros(m.ndof), 0.0, "mass").toarray()
+    assert M.sum() == pytest.approx(1.0)
+    h = 1.0 / n
+    v = 4 + 4 * (n + 1)
+    # six triangles of area h^2/2 around an interior vertex, each contributing area/6
+    assert M[v, v] == pytest.approx(6 * (h * h / 2) / 6.0)
+    r = m.residual(np.ones(m.ndof), 0.0, "mass")
+    assert r.sum() == pytest.approx(1.0)
+
+
+def test_kuhn_grid_3d_volume_and_orientation():
+    coords, cells = structured_simplex(3, [2, 3, 4], [0, 0, 0], [1, 2, 3])
+    mesh = Mesh(coords, cells)
+    assert mesh.ne == 2 * 3 * 4 * 6
+    assert mesh.volumes().sum() == pytest.approx(6.0)
+    # each cube splits into 6 tets sharing the main diagonal
+    assert np.all(mesh.volumes() > 0)
+
+
+def test_refinement_level_doubles_cells():
+    cfg = ParameterTree.from_text("[grid]\ncells = 3 2\nrefinement_level = 2\n")
+    m = Mesh.from_config(cfg.sub("grid"))
+    assert m.ne == 2 * (3 * 4) * (2 * 4)
+
+
+@pytest.mark.parametrize("text,val", [
+    ("2^3^2", 512.0), ("-2^2", -4.0), ("2*-3", -6.0), ("1+2*3", 7.0), ("(1+2)*3", 9.0),
+    ("1 < 2", 1.0), ("2 <= 1", 0.0), ("1 == 1", 1.0), ("1 = 1", 1.0), ("1 != 1", 0.0),
+    ("1 && 0", 0.0), ("1 || 0", 1.0), ("1 and 1", 1.0), ("0 or 0", 0.0), ("!0", 1.0),
+    ("1 ? 2 : 3", 2.0), ("0 ? 2 : 0 ? 4 : 5", 5.0), ("min(3, 1, 2)", 1.0), ("max(3, 1, 2)", 3.0),
+    ("sum(1,2,3)", 6.0), ("avg(1,2,3)", 2.0), ("log(_e)", 1.0), ("ln(1)", 0.0), ("log10(100)", 2.0),
+    ("log2(8)", 3.0), ("sqrt(16)", 4.0), ("abs(-3)", 3.0), ("sign(-2)", -1.0), ("rint(2.5)", 2.0),
+    ("pow(2, 10)", 1024.0), ("atan2(0, -1)", math.pi), ("7 % 3", 1.0), ("1e-2*100", 1.0),
+    (".5 + .5", 1.0), ("floor(-1.5)", -2.0), ("ceil(1.2)", 2.0), ("round(2.5)", 3.0),
+])
+def test_expression_semantics(text, val):
+    assert float(E.evaluate(E.parse(text), {})) == pytest.approx(val)
+
+
+def test_zero_expression_elision():
+    """functor_factory_parser.impl.hh:121-124: empty / all-zero expressions are no functor."""
+    for t in ("", "0", "0.0", "-0", "000", ".0"):
+        assert E.is_zero_literal(t)
+    for t in ("1", "0.1", "u", "0*u"):
+        assert not E.is_zero_literal(t)
+
+
+def test_user_function_and_interpolation():
+    ctx = E.Context(ParameterTree.from_text("""
+[parser_context.f]
+type = function
+expression = a, b: a*b + c
+[parser_context.c]
+type = constant
+value = 2
+[parser_context.tab]
+type = interpolation
+domain = 0 1 2
+range = 0 10 30
+""").sub("parser_context"))
+    assert E.Expression("f(3, 4)", ctx)({}) == pytest.approx(14.0)
+    assert E.Expression("tab(1.5)", ctx)({}) == pytest.approx(20.0)
+    assert E.Expression("tab(-1)", ctx)({}) == pytest.approx(0.0)
+    assert E.Expression("tab(5)", ctx)({}) == pytest.approx(30.0)
+
+
+def test_nested_user_function_rejected():
+    cfg = ParameterTree.from_text("""
+[parser_context.f]
+type = function
+expression = x: x
+[parser_context.g]
+type = function
+expression = x: f(x)
+""")
+    with pytest.raises(E.ExprError):
+        E.Context(cfg.sub("parser_context"))
+
+
+def test_alexander2_is_second_order():
+    """Alexander2 on u' = -u: global error ~ dt^2 (PDELab Alexander2Parameter)."""
+    ini = EXP_INI.replace("value = -2.", "value = -1.").replace("time_end = 10", "time_end = 1")
+    errs = []
+    for dt in (0.1, 0.05):
+        m = OracleModel(ini, {"model.time_step_operator.time_step_max": dt,
+                              "grid.refinement_level": 0})
+        x, t, _ = m.run()
+        errs.append(abs(x[0] - math.exp(-1.0)))
+    assert 3.5 < errs[0] / errs[1] < 4.5
+
+
+def test_rk_tables_are_consistent():
+    for name in ("ImplicitEuler", "Alexander2", "Heun", "Shu3", "RungeKutta4", "FractionalStepTheta",
+                 "Alexander3", "ExplicitEuler"):
+        A, B, D = rk_scheme(name)
+        for row in A:
+            assert abs(sum(row)) < 1e-14
+
+
+def test_snap_to_time_step_count():
+    """time_snap behaviour: evolve stops 2 dt before the end and snaps in equal steps."""
+    m = OracleModel(EXP_INI.replace("time_end = 10", "time_end = 1"),
+                    {"model.time_step_operator.time_step_max": "0.3"})
+    times = []
+    m.run(callback=lambda x, t: times.append(t))
+    assert times[-1] == pytest.approx(1.0)
+    assert all(f_le(a, b) for a, b in zip(times, times[1:]))
+
+
+def test_two_compartment_outflow_conserves_mass():
+    """Interface transmission T = k (a - b) moves mass between compartments without loss."""
+    ini = """
+[grid]
+cells = 8 8
+[compartments]
+left.expression = position_x < 0.5
+right.expression = position_x >= 0.5
+[model.scalar_field.a]
+compartment = left
+storage.expression = 1
+initial.expression = 1
+cross_diffusion.a.expression = 0.1
+outflow.right.expression = 0.5*(a - b)
+outflow.right.jacobian.a.expression = 0.5
+outflow.right.jacobian.b.expression = -0.5
+[model.scalar_field.b]
+compartment = right
+storage.expression = 1
+initial.expression = 0
+cross_diffusion.b.expression = 0.1
+outflow.left.expression = 0.5*(b - a)
+outflow.left.jacobian.b.expression = 0.5
+outflow.left.jacobian.a.expression = -0.5
+[model.time_step_operator]
+type = ImplicitEuler
+time_end = 0.5
+time_step_max = 0.1
+[model.time_step_operator.nonlinear_solver]
+convergence_condition.relative_tolerance = 1e-20
+"""
+    m = OracleModel(ini)
+    x0 = m.initial_state()
+    M = m.jacobian(x0, 0.0, "mass")
+    mass0 = M @ x0
+    x, t, _ = m.run()
+    mass1 = M @ x
+    assert abs(mass1.sum() - mass0.sum()) < 1e-10
+    a = m.species_values(x, "a")
+    b = m.species_values(x, "b")
+    assert a.max() < 1.0 and b.max() > 0.0

@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
 #pragma unroll
   for (int a = 0; a < NL; ++a)
 #pragma unroll
-    for (int s = 0; s < NS; ++s) c[a][s] = P.x[static_cast<int64_t>(nd[a]) * bs + s];
+    for (int s = 0; s < NS; ++s) c[a][s] = P.x ? P.x[static_cast<int64_t>(nd[a]) * bs + s] : 0.0;
   double g[NS][DIM];
 #pragma unroll
   for (int s = 0; s < NS; ++s)

@@ -5,15 +5,7 @@
 #include <string>
 
 #include "../../include/dcgpu.h"
-#include "model.hpp"
-#include "solver.hpp"
-
-struct dc_model {
-  std::unique_ptr<dcgpu::Model> model;
-  std::unique_ptr<dcgpu::Solver> solver;
-  cudaStream_t stream = nullptr;
-  dcgpu::DeviceBuffer<double> scratch_x, scratch_r, scratch_j;
-};
+#include "handle.hpp"
 
 namespace {
 

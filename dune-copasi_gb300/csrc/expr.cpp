@@ -331,6 +331,23 @@ bool ProgramBuilder::is_constant(int node, double* v) const {
   return true;
 }
 
+bool ProgramBuilder::depends_on(int node, const std::function<bool(uint16_t)>& pred) const {
+  std::vector<int> stack{node};
+  std::vector<char> seen(nodes_.size(), 0);
+  while (!stack.empty()) {
+    int k = stack.back();
+    stack.pop_back();
+    if (k < 0 || seen[k]) continue;
+    seen[k] = 1;
+    const Node& n = nodes_[k];
+    if (n.op == 255 && pred(n.input)) return true;
+    stack.push_back(n.a);
+    stack.push_back(n.b);
+    stack.push_back(n.c);
+  }
+  return false;
+}
+
 int ProgramBuilder::fold_or_make(uint8_t op, int a, int b, int c, int8_t imm) {
   double va = 0, vb = 0, vc = 0;
   bool ca = a < 0 || is_constant(a, &va);

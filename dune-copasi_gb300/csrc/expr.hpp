@@ -86,6 +86,8 @@ class ProgramBuilder {
   int add_output(int node);  // returns output index
   Program finish() const;
   bool is_constant(int node, double* v = nullptr) const;
+  // true when the value of `node` reads an input whose id satisfies `pred`
+  bool depends_on(int node, const std::function<bool(uint16_t)>& pred) const;
 
  private:
   struct Node {

@@ -1,0 +1,316 @@
+#include "krylov.cuh"
+
+#include <stdexcept>
+#include <string>
+
+namespace dcgpu {
+
+namespace {
+
+constexpr int kThreads = kReduceThreads;
+constexpr int kWarps = kThreads / 32;
+
+template <int NSUM>
+__device__ __forceinline__ void block_sum_to_thread0(double (&acc)[NSUM], double (*sh)[kWarps]) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NSUM; ++k) {
+    double v = acc[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) sh[k][warp] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NSUM; ++k) {
+      double v = 0.0;
+      for (int w = 0; w < kWarps; ++w) v += sh[k][w];
+      acc[k] = v;
+    }
+  }
+  __syncthreads();
+}
+
+// Deterministic grid reduction: partial sums per block, the last block to finish adds them
+// in index order.  Returns true in the last block, where thread 0 holds the totals in acc.
+template <int NSUM>
+__device__ __forceinline__ bool grid_sum(double (&acc)[NSUM], ReduceScratch rs) {
+  __shared__ double sh[NSUM][kWarps];
+  __shared__ bool last;
+  block_sum_to_thread0<NSUM>(acc, sh);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NSUM; ++k) rs.partial[blockIdx.x * 4 + k] = acc[k];
+    __threadfence();
+    const unsigned prev = atomicAdd(rs.counter, 1u);
+    last = (prev == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+#pragma unroll
+  for (int k = 0; k < NSUM; ++k) acc[k] = 0.0;
+  for (int b = threadIdx.x; b < static_cast<int>(gridDim.x); b += blockDim.x)
+#pragma unroll
+    for (int k = 0; k < NSUM; ++k) acc[k] += __ldcg(&rs.partial[b * 4 + k]);
+  block_sum_to_thread0<NSUM>(acc, sh);
+  if (threadIdx.x == 0) *rs.counter = 0u;
+  return threadIdx.x == 0;
+}
+
+__device__ __forceinline__ bool done(const double* sc) { return sc[KS_DONE] != 0.0; }
+
+template <class T>
+__global__ void __launch_bounds__(kThreads) k_init(T* x, T* r, T* rhat, T* p, T* v, int64_t n, double rel,
+                                                   ReduceScratch rs, double* sc) {
+  double acc[1] = {0.0};
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const T ri = r[i];
+    rhat[i] = ri;
+    p[i] = T(0);
+    v[i] = T(0);
+    x[i] = T(0);
+    acc[0] += static_cast<double>(ri) * static_cast<double>(ri);
+  }
+  if (grid_sum<1>(acc, rs)) {
+    const double rr = acc[0];
+    sc[KS_RR] = rr;
+    sc[KS_RR0] = rr;
+    sc[KS_RHO] = rr;
+    sc[KS_RHONEW] = rr;
+    sc[KS_ALPHA] = 1.0;
+    sc[KS_OMEGA] = 1.0;
+    sc[KS_BETA] = 1.0;
+    sc[KS_TARGET] = rel * rel * rr;
+    sc[KS_ITER] = 0.0;
+    sc[KS_DONE] = !isfinite(rr) ? kDoneNonFinite : (rr == 0.0 ? kDoneConverged : 0.0);
+  }
+}
+
+// (1) p = r + beta (p - omega v);  phat = D^-1 p   (one thread per block row)
+template <int B, class T, class V>
+__global__ void __launch_bounds__(kThreads) k_update_p(int nrows, T* __restrict__ p, const T* __restrict__ r,
+                                                       const T* __restrict__ v, const V* __restrict__ dinv,
+                                                       T* __restrict__ phat, const double* sc) {
+  if (done(sc)) return;
+  const V beta = static_cast<V>(sc[KS_BETA]), omega = static_cast<V>(sc[KS_OMEGA]);
+  const int stride = gridDim.x * blockDim.x;
+  for (int nd = blockIdx.x * blockDim.x + threadIdx.x; nd < nrows; nd += stride) {
+    const int64_t o = static_cast<int64_t>(nd) * B;
+    V pv[B];
+#pragma unroll
+    for (int i = 0; i < B; ++i) {
+      pv[i] = static_cast<V>(r[o + i]) + beta * (static_cast<V>(p[o + i]) - omega * static_cast<V>(v[o + i]));
+      p[o + i] = static_cast<T>(pv[i]);
+    }
+    const V* d = dinv + static_cast<int64_t>(nd) * B * B;
+#pragma unroll
+    for (int i = 0; i < B; ++i) {
+      V acc = V(0);
+#pragma unroll
+      for (int j = 0; j < B; ++j) acc += d[i * B + j] * pv[j];
+      phat[o + i] = static_cast<T>(acc);
+    }
+  }
+}
+
+// y = A x for one scalar row (block row br, row i inside the block)
+template <int B, class T, class V>
+__device__ __forceinline__ V row_product(int br, int i, const int32_t* __restrict__ rowptr,
+                                         const int32_t* __restrict__ colidx, const V* __restrict__ val,
+                                         const T* __restrict__ x) {
+  V acc = V(0);
+  const int k0 = rowptr[br], k1 = rowptr[br + 1];
+  for (int k = k0; k < k1; ++k) {
+    const int c = colidx[k];
+    const V* blk = val + static_cast<int64_t>(k) * B * B + i * B;
+    const T* xc = x + static_cast<int64_t>(c) * B;
+#pragma unroll
+    for (int j = 0; j < B; ++j) acc += blk[j] * static_cast<V>(xc[j]);
+  }
+  return acc;
+}
+
+// (2) v = A phat;  <rhat, v>;  alpha = rho / <rhat, v>
+template <int B, class T, class V>
+__global__ void __launch_bounds__(kThreads) k_spmv_rv(int nrows, const int32_t* __restrict__ rowptr,
+                                                      const int32_t* __restrict__ colidx, const V* __restrict__ val,
+                                                      const T* __restrict__ phat, T* __restrict__ v,
+                                                      const T* __restrict__ rhat, ReduceScratch rs, double* sc) {
+  if (done(sc)) return;
+  double acc[1] = {0.0};
+  const int64_t n = static_cast<int64_t>(nrows) * B;
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t row = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; row < n; row += stride) {
+    const V y = row_product<B, T, V>(static_cast<int>(row / B), static_cast<int>(row % B), rowptr, colidx, val, phat);
+    const T yt = static_cast<T>(y);
+    v[row] = yt;
+    acc[0] += static_cast<double>(rhat[row]) * static_cast<double>(yt);
+  }
+  if (grid_sum<1>(acc, rs)) {
+    const double rv = acc[0];
+    sc[KS_RV] = rv;
+    const double a = sc[KS_RHO] / rv;
+    if (!isfinite(rv)) sc[KS_DONE] = kDoneNonFinite;
+    else if (rv == 0.0 || !isfinite(a)) sc[KS_DONE] = kDoneBreakdown;
+    sc[KS_ALPHA] = isfinite(a) ? a : 0.0;
+  }
+}
+
+// (3) s = r - alpha v;  shat = D^-1 s;  ||s||^2
+template <int B, class T, class V>
+__global__ void __launch_bounds__(kThreads) k_update_s(int nrows, T* __restrict__ s, const T* __restrict__ r,
+                                                       const T* __restrict__ v, const V* __restrict__ dinv,
+                                                       T* __restrict__ shat, ReduceScratch rs, double* sc) {
+  if (done(sc)) return;
+  const V alpha = static_cast<V>(sc[KS_ALPHA]);
+  double acc[1] = {0.0};
+  const int stride = gridDim.x * blockDim.x;
+  for (int nd = blockIdx.x * blockDim.x + threadIdx.x; nd < nrows; nd += stride) {
+    const int64_t o = static_cast<int64_t>(nd) * B;
+    V sv[B];
+#pragma unroll
+    for (int i = 0; i < B; ++i) {
+      sv[i] = static_cast<V>(r[o + i]) - alpha * static_cast<V>(v[o + i]);
+      const T st = static_cast<T>(sv[i]);
+      s[o + i] = st;
+      acc[0] += static_cast<double>(st) * static_cast<double>(st);
+    }
+    const V* d = dinv + static_cast<int64_t>(nd) * B * B;
+#pragma unroll
+    for (int i = 0; i < B; ++i) {
+      V a2 = V(0);
+#pragma unroll
+      for (int j = 0; j < B; ++j) a2 += d[i * B + j] * sv[j];
+      shat[o + i] = static_cast<T>(a2);
+    }
+  }
+  if (grid_sum<1>(acc, rs)) sc[KS_SS] = acc[0];
+}
+
+// (4) t = A shat;  <t, s>, <t, t>;  omega = <t,s>/<t,t>
+template <int B, class T, class V>
+__global__ void __launch_bounds__(kThreads) k_spmv_omega(int nrows, const int32_t* __restrict__ rowptr,
+                                                         const int32_t* __restrict__ colidx,
+                                                         const V* __restrict__ val, const T* __restrict__ shat,
+                                                         T* __restrict__ t, const T* __restrict__ s,
+                                                         ReduceScratch rs, double* sc) {
+  if (done(sc)) return;
+  double acc[2] = {0.0, 0.0};
+  const int64_t n = static_cast<int64_t>(nrows) * B;
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t row = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; row < n; row += stride) {
+    const V y = row_product<B, T, V>(static_cast<int>(row / B), static_cast<int>(row % B), rowptr, colidx, val, shat);
+    const T yt = static_cast<T>(y);
+    t[row] = yt;
+    const double td = static_cast<double>(yt);
+    acc[0] += td * static_cast<double>(s[row]);
+    acc[1] += td * td;
+  }
+  if (grid_sum<2>(acc, rs)) {
+    sc[KS_TS] = acc[0];
+    sc[KS_TT] = acc[1];
+    double w = acc[1] != 0.0 ? acc[0] / acc[1] : 0.0;
+    if (!isfinite(w)) {
+      sc[KS_DONE] = kDoneNonFinite;
+      w = 0.0;
+    }
+    sc[KS_OMEGA] = w;
+  }
+}
+
+// (5) x += alpha phat + omega shat;  r = s - omega t;  ||r||^2, <rhat, r>;  convergence
+template <class T>
+__global__ void __launch_bounds__(kThreads) k_update_xr(int64_t n, T* __restrict__ x, T* __restrict__ r,
+                                                        const T* __restrict__ phat, const T* __restrict__ shat,
+                                                        const T* __restrict__ s, const T* __restrict__ t,
+                                                        const T* __restrict__ rhat, ReduceScratch rs, double* sc) {
+  if (done(sc)) return;
+  using C = T;
+  const C alpha = static_cast<C>(sc[KS_ALPHA]), omega = static_cast<C>(sc[KS_OMEGA]);
+  double acc[2] = {0.0, 0.0};
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
+    x[i] = x[i] + alpha * phat[i] + omega * shat[i];
+    const T ri = s[i] - omega * t[i];
+    r[i] = ri;
+    acc[0] += static_cast<double>(ri) * static_cast<double>(ri);
+    acc[1] += static_cast<double>(rhat[i]) * static_cast<double>(ri);
+  }
+  if (grid_sum<2>(acc, rs)) {
+    const double rr = acc[0], rho_new = acc[1];
+    sc[KS_RR] = rr;
+    sc[KS_RHONEW] = rho_new;
+    sc[KS_ITER] += 1.0;
+    if (!isfinite(rr) || !isfinite(rho_new)) {
+      sc[KS_DONE] = kDoneNonFinite;
+      return;
+    }
+    if (rr <= sc[KS_TARGET]) {
+      sc[KS_DONE] = kDoneConverged;
+      return;
+    }
+    const double beta = (rho_new / sc[KS_RHO]) * (sc[KS_ALPHA] / sc[KS_OMEGA]);
+    if (rho_new == 0.0 || sc[KS_OMEGA] == 0.0 || !isfinite(beta)) {
+      sc[KS_DONE] = kDoneBreakdown;
+      return;
+    }
+    sc[KS_BETA] = beta;
+    sc[KS_RHO] = rho_new;
+  }
+}
+
+inline int grid_for(int64_t n) {
+  int64_t b = (n + kThreads - 1) / kThreads;
+  if (b > kReduceBlocks) b = kReduceBlocks;
+  return static_cast<int>(b < 1 ? 1 : b);
+}
+
+}  // namespace
+
+template <class T>
+void krylov_init(const KrylovVectors<T>& k, int64_t n, double rel, ReduceScratch rs, double* sc, cudaStream_t s) {
+  count_launches(1);
+  k_init<T><<<kReduceBlocks, kThreads, 0, s>>>(k.x, k.r, k.rhat, k.p, k.v, n, rel, rs, sc);
+}
+
+template <class T, class V>
+void krylov_iteration(const Bsr& A, const V* vals, const V* dinv, const KrylovVectors<T>& k, ReduceScratch rs,
+                      double* sc, cudaStream_t s, cudaEvent_t* ev) {
+  const int64_t n = static_cast<int64_t>(A.nrows) * A.bs;
+  const int gn = grid_for(A.nrows);
+  count_launches(5);
+  auto mark = [&](int i) {
+    if (ev && cudaEventRecord(ev[i], s) != cudaSuccess) throw std::runtime_error("cudaEventRecord failed");
+  };
+#define DC_KR(B)                                                                                                 \
+  case B:                                                                                                        \
+    k_update_p<B, T, V><<<gn, kThreads, 0, s>>>(A.nrows, k.p, k.r, k.v, dinv, k.phat, sc);                        \
+    mark(0);                                                                                                     \
+    k_spmv_rv<B, T, V><<<kReduceBlocks, kThreads, 0, s>>>(A.nrows, A.rowptr, A.colidx, vals, k.phat, k.v, k.rhat, \
+                                                          rs, sc);                                                \
+    mark(1);                                                                                                     \
+    k_update_s<B, T, V><<<kReduceBlocks, kThreads, 0, s>>>(A.nrows, k.s, k.r, k.v, dinv, k.shat, rs, sc);         \
+    mark(2);                                                                                                     \
+    k_spmv_omega<B, T, V><<<kReduceBlocks, kThreads, 0, s>>>(A.nrows, A.rowptr, A.colidx, vals, k.shat, k.t, k.s, \
+                                                             rs, sc);                                             \
+    mark(3);                                                                                                     \
+    break;
+  switch (A.bs) {
+    DC_KR(1) DC_KR(2) DC_KR(3) DC_KR(4) DC_KR(5) DC_KR(6) DC_KR(7) DC_KR(8)
+    default: throw std::runtime_error("krylov: block size " + std::to_string(A.bs) + " unsupported");
+  }
+#undef DC_KR
+  k_update_xr<T><<<kReduceBlocks, kThreads, 0, s>>>(n, k.x, k.r, k.phat, k.shat, k.s, k.t, k.rhat, rs, sc);
+}
+
+template void krylov_init<double>(const KrylovVectors<double>&, int64_t, double, ReduceScratch, double*, cudaStream_t);
+template void krylov_init<float>(const KrylovVectors<float>&, int64_t, double, ReduceScratch, double*, cudaStream_t);
+template void krylov_iteration<double, double>(const Bsr&, const double*, const double*, const KrylovVectors<double>&,
+                                               ReduceScratch, double*, cudaStream_t, cudaEvent_t*);
+template void krylov_iteration<float, float>(const Bsr&, const float*, const float*, const KrylovVectors<float>&,
+                                             ReduceScratch, double*, cudaStream_t, cudaEvent_t*);
+
+}  // namespace dcgpu

@@ -1,0 +1,46 @@
+// Block-Jacobi preconditioned BiCGSTAB with device-side convergence control.
+//
+// Replaces the dune-istl BiCGSTABSolver that the reference's LinearSolver drives
+// (dune/copasi/model/make_step_operator.hh:102-146, solver/istl/factory/iterative.hh:76-109).
+// One iteration is five kernels: (1) p update fused with the block-Jacobi apply,
+// (2) SpMV fused with <rhat, v>, (3) s update fused with the block-Jacobi apply and ||s||^2,
+// (4) SpMV fused with <t, s> and <t, t>, (5) x / r update with ||r||^2 and <rhat, r>.
+// Every kernel starts by reading a device "done" flag and returns at once when the solve
+// has converged or broken down, so a CUDA graph of several iterations can be replayed
+// without a host round trip per iteration.  Reductions are deterministic.
+#pragma once
+
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "linalg.cuh"
+
+namespace dcgpu {
+
+// device scalar slots
+enum KrylovSlot : int {
+  KS_RHO = 0, KS_ALPHA = 1, KS_OMEGA = 2, KS_RHONEW = 3, KS_RV = 4, KS_TS = 5, KS_TT = 6,
+  KS_RR = 7, KS_SS = 8, KS_BETA = 9, KS_TARGET = 10, KS_DONE = 11, KS_ITER = 12, KS_RR0 = 13,
+  KS_COUNT = 16
+};
+// KS_DONE values
+constexpr double kDoneConverged = 1.0, kDoneBreakdown = 2.0, kDoneNonFinite = 3.0;
+
+template <class T>
+struct KrylovVectors {
+  T *x, *r, *rhat, *p, *v, *s, *t, *phat, *shat;
+};
+
+// r must hold the right-hand side; sets x = 0, rhat = r, p = v = 0 and the scalars;
+// target = (rel * ||r||)^2
+template <class T>
+void krylov_init(const KrylovVectors<T>& k, int64_t n, double rel, ReduceScratch rs, double* sc, cudaStream_t s);
+
+// one iteration (five launches); V is the matrix / preconditioner value type.  When `ev`
+// is given, ev[0..1] bracket the first SpMV kernel and ev[2..3] the second.
+template <class T, class V>
+void krylov_iteration(const Bsr& A, const V* vals, const V* dinv, const KrylovVectors<T>& k, ReduceScratch rs,
+                      double* sc, cudaStream_t s, cudaEvent_t* ev = nullptr);
+
+}  // namespace dcgpu

@@ -204,7 +204,8 @@ template <int B, class V, class X>
 __global__ void __launch_bounds__(256) k_spmv(int nrows, const int32_t* __restrict__ rowptr,
                                               const int32_t* __restrict__ colidx, const V* __restrict__ val,
                                               const X* __restrict__ x, X* __restrict__ y,
-                                              const X* __restrict__ b) {
+                                              const X* __restrict__ b, const double alpha,
+                                              const int accumulate) {
   const int64_t row = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (row >= static_cast<int64_t>(nrows) * B) return;
   const int br = static_cast<int>(row / B), i = static_cast<int>(row % B);
@@ -218,19 +219,21 @@ __global__ void __launch_bounds__(256) k_spmv(int nrows, const int32_t* __restri
 #pragma unroll
     for (int j = 0; j < B; ++j) acc += blk[j] * static_cast<V>(xc[j]);
   }
-  if (b) y[row] = static_cast<X>(static_cast<double>(b[row]) - acc);
+  if (accumulate) y[row] = static_cast<X>(static_cast<double>(y[row]) + alpha * static_cast<double>(acc));
+  else if (b) y[row] = static_cast<X>(static_cast<double>(b[row]) - acc);
   else y[row] = static_cast<X>(acc);
 }
 
 template <class V, class X>
-void spmv_dispatch(const Bsr& A, const V* val, const X* x, X* y, const X* b, cudaStream_t s) {
+void spmv_dispatch(const Bsr& A, const V* val, const X* x, X* y, const X* b, cudaStream_t s,
+                   double alpha = 1.0, int accumulate = 0) {
   const int64_t n = static_cast<int64_t>(A.nrows) * A.bs;
   if (n == 0) return;
   const int threads = 256;
   const int blocks = static_cast<int>((n + threads - 1) / threads);
   count_launches(1);
 #define DC_SPMV(B) \
-  case B: k_spmv<B, V, X><<<blocks, threads, 0, s>>>(A.nrows, A.rowptr, A.colidx, val, x, y, b); return;
+  case B: k_spmv<B, V, X><<<blocks, threads, 0, s>>>(A.nrows, A.rowptr, A.colidx, val, x, y, b, alpha, accumulate); return;
   switch (A.bs) {
     DC_SPMV(1) DC_SPMV(2) DC_SPMV(3) DC_SPMV(4) DC_SPMV(5) DC_SPMV(6) DC_SPMV(7) DC_SPMV(8)
     default: throw std::runtime_error("spmv: block size " + std::to_string(A.bs) + " unsupported");
@@ -369,6 +372,9 @@ void spmv32(const Bsr& A, const float* x, float* y, cudaStream_t s) {
 }
 void residual(const Bsr& A, const double* x, const double* b, double* r, cudaStream_t s) {
   spmv_dispatch<double, double>(A, A.val, x, r, b, s);
+}
+void spmv_acc(const Bsr& A, const double* vals, const double* x, double* y, double alpha, cudaStream_t s) {
+  spmv_dispatch<double, double>(A, vals, x, y, nullptr, s, alpha, 1);
 }
 
 void dot(const double* x, const double* y, int64_t n, ReduceScratch rs, int slot, cudaStream_t s) {

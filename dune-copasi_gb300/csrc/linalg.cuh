@@ -36,6 +36,8 @@ void spmv(const Bsr& A, const double* x, double* y, cudaStream_t s);
 void spmv32(const Bsr& A, const float* x, float* y, cudaStream_t s);
 // r = b - A x (fp64)
 void residual(const Bsr& A, const double* x, const double* b, double* r, cudaStream_t s);
+// y += alpha * V x with the pattern of A and the values V (fp64)
+void spmv_acc(const Bsr& A, const double* vals, const double* x, double* y, double alpha, cudaStream_t s);
 
 // result[slot] = <x, y>  (deterministic; fixed grid and order)
 void dot(const double* x, const double* y, int64_t n, ReduceScratch rs, int slot, cudaStream_t s);

@@ -116,6 +116,51 @@ Model::Model(const std::string& ini_text, const std::string& overrides) {
   upload_geometry();
   build_volume_groups();
   build_face_groups();
+  build_static_matrices();
+}
+
+void Model::build_static_matrices() {
+  const int64_t nvals = nnzb() * bs * bs;
+  for (const auto& g : vgroups) {
+    has_Ms |= g.static_mass;
+    has_Ks |= g.static_stiffness;
+  }
+  if (has_Ms) {
+    d_Ms.resize(nvals);
+    cuda_check(cudaMemset(d_Ms.get(), 0, nvals * sizeof(double)), "memset");
+  }
+  if (has_Ks) {
+    d_Ks.resize(nvals);
+    cuda_check(cudaMemset(d_Ks.get(), 0, nvals * sizeof(double)), "memset");
+  }
+  for (const auto& g : vgroups) {
+    if (g.static_terms.empty()) continue;
+    VolumeParams p{};
+    p.coords = d_coords.get();
+    p.verts = g.verts.get();
+    p.nodes = g.nodes.get();
+    p.bpos = g.bpos.get();
+    p.prog = g.prog_static.view();
+    p.res_terms = nullptr;
+    p.n_res_terms = 0;
+    p.jac_terms = g.d_static.get();
+    p.n_jac_terms = static_cast<int>(g.static_terms.size());
+    p.tables = tables;
+    p.x = nullptr;
+    p.r = nullptr;
+    p.bs = bs;
+    p.species_offset = species_offset[g.comp];
+    p.t = 0.0;
+    for (int form = 0; form < 2; ++form) {
+      if ((form == 0 && !g.static_mass) || (form == 1 && !g.static_stiffness)) continue;
+      p.J = form == 0 ? d_Ms.get() : d_Ks.get();
+      p.cm = form == 0 ? 1.0 : 0.0;
+      p.ca = form == 0 ? 0.0 : 1.0;
+      for (size_t k = 0; k + 1 < g.color_offsets.size(); ++k)
+        launch_volume(dim, g.ns, p, g.color_offsets[k], g.color_offsets[k + 1], 2, nullptr);
+    }
+  }
+  cuda_check(cudaDeviceSynchronize(), "static operator assembly");
 }
 
 void Model::build_species() {
@@ -507,9 +552,20 @@ void Model::build_volume_groups() {
       return -1;
     };
 
-    // two builders: residual-only program and residual+Jacobian program
-    for (int pass = 0; pass < 2; ++pass) {
-      const bool with_jac = pass == 1;
+    // A term is static when it is linear in the state with a coefficient that depends on
+    // neither the state nor time (constant or position-only storage / scalar diffusion
+    // without Jacobian entries).  Static terms are assembled once into the matrices Ms / Ks
+    // (residual = matrix x state, exactly, since these terms are symmetric in test and trial);
+    // the per-iteration kernels evaluate only the remaining, dynamic terms.
+    auto is_static_text = [&](const std::string& text) {
+      ProgramBuilder probe(ctx);
+      int node = probe.compile_text(text, res);
+      return !probe.depends_on(node, [](uint16_t id) { return id < IN_POSITION || id == IN_TIME; });
+    };
+    // three builders: static Jacobian program, dynamic residual-only, dynamic residual+Jacobian
+    for (int pass = 0; pass < 3; ++pass) {
+      const bool static_pass = pass == 0;
+      const bool with_jac = pass != 1;
       ProgramBuilder pb(ctx);
       std::vector<Term> rterms, jterms;
       int coef = 0;
@@ -555,19 +611,27 @@ void Model::build_volume_groups() {
         // mass form: storage (local_equations.hh:340-353)
         if (scfg.has_sub("storage"))
           if (auto st = scalar_fn(scfg.sub("storage"), species)) {
-            g.has_mass = true;
-            int o = out_of(st->value);
-            add_r(R_STORAGE, 0, i, i, o);
-            if (with_jac) {
-              add_j(J_STORAGE_SELF, 0, i, i, o);
-              for (const auto& [w, jt] : st->jac) {
-                int wl = local_of(w);
-                if (wl >= 0) add_j(J_MASS_U, 0, i, wl, out_of(jt));
+            const bool stat = st->jac.empty() && is_static_text(st->value);
+            if (static_pass) {
+              if (stat) {
+                g.static_mass = true;
+                add_j(J_STORAGE_SELF, 0, i, i, out_of(st->value));
+              }
+            } else if (!stat) {
+              g.has_mass = true;
+              int o = out_of(st->value);
+              add_r(R_STORAGE, 0, i, i, o);
+              if (with_jac) {
+                add_j(J_STORAGE_SELF, 0, i, i, o);
+                for (const auto& [w, jt] : st->jac) {
+                  int wl = local_of(w);
+                  if (wl >= 0) add_j(J_MASS_U, 0, i, wl, out_of(jt));
+                }
               }
             }
           }
         // stiffness form: reaction, velocity, diffusion (local_equations.hh:325-338)
-        if (scfg.has_sub("reaction"))
+        if (!static_pass && scfg.has_sub("reaction"))
           if (auto rf = scalar_fn(scfg.sub("reaction"), species)) {
             g.has_stiffness = true;
             add_r(R_REACTION, 1, i, i, out_of(rf->value));
@@ -577,7 +641,7 @@ void Model::build_volume_groups() {
                 if (wl >= 0) add_j(J_MASS, 1, i, wl, out_neg(jt));
               }
           }
-        if (scfg.has_sub("velocity")) {
+        if (!static_pass && scfg.has_sub("velocity")) {
           Ini vc = scfg.sub("velocity");
           if (auto comps = vector_fn(vc, dim)) {
             g.has_stiffness = true;
@@ -604,24 +668,39 @@ void Model::build_volume_groups() {
             if (!D) continue;
             const int wl = local_of(sp2.name);
             if (wl < 0) continue;  // gradient vanishes on this element
+            std::vector<std::pair<int, TensorFn>> djac;
+            Ini jc = dc.sub("jacobian");
+            for (const auto& sp3 : species)
+              if (jc.has_sub(sp3.name))
+                if (auto JD = tensor_fn(jc.sub(sp3.name), dim)) {
+                  int vl = local_of(sp3.name);
+                  if (vl >= 0) djac.emplace_back(vl, *JD);
+                }
+            const bool stat = !D->tensor && djac.empty() && is_static_text(D->entries[0]);
+            if (static_pass) {
+              if (stat) {
+                g.static_stiffness = true;
+                add_j(J_DIFF_SCALAR, 1, i, wl, out_of(D->entries[0]));
+              }
+              continue;
+            }
+            if (stat) continue;
             g.has_stiffness = true;
             int o = outs_of(D->entries);
             add_r(D->tensor ? R_DIFF_TENSOR : R_DIFF_SCALAR, 1, i, wl, o);
             if (with_jac) {
               add_j(D->tensor ? J_DIFF_TENSOR : J_DIFF_SCALAR, 1, i, wl, o);
-              Ini jc = dc.sub("jacobian");
-              for (const auto& sp3 : species)
-                if (jc.has_sub(sp3.name))
-                  if (auto JD = tensor_fn(jc.sub(sp3.name), dim)) {
-                    int vl = local_of(sp3.name);
-                    if (vl >= 0) add_j(JD->tensor ? J_DIFFJAC_TENSOR : J_DIFFJAC_SCALAR, 1, i, vl, outs_of(JD->entries));
-                  }
+              for (const auto& [vl, JD] : djac)
+                add_j(JD.tensor ? J_DIFFJAC_TENSOR : J_DIFFJAC_SCALAR, 1, i, vl, outs_of(JD.entries));
             }
           }
         }
       }
       if (coef > kMaxCoefficients) throw ConfigError("too many Jacobian terms in one compartment");
       if (pass == 0) {
+        g.prog_static.host = pb.finish();
+        g.static_terms = jterms;
+      } else if (pass == 1) {
         g.prog_res.host = pb.finish();
         g.res_terms_r = rterms;
       } else {
@@ -630,8 +709,10 @@ void Model::build_volume_groups() {
         g.jac_terms = jterms;
       }
     }
+    g.prog_static.upload();
     g.prog_res.upload();
     g.prog_all.upload();
+    g.d_static.upload(g.static_terms);
     g.d_res_r.upload(g.res_terms_r);
     g.d_res_a.upload(g.res_terms_a);
     g.d_jac.upload(g.jac_terms);
@@ -856,6 +937,17 @@ Bsr Model::bsr(double* val, float* val32) const {
 
 void Model::assemble(const double* x, double t, double cm, double ca, double* r, double* J, int mode,
                      cudaStream_t s) const {
+  // static part: r += (cm Ms + ca Ks) x, J += cm Ms + ca Ks
+  const Bsr A0 = bsr(nullptr, nullptr);
+  const int64_t nvals = nnzb() * bs * bs;
+  if ((mode & 1) && r) {
+    if (has_Ms && cm != 0.0) spmv_acc(A0, d_Ms.get(), x, r, cm, s);
+    if (has_Ks && ca != 0.0) spmv_acc(A0, d_Ks.get(), x, r, ca, s);
+  }
+  if ((mode & 2) && J) {
+    if (has_Ms && cm != 0.0) axpy(nvals, cm, d_Ms.get(), J, s);
+    if (has_Ks && ca != 0.0) axpy(nvals, ca, d_Ks.get(), J, s);
+  }
   for (const auto& g : vgroups) {
     if (!(cm != 0.0 && g.has_mass) && !(ca != 0.0 && g.has_stiffness)) continue;
     VolumeParams p{};

@@ -96,10 +96,12 @@ struct VolumeGroup {
   int64_t ne = 0;
   std::vector<int> color_offsets;  // colour c: [off[c], off[c+1])
   DeviceBuffer<int32_t> verts, nodes, bpos;
-  ProgramBundle prog_res, prog_all;
-  std::vector<Term> res_terms_r, res_terms_a, jac_terms;  // for prog_res / prog_all
-  DeviceBuffer<Term> d_res_r, d_res_a, d_jac;
-  bool has_mass = false, has_stiffness = false;
+  ProgramBundle prog_static, prog_res, prog_all;
+  std::vector<Term> static_terms;                          // for prog_static (Jacobian terms)
+  std::vector<Term> res_terms_r, res_terms_a, jac_terms;   // for prog_res / prog_all
+  DeviceBuffer<Term> d_static, d_res_r, d_res_a, d_jac;
+  bool has_mass = false, has_stiffness = false;            // dynamic terms present
+  bool static_mass = false, static_stiffness = false;      // static terms present
 };
 
 struct FaceGroup {
@@ -158,6 +160,10 @@ class Model {
   std::vector<VolumeGroup> vgroups;
   std::vector<FaceGroup> fgroups;
 
+  // static parts of the operator, assembled once: mass-form and stiffness-form BSR values
+  DeviceBuffer<double> d_Ms, d_Ks;
+  bool has_Ms = false, has_Ks = false;
+
   // host-side helpers
   std::vector<double> initial_state() const;        // reference DOF order
   void to_blocked(const std::vector<double>& ref, std::vector<double>& blk) const;
@@ -179,6 +185,7 @@ class Model {
   void build_face_groups();
   void build_pattern();
   void upload_geometry();
+  void build_static_matrices();
 };
 
 }  // namespace dcgpu

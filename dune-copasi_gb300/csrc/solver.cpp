@@ -148,6 +148,9 @@ Solver::~Solver() {
     cudaEventDestroy(p.b);
   }
   for (cudaEvent_t e : event_pool_) cudaEventDestroy(e);
+  for (auto& g : graphs_)
+    if (g) cudaGraphExecDestroy(g);
+  for (cudaEvent_t e : graph_events_) cudaEventDestroy(e);
 }
 
 void Solver::set_state(const std::vector<double>& ref, double t) {
@@ -240,50 +243,90 @@ void Solver::setup_preconditioner() {
   }
 }
 
-int Solver::bicgstab(const double* b, double* z, double rel_tol, int max_it, int* iters) {
-  // z = 0 start: r = b
-  Bsr A = model.bsr(J_.get(), nullptr);
-  const int64_t n = n_;
-  cuda_check(cudaMemsetAsync(z, 0, n * sizeof(double), stream), "memset");
-  cuda_check(cudaMemcpyAsync(kr_.get(), b, n * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");
+// Graph of kKrylovChunk BiCGSTAB iterations on this solver's fixed workspace (fp64 or
+// fp32); with profiling on, event-record nodes bracket the two SpMV kernels of every
+// iteration so their device time can be read after the replay.
+cudaGraphExec_t Solver::krylov_graph(bool fp32) {
+  const int slot = (fp32 ? 1 : 0) + (profiling_ ? 2 : 0);
+  if (graphs_[slot]) return graphs_[slot];
+  Bsr A = model.bsr(J_.get(), J32_.get());
   double* sc = scal_.get();
-  bicg_init(kr_.get(), krhat_.get(), kp_.get(), kv_.get(), n, rs_, sc, stream);
-  double h[11];
-  read_scalars(h, 0, 11);
-  const double r0 = std::sqrt(h[7]);
-  *iters = 0;
-  if (r0 == 0.0) return DC_OK;
-  if (!std::isfinite(r0)) return DC_ERR_DIVERGED;
-  const double target = rel_tol * r0;
-  for (int it = 1; it <= max_it; ++it) {
-    bicg_update_p(kp_.get(), kr_.get(), kv_.get(), n, sc, stream);
-    tbegin(2);
-    block_jacobi_apply(A.nrows, A.bs, dinv_.get(), kp_.get(), kphat_.get(), stream);
-    tend();
-    tbegin(1);
-    spmv(A, kphat_.get(), kv_.get(), stream);
-    tend();
-    bicg_alpha(krhat_.get(), kv_.get(), n, rs_, sc, stream);
-    bicg_s(ks_.get(), kr_.get(), kv_.get(), n, rs_, sc, stream);
-    tbegin(2);
-    block_jacobi_apply(A.nrows, A.bs, dinv_.get(), ks_.get(), kshat_.get(), stream);
-    tend();
-    tbegin(1);
-    spmv(A, kshat_.get(), kt_.get(), stream);
-    tend();
-    bicg_omega(kt_.get(), ks_.get(), n, rs_, sc, stream);
-    bicg_xr(z, kr_.get(), kphat_.get(), kshat_.get(), ks_.get(), kt_.get(), krhat_.get(), n, rs_, sc, stream);
-    read_scalars(h, 0, 11);
-    *iters = it;
-    const double rn = std::sqrt(h[7]);
-    if (!std::isfinite(rn)) return DC_ERR_DIVERGED;
-    if (rn <= target) return DC_OK;
-    if (h[10] != 0.0) {
-      // breakdown: accept if already good enough, otherwise report failure
-      return rn <= target ? DC_OK : DC_ERR_DIVERGED;
+  cudaEvent_t* ev = nullptr;
+  if (profiling_) {
+    if (graph_events_.empty()) {
+      graph_events_.resize(kKrylovChunk * 4);
+      for (auto& e : graph_events_) cuda_check(cudaEventCreate(&e), "cudaEventCreate");
+    }
+    ev = graph_events_.data();
+  }
+  cudaGraph_t g = nullptr;
+  cuda_check(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+  for (int k = 0; k < kKrylovChunk; ++k) {
+    cudaEvent_t* e = ev ? ev + 4 * k : nullptr;
+    if (fp32) {
+      KrylovVectors<float> kv{fx_.get(), fr_.get(), frhat_.get(), fp_.get(), fv_.get(), fs_.get(), ft_.get(),
+                              fphat_.get(), fshat_.get()};
+      krylov_iteration<float, float>(A, J32_.get(), fdinv_.get(), kv, rs_, sc, stream, e);
+    } else {
+      KrylovVectors<double> kv{kx_.get(), kr_.get(), krhat_.get(), kp_.get(), kv_.get(), ks_.get(), kt_.get(),
+                               kphat_.get(), kshat_.get()};
+      krylov_iteration<double, double>(A, J_.get(), dinv_.get(), kv, rs_, sc, stream, e);
     }
   }
-  return DC_ERR_TIMEOUT;
+  cuda_check(cudaStreamEndCapture(stream, &g), "cudaStreamEndCapture");
+  cuda_check(cudaGraphInstantiate(&graphs_[slot], g, 0), "cudaGraphInstantiate");
+  cudaGraphDestroy(g);
+  count_launches(-5LL * kKrylovChunk);  // the capture launched nothing; replays are counted
+  return graphs_[slot];
+}
+
+// Replays chunks of BiCGSTAB iterations until the device flag reports convergence,
+// breakdown or a non-finite value, or max_it iterations have run.  r (kr_ / fr_) holds
+// the right-hand side on entry; the solution is left in the Krylov x vector.
+int Solver::krylov_run(bool fp32, double rel, int max_it, int* iters) {
+  double* sc = scal_.get();
+  const int64_t n = n_;
+  if (fp32) {
+    KrylovVectors<float> kv{fx_.get(), fr_.get(), frhat_.get(), fp_.get(), fv_.get(), fs_.get(), ft_.get(),
+                            fphat_.get(), fshat_.get()};
+    krylov_init<float>(kv, n, rel, rs_, sc, stream);
+  } else {
+    KrylovVectors<double> kv{kx_.get(), kr_.get(), krhat_.get(), kp_.get(), kv_.get(), ks_.get(), kt_.get(),
+                             kphat_.get(), kshat_.get()};
+    krylov_init<double>(kv, n, rel, rs_, sc, stream);
+  }
+  cudaGraphExec_t exec = krylov_graph(fp32);
+  double h[KS_COUNT];
+  read_scalars(h, 0, KS_COUNT);
+  int it = 0;
+  while (h[KS_DONE] == 0.0 && it < max_it) {
+    cuda_check(cudaGraphLaunch(exec, stream), "cudaGraphLaunch");
+    count_launches(5LL * kKrylovChunk);
+    read_scalars(h, 0, KS_COUNT);
+    const int now = static_cast<int>(h[KS_ITER]);
+    if (profiling_) {
+      for (int k = 0; k < now - it && k < kKrylovChunk; ++k)
+        for (int pair = 0; pair < 2; ++pair) {
+          float ms = 0.0f;
+          cuda_check(cudaEventElapsedTime(&ms, graph_events_[4 * k + 2 * pair], graph_events_[4 * k + 2 * pair + 1]),
+                     "cudaEventElapsedTime");
+          kernel_times.ms[1] += ms;
+          kernel_times.calls[1] += 1;
+        }
+    }
+    it = now;
+  }
+  *iters = it;
+  if (h[KS_DONE] == kDoneConverged) return DC_OK;
+  if (h[KS_DONE] == 0.0) return DC_ERR_TIMEOUT;
+  return DC_ERR_DIVERGED;
+}
+
+int Solver::bicgstab(const double* b, double* z, double rel_tol, int max_it, int* iters) {
+  cuda_check(cudaMemcpyAsync(kr_.get(), b, n_ * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");
+  int st = krylov_run(false, rel_tol, max_it, iters);
+  cuda_check(cudaMemcpyAsync(z, kx_.get(), n_ * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");
+  return st;
 }
 
 // fp32 BiCGSTAB on the correction equation inside fp64 iterative refinement:
@@ -291,7 +334,6 @@ int Solver::bicgstab(const double* b, double* z, double rel_tol, int max_it, int
 int Solver::bicgstab_mixed(const double* b, double* z, double rel_tol, int max_it, int* iters) {
   Bsr A = model.bsr(J_.get(), J32_.get());
   const int64_t n = n_;
-  double* sc = scal_.get();
   cuda_check(cudaMemsetAsync(z, 0, n * sizeof(double), stream), "memset");
   const double b0 = std::sqrt(norm2(b));
   *iters = 0;
@@ -303,47 +345,24 @@ int Solver::bicgstab_mixed(const double* b, double* z, double rel_tol, int max_i
   int total = 0;
   for (int ref = 0; ref < 50 && total < max_it; ++ref) {
     // fp64 refinement residual r = b - J z (skip the SpMV for z = 0)
-    if (ref == 0) cuda_check(cudaMemcpyAsync(kr_.get(), b, n * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");
-    else residual(A, z, b, kr_.get(), stream);
-    if (ref > 0) {
+    if (ref == 0) {
+      cuda_check(cudaMemcpyAsync(kr_.get(), b, n * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");
+    } else {
+      residual(A, z, b, kr_.get(), stream);
       rn = std::sqrt(norm2(kr_.get()));
       if (!std::isfinite(rn)) return DC_ERR_DIVERGED;
-      if (rn <= target) { *iters = total; return DC_OK; }
+      if (rn <= target) {
+        *iters = total;
+        return DC_OK;
+      }
     }
     ++stats.refinements;
-    // scale into fp32 range
-    const double scale = 1.0 / rn;
-    to_float_scaled(n, kr_.get(), scale, fr_.get(), stream);
-    cuda_check(cudaMemsetAsync(fx_.get(), 0, n * sizeof(float), stream), "memset");
-    bicg_init32(fr_.get(), frhat_.get(), fp_.get(), fv_.get(), n, rs_, sc, stream);
-    double h[11];
-    read_scalars(h, 0, 11);
-    const double f0 = std::sqrt(h[7]);
-    const double ftarget = std::max(inner_red, 0.5 * target / rn) * f0;
-    for (int it = 1; it <= max_it - total; ++it) {
-      bicg_update_p32(fp_.get(), fr_.get(), fv_.get(), n, sc, stream);
-      tbegin(2);
-      block_jacobi_apply32(A.nrows, A.bs, fdinv_.get(), fp_.get(), fphat_.get(), stream);
-      tend();
-      tbegin(1);
-      spmv32(A, fphat_.get(), fv_.get(), stream);
-      tend();
-      bicg_alpha32(frhat_.get(), fv_.get(), n, rs_, sc, stream);
-      bicg_s32(fs_.get(), fr_.get(), fv_.get(), n, rs_, sc, stream);
-      tbegin(2);
-      block_jacobi_apply32(A.nrows, A.bs, fdinv_.get(), fs_.get(), fshat_.get(), stream);
-      tend();
-      tbegin(1);
-      spmv32(A, fshat_.get(), ft_.get(), stream);
-      tend();
-      bicg_omega32(ft_.get(), fs_.get(), n, rs_, sc, stream);
-      bicg_xr32(fx_.get(), fr_.get(), fphat_.get(), fshat_.get(), fs_.get(), ft_.get(), frhat_.get(), n, rs_, sc, stream);
-      read_scalars(h, 0, 11);
-      ++total;
-      const double fn = std::sqrt(h[7]);
-      if (!std::isfinite(fn)) return DC_ERR_DIVERGED;
-      if (fn <= ftarget || h[10] != 0.0) break;
-    }
+    // scale into fp32 range and solve the correction equation in fp32
+    to_float_scaled(n, kr_.get(), 1.0 / rn, fr_.get(), stream);
+    int it = 0;
+    const int st = krylov_run(true, std::max(inner_red, 0.5 * target / rn), max_it - total, &it);
+    total += it;
+    if (st == DC_ERR_DIVERGED && it == 0) return DC_ERR_DIVERGED;
     add_float_scaled(n, fx_.get(), rn, z, stream);
   }
   residual(A, z, b, kr_.get(), stream);

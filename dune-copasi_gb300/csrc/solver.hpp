@@ -17,6 +17,7 @@
 #include <string>
 #include <vector>
 
+#include "krylov.cuh"
 #include "model.hpp"
 
 namespace dcgpu {
@@ -105,6 +106,11 @@ class Solver {
   void linear_step(double* x, const std::function<void(const double*, double*)>& res,
                    const std::function<void(const double*)>& jac);
   void setup_preconditioner();
+  static constexpr int kKrylovChunk = 8;   // BiCGSTAB iterations per graph replay
+  cudaGraphExec_t graphs_[4] = {nullptr, nullptr, nullptr, nullptr};  // {fp64, fp32} x {plain, profiled}
+  std::vector<cudaEvent_t> graph_events_;
+  cudaGraphExec_t krylov_graph(bool fp32);
+  int krylov_run(bool fp32, double rel, int max_it, int* iters);
   int bicgstab(const double* b, double* z, double rel_tol, int max_it, int* iters);
   int bicgstab_mixed(const double* b, double* z, double rel_tol, int max_it, int* iters);
   double norm2(const double* v);

@@ -32,7 +32,7 @@ EXPORTED = [
     "dc_state_set", "dc_state_get_species", "dc_state_time", "dc_step", "dc_evolve",
     "dc_assemble", "dc_pattern", "dc_dof_map", "dc_stats", "dc_set_mixed_precision",
     "dc_expr_eval", "dc_stream_handle", "dc_launch_count", "dc_profile_enable", "dc_profile_get",
-    "dc_last_error",
+    "dc_assemble_residual_noalloc", "dc_last_error",
 ]
 
 
@@ -98,6 +98,7 @@ def load_library(path=LIB_PATH):
     lib.dc_stats.argtypes = [vp, P(ctypes.c_int64), P(ctypes.c_int64), P(ctypes.c_int64), P(ctypes.c_int64)]
     lib.dc_set_mixed_precision.argtypes = [vp, ctypes.c_int]
     lib.dc_expr_eval.argtypes = [ctypes.c_char_p, ctypes.c_char_p, P(ctypes.c_char_p), pd, i32, pd]
+    lib.dc_assemble_residual_noalloc.argtypes = [vp, pd, d, d, d, pd]
     lib.dc_stream_handle.argtypes = [vp, P(vp)]
     lib.dc_launch_count.argtypes = []
     lib.dc_profile_enable.argtypes = [vp, ctypes.c_int]
@@ -253,6 +254,16 @@ class Model:
                                      _ptr(r) if r is not None else None,
                                      _ptr(J) if J is not None else None, nj if J is not None else 0))
         return r, J
+
+    def residual_noalloc(self, x, t, cm, ca, out=None):
+        """Residual through the allocation-free entry point (staging in the library's fixed
+        device array; see include/dcgpu.h).  Returns the residual, or raises DcError."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        r = np.empty(self.ndof) if out is None else out
+        st = self._lib.dc_assemble_residual_noalloc(self._h, _ptr(x), float(t), float(cm), float(ca), _ptr(r))
+        if st != DC_OK:
+            raise DcError(st, "dc_assemble_residual_noalloc failed")
+        return r
 
     def pattern(self):
         nr = self.info["n_block_rows"]

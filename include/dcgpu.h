@@ -92,6 +92,19 @@ int dc_evolve(dc_model* model, double t_end, double* dt, dc_callback cb, void* u
  * cm * dM/dx + ca * dA/dx.  r and jac_values may be NULL. */
 int dc_assemble(dc_model* model, const double* x, double t, double cm, double ca, double* r, double* jac_values,
                 size_t n_jac_values);
+/* No counterpart in the reference.  Residual assembly that allocates nothing, for callers
+ * that cannot allocate device memory when they need a residual (their device memory is
+ * owned by another allocator, or cudaMalloc/cudaFree would synchronise the device inside a
+ * latency-bound loop).  Same result as dc_assemble(model, x, t, cm, ca, r, NULL, 0), with
+ * x and r host arrays in the reference DOF order.  The state and residual are staged in a
+ * fixed 16 MiB device array compiled into the library, held by every GPU that loads it:
+ * models with more than 2^20 DOF, or whose compartments carry different species counts,
+ * return DC_ERR_ARGUMENT.  All calls on a device share the array; calls that overlap on
+ * the GPU race.  The first call on each device (with that device current) looks up the
+ * array's address: make it before any stream capture.  Returns a status code only;
+ * dc_last_error() is not updated. */
+int dc_assemble_residual_noalloc(dc_model* model, const double* x, double t, double cm, double ca, double* r);
+
 /* BSR pattern of the Jacobian (block rows = (compartment, vertex) pairs) */
 int dc_pattern(const dc_model* model, int32_t* rowptr, size_t n_rowptr, int32_t* colidx, size_t n_colidx);
 /* map from reference DOF index to padded device index (node * block_size + species) */

@@ -184,9 +184,10 @@ def run_reference(args, rank, world):
 
 
 def spmv_bytes(ndof, nnzb, bs, nrows, vbytes):
-    """Algorithmic bytes of one BSR SpMV: values + block column indices + row pointers +
-    x read once + y written once."""
-    return nnzb * (bs * bs * vbytes + 4) + (nrows + 1) * 4 + 2 * ndof * vbytes
+    """Algorithmic bytes of one fused BiCGSTAB SpMV launch: BSR values + block column
+    indices + row pointers + x read once + y written once + the dot-product partner
+    vector read once."""
+    return nnzb * (bs * bs * vbytes + 4) + (nrows + 1) * 4 + 3 * ndof * vbytes
 
 
 def assembly_bytes(ne, nl, ns, ndof, nnz, jac):

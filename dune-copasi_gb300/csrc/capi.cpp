@@ -323,6 +323,79 @@ int dc_expr_eval(const char* expression, const char* context_ini, const char* co
   });
 }
 
+int dc_server_create(int64_t budget_bytes, int32_t max_active, dc_server** out) {
+  return guarded([&] {
+    if (!out) throw std::invalid_argument("null argument");
+    *out = nullptr;
+    auto s = std::make_unique<dc_server>();
+    s->server = std::make_unique<dcgpu::Server>(budget_bytes, max_active);
+    *out = s.release();
+    return DC_OK;
+  });
+}
+
+int dc_server_submit(dc_server* server, const char* ini_text, const char* overrides, const double* init_state,
+                     size_t n_init, int64_t* request_id) {
+  return guarded([&] {
+    if (!server || !ini_text || !request_id) throw std::invalid_argument("null argument");
+    std::vector<double> init;
+    if (init_state && n_init) init.assign(init_state, init_state + n_init);
+    *request_id = server->server->submit(ini_text, overrides ? overrides : "", std::move(init));
+    return DC_OK;
+  });
+}
+
+int dc_server_poll(dc_server* server, int32_t wait, dc_result* results, int32_t max, int32_t* n_out) {
+  return guarded([&] {
+    if (!server || !n_out || (max > 0 && !results)) throw std::invalid_argument("null argument");
+    auto done = server->server->poll(wait != 0, max);
+    for (size_t i = 0; i < done.size(); ++i) {
+      const auto& r = done[i];
+      dc_result& o = results[i];
+      o.request_id = r.id;
+      o.status = r.status;
+      o.reserved = 0;
+      o.queue_s = r.queue_s;
+      o.run_s = r.run_s;
+      o.latency_s = r.latency_s;
+      o.n_dof = r.ndof;
+      o.newton_iterations = r.newton_iterations;
+      o.linear_iterations = r.linear_iterations;
+      o.steps = r.steps;
+      o.bytes_estimate = r.bytes_estimate;
+      if (r.status != DC_OK && !r.error.empty()) g_last_error = r.error;
+    }
+    *n_out = static_cast<int32_t>(done.size());
+    return DC_OK;
+  });
+}
+
+int dc_server_take_state(dc_server* server, int64_t request_id, double* host_out, size_t n) {
+  return guarded([&] {
+    if (!server || !host_out) throw std::invalid_argument("null argument");
+    std::vector<double> v;
+    if (!server->server->take_state(request_id, v)) throw std::invalid_argument("no state for this request");
+    if (v.size() != n) throw std::invalid_argument("size mismatch");
+    std::memcpy(host_out, v.data(), n * sizeof(double));
+    return DC_OK;
+  });
+}
+
+int dc_server_estimate(const char* ini_text, const char* overrides, int64_t* bytes) {
+  return guarded([&] {
+    if (!ini_text || !bytes) throw std::invalid_argument("null argument");
+    *bytes = dcgpu::Server::estimate_bytes(ini_text, overrides ? overrides : "");
+    return DC_OK;
+  });
+}
+
+int dc_server_destroy(dc_server* server) {
+  return guarded([&] {
+    delete server;
+    return DC_OK;
+  });
+}
+
 int dc_stream_handle(const dc_model* model, void** stream) {
   return guarded([&] {
     if (!model || !stream) throw std::invalid_argument("null argument");

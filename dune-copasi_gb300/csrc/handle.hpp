@@ -4,7 +4,12 @@
 #include <memory>
 
 #include "model.hpp"
+#include "server.hpp"
 #include "solver.hpp"
+
+struct dc_server {
+  std::unique_ptr<dcgpu::Server> server;
+};
 
 struct dc_model {
   std::unique_ptr<dcgpu::Model> model;

@@ -282,8 +282,10 @@ void krylov_iteration(const Bsr& A, const V* vals, const V* dinv, const KrylovVe
   const int64_t n = static_cast<int64_t>(A.nrows) * A.bs;
   const int gn = grid_for(A.nrows);
   count_launches(5);
+  // inside a stream capture an event record becomes a graph node only with the external flag
   auto mark = [&](int i) {
-    if (ev && cudaEventRecord(ev[i], s) != cudaSuccess) throw std::runtime_error("cudaEventRecord failed");
+    if (ev && cudaEventRecordWithFlags(ev[i], s, cudaEventRecordExternal) != cudaSuccess)
+      throw std::runtime_error("cudaEventRecord failed");
   };
 #define DC_KR(B)                                                                                                 \
   case B:                                                                                                        \

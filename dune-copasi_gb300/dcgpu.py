@@ -32,7 +32,8 @@ EXPORTED = [
     "dc_state_set", "dc_state_get_species", "dc_state_time", "dc_step", "dc_evolve",
     "dc_assemble", "dc_pattern", "dc_dof_map", "dc_stats", "dc_set_mixed_precision",
     "dc_expr_eval", "dc_stream_handle", "dc_launch_count", "dc_profile_enable", "dc_profile_get",
-    "dc_assemble_residual_noalloc", "dc_last_error",
+    "dc_assemble_residual_noalloc", "dc_server_create", "dc_server_submit", "dc_server_poll",
+    "dc_server_take_state", "dc_server_estimate", "dc_server_destroy", "dc_last_error",
 ]
 
 
@@ -55,6 +56,14 @@ class StepInfo(ctypes.Structure):
                 ("newton_iterations", ctypes.c_int32), ("linear_iterations", ctypes.c_int32),
                 ("failed_attempts", ctypes.c_int32), ("status", ctypes.c_int32),
                 ("device_ms", ctypes.c_double)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("request_id", ctypes.c_int64), ("status", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("queue_s", ctypes.c_double), ("run_s", ctypes.c_double), ("latency_s", ctypes.c_double),
+                ("n_dof", ctypes.c_int64), ("newton_iterations", ctypes.c_int64),
+                ("linear_iterations", ctypes.c_int64), ("steps", ctypes.c_int64),
+                ("bytes_estimate", ctypes.c_int64)]
 
 
 CALLBACK = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p)
@@ -99,6 +108,12 @@ def load_library(path=LIB_PATH):
     lib.dc_set_mixed_precision.argtypes = [vp, ctypes.c_int]
     lib.dc_expr_eval.argtypes = [ctypes.c_char_p, ctypes.c_char_p, P(ctypes.c_char_p), pd, i32, pd]
     lib.dc_assemble_residual_noalloc.argtypes = [vp, pd, d, d, d, pd]
+    lib.dc_server_create.argtypes = [ctypes.c_int64, i32, P(vp)]
+    lib.dc_server_submit.argtypes = [vp, ctypes.c_char_p, ctypes.c_char_p, pd, sz, P(ctypes.c_int64)]
+    lib.dc_server_poll.argtypes = [vp, i32, P(Result), i32, P(i32)]
+    lib.dc_server_take_state.argtypes = [vp, ctypes.c_int64, pd, sz]
+    lib.dc_server_estimate.argtypes = [ctypes.c_char_p, ctypes.c_char_p, P(ctypes.c_int64)]
+    lib.dc_server_destroy.argtypes = [vp]
     lib.dc_stream_handle.argtypes = [vp, P(vp)]
     lib.dc_launch_count.argtypes = []
     lib.dc_profile_enable.argtypes = [vp, ctypes.c_int]
@@ -320,3 +335,67 @@ class Model:
 
 def launch_count():
     return int(load_library().dc_launch_count())
+
+
+def estimate_bytes(ini, overrides=None):
+    """Device footprint the server's admission control assumes for a request (host only)."""
+    lib = load_library()
+    ov = "\n".join("%s=%s" % (k, v) for k, v in overrides.items()).encode() if overrides else None
+    b = ctypes.c_int64()
+    _check(lib.dc_server_estimate(ini.encode(), ov, ctypes.byref(b)))
+    return b.value
+
+
+class Server:
+    """Request server: admits simulations by device-memory budget and runs them concurrently.
+
+    ``submit`` returns a request id; ``poll`` returns completed results as dicts;
+    ``take_state`` returns the final state of a completed request.
+    """
+
+    def __init__(self, budget_bytes, max_active=4):
+        self._lib = load_library()
+        h = ctypes.c_void_p()
+        _check(self._lib.dc_server_create(int(budget_bytes), int(max_active), ctypes.byref(h)))
+        self._h = h
+        self._ndof = {}
+
+    def submit(self, ini, overrides=None, init=None):
+        ov = "\n".join("%s=%s" % (k, v) for k, v in overrides.items()).encode() if overrides else None
+        rid = ctypes.c_int64()
+        if init is not None:
+            init = np.ascontiguousarray(init, dtype=np.float64)
+            _check(self._lib.dc_server_submit(self._h, ini.encode(), ov, _ptr(init), init.size, ctypes.byref(rid)))
+        else:
+            _check(self._lib.dc_server_submit(self._h, ini.encode(), ov, None, 0, ctypes.byref(rid)))
+        return rid.value
+
+    def poll(self, wait=True, max_results=64):
+        arr = (Result * max_results)()
+        n = ctypes.c_int32()
+        _check(self._lib.dc_server_poll(self._h, 1 if wait else 0, arr, max_results, ctypes.byref(n)))
+        out = []
+        for i in range(n.value):
+            r = {f: getattr(arr[i], f) for f, _ in Result._fields_}
+            self._ndof[r["request_id"]] = r["n_dof"]
+            out.append(r)
+        return out
+
+    def take_state(self, request_id):
+        n = self._ndof.get(request_id)
+        if n is None:
+            raise KeyError(request_id)
+        out = np.empty(n)
+        _check(self._lib.dc_server_take_state(self._h, int(request_id), _ptr(out), out.size))
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _check(self._lib.dc_server_destroy(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

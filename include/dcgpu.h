@@ -135,6 +135,40 @@ int64_t dc_launch_count(void);
 int dc_profile_enable(dc_model* model, int enabled);
 int dc_profile_get(const dc_model* model, double* ms, int64_t* calls, int32_t n_categories);
 
+/* Request server (no counterpart in the reference, which runs one simulation per
+ * process): simulations are submitted as INI text (+ optional initial state in the
+ * reference DOF order) and admitted as soon as their estimated device footprint fits
+ * into `budget_bytes` and one of `max_active` slots is free; admitted requests run
+ * concurrently, each on its own stream, and every result equals the same request run
+ * alone.  The server handle is internally synchronised. */
+typedef struct dc_server dc_server;
+
+typedef struct dc_result {
+  int64_t request_id;
+  int32_t status;       /* DC_OK or the failing status */
+  int32_t reserved;
+  double queue_s;       /* submit -> admission */
+  double run_s;         /* admission -> completion */
+  double latency_s;     /* submit -> completion */
+  int64_t n_dof;
+  int64_t newton_iterations;
+  int64_t linear_iterations;
+  int64_t steps;
+  int64_t bytes_estimate;
+} dc_result;
+
+int dc_server_create(int64_t budget_bytes, int32_t max_active, dc_server** out);
+int dc_server_submit(dc_server* server, const char* ini_text, const char* overrides, const double* init_state,
+                     size_t n_init, int64_t* request_id);
+/* completed results, up to max; wait != 0 blocks until one is available (or none pending) */
+int dc_server_poll(dc_server* server, int32_t wait, dc_result* results, int32_t max, int32_t* n_out);
+/* final state of a completed request (reference DOF order); the server then drops it */
+int dc_server_take_state(dc_server* server, int64_t request_id, double* host_out, size_t n);
+/* footprint estimate used for admission (host only, no GPU needed) */
+int dc_server_estimate(const char* ini_text, const char* overrides, int64_t* bytes);
+/* waits for every submitted request, then frees the server */
+int dc_server_destroy(dc_server* server);
+
 /* message of the last failure on this thread ("" if none) */
 const char* dc_last_error(void);
 

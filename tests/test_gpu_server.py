@@ -1,0 +1,130 @@
+"""Request server: admission by device-memory budget, concurrent execution, and results
+that are identical alone and in the mix."""
+
+import numpy as np
+import pytest
+
+import cases
+
+FAILING_INI = """
+[grid]
+cells = 6 6
+[compartments.domain]
+expression = 1
+[model.scalar_field.u]
+compartment = domain
+initial.expression = 1
+storage.expression = 1
+reaction.expression = log(u - 2)
+reaction.jacobian.u.expression = 1/(u - 2)
+cross_diffusion.u.expression = 0.1
+[model.time_step_operator]
+type = ImplicitEuler
+time_end = 1
+time_step_initial = 0.1
+time_step_min = 0.02
+time_step_max = 0.1
+"""
+
+
+def _requests():
+    out = []
+    for ini, init in (cases.small_heat(n=20, steps=4), cases.small_gray_scott(n=20, steps=3),
+                      cases.small_two_compartment(n=14, steps=3), cases.small_3d(n=4, steps=2)):
+        x0 = None
+        if init is not None:
+            from oracle.model import OracleModel
+            om = OracleModel(ini)
+            x0 = om.initial_state()
+            for sp in om.species:
+                verts = om.comp_vertices[sp.comp]
+                x0[om.dof(sp, verts)] = init(sp.name, om.mesh.coords[verts])
+        out.append((ini, x0))
+    return out
+
+
+def _drain(server, n):
+    results = {}
+    while len(results) < n:
+        for r in server.poll(wait=True):
+            results[r["request_id"]] = r
+    return results
+
+
+def test_estimate_grows_with_problem_size(dcgpu_lib):
+    small = dcgpu_lib.estimate_bytes(cases.small_gray_scott(n=16)[0])
+    large = dcgpu_lib.estimate_bytes(cases.small_gray_scott(n=64)[0])
+    assert 0 < small < large
+    # 16x the cells; the estimate carries a fixed 1 MiB allowance
+    assert (large - (1 << 20)) / (small - (1 << 20)) > 8
+
+
+@pytest.mark.gpu
+def test_results_identical_alone_and_in_the_mix(dcgpu_lib):
+    reqs = _requests()
+    alone = []
+    srv = dcgpu_lib.Server(budget_bytes=8 << 30, max_active=1)
+    for ini, x0 in reqs:
+        rid = srv.submit(ini, init=x0)
+        res = _drain(srv, 1)[rid]
+        assert res["status"] == 0
+        alone.append(srv.take_state(rid))
+    srv.close()
+    srv = dcgpu_lib.Server(budget_bytes=8 << 30, max_active=4)
+    ids = [srv.submit(ini, init=x0) for ini, x0 in reqs]
+    res = _drain(srv, len(ids))
+    for k, rid in enumerate(ids):
+        assert res[rid]["status"] == 0
+        assert res[rid]["latency_s"] >= res[rid]["run_s"] > 0
+        assert res[rid]["newton_iterations"] > 0
+        assert np.array_equal(srv.take_state(rid), alone[k]), k
+    srv.close()
+
+
+@pytest.mark.gpu
+def test_admission_respects_budget(dcgpu_lib):
+    ini, _ = cases.small_heat(n=32, steps=6)
+    est = dcgpu_lib.estimate_bytes(ini)
+    srv = dcgpu_lib.Server(budget_bytes=int(1.5 * est), max_active=4)
+    ids = [srv.submit(ini) for _ in range(3)]
+    res = _drain(srv, 3)
+    spans = []
+    for rid in ids:
+        r = res[rid]
+        assert r["status"] == 0
+        spans.append((r["queue_s"], r["queue_s"] + r["run_s"]))
+    # only one request fits the budget at a time: the admission windows do not overlap
+    spans.sort()
+    for (a0, a1), (b0, b1) in zip(spans, spans[1:]):
+        assert b0 >= a1 - 1e-3
+    srv.close()
+
+
+@pytest.mark.gpu
+def test_oversized_request_rejected(dcgpu_lib):
+    ini, _ = cases.small_heat(n=32, steps=2)
+    srv = dcgpu_lib.Server(budget_bytes=1 << 20, max_active=2)
+    rid = srv.submit(ini)
+    res = _drain(srv, 1)
+    assert res[rid]["status"] == 4
+    srv.close()
+
+
+@pytest.mark.gpu
+def test_failure_is_isolated(dcgpu_lib):
+    good_ini, _ = cases.small_heat(n=16, steps=3)
+    srv = dcgpu_lib.Server(budget_bytes=4 << 30, max_active=1)
+    rid = srv.submit(good_ini)
+    _drain(srv, 1)
+    ref = srv.take_state(rid)
+    srv.close()
+    srv = dcgpu_lib.Server(budget_bytes=4 << 30, max_active=3)
+    a = srv.submit(good_ini)
+    b = srv.submit(FAILING_INI)
+    c = srv.submit(good_ini)
+    res = _drain(srv, 3)
+    assert res[b]["status"] == 2
+    assert res[a]["status"] == 0 and res[c]["status"] == 0
+    assert np.array_equal(srv.take_state(a), ref)
+    assert np.array_equal(srv.take_state(c), ref)
+    srv.close()

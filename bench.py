@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--n", type=int, default=512)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=48,
+                    help="requests of the Poisson serving stream (0 disables the serving measurement)")
     return ap.parse_args()
 
 
@@ -183,6 +185,40 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def run_serving(dcgpu, n_requests, lam, max_active, precision, seed=20261203, budget=64 << 30):
+    """Poisson stream of random requests through the request server; returns latency
+    percentiles and the aggregate DOF x Newton-step throughput."""
+    import workloads as W
+    stream = W.serving_stream(n_requests, lam, seed, n2d=(32, 160), n3d=(12, 32), steps=(10, 40))
+    ov = {"model.time_step_operator.linear_solver.precision": "mixed"} if precision == "mixed" else None
+    srv = dcgpu.Server(budget, max_active)
+    t0 = time.perf_counter()
+    done = {}
+    for arrival, ini in stream:
+        while True:
+            now = time.perf_counter() - t0
+            for r in srv.poll(wait=False):
+                done[r["request_id"]] = r
+            if now >= arrival:
+                break
+            time.sleep(min(arrival - now, 0.002))
+        srv.submit(ini, overrides=ov)
+    while len(done) < len(stream):
+        for r in srv.poll(wait=True):
+            done[r["request_id"]] = r
+    wall = time.perf_counter() - t0
+    srv.close()
+    lat = sorted(r["latency_s"] for r in done.values())
+    ok = sum(1 for r in done.values() if r["status"] == 0)
+    work = sum(r["n_dof"] * r["newton_iterations"] for r in done.values())
+    import numpy as np
+    return {"requests": len(stream), "ok": ok, "lambda_per_s": lam, "max_active": max_active,
+            "precision": precision, "p50_latency_s": float(np.percentile(lat, 50)),
+            "p99_latency_s": float(np.percentile(lat, 99)), "wall_s": wall,
+            "value": work / wall, "unit": METRIC,
+            "mix": "2D N log-U[32,160] / 3D N log-U[12,32], 1-2 compartments, 1-8 species, 10-40 IE steps"}
+
+
 def spmv_bytes(ndof, nnzb, bs, nrows, vbytes):
     """Algorithmic bytes of one fused BiCGSTAB SpMV launch: BSR values + block column
     indices + row pointers + x read once + y written once + the dot-product partner
@@ -314,6 +350,10 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(ini, init)
+    serving = None
+    if args.serve_requests > 0:
+        serving = {"concurrent": run_serving(dcgpu, args.serve_requests, 50.0, 8, args.precision),
+                   "one_at_a_time": run_serving(dcgpu, args.serve_requests, 50.0, 1, args.precision)}
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f64+f32",
@@ -323,7 +363,8 @@ def main():
                        "linear_solver": "BiCGSTAB+block-Jacobi to 1e-13 (direct-solve semantics)",
                        "newton_rel_tol_sq": 1e-10, "l2_flush": "256 MiB write between timed steps",
                        "newton_iterations": newton, "krylov_iterations": linear},
-            "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches}
+            "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
+            "serving": serving}
     if rank == 0:
         print(json.dumps(line), flush=True)
     model.close()

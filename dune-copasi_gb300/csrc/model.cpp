@@ -160,7 +160,10 @@ void Model::build_static_matrices() {
         launch_volume(dim, g.ns, p, g.color_offsets[k], g.color_offsets[k + 1], 2, nullptr);
     }
   }
-  cuda_check(cudaDeviceSynchronize(), "static operator assembly");
+  // Every set-up copy, memset and kernel of the model went to the legacy default stream,
+  // which does not order against the non-blocking streams the solvers run on (and a
+  // pageable cudaMemcpy may return before its DMA lands): wait for all of it here.
+  cuda_check(cudaStreamSynchronize(cudaStreamLegacy), "model set-up");
 }
 
 void Model::build_species() {

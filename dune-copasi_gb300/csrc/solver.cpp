@@ -82,8 +82,8 @@ Solver::Solver(Model& m, cudaStream_t s) : model(m), stream(s) {
   scal_.resize(32);
   counter_.resize(1);
   status_.resize(1);
-  cuda_check(cudaMemset(counter_.get(), 0, sizeof(unsigned int)), "memset");
-  cuda_check(cudaMemset(scal_.get(), 0, 32 * sizeof(double)), "memset");
+  cuda_check(cudaMemsetAsync(counter_.get(), 0, sizeof(unsigned int), stream), "memset");
+  cuda_check(cudaMemsetAsync(scal_.get(), 0, 32 * sizeof(double), stream), "memset");
   cuda_check(cudaMallocHost(&pinned_, 32 * sizeof(double)), "cudaMallocHost");
   rs_.partial = partial_.get();
   rs_.counter = counter_.get();

@@ -218,6 +218,60 @@ def cross_diffusion_3d(n=128, steps=100, dt=0.01, newton_rel=1e-10, seed=SEED, l
     return ini, None
 
 
+def random_request(rng, n2d=(32, 512), n3d=(16, 64), steps=(20, 500), dt=0.05):
+    """One serving request: 2D (N^2 cells) or 3D (N^3 cubes), one or two compartments,
+    1-8 species per compartment, a seeded mass-action network, implicit Euler."""
+    three_d = bool(rng.integers(0, 2))
+    lo, hi = n3d if three_d else n2d
+    n = int(round(np.exp(rng.uniform(np.log(lo), np.log(hi)))))
+    two = bool(rng.integers(0, 2))
+    ns = int(rng.integers(1, 9))
+    nsteps = int(rng.integers(steps[0], steps[1] + 1))
+    dim = 3 if three_d else 2
+    lines = ["[grid]", "dimension = %d" % dim, "cells = " + " ".join([str(n)] * dim), ""]
+    r2 = " + ".join("(position_%s-0.5)^2" % a for a in "xyz"[:dim])
+    if two:
+        lines += ["[compartments]", "inner.expression = (%s) < 0.09" % r2, "outer.expression = (%s) >= 0.09" % r2, ""]
+        comps = [("inner", "a"), ("outer", "b")]
+    else:
+        lines += ["[compartments.domain]", "expression = 1", ""]
+        comps = [("domain", "a")]
+    for comp, prefix in comps:
+        names = ["%s%d" % (prefix, i) for i in range(ns)]
+        net = _mass_action(names, max(1, 2 * ns), rng)
+        for i, s in enumerate(names):
+            lines.append("[model.scalar_field.%s]" % s)
+            lines.append("compartment = %s" % comp)
+            lines.append("storage.expression = 1")
+            lines.append("initial.expression = %.6g" % rng.uniform(0.0, 1.0))
+            lines.append("cross_diffusion.%s.expression = %.17g" % (s, 10.0 ** rng.uniform(-4.0, -2.0)))
+            r, js = net[s]
+            if r != "0":
+                lines.append("reaction.expression = %s" % r)
+                for w, d in js.items():
+                    lines.append("reaction.jacobian.%s.expression = %s" % (w, d))
+            if two:
+                other = ("b" if prefix == "a" else "a") + str(i)
+                tgt = "outer" if comp == "inner" else "inner"
+                lines.append("outflow.%s.expression = 0.5*(%s - %s)" % (tgt, s, other))
+                lines.append("outflow.%s.jacobian.%s.expression = 0.5" % (tgt, s))
+                lines.append("outflow.%s.jacobian.%s.expression = -0.5" % (tgt, other))
+            lines.append("")
+    ini = "\n".join(lines) + "\n" + _tso("ImplicitEuler", dt, dt * nsteps, 1e-10)
+    return ini
+
+
+def serving_stream(n_requests=512, lam=50.0, seed=SEED, **kw):
+    """Poisson arrivals (rate lam per second) of random requests: [(arrival_s, ini)]."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for _ in range(n_requests):
+        t += rng.exponential(1.0 / lam)
+        out.append((t, random_request(rng, **kw)))
+    return out
+
+
 def apply_init(model_like, init, coords_of, setter):
     """Helper: evaluate ``init`` per species on its vertices and hand the values to ``setter``."""
     if init is None:

@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--n", type=int, default=512)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--serve-requests", type=int, default=48,
+    ap.add_argument("--serve-requests", type=int, default=32,
                     help="requests of the Poisson serving stream (0 disables the serving measurement)")
     return ap.parse_args()
 

@@ -15,7 +15,9 @@
 
 namespace dcgpu {
 
-// mode bit 1: residual, bit 2: Jacobian
+// mode bit 1: residual, bit 2: Jacobian; kVolumeNumericalJacobian: Jacobian by forward
+// differences of the residual terms (params.prog / res_terms must be the residual program)
+constexpr int kVolumeNumericalJacobian = 4;
 void launch_volume(int dim, int ns, const VolumeParams& p, int begin, int end, int mode,
                    cudaStream_t stream);
 void launch_faces(int dim, const FaceParams& p, int begin, int end, int mode, cudaStream_t stream);

@@ -401,13 +401,220 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
   }
 }
 
+// Local residual of one element for coefficients c (residual terms only, both forms).
+template <int DIM, int NS>
+__device__ void fd_local_residual(const VolumeParams& P, const double (&c)[DIM + 1][NS], const double (&X)[DIM + 1][DIM],
+                                  const double (&Bm)[DIM][DIM], const double (&G)[DIM + 1][DIM], double adet,
+                                  double vol, double (&rl)[DIM + 1][NS], double* R) {
+  constexpr int NL = DIM + 1;
+  constexpr int NQ = Rule<DIM>::NQ;
+  double g[NS][DIM];
+#pragma unroll
+  for (int s = 0; s < NS; ++s)
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) {
+      double acc = 0.0;
+#pragma unroll
+      for (int a = 0; a < NL; ++a) acc += c[a][s] * G[a][j];
+      g[s][j] = acc;
+    }
+#pragma unroll
+  for (int a = 0; a < NL; ++a)
+#pragma unroll
+    for (int s = 0; s < NS; ++s) rl[a][s] = 0.0;
+#pragma unroll 1
+  for (int q = 0; q < NQ; ++q) {
+    double u[NS];
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+      double acc = 0.0;
+#pragma unroll
+      for (int a = 0; a < NL; ++a) acc += c[a][s] * phi<DIM>(q, a);
+      u[s] = acc;
+    }
+    double xq[DIM];
+#pragma unroll
+    for (int i = 0; i < DIM; ++i) {
+      double acc = X[0][i];
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) acc += Bm[i][j] * Rule<DIM>::xi(q, j);
+      xq[i] = acc;
+    }
+    const double fq = Rule<DIM>::w(q) * adet;
+    for (int i = 0; i < P.prog.ninputs; ++i)
+      R[i] = volume_input<DIM, NS>(P.prog.inputs[i], u, g, xq, P.t, vol, P.species_offset);
+    run_program(P.prog, P.tables, R);
+    const uint8_t* out = P.prog.outputs;
+    double scal[NS], flux[NS][DIM];
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+      scal[s] = 0.0;
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) flux[s][j] = 0.0;
+    }
+    for (int t = 0; t < P.n_res_terms; ++t) {
+      const Term T = P.res_terms[t];
+      const double sc = T.form ? P.ca : P.cm;
+      const double o = R[out[T.out]];
+      double ut = 0.0, gw[DIM];
+#pragma unroll
+      for (int s = 0; s < NS; ++s)
+        if (s == T.test) ut = u[s];
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) {
+        gw[j] = 0.0;
+#pragma unroll
+        for (int s = 0; s < NS; ++s)
+          if (s == T.trial) gw[j] = g[s][j];
+      }
+      double ds = 0.0, df[DIM];
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) df[j] = 0.0;
+      switch (T.kind) {
+        case R_REACTION: ds = -o; break;
+        case R_STORAGE: ds = ut * o; break;
+        case R_VELOCITY:
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) df[j] = R[out[T.out + j]] * ut;
+          break;
+        case R_DIFF_SCALAR:
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) df[j] = -o * gw[j];
+          break;
+        case R_DIFF_TENSOR:
+#pragma unroll
+          for (int i = 0; i < DIM; ++i) {
+            double acc = 0.0;
+#pragma unroll
+            for (int j = 0; j < DIM; ++j) acc += R[out[T.out + i * DIM + j]] * gw[j];
+            df[i] = -acc;
+          }
+          break;
+        default: break;
+      }
+#pragma unroll
+      for (int s = 0; s < NS; ++s)
+        if (s == T.test) {
+          scal[s] += sc * ds;
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) flux[s][j] += sc * df[j];
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < NL; ++a) {
+      const double pa = phi<DIM>(q, a);
+#pragma unroll
+      for (int s = 0; s < NS; ++s) {
+        double fg = 0.0;
+#pragma unroll
+        for (int j = 0; j < DIM; ++j) fg += flux[s][j] * G[a][j];
+        rl[a][s] += (scal[s] * pa - fg) * fq;
+      }
+    }
+  }
+}
+
+// Numerical element Jacobian by forward differences of the local residual,
+// delta = eps (1 + |c|) per local coefficient (local_operator.hh:713-765).
+template <int DIM, int NS>
+__global__ void __launch_bounds__(128) k_volume_fd(const VolumeParams P, const int begin, const int end) {
+  constexpr int NL = DIM + 1;
+  const int k = begin + blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= end) return;
+  int nd[NL];
+  double X[NL][DIM];
+#pragma unroll
+  for (int a = 0; a < NL; ++a) {
+    const int v = P.verts[static_cast<int64_t>(k) * NL + a];
+    nd[a] = P.nodes[static_cast<int64_t>(k) * NL + a];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) X[a][d] = P.coords[static_cast<int64_t>(v) * DIM + d];
+  }
+  double Bm[DIM][DIM], Bi[DIM][DIM], det;
+#pragma unroll
+  for (int i = 0; i < DIM; ++i)
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) Bm[i][j] = X[j + 1][i] - X[0][i];
+  if constexpr (DIM == 2) {
+    det = Bm[0][0] * Bm[1][1] - Bm[0][1] * Bm[1][0];
+    const double id = 1.0 / det;
+    Bi[0][0] = Bm[1][1] * id;  Bi[0][1] = -Bm[0][1] * id;
+    Bi[1][0] = -Bm[1][0] * id; Bi[1][1] = Bm[0][0] * id;
+  } else {
+    const double c00 = Bm[1][1] * Bm[2][2] - Bm[1][2] * Bm[2][1];
+    const double c01 = Bm[1][2] * Bm[2][0] - Bm[1][0] * Bm[2][2];
+    const double c02 = Bm[1][0] * Bm[2][1] - Bm[1][1] * Bm[2][0];
+    det = Bm[0][0] * c00 + Bm[0][1] * c01 + Bm[0][2] * c02;
+    const double id = 1.0 / det;
+    Bi[0][0] = c00 * id;
+    Bi[1][0] = c01 * id;
+    Bi[2][0] = c02 * id;
+    Bi[0][1] = (Bm[0][2] * Bm[2][1] - Bm[0][1] * Bm[2][2]) * id;
+    Bi[1][1] = (Bm[0][0] * Bm[2][2] - Bm[0][2] * Bm[2][0]) * id;
+    Bi[2][1] = (Bm[0][1] * Bm[2][0] - Bm[0][0] * Bm[2][1]) * id;
+    Bi[0][2] = (Bm[0][1] * Bm[1][2] - Bm[0][2] * Bm[1][1]) * id;
+    Bi[1][2] = (Bm[0][2] * Bm[1][0] - Bm[0][0] * Bm[1][2]) * id;
+    Bi[2][2] = (Bm[0][0] * Bm[1][1] - Bm[0][1] * Bm[1][0]) * id;
+  }
+  const double adet = fabs(det);
+  const double vol = adet / (DIM == 2 ? 2.0 : 6.0);
+  double G[NL][DIM];
+#pragma unroll
+  for (int j = 0; j < DIM; ++j) {
+    double s = 0.0;
+#pragma unroll
+    for (int kk = 0; kk < DIM; ++kk) {
+      G[kk + 1][j] = Bi[kk][j];
+      s += Bi[kk][j];
+    }
+    G[0][j] = -s;
+  }
+  const int bs = P.bs, bs2 = bs * bs;
+  double c[NL][NS];
+#pragma unroll
+  for (int a = 0; a < NL; ++a)
+#pragma unroll
+    for (int s = 0; s < NS; ++s) c[a][s] = P.x[static_cast<int64_t>(nd[a]) * bs + s];
+  double R[kMaxDevRegisters];
+  double down[NL][NS], up[NL][NS];
+  fd_local_residual<DIM, NS>(P, c, X, Bm, G, adet, vol, down, R);
+  const int32_t* bp = P.bpos + static_cast<int64_t>(k) * NL * NL;
+#pragma unroll 1
+  for (int b = 0; b < NL; ++b) {
+#pragma unroll 1
+    for (int w = 0; w < NS; ++w) {
+      double cbw = 0.0;
+#pragma unroll
+      for (int bb = 0; bb < NL; ++bb)
+#pragma unroll
+        for (int ww = 0; ww < NS; ++ww)
+          if (bb == b && ww == w) cbw = c[bb][ww];
+      const double delta = P.fd_eps * (1.0 + fabs(cbw));
+      double cp[NL][NS];
+#pragma unroll
+      for (int bb = 0; bb < NL; ++bb)
+#pragma unroll
+        for (int ww = 0; ww < NS; ++ww) cp[bb][ww] = (bb == b && ww == w) ? cbw + delta : c[bb][ww];
+      fd_local_residual<DIM, NS>(P, cp, X, Bm, G, adet, vol, up, R);
+#pragma unroll
+      for (int a = 0; a < NL; ++a)
+#pragma unroll
+        for (int s = 0; s < NS; ++s)
+          P.J[static_cast<int64_t>(bp[a * NL + b]) * bs2 + s * bs + w] += (up[a][s] - down[a][s]) / delta;
+    }
+  }
+}
+
 template <int DIM, int NS>
 void launch_t(const VolumeParams& p, int begin, int end, int mode, cudaStream_t stream) {
   const int n = end - begin;
   if (n <= 0) return;
   const int threads = 128;
   count_launches(1);
-  k_volume<DIM, NS><<<(n + threads - 1) / threads, threads, 0, stream>>>(p, begin, end, mode);
+  if (mode == kVolumeNumericalJacobian)
+    k_volume_fd<DIM, NS><<<(n + threads - 1) / threads, threads, 0, stream>>>(p, begin, end);
+  else
+    k_volume<DIM, NS><<<(n + threads - 1) / threads, threads, 0, stream>>>(p, begin, end, mode);
 }
 
 }  // namespace

@@ -79,6 +79,7 @@ struct VolumeParams {
   int bs;                    // block size
   int species_offset;        // model-global index of local species 0
   double t, cm, ca;          // time, mass-form scale, stiffness-form scale
+  double fd_eps;             // numerical Jacobian: relative perturbation
 };
 
 struct FaceParams {

@@ -1,5 +1,7 @@
 #include "krylov.cuh"
 
+#include "amg.hpp"
+
 #include <stdexcept>
 #include <string>
 
@@ -89,8 +91,9 @@ __global__ void __launch_bounds__(kThreads) k_init(T* x, T* r, T* rhat, T* p, T*
   }
 }
 
-// (1) p = r + beta (p - omega v);  phat = D^-1 p   (one thread per block row)
-template <int B, class T, class V>
+// (1) p = r + beta (p - omega v);  phat = D^-1 p   (one thread per block row; with BJ
+// false the preconditioner is applied by a separate multigrid cycle)
+template <int B, class T, class V, bool BJ>
 __global__ void __launch_bounds__(kThreads) k_update_p(int nrows, T* __restrict__ p, const T* __restrict__ r,
                                                        const T* __restrict__ v, const V* __restrict__ dinv,
                                                        T* __restrict__ phat, const double* sc) {
@@ -105,6 +108,7 @@ __global__ void __launch_bounds__(kThreads) k_update_p(int nrows, T* __restrict_
       pv[i] = static_cast<V>(r[o + i]) + beta * (static_cast<V>(p[o + i]) - omega * static_cast<V>(v[o + i]));
       p[o + i] = static_cast<T>(pv[i]);
     }
+    if (!BJ) continue;
     const V* d = dinv + static_cast<int64_t>(nd) * B * B;
 #pragma unroll
     for (int i = 0; i < B; ++i) {
@@ -159,8 +163,8 @@ __global__ void __launch_bounds__(kThreads) k_spmv_rv(int nrows, const int32_t* 
   }
 }
 
-// (3) s = r - alpha v;  shat = D^-1 s;  ||s||^2
-template <int B, class T, class V>
+// (3) s = r - alpha v;  shat = D^-1 s (when BJ);  ||s||^2
+template <int B, class T, class V, bool BJ>
 __global__ void __launch_bounds__(kThreads) k_update_s(int nrows, T* __restrict__ s, const T* __restrict__ r,
                                                        const T* __restrict__ v, const V* __restrict__ dinv,
                                                        T* __restrict__ shat, ReduceScratch rs, double* sc) {
@@ -178,6 +182,7 @@ __global__ void __launch_bounds__(kThreads) k_update_s(int nrows, T* __restrict_
       s[o + i] = st;
       acc[0] += static_cast<double>(st) * static_cast<double>(st);
     }
+    if (!BJ) continue;
     const V* d = dinv + static_cast<int64_t>(nd) * B * B;
 #pragma unroll
     for (int i = 0; i < B; ++i) {
@@ -278,7 +283,7 @@ void krylov_init(const KrylovVectors<T>& k, int64_t n, double rel, ReduceScratch
 
 template <class T, class V>
 void krylov_iteration(const Bsr& A, const V* vals, const V* dinv, const KrylovVectors<T>& k, ReduceScratch rs,
-                      double* sc, cudaStream_t s, cudaEvent_t* ev) {
+                      double* sc, cudaStream_t s, cudaEvent_t* ev, const Amg* amg) {
   const int64_t n = static_cast<int64_t>(A.nrows) * A.bs;
   const int gn = grid_for(A.nrows);
   count_launches(5);
@@ -289,12 +294,23 @@ void krylov_iteration(const Bsr& A, const V* vals, const V* dinv, const KrylovVe
   };
 #define DC_KR(B)                                                                                                 \
   case B:                                                                                                        \
-    k_update_p<B, T, V><<<gn, kThreads, 0, s>>>(A.nrows, k.p, k.r, k.v, dinv, k.phat, sc);                        \
+    if (amg) {                                                                                                   \
+      k_update_p<B, T, V, false><<<gn, kThreads, 0, s>>>(A.nrows, k.p, k.r, k.v, dinv, k.phat, sc);              \
+      amg->apply<T>(k.p, k.phat, sc, KS_DONE, s);                                                                \
+    } else {                                                                                                     \
+      k_update_p<B, T, V, true><<<gn, kThreads, 0, s>>>(A.nrows, k.p, k.r, k.v, dinv, k.phat, sc);               \
+    }                                                                                                            \
     mark(0);                                                                                                     \
     k_spmv_rv<B, T, V><<<kReduceBlocks, kThreads, 0, s>>>(A.nrows, A.rowptr, A.colidx, vals, k.phat, k.v, k.rhat, \
                                                           rs, sc);                                                \
     mark(1);                                                                                                     \
-    k_update_s<B, T, V><<<kReduceBlocks, kThreads, 0, s>>>(A.nrows, k.s, k.r, k.v, dinv, k.shat, rs, sc);         \
+    if (amg) {                                                                                                   \
+      k_update_s<B, T, V, false><<<kReduceBlocks, kThreads, 0, s>>>(A.nrows, k.s, k.r, k.v, dinv, k.shat, rs,    \
+                                                                    sc);                                         \
+      amg->apply<T>(k.s, k.shat, sc, KS_DONE, s);                                                                \
+    } else {                                                                                                     \
+      k_update_s<B, T, V, true><<<kReduceBlocks, kThreads, 0, s>>>(A.nrows, k.s, k.r, k.v, dinv, k.shat, rs, sc); \
+    }                                                                                                            \
     mark(2);                                                                                                     \
     k_spmv_omega<B, T, V><<<kReduceBlocks, kThreads, 0, s>>>(A.nrows, A.rowptr, A.colidx, vals, k.shat, k.t, k.s, \
                                                              rs, sc);                                             \
@@ -311,8 +327,8 @@ void krylov_iteration(const Bsr& A, const V* vals, const V* dinv, const KrylovVe
 template void krylov_init<double>(const KrylovVectors<double>&, int64_t, double, ReduceScratch, double*, cudaStream_t);
 template void krylov_init<float>(const KrylovVectors<float>&, int64_t, double, ReduceScratch, double*, cudaStream_t);
 template void krylov_iteration<double, double>(const Bsr&, const double*, const double*, const KrylovVectors<double>&,
-                                               ReduceScratch, double*, cudaStream_t, cudaEvent_t*);
+                                               ReduceScratch, double*, cudaStream_t, cudaEvent_t*, const Amg*);
 template void krylov_iteration<float, float>(const Bsr&, const float*, const float*, const KrylovVectors<float>&,
-                                             ReduceScratch, double*, cudaStream_t, cudaEvent_t*);
+                                             ReduceScratch, double*, cudaStream_t, cudaEvent_t*, const Amg*);
 
 }  // namespace dcgpu

@@ -240,8 +240,7 @@ void Model::build_species() {
   if (jt != "analytical" && jt != "numerical")
     throw ConfigError("The option 'model.jacobian.type' must be either 'analytical' or 'numerical'");
   numerical_jacobian = (jt == "numerical") && !is_linear;
-  if (numerical_jacobian)
-    throw ConfigError("model.jacobian.type = numerical is not supported by the GPU engine");
+  fd_eps = mcfg.get_double("jacobian.epsilon", 1e-7);
   if (cfg.has_sub("model.domain.deformation") || mcfg.has_sub("domain"))
     if (mcfg.sub("domain").has_sub("deformation"))
       throw ConfigError("model.domain.deformation is not supported by the GPU engine");
@@ -743,6 +742,8 @@ void Model::build_face_groups() {
         }
   }
   if (!any) return;
+  if (numerical_jacobian)
+    throw ConfigError("model.jacobian.type = numerical together with outflow terms is not supported");
   Faces F = compute_faces(mesh);
   const int nl = dim + 1;
   // group key: (c_in, c_out, boundary)
@@ -973,6 +974,19 @@ void Model::assemble(const double* x, double t, double cm, double ca, double* r,
     p.t = t;
     p.cm = cm;
     p.ca = ca;
+    p.fd_eps = fd_eps;
+    if (numerical_jacobian && (mode & 2)) {
+      // jacobian.type = numerical: residual pass (if asked) + finite-difference Jacobian pass,
+      // both with the residual program and terms
+      p.prog = g.prog_res.view();
+      p.res_terms = g.d_res_r.get();
+      p.n_res_terms = static_cast<int>(g.res_terms_r.size());
+      for (size_t k = 0; k + 1 < g.color_offsets.size(); ++k) {
+        if (mode & 1) launch_volume(dim, g.ns, p, g.color_offsets[k], g.color_offsets[k + 1], 1, s);
+        if (J) launch_volume(dim, g.ns, p, g.color_offsets[k], g.color_offsets[k + 1], kVolumeNumericalJacobian, s);
+      }
+      continue;
+    }
     for (size_t k = 0; k + 1 < g.color_offsets.size(); ++k)
       launch_volume(dim, g.ns, p, g.color_offsets[k], g.color_offsets[k + 1], mode, s);
   }

@@ -133,6 +133,7 @@ class Model {
   std::vector<int> species_offset;              // global index of the first species of each compartment
   bool is_linear = false;
   bool numerical_jacobian = false;
+  double fd_eps = 1e-7;
   int bs = 1;
 
   // block rows

@@ -117,6 +117,19 @@ Solver::Solver(Model& m, cudaStream_t s) : model(m), stream(s) {
   }
   if (lin_direct_) lin_max_it_ = std::max(lin_max_it_, 5000);
   precond_ = ls.get("preconditioner.type", "Jacobi");
+  // every dune-istl preconditioner of the reference's registry (Richardson, Jacobi, SSOR,
+  // SOR, GaussSeidel, BlockJacobi, ILU variants) maps to block Jacobi on the device; "AMG"
+  // selects the aggregation multigrid V-cycle
+  use_amg_ = (precond_ == "AMG");
+  if (use_amg_) {
+    std::vector<int32_t> group(m.nnodes, 0);
+    for (size_t c = 0; c < m.comp_names.size(); ++c)
+      for (int64_t k = m.comp_node_offset[c]; k < m.comp_node_offset[c + 1]; ++k) group[k] = static_cast<int32_t>(c);
+    amg_.omega = ls.get_double("preconditioner.relaxation", 0.8);
+    amg_.coarse_sweeps = static_cast<int>(ls.get_long("preconditioner.coarse_sweeps", 6));
+    amg_.build(m.rowptr, m.colidx, m.diag, group, m.bs, static_cast<int>(ls.get_long("preconditioner.max_level", 10)),
+               static_cast<int>(ls.get_long("preconditioner.coarsen_target", 256)));
+  }
   const bool want_mixed = ls.get("precision", "double") == "mixed";
   dec_ = tso.get_double("time_step_decrease_factor", 0.5);
   inc_ = tso.get_double("time_step_increase_factor", 1.1);
@@ -241,6 +254,12 @@ void Solver::setup_preconditioner() {
     to_float(static_cast<int64_t>(model.nnzb()) * model.bs * model.bs, J_.get(), J32_.get(), stream);
     to_float(static_cast<int64_t>(model.nnodes) * model.bs * model.bs, dinv_.get(), fdinv_.get(), stream);
   }
+  if (use_amg_) {
+    amg_.setup(J_.get(), dinv_.get(), J32_.get(), fdinv_.get(), mixed_precision, status_.get(), stream);
+    cuda_check(cudaMemcpyAsync(&st, status_.get(), sizeof(int), cudaMemcpyDeviceToHost, stream), "status");
+    cuda_check(cudaStreamSynchronize(stream), "status");
+    if (st) throw StepFailure("singular diagonal block in a coarse multigrid level");
+  }
 }
 
 // Graph of kKrylovChunk BiCGSTAB iterations on this solver's fixed workspace (fp64 or
@@ -266,11 +285,11 @@ cudaGraphExec_t Solver::krylov_graph(bool fp32) {
     if (fp32) {
       KrylovVectors<float> kv{fx_.get(), fr_.get(), frhat_.get(), fp_.get(), fv_.get(), fs_.get(), ft_.get(),
                               fphat_.get(), fshat_.get()};
-      krylov_iteration<float, float>(A, J32_.get(), fdinv_.get(), kv, rs_, sc, stream, e);
+      krylov_iteration<float, float>(A, J32_.get(), fdinv_.get(), kv, rs_, sc, stream, e, use_amg_ ? &amg_ : nullptr);
     } else {
       KrylovVectors<double> kv{kx_.get(), kr_.get(), krhat_.get(), kp_.get(), kv_.get(), ks_.get(), kt_.get(),
                                kphat_.get(), kshat_.get()};
-      krylov_iteration<double, double>(A, J_.get(), dinv_.get(), kv, rs_, sc, stream, e);
+      krylov_iteration<double, double>(A, J_.get(), dinv_.get(), kv, rs_, sc, stream, e, use_amg_ ? &amg_ : nullptr);
     }
   }
   cuda_check(cudaStreamEndCapture(stream, &g), "cudaStreamEndCapture");
@@ -505,15 +524,19 @@ int Solver::do_step(double& dt, double* dt_used) {
     return true;
   };
   if (!check(dt)) return DC_ERR_DT_MIN;
+  // Without time_step_min the reference keeps halving until dt underflows; here a step
+  // gives up after kMaxRejections consecutive rejections (dt reduced by dec^60 ~ 1e-18).
+  constexpr int kMaxRejections = 60;
+  int rejections = 0;
   while (true) {
     try {
       one_step(dt);
       break;
     } catch (const StepFailure&) {
       ++stats.failed_steps;
-      // restore the state of the step's start (x_ is only overwritten on success)
+      // the state of the step's start is kept (x_ is only overwritten on success)
       dt = dt * dec_;
-      if (!check(dt)) return DC_ERR_DT_MIN;
+      if (!check(dt) || ++rejections >= kMaxRejections || dt == 0.0) return DC_ERR_DT_MIN;
     }
   }
   if (dt_used) *dt_used = dt;

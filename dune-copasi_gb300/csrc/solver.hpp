@@ -17,6 +17,7 @@
 #include <string>
 #include <vector>
 
+#include "amg.hpp"
 #include "krylov.cuh"
 #include "model.hpp"
 
@@ -152,6 +153,8 @@ class Solver {
   bool lin_direct_ = true;
   int lin_max_it_ = 500;
   std::string precond_ = "Jacobi";
+  bool use_amg_ = false;
+  Amg amg_;
   double dec_ = 0.5, inc_ = 1.1;
   bool has_min_ = false, has_max_ = false;
   double dt_min_ = 0.0, dt_max_ = 0.0;

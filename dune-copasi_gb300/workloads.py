@@ -26,13 +26,15 @@ import numpy as np
 SEED = 20261203
 
 
-def _tso(scheme, dt, t_end, newton_rel=None, linear="UMFPack", extra=""):
+def _tso(scheme, dt, t_end, newton_rel=None, linear="UMFPack", extra="", dt_min=None):
     s = ["[model.time_step_operator]",
          "type = %s" % scheme,
          "time_begin = 0",
          "time_end = %r" % t_end,
          "time_step_initial = %r" % dt,
          "time_step_max = %r" % dt]
+    if dt_min is not None:
+        s.append("time_step_min = %r" % dt_min)
     s.append("[model.time_step_operator.linear_solver]")
     s.append("type = %s" % linear)
     if newton_rel is not None:
@@ -107,15 +109,27 @@ cross_diffusion.v.expression = 1e-5
     return ini, init
 
 
-def _mass_action(names, n_reactions, rng):
-    """Random mass-action network: returns {species: (rate expr, {wrt: jac expr})}."""
+def _mass_action(names, n_reactions, rng, dissipative=False):
+    """Random mass-action network: returns {species: (rate expr, {wrt: jac expr})}.
+
+    Reactions have one or two reactants and one or two products. With ``dissipative``
+    a reaction has no more products than reactants and none of them is a reactant, so the
+    total amount never grows (no autocatalysis, no finite-time blow-up).
+    """
     terms = {s: [] for s in names}
     jac = {s: {} for s in names}
     for _ in range(n_reactions):
-        nre = int(rng.integers(1, 3))
-        npr = int(rng.integers(1, 3))
-        re = list(rng.choice(len(names), size=nre, replace=True))
-        pr = list(rng.choice(len(names), size=npr, replace=True))
+        if dissipative:
+            nre = int(rng.integers(1, 3)) if len(names) > 1 else 1
+            re = list(rng.choice(len(names), size=nre, replace=True))
+            others = [i for i in range(len(names)) if i not in re]
+            npr = min(int(rng.integers(0, nre + 1)), len(others))
+            pr = list(rng.choice(others, size=npr, replace=True)) if npr else []
+        else:
+            nre = int(rng.integers(1, 3))
+            npr = int(rng.integers(1, 3))
+            re = list(rng.choice(len(names), size=nre, replace=True))
+            pr = list(rng.choice(len(names), size=npr, replace=True))
         k = float(10.0 ** rng.uniform(-2.0, 1.0))
         kk = "%.17g" % k
         # rate = k * prod(reactants)
@@ -218,7 +232,7 @@ def cross_diffusion_3d(n=128, steps=100, dt=0.01, newton_rel=1e-10, seed=SEED, l
     return ini, None
 
 
-def random_request(rng, n2d=(32, 512), n3d=(16, 64), steps=(20, 500), dt=0.05):
+def random_request(rng, n2d=(32, 256), n3d=(16, 40), steps=(10, 100), dt=0.05):
     """One serving request: 2D (N^2 cells) or 3D (N^3 cubes), one or two compartments,
     1-8 species per compartment, a seeded mass-action network, implicit Euler."""
     three_d = bool(rng.integers(0, 2))
@@ -238,7 +252,7 @@ def random_request(rng, n2d=(32, 512), n3d=(16, 64), steps=(20, 500), dt=0.05):
         comps = [("domain", "a")]
     for comp, prefix in comps:
         names = ["%s%d" % (prefix, i) for i in range(ns)]
-        net = _mass_action(names, max(1, 2 * ns), rng)
+        net = _mass_action(names, max(1, 2 * ns), rng, dissipative=True)
         for i, s in enumerate(names):
             lines.append("[model.scalar_field.%s]" % s)
             lines.append("compartment = %s" % comp)
@@ -257,7 +271,7 @@ def random_request(rng, n2d=(32, 512), n3d=(16, 64), steps=(20, 500), dt=0.05):
                 lines.append("outflow.%s.jacobian.%s.expression = 0.5" % (tgt, s))
                 lines.append("outflow.%s.jacobian.%s.expression = -0.5" % (tgt, other))
             lines.append("")
-    ini = "\n".join(lines) + "\n" + _tso("ImplicitEuler", dt, dt * nsteps, 1e-10)
+    ini = "\n".join(lines) + "\n" + _tso("ImplicitEuler", dt, dt * nsteps, 1e-10, dt_min=dt * 1e-3)
     return ini
 
 

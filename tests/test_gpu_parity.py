@@ -142,6 +142,35 @@ def test_mixed_precision_matches_oracle(dcgpu_lib, case):
         assert abs(n_o - n_g) <= max(1, stages)
 
 
+@pytest.mark.parametrize("case", ["gray_scott", "two_compartment", "cross_diffusion_3d", "features_3d_padded"])
+@pytest.mark.parametrize("mixed", [False, True])
+def test_multigrid_preconditioner_matches_oracle(dcgpu_lib, case, mixed):
+    """Aggregation multigrid V-cycle as the BiCGSTAB preconditioner (fp64, and fp32 inside
+    fp64 refinement): same 1e-8 tolerance against the oracle's direct solves."""
+    ini, init = ALL_CASES[case]()
+    ov = {"model.time_step_operator.linear_solver.preconditioner.type": "AMG",
+          "model.time_step_operator.linear_solver.preconditioner.coarsen_target": "16"}
+    records = _run_both(dcgpu_lib, ini, init, mixed=mixed, overrides=ov)
+    for t, errs, n_o, n_g, stages in records:
+        for name, e in errs.items():
+            assert e <= STEP_TOL, (case, t, name, e)
+        assert abs(n_o - n_g) <= max(1, stages)
+
+
+@pytest.mark.parametrize("case", ["gray_scott", "cross_diffusion_3d"])
+def test_numerical_jacobian_matches_oracle(dcgpu_lib, case):
+    """model.jacobian.type = numerical: element-local forward differences with
+    delta = eps (1 + |c|) (local_operator.hh:713-765) on both sides."""
+    ini, init = ALL_CASES[case]()
+    ov = {"model.jacobian.type": "numerical",
+          "model.time_step_operator.nonlinear_solver.convergence_condition.relative_tolerance": "1e-20"}
+    records = _run_both(dcgpu_lib, ini, init, overrides=ov)
+    for t, errs, n_o, n_g, stages in records:
+        for name, e in errs.items():
+            assert e <= STEP_TOL, (case, t, name, e)
+        assert abs(n_o - n_g) <= max(1, stages)
+
+
 def test_linear_model_defect_correction(dcgpu_lib):
     """is_linear = true: one defect-correction solve per stage (make_step_operator.hh:210-245)."""
     import test_oracle as T

@@ -3,7 +3,8 @@
 Workload (the configuration the headline metric is quoted on): seeded Gray-Scott,
 2 species, unit square 512 x 512 P1 triangles (526,338 DOF), Alexander2 DIRK dt = 1,
 Newton relative tolerance 1e-10 (squared l2, as the reference), direct-solve semantics
-(the reference's default UMFPack is replaced by BiCGSTAB converged to 1e-13).
+(the reference's default UMFPack is replaced by BiCGSTAB converged to a relative
+residual of 1e-10).
 
 A "step" is one Alexander2 time step (2 stages x Newton iterations).  Timed per step with
 CUDA events on the engine's stream (dc_step_info.device_ms); the L2 cache is flushed
@@ -44,8 +45,12 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=512)
+    ap.add_argument("--workload", default="gray_scott", choices=["gray_scott", "cross_diffusion_3d"],
+                    help="gray_scott (headline, n = grid edge) or cross_diffusion_3d (n = cube edge)")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--large-n", type=int, default=128,
+                    help="cube edge of the HBM-resident SpMV measurement (0 disables it)")
     ap.add_argument("--serve-requests", type=int, default=32,
                     help="requests of the Poisson serving stream (0 disables the serving measurement)")
     return ap.parse_args()
@@ -61,24 +66,35 @@ def dist_setup(args):
     return rank, world
 
 
-def make_workload(n):
+def make_workload(n, kind="gray_scott"):
+    """(ini, init, dt, description) of the bench workload; gray_scott is the headline one."""
     import workloads as W
-    return W.gray_scott(n=n, steps=100000, dt=1.0)
+    if kind == "cross_diffusion_3d":
+        ini, init = W.cross_diffusion_3d(n=n, steps=100000, dt=0.01)
+        return ini, init, 0.01, {"workload": "cross_diffusion_3d_%d^3x6_p1_tets_alexander2_dt0.01" % n,
+                                 "mesh": "%d^3 cubes x 6 P1 tetrahedra" % n, "species": 3, "nl": 4}
+    ini, init = W.gray_scott(n=n, steps=100000, dt=1.0)
+    name = WORKLOAD if n == 512 else "gray_scott_%dx%d_p1_alexander2_dt1" % (n, n)
+    return ini, init, 1.0, {"workload": name, "mesh": "%dx%d P1 triangles" % (n, n), "species": 2, "nl": 3}
 
 
-def initial_vector(ini, init):
-    """Seeded initial state in the reference DOF order (built with the oracle's layout rules,
-    which the engine shares: compartment-major, vertex-major, species interleaved)."""
-    import numpy as np
-    from oracle.mesh import Mesh
-    from oracle.ini import ParameterTree
-    cfg = ParameterTree.from_text(ini)
-    mesh = Mesh.from_config(cfg.sub("grid"))
-    nv = mesh.nv
-    x = np.empty(2 * nv)
-    x[0::2] = init("u", mesh.coords)
-    x[1::2] = init("v", mesh.coords)
+def initial_vector(om, init):
+    """Seeded initial state in the reference DOF order for the CPU legs, from the oracle
+    model `om` (the GPU arm builds the same vector from its own model, Model.seeded_state)."""
+    x = om.initial_state()
+    for sp in (om.species if init is not None else []):
+        verts = om.comp_vertices[sp.comp]
+        x[om.dof(sp, verts)] = init(sp.name, om.mesh.coords[verts])
     return x
+
+
+def oracle_newton_iteration(om, x, dt):
+    """The work of one Newton iteration of an Alexander2 stage on the CPU oracle:
+    residual and Jacobian of M + gamma dt A at x, direct (SuperLU) solve, update."""
+    a = (1.0 - 0.5 * 2 ** 0.5) * dt
+    r = om.residual(x, 0.0, "mass") + a * om.residual(x, 0.0, "stiffness")
+    J = om.jacobian(x, 0.0, "mass") + a * om.jacobian(x, 0.0, "stiffness")
+    return x - om._solve(J, r)
 
 
 class ClockSampler:
@@ -134,41 +150,33 @@ class ClockSampler:
         return out
 
 
-def cpu_baseline(ini, init, newton_steps=1):
+def cpu_baseline(ini, init, dt, wdesc, newton_steps=1):
     """Oracle (numpy assembly + SuperLU) on the host: one Newton iteration of the full workload."""
-    import numpy as np
     from oracle.model import OracleModel
     om = OracleModel(ini)
-    x0 = initial_vector(ini, init)
-    a = 1.0 - 0.5 * 2 ** 0.5
+    x0 = initial_vector(om, init)
     t0 = time.perf_counter()
     for _ in range(newton_steps):
-        r = om.residual(x0, a, "mass") + a * om.residual(x0, a, "stiffness")
-        J = om.jacobian(x0, a, "mass") + a * om.jacobian(x0, a, "stiffness")
-        z = om._solve(J, r)
-        x0 = x0 - z
+        x0 = oracle_newton_iteration(om, x0, dt)
     dt = time.perf_counter() - t0
     return {"value": om.ndof * newton_steps / dt, "unit": METRIC, "cores": 1, "kind": "port",
             "sample": "%d Newton iteration(s) (residual + Jacobian assembly + SuperLU solve) of the "
-                      "%d-DOF Gray-Scott stage system, first Alexander2 stage" % (newton_steps, om.ndof),
+                      "%d-DOF %s stage system, first Alexander2 stage"
+                      % (newton_steps, om.ndof, wdesc["workload"]),
             "seconds": dt}
 
 
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    ini, init = make_workload(args.n)
+    ini, init, dt0, wdesc = make_workload(args.n, args.workload)
     from oracle.model import OracleModel
     om = OracleModel(ini)
-    x = initial_vector(ini, init)
-    a = 1.0 - 0.5 * 2 ** 0.5
+    x = initial_vector(om, init)
     times = []
     for k in range(args.warmup + args.steps):
         t0 = time.perf_counter()
-        r = om.residual(x, a, "mass") + a * om.residual(x, a, "stiffness")
-        J = om.jacobian(x, a, "mass") + a * om.jacobian(x, a, "stiffness")
-        z = om._solve(J, r)
-        x = x - z
+        x = oracle_newton_iteration(om, x, dt0)
         t1 = time.perf_counter()
         if k >= args.warmup:
             times.append(t1 - t0)
@@ -177,8 +185,9 @@ def run_reference(args, rank, world):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / len(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded Gray-Scott initial perturbation)",
-            "config": {"workload": WORKLOAD, "dof": om.ndof, "step": "one Newton iteration (assembly + SuperLU)"},
+            "data": "synthetic (seeded initial state)",
+            "config": {"workload": wdesc["workload"], "dof": om.ndof,
+                       "step": "one Newton iteration (assembly + SuperLU)"},
             "cpu_baseline": {"value": value, "unit": METRIC, "cores": 1, "kind": "port",
                              "sample": "one Newton iteration of the full workload per step"},
             "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -219,6 +228,37 @@ def run_serving(dcgpu, n_requests, lam, max_active, precision, seed=20261203, bu
             "mix": "2D N log-U[32,160] / 3D N log-U[12,32], 1-2 compartments, 1-8 species, 10-40 IE steps"}
 
 
+def large_spmv(dcgpu, precision, peak_gbs, n=128):
+    """SpMV roofline on an operator far larger than L2: the 3D cross-diffusion workload
+    (n^3 cubes x 6 tetrahedra, 3 species, ~6.4 M DOF at n = 128), one Alexander2 step with
+    per-kernel events; returns the fused-SpMV achieved bandwidth against the HBM peak."""
+    import workloads as W
+    ini, init = W.cross_diffusion_3d(n=n, steps=1, dt=0.01)
+    m = dcgpu.Model(ini)
+    if precision == "mixed":
+        m.set_mixed_precision(True)
+    m.set_state(m.seeded_state(init), 0.0)
+    m.step(0.01)  # first step: tuner, graphs
+    m.profile(True)
+    info = m.step(0.01)
+    kt = m.kernel_times()
+    m.profile(False)
+    fmt = m.spmv_format()
+    mi = m.info
+    ms, calls = kt["spmv"]
+    vb = 4 if precision == "mixed" else 8
+    alg = spmv_bytes(mi["n_dof"], mi["n_blocks"], mi["block_size"], mi["n_block_rows"], vb)
+    avg = ms * 1e-3 / max(calls, 1)
+    ach = alg / avg / 1e9 if avg > 0 else 0.0
+    m.close()
+    return {"workload": "cross_diffusion_3d_%d^3x6_tets_3_species" % n, "dof": mi["n_dof"],
+            "blocks": mi["n_blocks"], "block_size": mi["block_size"], "precision": precision,
+            "spmv_layout": fmt["format"], "tuner_us": {"bsr": fmt["bsr_us"], "sell": fmt["sell_us"]},
+            "algorithmic_bytes_per_launch": alg, "avg_launch_us": avg * 1e6, "launches": calls,
+            "achieved": ach, "peak": peak_gbs, "unit": "GB/s", "frac": ach / peak_gbs,
+            "newton_iterations": info["newton_iterations"], "krylov_iterations": info["linear_iterations"]}
+
+
 def spmv_bytes(ndof, nnzb, bs, nrows, vbytes):
     """Algorithmic bytes of one fused BiCGSTAB SpMV launch: BSR values + block column
     indices + row pointers + x read once + y written once + the dot-product partner
@@ -253,23 +293,22 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("gloo")
 
-    ini, init = make_workload(args.n)
+    ini, init, dt0, wdesc = make_workload(args.n, args.workload)
     model = dcgpu.Model(ini)
     if args.precision == "mixed":
         model.set_mixed_precision(True)
-    x0 = initial_vector(ini, init)
+    x0 = model.seeded_state(init)
     ndof = model.ndof
     model.set_state(x0, 0.0)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
 
-    dt = 1.0
+    dt = dt0
     for _ in range(args.warmup):
         dt = model.step(dt)["dt_next"]
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
 
-    model.profile(True)
     clocks = ClockSampler()
     clocks.start()
     launches0 = dcgpu.launch_count()
@@ -287,9 +326,19 @@ def main():
     launches = dcgpu.launch_count() - launches0
     torch.cuda.synchronize()
     clk = clocks.stop()
+    total_ms = sum(dev_ms)
+
+    # per-category kernel times from a second pass of the same number of steps with
+    # events around each kernel group (kept out of the timed pass above)
+    model.profile(True)
+    prof_dt = dt
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        prof_dt = model.step(prof_dt)["dt_next"]
+    torch.cuda.synchronize()
     kt = model.kernel_times()
     model.profile(False)
-    total_ms = sum(dev_ms)
     if dist:
         t = torch.tensor([total_ms], dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -332,24 +381,31 @@ def main():
     for name, (ms, calls) in kt.items():
         if calls:
             cats[name] = (ms, calls)
+    def cat_roof(name):
+        ms, calls = cats.get(name, (0.0, 1))
+        avg_s = ms * 1e-3 / max(calls, 1)
+        if name == "spmv":
+            alg = spmv_bytes(ndof, nnzb, bs, nrows, vbytes)
+        elif name == "assembly":
+            alg = assembly_bytes(ne, wdesc["nl"], wdesc["species"], ndof, nnzb * bs * bs, jac=True)
+        else:
+            alg = nrows * bs * bs * vbytes + 2 * ndof * vbytes
+        achieved = alg / avg_s / 1e9 if avg_s > 0 else 0.0
+        return {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": peak_gbs, "unit": "GB/s",
+                "frac": achieved / peak_gbs, "peak_source": peak_src, "traffic": None,
+                "algorithmic_bytes_per_launch": alg, "avg_launch_us": avg_s * 1e6, "launches": calls}
+
     dom = max(cats, key=lambda k: cats[k][0]) if cats else "spmv"
-    ms, calls = cats.get(dom, (0.0, 1))
-    avg_s = ms * 1e-3 / max(calls, 1)
-    if dom == "spmv":
-        alg = spmv_bytes(ndof, nnzb, bs, nrows, vbytes)
-    elif dom == "assembly":
-        alg = assembly_bytes(ne, 3, 2, ndof, nnzb * bs * bs, jac=True)
-    else:
-        alg = nrows * bs * bs * vbytes + 2 * ndof * vbytes
-    achieved = alg / avg_s / 1e9 if avg_s > 0 else 0.0
-    roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak_gbs, "unit": "GB/s",
-            "frac": achieved / peak_gbs, "peak_source": peak_src, "traffic": None,
-            "algorithmic_bytes_per_launch": alg, "avg_launch_us": avg_s * 1e6, "launches": calls,
-            "category_ms": {k: v[0] for k, v in cats.items()},
-            "category_launches": {k: v[1] for k, v in cats.items()}}
+    roof = cat_roof(dom)
+    roof["category_ms"] = {k: v[0] for k, v in cats.items()}
+    roof["category_launches"] = {k: v[1] for k, v in cats.items()}
+    roof["by_category"] = {k: cat_roof(k) for k in cats}
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(ini, init)
+        cpu = cpu_baseline(ini, init, dt0, wdesc)
+    roof["spmv_layout"] = model.spmv_format()
+    if args.large_n > 0:
+        roof["spmv_hbm_resident"] = large_spmv(dcgpu, args.precision, peak_gbs, args.large_n)
     serving = None
     if args.serve_requests > 0:
         serving = {"concurrent": run_serving(dcgpu, args.serve_requests, 50.0, 8, args.precision),
@@ -357,10 +413,11 @@ def main():
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f64+f32",
-            "data": "synthetic (seeded Gray-Scott initial perturbation, no dataset)",
-            "config": {"workload": WORKLOAD, "mesh": "%dx%d P1 triangles" % (args.n, args.n), "dof": ndof,
-                       "species": 2, "scheme": "Alexander2", "dt": 1.0, "precision": args.precision,
-                       "linear_solver": "BiCGSTAB+block-Jacobi to 1e-13 (direct-solve semantics)",
+            "data": "synthetic (seeded initial state, no dataset)",
+            "config": {"workload": wdesc["workload"], "mesh": wdesc["mesh"], "dof": ndof,
+                       "species": wdesc["species"], "scheme": "Alexander2", "dt": dt0, "precision": args.precision,
+                       "linear_solver": "BiCGSTAB+block-Jacobi to 1e-10 (direct-solve semantics)",
+                       "spmv_layout": model.spmv_format()["format"],
                        "newton_rel_tol_sq": 1e-10, "l2_flush": "256 MiB write between timed steps",
                        "newton_iterations": newton, "krylov_iterations": linear},
             "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,

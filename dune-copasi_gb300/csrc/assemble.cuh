@@ -25,5 +25,14 @@ void launch_faces(int dim, const FaceParams& p, int begin, int end, int mode, cu
 // with fewer species than the block size)
 void launch_pad_identity(const int32_t* diag, const int8_t* row_ns, int nrows, int bs, double* J,
                          double value, cudaStream_t stream);
+// constrained entries idx[0..n) (blocked vector index): op 0 sets v[idx] = val, op 1 zeroes them
+void launch_constraints(double* v, const int64_t* idx, const double* val, int64_t n, int op, cudaStream_t stream);
+struct ConstraintRows {
+  const int32_t* rowptr;
+  const int32_t* diag;
+};
+// the constrained rows of the BSR Jacobian become unit rows
+void launch_constraint_rows(double* J, const ConstraintRows& cr, const int64_t* idx, int64_t n, int bs,
+                            cudaStream_t stream);
 
 }  // namespace dcgpu

@@ -231,7 +231,42 @@ __global__ void k_pad_identity(const int32_t* diag, const int8_t* row_ns, int nr
   for (int s = row_ns[i]; s < bs; ++s) J[base + s * bs + s] += value;
 }
 
+// constrained entries (blocked index idx[k]): op 0 sets v[idx] = val, op 1 zeroes v[idx]
+__global__ void k_constraints(double* v, const int64_t* __restrict__ idx, const double* __restrict__ val, int64_t n,
+                              int op) {
+  const int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  v[idx[k]] = op == 0 ? val[k] : 0.0;
+}
+
+// constrained Jacobian rows become unit rows: a thread per constraint clears scalar row i
+// of block row br in every block of the row and puts 1 on the diagonal.  Constraints in
+// one block row have different i, so no two threads write the same entry.
+__global__ void k_constraint_rows(double* J, ConstraintRows cr, const int64_t* __restrict__ idx, int64_t n, int bs) {
+  const int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int64_t br = idx[k] / bs;
+  const int i = static_cast<int>(idx[k] % bs);
+  const int64_t bs2 = static_cast<int64_t>(bs) * bs;
+  for (int32_t b = cr.rowptr[br]; b < cr.rowptr[br + 1]; ++b)
+    for (int j = 0; j < bs; ++j) J[b * bs2 + i * bs + j] = 0.0;
+  J[static_cast<int64_t>(cr.diag[br]) * bs2 + i * bs + i] = 1.0;
+}
+
 }  // namespace
+
+void launch_constraints(double* v, const int64_t* idx, const double* val, int64_t n, int op, cudaStream_t stream) {
+  if (n <= 0) return;
+  count_launches(1);
+  k_constraints<<<static_cast<int>((n + 255) / 256), 256, 0, stream>>>(v, idx, val, n, op);
+}
+
+void launch_constraint_rows(double* J, const ConstraintRows& cr, const int64_t* idx, int64_t n, int bs,
+                            cudaStream_t stream) {
+  if (n <= 0) return;
+  count_launches(1);
+  k_constraint_rows<<<static_cast<int>((n + 127) / 128), 128, 0, stream>>>(J, cr, idx, n, bs);
+}
 
 void launch_faces(int dim, const FaceParams& p, int begin, int end, int mode, cudaStream_t stream) {
   const int n = end - begin;

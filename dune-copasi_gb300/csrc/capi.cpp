@@ -123,6 +123,35 @@ int dc_species_vertices(const dc_model* model, int32_t species, int64_t* vertex_
   });
 }
 
+int dc_vertex_coords(const dc_model* model, double* coords, size_t n) {
+  return guarded([&] {
+    if (!model || !coords) throw std::invalid_argument("null argument");
+    const auto& c = model->model->mesh.coords;
+    if (n != c.size()) throw std::invalid_argument("size mismatch");
+    std::memcpy(coords, c.data(), n * sizeof(double));
+    return DC_OK;
+  });
+}
+
+int dc_constraints(const dc_model* model, int64_t* dofs, double* values, size_t n, size_t* n_out) {
+  return guarded([&] {
+    if (!model || !n_out) throw std::invalid_argument("null argument");
+    const auto& m = *model->model;
+    *n_out = static_cast<size_t>(m.n_constraints);
+    if (!dofs && !values) return DC_OK;
+    if (n != static_cast<size_t>(m.n_constraints)) throw std::invalid_argument("size mismatch");
+    for (int64_t k = 0; k < m.n_constraints; ++k) {
+      const int64_t node = m.cons_idx[k] / m.bs;
+      const int local = static_cast<int>(m.cons_idx[k] % m.bs);
+      int c = 0;
+      while (node >= m.comp_node_offset[c + 1]) ++c;
+      if (dofs) dofs[k] = m.ref_dof(c, static_cast<int32_t>(node - m.comp_node_offset[c]), local);
+      if (values) values[k] = m.cons_val[k];
+    }
+    return DC_OK;
+  });
+}
+
 int dc_state_set_initial(dc_model* model) {
   return guarded([&] {
     if (!model) throw std::invalid_argument("null argument");
@@ -423,6 +452,17 @@ int dc_profile_get(const dc_model* model, double* ms, int64_t* calls, int32_t n_
       ms[c] = ok ? kt.ms[c] : 0.0;
       calls[c] = ok ? kt.calls[c] : 0;
     }
+    return DC_OK;
+  });
+}
+
+int dc_spmv_format(const dc_model* model, int32_t* format, double* bsr_us, double* sell_us) {
+  return guarded([&] {
+    if (!model || !format) throw std::invalid_argument("null argument");
+    const auto& s = *model->solver;
+    *format = s.spmv_format;
+    if (bsr_us) *bsr_us = s.spmv_tune_us[0];
+    if (sell_us) *sell_us = s.spmv_tune_us[1];
     return DC_OK;
   });
 }

@@ -163,6 +163,38 @@ __global__ void __launch_bounds__(kThreads) k_spmv_rv(int nrows, const int32_t* 
   }
 }
 
+// (2) on the SELL-32 layout: a warp per slice of 32 block rows, a lane per block row
+template <int B, class T, class V>
+__global__ void __launch_bounds__(kThreads) k_sell_rv(Sell S, const V* __restrict__ val, const T* __restrict__ phat,
+                                                      T* __restrict__ v, const T* __restrict__ rhat,
+                                                      ReduceScratch rs, double* sc) {
+  if (done(sc)) return;
+  double acc[1] = {0.0};
+  const int lane = threadIdx.x & 31;
+  const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+  for (int64_t sl = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; sl < S.nslices; sl += nw) {
+    V y[B];
+    sell_lane_rows<B, T, V>(S, sl, lane, val, phat, y);
+    const int64_t br = sl * 32 + lane;
+    if (br < S.nrows) {
+#pragma unroll
+      for (int i = 0; i < B; ++i) {
+        const T yt = static_cast<T>(y[i]);
+        v[br * B + i] = yt;
+        acc[0] += static_cast<double>(rhat[br * B + i]) * static_cast<double>(yt);
+      }
+    }
+  }
+  if (grid_sum<1>(acc, rs)) {
+    const double rv = acc[0];
+    sc[KS_RV] = rv;
+    const double a = sc[KS_RHO] / rv;
+    if (!isfinite(rv)) sc[KS_DONE] = kDoneNonFinite;
+    else if (rv == 0.0 || !isfinite(a)) sc[KS_DONE] = kDoneBreakdown;
+    sc[KS_ALPHA] = isfinite(a) ? a : 0.0;
+  }
+}
+
 // (3) s = r - alpha v;  shat = D^-1 s (when BJ);  ||s||^2
 template <int B, class T, class V, bool BJ>
 __global__ void __launch_bounds__(kThreads) k_update_s(int nrows, T* __restrict__ s, const T* __restrict__ r,
@@ -213,6 +245,42 @@ __global__ void __launch_bounds__(kThreads) k_spmv_omega(int nrows, const int32_
     const double td = static_cast<double>(yt);
     acc[0] += td * static_cast<double>(s[row]);
     acc[1] += td * td;
+  }
+  if (grid_sum<2>(acc, rs)) {
+    sc[KS_TS] = acc[0];
+    sc[KS_TT] = acc[1];
+    double w = acc[1] != 0.0 ? acc[0] / acc[1] : 0.0;
+    if (!isfinite(w)) {
+      sc[KS_DONE] = kDoneNonFinite;
+      w = 0.0;
+    }
+    sc[KS_OMEGA] = w;
+  }
+}
+
+// (4) on the SELL-32 layout
+template <int B, class T, class V>
+__global__ void __launch_bounds__(kThreads) k_sell_omega(Sell S, const V* __restrict__ val,
+                                                         const T* __restrict__ shat, T* __restrict__ t,
+                                                         const T* __restrict__ s, ReduceScratch rs, double* sc) {
+  if (done(sc)) return;
+  double acc[2] = {0.0, 0.0};
+  const int lane = threadIdx.x & 31;
+  const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+  for (int64_t sl = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; sl < S.nslices; sl += nw) {
+    V y[B];
+    sell_lane_rows<B, T, V>(S, sl, lane, val, shat, y);
+    const int64_t br = sl * 32 + lane;
+    if (br < S.nrows) {
+#pragma unroll
+      for (int i = 0; i < B; ++i) {
+        const T yt = static_cast<T>(y[i]);
+        t[br * B + i] = yt;
+        const double td = static_cast<double>(yt);
+        acc[0] += td * static_cast<double>(s[br * B + i]);
+        acc[1] += td * td;
+      }
+    }
   }
   if (grid_sum<2>(acc, rs)) {
     sc[KS_TS] = acc[0];
@@ -283,7 +351,7 @@ void krylov_init(const KrylovVectors<T>& k, int64_t n, double rel, ReduceScratch
 
 template <class T, class V>
 void krylov_iteration(const Bsr& A, const V* vals, const V* dinv, const KrylovVectors<T>& k, ReduceScratch rs,
-                      double* sc, cudaStream_t s, cudaEvent_t* ev, const Amg* amg) {
+                      double* sc, cudaStream_t s, cudaEvent_t* ev, const Amg* amg, const Sell* sell) {
   const int64_t n = static_cast<int64_t>(A.nrows) * A.bs;
   const int gn = grid_for(A.nrows);
   count_launches(5);
@@ -301,8 +369,11 @@ void krylov_iteration(const Bsr& A, const V* vals, const V* dinv, const KrylovVe
       k_update_p<B, T, V, true><<<gn, kThreads, 0, s>>>(A.nrows, k.p, k.r, k.v, dinv, k.phat, sc);               \
     }                                                                                                            \
     mark(0);                                                                                                     \
-    k_spmv_rv<B, T, V><<<kReduceBlocks, kThreads, 0, s>>>(A.nrows, A.rowptr, A.colidx, vals, k.phat, k.v, k.rhat, \
-                                                          rs, sc);                                                \
+    if (sell)                                                                                                    \
+      k_sell_rv<B, T, V><<<kReduceBlocks, kThreads, 0, s>>>(*sell, vals, k.phat, k.v, k.rhat, rs, sc);           \
+    else                                                                                                         \
+      k_spmv_rv<B, T, V><<<kReduceBlocks, kThreads, 0, s>>>(A.nrows, A.rowptr, A.colidx, vals, k.phat, k.v,      \
+                                                            k.rhat, rs, sc);                                     \
     mark(1);                                                                                                     \
     if (amg) {                                                                                                   \
       k_update_s<B, T, V, false><<<kReduceBlocks, kThreads, 0, s>>>(A.nrows, k.s, k.r, k.v, dinv, k.shat, rs,    \
@@ -312,8 +383,11 @@ void krylov_iteration(const Bsr& A, const V* vals, const V* dinv, const KrylovVe
       k_update_s<B, T, V, true><<<kReduceBlocks, kThreads, 0, s>>>(A.nrows, k.s, k.r, k.v, dinv, k.shat, rs, sc); \
     }                                                                                                            \
     mark(2);                                                                                                     \
-    k_spmv_omega<B, T, V><<<kReduceBlocks, kThreads, 0, s>>>(A.nrows, A.rowptr, A.colidx, vals, k.shat, k.t, k.s, \
-                                                             rs, sc);                                             \
+    if (sell)                                                                                                    \
+      k_sell_omega<B, T, V><<<kReduceBlocks, kThreads, 0, s>>>(*sell, vals, k.shat, k.t, k.s, rs, sc);           \
+    else                                                                                                         \
+      k_spmv_omega<B, T, V><<<kReduceBlocks, kThreads, 0, s>>>(A.nrows, A.rowptr, A.colidx, vals, k.shat, k.t,   \
+                                                               k.s, rs, sc);                                     \
     mark(3);                                                                                                     \
     break;
   switch (A.bs) {
@@ -327,8 +401,10 @@ void krylov_iteration(const Bsr& A, const V* vals, const V* dinv, const KrylovVe
 template void krylov_init<double>(const KrylovVectors<double>&, int64_t, double, ReduceScratch, double*, cudaStream_t);
 template void krylov_init<float>(const KrylovVectors<float>&, int64_t, double, ReduceScratch, double*, cudaStream_t);
 template void krylov_iteration<double, double>(const Bsr&, const double*, const double*, const KrylovVectors<double>&,
-                                               ReduceScratch, double*, cudaStream_t, cudaEvent_t*, const Amg*);
+                                               ReduceScratch, double*, cudaStream_t, cudaEvent_t*, const Amg*,
+                                               const Sell*);
 template void krylov_iteration<float, float>(const Bsr&, const float*, const float*, const KrylovVectors<float>&,
-                                             ReduceScratch, double*, cudaStream_t, cudaEvent_t*, const Amg*);
+                                             ReduceScratch, double*, cudaStream_t, cudaEvent_t*, const Amg*,
+                                             const Sell*);
 
 }  // namespace dcgpu

@@ -39,10 +39,12 @@ void krylov_init(const KrylovVectors<T>& k, int64_t n, double rel, ReduceScratch
 
 // one iteration (five launches); V is the matrix / preconditioner value type.  When `ev`
 // is given, ev[0..1] bracket the first SpMV kernel and ev[2..3] the second.
-// With `amg`, the preconditioner is one multigrid V-cycle instead of block Jacobi.
+// With `amg`, the preconditioner is one multigrid V-cycle instead of block Jacobi.  With
+// `sell`, the two SpMVs read `vals` in that SELL-32 layout instead of A's BSR layout.
 class Amg;
 template <class T, class V>
 void krylov_iteration(const Bsr& A, const V* vals, const V* dinv, const KrylovVectors<T>& k, ReduceScratch rs,
-                      double* sc, cudaStream_t s, cudaEvent_t* ev = nullptr, const Amg* amg = nullptr);
+                      double* sc, cudaStream_t s, cudaEvent_t* ev = nullptr, const Amg* amg = nullptr,
+                      const Sell* sell = nullptr);
 
 }  // namespace dcgpu

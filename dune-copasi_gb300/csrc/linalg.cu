@@ -337,6 +337,15 @@ __global__ void k_axpy(int64_t n, double a, const double* x, double* y) {
   for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride)
     y[i] += a * x[i];
 }
+// out = a x + b y with x or y optional; the rounding is that of y1 = a x, then y1 += b y
+__global__ void k_combine(int64_t n, double a, const double* __restrict__ x, double b, const double* __restrict__ y,
+                          double* __restrict__ out) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const double ax = x ? a * x[i] : 0.0;
+    out[i] = y ? __fma_rn(b, y[i], ax) : ax;
+  }
+}
 __global__ void k_scale_copy(int64_t n, double a, const double* x, double* y) {
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
   for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride)
@@ -369,6 +378,81 @@ void spmv(const Bsr& A, const double* x, double* y, cudaStream_t s) {
 }
 void spmv32(const Bsr& A, const float* x, float* y, cudaStream_t s) {
   spmv_dispatch<float, float>(A, A.val32, x, y, nullptr, s);
+}
+
+namespace {
+
+// one thread per (slice, lane): copies the lane's blocks into its SELL slots as fp32 and
+// zero-fills the slots past the end of its row; the 32 lanes of a slice write each slot
+// entry as one contiguous 128-byte line
+template <int B>
+__global__ void __launch_bounds__(256) k_bsr_to_sell(Sell S, const int32_t* __restrict__ rowptr,
+                                                     const double* __restrict__ val, float* __restrict__ out) {
+  const int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= S.nslices * 32) return;
+  const int64_t sl = t >> 5;
+  const int lane = static_cast<int>(t & 31);
+  const int64_t o0 = S.off[sl];
+  const int w = static_cast<int>(S.off[sl + 1] - o0);
+  int k0 = 0, len = 0;
+  if (t < S.nrows) {
+    k0 = rowptr[t];
+    len = rowptr[t + 1] - k0;
+  }
+  for (int k = 0; k < w; ++k) {
+    float* dst = out + (o0 + k) * (32 * B * B) + lane;
+    const double* src = val + static_cast<int64_t>(k0 + k) * (B * B);
+#pragma unroll
+    for (int e = 0; e < B * B; ++e) dst[e * 32] = k < len ? static_cast<float>(src[e]) : 0.0f;
+  }
+}
+
+template <int B>
+__global__ void __launch_bounds__(256) k_sell_spmv(Sell S, const float* __restrict__ val, const float* __restrict__ x,
+                                                   float* __restrict__ y) {
+  const int64_t sl = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  if (sl >= S.nslices) return;
+  const int lane = threadIdx.x & 31;
+  float acc[B];
+  sell_lane_rows<B, float, float>(S, sl, lane, val, x, acc);
+  const int64_t br = sl * 32 + lane;
+  if (br < S.nrows)
+#pragma unroll
+    for (int i = 0; i < B; ++i) y[br * B + i] = acc[i];
+}
+
+}  // namespace
+
+void bsr_to_sell(const Bsr& A, const double* val, const Sell& S, float* out, cudaStream_t s) {
+  if (S.nslices == 0) return;
+  const int threads = 256;
+  const int blocks = static_cast<int>((S.nslices * 32 + threads - 1) / threads);
+  count_launches(1);
+#define DC_B2S(B) \
+  case B: k_bsr_to_sell<B><<<blocks, threads, 0, s>>>(S, A.rowptr, val, out); return;
+  switch (S.bs) {
+    DC_B2S(1) DC_B2S(2) DC_B2S(3) DC_B2S(4) DC_B2S(5) DC_B2S(6) DC_B2S(7) DC_B2S(8)
+    default: throw std::runtime_error("sell: block size unsupported");
+  }
+#undef DC_B2S
+}
+
+void spmv_sell32(const Sell& S, const float* val, const float* x, float* y, cudaStream_t s) {
+  if (S.nslices == 0) return;
+  const int threads = 256;
+  const int blocks = static_cast<int>((S.nslices * 32 + threads - 1) / threads);
+  count_launches(1);
+#define DC_SS(B) \
+  case B: k_sell_spmv<B><<<blocks, threads, 0, s>>>(S, val, x, y); return;
+  switch (S.bs) {
+    DC_SS(1) DC_SS(2) DC_SS(3) DC_SS(4) DC_SS(5) DC_SS(6) DC_SS(7) DC_SS(8)
+    default: throw std::runtime_error("sell: block size unsupported");
+  }
+#undef DC_SS
+}
+
+void spmv32_vals(const Bsr& A, const float* val, const float* x, float* y, cudaStream_t s) {
+  spmv_dispatch<float, float>(A, val, x, y, nullptr, s);
 }
 void residual(const Bsr& A, const double* x, const double* b, double* r, cudaStream_t s) {
   spmv_dispatch<double, double>(A, A.val, x, r, b, s);
@@ -460,6 +544,9 @@ void axpby(int64_t n, double a, const double* x, double b, double* y, cudaStream
 }
 void scale_copy(int64_t n, double a, const double* x, double* y, cudaStream_t s) {
   if (n > 0) k_scale_copy<<<ew_blocks(n), 256, 0, s>>>(n, a, x, y);
+}
+void combine(int64_t n, double a, const double* x, double b, const double* y, double* out, cudaStream_t s) {
+  if (n > 0) k_combine<<<ew_blocks(n), 256, 0, s>>>(n, a, x, b, y, out);
 }
 void to_float(int64_t n, const double* x, float* y, cudaStream_t s) {
   if (n > 0) k_to_float<<<ew_blocks(n), 256, 0, s>>>(n, x, 1.0, y);

@@ -9,6 +9,8 @@
 
 #include <cuda_runtime.h>
 
+#include "sell.cuh"
+
 namespace dcgpu {
 
 struct Bsr {
@@ -34,6 +36,12 @@ constexpr int kReduceThreads = 256;
 void spmv(const Bsr& A, const double* x, double* y, cudaStream_t s);
 // y = A x   (fp32 values, fp32 vectors)
 void spmv32(const Bsr& A, const float* x, float* y, cudaStream_t s);
+// y = A x with the fp32 values `val` of A's pattern (thread per scalar row)
+void spmv32_vals(const Bsr& A, const float* val, const float* x, float* y, cudaStream_t s);
+// fp32 SELL-32 copy of the fp64 BSR values `val` (pattern of A, layout S); padding zeroed
+void bsr_to_sell(const Bsr& A, const double* val, const Sell& S, float* out, cudaStream_t s);
+// y = A x on the SELL-32 layout (warp per slice, lane per block row)
+void spmv_sell32(const Sell& S, const float* val, const float* x, float* y, cudaStream_t s);
 // r = b - A x (fp64)
 void residual(const Bsr& A, const double* x, const double* b, double* r, cudaStream_t s);
 // y += alpha * V x with the pattern of A and the values V (fp64)
@@ -88,6 +96,8 @@ void count_launches(long long n);
 void axpy(int64_t n, double a, const double* x, double* y, cudaStream_t s);          // y += a x
 void axpby(int64_t n, double a, const double* x, double b, double* y, cudaStream_t s); // y = a x + b y
 void scale_copy(int64_t n, double a, const double* x, double* y, cudaStream_t s);     // y = a x
+// out = a x + b y; x or y may be null (its term is left out)
+void combine(int64_t n, double a, const double* x, double b, const double* y, double* out, cudaStream_t s);
 void to_float(int64_t n, const double* x, float* y, cudaStream_t s);
 void add_float(int64_t n, const float* x, double* y, cudaStream_t s);                 // y += x
 void to_float_scaled(int64_t n, const double* x, double scale, float* y, cudaStream_t s);

@@ -117,6 +117,7 @@ Model::Model(const std::string& ini_text, const std::string& overrides) {
   build_volume_groups();
   build_face_groups();
   build_static_matrices();
+  build_constraints();
 }
 
 void Model::build_static_matrices() {
@@ -133,6 +134,7 @@ void Model::build_static_matrices() {
     d_Ks.resize(nvals);
     cuda_check(cudaMemset(d_Ks.get(), 0, nvals * sizeof(double)), "memset");
   }
+  if (has_Ms || has_Ks) d_Cs.resize(nvals);
   for (const auto& g : vgroups) {
     if (g.static_terms.empty()) continue;
     VolumeParams p{};
@@ -417,6 +419,31 @@ void Model::build_pattern() {
   d_rowptr.upload(rowptr);
   d_colidx.upload(colidx);
   d_diag.upload(diag);
+
+  // SELL-32 slices of the same pattern: slot offsets and block columns (padding slots point
+  // at the lane's own row, or at row 0 past the last row)
+  const int64_t nsl = (nnodes + 31) / 32;
+  std::vector<int64_t> soff(nsl + 1, 0);
+  for (int64_t sl = 0; sl < nsl; ++sl) {
+    int w = 0;
+    for (int64_t br = sl * 32; br < std::min<int64_t>(nnodes, sl * 32 + 32); ++br)
+      w = std::max(w, rowptr[br + 1] - rowptr[br]);
+    soff[sl + 1] = soff[sl] + w;
+  }
+  std::vector<int32_t> scols(static_cast<size_t>(soff[nsl]) * 32);
+  for (int64_t sl = 0; sl < nsl; ++sl) {
+    const int w = static_cast<int>(soff[sl + 1] - soff[sl]);
+    for (int lane = 0; lane < 32; ++lane) {
+      const int64_t br = sl * 32 + lane;
+      const int len = br < nnodes ? rowptr[br + 1] - rowptr[br] : 0;
+      for (int k = 0; k < w; ++k)
+        scols[(soff[sl] + k) * 32 + lane] =
+            k < len ? colidx[rowptr[br] + k] : static_cast<int32_t>(br < nnodes ? br : 0);
+    }
+  }
+  sell_slots = soff[nsl];
+  d_sell_off.upload(soff);
+  d_sell_cols.upload(scols);
   d_row_ns.upload(row_ns);
 }
 
@@ -939,19 +966,53 @@ Bsr Model::bsr(double* val, float* val32) const {
   return A;
 }
 
+Sell Model::sell() const {
+  Sell S;
+  S.nrows = static_cast<int>(nnodes);
+  S.bs = bs;
+  S.nslices = (nnodes + 31) / 32;
+  S.nslots = sell_slots;
+  S.off = d_sell_off.get();
+  S.cols = d_sell_cols.get();
+  return S;
+}
+
 void Model::assemble(const double* x, double t, double cm, double ca, double* r, double* J, int mode,
                      cudaStream_t s) const {
-  // static part: r += (cm Ms + ca Ks) x, J += cm Ms + ca Ks
+  // static part: r += (cm Ms + ca Ks) x, J (+)= cm Ms + ca Ks
   const Bsr A0 = bsr(nullptr, nullptr);
   const int64_t nvals = nnzb() * bs * bs;
+  const bool use_m = has_Ms && cm != 0.0, use_k = has_Ks && ca != 0.0;
+  const double* C = nullptr;
+  if ((use_m || use_k) && (mode & 2) && J) {
+    if (!cs_valid || cs_cm != cm || cs_ca != ca) {
+      if (d_Cs.size() != static_cast<size_t>(nvals)) d_Cs.resize(nvals);
+      combine(nvals, cm, use_m ? d_Ms.get() : nullptr, ca, use_k ? d_Ks.get() : nullptr, d_Cs.get(), s);
+      cs_cm = cm;
+      cs_ca = ca;
+      cs_valid = true;
+    }
+    C = d_Cs.get();
+  } else if ((use_m || use_k) && cs_valid && cs_cm == cm && cs_ca == ca) {
+    C = d_Cs.get();
+  }
   if ((mode & 1) && r) {
-    if (has_Ms && cm != 0.0) spmv_acc(A0, d_Ms.get(), x, r, cm, s);
-    if (has_Ks && ca != 0.0) spmv_acc(A0, d_Ks.get(), x, r, ca, s);
+    if (C) {
+      spmv_acc(A0, C, x, r, 1.0, s);
+    } else {
+      if (use_m) spmv_acc(A0, d_Ms.get(), x, r, cm, s);
+      if (use_k) spmv_acc(A0, d_Ks.get(), x, r, ca, s);
+    }
   }
   if ((mode & 2) && J) {
-    if (has_Ms && cm != 0.0) axpy(nvals, cm, d_Ms.get(), J, s);
-    if (has_Ks && ca != 0.0) axpy(nvals, ca, d_Ks.get(), J, s);
+    if (mode & kAssembleOverwriteJacobian) {
+      if (C) cuda_check(cudaMemcpyAsync(J, C, nvals * sizeof(double), cudaMemcpyDeviceToDevice, s), "copy");
+      else cuda_check(cudaMemsetAsync(J, 0, nvals * sizeof(double), s), "memset");
+    } else if (C) {
+      axpy(nvals, 1.0, C, J, s);
+    }
   }
+  mode &= 3;
   for (const auto& g : vgroups) {
     if (!(cm != 0.0 && g.has_mass) && !(ca != 0.0 && g.has_stiffness)) continue;
     VolumeParams p{};

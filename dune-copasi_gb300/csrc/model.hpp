@@ -164,6 +164,22 @@ class Model {
   // static parts of the operator, assembled once: mass-form and stiffness-form BSR values
   DeviceBuffer<double> d_Ms, d_Ks;
   bool has_Ms = false, has_Ks = false;
+  // cm Ms + ca Ks for the last (cm, ca) a Jacobian was assembled with: a DIRK stage keeps
+  // its (cm, ca) for all its Newton iterations, so one combination serves the stage's
+  // Jacobian copies and residual products
+  mutable DeviceBuffer<double> d_Cs;
+  mutable double cs_cm = 0.0, cs_ca = 0.0;
+  mutable bool cs_valid = false;
+
+  // Dirichlet constraints: blocked vector indices (ascending) and values
+  std::vector<int64_t> cons_idx;
+  std::vector<double> cons_val;
+  int64_t n_constraints = 0;
+  DeviceBuffer<int64_t> d_cons_idx;
+  DeviceBuffer<double> d_cons_val;
+  void apply_constraints(double* x, cudaStream_t s) const;   // x[idx] = val
+  void constrain_residual(double* r, cudaStream_t s) const;  // r[idx] = 0
+  void constrain_jacobian(double* J, cudaStream_t s) const;  // unit rows
 
   // host-side helpers
   std::vector<double> initial_state() const;        // reference DOF order
@@ -173,10 +189,16 @@ class Model {
 
   // assemble into r (residual, may be null) and J (BSR values, may be null):
   //   r += cm * M(x, t) + ca * A(x, t),  J += cm * dM/dx + ca * dA/dx
-  // mode bit 1: residual, bit 2: Jacobian.
+  // mode bit 1: residual, bit 2: Jacobian; with kAssembleOverwriteJacobian the Jacobian is
+  // overwritten (J = cm dM/dx + ca dA/dx) instead of added to, and its prior contents are ignored.
+  static constexpr int kAssembleOverwriteJacobian = 8;
   void assemble(const double* x, double t, double cm, double ca, double* r, double* J, int mode,
                 cudaStream_t s) const;
   Bsr bsr(double* val, float* val32) const;
+  Sell sell() const;  // SELL-32 layout of the pattern (values sized sell_slots * 32 * bs * bs)
+  int64_t sell_slots = 0;
+  DeviceBuffer<int64_t> d_sell_off;
+  DeviceBuffer<int32_t> d_sell_cols;
   int64_t nnzb() const { return static_cast<int64_t>(colidx.size()); }
 
  private:
@@ -187,6 +209,7 @@ class Model {
   void build_pattern();
   void upload_geometry();
   void build_static_matrices();
+  void build_constraints();
 };
 
 }  // namespace dcgpu

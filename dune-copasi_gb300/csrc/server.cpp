@@ -68,7 +68,7 @@ int64_t Server::estimate_bytes(const std::string& ini, const std::string& overri
   const double nnzb = nnodes * (dim == 2 ? 7.0 : 15.0);
   const double vals = nnzb * bs * bs * 8.0;
   const double n = nnodes * bs;
-  double bytes = 3.5 * vals                      // J, static mass / stiffness, fp32 copy
+  double bytes = 4.5 * vals                      // J, static mass / stiffness / combination, fp32 copy
                  + 1.5 * nnodes * bs * bs * 8.0  // block-Jacobi inverses (fp64 + fp32)
                  + 25.0 * n * 8.0                // state, stages, Krylov vectors
                  + nnzb * 4.0 + nnodes * 8.0     // pattern

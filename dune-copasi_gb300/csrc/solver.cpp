@@ -116,6 +116,12 @@ Solver::Solver(Model& m, cudaStream_t s) : model(m), stream(s) {
     lin_max_it_ = static_cast<int>(r.back());
   }
   if (lin_direct_) lin_max_it_ = std::max(lin_max_it_, 5000);
+  // relative residual reduction that stands in for an exact direct solve inside Newton: a
+  // correction off by 1e-10 (times the condition number) of its size is absorbed by the
+  // next Newton iteration and leaves the converged stage solution within that fraction of
+  // the last correction of the direct-solve one
+  direct_tol_ = ls.get_double("direct_tolerance", 1e-10);
+  if (!(direct_tol_ > 0.0 && direct_tol_ < 1.0)) throw ConfigError("linear_solver.direct_tolerance must be in (0, 1)");
   precond_ = ls.get("preconditioner.type", "Jacobi");
   // every dune-istl preconditioner of the reference's registry (Richardson, Jacobi, SSOR,
   // SOR, GaussSeidel, BlockJacobi, ILU variants) maps to block Jacobi on the device; "AMG"
@@ -131,6 +137,12 @@ Solver::Solver(Model& m, cudaStream_t s) : model(m), stream(s) {
                static_cast<int>(ls.get_long("preconditioner.coarsen_target", 256)));
   }
   const bool want_mixed = ls.get("precision", "double") == "mixed";
+  const std::string fmt = ls.get("spmv", "auto");
+  if (fmt == "auto") spmv_request_ = kSpmvAuto;
+  else if (fmt == "bsr") spmv_request_ = kSpmvBsr;
+  else if (fmt == "sell") spmv_request_ = kSpmvSell;
+  else throw ConfigError("linear_solver.spmv must be auto, bsr or sell, not '" + fmt + "'");
+  spmv_format = spmv_request_;
   dec_ = tso.get_double("time_step_decrease_factor", 0.5);
   inc_ = tso.get_double("time_step_increase_factor", 1.1);
   has_min_ = tso.has_key("time_step_min");
@@ -150,8 +162,40 @@ void Solver::enable_mixed(bool on) {
     fr_.resize(n_); frhat_.resize(n_); fp_.resize(n_); fv_.resize(n_); fs_.resize(n_); ft_.resize(n_);
     fphat_.resize(n_); fshat_.resize(n_); fx_.resize(n_); fb_.resize(n_);
     fdinv_.resize(static_cast<size_t>(model.nnodes) * model.bs * model.bs);
-    J32_.resize(static_cast<size_t>(model.nnzb()) * model.bs * model.bs);
+    if (spmv_request_ != kSpmvSell || use_amg_) J32_.resize(static_cast<size_t>(model.nnzb()) * model.bs * model.bs);
+    if (spmv_request_ != kSpmvBsr) Js32_.resize(static_cast<size_t>(model.sell_slots) * 32 * model.bs * model.bs);
   }
+}
+
+// Times the thread-per-row BSR SpMV and the warp-per-slice SELL-32 SpMV on the current fp32
+// operator (both copies must be filled), five launches each after one warm-up, and keeps
+// the faster layout for the rest of the run.
+void Solver::tune_spmv() {
+  const Bsr A = model.bsr(J_.get(), J32_.get());
+  const Sell S = model.sell();
+  cudaEvent_t e0, e1;
+  cuda_check(cudaEventCreate(&e0), "cudaEventCreate");
+  cuda_check(cudaEventCreate(&e1), "cudaEventCreate");
+  constexpr int kReps = 5;
+  for (int f = 0; f < 2; ++f) {
+    auto run = [&] {
+      if (f == 0) spmv32_vals(A, J32_.get(), fp_.get(), fv_.get(), stream);
+      else spmv_sell32(S, Js32_.get(), fp_.get(), fv_.get(), stream);
+    };
+    run();
+    cuda_check(cudaEventRecord(e0, stream), "cudaEventRecord");
+    for (int k = 0; k < kReps; ++k) run();
+    cuda_check(cudaEventRecord(e1, stream), "cudaEventRecord");
+    cuda_check(cudaEventSynchronize(e1), "cudaEventSynchronize");
+    float ms = 0.0f;
+    cuda_check(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+    spmv_tune_us[f] = 1e3 * ms / kReps;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  spmv_format = spmv_tune_us[1] < spmv_tune_us[0] ? kSpmvSell : kSpmvBsr;
+  if (spmv_format == kSpmvBsr) Js32_.resize(0);
+  else if (!use_amg_) J32_.resize(0);
 }
 
 Solver::~Solver() {
@@ -251,8 +295,14 @@ void Solver::setup_preconditioner() {
   cuda_check(cudaStreamSynchronize(stream), "status");
   if (st) throw StepFailure("singular diagonal block in the Jacobian");
   if (mixed_precision) {
-    to_float(static_cast<int64_t>(model.nnzb()) * model.bs * model.bs, J_.get(), J32_.get(), stream);
+    // the BSR copy feeds the BSR SpMV, the tuner and the multigrid fine level; the SELL-32
+    // copy feeds the SELL SpMV
+    const bool need_bsr = spmv_format != kSpmvSell || use_amg_;
+    const bool need_sell = spmv_format != kSpmvBsr;
+    if (need_bsr) to_float(static_cast<int64_t>(model.nnzb()) * model.bs * model.bs, J_.get(), J32_.get(), stream);
+    if (need_sell) bsr_to_sell(A, J_.get(), model.sell(), Js32_.get(), stream);
     to_float(static_cast<int64_t>(model.nnodes) * model.bs * model.bs, dinv_.get(), fdinv_.get(), stream);
+    if (spmv_format == kSpmvAuto) tune_spmv();
   }
   if (use_amg_) {
     amg_.setup(J_.get(), dinv_.get(), J32_.get(), fdinv_.get(), mixed_precision, status_.get(), stream);
@@ -285,7 +335,10 @@ cudaGraphExec_t Solver::krylov_graph(bool fp32) {
     if (fp32) {
       KrylovVectors<float> kv{fx_.get(), fr_.get(), frhat_.get(), fp_.get(), fv_.get(), fs_.get(), ft_.get(),
                               fphat_.get(), fshat_.get()};
-      krylov_iteration<float, float>(A, J32_.get(), fdinv_.get(), kv, rs_, sc, stream, e, use_amg_ ? &amg_ : nullptr);
+      const bool sell = spmv_format == kSpmvSell;
+      const Sell S = model.sell();
+      krylov_iteration<float, float>(A, sell ? Js32_.get() : J32_.get(), fdinv_.get(), kv, rs_, sc, stream, e,
+                                     use_amg_ ? &amg_ : nullptr, sell ? &S : nullptr);
     } else {
       KrylovVectors<double> kv{kx_.get(), kr_.get(), krhat_.get(), kp_.get(), kv_.get(), ks_.get(), kt_.get(),
                                kphat_.get(), kshat_.get()};
@@ -410,7 +463,10 @@ void Solver::linear_step(double* x, const std::function<void(const double*, doub
   res(x, r_.get());
   jac(x);
   int it = 0;
-  const double tol = lin_direct_ ? 1e-13 : lin_rel_;
+  // a linear model's stage solution is this one solve, with no Newton iteration after it to
+  // absorb the solve's error: direct-solve semantics here keep the near-machine-precision
+  // reduction
+  const double tol = lin_direct_ ? std::min(direct_tol_, 1e-13) : lin_rel_;
   int st = linear_solve(r_.get(), z_.get(), tol, &it);
   if (st != DC_OK) throw StepFailure("linear solver did not converge");
   axpy(n_, -1.0, z_.get(), x, stream);
@@ -443,7 +499,7 @@ void Solver::newton(double* x, const std::function<void(const double*, double*)>
     }
     double red;
     if (lin_direct_) {
-      red = 1e-13;
+      red = direct_tol_;
     } else if (dx_fixed_) {
       red = dx_min_rel_;
     } else {
@@ -477,7 +533,6 @@ void Solver::one_step(double dt) {
   for (int j = 0; j <= s; ++j) ts[j] = t + tab.D[j] * dt;
   cuda_check(cudaMemcpyAsync(us_[0].get(), x_.get(), n_ * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");
   cuda_check(cudaMemcpyAsync(stage_.get(), x_.get(), n_ * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");
-  const int64_t nj = static_cast<int64_t>(model.nnzb()) * model.bs * model.bs;
   for (int i = 1; i <= s; ++i) {
     const auto& a = tab.A[i - 1];
     const auto& b = tab.B[i - 1];
@@ -496,18 +551,22 @@ void Solver::one_step(double dt) {
       tbegin(0);
       model.assemble(y, ti, ai, bi, r, nullptr, 1, stream);
       tend();
+      model.constrain_residual(r, stream);
       ++stats.assemblies;
     };
     auto jac = [&](const double* y) {
-      cuda_check(cudaMemsetAsync(J_.get(), 0, nj * sizeof(double), stream), "memset");
       tbegin(0);
-      model.assemble(y, ti, ai, bi, nullptr, J_.get(), 2, stream);
+      model.assemble(y, ti, ai, bi, nullptr, J_.get(), 2 | Model::kAssembleOverwriteJacobian, stream);
       tend();
       if (model.padded)
         launch_pad_identity(model.d_diag.get(), model.d_row_ns.get(), static_cast<int>(model.nnodes), model.bs,
                             J_.get(), 1.0, stream);
+      model.constrain_jacobian(J_.get(), stream);
       ++stats.assemblies;
     };
+    // constrained entries take their values before the stage solve; zero residual rows and
+    // unit Jacobian rows keep them there
+    model.apply_constraints(stage_.get(), stream);
     if (model.is_linear) linear_step(stage_.get(), res, jac);
     else newton(stage_.get(), res, jac);
     cuda_check(cudaMemcpyAsync(us_[i].get(), stage_.get(), n_ * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");

@@ -137,6 +137,7 @@ class Solver {
   DeviceBuffer<double> kr_, krhat_, kp_, kv_, ks_, kt_, kphat_, kshat_, kx_, dinv_;
   DeviceBuffer<float> fr_, frhat_, fp_, fv_, fs_, ft_, fphat_, fshat_, fx_, fdinv_, fb_;
   DeviceBuffer<float> J32_;
+  DeviceBuffer<float> Js32_;  // fp32 operator in the SELL-32 layout
   DeviceBuffer<double> partial_, scal_;
   DeviceBuffer<unsigned int> counter_;
   DeviceBuffer<int> status_;
@@ -151,10 +152,21 @@ class Solver {
   std::string norm_ = "l_2";
   double lin_rel_ = 1e-4;
   bool lin_direct_ = true;
+  double direct_tol_ = 1e-10;
   int lin_max_it_ = 500;
   std::string precond_ = "Jacobi";
   bool use_amg_ = false;
   Amg amg_;
+  // fp32 SpMV layout: kSpmvAuto times both on the first fp32 operator and keeps the faster
+  int spmv_request_ = kSpmvAuto;
+  void tune_spmv();
+
+ public:
+  static constexpr int kSpmvAuto = -1, kSpmvBsr = 0, kSpmvSell = 1;
+  int spmv_format = kSpmvAuto;     // the layout in use (auto until tuned)
+  double spmv_tune_us[2] = {0.0, 0.0};  // BSR / SELL-32 SpMV time measured by the tuner
+
+ private:
   double dec_ = 0.5, inc_ = 1.1;
   bool has_min_ = false, has_max_ = false;
   double dt_min_ = 0.0, dt_max_ = 0.0;

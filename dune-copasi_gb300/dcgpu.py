@@ -34,6 +34,7 @@ EXPORTED = [
     "dc_expr_eval", "dc_stream_handle", "dc_launch_count", "dc_profile_enable", "dc_profile_get",
     "dc_assemble_residual_noalloc", "dc_server_create", "dc_server_submit", "dc_server_poll",
     "dc_server_take_state", "dc_server_estimate", "dc_server_destroy", "dc_last_error",
+    "dc_spmv_format", "dc_vertex_coords", "dc_constraints",
 ]
 
 
@@ -118,6 +119,9 @@ def load_library(path=LIB_PATH):
     lib.dc_launch_count.argtypes = []
     lib.dc_profile_enable.argtypes = [vp, ctypes.c_int]
     lib.dc_profile_get.argtypes = [vp, pd, P(ctypes.c_int64), i32]
+    lib.dc_spmv_format.argtypes = [vp, P(i32), pd, pd]
+    lib.dc_vertex_coords.argtypes = [vp, pd, sz]
+    lib.dc_constraints.argtypes = [vp, P(ctypes.c_int64), pd, sz, P(sz)]
     lib.dc_last_error.argtypes = []
     lib.dc_last_error.restype = ctypes.c_char_p
     for name in EXPORTED:
@@ -228,6 +232,49 @@ class Model:
         _check(self._lib.dc_species_vertices(self._h, s, _ptr(out, ctypes.c_int64), out.size))
         return out
 
+    def vertex_coords(self):
+        """(n_vertices, dim) vertex coordinates of the grid."""
+        out = np.empty((self.info["n_vertices"], self.info["dim"]))
+        _check(self._lib.dc_vertex_coords(self._h, _ptr(out), out.size))
+        return out
+
+    def constraints(self):
+        """(reference DOF indices, values) of the Dirichlet constraints, sorted by DOF."""
+        n = ctypes.c_size_t(0)
+        _check(self._lib.dc_constraints(self._h, None, None, 0, ctypes.byref(n)))
+        dofs = np.empty(n.value, np.int64)
+        vals = np.empty(n.value)
+        if n.value:
+            _check(self._lib.dc_constraints(self._h, _ptr(dofs, ctypes.c_int64), _ptr(vals), n.value,
+                                            ctypes.byref(n)))
+        order = np.argsort(dofs, kind="stable")
+        return dofs[order], vals[order]
+
+    def seeded_state(self, init):
+        """State vector (reference DOF order) with init(species name, vertex coords) per
+        species; species for which init returns None keep their initial.expression values."""
+        x = self.state()
+        if init is None:
+            return x
+        coords = self.vertex_coords()
+        off = 0
+        names = self.species
+        i = 0
+        while i < len(names):
+            verts = self.species_vertices(names[i])
+            group = [names[i]]
+            while i + len(group) < len(names) and \
+                    np.array_equal(self.species_vertices(names[i + len(group)]), verts):
+                group.append(names[i + len(group)])
+            ns = len(group)
+            for k, name in enumerate(group):
+                v = init(name, coords[verts])
+                if v is not None:
+                    x[off + k: off + ns * len(verts): ns] = v
+            off += ns * len(verts)
+            i += ns
+        return x
+
     def species_values(self, name):
         s = self.species_index(name)
         n = ctypes.c_int64()
@@ -331,6 +378,15 @@ class Model:
         calls = np.zeros(3, np.int64)
         _check(self._lib.dc_profile_get(self._h, _ptr(ms), _ptr(calls, ctypes.c_int64), 3))
         return {k: (float(ms[i]), int(calls[i])) for i, k in enumerate(("assembly", "spmv", "precond"))}
+
+    def spmv_format(self):
+        """Layout of the fp32 Krylov operator and the tuner's SpMV times:
+        {"format": "auto"|"bsr"|"sell", "bsr_us": t, "sell_us": t}."""
+        f = ctypes.c_int32(0)
+        a = ctypes.c_double(0.0)
+        b = ctypes.c_double(0.0)
+        _check(self._lib.dc_spmv_format(self._h, ctypes.byref(f), ctypes.byref(a), ctypes.byref(b)))
+        return {"format": {-1: "auto", 0: "bsr", 1: "sell"}[f.value], "bsr_us": a.value, "sell_us": b.value}
 
 
 def launch_count():

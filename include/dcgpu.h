@@ -67,6 +67,14 @@ int dc_model_info_get(const dc_model* model, dc_model_info* info);
 int dc_species_name(const dc_model* model, int32_t species, char* buf, size_t len);
 int dc_species_size(const dc_model* model, int32_t species, int64_t* n_vertices);
 int dc_species_vertices(const dc_model* model, int32_t species, int64_t* vertex_ids, size_t n);
+/* vertex coordinates, n_vertices x dim row-major (the grid's Geometry::corner values the
+ * reference's nodal interpolation evaluates at, model/interpolate.hh:21-78) */
+int dc_vertex_coords(const dc_model* model, double* coords, size_t n);
+/* Dirichlet constraints from constrain.{boundary,skeleton}.expression (replaces the
+ * constraints container filled by model/constraints.hh:51-199): *n_out receives their
+ * number; with dofs / values non-null (n == *n_out) the constrained reference DOF indices
+ * (ascending in the engine's blocked order) and their values are copied out. */
+int dc_constraints(const dc_model* model, int64_t* dofs, double* values, size_t n, size_t* n_out);
 
 /* Replaces make_initial + interpolate (dune/copasi/model/make_initial.hh:24-90,
  * interpolate.hh:21-78): nodal interpolation of initial.expression at time_begin. */
@@ -134,6 +142,12 @@ int dc_stream_handle(const dc_model* model, void** stream);
 int64_t dc_launch_count(void);
 int dc_profile_enable(dc_model* model, int enabled);
 int dc_profile_get(const dc_model* model, double* ms, int64_t* calls, int32_t n_categories);
+
+/* Layout of the single-precision Krylov operator (no reference counterpart): -1 = not yet
+ * chosen, 0 = BSR with a thread per scalar row, 1 = SELL-32 with a warp per 32 block rows.
+ * `linear_solver.spmv = auto` (default) times both on the first fp32 operator and keeps the
+ * faster; bsr_us / sell_us receive those times in microseconds (0 when not tuned). */
+int dc_spmv_format(const dc_model* model, int32_t* format, double* bsr_us, double* sell_us);
 
 /* Request server (no counterpart in the reference, which runs one simulation per
  * process): simulations are submitted as INI text (+ optional initial state in the

@@ -159,6 +159,7 @@ class OracleModel:
         self._setup_dofs()
         self._setup_geometry()
         self._setup_faces()
+        self._setup_constraints()
         self._pattern_cache = {}
         tso = mcfg.sub("time_step_operator")
         self.tso = tso
@@ -221,6 +222,140 @@ class OracleModel:
         self.face_l0 = l0[keep]
         self.face_e1 = e1[keep]
         self.face_l1 = l1[keep]
+
+    def _setup_constraints(self):
+        """Dirichlet (translation) constraints, model/constraints.hh:51-199.
+
+        constrain.boundary / constrain.skeleton expressions of a species are evaluated once
+        (time = NaN) at the P1 vertices of the faces of the species' compartment: a face with
+        no neighbour cell in the compartment is a boundary face (in_boundary = 1, normal
+        pointing out of the compartment cell); a face with the compartment on both sides is a
+        skeleton face (in_skeleton = 1, evaluated from both cells, normal out of each) and
+        constrains only vertices that lie on no boundary face (constraints.hh:178).  A value
+        of no_value (DBL_MAX) leaves the vertex free.  When several faces give a vertex a
+        value, the first in (sorted vertex ids, inside before outside) order wins.
+        P1 has no cell-interior DOFs, so constrain.volume never applies (constraints.hh:104).
+        Result: self.cons_dofs (sorted), self.cons_vals.
+        """
+        m = self.mesh
+        d = self.dim
+        sf = self.mcfg.sub("scalar_field")
+        todo = []
+        for sp_ in self.species:
+            c = sf.sub(sp_.name)
+            for kind in ("boundary", "skeleton"):
+                key = "constrain." + kind
+                if c.has_sub(key):
+                    ex = F._scalar(c.sub(key), self.ctx)
+                    if ex is not None:
+                        todo.append((sp_, kind, ex))
+        self.cons_dofs = np.zeros(0, np.int64)
+        self.cons_vals = np.zeros(0)
+        if not todo:
+            return
+        fv, e0, _l0, e1, _l1 = m.faces()
+        has1 = e1 >= 0
+        e1s = np.where(has1, e1, 0)
+        dofs, vals = [], []
+        for sp_, kind, ex in todo:
+            mask = self.comp_mask[sp_.comp]
+            in0 = mask[e0]
+            in1 = has1 & mask[e1s]
+            bnd = in0 ^ in1
+            bverts = np.zeros(m.nv, bool)
+            bverts[fv[bnd].ravel()] = True
+            if kind == "boundary":
+                sel = np.nonzero(bnd)[0]
+                sides = [(sel, np.where(in0[sel], e0[sel], e1s[sel]))]
+                flags = (1.0, 0.0)
+            else:
+                sel = np.nonzero(in0 & in1)[0]
+                sides = [(sel, e0[sel]), (sel, e1s[sel])]
+                flags = (0.0, 1.0)
+            # candidate (face order, side, vertex) triples
+            cand_v, cand_pos, cand_n, cand_vol, cand_key = [], [], [], [], []
+            for side, (fs, cells) in enumerate(sides):
+                fvc = m.coords[fv[fs]]                       # [k, d, d]
+                f0 = fvc[:, 0, :]
+                T = np.stack([fvc[:, j, :] - f0 for j in range(1, d)], axis=2)
+                if d == 2:
+                    nrm = np.stack([T[:, 1, 0], -T[:, 0, 0]], axis=1)
+                    meas = np.linalg.norm(T[:, :, 0], axis=1)
+                else:
+                    nrm = np.cross(T[:, :, 0], T[:, :, 1])
+                    meas = 0.5 * np.linalg.norm(nrm, axis=1)
+                nrm = nrm / np.linalg.norm(nrm, axis=1)[:, None]
+                ctr = m.coords[m.cells[cells]].mean(axis=1)
+                flip = np.einsum("ni,ni->n", nrm, f0 - ctr) < 0
+                nrm[flip] *= -1.0
+                for j in range(d):
+                    v = fv[fs, j]
+                    cand_v.append(v)
+                    cand_pos.append(m.coords[v])
+                    cand_n.append(nrm)
+                    cand_vol.append(meas)
+                    cand_key.append(fs * 2 + side)
+            v = np.concatenate(cand_v)
+            pos = np.concatenate(cand_pos)
+            nr = np.concatenate(cand_n)
+            fvol = np.concatenate(cand_vol)
+            key = np.concatenate(cand_key)
+            if kind == "skeleton":
+                keep = ~bverts[v]
+                v, pos, nr, fvol, key = v[keep], pos[keep], nr[keep], fvol[keep], key[keep]
+            if v.size == 0:
+                continue
+            env = {"time": float("nan"), "integration_factor": 0.0, "in_volume": 0.0,
+                   "in_boundary": flags[0], "in_skeleton": flags[1], "no_value": np.finfo(float).max,
+                   "entity_volume": fvol}
+            for j in range(3):
+                env["position_" + AXES[j]] = pos[:, j] if j < d else 0.0
+                env["normal_" + AXES[j]] = nr[:, j] if j < d else 0.0
+            val = np.broadcast_to(np.asarray(ex(env), float), v.shape).copy()
+            ok = val != np.finfo(float).max
+            v, val, key = v[ok], val[ok], key[ok]
+            order = np.lexsort((key, v))                     # by vertex, then face order
+            v, val = v[order], val[order]
+            first = np.ones(v.shape[0], bool)
+            first[1:] = v[1:] != v[:-1]
+            dofs.append(self.dof(sp_, v[first]))
+            vals.append(val[first])
+        if dofs:
+            dd = np.concatenate(dofs)
+            vv = np.concatenate(vals)
+            # a species may carry both kinds: the boundary entry comes first and wins
+            order = np.argsort(dd, kind="stable")
+            dd, vv = dd[order], vv[order]
+            first = np.ones(dd.shape[0], bool)
+            first[1:] = dd[1:] != dd[:-1]
+            self.cons_dofs = dd[first]
+            self.cons_vals = vv[first]
+
+    def apply_constraints(self, x):
+        """x with the constrained entries set to their values (a copy)."""
+        if self.cons_dofs.size == 0:
+            return x
+        x = x.copy()
+        x[self.cons_dofs] = self.cons_vals
+        return x
+
+    def _constrain_residual(self, r):
+        if self.cons_dofs.size:
+            r[self.cons_dofs] = 0.0
+        return r
+
+    def _constrain_jacobian(self, J):
+        """Constrained rows become unit rows."""
+        if self.cons_dofs.size == 0:
+            return J
+        J = J.tocsr(copy=True)
+        mask = np.zeros(self.ndof, bool)
+        mask[self.cons_dofs] = True
+        rows = np.repeat(np.arange(self.ndof), np.diff(J.indptr))
+        J.data[mask[rows]] = 0.0
+        J = J + sp.csr_matrix((np.ones(self.cons_dofs.size), (self.cons_dofs, self.cons_dofs)),
+                              shape=J.shape)
+        return J
 
     # ---------------------------------------------------------------- state helpers
     def initial_state(self):
@@ -603,7 +738,7 @@ class OracleModel:
                     r += ai * self.residual(y, ti, "mass")
                 if bi != 0.0:
                     r += bi * self.residual(y, ti, "stiffness")
-                return r
+                return self._constrain_residual(r)
 
             def jac(y, ai=ai, bi=bi, ti=ti):
                 J = sp.csr_matrix((self.ndof, self.ndof))
@@ -611,8 +746,11 @@ class OracleModel:
                     J = J + ai * self.jacobian(y, ti, "mass")
                 if bi != 0.0:
                     J = J + bi * self.jacobian(y, ti, "stiffness")
-                return J
+                return self._constrain_jacobian(J)
 
+            # constrained entries take their values before the stage solve; their residual
+            # rows are zero and their Jacobian rows unit rows, so the solve keeps them
+            x = self.apply_constraints(x)
             if self.is_linear:
                 x = self._linear_solve_step(res, jac, x, stats)
             else:

@@ -137,3 +137,101 @@ time_step_max = 0.1
 [model.time_step_operator.nonlinear_solver]
 convergence_condition.relative_tolerance = 1e-16
 """
+
+# Poisson problem with a quadratic exact solution: -div(grad u) = -2 dim, u = |x|^2 on the
+# boundary (constrain.boundary), linear model, one implicit Euler step; P1 on the Kuhn
+# split is nodally exact for it.
+POISSON_INI = """
+[grid]
+dimension = 2
+cells = 12 12
+
+[compartments.domain]
+expression = 1
+
+[parser_context.dim]
+type = constant
+value = 2
+
+[model]
+is_linear = true
+
+[model.scalar_field.u]
+compartment = domain
+initial.expression = 0
+cross_diffusion.u.expression = 1
+reaction.expression = -2*dim
+constrain.boundary.expression = in_boundary ? position_x^2 + position_y^2 + position_z^2 : no_value
+
+[model.time_step_operator]
+type = ImplicitEuler
+time_end = 0.1
+time_step_initial = 0.1
+time_step_max = 0.1
+"""
+
+# Two compartments, two species each: the left part of the outer boundary held by a
+# constrain.boundary expression that also reads normal and face measure, interior vertices
+# of a strip held by constrain.skeleton, one species whose constraint is the zero literal
+# (no constraint at all), a transient nonlinear model stepped with Alexander2.
+CONSTRAINED_INI = """
+[grid]
+dimension = 2
+cells = 10 10
+
+[compartments]
+left.expression = position_x < 0.6
+right.expression = position_x >= 0.6
+
+[model.scalar_field.a]
+compartment = left
+initial.expression = 0.2 + position_y
+storage.expression = 1
+cross_diffusion.a.expression = 0.05
+reaction.expression = -a*b
+reaction.jacobian.a.expression = -b
+reaction.jacobian.b.expression = -a
+constrain.boundary.expression = position_x < 1e-12 ? 1 + position_y + 0*normal_x + 0*entity_volume : no_value
+outflow.right.expression = 0.3*(a - c)
+outflow.right.jacobian.a.expression = 0.3
+outflow.right.jacobian.c.expression = -0.3
+
+[model.scalar_field.b]
+compartment = left
+initial.expression = 0.5
+storage.expression = 1
+cross_diffusion.b.expression = 0.02
+reaction.expression = -a*b
+reaction.jacobian.a.expression = -b
+reaction.jacobian.b.expression = -a
+constrain.skeleton.expression = position_y > 0.45 and position_y < 0.55 ? 0.9 : no_value
+
+[model.scalar_field.c]
+compartment = right
+initial.expression = 0.1
+storage.expression = 1
+cross_diffusion.c.expression = 0.04
+constrain.boundary.expression = 0
+outflow.left.expression = 0.3*(c - a)
+outflow.left.jacobian.c.expression = 0.3
+outflow.left.jacobian.a.expression = -0.3
+
+[model.scalar_field.d]
+compartment = right
+initial.expression = 0.3
+storage.expression = 1
+cross_diffusion.d.expression = 0.01
+reaction.expression = 0.2*c - 0.1*d
+reaction.jacobian.c.expression = 0.2
+reaction.jacobian.d.expression = -0.1
+constrain.boundary.expression = normal_y > 0.5 ? 0.25 + 0*entity_volume : no_value
+
+[model.time_step_operator]
+type = Alexander2
+time_end = 0.2
+time_step_initial = 0.05
+time_step_max = 0.05
+
+[model.time_step_operator.nonlinear_solver]
+convergence_condition.relative_tolerance = 1e-16
+"""

@@ -49,7 +49,32 @@ ALL_CASES = {
     "cross_diffusion_3d": cases.small_3d,
     "features_2d": lambda: (cases.FEATURES_INI, None),
     "features_3d_padded": lambda: (cases.FEATURES_3D_INI, None),
+    "poisson_constrained": lambda: (cases.POISSON_INI, None),
+    "two_compartment_constrained": lambda: (cases.CONSTRAINED_INI, None),
 }
+
+
+@pytest.mark.parametrize("case", ["poisson_constrained", "two_compartment_constrained", "gray_scott"])
+def test_constraints_match_oracle(dcgpu_lib, case):
+    """Same constrained DOFs (exactly) and values (to rounding) as the oracle's reading of
+    constrain.{boundary,skeleton}.expression."""
+    ini, _ = ALL_CASES[case]()
+    om = OracleModel(ini)
+    gm = dcgpu_lib.Model(ini)
+    dofs, vals = gm.constraints()
+    assert np.array_equal(dofs, om.cons_dofs)
+    assert np.allclose(vals, om.cons_vals, rtol=1e-14, atol=1e-15)
+    gm.close()
+
+
+def test_poisson_constrained_is_nodally_exact(dcgpu_lib):
+    ini, _ = ALL_CASES["poisson_constrained"]()
+    gm = dcgpu_lib.Model(ini)
+    gm.evolve(0.1, 0.1)
+    x = gm.state()
+    c = gm.vertex_coords()
+    assert np.abs(x - (c[:, 0] ** 2 + c[:, 1] ** 2)).max() < 1e-9
+    gm.close()
 
 
 @pytest.mark.parametrize("case", sorted(ALL_CASES))
@@ -132,14 +157,40 @@ def test_time_stepping_matches_oracle(dcgpu_lib, case):
 
 
 @pytest.mark.parametrize("case", ["gray_scott", "two_compartment", "cross_diffusion_3d", "features_3d_padded"])
-def test_mixed_precision_matches_oracle(dcgpu_lib, case):
-    """fp32 BiCGSTAB inside fp64 iterative refinement: same tolerance against the fp64 oracle."""
+@pytest.mark.parametrize("fmt", ["auto", "bsr", "sell"])
+def test_mixed_precision_matches_oracle(dcgpu_lib, case, fmt):
+    """fp32 BiCGSTAB inside fp64 iterative refinement, with the fp32 operator in BSR or
+    SELL-32 layout or the tuner's choice: same tolerance against the fp64 oracle."""
     ini, init = ALL_CASES[case]()
-    records = _run_both(dcgpu_lib, ini, init, mixed=True)
+    ov = {"model.time_step_operator.linear_solver.spmv": fmt}
+    records = _run_both(dcgpu_lib, ini, init, mixed=True, overrides=ov)
     for t, errs, n_o, n_g, stages in records:
         for name, e in errs.items():
             assert e <= STEP_TOL, (case, t, name, e)
         assert abs(n_o - n_g) <= max(1, stages)
+
+
+def test_spmv_tuner_reports_choice(dcgpu_lib):
+    """linear_solver.spmv = auto: both layouts are timed on the first fp32 operator and the
+    faster one is kept; forced layouts are reported as given and not timed."""
+    ini, init = cases.small_gray_scott()
+    gm = dcgpu_lib.Model(ini)
+    assert gm.spmv_format()["format"] == "auto"
+    gm.set_mixed_precision(True)
+    gm.step(1.0)
+    f = gm.spmv_format()
+    assert f["format"] in ("bsr", "sell")
+    assert f["bsr_us"] > 0 and f["sell_us"] > 0
+    assert (f["format"] == "sell") == (f["sell_us"] < f["bsr_us"])
+    gm.close()
+    gm = dcgpu_lib.Model(ini, {"model.time_step_operator.linear_solver.spmv": "sell"})
+    gm.set_mixed_precision(True)
+    gm.step(1.0)
+    f = gm.spmv_format()
+    assert f["format"] == "sell" and f["bsr_us"] == 0 and f["sell_us"] == 0
+    gm.close()
+    with pytest.raises(dcgpu_lib.DcError):
+        dcgpu_lib.Model(ini, {"model.time_step_operator.linear_solver.spmv": "csr"})
 
 
 @pytest.mark.parametrize("case", ["gray_scott", "two_compartment", "cross_diffusion_3d", "features_3d_padded"])

@@ -310,3 +310,36 @@ convergence_condition.relative_tolerance = 1e-20
     a = m.species_values(x, "a")
     b = m.species_values(x, "b")
     assert a.max() < 1.0 and b.max() > 0.0
+
+
+def test_poisson_constraints_nodally_exact():
+    """constrain.boundary holds |x|^2 on the boundary of -lap u = -4; P1 on the Kuhn split
+    reproduces the quadratic at the vertices (the reference's poisson test checks the L2
+    error only, against a loose threshold)."""
+    import cases
+    om = OracleModel(cases.POISSON_INI)
+    assert om.cons_dofs.size == 4 * 12
+    x, t, *_ = om.run()
+    c = om.mesh.coords
+    assert t == pytest.approx(0.1)
+    assert np.abs(x - (c[:, 0] ** 2 + c[:, 1] ** 2)).max() < 1e-12
+
+
+def test_constraint_selection_rules():
+    """Boundary faces of a compartment include its interface; skeleton constraints skip
+    vertices on any boundary face; the zero literal is no constraint; constrained values
+    are held through the time steps."""
+    import cases
+    om = OracleModel(cases.CONSTRAINED_INI)
+    counts = {}
+    for sp_ in om.species:
+        d = om.dof(sp_, om.comp_vertices[sp_.comp])
+        counts[sp_.name] = int(np.isin(d, om.cons_dofs).sum())
+    assert counts == {"a": 11, "b": 5, "c": 0, "d": 5}
+    sp_a = next(s for s in om.species if s.name == "a")
+    va = om.comp_vertices[sp_a.comp]
+    da = om.dof(sp_a, va)
+    held = np.isin(da, om.cons_dofs)
+    assert np.allclose(om.mesh.coords[va[held], 0], 0.0)
+    x, t, *_ = om.run()
+    assert np.array_equal(x[om.cons_dofs], om.cons_vals)

@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--workload", default="gray_scott", choices=["gray_scott", "cross_diffusion_3d"],
                     help="gray_scott (headline, n = grid edge) or cross_diffusion_3d (n = cube edge)")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--spmv", default="auto", choices=["auto", "bsr", "sell"],
+                    help="layout of the fp32 Krylov operator (linear_solver.spmv)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--large-n", type=int, default=128,
                     help="cube edge of the HBM-resident SpMV measurement (0 disables it)")
@@ -228,13 +230,13 @@ def run_serving(dcgpu, n_requests, lam, max_active, precision, seed=20261203, bu
             "mix": "2D N log-U[32,160] / 3D N log-U[12,32], 1-2 compartments, 1-8 species, 10-40 IE steps"}
 
 
-def large_spmv(dcgpu, precision, peak_gbs, n=128):
+def large_spmv(dcgpu, precision, peak_gbs, n=128, spmv="auto"):
     """SpMV roofline on an operator far larger than L2: the 3D cross-diffusion workload
     (n^3 cubes x 6 tetrahedra, 3 species, ~6.4 M DOF at n = 128), one Alexander2 step with
     per-kernel events; returns the fused-SpMV achieved bandwidth against the HBM peak."""
     import workloads as W
     ini, init = W.cross_diffusion_3d(n=n, steps=1, dt=0.01)
-    m = dcgpu.Model(ini)
+    m = dcgpu.Model(ini, {"model.time_step_operator.linear_solver.spmv": spmv})
     if precision == "mixed":
         m.set_mixed_precision(True)
     m.set_state(m.seeded_state(init), 0.0)
@@ -294,7 +296,7 @@ def main():
         dist.init_process_group("gloo")
 
     ini, init, dt0, wdesc = make_workload(args.n, args.workload)
-    model = dcgpu.Model(ini)
+    model = dcgpu.Model(ini, {"model.time_step_operator.linear_solver.spmv": args.spmv})
     if args.precision == "mixed":
         model.set_mixed_precision(True)
     x0 = model.seeded_state(init)
@@ -405,7 +407,7 @@ def main():
         cpu = cpu_baseline(ini, init, dt0, wdesc)
     roof["spmv_layout"] = model.spmv_format()
     if args.large_n > 0:
-        roof["spmv_hbm_resident"] = large_spmv(dcgpu, args.precision, peak_gbs, args.large_n)
+        roof["spmv_hbm_resident"] = large_spmv(dcgpu, args.precision, peak_gbs, args.large_n, args.spmv)
     serving = None
     if args.serve_requests > 0:
         serving = {"concurrent": run_serving(dcgpu, args.serve_requests, 50.0, 8, args.precision),

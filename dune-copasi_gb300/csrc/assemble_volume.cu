@@ -43,6 +43,25 @@ __device__ __forceinline__ double phi(int q, int a) {
   return Rule<DIM>::xi(q, a - 1);
 }
 
+// Both rules have one point per vertex: point q carries the large barycentric weight
+// alpha at vertex vertex_of<DIM>(q) and beta elsewhere, so phi_a(q) phi_b(q) =
+// beta^2 + beta (alpha - beta) ([a = v(q)] + [b = v(q)]) + (alpha - beta)^2 [a = b = v(q)].
+// A mass-type element matrix sum_q c_q phi_a(q) phi_b(q) is then
+// beta^2 S + k1 (c_a + c_b) + [a = b] k2 c_a with S = sum_q c_q and c_a the weight of the
+// point at vertex a: two additions per entry instead of NQ multiply-adds.
+template <int DIM>
+__device__ __forceinline__ constexpr int point_of_vertex(int a) {
+  // 2D: points 0, 1, 2 sit at vertices 1, 2, 0; 3D: point q at vertex q
+  return DIM == 2 ? (a == 0 ? 2 : a - 1) : a;
+}
+template <int DIM> struct MassConst;
+template <> struct MassConst<2> {
+  static constexpr double alpha = 2.0 / 3.0, beta = 1.0 / 6.0;
+};
+template <> struct MassConst<3> {
+  static constexpr double alpha = 0.5854101966249685, beta = 0.1381966011250105;
+};
+
 template <int DIM, int NS>
 __device__ __forceinline__ double volume_input(uint16_t id, const double (&u)[NS],
                                                const double (&g)[NS][DIM], const double (&xq)[DIM],
@@ -359,18 +378,36 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
       const Term T = P.jac_terms[t];
       const int te = T.test;
       const int tr = (T.kind == J_STORAGE_SELF || T.kind == J_VELOCITY) ? T.test : T.trial;
+      if (T.kind == J_MASS || T.kind == J_MASS_U || T.kind == J_STORAGE_SELF) {
+        constexpr double al = MassConst<DIM>::alpha, be = MassConst<DIM>::beta;
+        constexpr double k1 = be * (al - be), k2 = (al - be) * (al - be);
+        double S = 0.0, ta[NL], ca[NL];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) S += coef[T.coef + q];
+#pragma unroll
+        for (int a = 0; a < NL; ++a) {
+          ca[a] = coef[T.coef + point_of_vertex<DIM>(a)];
+          ta[a] = k1 * ca[a];
+        }
+        const double base = (be * be) * S;
+#pragma unroll
+        for (int a = 0; a < NL; ++a) {
+          P.J[static_cast<int64_t>(blk[a][a]) * bs2 + te * bs + tr] += base + 2.0 * ta[a] + k2 * ca[a];
+#pragma unroll
+          for (int b = a + 1; b < NL; ++b) {
+            const double v = base + ta[a] + ta[b];
+            P.J[static_cast<int64_t>(blk[a][b]) * bs2 + te * bs + tr] += v;
+            P.J[static_cast<int64_t>(blk[b][a]) * bs2 + te * bs + tr] += v;
+          }
+        }
+        continue;
+      }
 #pragma unroll
       for (int a = 0; a < NL; ++a) {
 #pragma unroll
         for (int b = 0; b < NL; ++b) {
           double v = 0.0;
           switch (T.kind) {
-            case J_MASS:
-            case J_MASS_U:
-            case J_STORAGE_SELF:
-#pragma unroll
-              for (int q = 0; q < NQ; ++q) v += coef[T.coef + q] * (phi<DIM>(q, a) * phi<DIM>(q, b));
-              break;
             case J_DIFF_SCALAR: {
               double gg = 0.0;
 #pragma unroll

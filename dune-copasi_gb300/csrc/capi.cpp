@@ -456,6 +456,32 @@ int dc_profile_get(const dc_model* model, double* ms, int64_t* calls, int32_t n_
   });
 }
 
+int dc_reduce(const dc_model* model, const char* reduce_ini, dc_reduce_value* out, size_t n, size_t* n_out) {
+  return guarded([&] {
+    if (!model || !n_out) throw std::invalid_argument("null argument");
+    const auto& m = *model->model;
+    dcgpu::Ini sec;
+    if (reduce_ini) {
+      dcgpu::Ini t = dcgpu::Ini::parse(reduce_ini);
+      sec = t.has_sub("model.reduce") ? t.sub("model.reduce") : t;
+    } else {
+      sec = m.cfg.sub("model").sub("reduce");
+    }
+    *n_out = sec.sub_keys().size();
+    if (!out) return DC_OK;
+    if (n < *n_out) throw std::invalid_argument("output array too small");
+    auto res = m.reduce(model->solver->state_device(), model->solver->time(), sec, model->stream);
+    for (size_t k = 0; k < res.size(); ++k) {
+      std::memset(out[k].key, 0, sizeof(out[k].key));
+      std::strncpy(out[k].key, res[k].key.c_str(), sizeof(out[k].key) - 1);
+      out[k].value = res[k].value;
+      out[k].error = res[k].error ? 1 : 0;
+      out[k].warn = res[k].warn ? 1 : 0;
+    }
+    return DC_OK;
+  });
+}
+
 int dc_spmv_format(const dc_model* model, int32_t* format, double* bsr_us, double* sell_us) {
   return guarded([&] {
     if (!model || !format) throw std::invalid_argument("null argument");

@@ -482,21 +482,60 @@ int ProgramBuilder::add_output(int node) {
 
 Program ProgramBuilder::finish() const {
   Program p;
-  const int n = static_cast<int>(nodes_.size());
+  // Divisions that share a non-constant divisor (Vmax*s/(Km+s) next to its derivative
+  // Vmax*Km/(Km+s)^2 ...) take one reciprocal and multiply: a FP64 division costs a
+  // reciprocal plus refinement, a multiplication one FMA-pipe instruction.  a*(1/d) is
+  // within 1.5 ulp of a/d.
+  std::vector<int> div_uses(nodes_.size(), 0);
+  for (const Node& nd : nodes_)
+    if (nd.op == OP_DIV && nd.b >= 0 && !is_constant(nd.b, nullptr)) ++div_uses[nd.b];
+  std::vector<Node> nodes;
+  nodes.reserve(nodes_.size() + 8);
+  std::vector<int> remap(nodes_.size(), -1), rcp_of(nodes_.size(), -1);
+  auto mapped = [&](int k) { return k >= 0 ? remap[k] : -1; };
+  for (size_t i = 0; i < nodes_.size(); ++i) {
+    Node nd = nodes_[i];
+    if (nd.op == OP_DIV && nd.b >= 0 && div_uses[nd.b] >= 2) {
+      if (rcp_of[nd.b] < 0) {
+        Node r;
+        r.op = OP_RECIP;
+        r.a = remap[nd.b];
+        r.b = -1;
+        r.c = -1;
+        nodes.push_back(r);
+        rcp_of[nd.b] = static_cast<int>(nodes.size()) - 1;
+      }
+      Node m;
+      m.op = OP_MUL;
+      m.a = remap[nd.a];
+      m.b = rcp_of[nd.b];
+      m.c = -1;
+      nodes.push_back(m);
+    } else {
+      nd.a = mapped(nd.a);
+      nd.b = mapped(nd.b);
+      nd.c = mapped(nd.c);
+      nodes.push_back(nd);
+    }
+    remap[i] = static_cast<int>(nodes.size()) - 1;
+  }
+  std::vector<int> outputs;
+  for (int o : outputs_) outputs.push_back(remap[o]);
+  const int n = static_cast<int>(nodes.size());
   // live range ends
   std::vector<int> last(n, -1);
   for (int i = 0; i < n; ++i) {
-    const Node& nd = nodes_[i];
+    const Node& nd = nodes[i];
     for (int k : {nd.a, nd.b, nd.c})
       if (k >= 0) last[k] = std::max(last[k], i);
   }
-  for (int o : outputs_) last[o] = n;  // outputs stay live to the end
+  for (int o : outputs) last[o] = n;  // outputs stay live to the end
   // reachable nodes only
   std::vector<char> need(n, 0);
-  for (int o : outputs_) need[o] = 1;
+  for (int o : outputs) need[o] = 1;
   for (int i = n - 1; i >= 0; --i) {
     if (!need[i]) continue;
-    const Node& nd = nodes_[i];
+    const Node& nd = nodes[i];
     for (int k : {nd.a, nd.b, nd.c})
       if (k >= 0) need[k] = 1;
   }
@@ -505,9 +544,9 @@ Program ProgramBuilder::finish() const {
   int nregs = 0;
   // inputs first, in registers 0..
   for (int i = 0; i < n; ++i) {
-    if (need[i] && nodes_[i].op == 255) {
+    if (need[i] && nodes[i].op == 255) {
       reg[i] = nregs++;
-      p.inputs.push_back(nodes_[i].input);
+      p.inputs.push_back(nodes[i].input);
     }
   }
   // simple linear scan: expire operands whose last use is this node
@@ -516,7 +555,7 @@ Program ProgramBuilder::finish() const {
     if (need[i] && last[i] >= 0 && last[i] < n) expire[last[i]].push_back(i);
   for (int i = 0; i < n; ++i) {
     if (!need[i]) continue;
-    const Node& nd = nodes_[i];
+    const Node& nd = nodes[i];
     if (nd.op == 255) continue;
     // operands that die here can give their register to the result
     for (int k : expire[i])
@@ -544,7 +583,7 @@ Program ProgramBuilder::finish() const {
     }
     p.code.push_back(ins);
   }
-  for (int o : outputs_) p.outputs.push_back(static_cast<uint8_t>(reg[o]));
+  for (int o : outputs) p.outputs.push_back(static_cast<uint8_t>(reg[o]));
   p.nregs = nregs;
   return p;
 }

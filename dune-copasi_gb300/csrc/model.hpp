@@ -73,6 +73,13 @@ class DeviceBuffer {
   size_t n_ = 0;
 };
 
+struct ReduceResult {
+  std::string key;
+  double value = 0.0;
+  bool error = false;
+  bool warn = false;
+};
+
 struct SpeciesInfo {
   std::string name;
   int comp = 0;   // compartment index
@@ -180,6 +187,11 @@ class Model {
   void apply_constraints(double* x, cudaStream_t s) const;   // x[idx] = val
   void constrain_residual(double* r, cudaStream_t s) const;  // r[idx] = 0
   void constrain_jacobian(double* J, cudaStream_t s) const;  // unit rows
+
+  // transform/reduce operators of a reduce section on the blocked state x (device)
+  std::vector<ReduceResult> reduce(const double* x, double t, const Ini& reduce_cfg, cudaStream_t s) const;
+  mutable DeviceBuffer<int32_t> d_red_cells, d_red_nodes, d_red_comp;
+  mutable DeviceBuffer<int8_t> d_red_spc, d_red_spl;
 
   // host-side helpers
   std::vector<double> initial_state() const;        // reference DOF order

@@ -68,6 +68,7 @@ class Solver {
   void set_state(const std::vector<double>& ref, double t);
   std::vector<double> get_state() const;
   double time() const { return t_; }
+  const double* state_device() const { return x_.get(); }  // blocked state
   const double* device_state() const { return x_.get(); }
   double* device_state() { return x_.get(); }
 

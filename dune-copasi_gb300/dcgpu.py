@@ -34,8 +34,13 @@ EXPORTED = [
     "dc_expr_eval", "dc_stream_handle", "dc_launch_count", "dc_profile_enable", "dc_profile_get",
     "dc_assemble_residual_noalloc", "dc_server_create", "dc_server_submit", "dc_server_poll",
     "dc_server_take_state", "dc_server_estimate", "dc_server_destroy", "dc_last_error",
-    "dc_spmv_format", "dc_vertex_coords", "dc_constraints",
+    "dc_spmv_format", "dc_vertex_coords", "dc_constraints", "dc_reduce",
 ]
+
+
+class ReduceValue(ctypes.Structure):
+    _fields_ = [("key", ctypes.c_char * 64), ("value", ctypes.c_double), ("error", ctypes.c_int32),
+                ("warn", ctypes.c_int32)]
 
 
 class DcError(RuntimeError):
@@ -122,6 +127,7 @@ def load_library(path=LIB_PATH):
     lib.dc_spmv_format.argtypes = [vp, P(i32), pd, pd]
     lib.dc_vertex_coords.argtypes = [vp, pd, sz]
     lib.dc_constraints.argtypes = [vp, P(ctypes.c_int64), pd, sz, P(sz)]
+    lib.dc_reduce.argtypes = [vp, ctypes.c_char_p, P(ReduceValue), sz, P(sz)]
     lib.dc_last_error.argtypes = []
     lib.dc_last_error.restype = ctypes.c_char_p
     for name in EXPORTED:
@@ -237,6 +243,24 @@ class Model:
         out = np.empty((self.info["n_vertices"], self.info["dim"]))
         _check(self._lib.dc_vertex_coords(self._h, _ptr(out), out.size))
         return out
+
+    def reduce(self, reduce_ini=None):
+        """Transform/reduce operators on the current state: ({key: value}, [error keys],
+        [warning keys]); reduce_ini None uses the model's [model.reduce] section."""
+        text = reduce_ini.encode() if reduce_ini is not None else None
+        n = ctypes.c_size_t(0)
+        _check(self._lib.dc_reduce(self._h, text, None, 0, ctypes.byref(n)))
+        arr = (ReduceValue * max(n.value, 1))()
+        _check(self._lib.dc_reduce(self._h, text, arr, n.value, ctypes.byref(n)))
+        vals, errs, warns = {}, [], []
+        for k in range(n.value):
+            key = arr[k].key.decode()
+            vals[key] = arr[k].value
+            if arr[k].error:
+                errs.append(key)
+            elif arr[k].warn:
+                warns.append(key)
+        return vals, errs, warns
 
     def constraints(self):
         """(reference DOF indices, values) of the Dirichlet constraints, sorted by DOF."""

@@ -143,6 +143,21 @@ int64_t dc_launch_count(void);
 int dc_profile_enable(dc_model* model, int enabled);
 int dc_profile_get(const dc_model* model, double* ms, int64_t* calls, int32_t n_categories);
 
+/* Transform/reduce operators on the current state (replaces Model::reduce,
+ * dune/copasi/model/model.hh:24-101, implemented in model/diffusion_reaction/reduce.hh:40-285).
+ * reduce_ini: ini text holding a [model.reduce] section or the section's keys at top level
+ * ("mass.evaluation.expression = u*integration_factor" ...); NULL uses the model's own
+ * [model.reduce].  *n_out receives the number of keys; with out non-null (n >= *n_out) the
+ * results are written in key order.  A key whose error.expression evaluates non-zero has
+ * error = 1 (the reference then throws ReductionError); warn likewise for warn.expression. */
+typedef struct dc_reduce_value {
+  char key[64];
+  double value;
+  int32_t error;
+  int32_t warn;
+} dc_reduce_value;
+int dc_reduce(const dc_model* model, const char* reduce_ini, dc_reduce_value* out, size_t n, size_t* n_out);
+
 /* Layout of the single-precision Krylov operator (no reference counterpart): -1 = not yet
  * chosen, 0 = BSR with a thread per scalar row, 1 = SELL-32 with a warp per 32 block rows.
  * `linear_solver.spmv = auto` (default) times both on the first fp32 operator and keeps the

@@ -42,6 +42,36 @@ def element_rule(dim):
     return pts, w
 
 
+def reduce_rule(dim):
+    """Rule of the reduce operators, which ask dune-geometry for order 4 (reduce.hh:179-180).
+
+    dune-geometry's tables are not available here; these are symmetric rules whose orbit
+    parameters solve the moment equations: triangles, 6 points (two (a, a, 1-2a) orbits),
+    exact to degree 4; tetrahedra, 14 points (two (a, a, a, 1-3a) orbits and one
+    (b, b, 1/2-b, 1/2-b) orbit), exact to degree 5.  Points are listed by barycentric
+    coordinates (lambda_0..lambda_d); returns (reference points [nq, d], weights summing
+    to the reference volume).
+    """
+    if dim == 2:
+        a1, a2 = 0.4459484909159645, 0.09157621350977077
+        w1, w2 = 0.11169079483900554, 0.05497587182766112
+        bary = []
+        for a in (a1, a2):
+            bary += [[a, a, 1 - 2 * a], [a, 1 - 2 * a, a], [1 - 2 * a, a, a]]
+        w = [w1] * 3 + [w2] * 3
+    else:
+        a1, a2, b = 0.0927352503108912, 0.3108859192633006, 0.0455037041256496
+        w1, w2, w3 = 0.01224884051939366, 0.01878132095300264, 0.007091003462846911
+        bary = []
+        for a in (a1, a2):
+            bary += [[a, a, a, 1 - 3 * a], [a, a, 1 - 3 * a, a], [a, 1 - 3 * a, a, a], [1 - 3 * a, a, a, a]]
+        c = 0.5 - b
+        bary += [[b, b, c, c], [b, c, b, c], [b, c, c, b], [c, b, b, c], [c, b, c, b], [c, c, b, b]]
+        w = [w1] * 4 + [w2] * 4 + [w3] * 6
+    bary = np.array(bary)
+    return bary[:, 1:].copy(), np.array(w)
+
+
 def face_rule(dim):
     """Rule on the reference face (dim-1 simplex)."""
     if dim == 2:

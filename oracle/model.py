@@ -378,6 +378,100 @@ class OracleModel:
             x[self.dof(sp_, verts)] = val
         return x
 
+    def reduce(self, x, t, cfg=None):
+        """Transform/reduce operators, model/diffusion_reaction/reduce.hh:40-285.
+
+        For every key of the [model.reduce] section (or `cfg`): value = initial.value
+        (default 0); then, over every cell in grid order and every point of the order-4 rule
+        (F.reduce_rule), value = reduction(evaluation, value) with reduction the user
+        function `init, val: ...` (default: +).  The per-thread value is then combined with
+        initial.value once more (reduce.hh:237-241, one thread), transformation `arg: ...`
+        is applied, and error `arg: ...` / warn `arg: ...` flag the key when non-zero.
+        Variables: species values and gradients (0 for species whose compartment does not
+        contain the cell), position_*, integration_factor = weight x |det J|, time,
+        entity_volume = cell volume, in_volume = 1.
+        Returns ({key: value}, [error keys], [warning keys]).
+        """
+        if cfg is None:
+            if not self.mcfg.has_sub("reduce"):
+                return {}, [], []
+            cfg = self.mcfg.sub("reduce")
+        keys = cfg.sub_keys()
+        if not keys:
+            return {}, [], []
+        m = self.mesh
+        d = self.dim
+        qp, qw = F.reduce_rule(d)
+        phi = F.p1_values(qp)                                     # [nq, nl]
+        nq = qw.shape[0]
+        xq = self.v0[:, None, :] + np.einsum("nij,qj->nqi", self.B, qp)
+        env = {"time": t, "integration_factor": np.abs(self.det)[:, None] * qw[None, :],
+               "entity_volume": np.repeat(self.vol[:, None], nq, axis=1), "in_volume": 1.0,
+               "in_boundary": 0.0, "in_skeleton": 0.0, "no_value": np.finfo(float).max}
+        for j in range(3):
+            env["position_" + AXES[j]] = xq[:, :, j] if j < d else 0.0
+        for sp_ in self.species:
+            inside = self.comp_mask[sp_.comp]
+            vloc = self.comp_vloc[sp_.comp]
+            cells = m.cells
+            ok = inside & np.all(vloc[cells] >= 0, axis=1)
+            c = np.zeros(cells.shape)
+            c[ok] = x[self.comp_offset[sp_.comp] + vloc[cells[ok]] * self.ns[sp_.comp] + sp_.local]
+            env[sp_.name] = c @ phi.T                               # [ne, nq]
+            g = np.einsum("na,naj->nj", c, self.G)                  # [ne, d]
+            for j in range(3):
+                env["grad_%s_%s" % (sp_.name, AXES[j])] = (
+                    np.repeat(g[:, j:j + 1], nq, axis=1) if j < d else 0.0)
+        values, errors, warns = {}, [], []
+        for key in keys:
+            sub = cfg.sub(key)
+            init = sub.get_float("initial.value", 0.0)
+            ev = F._scalar(sub.sub("evaluation"), self.ctx) if sub.has_sub("evaluation") else None
+            vals = (np.zeros((m.ne, nq)) if ev is None
+                    else np.broadcast_to(np.asarray(ev(env), float), (m.ne, nq))).ravel()
+            red = sub.get("reduction.expression") if sub.has_sub("reduction") else None
+            acc = self._fold(red, vals, init)
+            acc = self._fold(red, np.array([acc]), init)             # thread combine
+            for part in ("transformation",):
+                if sub.has_sub(part):
+                    acc = float(self._call1(sub.get(part + ".expression"), acc))
+            if sub.has_sub("error") and self._call1(sub.get("error.expression"), acc) != 0.0:
+                errors.append(key)
+            elif sub.has_sub("warn") and self._call1(sub.get("warn.expression"), acc) != 0.0:
+                warns.append(key)
+            values[key] = acc
+        return values, errors, warns
+
+    def _call1(self, text, arg):
+        f = E.parse_function_definition(text)
+        if len(f.args) != 1:
+            raise ValueError("function must have exactly 1 argument: %r" % text)
+        env = self.ctx.env()
+        env[f.args[0]] = arg
+        return float(E.evaluate(f.body, env, self.ctx.functions))
+
+    def _fold(self, text, vals, init):
+        """acc = f(v, acc) over vals in order, starting from init (f = + by default)."""
+        if text is None:
+            return float(np.cumsum(np.concatenate([[init], vals]))[-1])
+        f = E.parse_function_definition(text)
+        if len(f.args) != 2:
+            raise ValueError("Reduction arguments must be exactly 2")
+        a, b = f.args
+        body = text[text.find(":") + 1:].replace(" ", "")
+        if body in ("%s+%s" % (a, b), "%s+%s" % (b, a)):
+            return float(np.cumsum(np.concatenate([[init], vals]))[-1])
+        for fn, op in (("max", np.max), ("min", np.min)):
+            if body in ("%s(%s,%s)" % (fn, a, b), "%s(%s,%s)" % (fn, b, a)):
+                return float(op(np.concatenate([[init], vals])))
+        acc = init
+        env = self.ctx.env()
+        for v in vals:
+            env[a] = float(v)
+            env[b] = acc
+            acc = float(E.evaluate(f.body, env, self.ctx.functions))
+        return acc
+
     def species_values(self, x, name):
         sp_ = next(s for s in self.species if s.name == name)
         return x[self.dof(sp_, self.comp_vertices[sp_.comp])]

@@ -235,3 +235,48 @@ time_step_max = 0.05
 [model.time_step_operator.nonlinear_solver]
 convergence_condition.relative_tolerance = 1e-16
 """
+
+# transform/reduce operators of the exponential-decay model: an integral, a max with an
+# explicit reduction and initial value, an L2 error with transformation and error check,
+# and a reduction function outside the sum/max/min forms (folded in cell order)
+REDUCE_SECTION = """
+[model.reduce]
+mass.evaluation.expression = u*integration_factor
+umax.evaluation.expression = u
+umax.reduction.expression = acc, val: max(acc, val)
+umax.initial.value = -1e100
+err.evaluation.expression = (u - exp(grow_rate*time))^2 * integration_factor
+err.transformation.expression = e: sqrt(e)
+err.error.expression = e: e > 5e-3
+area.evaluation.expression = integration_factor
+area.warn.expression = a: a > 0.5
+mixed.evaluation.expression = u*position_x + grad_u_x
+mixed.reduction.expression = p, q: q + 0.5*p
+"""
+
+DECAY_INI = """
+[grid]
+dimension = 2
+cells = 6 5
+extensions = 1.2 1
+
+[compartments.domain]
+expression = 1
+
+[parser_context.grow_rate]
+type = constant
+value = -2
+
+[model.scalar_field.u]
+compartment = domain
+initial.expression = 1 + 0.01*position_x*position_y
+storage.expression = 1
+reaction.expression = grow_rate*u
+reaction.jacobian.u.expression = grow_rate
+
+[model.time_step_operator]
+type = ImplicitEuler
+time_end = 0.5
+time_step_initial = 0.1
+time_step_max = 0.1
+""" + REDUCE_SECTION

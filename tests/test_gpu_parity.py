@@ -343,3 +343,41 @@ time_step_max = 0.1
     records = _run_both(dcgpu_lib, ini, None)
     for t, errs, *_ in records:
         assert errs["u"] <= STEP_TOL
+
+
+def test_reduce_matches_oracle(dcgpu_lib):
+    """Transform/reduce operators on the initial state and after the run: sums to 1e-12,
+    max exactly, the general fold and the error/warn flags as the oracle."""
+    ini = cases.DECAY_INI
+    om = OracleModel(ini)
+    gm = dcgpu_lib.Model(ini)
+    for when in ("initial", "final"):
+        if when == "final":
+            x, t, *_ = om.run()
+            gm.evolve(0.5, 0.1)
+        else:
+            x, t = om.initial_state(), 0.0
+        vo, eo, wo = om.reduce(x, t)
+        vg, eg, wg = gm.reduce()
+        assert set(vg) == set(vo)
+        for k in vo:
+            assert vg[k] == pytest.approx(vo[k], rel=1e-10, abs=1e-14), (when, k)
+        assert sorted(eg) == sorted(eo) and sorted(wg) == sorted(wo)
+    # an explicit reduce section on a two-compartment 3D model (gradients, per-compartment species)
+    sec = """
+[model.reduce]
+pmass.evaluation.expression = p*integration_factor
+qgrad.evaluation.expression = (grad_q_x + 2*grad_q_z)*integration_factor
+rmin.evaluation.expression = r + position_y
+rmin.reduction.expression = a, b: min(b, a)
+rmin.initial.value = 1e100
+vol.evaluation.expression = entity_volume*integration_factor
+"""
+    om = OracleModel(cases.FEATURES_3D_INI)
+    gm = dcgpu_lib.Model(cases.FEATURES_3D_INI)
+    from oracle.ini import ParameterTree
+    vo, _, _ = om.reduce(om.initial_state(), 0.0, ParameterTree.from_text(sec).sub("model.reduce"))
+    vg, _, _ = gm.reduce(sec)
+    for k in vo:
+        assert vg[k] == pytest.approx(vo[k], rel=1e-10, abs=1e-14), k
+    gm.close()

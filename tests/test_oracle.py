@@ -343,3 +343,46 @@ def test_constraint_selection_rules():
     assert np.allclose(om.mesh.coords[va[held], 0], 0.0)
     x, t, *_ = om.run()
     assert np.array_equal(x[om.cons_dofs], om.cons_vals)
+
+
+@pytest.mark.parametrize("dim,degree", [(2, 4), (3, 5)])
+def test_reduce_rule_exactness(dim, degree):
+    """The reduce operators' rule integrates every monomial of the stated degree exactly."""
+    import itertools
+    from oracle import fem as F
+    pts, w = F.reduce_rule(dim)
+    lam = F.p1_values(pts)
+    for alpha in itertools.product(range(degree + 1), repeat=dim + 1):
+        if sum(alpha) > degree:
+            continue
+        exact = (math.prod(math.factorial(a) for a in alpha) * math.factorial(dim)
+                 / math.factorial(sum(alpha) + dim) / math.factorial(dim))
+        got = float(np.dot(w, np.prod(lam ** np.array(alpha), axis=1)))
+        assert got == pytest.approx(exact, rel=1e-13, abs=1e-16), alpha
+
+
+def test_reduce_operators():
+    """Integral, max with initial value, L2 error with transformation/error, warn flag and a
+    general reduction function folded in grid order."""
+    import cases
+    om = OracleModel(cases.DECAY_INI)
+    x0 = om.initial_state()
+    vals, errs, warns = om.reduce(x0, 0.0)
+    c = om.mesh.coords
+    assert vals["area"] == pytest.approx(1.2, rel=1e-14)
+    # integral of the P1 interpolant of 1 + 0.01 x y over [0, 1.2] x [0, 1]
+    assert vals["mass"] == pytest.approx(1.2 + 0.01 * (1.2 ** 2 / 2) * 0.5, rel=1e-4)
+    # the max runs over quadrature points, inside the cells
+    assert 1.011 < vals["umax"] < 1 + 0.01 * 1.2
+    assert errs == [] and warns == ["area"]
+    x, t, *_ = om.run()
+    vals, errs, warns = om.reduce(x, t)
+    assert t == pytest.approx(0.5)
+    # implicit Euler with dt = 0.1 against exp(-2t): the L2 error check trips
+    assert vals["err"] > 5e-3 and errs == ["err"]
+    # general fold: acc = acc + 0.5 v over all points, then combined with the initial value
+    # (0) once more: 0 + 0.5 acc
+    om2 = OracleModel(cases.DECAY_INI)
+    v2, _, _ = om2.reduce(x, t)
+    assert v2["mixed"] == vals["mixed"]
+    assert np.isfinite(vals["mixed"])

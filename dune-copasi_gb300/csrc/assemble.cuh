@@ -21,6 +21,13 @@ constexpr int kVolumeNumericalJacobian = 4;
 void launch_volume(int dim, int ns, const VolumeParams& p, int begin, int end, int mode,
                    cudaStream_t stream);
 void launch_faces(int dim, const FaceParams& p, int begin, int end, int mode, cudaStream_t stream);
+// volume assembly is two-phase: k_volume writes per-element outputs (er / ej of
+// VolumeParams), these gathers add them into r / J per node / block in list order
+void launch_gather_residual(double* r, int bs, int ns, int64_t node_begin, int64_t nnodes, const int64_t* ptr,
+                            const int32_t* list, const double* er, cudaStream_t stream);
+void launch_gather_jacobian(double* J, int bs, int nslot, const int32_t* slot_pos, int64_t block_begin,
+                            int64_t nblocks, const int64_t* ptr, const int32_t* list, const double* ej,
+                            cudaStream_t stream);
 // J[diag[i]] block gets identity in the padded slots s >= ns_of_row (rows of compartments
 // with fewer species than the block size)
 void launch_pad_identity(const int32_t* diag, const int8_t* row_ns, int nrows, int bs, double* J,

@@ -360,54 +360,51 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
     }
   }
 
+  // element outputs: residual vector and Jacobian slot values, each written exactly once
+  // (the gather kernels below add them into r and J in a fixed order)
   if (do_res) {
+    double* er = P.er + static_cast<int64_t>(k) * NL * NS;
 #pragma unroll
     for (int a = 0; a < NL; ++a)
 #pragma unroll
-      for (int s = 0; s < NS; ++s) P.r[static_cast<int64_t>(nd[a]) * bs + s] += rl[a][s];
+      for (int s = 0; s < NS; ++s) er[a * NS + s] = rl[a][s];
   }
   if (do_jac) {
-    const int bs2 = bs * bs;
-    const int32_t* bp = P.bpos + static_cast<int64_t>(k) * NL * NL;
-    int blk[NL][NL];
-#pragma unroll
-    for (int a = 0; a < NL; ++a)
-#pragma unroll
-      for (int b = 0; b < NL; ++b) blk[a][b] = bp[a * NL + b];
+    constexpr double al = MassConst<DIM>::alpha, be = MassConst<DIM>::beta;
+    constexpr double k1 = be * (al - be), k2 = (al - be) * (al - be);
+    // mass-type terms: beta^2 S into the spare coefficient slot after the nq point weights
     for (int t = 0; t < P.n_jac_terms; ++t) {
       const Term T = P.jac_terms[t];
-      const int te = T.test;
-      const int tr = (T.kind == J_STORAGE_SELF || T.kind == J_VELOCITY) ? T.test : T.trial;
       if (T.kind == J_MASS || T.kind == J_MASS_U || T.kind == J_STORAGE_SELF) {
-        constexpr double al = MassConst<DIM>::alpha, be = MassConst<DIM>::beta;
-        constexpr double k1 = be * (al - be), k2 = (al - be) * (al - be);
-        double S = 0.0, ta[NL], ca[NL];
+        double S = 0.0;
 #pragma unroll
         for (int q = 0; q < NQ; ++q) S += coef[T.coef + q];
-#pragma unroll
-        for (int a = 0; a < NL; ++a) {
-          ca[a] = coef[T.coef + point_of_vertex<DIM>(a)];
-          ta[a] = k1 * ca[a];
-        }
-        const double base = (be * be) * S;
-#pragma unroll
-        for (int a = 0; a < NL; ++a) {
-          P.J[static_cast<int64_t>(blk[a][a]) * bs2 + te * bs + tr] += base + 2.0 * ta[a] + k2 * ca[a];
-#pragma unroll
-          for (int b = a + 1; b < NL; ++b) {
-            const double v = base + ta[a] + ta[b];
-            P.J[static_cast<int64_t>(blk[a][b]) * bs2 + te * bs + tr] += v;
-            P.J[static_cast<int64_t>(blk[b][a]) * bs2 + te * bs + tr] += v;
-          }
-        }
-        continue;
+        coef[T.coef + NQ] = (be * be) * S;
       }
+    }
+    const int nslot = P.n_slots;
+    double* ej = P.ej + static_cast<int64_t>(k) * NL * NL * nslot;
+    // terms are sorted by slot (distinct test/trial species pair); one store per slot and
+    // local pair.  With only mass-type terms the element matrix is symmetric in (a, b).
 #pragma unroll
-      for (int a = 0; a < NL; ++a) {
+    for (int a = 0; a < NL; ++a) {
 #pragma unroll
-        for (int b = 0; b < NL; ++b) {
+      for (int b = 0; b < NL; ++b) {
+        if (P.all_mass && b < a) continue;
+        int cur = -1;
+        double acc = 0.0;
+        for (int t = 0; t < P.n_jac_terms; ++t) {
+          const Term T = P.jac_terms[t];
           double v = 0.0;
           switch (T.kind) {
+            case J_MASS:
+            case J_MASS_U:
+            case J_STORAGE_SELF: {
+              const double ca = coef[T.coef + point_of_vertex<DIM>(a)];
+              v = coef[T.coef + NQ] + k1 * (ca + coef[T.coef + point_of_vertex<DIM>(b)]);
+              if (a == b) v += k2 * ca;
+              break;
+            }
             case J_DIFF_SCALAR: {
               double gg = 0.0;
 #pragma unroll
@@ -431,11 +428,50 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
               for (int j = 0; j < DIM; ++j) v += coef[T.coef + a * DIM + j] * G[b][j];
               break;
           }
-          P.J[static_cast<int64_t>(blk[a][b]) * bs2 + te * bs + tr] += v;
+          if (T.slot != cur) {
+            if (cur >= 0) {
+              ej[(a * NL + b) * nslot + cur] = acc;
+              if (P.all_mass && a != b) ej[(b * NL + a) * nslot + cur] = acc;
+            }
+            cur = T.slot;
+            acc = 0.0;
+          }
+          acc += v;
+        }
+        if (cur >= 0) {
+          ej[(a * NL + b) * nslot + cur] = acc;
+          if (P.all_mass && a != b) ej[(b * NL + a) * nslot + cur] = acc;
         }
       }
     }
   }
+}
+
+// r[node, s] += sum of the element residual entries of the node's (element, vertex) list
+__global__ void k_gather_residual(double* __restrict__ r, int bs, int ns, int64_t node_begin, int64_t nnodes,
+                                  const int64_t* __restrict__ ptr, const int32_t* __restrict__ list,
+                                  const double* __restrict__ er) {
+  const int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= nnodes * ns) return;
+  const int64_t n = t / ns;
+  const int s = static_cast<int>(t % ns);
+  double acc = 0.0;
+  for (int64_t i = ptr[n]; i < ptr[n + 1]; ++i) acc += er[static_cast<int64_t>(list[i]) * ns + s];
+  r[(node_begin + n) * bs + s] += acc;
+}
+
+// J[block, slot position] += sum of the element Jacobian values of the block's
+// (element, local pair) list
+__global__ void k_gather_jacobian(double* __restrict__ J, int bs2, int nslot, const int32_t* __restrict__ slot_pos,
+                                  int64_t block_begin, int64_t nblocks, const int64_t* __restrict__ ptr,
+                                  const int32_t* __restrict__ list, const double* __restrict__ ej) {
+  const int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= nblocks * nslot) return;
+  const int64_t b = t / nslot;
+  const int m = static_cast<int>(t % nslot);
+  double acc = 0.0;
+  for (int64_t i = ptr[b]; i < ptr[b + 1]; ++i) acc += ej[static_cast<int64_t>(list[i]) * nslot + m];
+  J[(block_begin + b) * bs2 + slot_pos[m]] += acc;
 }
 
 // Local residual of one element for coefficients c (residual terms only, both forms).
@@ -655,6 +691,25 @@ void launch_t(const VolumeParams& p, int begin, int end, int mode, cudaStream_t 
 }
 
 }  // namespace
+
+void launch_gather_residual(double* r, int bs, int ns, int64_t node_begin, int64_t nnodes, const int64_t* ptr,
+                            const int32_t* list, const double* er, cudaStream_t stream) {
+  const int64_t n = nnodes * ns;
+  if (n <= 0) return;
+  count_launches(1);
+  k_gather_residual<<<static_cast<int>((n + 255) / 256), 256, 0, stream>>>(r, bs, ns, node_begin, nnodes, ptr, list,
+                                                                           er);
+}
+
+void launch_gather_jacobian(double* J, int bs, int nslot, const int32_t* slot_pos, int64_t block_begin,
+                            int64_t nblocks, const int64_t* ptr, const int32_t* list, const double* ej,
+                            cudaStream_t stream) {
+  const int64_t n = nblocks * nslot;
+  if (n <= 0) return;
+  count_launches(1);
+  k_gather_jacobian<<<static_cast<int>((n + 255) / 256), 256, 0, stream>>>(J, bs * bs, nslot, slot_pos, block_begin,
+                                                                           nblocks, ptr, list, ej);
+}
 
 void launch_volume(int dim, int ns, const VolumeParams& p, int begin, int end, int mode,
                    cudaStream_t stream) {

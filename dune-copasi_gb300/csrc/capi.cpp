@@ -171,6 +171,14 @@ int dc_state_get(const dc_model* model, double* host_out, size_t n) {
   });
 }
 
+int dc_write_vtk(const dc_model* model, const char* path, int append) {
+  return guarded([&] {
+    if (!model || !path) throw std::invalid_argument("null argument");
+    model->model->write_vtk(model->solver->get_state(), model->solver->time(), path, append != 0);
+    return DC_OK;
+  });
+}
+
 int dc_state_set(dc_model* model, const double* host_in, size_t n, double time) {
   return guarded([&] {
     if (!model || !host_in) throw std::invalid_argument("null argument");

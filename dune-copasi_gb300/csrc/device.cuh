@@ -53,7 +53,7 @@ struct Term {
   uint8_t test;     // local species index (compartment of the element / face side)
   uint8_t trial;    // local species index of the trial / gradient species
   uint8_t side;     // faces: 0 = trial lives on this side, 1 = on the other side
-  uint8_t pad;
+  uint8_t slot;     // volume Jacobian terms: index of the (test, trial) pair in the element output
   uint16_t out;     // first program output
   uint16_t coef;    // Jacobian terms: offset into the per-thread coefficient array
   uint16_t pad2;
@@ -80,6 +80,11 @@ struct VolumeParams {
   int species_offset;        // model-global index of local species 0
   double t, cm, ca;          // time, mass-form scale, stiffness-form scale
   double fd_eps;             // numerical Jacobian: relative perturbation
+  // element outputs of k_volume (gathered into r / J afterwards)
+  double* er;                // residual: (k * nl + a) * ns + s
+  double* ej;                // Jacobian: ((k * nl + a) * nl + b) * n_slots + slot
+  int n_slots;               // distinct (test, trial) pairs of the Jacobian terms
+  int all_mass;              // every Jacobian term is mass-type: symmetric element matrix
 };
 
 struct FaceParams {

@@ -1,7 +1,10 @@
 #include "mesh.hpp"
 
 #include <algorithm>
+#include <fstream>
 #include <numeric>
+#include <sstream>
+#include <unordered_map>
 
 namespace dcgpu {
 
@@ -63,8 +66,82 @@ Mesh make_structured_simplex_mesh(int dim, const std::vector<int>& cells,
   return m;
 }
 
+// Gmsh MSH 2.x ASCII (the format Dune's GmshReader reads, make_multi_domain_grid.hh:66-76):
+// nodes in file order (ids mapped to 0..n-1), the elements of the grid's dimension (type 2
+// triangles, type 4 tetrahedra) in file order, lower-dimensional elements skipped; the first
+// tag of an element is its physical entity, kept as the cell data "gmsh_id".
+Mesh read_gmsh(const std::string& path, int dim) {
+  std::ifstream in(path);
+  if (!in) throw ConfigError("cannot open grid file '" + path + "'");
+  Mesh m;
+  m.dim = dim;
+  std::unordered_map<long, int32_t> idmap;
+  std::vector<double> phys;
+  const int want = dim == 2 ? 2 : 4;
+  std::string line;
+  bool have_nodes = false;
+  while (std::getline(in, line)) {
+    line = trim(line);
+    if (line == "$MeshFormat") {
+      std::getline(in, line);
+      std::istringstream ss(line);
+      std::string ver;
+      int ftype = 1;
+      ss >> ver >> ftype;
+      if (ver.empty() || ver[0] != '2' || ftype != 0) throw ConfigError("only ASCII Gmsh MSH 2.x files are supported");
+    } else if (line == "$Nodes") {
+      std::getline(in, line);
+      const long n = std::stol(line);
+      m.coords.assign(static_cast<size_t>(n) * dim, 0.0);
+      for (long k = 0; k < n; ++k) {
+        std::getline(in, line);
+        std::istringstream ss(line);
+        long id;
+        double xyz[3] = {0, 0, 0};
+        ss >> id >> xyz[0] >> xyz[1] >> xyz[2];
+        if (!ss && !(dim == 2 && ss.eof())) throw ConfigError("malformed node line in '" + path + "'");
+        idmap[id] = static_cast<int32_t>(k);
+        for (int d = 0; d < dim; ++d) m.coords[k * dim + d] = xyz[d];
+      }
+      m.nv = n;
+      have_nodes = true;
+    } else if (line == "$Elements") {
+      std::getline(in, line);
+      const long n = std::stol(line);
+      for (long k = 0; k < n; ++k) {
+        std::getline(in, line);
+        std::istringstream ss(line);
+        long id, typ, ntags;
+        ss >> id >> typ >> ntags;
+        std::vector<long> tags(ntags);
+        for (auto& t : tags) ss >> t;
+        if (typ != want) continue;
+        for (int a = 0; a <= dim; ++a) {
+          long v;
+          ss >> v;
+          auto it = idmap.find(v);
+          if (!ss || it == idmap.end()) throw ConfigError("malformed element line in '" + path + "'");
+          m.cells.push_back(it->second);
+        }
+        phys.push_back(ntags > 0 ? static_cast<double>(tags[0]) : 0.0);
+      }
+    }
+  }
+  if (!have_nodes || phys.empty())
+    throw ConfigError("grid file '" + path + "' has no nodes or no " + std::to_string(dim) + "D elements");
+  m.ne = static_cast<int64_t>(phys.size());
+  m.cell_data["gmsh_id"] = phys;
+  return m;
+}
+
 Mesh make_mesh_from_config(const Ini& grid) {
-  if (grid.has_key("path")) throw ConfigError("Gmsh grid files are not supported (grid.path)");
+  if (grid.has_key("path")) {
+    const int dim = static_cast<int>(grid.get_long("dimension", 2));
+    if (dim != 2 && dim != 3) throw ConfigError("only grid.dimension 2 or 3 is supported");
+    if (grid.get_long("refinement_level", 0) != 0)
+      throw ConfigError("grid.refinement_level is not supported together with grid.path");
+    return read_gmsh(grid.get("path", ""), dim);
+  }
   int dim = 2;
   if (grid.has_key("dimension")) dim = static_cast<int>(grid.get_long("dimension", 2));
   else if (grid.has_key("extensions")) dim = static_cast<int>(grid.get_doubles("extensions", {}).size());

@@ -10,6 +10,7 @@
 #pragma once
 
 #include <cstdint>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -24,7 +25,10 @@ struct Mesh {
   std::vector<double> coords;    // nv * dim
   std::vector<int32_t> cells;    // ne * (dim + 1)
   std::vector<int> cells_per_axis;
+  // per-cell data visible to compartment expressions ("gmsh_id" of Gmsh grids)
+  std::map<std::string, std::vector<double>> cell_data;
 };
+Mesh read_gmsh(const std::string& path, int dim);
 
 Mesh make_structured_simplex_mesh(int dim, const std::vector<int>& cells,
                                   const std::vector<double>& origin,

@@ -153,13 +153,19 @@ void Model::build_static_matrices() {
     p.bs = bs;
     p.species_offset = species_offset[g.comp];
     p.t = 0.0;
+    p.er = d_er.get();
+    p.ej = d_ej.get();
+    p.n_slots = g.slots_static;
+    p.all_mass = g.static_all_mass ? 1 : 0;
     for (int form = 0; form < 2; ++form) {
       if ((form == 0 && !g.static_mass) || (form == 1 && !g.static_stiffness)) continue;
-      p.J = form == 0 ? d_Ms.get() : d_Ks.get();
+      double* target = form == 0 ? d_Ms.get() : d_Ks.get();
+      p.J = target;
       p.cm = form == 0 ? 1.0 : 0.0;
       p.ca = form == 0 ? 0.0 : 1.0;
-      for (size_t k = 0; k + 1 < g.color_offsets.size(); ++k)
-        launch_volume(dim, g.ns, p, g.color_offsets[k], g.color_offsets[k + 1], 2, nullptr);
+      launch_volume(dim, g.ns, p, 0, static_cast<int>(g.ne), 2, nullptr);
+      launch_gather_jacobian(target, bs, g.slots_static, g.slot_pos_static.get(), g.block_begin, g.nblocks,
+                             g.blist_ptr.get(), g.blist.get(), d_ej.get(), nullptr);
     }
   }
   // Every set-up copy, memset and kernel of the model went to the legacy default stream,
@@ -181,6 +187,8 @@ void Model::build_species() {
     std::string type = sub.get("type", "expression");
     if (type != "expression") throw ConfigError("Not know type '" + type + "' of compartment");
     ProgramBuilder pb(ctx);
+    // cell-data keys (Gmsh "gmsh_id") are variables, given as inputs after the position
+    std::vector<const std::vector<double>*> cdata;
     Resolver res = [&](const std::string& nm) -> std::optional<Symbol> {
       for (int d = 0; d < 3; ++d)
         if (nm == std::string("position_") + kAxes[d]) {
@@ -188,6 +196,15 @@ void Model::build_species() {
           if (d < dim) { s.is_input = true; s.input = static_cast<uint16_t>(IN_POSITION + d); }
           return s;
         }
+      auto it = mesh.cell_data.find(nm);
+      if (it != mesh.cell_data.end()) {
+        Symbol s;
+        s.is_input = true;
+        size_t k = std::find(cdata.begin(), cdata.end(), &it->second) - cdata.begin();
+        if (k == cdata.size()) cdata.push_back(&it->second);
+        s.input = static_cast<uint16_t>(IN_SPECIES + k);
+        return s;
+      }
       return std::nullopt;
     };
     pb.add_output(pb.compile_text(sub.at("expression"), res));
@@ -198,7 +215,8 @@ void Model::build_species() {
       for (int a = 0; a < nl; ++a)
         for (int d = 0; d < dim; ++d) ctr[d] += mesh.coords[mesh.cells[e * nl + a] * dim + d];
       for (int d = 0; d < dim; ++d) ctr[d] /= nl;
-      for (size_t i = 0; i < p.inputs.size(); ++i) in[i] = ctr[p.inputs[i] - IN_POSITION];
+      for (size_t i = 0; i < p.inputs.size(); ++i)
+        in[i] = p.inputs[i] >= IN_POSITION ? ctr[p.inputs[i] - IN_POSITION] : (*cdata[p.inputs[i] - IN_SPECIES])[e];
       mask[c][e] = run_program_host(p, ctx, in.data()) != 0.0;
     }
   }
@@ -545,6 +563,37 @@ void Model::build_volume_groups() {
     g.nodes.upload(nodes);
     g.bpos.upload(bpos);
 
+    // gather lists of the two-phase assembly: for every node of the compartment its
+    // (element, local vertex) pairs, for every block of the compartment's rows its
+    // (element, local pair) triples, each in ascending element order
+    if (g.ne * nl * nl > INT32_MAX) throw ConfigError("compartment too large for 32-bit gather lists");
+    g.node_begin = comp_node_offset[c];
+    g.nnodes = comp_node_offset[c + 1] - g.node_begin;
+    g.block_begin = rowptr[g.node_begin];
+    g.nblocks = rowptr[g.node_begin + g.nnodes] - g.block_begin;
+    {
+      std::vector<int64_t> rp(g.nnodes + 1, 0), bp(g.nblocks + 1, 0);
+      for (int64_t j = 0; j < g.ne; ++j)
+        for (int a = 0; a < nl; ++a) {
+          rp[nodes[j * nl + a] - g.node_begin + 1]++;
+          for (int b = 0; b < nl; ++b) bp[bpos[(j * nl + a) * nl + b] - g.block_begin + 1]++;
+        }
+      for (int64_t i = 0; i < g.nnodes; ++i) rp[i + 1] += rp[i];
+      for (int64_t i = 0; i < g.nblocks; ++i) bp[i + 1] += bp[i];
+      std::vector<int32_t> rl(g.ne * nl), bl(g.ne * nl * nl);
+      std::vector<int64_t> rc(rp.begin(), rp.end() - 1), bc(bp.begin(), bp.end() - 1);
+      for (int64_t j = 0; j < g.ne; ++j)
+        for (int a = 0; a < nl; ++a) {
+          rl[rc[nodes[j * nl + a] - g.node_begin]++] = static_cast<int32_t>(j * nl + a);
+          for (int b = 0; b < nl; ++b)
+            bl[bc[bpos[(j * nl + a) * nl + b] - g.block_begin]++] = static_cast<int32_t>((j * nl + a) * nl + b);
+        }
+      g.rlist_ptr.upload(rp);
+      g.rlist.upload(rl);
+      g.blist_ptr.upload(bp);
+      g.blist.upload(bl);
+    }
+
     // symbols of a volume program of compartment c
     Resolver res = [&](const std::string& nm) -> std::optional<Symbol> {
       Symbol s;
@@ -618,7 +667,8 @@ void Model::build_volume_groups() {
         T.trial = static_cast<uint8_t>(trial);
         T.out = static_cast<uint16_t>(out);
         T.coef = static_cast<uint16_t>(coef);
-        int sz = (kind == J_MASS || kind == J_MASS_U || kind == J_STORAGE_SELF) ? nq
+        // mass-type terms: nq point weights + one slot for beta^2 (sum of the weights)
+        int sz = (kind == J_MASS || kind == J_MASS_U || kind == J_STORAGE_SELF) ? nq + 1
                : (kind == J_DIFF_SCALAR) ? 1
                : (kind == J_DIFF_TENSOR) ? dim * dim : nl * dim;
         coef += sz;
@@ -726,6 +776,29 @@ void Model::build_volume_groups() {
         }
       }
       if (coef > kMaxCoefficients) throw ConfigError("too many Jacobian terms in one compartment");
+      // Jacobian slots: one per distinct (test, trial) pair, terms sorted by slot so the
+      // volume kernel writes each slot of each local pair once
+      auto assign_slots = [&](std::vector<Term>& terms, int& nslot, bool& all_mass, DeviceBuffer<int32_t>& pos) {
+        std::map<std::pair<int, int>, int> idx;
+        std::vector<int32_t> p;
+        all_mass = true;
+        for (auto& T : terms) {
+          const int te = T.test;
+          const int tr = (T.kind == J_STORAGE_SELF || T.kind == J_VELOCITY) ? T.test : T.trial;
+          auto it = idx.find({te, tr});
+          if (it == idx.end()) {
+            it = idx.emplace(std::make_pair(te, tr), static_cast<int>(p.size())).first;
+            p.push_back(te * bs + tr);
+          }
+          T.slot = static_cast<uint8_t>(it->second);
+          if (!(T.kind == J_MASS || T.kind == J_MASS_U || T.kind == J_STORAGE_SELF)) all_mass = false;
+        }
+        std::stable_sort(terms.begin(), terms.end(), [](const Term& a, const Term& b) { return a.slot < b.slot; });
+        nslot = static_cast<int>(p.size());
+        pos.upload(p);
+      };
+      if (pass == 0) assign_slots(jterms, g.slots_static, g.static_all_mass, g.slot_pos_static);
+      if (pass == 2) assign_slots(jterms, g.slots_dyn, g.dyn_all_mass, g.slot_pos_dyn);
       if (pass == 0) {
         g.prog_static.host = pb.finish();
         g.static_terms = jterms;
@@ -747,6 +820,13 @@ void Model::build_volume_groups() {
     g.d_jac.upload(g.jac_terms);
     vgroups.push_back(std::move(g));
   }
+  int64_t er_max = 0, ej_max = 0;
+  for (const auto& g : vgroups) {
+    er_max = std::max<int64_t>(er_max, g.ne * nl * g.ns);
+    ej_max = std::max<int64_t>(ej_max, g.ne * nl * nl * std::max(g.slots_dyn, g.slots_static));
+  }
+  d_er.resize(er_max);
+  d_ej.resize(ej_max);
 }
 
 // ------------------------------------------------------------------ face groups
@@ -1036,20 +1116,34 @@ void Model::assemble(const double* x, double t, double cm, double ca, double* r,
     p.cm = cm;
     p.ca = ca;
     p.fd_eps = fd_eps;
+    p.er = d_er.get();
+    p.ej = d_ej.get();
+    p.n_slots = g.slots_dyn;
+    p.all_mass = g.dyn_all_mass ? 1 : 0;
+    const int ne = static_cast<int>(g.ne);
     if (numerical_jacobian && (mode & 2)) {
-      // jacobian.type = numerical: residual pass (if asked) + finite-difference Jacobian pass,
-      // both with the residual program and terms
+      // jacobian.type = numerical: residual pass (if asked) + finite-difference Jacobian pass
+      // (coloured scatter), both with the residual program and terms
       p.prog = g.prog_res.view();
       p.res_terms = g.d_res_r.get();
       p.n_res_terms = static_cast<int>(g.res_terms_r.size());
-      for (size_t k = 0; k + 1 < g.color_offsets.size(); ++k) {
-        if (mode & 1) launch_volume(dim, g.ns, p, g.color_offsets[k], g.color_offsets[k + 1], 1, s);
-        if (J) launch_volume(dim, g.ns, p, g.color_offsets[k], g.color_offsets[k + 1], kVolumeNumericalJacobian, s);
+      if ((mode & 1) && r) {
+        launch_volume(dim, g.ns, p, 0, ne, 1, s);
+        launch_gather_residual(r, bs, g.ns, g.node_begin, g.nnodes, g.rlist_ptr.get(), g.rlist.get(), d_er.get(), s);
       }
+      if (J)
+        for (size_t k = 0; k + 1 < g.color_offsets.size(); ++k)
+          launch_volume(dim, g.ns, p, g.color_offsets[k], g.color_offsets[k + 1], kVolumeNumericalJacobian, s);
       continue;
     }
-    for (size_t k = 0; k + 1 < g.color_offsets.size(); ++k)
-      launch_volume(dim, g.ns, p, g.color_offsets[k], g.color_offsets[k + 1], mode, s);
+    // two-phase: element outputs for all cells of the compartment in one launch, then the
+    // per-node / per-block gathers (fixed order, no atomics, no colouring)
+    launch_volume(dim, g.ns, p, 0, ne, mode, s);
+    if ((mode & 1) && r)
+      launch_gather_residual(r, bs, g.ns, g.node_begin, g.nnodes, g.rlist_ptr.get(), g.rlist.get(), d_er.get(), s);
+    if ((mode & 2) && J && g.slots_dyn > 0)
+      launch_gather_jacobian(J, bs, g.slots_dyn, g.slot_pos_dyn.get(), g.block_begin, g.nblocks, g.blist_ptr.get(),
+                             g.blist.get(), d_ej.get(), s);
   }
   if (ca != 0.0) {
     for (const auto& g : fgroups) {

@@ -13,6 +13,7 @@
 #pragma once
 
 #include <cstdint>
+#include <map>
 #include <memory>
 #include <string>
 #include <vector>
@@ -109,6 +110,14 @@ struct VolumeGroup {
   DeviceBuffer<Term> d_static, d_res_r, d_res_a, d_jac;
   bool has_mass = false, has_stiffness = false;            // dynamic terms present
   bool static_mass = false, static_stiffness = false;      // static terms present
+  // two-phase assembly: Jacobian slots (distinct test/trial pairs) of the static and the
+  // dynamic term lists, and the gather lists of the compartment's nodes and blocks
+  int slots_static = 0, slots_dyn = 0;
+  bool static_all_mass = false, dyn_all_mass = false;
+  DeviceBuffer<int32_t> slot_pos_static, slot_pos_dyn;     // test * bs + trial per slot
+  int64_t node_begin = 0, nnodes = 0, block_begin = 0, nblocks = 0;
+  DeviceBuffer<int64_t> rlist_ptr, blist_ptr;
+  DeviceBuffer<int32_t> rlist, blist;                     // k * nl + a ; (k * nl + a) * nl + b
 };
 
 struct FaceGroup {
@@ -167,6 +176,8 @@ class Model {
 
   std::vector<VolumeGroup> vgroups;
   std::vector<FaceGroup> fgroups;
+  // element outputs of the volume kernel (sized for the largest group; groups run in order)
+  DeviceBuffer<double> d_er, d_ej;
 
   // static parts of the operator, assembled once: mass-form and stiffness-form BSR values
   DeviceBuffer<double> d_Ms, d_Ks;
@@ -192,6 +203,10 @@ class Model {
   std::vector<ReduceResult> reduce(const double* x, double t, const Ini& reduce_cfg, cudaStream_t s) const;
   mutable DeviceBuffer<int32_t> d_red_cells, d_red_nodes, d_red_comp;
   mutable DeviceBuffer<int8_t> d_red_spc, d_red_spl;
+
+  // VTK output of a reference-order state (vtk.cpp); time series per output path
+  void write_vtk(const std::vector<double>& x_ref, double t, const std::string& path, bool append) const;
+  mutable std::map<std::string, std::vector<double>> vtk_steps;
 
   // host-side helpers
   std::vector<double> initial_state() const;        // reference DOF order

@@ -50,7 +50,12 @@ int64_t Server::estimate_bytes(const std::string& ini, const std::string& overri
     nv *= c + 1.0;
     ncube *= c;
   }
-  const double ne = ncube * (dim == 2 ? 2.0 : 6.0);
+  double ne = ncube * (dim == 2 ? 2.0 : 6.0);
+  if (grid.has_key("path")) {
+    Mesh m = read_gmsh(grid.get("path", ""), dim);
+    nv = static_cast<double>(m.nv);
+    ne = static_cast<double>(m.ne);
+  }
   const int nl = dim + 1;
   // species per compartment
   Ini sf = cfg.sub("model").sub("scalar_field");
@@ -72,7 +77,9 @@ int64_t Server::estimate_bytes(const std::string& ini, const std::string& overri
                  + 1.5 * nnodes * bs * bs * 8.0  // block-Jacobi inverses (fp64 + fp32)
                  + 25.0 * n * 8.0                // state, stages, Krylov vectors
                  + nnzb * 4.0 + nnodes * 8.0     // pattern
-                 + ne * (2.0 * nl * 4.0 + nl * nl * 4.0) + nv * dim * 8.0;  // cells, nodes, bpos, coords
+                 + ne * (2.0 * nl * 4.0 + nl * nl * 4.0) + nv * dim * 8.0   // cells, nodes, bpos, coords
+                 + ne * nl * (nl * bs * bs + bs) * 8.0                      // element outputs (upper bound)
+                 + ne * nl * (nl + 1) * 4.0 + (nnodes + nnzb) * 8.0;        // gather lists
   return static_cast<int64_t>(bytes * 1.2) + (int64_t{1} << 20);
 }
 

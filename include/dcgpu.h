@@ -83,6 +83,13 @@ int dc_state_set_initial(dc_model* model);
  * model/model.hh:36-42): compartment-major, vertex-major, species interleaved */
 int dc_state_get(const dc_model* model, double* host_out, size_t n);
 int dc_state_set(dc_model* model, const double* host_in, size_t n, double time);
+
+/* VTK output of the current state (replaces Model::write_vtk, dune/copasi/model/model.hh:88,
+ * model_multi_compartment.impl.hh:219-293, driven by writer.vtk.path in the reference CLI):
+ * per compartment "<path>/<stem>-<compartment>-NNNNN.vtu" (stem = last component of path,
+ * NNNNN = call index for this path) with one vertex field per species, and the time series
+ * "<path>/<stem>-<compartment>.pvd".  append = 0 starts a new series. */
+int dc_write_vtk(const dc_model* model, const char* path, int append);
 int dc_state_get_species(const dc_model* model, int32_t species, double* host_out, size_t n);
 int dc_state_time(const dc_model* model, double* time);
 

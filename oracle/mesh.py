@@ -10,7 +10,9 @@ Restates dune/copasi/grid/make_multi_domain_grid.hh:
     level r is built directly as cells * 2**r;
   * :118-154,166-194 compartment marking: each compartment's expression is evaluated
     at the cell centre and the cell belongs to the compartment when the value != 0;
-    compartment ids follow the order of ``[compartments]`` in the configuration.
+    compartment ids follow the order of ``[compartments]`` in the configuration;
+  * :66-76 ``grid.path``: a Gmsh file (read_gmsh), whose physical entities become the cell
+    data ``gmsh_id`` visible to the compartment expressions (:112-132).
 """
 
 import itertools
@@ -55,19 +57,70 @@ def structured_simplex(dim, cells, origin, extensions):
     return coords, simplices
 
 
+def read_gmsh(path, dim):
+    """Gmsh MSH 2.x ASCII file (the format Dune's GmshReader reads,
+    make_multi_domain_grid.hh:66-76): nodes in file order (ids mapped to 0..n-1); the
+    elements of the grid's dimension (type 2 triangles in 2D, type 4 tetrahedra in 3D) in
+    file order; lower-dimensional elements are skipped; the first tag of an element is its
+    physical entity, exposed as the cell data ``gmsh_id``.  Returns (coords, cells, gmsh_id).
+    """
+    with open(path) as f:
+        lines = [ln.strip() for ln in f]
+    i = 0
+    coords = None
+    cells, phys = [], []
+    idmap = {}
+    want = 2 if dim == 2 else 4
+    while i < len(lines):
+        tag = lines[i]
+        if tag == "$MeshFormat":
+            ver = lines[i + 1].split()
+            if not ver[0].startswith("2") or ver[1] != "0":
+                raise ValueError("only ASCII Gmsh MSH 2.x files are supported")
+            i += 3
+        elif tag == "$Nodes":
+            n = int(lines[i + 1])
+            coords = np.zeros((n, dim))
+            for k in range(n):
+                parts = lines[i + 2 + k].split()
+                idmap[int(parts[0])] = k
+                coords[k] = [float(v) for v in parts[1:1 + dim]]
+            i += n + 3
+        elif tag == "$Elements":
+            n = int(lines[i + 1])
+            for k in range(n):
+                parts = [int(v) for v in lines[i + 2 + k].split()]
+                typ, ntags = parts[1], parts[2]
+                if typ != want:
+                    continue
+                phys.append(parts[3] if ntags > 0 else 0)
+                cells.append([idmap[v] for v in parts[3 + ntags:3 + ntags + dim + 1]])
+            i += n + 3
+        else:
+            i += 1
+    if coords is None or not cells:
+        raise ValueError("Gmsh file without nodes or %dD elements: %r" % (dim, path))
+    return coords, np.asarray(cells, np.int64), np.asarray(phys, float)
+
+
 class Mesh:
-    def __init__(self, coords, cells):
+    def __init__(self, coords, cells, cell_data=None):
         self.coords = np.ascontiguousarray(coords, float)
         self.cells = np.ascontiguousarray(cells, np.int64)
         self.dim = self.coords.shape[1]
         self.nv = self.coords.shape[0]
         self.ne = self.cells.shape[0]
+        self.cell_data = cell_data or {}
 
     @classmethod
     def from_config(cls, cfg):
         """cfg: the ``grid`` ParameterTree."""
         if cfg.has_key("path"):
-            raise NotImplementedError("Gmsh grids are not supported by this oracle")
+            dim = cfg.get_int("dimension", 2)
+            if cfg.get_int("refinement_level", 0) != 0:
+                raise NotImplementedError("refinement of Gmsh grids is not supported")
+            coords, cells, phys = read_gmsh(cfg.get("path"), dim)
+            return cls(coords, cells, {"gmsh_id": phys})
         if cfg.has_key("dimension"):
             dim = cfg.get_int("dimension")
         elif cfg.has_key("extensions"):
@@ -133,7 +186,7 @@ def mark_compartments(mesh, comp_cfg, context):
     """Return (names, mask[ncomp, ne]) evaluating each expression at the cell centres."""
     names = comp_cfg.sub_keys()
     ctr = mesh.centers()
-    env = {}
+    env = dict(mesh.cell_data)       # cell data keys are variables (make_multi_domain_grid.hh:124-132)
     for d in range(3):
         env["position_" + AXES[d]] = ctr[:, d] if d < mesh.dim else 0.0
     masks = []

@@ -280,3 +280,76 @@ time_end = 0.5
 time_step_initial = 0.1
 time_step_max = 0.1
 """ + REDUCE_SECTION
+
+
+def write_gmsh(path, dim=2, n=8, seed=5):
+    """A Gmsh MSH 2.2 ASCII file of the Kuhn-split unit square / cube with interior vertices
+    displaced by up to 0.2 h (an unstructured-looking grid), node ids offset and with a gap,
+    physical entity 1 for cells whose centre has x < 0.5 and 2 otherwise, and boundary
+    line / point elements that the reader must skip."""
+    from oracle.mesh import structured_simplex
+    coords, cells = structured_simplex(dim, [n] * dim, [0.0] * dim, [1.0] * dim)
+    rng = np.random.default_rng(seed)
+    interior = np.all((coords > 1e-12) & (coords < 1 - 1e-12), axis=1)
+    coords = coords.copy()
+    coords[interior] += rng.uniform(-0.2, 0.2, (interior.sum(), dim)) / n
+    ids = np.arange(coords.shape[0]) + 10
+    ids[coords.shape[0] // 2:] += 7                      # a gap in the node ids
+    ctr = coords[cells].mean(axis=1)
+    phys = np.where(ctr[:, 0] < 0.5, 1, 2)
+    lines = ["$MeshFormat", "2.2 0 8", "$EndMeshFormat", "$Nodes", str(coords.shape[0])]
+    for k in range(coords.shape[0]):
+        xyz = list(coords[k]) + [0.0] * (3 - dim)
+        lines.append("%d %.17g %.17g %.17g" % (ids[k], *xyz))
+    lines += ["$EndNodes", "$Elements"]
+    elems = ["1 15 2 9 9 %d" % ids[0], "2 1 2 7 7 %d %d" % (ids[0], ids[1])]
+    typ = 2 if dim == 2 else 4
+    for e in range(cells.shape[0]):
+        elems.append("%d %d 2 %d %d " % (e + 3, typ, phys[e], 100 + phys[e]) + " ".join(str(ids[v]) for v in cells[e]))
+    lines += [str(len(elems))] + elems + ["$EndElements"]
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+    return coords, cells, phys
+
+
+def gmsh_ini(path, dim=2):
+    """Two compartments selected by the Gmsh physical entity, one species each coupled
+    through an outflow term, Alexander2 steps."""
+    return """
+[grid]
+dimension = %d
+path = %s
+
+[compartments]
+left.expression = gmsh_id == 1
+right.expression = gmsh_id == 2
+
+[model.scalar_field.u]
+compartment = left
+initial.expression = 1 + position_x*position_y
+storage.expression = 1
+cross_diffusion.u.expression = 0.05
+reaction.expression = -0.5*u^2
+reaction.jacobian.u.expression = -u
+outflow.right.expression = 0.3*(u - v)
+outflow.right.jacobian.u.expression = 0.3
+outflow.right.jacobian.v.expression = -0.3
+
+[model.scalar_field.v]
+compartment = right
+initial.expression = 0.2
+storage.expression = 1
+cross_diffusion.v.expression = 0.02
+outflow.left.expression = 0.3*(v - u)
+outflow.left.jacobian.v.expression = 0.3
+outflow.left.jacobian.u.expression = -0.3
+
+[model.time_step_operator]
+type = Alexander2
+time_end = 0.2
+time_step_initial = 0.05
+time_step_max = 0.05
+
+[model.time_step_operator.nonlinear_solver]
+convergence_condition.relative_tolerance = 1e-16
+""" % (dim, path)

@@ -353,8 +353,11 @@ def test_reduce_matches_oracle(dcgpu_lib):
     gm = dcgpu_lib.Model(ini)
     for when in ("initial", "final"):
         if when == "final":
+            # both reduce the same state (the two runs agree to the stepping tolerance only)
             x, t, *_ = om.run()
             gm.evolve(0.5, 0.1)
+            assert np.abs(gm.state() - x).max() <= STEP_TOL * np.abs(x).max()
+            gm.set_state(x, t)
         else:
             x, t = om.initial_state(), 0.0
         vo, eo, wo = om.reduce(x, t)
@@ -381,3 +384,54 @@ vol.evaluation.expression = entity_volume*integration_factor
     for k in vo:
         assert vg[k] == pytest.approx(vo[k], rel=1e-10, abs=1e-14), k
     gm.close()
+
+
+def test_vtk_output_round_trip(dcgpu_lib, tmp_path):
+    """Per compartment a .vtu piece with the compartment's cells and one vertex field per
+    species, and a .pvd time series that lists every written step."""
+    import xml.etree.ElementTree as ET
+    ini, init = ALL_CASES["two_compartment_constrained"]()
+    gm = dcgpu_lib.Model(ini)
+    out = tmp_path / "run"
+    gm.write_vtk(out, append=False)
+    gm.step(0.05)
+    gm.write_vtk(out)
+    x = gm.state()
+    coords = gm.vertex_coords()
+    off = 0
+    for comp, names in (("left", ["a", "b"]), ("right", ["c", "d"])):
+        verts = gm.species_vertices(names[0])
+        pvd = ET.parse(out / ("run-%s.pvd" % comp)).getroot()
+        files = [d.get("file") for d in pvd.iter("DataSet")]
+        times = [float(d.get("timestep")) for d in pvd.iter("DataSet")]
+        assert files == ["run-%s-00000.vtu" % comp, "run-%s-00001.vtu" % comp]
+        assert times == [0.0, pytest.approx(0.05)]
+        piece = ET.parse(out / files[1]).getroot().find("UnstructuredGrid/Piece")
+        assert int(piece.get("NumberOfPoints")) == len(verts)
+        arrays = {a.get("Name"): np.array(a.text.split(), float) for a in piece.find("PointData")}
+        for k, nm in enumerate(names):
+            np.testing.assert_array_equal(arrays[nm], x[off + k: off + len(names) * len(verts): len(names)])
+        pts = np.array(piece.find("Points/DataArray").text.split(), float).reshape(-1, 3)
+        np.testing.assert_array_equal(pts[:, :2], coords[verts])
+        off += len(names) * len(verts)
+    gm.close()
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_gmsh_grid_matches_oracle(dcgpu_lib, tmp_path, dim):
+    """An unstructured (perturbed) Gmsh grid with compartments chosen by physical entity:
+    same layout and the same time steps as the oracle."""
+    path = tmp_path / "grid.msh"
+    cases.write_gmsh(str(path), dim=dim, n=6 if dim == 2 else 3)
+    ini = cases.gmsh_ini(str(path), dim)
+    om = OracleModel(ini)
+    gm = dcgpu_lib.Model(ini)
+    np.testing.assert_array_equal(gm.vertex_coords(), om.mesh.coords)
+    for sp in om.species:
+        assert np.array_equal(gm.species_vertices(sp.name), om.comp_vertices[sp.comp])
+    gm.close()
+    records = _run_both(dcgpu_lib, ini, None)
+    for t, errs, n_o, n_g, stages in records:
+        for name, e in errs.items():
+            assert e <= STEP_TOL, (dim, t, name, e)
+        assert abs(n_o - n_g) <= max(1, stages)

@@ -386,3 +386,18 @@ def test_reduce_operators():
     v2, _, _ = om2.reduce(x, t)
     assert v2["mixed"] == vals["mixed"]
     assert np.isfinite(vals["mixed"])
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_gmsh_grid_and_physical_compartments(tmp_path, dim):
+    """grid.path: MSH 2.2 ASCII nodes and elements in file order, lower-dimensional elements
+    skipped, node ids remapped, gmsh_id (first tag) usable in compartment expressions."""
+    import cases
+    path = tmp_path / "grid.msh"
+    coords, cells, phys = cases.write_gmsh(str(path), dim=dim, n=4)
+    om = OracleModel(cases.gmsh_ini(str(path), dim))
+    assert np.array_equal(om.mesh.coords, coords)
+    assert np.array_equal(om.mesh.cells, cells)
+    assert np.array_equal(om.comp_mask[0], phys == 1) and np.array_equal(om.comp_mask[1], phys == 2)
+    x, t, *_ = om.run()
+    assert t == pytest.approx(0.2) and np.all(np.isfinite(x))

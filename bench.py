@@ -9,8 +9,12 @@ residual of 1e-10).
 A "step" is one Alexander2 time step (2 stages x Newton iterations).  Timed per step with
 CUDA events on the engine's stream (dc_step_info.device_ms); the L2 cache is flushed
 between timed steps (a 256 MiB write).  value = DOF x Newton iterations of all timed
-steps / sum of device step times.  e2e = the same through the public C ABI with host
-buffers: state upload (pinned->device), step, state download, host-timed.
+steps / sum of device step times, for the mixed-precision path (fp32 Krylov in fp64
+refinement) by default; "plain_fp64" is the plain FP64 path on the same workload and steps,
+with the per-species relative L2 deviation of the mixed state from it.  e2e = the same
+through the public C ABI with host buffers: state upload (pinned->device), step, state
+download, host-timed.  "serving" runs a Poisson stream of random requests through the
+request server: served concurrently with mixed precision, and one at a time in plain FP64.
 
 --impl reference times the CPU restatement of the reference algorithm (numpy assembly +
 SuperLU direct solve, the oracle) on the host cores, one Newton iteration of the full
@@ -47,9 +51,15 @@ def parse():
     ap.add_argument("--n", type=int, default=512)
     ap.add_argument("--workload", default="gray_scott", choices=["gray_scott", "cross_diffusion_3d"],
                     help="gray_scott (headline, n = grid edge) or cross_diffusion_3d (n = cube edge)")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"],
+                    help="mixed (default): fp32 Krylov in fp64 refinement, measured against the plain "
+                         "FP64 path on the same workload; fp64: the plain path alone")
+    ap.add_argument("--no-plain-fp64", action="store_true",
+                    help="skip the plain FP64 comparison run of the mixed path")
     ap.add_argument("--spmv", default="auto", choices=["auto", "bsr", "sell"],
                     help="layout of the fp32 Krylov operator (linear_solver.spmv)")
+    ap.add_argument("--precond", default="Jacobi", choices=["Jacobi", "AMG"],
+                    help="BiCGSTAB preconditioner (linear_solver.preconditioner.type)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--large-n", type=int, default=128,
                     help="cube edge of the HBM-resident SpMV measurement (0 disables it)")
@@ -296,7 +306,8 @@ def main():
         dist.init_process_group("gloo")
 
     ini, init, dt0, wdesc = make_workload(args.n, args.workload)
-    model = dcgpu.Model(ini, {"model.time_step_operator.linear_solver.spmv": args.spmv})
+    model = dcgpu.Model(ini, {"model.time_step_operator.linear_solver.spmv": args.spmv,
+                              "model.time_step_operator.linear_solver.preconditioner.type": args.precond})
     if args.precision == "mixed":
         model.set_mixed_precision(True)
     x0 = model.seeded_state(init)
@@ -311,24 +322,48 @@ def main():
         dist.barrier()
     torch.cuda.synchronize()
 
+    def timed_steps(m, d):
+        """K steps, L2 flushed before each, device time of each step from its CUDA events."""
+        ms, nit, lit = [], 0, 0
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            inf = m.step(d)
+            d = inf["dt_next"]
+            ms.append(inf["device_ms"])
+            nit += inf["newton_iterations"]
+            lit += inf["linear_iterations"]
+        torch.cuda.synchronize()
+        return sum(ms), nit, lit, d
+
     clocks = ClockSampler()
     clocks.start()
     launches0 = dcgpu.launch_count()
-    dev_ms = []
-    newton = 0
-    linear = 0
-    for _ in range(args.steps):
-        flush.zero_()
-        torch.cuda.synchronize()
-        info = model.step(dt)
-        dt = info["dt_next"]
-        dev_ms.append(info["device_ms"])
-        newton += info["newton_iterations"]
-        linear += info["linear_iterations"]
+    total_ms, newton, linear, dt = timed_steps(model, dt)
     launches = dcgpu.launch_count() - launches0
-    torch.cuda.synchronize()
     clk = clocks.stop()
-    total_ms = sum(dev_ms)
+
+    # the plain FP64 path on the same workload and steps, for the metric's comparison, and
+    # the mixed path's deviation from it (per-species relative L2 after W + K steps)
+    plain = None
+    if args.precision == "mixed" and not args.no_plain_fp64:
+        xm = model.state()
+        ref = dcgpu.Model(ini, {"model.time_step_operator.linear_solver.preconditioner.type": args.precond})
+        ref.set_state(x0, 0.0)
+        d = dt0
+        for _ in range(args.warmup):
+            d = ref.step(d)["dt_next"]
+        p_ms, p_newton, p_linear, d = timed_steps(ref, d)
+        xf = ref.state()
+        errs = []
+        for name in ref.species:
+            idx = ref.species_dofs(name)
+            nb = float(np.linalg.norm(xf[idx]))
+            errs.append(float(np.linalg.norm(xm[idx] - xf[idx])) / (nb if nb > 0 else 1.0))
+        plain = {"value": world * ndof * p_newton / (p_ms * 1e-3), "unit": METRIC,
+                 "ms_per_step": p_ms / args.steps, "newton_iterations": p_newton, "krylov_iterations": p_linear,
+                 "max_species_rel_l2_mixed_vs_fp64": max(errs)}
+        ref.close()
 
     # per-category kernel times from a second pass of the same number of steps with
     # events around each kernel group (kept out of the timed pass above)
@@ -410,18 +445,23 @@ def main():
         roof["spmv_hbm_resident"] = large_spmv(dcgpu, args.precision, peak_gbs, args.large_n, args.spmv)
     serving = None
     if args.serve_requests > 0:
-        serving = {"concurrent": run_serving(dcgpu, args.serve_requests, 50.0, 8, args.precision),
-                   "one_at_a_time": run_serving(dcgpu, args.serve_requests, 50.0, 1, args.precision)}
+        served = run_serving(dcgpu, args.serve_requests, 50.0, 8, args.precision)
+        alone = run_serving(dcgpu, args.serve_requests, 50.0, 1, "fp64")
+        serving = {"served_concurrent": served, "plain_fp64_one_at_a_time": alone,
+                   "speedup": served["value"] / alone["value"] if alone["value"] > 0 else None}
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f64+f32",
             "data": "synthetic (seeded initial state, no dataset)",
             "config": {"workload": wdesc["workload"], "mesh": wdesc["mesh"], "dof": ndof,
                        "species": wdesc["species"], "scheme": "Alexander2", "dt": dt0, "precision": args.precision,
-                       "linear_solver": "BiCGSTAB+block-Jacobi to 1e-10 (direct-solve semantics)",
+                       "linear_solver": "BiCGSTAB+%s to 1e-10 (direct-solve semantics)"
+                                        % ("block-Jacobi" if args.precond == "Jacobi" else "aggregation-AMG"),
                        "spmv_layout": model.spmv_format()["format"],
                        "newton_rel_tol_sq": 1e-10, "l2_flush": "256 MiB write between timed steps",
                        "newton_iterations": newton, "krylov_iterations": linear},
+            "plain_fp64": plain,
+            "speedup_vs_plain_fp64": (value / plain["value"]) if plain else None,
             "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
             "serving": serving}
     if rank == 0:

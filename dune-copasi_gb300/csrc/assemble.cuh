@@ -25,8 +25,9 @@ void launch_faces(int dim, const FaceParams& p, int begin, int end, int mode, cu
 // VolumeParams), these gathers add them into r / J per node / block in list order
 void launch_gather_residual(double* r, int bs, int ns, int64_t node_begin, int64_t nnodes, const int64_t* ptr,
                             const int32_t* list, const double* er, cudaStream_t stream);
+// (f32: the element values are floats, summed in fp32)
 void launch_gather_jacobian(double* J, int bs, int nslot, const int32_t* slot_pos, int64_t block_begin,
-                            int64_t nblocks, const int64_t* ptr, const int32_t* list, const double* ej,
+                            int64_t nblocks, const int64_t* ptr, const int32_t* list, const double* ej, bool f32,
                             cudaStream_t stream);
 // J[diag[i]] block gets identity in the padded slots s >= ns_of_row (rows of compartments
 // with fewer species than the block size)

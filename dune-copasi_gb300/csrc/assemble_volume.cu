@@ -101,6 +101,78 @@ __device__ __forceinline__ double volume_input(uint16_t id, const double (&u)[NS
   }
 }
 
+// Element Jacobian slot values from the per-term coefficients: for every local pair (a, b)
+// the terms (sorted by slot) are summed per slot and each slot stored once.  With only
+// mass-type terms the element matrix is symmetric and only a <= b is evaluated.  JT is the
+// arithmetic and storage type (fp64, or fp32 for the mixed-precision path).
+template <int DIM, class JT>
+__device__ __forceinline__ void element_jacobian(const VolumeParams& P, const JT* coef, const JT (&G)[DIM + 1][DIM],
+                                                 JT* ej) {
+  constexpr int NL = DIM + 1;
+  constexpr int NQ = Rule<DIM>::NQ;
+  constexpr double al = MassConst<DIM>::alpha, be = MassConst<DIM>::beta;
+  const JT k1 = static_cast<JT>(be * (al - be)), k2 = static_cast<JT>((al - be) * (al - be));
+  const int nslot = P.n_slots;
+#pragma unroll
+  for (int a = 0; a < NL; ++a) {
+#pragma unroll
+    for (int b = 0; b < NL; ++b) {
+      if (P.all_mass && b < a) continue;
+      int cur = -1;
+      JT acc = JT(0);
+      for (int t = 0; t < P.n_jac_terms; ++t) {
+        const Term T = P.jac_terms[t];
+        JT v = JT(0);
+        switch (T.kind) {
+          case J_MASS:
+          case J_MASS_U:
+          case J_STORAGE_SELF: {
+            const JT ca = coef[T.coef + point_of_vertex<DIM>(a)];
+            v = coef[T.coef + NQ] + k1 * (ca + coef[T.coef + point_of_vertex<DIM>(b)]);
+            if (a == b) v += k2 * ca;
+            break;
+          }
+          case J_DIFF_SCALAR: {
+            JT gg = JT(0);
+#pragma unroll
+            for (int j = 0; j < DIM; ++j) gg += G[a][j] * G[b][j];
+            v = coef[T.coef] * gg;
+            break;
+          }
+          case J_DIFF_TENSOR:
+            // (T G_a) . G_b
+#pragma unroll
+            for (int i = 0; i < DIM; ++i) {
+              JT tg = JT(0);
+#pragma unroll
+              for (int j = 0; j < DIM; ++j) tg += coef[T.coef + i * DIM + j] * G[a][j];
+              v += tg * G[b][i];
+            }
+            break;
+          default:
+            // phi_a-weighted vector . G_b
+#pragma unroll
+            for (int j = 0; j < DIM; ++j) v += coef[T.coef + a * DIM + j] * G[b][j];
+            break;
+        }
+        if (T.slot != cur) {
+          if (cur >= 0) {
+            ej[(a * NL + b) * nslot + cur] = acc;
+            if (P.all_mass && a != b) ej[(b * NL + a) * nslot + cur] = acc;
+          }
+          cur = T.slot;
+          acc = JT(0);
+        }
+        acc += v;
+      }
+      if (cur >= 0) {
+        ej[(a * NL + b) * nslot + cur] = acc;
+        if (P.all_mass && a != b) ej[(b * NL + a) * nslot + cur] = acc;
+      }
+    }
+  }
+}
+
 template <int DIM, int NS>
 __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int begin, const int end,
                                                 const int mode) {
@@ -167,14 +239,17 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
   for (int a = 0; a < NL; ++a)
 #pragma unroll
     for (int s = 0; s < NS; ++s) c[a][s] = P.x ? P.x[static_cast<int64_t>(nd[a]) * bs + s] : 0.0;
+  // state gradients only when a program reads them or a term takes one (uniform branch)
   double g[NS][DIM];
 #pragma unroll
   for (int s = 0; s < NS; ++s)
 #pragma unroll
     for (int j = 0; j < DIM; ++j) {
       double acc = 0.0;
+      if (P.need_grad) {
 #pragma unroll
-      for (int a = 0; a < NL; ++a) acc += c[a][s] * G[a][j];
+        for (int a = 0; a < NL; ++a) acc += c[a][s] * G[a][j];
+      }
       g[s][j] = acc;
     }
 
@@ -186,11 +261,12 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
 #pragma unroll
     for (int s = 0; s < NS; ++s) rl[a][s] = 0.0;
   double coef[kMaxCoefficients];
+  int ncoef = 0;
   if (do_jac) {
-    int ncoef = 0;
     for (int t = 0; t < P.n_jac_terms; ++t) {
       const Term T = P.jac_terms[t];
-      int sz = (T.kind == J_MASS || T.kind == J_MASS_U || T.kind == J_STORAGE_SELF) ? NQ
+      // mass-type terms: nq point weights + the beta^2 S slot
+      int sz = (T.kind == J_MASS || T.kind == J_MASS_U || T.kind == J_STORAGE_SELF) ? NQ + 1
              : (T.kind == J_DIFF_SCALAR) ? 1
              : (T.kind == J_DIFF_TENSOR) ? DIM * DIM
                                          : NL * DIM;
@@ -214,8 +290,10 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
 #pragma unroll
     for (int i = 0; i < DIM; ++i) {
       double acc = X[0][i];
+      if (P.need_pos) {
 #pragma unroll
-      for (int j = 0; j < DIM; ++j) acc += Bm[i][j] * Rule<DIM>::xi(q, j);
+        for (int j = 0; j < DIM; ++j) acc += Bm[i][j] * Rule<DIM>::xi(q, j);
+      }
       xq[i] = acc;
     }
     const double fq = Rule<DIM>::w(q) * adet;
@@ -288,8 +366,10 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
 #pragma unroll
         for (int s = 0; s < NS; ++s) {
           double fg = 0.0;
+          if (P.has_flux) {
 #pragma unroll
-          for (int j = 0; j < DIM; ++j) fg += flux[s][j] * G[a][j];
+            for (int j = 0; j < DIM; ++j) fg += flux[s][j] * G[a][j];
+          }
           rl[a][s] += (scal[s] * pa - fg) * fq;
         }
       }
@@ -370,8 +450,7 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
       for (int s = 0; s < NS; ++s) er[a * NS + s] = rl[a][s];
   }
   if (do_jac) {
-    constexpr double al = MassConst<DIM>::alpha, be = MassConst<DIM>::beta;
-    constexpr double k1 = be * (al - be), k2 = (al - be) * (al - be);
+    constexpr double be = MassConst<DIM>::beta;
     // mass-type terms: beta^2 S into the spare coefficient slot after the nq point weights
     for (int t = 0; t < P.n_jac_terms; ++t) {
       const Term T = P.jac_terms[t];
@@ -382,96 +461,51 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
         coef[T.coef + NQ] = (be * be) * S;
       }
     }
-    const int nslot = P.n_slots;
-    double* ej = P.ej + static_cast<int64_t>(k) * NL * NL * nslot;
-    // terms are sorted by slot (distinct test/trial species pair); one store per slot and
-    // local pair.  With only mass-type terms the element matrix is symmetric in (a, b).
+    const int64_t off = static_cast<int64_t>(k) * NL * NL * P.n_slots;
+    if (P.jac_f32) {
+      // mixed precision: the element Jacobian in fp32 (the fp32 Krylov operator is built
+      // from it; the residual stays fp64)
+      float cf[kMaxCoefficients];
+      for (int i = 0; i < ncoef; ++i) cf[i] = static_cast<float>(coef[i]);
+      float Gf[NL][DIM];
 #pragma unroll
-    for (int a = 0; a < NL; ++a) {
+      for (int a = 0; a < NL; ++a)
 #pragma unroll
-      for (int b = 0; b < NL; ++b) {
-        if (P.all_mass && b < a) continue;
-        int cur = -1;
-        double acc = 0.0;
-        for (int t = 0; t < P.n_jac_terms; ++t) {
-          const Term T = P.jac_terms[t];
-          double v = 0.0;
-          switch (T.kind) {
-            case J_MASS:
-            case J_MASS_U:
-            case J_STORAGE_SELF: {
-              const double ca = coef[T.coef + point_of_vertex<DIM>(a)];
-              v = coef[T.coef + NQ] + k1 * (ca + coef[T.coef + point_of_vertex<DIM>(b)]);
-              if (a == b) v += k2 * ca;
-              break;
-            }
-            case J_DIFF_SCALAR: {
-              double gg = 0.0;
-#pragma unroll
-              for (int j = 0; j < DIM; ++j) gg += G[a][j] * G[b][j];
-              v = coef[T.coef] * gg;
-              break;
-            }
-            case J_DIFF_TENSOR:
-              // (T G_a) . G_b
-#pragma unroll
-              for (int i = 0; i < DIM; ++i) {
-                double tg = 0.0;
-#pragma unroll
-                for (int j = 0; j < DIM; ++j) tg += coef[T.coef + i * DIM + j] * G[a][j];
-                v += tg * G[b][i];
-              }
-              break;
-            default:
-              // phi_a-weighted vector . G_b
-#pragma unroll
-              for (int j = 0; j < DIM; ++j) v += coef[T.coef + a * DIM + j] * G[b][j];
-              break;
-          }
-          if (T.slot != cur) {
-            if (cur >= 0) {
-              ej[(a * NL + b) * nslot + cur] = acc;
-              if (P.all_mass && a != b) ej[(b * NL + a) * nslot + cur] = acc;
-            }
-            cur = T.slot;
-            acc = 0.0;
-          }
-          acc += v;
-        }
-        if (cur >= 0) {
-          ej[(a * NL + b) * nslot + cur] = acc;
-          if (P.all_mass && a != b) ej[(b * NL + a) * nslot + cur] = acc;
-        }
-      }
+        for (int j = 0; j < DIM; ++j) Gf[a][j] = static_cast<float>(G[a][j]);
+      element_jacobian<DIM, float>(P, cf, Gf, reinterpret_cast<float*>(P.ej) + off);
+    } else {
+      element_jacobian<DIM, double>(P, coef, G, P.ej + off);
     }
   }
 }
 
-// r[node, s] += sum of the element residual entries of the node's (element, vertex) list
-__global__ void k_gather_residual(double* __restrict__ r, int bs, int ns, int64_t node_begin, int64_t nnodes,
+// r[node, s] += sum of the element residual entries of the node's (element, vertex) list;
+// a thread per (node, species), species fastest, 32-bit index arithmetic
+__global__ void k_gather_residual(double* __restrict__ r, int bs, unsigned ns, int64_t node_begin, unsigned ntotal,
                                   const int64_t* __restrict__ ptr, const int32_t* __restrict__ list,
                                   const double* __restrict__ er) {
-  const int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (t >= nnodes * ns) return;
-  const int64_t n = t / ns;
-  const int s = static_cast<int>(t % ns);
+  const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntotal) return;
+  const unsigned n = t / ns, s = t - n * ns;
   double acc = 0.0;
   for (int64_t i = ptr[n]; i < ptr[n + 1]; ++i) acc += er[static_cast<int64_t>(list[i]) * ns + s];
   r[(node_begin + n) * bs + s] += acc;
 }
 
-// J[block, slot position] += sum of the element Jacobian values of the block's
-// (element, local pair) list
-__global__ void k_gather_jacobian(double* __restrict__ J, int bs2, int nslot, const int32_t* __restrict__ slot_pos,
-                                  int64_t block_begin, int64_t nblocks, const int64_t* __restrict__ ptr,
-                                  const int32_t* __restrict__ list, const double* __restrict__ ej) {
-  const int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (t >= nblocks * nslot) return;
-  const int64_t b = t / nslot;
-  const int m = static_cast<int>(t % nslot);
-  double acc = 0.0;
+// J[block, slot position] += sum of the element Jacobian values (type E) of the block's
+// (element, local pair) list.  A thread per (block, slot), slot fastest, so the threads of a
+// warp read neighbouring element values and write neighbouring entries; 32-bit index
+// arithmetic (the host checks nblocks * nslot < 2^32; 64-bit division is a long routine).
+template <class E>
+__global__ void k_gather_jacobian(double* __restrict__ J, int bs2, unsigned nslot, const int32_t* __restrict__ slot_pos,
+                                  int64_t block_begin, unsigned ntotal, const int64_t* __restrict__ ptr,
+                                  const int32_t* __restrict__ list, const E* __restrict__ ej) {
+  const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntotal) return;
+  const unsigned b = t / nslot, m = t - b * nslot;
+  E acc = E(0);
   for (int64_t i = ptr[b]; i < ptr[b + 1]; ++i) acc += ej[static_cast<int64_t>(list[i]) * nslot + m];
-  J[(block_begin + b) * bs2 + slot_pos[m]] += acc;
+  J[(block_begin + b) * bs2 + slot_pos[m]] += static_cast<double>(acc);
 }
 
 // Local residual of one element for coefficients c (residual terms only, both forms).
@@ -694,21 +728,29 @@ void launch_t(const VolumeParams& p, int begin, int end, int mode, cudaStream_t 
 
 void launch_gather_residual(double* r, int bs, int ns, int64_t node_begin, int64_t nnodes, const int64_t* ptr,
                             const int32_t* list, const double* er, cudaStream_t stream) {
-  const int64_t n = nnodes * ns;
-  if (n <= 0) return;
+  if (nnodes <= 0 || ns <= 0) return;
+  const int64_t total = nnodes * ns;
+  if (total >= (int64_t{1} << 32) - 256) throw std::runtime_error("gather: more than 2^32 node entries");
   count_launches(1);
-  k_gather_residual<<<static_cast<int>((n + 255) / 256), 256, 0, stream>>>(r, bs, ns, node_begin, nnodes, ptr, list,
-                                                                           er);
+  k_gather_residual<<<static_cast<unsigned>((total + 255) / 256), 256, 0, stream>>>(
+      r, bs, static_cast<unsigned>(ns), node_begin, static_cast<unsigned>(total), ptr, list, er);
 }
 
 void launch_gather_jacobian(double* J, int bs, int nslot, const int32_t* slot_pos, int64_t block_begin,
-                            int64_t nblocks, const int64_t* ptr, const int32_t* list, const double* ej,
+                            int64_t nblocks, const int64_t* ptr, const int32_t* list, const double* ej, bool f32,
                             cudaStream_t stream) {
-  const int64_t n = nblocks * nslot;
-  if (n <= 0) return;
+  if (nblocks <= 0 || nslot <= 0) return;
+  const int64_t total = nblocks * nslot;
+  if (total >= (int64_t{1} << 32) - 256) throw std::runtime_error("gather: more than 2^32 block entries");
   count_launches(1);
-  k_gather_jacobian<<<static_cast<int>((n + 255) / 256), 256, 0, stream>>>(J, bs * bs, nslot, slot_pos, block_begin,
-                                                                           nblocks, ptr, list, ej);
+  const unsigned grid = static_cast<unsigned>((total + 255) / 256);
+  if (f32)
+    k_gather_jacobian<float><<<grid, 256, 0, stream>>>(J, bs * bs, static_cast<unsigned>(nslot), slot_pos, block_begin,
+                                                       static_cast<unsigned>(total), ptr, list,
+                                                       reinterpret_cast<const float*>(ej));
+  else
+    k_gather_jacobian<double><<<grid, 256, 0, stream>>>(J, bs * bs, static_cast<unsigned>(nslot), slot_pos,
+                                                        block_begin, static_cast<unsigned>(total), ptr, list, ej);
 }
 
 void launch_volume(int dim, int ns, const VolumeParams& p, int begin, int end, int mode,

@@ -85,6 +85,11 @@ struct VolumeParams {
   double* ej;                // Jacobian: ((k * nl + a) * nl + b) * n_slots + slot
   int n_slots;               // distinct (test, trial) pairs of the Jacobian terms
   int all_mass;              // every Jacobian term is mass-type: symmetric element matrix
+  int jac_f32;               // element Jacobian in fp32 (ej then holds floats)
+  // work the kernel may skip (uniform flags set from the program inputs and term kinds)
+  int need_pos;              // a program reads position_*
+  int need_grad;             // a program reads a gradient or a term takes one
+  int has_flux;              // a residual term contributes a flux (velocity / diffusion)
 };
 
 struct FaceParams {

@@ -341,7 +341,208 @@ inline int grid_for(int64_t n) {
   return static_cast<int>(b < 1 ? 1 : b);
 }
 
+// ---------------------------------------------------------------- preconditioned CG
+// Slots: KS_RHO = <r, z>, KS_ALPHA, KS_BETA, KS_RR = ||r||^2, KS_TARGET, KS_DONE, KS_ITER.
+// Vectors: x, r, p, z (= s), q (= v).
+
+// x = 0, p = 0, ||r||^2, target; with BJ also z = D^-1 r, rho = <r, z>, beta = 0
+template <int B, class T, class V, bool BJ>
+__global__ void __launch_bounds__(kThreads) k_cg_init(int nrows, T* x, const T* r, T* p, T* z,
+                                                      const V* __restrict__ dinv, double rel, ReduceScratch rs,
+                                                      double* sc) {
+  double acc[2] = {0.0, 0.0};
+  const int stride = gridDim.x * blockDim.x;
+  for (int nd = blockIdx.x * blockDim.x + threadIdx.x; nd < nrows; nd += stride) {
+    const int64_t o = static_cast<int64_t>(nd) * B;
+    V rv[B];
+#pragma unroll
+    for (int i = 0; i < B; ++i) {
+      x[o + i] = T(0);
+      p[o + i] = T(0);
+      rv[i] = static_cast<V>(r[o + i]);
+      acc[0] += static_cast<double>(r[o + i]) * static_cast<double>(r[o + i]);
+    }
+    if (!BJ) continue;
+    const V* d = dinv + static_cast<int64_t>(nd) * B * B;
+#pragma unroll
+    for (int i = 0; i < B; ++i) {
+      V a = V(0);
+#pragma unroll
+      for (int j = 0; j < B; ++j) a += d[i * B + j] * rv[j];
+      const T zt = static_cast<T>(a);
+      z[o + i] = zt;
+      acc[1] += static_cast<double>(r[o + i]) * static_cast<double>(zt);
+    }
+  }
+  if (grid_sum<2>(acc, rs)) {
+    const double rr = acc[0];
+    sc[KS_RR] = rr;
+    sc[KS_RR0] = rr;
+    sc[KS_TARGET] = rel * rel * rr;
+    sc[KS_ITER] = 0.0;
+    sc[KS_BETA] = 0.0;
+    sc[KS_RHO] = BJ ? acc[1] : 0.0;
+    sc[KS_DONE] = !isfinite(rr) ? kDoneNonFinite : (rr == 0.0 ? kDoneConverged : 0.0);
+  }
+}
+
+// p = z + beta p
+template <class T>
+__global__ void __launch_bounds__(kThreads) k_cg_p(int64_t n, T* __restrict__ p, const T* __restrict__ z,
+                                                   const double* sc) {
+  if (done(sc)) return;
+  const T beta = static_cast<T>(sc[KS_BETA]);
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride)
+    p[i] = z[i] + beta * p[i];
+}
+
+// x += alpha p; r -= alpha q; ||r||^2 and the convergence test; with BJ also z = D^-1 r,
+// <r, z>, beta = <r, z> / rho and rho = <r, z>
+template <int B, class T, class V, bool BJ>
+__global__ void __launch_bounds__(kThreads) k_cg_update(int nrows, T* __restrict__ x, T* __restrict__ r,
+                                                        T* __restrict__ z, const T* __restrict__ p,
+                                                        const T* __restrict__ q, const V* __restrict__ dinv,
+                                                        ReduceScratch rs, double* sc) {
+  if (done(sc)) return;
+  const T alpha = static_cast<T>(sc[KS_ALPHA]);
+  double acc[2] = {0.0, 0.0};
+  const int stride = gridDim.x * blockDim.x;
+  for (int nd = blockIdx.x * blockDim.x + threadIdx.x; nd < nrows; nd += stride) {
+    const int64_t o = static_cast<int64_t>(nd) * B;
+    V rv[B];
+#pragma unroll
+    for (int i = 0; i < B; ++i) {
+      x[o + i] = x[o + i] + alpha * p[o + i];
+      const T ri = r[o + i] - alpha * q[o + i];
+      r[o + i] = ri;
+      rv[i] = static_cast<V>(ri);
+      acc[0] += static_cast<double>(ri) * static_cast<double>(ri);
+    }
+    if (!BJ) continue;
+    const V* d = dinv + static_cast<int64_t>(nd) * B * B;
+#pragma unroll
+    for (int i = 0; i < B; ++i) {
+      V a = V(0);
+#pragma unroll
+      for (int j = 0; j < B; ++j) a += d[i * B + j] * rv[j];
+      const T zt = static_cast<T>(a);
+      z[o + i] = zt;
+      acc[1] += static_cast<double>(rv[i]) * static_cast<double>(zt);
+    }
+  }
+  if (grid_sum<2>(acc, rs)) {
+    const double rr = acc[0];
+    sc[KS_RR] = rr;
+    sc[KS_ITER] += 1.0;
+    if (!isfinite(rr)) {
+      sc[KS_DONE] = kDoneNonFinite;
+      return;
+    }
+    if (rr <= sc[KS_TARGET]) {
+      sc[KS_DONE] = kDoneConverged;
+      return;
+    }
+    if (BJ) {
+      const double rz = acc[1], beta = rz / sc[KS_RHO];
+      if (rz == 0.0 || !isfinite(beta)) {
+        sc[KS_DONE] = kDoneBreakdown;
+        return;
+      }
+      sc[KS_BETA] = beta;
+      sc[KS_RHO] = rz;
+    }
+  }
+}
+
+// with a separate preconditioner: <r, z>, beta (0 on the first call), rho
+template <class T>
+__global__ void __launch_bounds__(kThreads) k_cg_rz(int64_t n, const T* __restrict__ r, const T* __restrict__ z,
+                                                    ReduceScratch rs, double* sc) {
+  if (done(sc)) return;
+  double acc[1] = {0.0};
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride)
+    acc[0] += static_cast<double>(r[i]) * static_cast<double>(z[i]);
+  if (grid_sum<1>(acc, rs)) {
+    const double rz = acc[0];
+    const bool first = sc[KS_ITER] == 0.0;
+    const double beta = first ? 0.0 : rz / sc[KS_RHO];
+    if (!isfinite(rz) || rz == 0.0 || !isfinite(beta)) {
+      sc[KS_DONE] = isfinite(rz) ? kDoneBreakdown : kDoneNonFinite;
+      return;
+    }
+    sc[KS_BETA] = beta;
+    sc[KS_RHO] = rz;
+  }
+}
+
 }  // namespace
+
+template <class T, class V>
+void cg_init(const Bsr& A, const V* dinv, const KrylovVectors<T>& k, double rel, ReduceScratch rs, double* sc,
+             cudaStream_t s, const Amg* amg) {
+  count_launches(amg ? 2 : 1);
+#define DC_CGI(B)                                                                                              \
+  case B:                                                                                                      \
+    if (amg)                                                                                                   \
+      k_cg_init<B, T, V, false><<<kReduceBlocks, kThreads, 0, s>>>(A.nrows, k.x, k.r, k.p, k.s, dinv, rel, rs, \
+                                                                   sc);                                        \
+    else                                                                                                       \
+      k_cg_init<B, T, V, true><<<kReduceBlocks, kThreads, 0, s>>>(A.nrows, k.x, k.r, k.p, k.s, dinv, rel, rs,  \
+                                                                  sc);                                         \
+    break;
+  switch (A.bs) {
+    DC_CGI(1) DC_CGI(2) DC_CGI(3) DC_CGI(4) DC_CGI(5) DC_CGI(6) DC_CGI(7) DC_CGI(8)
+    default: throw std::runtime_error("cg: block size " + std::to_string(A.bs) + " unsupported");
+  }
+#undef DC_CGI
+  if (amg) {
+    amg->apply<T>(k.r, k.s, sc, KS_DONE, s);
+    k_cg_rz<T><<<kReduceBlocks, kThreads, 0, s>>>(static_cast<int64_t>(A.nrows) * A.bs, k.r, k.s, rs, sc);
+  }
+}
+
+template <class T, class V>
+void cg_iteration(const Bsr& A, const V* vals, const V* dinv, const KrylovVectors<T>& k, ReduceScratch rs,
+                  double* sc, cudaStream_t s, const Amg* amg, const Sell* sell) {
+  const int64_t n = static_cast<int64_t>(A.nrows) * A.bs;
+  count_launches(amg ? 4 : 3);
+  k_cg_p<T><<<grid_for(n), kThreads, 0, s>>>(n, k.p, k.s, sc);
+#define DC_CG(B)                                                                                                  \
+  case B:                                                                                                         \
+    /* q = A p, alpha = rho / <p, q>: the BiCGSTAB SpMV kernel with rhat = p */                                   \
+    if (sell)                                                                                                     \
+      k_sell_rv<B, T, V><<<kReduceBlocks, kThreads, 0, s>>>(*sell, vals, k.p, k.v, k.p, rs, sc);                  \
+    else                                                                                                          \
+      k_spmv_rv<B, T, V><<<kReduceBlocks, kThreads, 0, s>>>(A.nrows, A.rowptr, A.colidx, vals, k.p, k.v, k.p, rs, \
+                                                            sc);                                                  \
+    if (amg)                                                                                                      \
+      k_cg_update<B, T, V, false><<<kReduceBlocks, kThreads, 0, s>>>(A.nrows, k.x, k.r, k.s, k.p, k.v, dinv, rs, \
+                                                                     sc);                                         \
+    else                                                                                                          \
+      k_cg_update<B, T, V, true><<<kReduceBlocks, kThreads, 0, s>>>(A.nrows, k.x, k.r, k.s, k.p, k.v, dinv, rs,  \
+                                                                    sc);                                          \
+    break;
+  switch (A.bs) {
+    DC_CG(1) DC_CG(2) DC_CG(3) DC_CG(4) DC_CG(5) DC_CG(6) DC_CG(7) DC_CG(8)
+    default: throw std::runtime_error("cg: block size " + std::to_string(A.bs) + " unsupported");
+  }
+#undef DC_CG
+  if (amg) {
+    amg->apply<T>(k.r, k.s, sc, KS_DONE, s);
+    k_cg_rz<T><<<kReduceBlocks, kThreads, 0, s>>>(n, k.r, k.s, rs, sc);
+  }
+}
+
+template void cg_init<double, double>(const Bsr&, const double*, const KrylovVectors<double>&, double, ReduceScratch,
+                                      double*, cudaStream_t, const Amg*);
+template void cg_init<float, float>(const Bsr&, const float*, const KrylovVectors<float>&, double, ReduceScratch,
+                                    double*, cudaStream_t, const Amg*);
+template void cg_iteration<double, double>(const Bsr&, const double*, const double*, const KrylovVectors<double>&,
+                                           ReduceScratch, double*, cudaStream_t, const Amg*, const Sell*);
+template void cg_iteration<float, float>(const Bsr&, const float*, const float*, const KrylovVectors<float>&,
+                                         ReduceScratch, double*, cudaStream_t, const Amg*, const Sell*);
 
 template <class T>
 void krylov_init(const KrylovVectors<T>& k, int64_t n, double rel, ReduceScratch rs, double* sc, cudaStream_t s) {

@@ -42,6 +42,19 @@ void krylov_init(const KrylovVectors<T>& k, int64_t n, double rel, ReduceScratch
 // With `amg`, the preconditioner is one multigrid V-cycle instead of block Jacobi.  With
 // `sell`, the two SpMVs read `vals` in that SELL-32 layout instead of A's BSR layout.
 class Amg;
+
+// Preconditioned CG (dune-istl CGSolver; also used for GeneralizedPCG / RestartedFCG /
+// CompleteFCG, which coincide with CG for a fixed preconditioner).  cg_init: x = 0, z =
+// M^-1 r, rho = <r, z>; one iteration: p = z + beta p; q = A p, alpha = rho / <p, q>;
+// x += alpha p, r -= alpha q, z = M^-1 r, beta = <r, z>_new / rho.  Vectors: x, r, p,
+// z in `s`, q in `v`.  Same device scalars, done flag and graph capture as BiCGSTAB.
+template <class T, class V>
+void cg_init(const Bsr& A, const V* dinv, const KrylovVectors<T>& k, double rel, ReduceScratch rs, double* sc,
+             cudaStream_t s, const Amg* amg = nullptr);
+template <class T, class V>
+void cg_iteration(const Bsr& A, const V* vals, const V* dinv, const KrylovVectors<T>& k, ReduceScratch rs,
+                  double* sc, cudaStream_t s, const Amg* amg = nullptr, const Sell* sell = nullptr);
+
 template <class T, class V>
 void krylov_iteration(const Bsr& A, const V* vals, const V* dinv, const KrylovVectors<T>& k, ReduceScratch rs,
                       double* sc, cudaStream_t s, cudaEvent_t* ev = nullptr, const Amg* amg = nullptr,

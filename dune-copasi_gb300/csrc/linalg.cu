@@ -370,8 +370,13 @@ __global__ void k_fill(int64_t n, double v, double* y) {
 }  // namespace
 
 static std::atomic<long long> g_launches{0};
+static thread_local long long t_launches = 0;
 long long launch_count() { return g_launches.load(); }
-void count_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+long long launch_count_this_thread() { return t_launches; }
+void count_launches(long long n) {
+  g_launches.fetch_add(n, std::memory_order_relaxed);
+  t_launches += n;
+}
 
 void spmv(const Bsr& A, const double* x, double* y, cudaStream_t s) {
   spmv_dispatch<double, double>(A, A.val, x, y, nullptr, s);

@@ -90,6 +90,7 @@ void bicg_xr32(float* x, float* r, const float* phat, const float* shat, const f
 
 // number of kernels this library has launched (all threads, all models)
 long long launch_count();
+long long launch_count_this_thread();  // launches counted by the calling host thread
 void count_launches(long long n);
 
 // elementwise helpers

@@ -120,6 +120,22 @@ Model::Model(const std::string& ini_text, const std::string& overrides) {
   build_constraints();
 }
 
+// uniform skip flags of the volume kernel for one program and its term lists
+static void set_volume_flags(VolumeParams& p, const Program& prog, const std::vector<Term>& res,
+                             const std::vector<Term>& jac) {
+  p.need_pos = p.need_grad = p.has_flux = 0;
+  for (uint16_t id : prog.inputs) {
+    if (id >= IN_POSITION && id < IN_NORMAL) p.need_pos = 1;
+    if (id >= IN_GRAD && id < IN_POSITION) p.need_grad = 1;
+  }
+  for (const Term& T : res) {
+    if (T.kind == R_VELOCITY || T.kind == R_DIFF_SCALAR || T.kind == R_DIFF_TENSOR) p.has_flux = 1;
+    if (T.kind == R_DIFF_SCALAR || T.kind == R_DIFF_TENSOR) p.need_grad = 1;
+  }
+  for (const Term& T : jac)
+    if (T.kind == J_DIFFJAC_SCALAR || T.kind == J_DIFFJAC_TENSOR) p.need_grad = 1;
+}
+
 void Model::build_static_matrices() {
   const int64_t nvals = nnzb() * bs * bs;
   for (const auto& g : vgroups) {
@@ -157,6 +173,7 @@ void Model::build_static_matrices() {
     p.ej = d_ej.get();
     p.n_slots = g.slots_static;
     p.all_mass = g.static_all_mass ? 1 : 0;
+    set_volume_flags(p, g.prog_static.host, {}, g.static_terms);
     for (int form = 0; form < 2; ++form) {
       if ((form == 0 && !g.static_mass) || (form == 1 && !g.static_stiffness)) continue;
       double* target = form == 0 ? d_Ms.get() : d_Ks.get();
@@ -165,7 +182,7 @@ void Model::build_static_matrices() {
       p.ca = form == 0 ? 0.0 : 1.0;
       launch_volume(dim, g.ns, p, 0, static_cast<int>(g.ne), 2, nullptr);
       launch_gather_jacobian(target, bs, g.slots_static, g.slot_pos_static.get(), g.block_begin, g.nblocks,
-                             g.blist_ptr.get(), g.blist.get(), d_ej.get(), nullptr);
+                             g.blist_ptr.get(), g.blist.get(), d_ej.get(), false, nullptr);
     }
   }
   // Every set-up copy, memset and kernel of the model went to the legacy default stream,
@@ -1092,6 +1109,7 @@ void Model::assemble(const double* x, double t, double cm, double ca, double* r,
       axpy(nvals, 1.0, C, J, s);
     }
   }
+  const bool jac_f32 = (mode & kAssembleJacobianF32) != 0;
   mode &= 3;
   for (const auto& g : vgroups) {
     if (!(cm != 0.0 && g.has_mass) && !(ca != 0.0 && g.has_stiffness)) continue;
@@ -1120,6 +1138,9 @@ void Model::assemble(const double* x, double t, double cm, double ca, double* r,
     p.ej = d_ej.get();
     p.n_slots = g.slots_dyn;
     p.all_mass = g.dyn_all_mass ? 1 : 0;
+    p.jac_f32 = jac_f32 ? 1 : 0;
+    if (jac) set_volume_flags(p, g.prog_all.host, g.res_terms_a, g.jac_terms);
+    else set_volume_flags(p, g.prog_res.host, g.res_terms_r, {});
     const int ne = static_cast<int>(g.ne);
     if (numerical_jacobian && (mode & 2)) {
       // jacobian.type = numerical: residual pass (if asked) + finite-difference Jacobian pass
@@ -1127,6 +1148,7 @@ void Model::assemble(const double* x, double t, double cm, double ca, double* r,
       p.prog = g.prog_res.view();
       p.res_terms = g.d_res_r.get();
       p.n_res_terms = static_cast<int>(g.res_terms_r.size());
+      set_volume_flags(p, g.prog_res.host, g.res_terms_r, {});
       if ((mode & 1) && r) {
         launch_volume(dim, g.ns, p, 0, ne, 1, s);
         launch_gather_residual(r, bs, g.ns, g.node_begin, g.nnodes, g.rlist_ptr.get(), g.rlist.get(), d_er.get(), s);
@@ -1143,7 +1165,7 @@ void Model::assemble(const double* x, double t, double cm, double ca, double* r,
       launch_gather_residual(r, bs, g.ns, g.node_begin, g.nnodes, g.rlist_ptr.get(), g.rlist.get(), d_er.get(), s);
     if ((mode & 2) && J && g.slots_dyn > 0)
       launch_gather_jacobian(J, bs, g.slots_dyn, g.slot_pos_dyn.get(), g.block_begin, g.nblocks, g.blist_ptr.get(),
-                             g.blist.get(), d_ej.get(), s);
+                             g.blist.get(), d_ej.get(), jac_f32, s);
   }
   if (ca != 0.0) {
     for (const auto& g : fgroups) {

@@ -219,6 +219,9 @@ class Model {
   // mode bit 1: residual, bit 2: Jacobian; with kAssembleOverwriteJacobian the Jacobian is
   // overwritten (J = cm dM/dx + ca dA/dx) instead of added to, and its prior contents are ignored.
   static constexpr int kAssembleOverwriteJacobian = 8;
+  // kAssembleJacobianF32: the per-element Jacobian values of the state-dependent terms are
+  // computed and gathered in fp32 (mixed precision; the residual and the static part stay fp64)
+  static constexpr int kAssembleJacobianF32 = 16;
   void assemble(const double* x, double t, double cm, double ca, double* r, double* J, int mode,
                 cudaStream_t s) const;
   Bsr bsr(double* val, float* val32) const;

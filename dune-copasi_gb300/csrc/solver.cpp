@@ -109,6 +109,16 @@ Solver::Solver(Model& m, cudaStream_t s) : model(m), stream(s) {
   // direct solvers of the reference (UMFPack default, SuperLU, DenseInverse) are replaced
   // by a BiCGSTAB solve converged to near machine precision
   lin_direct_ = (lt == "UMFPack" || lt == "SuperLU" || lt == "DenseInverse");
+  // iterative registry of solver/istl/factory/iterative.hh:84-105: CG and the flexible /
+  // generalized PCG variants (identical to CG for a fixed preconditioner) run as CG; the
+  // others (Loop, Gradient, MINRES, the GMRes variants) converge to the same solution of the
+  // same correction equation and run as BiCGSTAB
+  if (!lin_direct_) {
+    if (lt == "CG" || lt == "GeneralizedPCG" || lt == "RestartedFCG" || lt == "CompleteFCG") krylov_cg_ = true;
+    else if (lt != "BiCGSTAB" && lt != "Loop" && lt != "Gradient" && lt != "MINRES" && lt != "RestartedGMRes" &&
+             lt != "RestartedFlexibleGMRes")
+      throw ConfigError("Not known linear solver type '" + lt + "'");
+  }
   lin_rel_ = ls.get_double("convergence_condition.relative_tolerance", 1e-4);
   lin_max_it_ = 500;
   if (ls.has_key("convergence_condition.iteration_range")) {
@@ -137,6 +147,19 @@ Solver::Solver(Model& m, cudaStream_t s) : model(m), stream(s) {
                static_cast<int>(ls.get_long("preconditioner.coarsen_target", 256)));
   }
   const bool want_mixed = ls.get("precision", "double") == "mixed";
+  // linear_solver.matrix_free (make_step_operator.hh:201,289-293): the reference then applies
+  // the stage Jacobian through the local operators' jacobian_apply without a matrix.  The
+  // products are the same; here they always come from the assembled matrix, because an
+  // element-wise re-evaluation of the FP64 term programs per Krylov iteration costs a full
+  // assembly per SpMV on GB300's FP64 pipe, while the assembled fp32/fp64 SpMV streams at
+  // the HBM rate.  The key is read (and validated) for drop-in compatibility.
+  (void)ls.get_bool("matrix_free", false);
+  // mixed precision only: precision of the state-dependent Jacobian terms (single, default,
+  // or double)
+  const std::string jp = ls.get("jacobian_precision", "single");
+  if (jp != "single" && jp != "double")
+    throw ConfigError("linear_solver.jacobian_precision must be single or double, not '" + jp + "'");
+  jac_f32_ = jp == "single";
   const std::string fmt = ls.get("spmv", "auto");
   if (fmt == "auto") spmv_request_ = kSpmvAuto;
   else if (fmt == "bsr") spmv_request_ = kSpmvBsr;
@@ -329,43 +352,54 @@ cudaGraphExec_t Solver::krylov_graph(bool fp32) {
     ev = graph_events_.data();
   }
   cudaGraph_t g = nullptr;
+  const long long before = launch_count_this_thread();
   cuda_check(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
   for (int k = 0; k < kKrylovChunk; ++k) {
     cudaEvent_t* e = ev ? ev + 4 * k : nullptr;
+    const Amg* amg = use_amg_ ? &amg_ : nullptr;
     if (fp32) {
       KrylovVectors<float> kv{fx_.get(), fr_.get(), frhat_.get(), fp_.get(), fv_.get(), fs_.get(), ft_.get(),
                               fphat_.get(), fshat_.get()};
       const bool sell = spmv_format == kSpmvSell;
       const Sell S = model.sell();
-      krylov_iteration<float, float>(A, sell ? Js32_.get() : J32_.get(), fdinv_.get(), kv, rs_, sc, stream, e,
-                                     use_amg_ ? &amg_ : nullptr, sell ? &S : nullptr);
+      const float* vals = sell ? Js32_.get() : J32_.get();
+      if (krylov_cg_) cg_iteration<float, float>(A, vals, fdinv_.get(), kv, rs_, sc, stream, amg, sell ? &S : nullptr);
+      else krylov_iteration<float, float>(A, vals, fdinv_.get(), kv, rs_, sc, stream, e, amg, sell ? &S : nullptr);
     } else {
       KrylovVectors<double> kv{kx_.get(), kr_.get(), krhat_.get(), kp_.get(), kv_.get(), ks_.get(), kt_.get(),
                                kphat_.get(), kshat_.get()};
-      krylov_iteration<double, double>(A, J_.get(), dinv_.get(), kv, rs_, sc, stream, e, use_amg_ ? &amg_ : nullptr);
+      if (krylov_cg_) cg_iteration<double, double>(A, J_.get(), dinv_.get(), kv, rs_, sc, stream, amg);
+      else krylov_iteration<double, double>(A, J_.get(), dinv_.get(), kv, rs_, sc, stream, e, amg);
     }
   }
   cuda_check(cudaStreamEndCapture(stream, &g), "cudaStreamEndCapture");
   cuda_check(cudaGraphInstantiate(&graphs_[slot], g, 0), "cudaGraphInstantiate");
   cudaGraphDestroy(g);
-  count_launches(-5LL * kKrylovChunk);  // the capture launched nothing; replays are counted
+  // the capture launched nothing; replays are counted
+  const long long captured = launch_count_this_thread() - before;
+  launches_per_iter_ = static_cast<int>(captured / kKrylovChunk);
+  count_launches(-captured);
   return graphs_[slot];
 }
 
-// Replays chunks of BiCGSTAB iterations until the device flag reports convergence,
-// breakdown or a non-finite value, or max_it iterations have run.  r (kr_ / fr_) holds
-// the right-hand side on entry; the solution is left in the Krylov x vector.
+// Replays chunks of Krylov (BiCGSTAB or CG) iterations until the device flag reports
+// convergence, breakdown or a non-finite value, or max_it iterations have run.  r (kr_ /
+// fr_) holds the right-hand side on entry; the solution is left in the Krylov x vector.
 int Solver::krylov_run(bool fp32, double rel, int max_it, int* iters) {
   double* sc = scal_.get();
   const int64_t n = n_;
+  const Bsr A = model.bsr(J_.get(), J32_.get());
+  const Amg* amg = use_amg_ ? &amg_ : nullptr;
   if (fp32) {
     KrylovVectors<float> kv{fx_.get(), fr_.get(), frhat_.get(), fp_.get(), fv_.get(), fs_.get(), ft_.get(),
                             fphat_.get(), fshat_.get()};
-    krylov_init<float>(kv, n, rel, rs_, sc, stream);
+    if (krylov_cg_) cg_init<float, float>(A, fdinv_.get(), kv, rel, rs_, sc, stream, amg);
+    else krylov_init<float>(kv, n, rel, rs_, sc, stream);
   } else {
     KrylovVectors<double> kv{kx_.get(), kr_.get(), krhat_.get(), kp_.get(), kv_.get(), ks_.get(), kt_.get(),
                              kphat_.get(), kshat_.get()};
-    krylov_init<double>(kv, n, rel, rs_, sc, stream);
+    if (krylov_cg_) cg_init<double, double>(A, dinv_.get(), kv, rel, rs_, sc, stream, amg);
+    else krylov_init<double>(kv, n, rel, rs_, sc, stream);
   }
   cudaGraphExec_t exec = krylov_graph(fp32);
   double h[KS_COUNT];
@@ -373,7 +407,7 @@ int Solver::krylov_run(bool fp32, double rel, int max_it, int* iters) {
   int it = 0;
   while (h[KS_DONE] == 0.0 && it < max_it) {
     cuda_check(cudaGraphLaunch(exec, stream), "cudaGraphLaunch");
-    count_launches(5LL * kKrylovChunk);
+    count_launches(static_cast<long long>(launches_per_iter_) * kKrylovChunk);
     read_scalars(h, 0, KS_COUNT);
     const int now = static_cast<int>(h[KS_ITER]);
     if (profiling_) {
@@ -457,11 +491,9 @@ int Solver::linear_solve(const double* b, double* z, double rel_tol, int* iters)
   return st;
 }
 
-void Solver::linear_step(double* x, const std::function<void(const double*, double*)>& res,
-                         const std::function<void(const double*)>& jac) {
+void Solver::linear_step(double* x, const ResFn& resjac) {
   // make_step_operator.hh:210-245: b = F(x); solve J z = b; x -= z
-  res(x, r_.get());
-  jac(x);
+  resjac(x, r_.get());
   int it = 0;
   // a linear model's stage solution is this one solve, with no Newton iteration after it to
   // absorb the solve's error: direct-solve semantics here keep the near-machine-precision
@@ -472,8 +504,7 @@ void Solver::linear_step(double* x, const std::function<void(const double*, doub
   axpy(n_, -1.0, z_.get(), x, stream);
 }
 
-void Solver::newton(double* x, const std::function<void(const double*, double*)>& res,
-                    const std::function<void(const double*)>& jac) {
+void Solver::newton(double* x, const ResFn& res, const JacFn& jac, const ResFn& resjac) {
   auto norm = [&](const double* v) -> double {
     if (norm_ == "l_2") return norm2(v);  // two_norm2: the SQUARED norm (make_step_operator.hh:274-276)
     std::vector<double> h(n_);
@@ -483,20 +514,24 @@ void Solver::newton(double* x, const std::function<void(const double*, double*)>
     for (double e : h) acc = (norm_ == "l_inf") ? std::max(acc, std::fabs(e)) : acc + std::fabs(e);
     return acc;
   };
-  res(x, r_.get());
+  // the first iterate always needs its Jacobian (unless it already satisfies the test):
+  // residual and Jacobian come from one assembly pass there
+  resjac(x, r_.get());
+  bool jac_at_x = true;
   double defect = norm(r_.get());
   const double first = defect;
   double prev = defect;
   int it = 0;
-  bool have_jac = false;
+  bool have_jac = true;
   while (true) {
     if (!std::isfinite(defect)) throw StepFailure("Newton defect is not finite");
     if (it >= it_min_ && (defect <= newton_abs_ || defect < first * newton_rel_ || defect == 0.0)) break;
     if (it >= it_max_) throw StepFailure("Newton did not converge within the iteration range", DC_ERR_DIVERGED);
-    if (!have_jac || lin_threshold_ <= 0.0 || !(prev > 0.0 && defect / prev < lin_threshold_)) {
+    if (!jac_at_x && (!have_jac || lin_threshold_ <= 0.0 || !(prev > 0.0 && defect / prev < lin_threshold_))) {
       jac(x);
       have_jac = true;
     }
+    jac_at_x = false;
     double red;
     if (lin_direct_) {
       red = direct_tol_;
@@ -554,21 +589,39 @@ void Solver::one_step(double dt) {
       model.constrain_residual(r, stream);
       ++stats.assemblies;
     };
-    auto jac = [&](const double* y) {
-      tbegin(0);
-      model.assemble(y, ti, ai, bi, nullptr, J_.get(), 2 | Model::kAssembleOverwriteJacobian, stream);
-      tend();
+    // mixed precision inside Newton: the state-dependent Jacobian terms in fp32 (the
+    // Jacobian only steers the Newton correction; the residual, the static part and the
+    // refinement stay fp64).  A linear model's single solve is its stage solution, so it
+    // keeps the fp64 Jacobian.
+    const int jmode = Model::kAssembleOverwriteJacobian |
+                      ((mixed_precision && jac_f32_ && !model.is_linear) ? Model::kAssembleJacobianF32 : 0);
+    auto finish_jac = [&]() {
       if (model.padded)
         launch_pad_identity(model.d_diag.get(), model.d_row_ns.get(), static_cast<int>(model.nnodes), model.bs,
                             J_.get(), 1.0, stream);
       model.constrain_jacobian(J_.get(), stream);
+    };
+    auto jac = [&](const double* y) {
+      tbegin(0);
+      model.assemble(y, ti, ai, bi, nullptr, J_.get(), 2 | jmode, stream);
+      tend();
+      finish_jac();
       ++stats.assemblies;
+    };
+    auto resjac = [&](const double* y, double* r) {
+      cuda_check(cudaMemcpyAsync(r, const_.get(), n_ * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");
+      tbegin(0);
+      model.assemble(y, ti, ai, bi, r, J_.get(), 3 | jmode, stream);
+      tend();
+      model.constrain_residual(r, stream);
+      finish_jac();
+      stats.assemblies += 2;
     };
     // constrained entries take their values before the stage solve; zero residual rows and
     // unit Jacobian rows keep them there
     model.apply_constraints(stage_.get(), stream);
-    if (model.is_linear) linear_step(stage_.get(), res, jac);
-    else newton(stage_.get(), res, jac);
+    if (model.is_linear) linear_step(stage_.get(), resjac);
+    else newton(stage_.get(), res, jac, resjac);
     cuda_check(cudaMemcpyAsync(us_[i].get(), stage_.get(), n_ * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");
   }
   cuda_check(cudaMemcpyAsync(x_.get(), stage_.get(), n_ * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");

@@ -103,10 +103,12 @@ class Solver {
   cudaStream_t stream;
 
  private:
-  void newton(double* x, const std::function<void(const double*, double*)>& res,
-              const std::function<void(const double*)>& jac);
-  void linear_step(double* x, const std::function<void(const double*, double*)>& res,
-                   const std::function<void(const double*)>& jac);
+  // res: residual at y; jac: Jacobian at y; resjac: both in one assembly pass
+  using ResFn = std::function<void(const double*, double*)>;
+  using JacFn = std::function<void(const double*)>;
+  void newton(double* x, const ResFn& res, const JacFn& jac, const ResFn& resjac);
+  void linear_step(double* x, const ResFn& resjac);
+  bool jac_f32_ = true;  // mixed precision: state-dependent Jacobian terms in fp32
   void setup_preconditioner();
   static constexpr int kKrylovChunk = 8;   // BiCGSTAB iterations per graph replay
   cudaGraphExec_t graphs_[4] = {nullptr, nullptr, nullptr, nullptr};  // {fp64, fp32} x {plain, profiled}
@@ -153,6 +155,8 @@ class Solver {
   std::string norm_ = "l_2";
   double lin_rel_ = 1e-4;
   bool lin_direct_ = true;
+  bool krylov_cg_ = false;        // preconditioned CG instead of BiCGSTAB
+  int launches_per_iter_ = 5;     // kernels of one captured Krylov iteration
   double direct_tol_ = 1e-10;
   int lin_max_it_ = 500;
   std::string precond_ = "Jacobi";

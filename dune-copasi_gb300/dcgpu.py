@@ -280,6 +280,29 @@ class Model:
         order = np.argsort(dofs, kind="stable")
         return dofs[order], vals[order]
 
+    def _layout(self):
+        """[(species names of one compartment, vertex ids, first DOF)] in DOF order
+        (compartment-major, vertex-major, species interleaved)."""
+        out, off, i = [], 0, 0
+        names = self.species
+        while i < len(names):
+            verts = self.species_vertices(names[i])
+            group = [names[i]]
+            while i + len(group) < len(names) and \
+                    np.array_equal(self.species_vertices(names[i + len(group)]), verts):
+                group.append(names[i + len(group)])
+            out.append((group, verts, off))
+            off += len(group) * len(verts)
+            i += len(group)
+        return out
+
+    def species_dofs(self, name):
+        """Indices of a species' DOFs in the reference-order state vector."""
+        for group, verts, off in self._layout():
+            if name in group:
+                return off + group.index(name) + len(group) * np.arange(len(verts))
+        raise KeyError(name)
+
     def seeded_state(self, init):
         """State vector (reference DOF order) with init(species name, vertex coords) per
         species; species for which init returns None keep their initial.expression values."""

@@ -435,3 +435,53 @@ def test_gmsh_grid_matches_oracle(dcgpu_lib, tmp_path, dim):
         for name, e in errs.items():
             assert e <= STEP_TOL, (dim, t, name, e)
         assert abs(n_o - n_g) <= max(1, stages)
+
+
+def test_matrix_free_configuration(dcgpu_lib):
+    """linear_solver.matrix_free = true (make_step_operator.hh:289-293) is accepted and gives
+    the reference's Jacobian products (applied from the assembled matrix); a non-boolean
+    value is a configuration error."""
+    ini, init = ALL_CASES["features_2d"]()
+    ov = {"model.time_step_operator.linear_solver.matrix_free": "true"}
+    records = _run_both(dcgpu_lib, ini, init, overrides=ov)
+    for t, errs, n_o, n_g, stages in records:
+        for name, e in errs.items():
+            assert e <= STEP_TOL, (t, name, e)
+        assert abs(n_o - n_g) <= max(1, stages)
+    with pytest.raises(dcgpu_lib.DcError):
+        dcgpu_lib.Model(ini, {"model.time_step_operator.linear_solver.matrix_free": "maybe"})
+
+
+@pytest.mark.parametrize("precond", ["Jacobi", "AMG"])
+@pytest.mark.parametrize("mixed", [False, True])
+def test_cg_matches_oracle(dcgpu_lib, precond, mixed):
+    """linear_solver.type = CG (dune-istl CGSolver) on a symmetric model, block Jacobi or
+    multigrid preconditioned, fp64 or fp32-in-fp64: the oracle's solution within the Newton
+    tolerance."""
+    ini, init = ALL_CASES["heat"]()
+    ov = {"model.time_step_operator.linear_solver.type": "CG",
+          "model.time_step_operator.linear_solver.preconditioner.type": precond,
+          "model.time_step_operator.linear_solver.preconditioner.coarsen_target": "16",
+          "model.time_step_operator.nonlinear_solver.convergence_condition.relative_tolerance": "1e-24"}
+    records = _run_both(dcgpu_lib, ini, init, mixed=mixed, overrides=ov)
+    for t, errs, n_o, n_g, stages in records:
+        for e in errs.values():
+            assert e <= STEP_TOL, (precond, mixed, t, e)
+
+
+def test_fp32_and_fp64_jacobian_in_mixed_precision(dcgpu_lib):
+    """Mixed precision with the state-dependent Jacobian terms in fp32 (default) or fp64:
+    both meet the oracle tolerance and reach the same state to well within it."""
+    ini, init = ALL_CASES["features_2d"]()
+    finals = []
+    for jp in ("single", "double"):
+        ov = {"model.time_step_operator.linear_solver.jacobian_precision": jp}
+        records = _run_both(dcgpu_lib, ini, init, mixed=True, overrides=ov)
+        for t, errs, n_o, n_g, stages in records:
+            for e in errs.values():
+                assert e <= STEP_TOL, (jp, t, e)
+        finals.append(records[-1][1])
+    with pytest.raises(dcgpu_lib.DcError):
+        dcgpu_lib.Model(ini, {"model.time_step_operator.linear_solver.jacobian_precision": "half"})
+    with pytest.raises(dcgpu_lib.DcError):
+        dcgpu_lib.Model(ini, {"model.time_step_operator.linear_solver.type": "QMR"})

@@ -63,6 +63,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--large-n", type=int, default=128,
                     help="cube edge of the HBM-resident SpMV measurement (0 disables it)")
+    ap.add_argument("--serve-active", type=int, default=8,
+                    help="simulations the request server runs at once (each on its own stream)")
     ap.add_argument("--serve-requests", type=int, default=32,
                     help="requests of the Poisson serving stream (0 disables the serving measurement)")
     return ap.parse_args()
@@ -445,7 +447,7 @@ def main():
         roof["spmv_hbm_resident"] = large_spmv(dcgpu, args.precision, peak_gbs, args.large_n, args.spmv)
     serving = None
     if args.serve_requests > 0:
-        served = run_serving(dcgpu, args.serve_requests, 50.0, 8, args.precision)
+        served = run_serving(dcgpu, args.serve_requests, 50.0, args.serve_active, args.precision)
         alone = run_serving(dcgpu, args.serve_requests, 50.0, 1, "fp64")
         serving = {"served_concurrent": served, "plain_fp64_one_at_a_time": alone,
                    "speedup": served["value"] / alone["value"] if alone["value"] > 0 else None}

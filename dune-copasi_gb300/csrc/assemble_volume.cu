@@ -360,25 +360,39 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
           }
         }
       }
+      // rl[a][s] += (scal[s] phi_a - flux[s] . G_a) fq, with the factor fq applied once per
+      // species rather than per entry (one FMA per entry for the scalar part)
+      double ts[NS];
+#pragma unroll
+      for (int s = 0; s < NS; ++s) ts[s] = scal[s] * fq;
 #pragma unroll
       for (int a = 0; a < NL; ++a) {
         const double pa = phi<DIM>(q, a);
 #pragma unroll
-        for (int s = 0; s < NS; ++s) {
-          double fg = 0.0;
-          if (P.has_flux) {
+        for (int s = 0; s < NS; ++s) rl[a][s] = fma(ts[s], pa, rl[a][s]);
+      }
+      if (P.has_flux) {
 #pragma unroll
-            for (int j = 0; j < DIM; ++j) fg += flux[s][j] * G[a][j];
+        for (int s = 0; s < NS; ++s) {
+          double tf[DIM];
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) tf[j] = flux[s][j] * fq;
+#pragma unroll
+          for (int a = 0; a < NL; ++a) {
+            double fg = 0.0;
+#pragma unroll
+            for (int j = 0; j < DIM; ++j) fg = fma(tf[j], G[a][j], fg);
+            rl[a][s] -= fg;
           }
-          rl[a][s] += (scal[s] * pa - fg) * fq;
         }
       }
     }
 
     if (do_jac) {
+      const double scm = P.cm * fq, sca = P.ca * fq;
       for (int t = 0; t < P.n_jac_terms; ++t) {
         const Term T = P.jac_terms[t];
-        const double sc = (T.form ? P.ca : P.cm) * fq;
+        const double sc = T.form ? sca : scm;
         const double o = R[out[T.out]];
         double ut = 0.0;
 #pragma unroll

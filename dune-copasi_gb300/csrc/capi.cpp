@@ -59,6 +59,18 @@ int dc_model_create(const char* ini_text, const char* overrides, dc_model** out)
   });
 }
 
+int dc_config_get(const dc_model* model, const char* key, char* buf, size_t len) {
+  return guarded([&] {
+    if (!model || !key || !buf || len == 0) throw std::invalid_argument("null argument");
+    const auto& cfg = model->model->cfg;
+    if (!cfg.has_key(key)) throw dcgpu::ConfigError(std::string("no configuration key '") + key + "'");
+    const std::string v = cfg.get(key, "");
+    std::strncpy(buf, v.c_str(), len - 1);
+    buf[len - 1] = '\0';
+    return DC_OK;
+  });
+}
+
 int dc_model_destroy(dc_model* model) {
   return guarded([&] {
     if (!model) return DC_OK;

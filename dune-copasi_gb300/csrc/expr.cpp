@@ -190,6 +190,11 @@ ParserContext::ParserContext(const Ini& cfg) {
     if (type == "constant") {
       constants[name] = sub.get_double("value", 0.0);
     } else if (type == "function") {
+      // context.cc:237-280 can replace a 1-argument function by a table lookup; that
+      // variant is not provided here, and silently evaluating the exact function instead
+      // would change the results by the table's resolution
+      if (sub.get_bool("interpolate", false))
+        throw ConfigError("parser_context." + name + ".interpolate = true is not supported");
       std::string e = sub.at("expression");
       auto colon = e.find(':');
       if (colon == std::string::npos)

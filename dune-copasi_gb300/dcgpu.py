@@ -34,7 +34,7 @@ EXPORTED = [
     "dc_expr_eval", "dc_stream_handle", "dc_launch_count", "dc_profile_enable", "dc_profile_get",
     "dc_assemble_residual_noalloc", "dc_server_create", "dc_server_submit", "dc_server_poll",
     "dc_server_take_state", "dc_server_estimate", "dc_server_destroy", "dc_last_error",
-    "dc_spmv_format", "dc_vertex_coords", "dc_constraints", "dc_reduce", "dc_write_vtk",
+    "dc_spmv_format", "dc_vertex_coords", "dc_constraints", "dc_reduce", "dc_write_vtk", "dc_config_get",
 ]
 
 
@@ -129,6 +129,7 @@ def load_library(path=LIB_PATH):
     lib.dc_constraints.argtypes = [vp, P(ctypes.c_int64), pd, sz, P(sz)]
     lib.dc_reduce.argtypes = [vp, ctypes.c_char_p, P(ReduceValue), sz, P(sz)]
     lib.dc_write_vtk.argtypes = [vp, ctypes.c_char_p, ctypes.c_int]
+    lib.dc_config_get.argtypes = [vp, ctypes.c_char_p, ctypes.c_char_p, sz]
     lib.dc_last_error.argtypes = []
     lib.dc_last_error.restype = ctypes.c_char_p
     for name in EXPORTED:
@@ -244,6 +245,12 @@ class Model:
         out = np.empty((self.info["n_vertices"], self.info["dim"]))
         _check(self._lib.dc_vertex_coords(self._h, _ptr(out), out.size))
         return out
+
+    def config_get(self, key):
+        """Value of a configuration key (after overrides), or None when absent."""
+        buf = ctypes.create_string_buffer(4096)
+        st = self._lib.dc_config_get(self._h, key.encode(), buf, 4096)
+        return buf.value.decode() if st == DC_OK else None
 
     def write_vtk(self, path, append=True):
         """VTK output of the current state: per compartment <path>/<stem>-<compartment>-NNNNN.vtu

@@ -60,6 +60,11 @@ typedef void (*dc_callback)(const dc_model* model, double time, void* user);
  * content; `overrides` holds "key=value" lines (the CLI's --key=value, src/dune_copasi.cc:
  * 270-288) or is NULL.  The state is initialised from the initial conditions. */
 int dc_model_create(const char* ini_text, const char* overrides, dc_model** out);
+/* Value of a configuration key after the overrides (Dune::ParameterTree::get on the model's
+ * configuration): copies the value into buf (NUL-terminated, truncated to len); returns
+ * DC_ERR_CONFIG when the key is absent.  For callers such as the CLI's writer / reduce
+ * settings (src/dune_copasi.cc:403-423). */
+int dc_config_get(const dc_model* model, const char* key, char* buf, size_t len);
 int dc_model_destroy(dc_model* model);
 int dc_model_info_get(const dc_model* model, dc_model_info* info);
 

@@ -434,6 +434,8 @@ class Context:
             if typ == "constant":
                 self.constants[name] = float(sub["value"])
             elif typ == "function":
+                if sub.get_bool("interpolate", False):
+                    raise ExprError("parser_context.%s.interpolate = true is not supported" % name)
                 self.functions[name] = parse_function_definition(sub["expression"])
             elif typ == "interpolation":
                 dom = sub.get_floats("domain")

@@ -63,7 +63,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--large-n", type=int, default=128,
                     help="cube edge of the HBM-resident SpMV measurement (0 disables it)")
-    ap.add_argument("--serve-active", type=int, default=8,
+    ap.add_argument("--serve-active", type=int, default=16,
                     help="simulations the request server runs at once (each on its own stream)")
     ap.add_argument("--serve-requests", type=int, default=32,
                     help="requests of the Poisson serving stream (0 disables the serving measurement)")

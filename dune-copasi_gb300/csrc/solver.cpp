@@ -4,8 +4,10 @@
 #include <cfloat>
 #include <cmath>
 #include <limits>
+#include <type_traits>
 
 #include "assemble.cuh"
+#include "gmres.cuh"
 #include "linalg.cuh"
 
 namespace dcgpu {
@@ -110,14 +112,21 @@ Solver::Solver(Model& m, cudaStream_t s) : model(m), stream(s) {
   // by a BiCGSTAB solve converged to near machine precision
   lin_direct_ = (lt == "UMFPack" || lt == "SuperLU" || lt == "DenseInverse");
   // iterative registry of solver/istl/factory/iterative.hh:84-105: CG and the flexible /
-  // generalized PCG variants (identical to CG for a fixed preconditioner) run as CG; the
-  // others (Loop, Gradient, MINRES, the GMRes variants) converge to the same solution of the
-  // same correction equation and run as BiCGSTAB
+  // generalized PCG variants (identical to CG for a fixed preconditioner) run as CG, the
+  // GMRes variants as restarted GMRES (restart key as iterative.hh:63-64); Loop, Gradient
+  // and MINRES converge to the same solution of the same correction equation and run as
+  // BiCGSTAB
   if (!lin_direct_) {
-    if (lt == "CG" || lt == "GeneralizedPCG" || lt == "RestartedFCG" || lt == "CompleteFCG") krylov_cg_ = true;
-    else if (lt != "BiCGSTAB" && lt != "Loop" && lt != "Gradient" && lt != "MINRES" && lt != "RestartedGMRes" &&
-             lt != "RestartedFlexibleGMRes")
+    if (lt == "CG" || lt == "GeneralizedPCG" || lt == "RestartedFCG" || lt == "CompleteFCG") {
+      krylov_cg_ = true;
+    } else if (lt == "RestartedGMRes" || lt == "RestartedFlexibleGMRes") {
+      // the flexible variant equals GMRES for a fixed preconditioner
+      krylov_gmres_ = true;
+      gmres_restart_ = static_cast<int>(ls.get_long("restart", 40));
+      if (gmres_restart_ < 1 || gmres_restart_ > 500) throw ConfigError("linear_solver.restart must be in [1, 500]");
+    } else if (lt != "BiCGSTAB" && lt != "Loop" && lt != "Gradient" && lt != "MINRES") {
       throw ConfigError("Not known linear solver type '" + lt + "'");
+    }
   }
   lin_rel_ = ls.get_double("convergence_condition.relative_tolerance", 1e-4);
   lin_max_it_ = 500;
@@ -382,10 +391,147 @@ cudaGraphExec_t Solver::krylov_graph(bool fp32) {
   return graphs_[slot];
 }
 
+// Restarted GMRES with right preconditioning (dune-istl RestartedGMResSolver semantics:
+// restart length m, relative reduction of the residual norm), classical Gram-Schmidt with
+// one re-orthogonalisation pass, Givens rotations on the host (one synchronisation per
+// iteration).  Right-hand side in kr_ / fr_, solution left in kx_ / fx_.
+template <class T>
+int Solver::gmres_t(double rel, int max_it, int* iters) {
+  constexpr bool f32 = std::is_same_v<T, float>;
+  const int64_t n = n_;
+  const int m = gmres_restart_;
+  DeviceBuffer<T>& Vbuf = [&]() -> DeviceBuffer<T>& {
+    if constexpr (f32) return gV32_;
+    else return gV_;
+  }();
+  if (Vbuf.size() != static_cast<size_t>(m + 1) * n) Vbuf.resize(static_cast<size_t>(m + 1) * n);
+  if (gh_.size() < static_cast<size_t>(3 * (m + 2))) gh_.resize(3 * (m + 2));
+  if (gpart_.size() < static_cast<size_t>(kGmresBlocks) * (m + 1)) gpart_.resize(static_cast<size_t>(kGmresBlocks) * (m + 1));
+  T* V = Vbuf.get();
+  T* b = f32 ? reinterpret_cast<T*>(fr_.get()) : reinterpret_cast<T*>(kr_.get());
+  T* x = f32 ? reinterpret_cast<T*>(fx_.get()) : reinterpret_cast<T*>(kx_.get());
+  T* r = f32 ? reinterpret_cast<T*>(frhat_.get()) : reinterpret_cast<T*>(krhat_.get());
+  T* z = f32 ? reinterpret_cast<T*>(fphat_.get()) : reinterpret_cast<T*>(kphat_.get());
+  T* u = f32 ? reinterpret_cast<T*>(fv_.get()) : reinterpret_cast<T*>(kv_.get());
+  double* h1 = gh_.get();
+  double* h2 = gh_.get() + (m + 2);
+  double* hn = gh_.get() + 2 * (m + 2);
+  const Bsr A = model.bsr(J_.get(), J32_.get());
+  const Sell S = model.sell();
+  // the multigrid cycle checks a device "done" flag: keep it cleared
+  cuda_check(cudaMemsetAsync(scal_.get(), 0, KS_COUNT * sizeof(double), stream), "memset");
+  auto precond = [&](const T* in, T* out) {
+    if (use_amg_) {
+      amg_.apply<T>(in, out, scal_.get(), KS_DONE, stream);
+    } else if constexpr (f32) {
+      block_jacobi_apply32(static_cast<int>(model.nnodes), model.bs, fdinv_.get(), in, out, stream);
+    } else {
+      block_jacobi_apply(static_cast<int>(model.nnodes), model.bs, dinv_.get(), in, out, stream);
+    }
+  };
+  auto apply_A = [&](const T* in, T* out) {
+    if constexpr (f32) {
+      if (spmv_format == kSpmvSell) spmv_sell32(S, Js32_.get(), in, out, stream);
+      else spmv32_vals(A, J32_.get(), in, out, stream);
+    } else {
+      spmv(A, in, out, stream);
+    }
+  };
+  auto norm = [&](const T* v) {
+    gmres_mdot<T>(v, n, 1, v, hn, gpart_.get(), false, stream);
+    double h = 0.0;
+    cuda_check(cudaMemcpyAsync(&h, hn, sizeof(double), cudaMemcpyDeviceToHost, stream), "gmres");
+    cuda_check(cudaStreamSynchronize(stream), "gmres");
+    return std::sqrt(h);
+  };
+  cuda_check(cudaMemsetAsync(x, 0, n * sizeof(T), stream), "memset");
+  cuda_check(cudaMemcpyAsync(r, b, n * sizeof(T), cudaMemcpyDeviceToDevice, stream), "copy");
+  const double beta0 = norm(r);
+  *iters = 0;
+  if (beta0 == 0.0) return DC_OK;
+  if (!std::isfinite(beta0)) return DC_ERR_DIVERGED;
+  const double target = rel * beta0;
+  double beta = beta0;
+  std::vector<double> H(static_cast<size_t>(m + 1) * m), cs(m), sn(m), g(m + 1), hc1(m + 1), hc2(m + 1);
+  int total = 0;
+  while (true) {
+    gmres_scale_value<T>(V, r, n, 1.0 / beta, stream);
+    std::fill(g.begin(), g.end(), 0.0);
+    g[0] = beta;
+    int k = 0;
+    for (int j = 0; j < m && total < max_it; ++j) {
+      T* vj1 = V + static_cast<int64_t>(j + 1) * n;
+      precond(V + static_cast<int64_t>(j) * n, z);
+      apply_A(z, vj1);
+      gmres_mdot<T>(V, n, j + 1, vj1, h1, gpart_.get(), false, stream);
+      gmres_maxpy<T>(vj1, V, n, j + 1, h1, -1.0, stream);
+      gmres_mdot<T>(V, n, j + 1, vj1, h2, gpart_.get(), false, stream);
+      gmres_maxpy<T>(vj1, V, n, j + 1, h2, -1.0, stream);
+      gmres_mdot<T>(vj1, n, 1, vj1, hn, gpart_.get(), false, stream);
+      cuda_check(cudaMemcpyAsync(hc1.data(), h1, (j + 1) * sizeof(double), cudaMemcpyDeviceToHost, stream), "gmres");
+      cuda_check(cudaMemcpyAsync(hc2.data(), h2, (j + 1) * sizeof(double), cudaMemcpyDeviceToHost, stream), "gmres");
+      double nn = 0.0;
+      cuda_check(cudaMemcpyAsync(&nn, hn, sizeof(double), cudaMemcpyDeviceToHost, stream), "gmres");
+      cuda_check(cudaStreamSynchronize(stream), "gmres");
+      const double hj1 = std::sqrt(nn);
+      if (!std::isfinite(hj1)) return DC_ERR_DIVERGED;
+      double* col = &H[static_cast<size_t>(j) * (m + 1)];
+      for (int i = 0; i <= j; ++i) col[i] = hc1[i] + hc2[i];
+      col[j + 1] = hj1;
+      if (hj1 > 0.0) gmres_scale_value<T>(vj1, vj1, n, 1.0 / hj1, stream);
+      // previous rotations, then the one that zeroes col[j + 1]
+      for (int i = 0; i < j; ++i) {
+        const double t0 = cs[i] * col[i] + sn[i] * col[i + 1];
+        col[i + 1] = -sn[i] * col[i] + cs[i] * col[i + 1];
+        col[i] = t0;
+      }
+      const double den = std::hypot(col[j], col[j + 1]);
+      cs[j] = den > 0.0 ? col[j] / den : 1.0;
+      sn[j] = den > 0.0 ? col[j + 1] / den : 0.0;
+      col[j] = den;
+      col[j + 1] = 0.0;
+      g[j + 1] = -sn[j] * g[j];
+      g[j] = cs[j] * g[j];
+      ++total;
+      k = j + 1;
+      if (std::fabs(g[j + 1]) <= target || hj1 == 0.0) break;
+    }
+    if (k == 0) break;
+    // y = H^-1 g (upper triangular), x += M^-1 (V y)
+    std::vector<double> y(k);
+    for (int i = k - 1; i >= 0; --i) {
+      double s = g[i];
+      for (int l = i + 1; l < k; ++l) s -= H[static_cast<size_t>(l) * (m + 1) + i] * y[l];
+      const double d = H[static_cast<size_t>(i) * (m + 1) + i];
+      y[i] = d != 0.0 ? s / d : 0.0;
+    }
+    cuda_check(cudaMemcpyAsync(h1, y.data(), k * sizeof(double), cudaMemcpyHostToDevice, stream), "gmres");
+    cuda_check(cudaMemsetAsync(u, 0, n * sizeof(T), stream), "memset");
+    gmres_maxpy<T>(u, V, n, k, h1, 1.0, stream);
+    precond(u, z);
+    const double one = 1.0;
+    cuda_check(cudaMemcpyAsync(h2, &one, sizeof(double), cudaMemcpyHostToDevice, stream), "gmres");
+    gmres_maxpy<T>(x, z, n, 1, h2, 1.0, stream);
+    // true residual of the restart
+    apply_A(x, r);
+    gmres_sub_from<T>(r, b, n, stream);
+    beta = norm(r);
+    if (!std::isfinite(beta)) return DC_ERR_DIVERGED;
+    if (beta <= target) {
+      *iters = total;
+      return DC_OK;
+    }
+    if (total >= max_it) break;
+  }
+  *iters = total;
+  return beta <= target ? DC_OK : DC_ERR_TIMEOUT;
+}
+
 // Replays chunks of Krylov (BiCGSTAB or CG) iterations until the device flag reports
 // convergence, breakdown or a non-finite value, or max_it iterations have run.  r (kr_ /
 // fr_) holds the right-hand side on entry; the solution is left in the Krylov x vector.
 int Solver::krylov_run(bool fp32, double rel, int max_it, int* iters) {
+  if (krylov_gmres_) return fp32 ? gmres_t<float>(rel, max_it, iters) : gmres_t<double>(rel, max_it, iters);
   double* sc = scal_.get();
   const int64_t n = n_;
   const Bsr A = model.bsr(J_.get(), J32_.get());

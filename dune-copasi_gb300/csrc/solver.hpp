@@ -156,6 +156,12 @@ class Solver {
   double lin_rel_ = 1e-4;
   bool lin_direct_ = true;
   bool krylov_cg_ = false;        // preconditioned CG instead of BiCGSTAB
+  bool krylov_gmres_ = false;     // restarted GMRES (right-preconditioned) instead of BiCGSTAB
+  int gmres_restart_ = 40;
+  DeviceBuffer<double> gV_, gh_, gpart_;
+  DeviceBuffer<float> gV32_;
+  template <class T>
+  int gmres_t(double rel, int max_it, int* iters);
   int launches_per_iter_ = 5;     // kernels of one captured Krylov iteration
   double direct_tol_ = 1e-10;
   int lin_max_it_ = 500;

@@ -485,3 +485,22 @@ def test_fp32_and_fp64_jacobian_in_mixed_precision(dcgpu_lib):
         dcgpu_lib.Model(ini, {"model.time_step_operator.linear_solver.jacobian_precision": "half"})
     with pytest.raises(dcgpu_lib.DcError):
         dcgpu_lib.Model(ini, {"model.time_step_operator.linear_solver.type": "QMR"})
+
+
+@pytest.mark.parametrize("restart,precond,mixed", [(40, "Jacobi", False), (5, "Jacobi", False),
+                                                   (10, "AMG", False), (10, "Jacobi", True)])
+def test_gmres_matches_oracle(dcgpu_lib, restart, precond, mixed):
+    """linear_solver.type = RestartedGMRes (right-preconditioned, restart m) on a
+    non-symmetric model (velocity and tensor diffusion): the oracle's solution within the
+    Newton tolerance, also with short restarts, multigrid, and fp32 inside fp64 refinement."""
+    ini, init = ALL_CASES["features_2d"]()
+    ov = {"model.time_step_operator.linear_solver.type": "RestartedGMRes",
+          "model.time_step_operator.linear_solver.restart": str(restart),
+          "model.time_step_operator.linear_solver.preconditioner.type": precond,
+          "model.time_step_operator.linear_solver.preconditioner.coarsen_target": "16",
+          "model.time_step_operator.linear_solver.convergence_condition.relative_tolerance": "1e-12",
+          "model.time_step_operator.nonlinear_solver.convergence_condition.relative_tolerance": "1e-24"}
+    records = _run_both(dcgpu_lib, ini, init, mixed=mixed, overrides=ov)
+    for t, errs, n_o, n_g, stages in records:
+        for e in errs.values():
+            assert e <= STEP_TOL, (restart, precond, mixed, t, e)

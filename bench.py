@@ -48,7 +48,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n", type=int, default=512)
+    # "--grid" is the spelling to use after a torchrun launcher, whose own parser reads
+    # "--n" as an ambiguous abbreviation of its options
+    ap.add_argument("--n", "--grid", dest="n", type=int, default=512)
     ap.add_argument("--workload", default="gray_scott", choices=["gray_scott", "cross_diffusion_3d"],
                     help="gray_scott (headline, n = grid edge) or cross_diffusion_3d (n = cube edge)")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"],
@@ -68,6 +70,17 @@ def parse():
     ap.add_argument("--serve-requests", type=int, default=32,
                     help="requests of the Poisson serving stream (0 disables the serving measurement)")
     return ap.parse_args()
+
+
+def max_over_ranks(x, dist):
+    """The largest of the ranks' values (the slowest replica sets the time); x itself when
+    not distributed."""
+    if not dist:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
 
 def dist_setup(args):
@@ -378,10 +391,7 @@ def main():
     torch.cuda.synchronize()
     kt = model.kernel_times()
     model.profile(False)
-    if dist:
-        t = torch.tensor([total_ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, dist)
     value = world * ndof * newton / (total_ms * 1e-3)
 
     # end to end through the C ABI with host buffers (upload, step, download)

@@ -85,117 +85,6 @@ struct StoreFin {
   __device__ void operator()(const double (&t)[1]) const { *out = t[0]; }
 };
 
-// ---------------------------------------------------------------- BiCGSTAB pieces
-
-template <class T>
-struct InitBody {
-  const T* r; T* rhat; T* p; T* v;
-  __device__ void operator()(int64_t i, double (&acc)[1]) const {
-    const T ri = r[i];
-    rhat[i] = ri;
-    p[i] = T(0);
-    v[i] = T(0);
-    acc[0] += static_cast<double>(ri) * static_cast<double>(ri);
-  }
-};
-struct InitFin {
-  double* sc;
-  __device__ void operator()(const double (&t)[1]) const {
-    sc[7] = t[0];
-    sc[3] = t[0];
-    sc[1] = 1.0;
-    sc[2] = 1.0;
-    sc[9] = t[0];       // beta = (rho_new / 1) * (1 / 1)
-    sc[0] = t[0];
-    sc[10] = (t[0] == 0.0 || !isfinite(t[0])) ? 1.0 : 0.0;
-  }
-};
-
-template <class T>
-__global__ void k_update_p(T* p, const T* r, const T* v, int64_t n, const double* sc) {
-  const double beta = sc[9], omega = sc[2];
-  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride)
-    p[i] = static_cast<T>(static_cast<double>(r[i]) + beta * (static_cast<double>(p[i]) - omega * static_cast<double>(v[i])));
-}
-
-template <class T>
-struct Dot1Body {
-  const T* a; const T* b;
-  __device__ void operator()(int64_t i, double (&acc)[1]) const {
-    acc[0] += static_cast<double>(a[i]) * static_cast<double>(b[i]);
-  }
-};
-struct AlphaFin {
-  double* sc;
-  __device__ void operator()(const double (&t)[1]) const {
-    sc[4] = t[0];
-    const double a = sc[0] / t[0];
-    if (t[0] == 0.0 || !isfinite(a)) sc[10] = 1.0;
-    sc[1] = isfinite(a) ? a : 0.0;
-  }
-};
-
-template <class T>
-struct SBody {
-  T* s; const T* r; const T* v; const double* sc;
-  __device__ void operator()(int64_t i, double (&acc)[1]) const {
-    const double si = static_cast<double>(r[i]) - sc[1] * static_cast<double>(v[i]);
-    const T st = static_cast<T>(si);
-    s[i] = st;
-    acc[0] += static_cast<double>(st) * static_cast<double>(st);
-  }
-};
-struct SFin {
-  double* sc;
-  __device__ void operator()(const double (&t)[1]) const { sc[8] = t[0]; }
-};
-
-template <class T>
-struct OmegaBody {
-  const T* t; const T* s;
-  __device__ void operator()(int64_t i, double (&acc)[2]) const {
-    const double ti = static_cast<double>(t[i]);
-    acc[0] += ti * static_cast<double>(s[i]);
-    acc[1] += ti * ti;
-  }
-};
-struct OmegaFin {
-  double* sc;
-  __device__ void operator()(const double (&t)[2]) const {
-    sc[5] = t[0];
-    sc[6] = t[1];
-    double w = t[1] != 0.0 ? t[0] / t[1] : 0.0;
-    if (!isfinite(w)) { w = 0.0; sc[10] = 1.0; }
-    sc[2] = w;
-  }
-};
-
-template <class T>
-struct XrBody {
-  T* x; T* r; const T* phat; const T* shat; const T* s; const T* t; const T* rhat; const double* sc;
-  __device__ void operator()(int64_t i, double (&acc)[2]) const {
-    const double alpha = sc[1], omega = sc[2];
-    x[i] = static_cast<T>(static_cast<double>(x[i]) + alpha * static_cast<double>(phat[i]) +
-                          omega * static_cast<double>(shat[i]));
-    const T ri = static_cast<T>(static_cast<double>(s[i]) - omega * static_cast<double>(t[i]));
-    r[i] = ri;
-    acc[0] += static_cast<double>(ri) * static_cast<double>(ri);
-    acc[1] += static_cast<double>(rhat[i]) * static_cast<double>(ri);
-  }
-};
-struct XrFin {
-  double* sc;
-  __device__ void operator()(const double (&t)[2]) const {
-    sc[7] = t[0];
-    sc[3] = t[1];
-    const double beta = (t[1] / sc[0]) * (sc[1] / sc[2]);
-    if (t[1] == 0.0 || sc[2] == 0.0 || !isfinite(beta)) sc[10] = 1.0;
-    sc[9] = isfinite(beta) ? beta : 0.0;
-    sc[0] = t[1];
-  }
-};
-
 // ---------------------------------------------------------------- SpMV
 // one thread per scalar row of the BSR matrix; the bs values of a block row segment
 // are contiguous, neighbouring threads read neighbouring segments
@@ -487,58 +376,6 @@ void block_jacobi_apply(int nrows, int bs, const double* dinv, const double* x, 
 }
 void block_jacobi_apply32(int nrows, int bs, const float* dinv, const float* x, float* y, cudaStream_t s) {
   bj_apply_dispatch<float, float>(nrows, bs, dinv, x, y, s);
-}
-
-void bicg_init(const double* r, double* rhat, double* p, double* v, int64_t n, ReduceScratch rs,
-               double* sc, cudaStream_t s) {
-  reduce<1>(n, InitBody<double>{r, rhat, p, v}, InitFin{sc}, rs, s);
-}
-void bicg_update_p(double* p, const double* r, const double* v, int64_t n, const double* sc,
-                   cudaStream_t s) {
-  k_update_p<double><<<ew_blocks(n), 256, 0, s>>>(p, r, v, n, sc);
-}
-void bicg_alpha(const double* rhat, const double* v, int64_t n, ReduceScratch rs, double* sc,
-                cudaStream_t s) {
-  reduce<1>(n, Dot1Body<double>{rhat, v}, AlphaFin{sc}, rs, s);
-}
-void bicg_s(double* s_, const double* r, const double* v, int64_t n, ReduceScratch rs, double* sc,
-            cudaStream_t s) {
-  reduce<1>(n, SBody<double>{s_, r, v, sc}, SFin{sc}, rs, s);
-}
-void bicg_omega(const double* t, const double* s_, int64_t n, ReduceScratch rs, double* sc,
-                cudaStream_t s) {
-  reduce<2>(n, OmegaBody<double>{t, s_}, OmegaFin{sc}, rs, s);
-}
-void bicg_xr(double* x, double* r, const double* phat, const double* shat, const double* s_,
-             const double* t, const double* rhat, int64_t n, ReduceScratch rs, double* sc,
-             cudaStream_t s) {
-  reduce<2>(n, XrBody<double>{x, r, phat, shat, s_, t, rhat, sc}, XrFin{sc}, rs, s);
-}
-
-void bicg_init32(const float* r, float* rhat, float* p, float* v, int64_t n, ReduceScratch rs,
-                 double* sc, cudaStream_t s) {
-  reduce<1>(n, InitBody<float>{r, rhat, p, v}, InitFin{sc}, rs, s);
-}
-void bicg_update_p32(float* p, const float* r, const float* v, int64_t n, const double* sc,
-                     cudaStream_t s) {
-  k_update_p<float><<<ew_blocks(n), 256, 0, s>>>(p, r, v, n, sc);
-}
-void bicg_alpha32(const float* rhat, const float* v, int64_t n, ReduceScratch rs, double* sc,
-                  cudaStream_t s) {
-  reduce<1>(n, Dot1Body<float>{rhat, v}, AlphaFin{sc}, rs, s);
-}
-void bicg_s32(float* s_, const float* r, const float* v, int64_t n, ReduceScratch rs, double* sc,
-              cudaStream_t s) {
-  reduce<1>(n, SBody<float>{s_, r, v, sc}, SFin{sc}, rs, s);
-}
-void bicg_omega32(const float* t, const float* s_, int64_t n, ReduceScratch rs, double* sc,
-                  cudaStream_t s) {
-  reduce<2>(n, OmegaBody<float>{t, s_}, OmegaFin{sc}, rs, s);
-}
-void bicg_xr32(float* x, float* r, const float* phat, const float* shat, const float* s_,
-               const float* t, const float* rhat, int64_t n, ReduceScratch rs, double* sc,
-               cudaStream_t s) {
-  reduce<2>(n, XrBody<float>{x, r, phat, shat, s_, t, rhat, sc}, XrFin{sc}, rs, s);
 }
 
 void axpy(int64_t n, double a, const double* x, double* y, cudaStream_t s) {

@@ -56,38 +56,6 @@ void block_jacobi_setup(const Bsr& A, const int32_t* diag, double* dinv, int* st
 void block_jacobi_apply(int nrows, int bs, const double* dinv, const double* x, double* y, cudaStream_t s);
 void block_jacobi_apply32(int nrows, int bs, const float* dinv, const float* x, float* y, cudaStream_t s);
 
-// BiCGSTAB fused steps; scalars live in sc[] on the device:
-//   sc[0]=rho  sc[1]=alpha  sc[2]=omega  sc[3]=rho_new  sc[4]=<rhat,v>  sc[5]=<t,s>
-//   sc[6]=<t,t> sc[7]=||r||^2  sc[8]=||s||^2  sc[9]=beta  sc[10]=breakdown flag
-void bicg_init(const double* r, double* rhat, double* p, double* v, int64_t n, ReduceScratch rs,
-               double* sc, cudaStream_t s);
-void bicg_update_p(double* p, const double* r, const double* v, int64_t n, const double* sc,
-                   cudaStream_t s);
-void bicg_alpha(const double* rhat, const double* v, int64_t n, ReduceScratch rs, double* sc,
-                cudaStream_t s);
-void bicg_s(double* s_, const double* r, const double* v, int64_t n, ReduceScratch rs, double* sc,
-            cudaStream_t s);
-void bicg_omega(const double* t, const double* s_, int64_t n, ReduceScratch rs, double* sc,
-                cudaStream_t s);
-void bicg_xr(double* x, double* r, const double* phat, const double* shat, const double* s_,
-             const double* t, const double* rhat, int64_t n, ReduceScratch rs, double* sc,
-             cudaStream_t s);
-
-// float variants for the mixed-precision inner solve (reductions stay in fp64)
-void bicg_init32(const float* r, float* rhat, float* p, float* v, int64_t n, ReduceScratch rs,
-                 double* sc, cudaStream_t s);
-void bicg_update_p32(float* p, const float* r, const float* v, int64_t n, const double* sc,
-                     cudaStream_t s);
-void bicg_alpha32(const float* rhat, const float* v, int64_t n, ReduceScratch rs, double* sc,
-                  cudaStream_t s);
-void bicg_s32(float* s_, const float* r, const float* v, int64_t n, ReduceScratch rs, double* sc,
-              cudaStream_t s);
-void bicg_omega32(const float* t, const float* s_, int64_t n, ReduceScratch rs, double* sc,
-                  cudaStream_t s);
-void bicg_xr32(float* x, float* r, const float* phat, const float* shat, const float* s_,
-               const float* t, const float* rhat, int64_t n, ReduceScratch rs, double* sc,
-               cudaStream_t s);
-
 // number of kernels this library has launched (all threads, all models)
 long long launch_count();
 long long launch_count_this_thread();  // launches counted by the calling host thread

@@ -62,6 +62,9 @@ def parse():
                     help="layout of the fp32 Krylov operator (linear_solver.spmv)")
     ap.add_argument("--precond", default="Jacobi", choices=["Jacobi", "AMG"],
                     help="BiCGSTAB preconditioner (linear_solver.preconditioner.type)")
+    ap.add_argument("--single-launch", default="on", choices=["on", "off"],
+                    help="BiCGSTAB as one cooperative launch per solve (on) or one launch per "
+                         "phase from a CUDA graph (off) (linear_solver.single_launch)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--large-n", type=int, default=128,
                     help="cube edge of the HBM-resident SpMV measurement (0 disables it)")
@@ -261,29 +264,48 @@ def large_spmv(dcgpu, precision, peak_gbs, n=128, spmv="auto"):
     per-kernel events; returns the fused-SpMV achieved bandwidth against the HBM peak."""
     import workloads as W
     ini, init = W.cross_diffusion_3d(n=n, steps=1, dt=0.01)
-    m = dcgpu.Model(ini, {"model.time_step_operator.linear_solver.spmv": spmv})
-    if precision == "mixed":
-        m.set_mixed_precision(True)
-    m.set_state(m.seeded_state(init), 0.0)
-    m.step(0.01)  # first step: tuner, graphs
-    m.profile(True)
-    info = m.step(0.01)
-    kt = m.kernel_times()
-    m.profile(False)
-    fmt = m.spmv_format()
-    mi = m.info
-    ms, calls = kt["spmv"]
     vb = 4 if precision == "mixed" else 8
+
+    def one(single):
+        m = dcgpu.Model(ini, {"model.time_step_operator.linear_solver.spmv": spmv,
+                              "model.time_step_operator.linear_solver.single_launch": single})
+        if precision == "mixed":
+            m.set_mixed_precision(True)
+        m.set_state(m.seeded_state(init), 0.0)
+        m.step(0.01)  # first step: tuner, graphs
+        m.profile(True)
+        info = m.step(0.01)
+        kt = m.kernel_times()
+        m.profile(False)
+        fmt = m.spmv_format()
+        mi = m.info
+        m.close()
+        return info, kt, fmt, mi
+
+    # per-phase launches: the fused SpMV kernel timed on its own
+    info, kt, fmt, mi = one("false")
+    ms, calls = kt["spmv"]
     alg = spmv_bytes(mi["n_dof"], mi["n_blocks"], mi["block_size"], mi["n_block_rows"], vb)
     avg = ms * 1e-3 / max(calls, 1)
     ach = alg / avg / 1e9 if avg > 0 else 0.0
-    m.close()
-    return {"workload": "cross_diffusion_3d_%d^3x6_tets_3_species" % n, "dof": mi["n_dof"],
-            "blocks": mi["n_blocks"], "block_size": mi["block_size"], "precision": precision,
-            "spmv_layout": fmt["format"], "tuner_us": {"bsr": fmt["bsr_us"], "sell": fmt["sell_us"]},
-            "algorithmic_bytes_per_launch": alg, "avg_launch_us": avg * 1e6, "launches": calls,
+    out = {"workload": "cross_diffusion_3d_%d^3x6_tets_3_species" % n, "dof": mi["n_dof"],
+           "blocks": mi["n_blocks"], "block_size": mi["block_size"], "precision": precision,
+           "spmv_layout": fmt["format"], "tuner_us": {"bsr": fmt["bsr_us"], "sell": fmt["sell_us"]},
+           "algorithmic_bytes_per_launch": alg, "avg_launch_us": avg * 1e6, "launches": calls,
+           "achieved": ach, "peak": peak_gbs, "unit": "GB/s", "frac": ach / peak_gbs,
+           "newton_iterations": info["newton_iterations"], "krylov_iterations": info["linear_iterations"]}
+    # single-launch solve: whole BiCGSTAB iterations on the same operator
+    info, kt, fmt, mi = one("true")
+    ms, iters = kt["krylov_iteration"]
+    if iters:
+        alg = krylov_iteration_bytes(mi["n_dof"], mi["n_blocks"], mi["block_size"], mi["n_block_rows"], vb)
+        avg = ms * 1e-3 / iters
+        ach = alg / avg / 1e9 if avg > 0 else 0.0
+        out["single_launch_iteration"] = {
+            "algorithmic_bytes_per_iteration": alg, "avg_iteration_us": avg * 1e6, "iterations": iters,
             "achieved": ach, "peak": peak_gbs, "unit": "GB/s", "frac": ach / peak_gbs,
-            "newton_iterations": info["newton_iterations"], "krylov_iterations": info["linear_iterations"]}
+            "spmv_layout": fmt["format"]}
+    return out
 
 
 def spmv_bytes(ndof, nnzb, bs, nrows, vbytes):
@@ -291,6 +313,16 @@ def spmv_bytes(ndof, nnzb, bs, nrows, vbytes):
     indices + row pointers + x read once + y written once + the dot-product partner
     vector read once."""
     return nnzb * (bs * bs * vbytes + 4) + (nrows + 1) * 4 + 3 * ndof * vbytes
+
+
+def krylov_iteration_bytes(ndof, nnzb, bs, nrows, vbytes):
+    """Algorithmic bytes of one iteration of the single-launch BiCGSTAB + block Jacobi:
+    two fused SpMVs (as spmv_bytes), the p update with its Jacobi apply (r, p, v read;
+    p, phat written; the inverse diagonal blocks read), the s update with its Jacobi apply
+    (r, v read; s, shat written; the blocks read) and the x / r update (x, phat, shat, s,
+    t, rhat read; x, r written)."""
+    return (2 * spmv_bytes(ndof, nnzb, bs, nrows, vbytes) + (5 + 4 + 8) * ndof * vbytes
+            + 2 * nrows * bs * bs * vbytes)
 
 
 def assembly_bytes(ne, nl, ns, ndof, nnz, jac):
@@ -321,8 +353,10 @@ def main():
         dist.init_process_group("gloo")
 
     ini, init, dt0, wdesc = make_workload(args.n, args.workload)
+    single = "true" if args.single_launch == "on" else "false"
     model = dcgpu.Model(ini, {"model.time_step_operator.linear_solver.spmv": args.spmv,
-                              "model.time_step_operator.linear_solver.preconditioner.type": args.precond})
+                              "model.time_step_operator.linear_solver.preconditioner.type": args.precond,
+                              "model.time_step_operator.linear_solver.single_launch": single})
     if args.precision == "mixed":
         model.set_mixed_precision(True)
     x0 = model.seeded_state(init)
@@ -363,7 +397,8 @@ def main():
     plain = None
     if args.precision == "mixed" and not args.no_plain_fp64:
         xm = model.state()
-        ref = dcgpu.Model(ini, {"model.time_step_operator.linear_solver.preconditioner.type": args.precond})
+        ref = dcgpu.Model(ini, {"model.time_step_operator.linear_solver.preconditioner.type": args.precond,
+                                "model.time_step_operator.linear_solver.single_launch": single})
         ref.set_state(x0, 0.0)
         d = dt0
         for _ in range(args.warmup):
@@ -435,14 +470,20 @@ def main():
         avg_s = ms * 1e-3 / max(calls, 1)
         if name == "spmv":
             alg = spmv_bytes(ndof, nnzb, bs, nrows, vbytes)
+        elif name == "krylov_iteration":
+            alg = krylov_iteration_bytes(ndof, nnzb, bs, nrows, vbytes)
         elif name == "assembly":
             alg = assembly_bytes(ne, wdesc["nl"], wdesc["species"], ndof, nnzb * bs * bs, jac=True)
         else:
             alg = nrows * bs * bs * vbytes + 2 * ndof * vbytes
         achieved = alg / avg_s / 1e9 if avg_s > 0 else 0.0
-        return {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": peak_gbs, "unit": "GB/s",
-                "frac": achieved / peak_gbs, "peak_source": peak_src, "traffic": None,
-                "algorithmic_bytes_per_launch": alg, "avg_launch_us": avg_s * 1e6, "launches": calls}
+        r = {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": peak_gbs, "unit": "GB/s",
+             "frac": achieved / peak_gbs, "peak_source": peak_src, "traffic": None,
+             "algorithmic_bytes_per_launch": alg, "avg_launch_us": avg_s * 1e6, "launches": calls}
+        if name == "krylov_iteration":
+            # one cooperative launch runs a whole solve: bytes and time are per iteration
+            r["per"] = "BiCGSTAB iteration inside k_bicgstab_fused"
+        return r
 
     dom = max(cats, key=lambda k: cats[k][0]) if cats else "spmv"
     roof = cat_roof(dom)
@@ -470,6 +511,8 @@ def main():
                        "linear_solver": "BiCGSTAB+%s to 1e-10 (direct-solve semantics)"
                                         % ("block-Jacobi" if args.precond == "Jacobi" else "aggregation-AMG"),
                        "spmv_layout": model.spmv_format()["format"],
+                       "krylov_launch": "single cooperative launch per solve" if single == "true"
+                                        else "one launch per phase, CUDA graph of 8 iterations",
                        "newton_rel_tol_sq": 1e-10, "l2_flush": "256 MiB write between timed steps",
                        "newton_iterations": newton, "krylov_iterations": linear},
             "plain_fp64": plain,

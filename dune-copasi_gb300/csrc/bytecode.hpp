@@ -25,6 +25,8 @@ enum Op : uint8_t {
   OP_SEL,      // r[dst] = r[a] != 0 ? r[b] : r[c]
   OP_POWI,     // r[dst] = r[a] ^ (int8)c   (small integer exponent, by multiplication)
   OP_INTERP,   // r[dst] = table[b](r[a])  (1-D linear interpolation, clamped)
+  OP_FTAB,     // r[dst] = tabulated function b at r[a]  (`interpolate = true` functions)
+  OP_TIFF,     // r[dst] = grayscale image b at (r[a], r[c])
   OP_COUNT
 };
 
@@ -49,5 +51,7 @@ enum InputKind : uint16_t {
 
 constexpr int kMaxRegisters = 64;
 constexpr int kMaxInterpTables = 16;
+constexpr int kMaxFnTables = 64;
+constexpr int kMaxImages = 32;
 
 }  // namespace dcgpu

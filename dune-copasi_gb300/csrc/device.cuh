@@ -4,6 +4,7 @@
 #include <cstdint>
 
 #include "bytecode.hpp"
+#include "lookup.hpp"
 
 namespace dcgpu {
 
@@ -16,12 +17,17 @@ struct DevProgram {
   int ncode = 0, ninputs = 0, noutputs = 0, nregs = 0;
 };
 
-// 1-D interpolation tables of the parser context
+// Lookup tables of the parser context: 1-D interpolation tables, tabulated functions and
+// grayscale images
 struct DevTables {
   const double* x = nullptr;
   const double* y = nullptr;
   const int* off = nullptr;
   const int* len = nullptr;
+  const FnTableDesc* ft = nullptr;   // tabulated functions, values in ftg
+  const double* ftg = nullptr;
+  const ImageDesc* im = nullptr;     // images, pixels in imp
+  const double* imp = nullptr;
 };
 
 // Volume term kinds (residual and Jacobian of local_operator.hh:417-707).

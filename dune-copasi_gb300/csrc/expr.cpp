@@ -184,17 +184,27 @@ std::optional<double> literal_value(const std::string& text) {
 // ------------------------------------------------------------------ parser context
 
 ParserContext::ParserContext(const Ini& cfg) {
+  std::vector<std::pair<std::string, Ini>> tabulate;  // `interpolate = true` functions
   for (const auto& name : cfg.sub_keys()) {
     Ini sub = cfg.sub(name);
     std::string type = sub.get("type", "");
     if (type == "constant") {
       constants[name] = sub.get_double("value", 0.0);
+    } else if (type == "tiff") {
+      if (static_cast<int>(image_data.size()) >= kMaxImages) throw ConfigError("too many tiff images");
+      images[name] = static_cast<int>(image_data.size());
+      image_data.push_back(read_tiff_gray(sub.at("path")));
+    } else if (type == "random_field") {
+      // context.cc:93-160 needs the optional parafields library; a reference build without
+      // it rejects the type with this message
+      throw ConfigError("Library was compiled without random fields support");
+    } else if (type == "cell_data") {
+      throw ConfigError("cell data is not implemented");  // context.cc:161-162
     } else if (type == "function") {
-      // context.cc:237-280 can replace a 1-argument function by a table lookup; that
-      // variant is not provided here, and silently evaluating the exact function instead
-      // would change the results by the table's resolution
-      if (sub.get_bool("interpolate", false))
-        throw ConfigError("parser_context." + name + ".interpolate = true is not supported");
+      if (sub.get_bool("interpolate", false)) {
+        tabulate.emplace_back(name, sub);
+        continue;
+      }
       std::string e = sub.at("expression");
       auto colon = e.find(':');
       if (colon == std::string::npos)
@@ -222,8 +232,104 @@ ParserContext::ParserContext(const Ini& cfg) {
       tables[name] = static_cast<int>(interp.size());
       interp.push_back(t);
     } else {
-      throw ConfigError("unsupported parser_context type '" + type + "' for '" + name + "'");
+      throw ConfigError("Unknown type " + type);
     }
+  }
+
+  // context.cc:237-280: a 1-argument function evaluated on intervals + 1 points of its
+  // domain and replaced by a lookup into those values.  The bodies see the constants,
+  // interpolation tables and images, not other expression functions (tables made here are
+  // registered only after all of them are built).
+  std::vector<std::pair<std::string, FnTable>> made;
+  for (const auto& [name, sub] : tabulate) {
+    std::string e = sub.at("expression");
+    auto colon = e.find(':');
+    if (colon == std::string::npos) throw ConfigError("Function arguments must precede a colon ':'");
+    std::vector<std::string> args;
+    std::stringstream ss(e.substr(0, colon));
+    for (std::string a; std::getline(ss, a, ',');)
+      if (!trim(a).empty()) args.push_back(trim(a));
+    if (args.size() != 1)
+      throw ConfigError("Cannot interpolate '" + name + "' function with " + std::to_string(args.size()) +
+                        " arguments");
+    const long intervals = sub.get_long("interpolation.intervals", 1000);
+    if (intervals > 100000) throw ConfigError("Number of interpolation intervals is too big!");
+    if (intervals < 1) throw ConfigError("At least one interval is required in function " + name);
+    const auto dom = sub.get_doubles("interpolation.domain." + args[0], {0.0, 1.0});
+    if (dom.size() != 2) throw ConfigError("interpolation.domain." + args[0] + " needs two values");
+    if (dom[0] >= dom[1]) {
+      std::ostringstream m;
+      m << "Domain arguments (" << dom[0] << ", " << dom[1] << ") of function " << name << " are not ordered";
+      throw ConfigError(m.str());
+    }
+    const std::string ooo = sub.get("interpolation.out_of_bounds", "error");
+    if (ooo != "clamp" && ooo != "error")
+      throw ConfigError("Not known '" + name + ".interpolation.out_of_bounds = " + ooo + "'");
+    ProgramBuilder pb(*this);
+    std::map<std::string, int> bound{{args[0], pb.input(0)}};
+    pb.add_output(pb.compile_function_body(parse_expression(e.substr(colon + 1)), bound));
+    const Program p = pb.finish();
+    FnTable t;
+    t.desc.d0 = dom[0];
+    t.desc.d1 = dom[1];
+    t.desc.intervals = static_cast<uint32_t>(intervals);
+    t.desc.clamp = ooo == "clamp" ? 1 : 0;
+    const double nf = static_cast<double>(intervals);
+    const double width = (dom[1] - dom[0]) / nf;
+    t.desc.ctn = nf / (dom[1] - dom[0]);
+    t.g.resize(static_cast<size_t>(intervals) + 1);
+    for (size_t i = 0; i < t.g.size(); ++i) {
+      const double x = dom[0] + static_cast<double>(i) * width;
+      t.g[i] = run_program_host(p, *this, &x);
+    }
+    made.emplace_back(name, std::move(t));
+  }
+  for (auto& [name, t] : made) {
+    if (static_cast<int>(fn_table_data.size()) >= kMaxFnTables) throw ConfigError("too many tabulated functions");
+    fn_tables[name] = static_cast<int>(fn_table_data.size());
+    fn_table_data.push_back(std::move(t));
+  }
+}
+
+double run_program_host(const Program& p, const ParserContext& ctx, const double* inputs, int output) {
+  std::vector<double> R(std::max(p.nregs, 1), 0.0);
+  for (size_t i = 0; i < p.inputs.size(); ++i) R[i] = inputs[i];
+  for (const Instr& ins : p.code) {
+    if (ins.op == OP_CONST) {
+      R[ins.dst] = p.consts[ins.a | (ins.b << 8)];
+    } else if (ins.op == OP_INTERP || ins.op == OP_FTAB || ins.op == OP_TIFF) {
+      R[ins.dst] = eval_lookup(ctx, ins.op, ins.b, R[ins.a], R[ins.c]);
+    } else {
+      R[ins.dst] = eval_op(ins.op, R[ins.a], R[ins.b], R[ins.c], static_cast<int8_t>(ins.c), nullptr);
+    }
+  }
+  return R[p.outputs.at(output)];
+}
+
+double eval_lookup(const ParserContext& ctx, uint8_t op, int index, double a, double c) {
+  switch (op) {
+    case OP_INTERP: {
+      const InterpTable& t = ctx.interp.at(index);
+      return interp_lookup(t.x.data(), t.y.data(), static_cast<int>(t.x.size()), a);
+    }
+    case OP_FTAB: {
+      const FnTable& t = ctx.fn_table_data.at(index);
+      FnTableDesc d = t.desc;
+      d.off = 0;
+      return ftab_lookup(d, t.g.data(), a);
+    }
+    case OP_TIFF: {
+      const TiffGray& im = ctx.image_data.at(index);
+      ImageDesc d;
+      d.rows = im.rows;
+      d.cols = im.cols;
+      d.x_res = im.x_res;
+      d.y_res = im.y_res;
+      d.x_off = im.x_off;
+      d.y_off = im.y_off;
+      return image_lookup(d, im.px.data(), a, c);
+    }
+    default: return std::nan("");
   }
 }
 
@@ -287,16 +393,9 @@ double eval_op(uint8_t op, double a, double b, double c, int8_t imm, const Inter
       while (n) { if (n & 1) r *= x; x *= x; n >>= 1; }
       return imm < 0 ? 1.0 / r : r;
     }
-    case OP_INTERP: {
-      const auto& X = table->x;
-      const auto& Y = table->y;
-      if (a <= X.front()) return Y.front();
-      if (a > X.back()) return Y.back();
-      size_t k = 1;
-      while (k < X.size() && X[k] < a) ++k;
-      double s = (a - X[k - 1]) / (X[k] - X[k - 1]);
-      return Y[k - 1] + s * (Y[k] - Y[k - 1]);
-    }
+    case OP_INTERP:
+      if (!table) return std::nan("");
+      return interp_lookup(table->x.data(), table->y.data(), static_cast<int>(table->x.size()), a);
     default: return std::nan("");
   }
 }
@@ -389,6 +488,11 @@ int ProgramBuilder::compile(const AstPtr& ast, const Resolver& resolve) {
   return compile_rec(ast, resolve, nullptr);
 }
 
+int ProgramBuilder::compile_function_body(const AstPtr& body, const std::map<std::string, int>& args) {
+  Resolver none = [](const std::string&) -> std::optional<Symbol> { return std::nullopt; };
+  return compile_rec(body, none, &args);
+}
+
 int ProgramBuilder::compile_rec(const AstPtr& ast, const Resolver& resolve,
                                 const std::map<std::string, int>* args) {
   switch (ast->kind) {
@@ -446,6 +550,27 @@ int ProgramBuilder::compile_rec(const AstPtr& ast, const Resolver& resolve,
         double v;
         if (is_constant(a[0], &v)) return constant(eval_op(OP_INTERP, v, 0, 0, 0, &ctx_.interp[tb->second]));
         Node n; n.op = OP_INTERP; n.a = a[0]; n.imm = static_cast<int8_t>(tb->second);
+        return intern(n);
+      }
+      // functions tabulated with `interpolate = true`: expression functions, so a body may
+      // not call them either
+      auto ft = ctx_.fn_tables.find(f);
+      if (ft != ctx_.fn_tables.end()) {
+        if (args) throw ConfigError("user function '" + f + "' may not call other user functions");
+        if (a.size() != 1) throw ConfigError("function '" + f + "' takes 1 arguments");
+        double v;
+        if (is_constant(a[0], &v)) return constant(eval_lookup(ctx_, OP_FTAB, ft->second, v, 0.0));
+        Node n; n.op = OP_FTAB; n.a = a[0]; n.imm = static_cast<int8_t>(ft->second);
+        return intern(n);
+      }
+      // grayscale images: f(x, y)
+      auto im = ctx_.images.find(f);
+      if (im != ctx_.images.end()) {
+        if (a.size() != 2) throw ConfigError("tiff function '" + f + "' takes two arguments");
+        double vx, vy;
+        if (is_constant(a[0], &vx) && is_constant(a[1], &vy))
+          return constant(eval_lookup(ctx_, OP_TIFF, im->second, vx, vy));
+        Node n; n.op = OP_TIFF; n.a = a[0]; n.c = a[1]; n.imm = static_cast<int8_t>(im->second);
         return intern(n);
       }
       static const std::map<std::string, uint8_t> un = {
@@ -584,7 +709,7 @@ Program ProgramBuilder::finish() const {
       ins.b = nd.b >= 0 ? static_cast<uint8_t>(reg[nd.b]) : 0;
       ins.c = nd.c >= 0 ? static_cast<uint8_t>(reg[nd.c]) : 0;
       if (nd.op == OP_POWI) ins.c = static_cast<uint8_t>(nd.imm);
-      if (nd.op == OP_INTERP) ins.b = static_cast<uint8_t>(nd.imm);
+      if (nd.op == OP_INTERP || nd.op == OP_FTAB || nd.op == OP_TIFF) ins.b = static_cast<uint8_t>(nd.imm);
     }
     p.code.push_back(ins);
   }

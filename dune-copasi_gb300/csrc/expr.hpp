@@ -5,8 +5,9 @@
 // documented in doc/docusaurus/docs/math_expr.mdx: muParser precedence (? : < || < && <
 // comparisons < + - and prefix sign < * / % < ^ right-associative), 1/0 booleans,
 // muParser and ExprTk built-in functions, parser_context constants, user functions of up
-// to four arguments (src/dune/copasi/parser/context.cc:289-330) and 1-D interpolation
-// tables (context.cc:68-92).
+// to four arguments (src/dune/copasi/parser/context.cc:289-330), 1-D interpolation
+// tables (context.cc:68-92), functions tabulated with `interpolate = true`
+// (context.cc:237-280) and grayscale TIFF images (context.cc:62-67).
 #pragma once
 
 #include <functional>
@@ -19,6 +20,8 @@
 
 #include "bytecode.hpp"
 #include "ini.hpp"
+#include "lookup.hpp"
+#include "tiff.hpp"
 
 namespace dcgpu {
 
@@ -46,6 +49,12 @@ struct InterpTable {
   std::vector<double> x, y;
 };
 
+// a 1-argument function replaced by its values on a uniform grid (`interpolate = true`)
+struct FnTable {
+  FnTableDesc desc;           // desc.off = 0 here; set when the tables are packed
+  std::vector<double> g;      // intervals + 1 values
+};
+
 class ParserContext {
  public:
   ParserContext() = default;
@@ -54,7 +63,14 @@ class ParserContext {
   std::map<std::string, UserFunction> functions;
   std::map<std::string, int> tables;  // name -> index into interp
   std::vector<InterpTable> interp;
+  std::map<std::string, int> fn_tables;  // name -> index into fn_table_data
+  std::vector<FnTable> fn_table_data;
+  std::map<std::string, int> images;     // name -> index into image_data (`tiff` entries)
+  std::vector<TiffGray> image_data;
 };
+
+// host value of a table op (OP_INTERP, OP_FTAB, OP_TIFF) with table `index`
+double eval_lookup(const ParserContext& ctx, uint8_t op, int index, double a, double c);
 
 // Value of a symbol: either a program input or a constant.
 struct Symbol {
@@ -79,6 +95,9 @@ class ProgramBuilder {
   // compile an expression; returns a node id
   int compile(const AstPtr& ast, const Resolver& resolve);
   int compile_text(const std::string& text, const Resolver& resolve);
+  // a parser-context function body: only its arguments (bound to nodes) and the
+  // context-independent symbols (constants, interpolation tables, images) are visible
+  int compile_function_body(const AstPtr& body, const std::map<std::string, int>& args);
   int constant(double v);
   int input(uint16_t id);
   int binary(uint8_t op, int a, int b);
@@ -107,7 +126,13 @@ class ProgramBuilder {
   std::vector<int> outputs_;
 };
 
-// host evaluation of one op (constant folding and host-side checks)
+// host evaluation of one op (constant folding and host-side checks); table ops go through
+// eval_lookup
 double eval_op(uint8_t op, double a, double b, double c, int8_t imm, const InterpTable* table);
+
+// host evaluation of a compiled program (setup-time expressions: compartments, initial
+// conditions, tabulated functions); inputs are given in the program's input order
+double run_program_host(const Program& p, const ParserContext& ctx, const double* inputs,
+                        int output = 0);
 
 }  // namespace dcgpu

@@ -8,18 +8,7 @@
 namespace dcgpu {
 
 __device__ __forceinline__ double interp_table(const DevTables& T, int tab, double x) {
-  const double* X = T.x + T.off[tab];
-  const double* Y = T.y + T.off[tab];
-  const int n = T.len[tab];
-  if (x <= X[0]) return Y[0];
-  if (x > X[n - 1]) return Y[n - 1];
-  int lo = 0, hi = n - 1;  // X[lo] < x <= X[hi]
-  while (hi - lo > 1) {
-    int mid = (lo + hi) >> 1;
-    if (X[mid] < x) lo = mid; else hi = mid;
-  }
-  double s = (x - X[lo]) / (X[hi] - X[lo]);
-  return Y[lo] + s * (Y[hi] - Y[lo]);
+  return interp_lookup(T.x + T.off[tab], T.y + T.off[tab], T.len[tab], x);
 }
 
 __device__ __forceinline__ double apply_op(const Instr ins, double a, double b, double c,
@@ -87,6 +76,8 @@ __device__ __forceinline__ double apply_op(const Instr ins, double a, double b, 
       return e < 0 ? 1.0 / r : r;
     }
     case OP_INTERP: return interp_table(T, ins.b, a);
+    case OP_FTAB: return ftab_lookup(T.ft[ins.b], T.ftg, a);
+    case OP_TIFF: return image_lookup(T.im[ins.b], T.imp, a, c);
     default: return __longlong_as_double(0x7ff8000000000000ULL);
   }
 }
@@ -101,8 +92,9 @@ __device__ __forceinline__ void run_program(const DevProgram& P, const DevTables
       v = P.consts[ins.a | (ins.b << 8)];
     } else {
       const double a = R[ins.a];
-      const double b = (ins.op == OP_POWI || ins.op == OP_INTERP) ? 0.0 : R[ins.b];
-      const double c = (ins.op == OP_SEL) ? R[ins.c] : 0.0;
+      const bool table = ins.op == OP_INTERP || ins.op == OP_FTAB || ins.op == OP_TIFF;
+      const double b = (ins.op == OP_POWI || table) ? 0.0 : R[ins.b];
+      const double c = (ins.op == OP_SEL || ins.op == OP_TIFF) ? R[ins.c] : 0.0;
       v = apply_op(ins, a, b, c, T);
     }
     R[ins.dst] = v;

@@ -61,12 +61,61 @@ __device__ __forceinline__ bool grid_sum(double (&acc)[NSUM], ReduceScratch rs) 
   return threadIdx.x == 0;
 }
 
+// The same from the threads' partial sums in the vector precision A: a thread accumulates
+// its few elements in A (GB300's FP64 rate is 1/58 of its FP32 rate; a per-element FP64
+// product and conversion made the fp32 solve's dot products FP64-bound), the sums across
+// threads and blocks are FP64.  The totals are left in tot (thread 0 of the last block).
+template <int NSUM, class A>
+__device__ __forceinline__ bool grid_sum(const A (&part)[NSUM], double (&tot)[NSUM], ReduceScratch rs) {
+  __shared__ double sh[NSUM][kWarps];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // warp sums in A, one conversion per warp
+#pragma unroll
+  for (int k = 0; k < NSUM; ++k) {
+    A v = part[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) sh[k][warp] = static_cast<double>(v);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NSUM; ++k) {
+      double v = 0.0;
+      for (int w = 0; w < kWarps; ++w) v += sh[k][w];
+      rs.partial[blockIdx.x * 4 + k] = v;
+    }
+    __threadfence();
+    const unsigned prev = atomicAdd(rs.counter, 1u);
+    last = (prev == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  // the last block: warp 0 adds the block partials in index order
+  if (warp == 0) {
+#pragma unroll
+    for (int k = 0; k < NSUM; ++k) tot[k] = 0.0;
+    for (int b = lane; b < static_cast<int>(gridDim.x); b += 32)
+#pragma unroll
+      for (int k = 0; k < NSUM; ++k) tot[k] += __ldcg(&rs.partial[b * 4 + k]);
+#pragma unroll
+    for (int k = 0; k < NSUM; ++k)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) tot[k] += __shfl_down_sync(0xffffffffu, tot[k], o);
+  }
+  if (threadIdx.x == 0) *rs.counter = 0u;
+  return threadIdx.x == 0;
+}
+
 __device__ __forceinline__ bool done(const double* sc) { return sc[KS_DONE] != 0.0; }
 
 template <class T>
 __global__ void __launch_bounds__(kThreads) k_init(T* x, T* r, T* rhat, T* p, T* v, int64_t n, double rel,
                                                    ReduceScratch rs, double* sc) {
-  double acc[1] = {0.0};
+  T part[1] = {T(0)};
+  double acc[1];
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
   for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
     const T ri = r[i];
@@ -74,9 +123,9 @@ __global__ void __launch_bounds__(kThreads) k_init(T* x, T* r, T* rhat, T* p, T*
     p[i] = T(0);
     v[i] = T(0);
     x[i] = T(0);
-    acc[0] += static_cast<double>(ri) * static_cast<double>(ri);
+    part[0] += ri * ri;
   }
-  if (grid_sum<1>(acc, rs)) {
+  if (grid_sum<1>(part, acc, rs)) {
     const double rr = acc[0];
     sc[KS_RR] = rr;
     sc[KS_RR0] = rr;
@@ -144,16 +193,17 @@ __global__ void __launch_bounds__(kThreads) k_spmv_rv(int nrows, const int32_t* 
                                                       const T* __restrict__ phat, T* __restrict__ v,
                                                       const T* __restrict__ rhat, ReduceScratch rs, double* sc) {
   if (done(sc)) return;
-  double acc[1] = {0.0};
+  T part[1] = {T(0)};
+  double acc[1];
   const int64_t n = static_cast<int64_t>(nrows) * B;
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
   for (int64_t row = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; row < n; row += stride) {
     const V y = row_product<B, T, V>(static_cast<int>(row / B), static_cast<int>(row % B), rowptr, colidx, val, phat);
     const T yt = static_cast<T>(y);
     v[row] = yt;
-    acc[0] += static_cast<double>(rhat[row]) * static_cast<double>(yt);
+    part[0] += rhat[row] * yt;
   }
-  if (grid_sum<1>(acc, rs)) {
+  if (grid_sum<1>(part, acc, rs)) {
     const double rv = acc[0];
     sc[KS_RV] = rv;
     const double a = sc[KS_RHO] / rv;
@@ -169,7 +219,8 @@ __global__ void __launch_bounds__(kThreads) k_sell_rv(Sell S, const V* __restric
                                                       T* __restrict__ v, const T* __restrict__ rhat,
                                                       ReduceScratch rs, double* sc) {
   if (done(sc)) return;
-  double acc[1] = {0.0};
+  T part[1] = {T(0)};
+  double acc[1];
   const int lane = threadIdx.x & 31;
   const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
   for (int64_t sl = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; sl < S.nslices; sl += nw) {
@@ -181,11 +232,11 @@ __global__ void __launch_bounds__(kThreads) k_sell_rv(Sell S, const V* __restric
       for (int i = 0; i < B; ++i) {
         const T yt = static_cast<T>(y[i]);
         v[br * B + i] = yt;
-        acc[0] += static_cast<double>(rhat[br * B + i]) * static_cast<double>(yt);
+        part[0] += rhat[br * B + i] * yt;
       }
     }
   }
-  if (grid_sum<1>(acc, rs)) {
+  if (grid_sum<1>(part, acc, rs)) {
     const double rv = acc[0];
     sc[KS_RV] = rv;
     const double a = sc[KS_RHO] / rv;
@@ -202,7 +253,8 @@ __global__ void __launch_bounds__(kThreads) k_update_s(int nrows, T* __restrict_
                                                        T* __restrict__ shat, ReduceScratch rs, double* sc) {
   if (done(sc)) return;
   const V alpha = static_cast<V>(sc[KS_ALPHA]);
-  double acc[1] = {0.0};
+  T part[1] = {T(0)};
+  double acc[1];
   const int stride = gridDim.x * blockDim.x;
   for (int nd = blockIdx.x * blockDim.x + threadIdx.x; nd < nrows; nd += stride) {
     const int64_t o = static_cast<int64_t>(nd) * B;
@@ -212,7 +264,7 @@ __global__ void __launch_bounds__(kThreads) k_update_s(int nrows, T* __restrict_
       sv[i] = static_cast<V>(r[o + i]) - alpha * static_cast<V>(v[o + i]);
       const T st = static_cast<T>(sv[i]);
       s[o + i] = st;
-      acc[0] += static_cast<double>(st) * static_cast<double>(st);
+      part[0] += st * st;
     }
     if (!BJ) continue;
     const V* d = dinv + static_cast<int64_t>(nd) * B * B;
@@ -224,7 +276,7 @@ __global__ void __launch_bounds__(kThreads) k_update_s(int nrows, T* __restrict_
       shat[o + i] = static_cast<T>(a2);
     }
   }
-  if (grid_sum<1>(acc, rs)) sc[KS_SS] = acc[0];
+  if (grid_sum<1>(part, acc, rs)) sc[KS_SS] = acc[0];
 }
 
 // (4) t = A shat;  <t, s>, <t, t>;  omega = <t,s>/<t,t>
@@ -235,18 +287,18 @@ __global__ void __launch_bounds__(kThreads) k_spmv_omega(int nrows, const int32_
                                                          T* __restrict__ t, const T* __restrict__ s,
                                                          ReduceScratch rs, double* sc) {
   if (done(sc)) return;
-  double acc[2] = {0.0, 0.0};
+  T part[2] = {T(0), T(0)};
+  double acc[2];
   const int64_t n = static_cast<int64_t>(nrows) * B;
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
   for (int64_t row = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; row < n; row += stride) {
     const V y = row_product<B, T, V>(static_cast<int>(row / B), static_cast<int>(row % B), rowptr, colidx, val, shat);
     const T yt = static_cast<T>(y);
     t[row] = yt;
-    const double td = static_cast<double>(yt);
-    acc[0] += td * static_cast<double>(s[row]);
-    acc[1] += td * td;
+    part[0] += yt * s[row];
+    part[1] += yt * yt;
   }
-  if (grid_sum<2>(acc, rs)) {
+  if (grid_sum<2>(part, acc, rs)) {
     sc[KS_TS] = acc[0];
     sc[KS_TT] = acc[1];
     double w = acc[1] != 0.0 ? acc[0] / acc[1] : 0.0;
@@ -264,7 +316,8 @@ __global__ void __launch_bounds__(kThreads) k_sell_omega(Sell S, const V* __rest
                                                          const T* __restrict__ shat, T* __restrict__ t,
                                                          const T* __restrict__ s, ReduceScratch rs, double* sc) {
   if (done(sc)) return;
-  double acc[2] = {0.0, 0.0};
+  T part[2] = {T(0), T(0)};
+  double acc[2];
   const int lane = threadIdx.x & 31;
   const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
   for (int64_t sl = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; sl < S.nslices; sl += nw) {
@@ -276,13 +329,12 @@ __global__ void __launch_bounds__(kThreads) k_sell_omega(Sell S, const V* __rest
       for (int i = 0; i < B; ++i) {
         const T yt = static_cast<T>(y[i]);
         t[br * B + i] = yt;
-        const double td = static_cast<double>(yt);
-        acc[0] += td * static_cast<double>(s[br * B + i]);
-        acc[1] += td * td;
+        part[0] += yt * s[br * B + i];
+        part[1] += yt * yt;
       }
     }
   }
-  if (grid_sum<2>(acc, rs)) {
+  if (grid_sum<2>(part, acc, rs)) {
     sc[KS_TS] = acc[0];
     sc[KS_TT] = acc[1];
     double w = acc[1] != 0.0 ? acc[0] / acc[1] : 0.0;
@@ -303,16 +355,17 @@ __global__ void __launch_bounds__(kThreads) k_update_xr(int64_t n, T* __restrict
   if (done(sc)) return;
   using C = T;
   const C alpha = static_cast<C>(sc[KS_ALPHA]), omega = static_cast<C>(sc[KS_OMEGA]);
-  double acc[2] = {0.0, 0.0};
+  T part[2] = {T(0), T(0)};
+  double acc[2];
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
   for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
     x[i] = x[i] + alpha * phat[i] + omega * shat[i];
     const T ri = s[i] - omega * t[i];
     r[i] = ri;
-    acc[0] += static_cast<double>(ri) * static_cast<double>(ri);
-    acc[1] += static_cast<double>(rhat[i]) * static_cast<double>(ri);
+    part[0] += ri * ri;
+    part[1] += rhat[i] * ri;
   }
-  if (grid_sum<2>(acc, rs)) {
+  if (grid_sum<2>(part, acc, rs)) {
     const double rr = acc[0], rho_new = acc[1];
     sc[KS_RR] = rr;
     sc[KS_RHONEW] = rho_new;
@@ -350,7 +403,8 @@ template <int B, class T, class V, bool BJ>
 __global__ void __launch_bounds__(kThreads) k_cg_init(int nrows, T* x, const T* r, T* p, T* z,
                                                       const V* __restrict__ dinv, double rel, ReduceScratch rs,
                                                       double* sc) {
-  double acc[2] = {0.0, 0.0};
+  T part[2] = {T(0), T(0)};
+  double acc[2];
   const int stride = gridDim.x * blockDim.x;
   for (int nd = blockIdx.x * blockDim.x + threadIdx.x; nd < nrows; nd += stride) {
     const int64_t o = static_cast<int64_t>(nd) * B;
@@ -360,7 +414,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_init(int nrows, T* x, const T* 
       x[o + i] = T(0);
       p[o + i] = T(0);
       rv[i] = static_cast<V>(r[o + i]);
-      acc[0] += static_cast<double>(r[o + i]) * static_cast<double>(r[o + i]);
+      part[0] += r[o + i] * r[o + i];
     }
     if (!BJ) continue;
     const V* d = dinv + static_cast<int64_t>(nd) * B * B;
@@ -371,10 +425,10 @@ __global__ void __launch_bounds__(kThreads) k_cg_init(int nrows, T* x, const T* 
       for (int j = 0; j < B; ++j) a += d[i * B + j] * rv[j];
       const T zt = static_cast<T>(a);
       z[o + i] = zt;
-      acc[1] += static_cast<double>(r[o + i]) * static_cast<double>(zt);
+      part[1] += r[o + i] * zt;
     }
   }
-  if (grid_sum<2>(acc, rs)) {
+  if (grid_sum<2>(part, acc, rs)) {
     const double rr = acc[0];
     sc[KS_RR] = rr;
     sc[KS_RR0] = rr;
@@ -406,7 +460,8 @@ __global__ void __launch_bounds__(kThreads) k_cg_update(int nrows, T* __restrict
                                                         ReduceScratch rs, double* sc) {
   if (done(sc)) return;
   const T alpha = static_cast<T>(sc[KS_ALPHA]);
-  double acc[2] = {0.0, 0.0};
+  T part[2] = {T(0), T(0)};
+  double acc[2];
   const int stride = gridDim.x * blockDim.x;
   for (int nd = blockIdx.x * blockDim.x + threadIdx.x; nd < nrows; nd += stride) {
     const int64_t o = static_cast<int64_t>(nd) * B;
@@ -417,7 +472,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_update(int nrows, T* __restrict
       const T ri = r[o + i] - alpha * q[o + i];
       r[o + i] = ri;
       rv[i] = static_cast<V>(ri);
-      acc[0] += static_cast<double>(ri) * static_cast<double>(ri);
+      part[0] += ri * ri;
     }
     if (!BJ) continue;
     const V* d = dinv + static_cast<int64_t>(nd) * B * B;
@@ -428,10 +483,10 @@ __global__ void __launch_bounds__(kThreads) k_cg_update(int nrows, T* __restrict
       for (int j = 0; j < B; ++j) a += d[i * B + j] * rv[j];
       const T zt = static_cast<T>(a);
       z[o + i] = zt;
-      acc[1] += static_cast<double>(rv[i]) * static_cast<double>(zt);
+      part[1] += rv[i] * zt;
     }
   }
-  if (grid_sum<2>(acc, rs)) {
+  if (grid_sum<2>(part, acc, rs)) {
     const double rr = acc[0];
     sc[KS_RR] = rr;
     sc[KS_ITER] += 1.0;
@@ -460,11 +515,12 @@ template <class T>
 __global__ void __launch_bounds__(kThreads) k_cg_rz(int64_t n, const T* __restrict__ r, const T* __restrict__ z,
                                                     ReduceScratch rs, double* sc) {
   if (done(sc)) return;
-  double acc[1] = {0.0};
+  T part[1] = {T(0)};
+  double acc[1];
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
   for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride)
-    acc[0] += static_cast<double>(r[i]) * static_cast<double>(z[i]);
-  if (grid_sum<1>(acc, rs)) {
+    part[0] += r[i] * z[i];
+  if (grid_sum<1>(part, acc, rs)) {
     const double rz = acc[0];
     const bool first = sc[KS_ITER] == 0.0;
     const double beta = first ? 0.0 : rz / sc[KS_RHO];

@@ -22,10 +22,52 @@ namespace dcgpu {
 enum KrylovSlot : int {
   KS_RHO = 0, KS_ALPHA = 1, KS_OMEGA = 2, KS_RHONEW = 3, KS_RV = 4, KS_TS = 5, KS_TT = 6,
   KS_RR = 7, KS_SS = 8, KS_BETA = 9, KS_TARGET = 10, KS_DONE = 11, KS_ITER = 12, KS_RR0 = 13,
+  KS_FAULT = 14,    // single-launch solve: 1 when a grid-barrier wait gave up
+  KS_BARRIER = 15,  // single-launch solve: the barrier's arrival counter and generation (2 x u32)
   KS_COUNT = 16
 };
 // KS_DONE values
 constexpr double kDoneConverged = 1.0, kDoneBreakdown = 2.0, kDoneNonFinite = 3.0;
+
+// ---------------------------------------------------------------- single-launch BiCGSTAB
+// The whole preconditioned BiCGSTAB solve in ONE cooperative launch: the phases of an
+// iteration are separated by grid-wide barriers instead of kernel boundaries, every block
+// folds the per-block partial sums itself (same values, same order, so every block takes
+// the same convergence decision), and the loop runs on the device until convergence,
+// breakdown or max_it.  Same arithmetic per element as the five-kernel iteration below.
+// On the SELL-32 operator with block size <= 4 an iteration has three phases: each SpMV
+// forms the preconditioned vector it multiplies (D^-1 (r + beta (p - omega v)), then
+// D^-1 (r - alpha v)) for every column it gathers, instead of reading it from a vector
+// written in a phase of its own; the BSR operator keeps five phases.
+// Each barrier wait is bounded in time; a wait that gives up sets sc[KS_FAULT] and the
+// kernel returns.  Block Jacobi only (no multigrid cycle inside the kernel).
+template <class T, class V>
+struct FusedBicgArgs {
+  int nrows = 0;
+  const int32_t* rowptr = nullptr;  // BSR operator (used when sell is false)
+  const int32_t* colidx = nullptr;
+  Sell S{};                         // SELL-32 operator (used when sell is true)
+  const V* vals = nullptr;          // operator values in the chosen layout
+  const V* dinv = nullptr;          // block-Jacobi inverses
+  T *x, *r, *rhat, *p, *v, *s, *t, *phat, *shat;
+  T *p2, *v2;                       // second p and v buffers (the SELL variant alternates them)
+  double* partial = nullptr;        // 5 * gridDim.x doubles
+  double* sc = nullptr;             // device scalars (KrylovSlot)
+  double rel = 0.0;
+  int max_it = 0;
+};
+// Launch plan of the single-launch solve for block size bs: false when the device cannot
+// run it (no cooperative launch, unsupported block size).  blocks is bounded by what is
+// co-resident on the device and by the problem size; `slots` is the share of the device
+// the grid holds, in units of which the device has `capacity` (co-resident blocks at the
+// kernels' minimum occupancy), so that grids in flight together can be kept within it.
+template <class T, class V>
+bool fused_bicgstab_plan(int bs, bool sell, int nrows, int* blocks, int* slots, int* capacity);
+// partial-sum doubles the solve needs for `blocks` blocks
+inline int64_t fused_bicgstab_partials(int blocks) { return 5 * static_cast<int64_t>(blocks); }
+// resets the barrier words and the fault flag, then launches the solve on `s`
+template <class T, class V>
+void fused_bicgstab(int bs, bool sell, int blocks, const FusedBicgArgs<T, V>& a, cudaStream_t s);
 
 template <class T>
 struct KrylovVectors {

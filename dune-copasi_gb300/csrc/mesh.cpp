@@ -204,18 +204,4 @@ Faces compute_faces(const Mesh& m) {
   return f;
 }
 
-double run_program_host(const Program& p, const ParserContext& ctx, const double* inputs, int output) {
-  std::vector<double> R(std::max(p.nregs, 1), 0.0);
-  for (size_t i = 0; i < p.inputs.size(); ++i) R[i] = inputs[i];
-  for (const Instr& ins : p.code) {
-    if (ins.op == OP_CONST) {
-      R[ins.dst] = p.consts[ins.a | (ins.b << 8)];
-      continue;
-    }
-    const InterpTable* tb = (ins.op == OP_INTERP) ? &ctx.interp[ins.b] : nullptr;
-    R[ins.dst] = eval_op(ins.op, R[ins.a], R[ins.b], R[ins.c], static_cast<int8_t>(ins.c), tb);
-  }
-  return R[p.outputs.at(output)];
-}
-
 }  // namespace dcgpu

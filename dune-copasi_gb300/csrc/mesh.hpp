@@ -45,9 +45,4 @@ struct Faces {
 };
 Faces compute_faces(const Mesh& m);
 
-// host evaluation of a compiled program (setup-time expressions: compartments, initial
-// conditions); inputs are given in the program's input order
-double run_program_host(const Program& p, const ParserContext& ctx, const double* inputs,
-                        int output = 0);
-
 }  // namespace dcgpu

@@ -514,6 +514,37 @@ void Model::upload_geometry() {
   tables.y = d_tab_y.get();
   tables.off = d_tab_off.get();
   tables.len = d_tab_len.get();
+  // tabulated functions and images: descriptors + one packed value array each
+  std::vector<FnTableDesc> fd;
+  std::vector<double> fg;
+  for (const auto& t : ctx.fn_table_data) {
+    FnTableDesc d = t.desc;
+    d.off = static_cast<int64_t>(fg.size());
+    fd.push_back(d);
+    fg.insert(fg.end(), t.g.begin(), t.g.end());
+  }
+  std::vector<ImageDesc> id;
+  std::vector<double> ip;
+  for (const auto& im : ctx.image_data) {
+    ImageDesc d;
+    d.off = static_cast<int64_t>(ip.size());
+    d.rows = im.rows;
+    d.cols = im.cols;
+    d.x_res = im.x_res;
+    d.y_res = im.y_res;
+    d.x_off = im.x_off;
+    d.y_off = im.y_off;
+    id.push_back(d);
+    ip.insert(ip.end(), im.px.begin(), im.px.end());
+  }
+  d_ftab_desc.upload(fd);
+  d_ftab_val.upload(fg);
+  d_img_desc.upload(id);
+  d_img_px.upload(ip);
+  tables.ft = d_ftab_desc.get();
+  tables.ftg = d_ftab_val.get();
+  tables.im = d_img_desc.get();
+  tables.imp = d_img_px.get();
 }
 
 // greedy colouring: elements (or faces) sharing a vertex get different colours

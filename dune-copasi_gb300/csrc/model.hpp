@@ -172,6 +172,10 @@ class Model {
   std::vector<DeviceBuffer<int32_t>> d_comp_vnode;
   DeviceBuffer<double> d_tab_x, d_tab_y;
   DeviceBuffer<int> d_tab_off, d_tab_len;
+  DeviceBuffer<FnTableDesc> d_ftab_desc;
+  DeviceBuffer<double> d_ftab_val;
+  DeviceBuffer<ImageDesc> d_img_desc;
+  DeviceBuffer<double> d_img_px;
   DevTables tables{};
 
   std::vector<VolumeGroup> vgroups;

@@ -24,8 +24,10 @@ struct Sell {
 };
 
 #ifdef __CUDACC__
-// y rows of slice `sl` for lane `lane`: acc[i] = sum over the lane's blocks of A(i, :) x
-template <int B, class T, class V>
+// y rows of slice `sl` for lane `lane`: acc[i] = sum over the lane's blocks of A(i, :) x.
+// kCoherent reads x through L2 only (ld.global.cg), for kernels in which other blocks write x
+// between grid-wide barriers; the operator itself is read-only and uses the read-only path.
+template <int B, class T, class V, bool kCoherent = false>
 __device__ __forceinline__ void sell_lane_rows(const Sell& S, int64_t sl, int lane, const V* __restrict__ val,
                                                const T* __restrict__ x, V (&acc)[B]) {
 #pragma unroll
@@ -34,12 +36,40 @@ __device__ __forceinline__ void sell_lane_rows(const Sell& S, int64_t sl, int la
   const int32_t* __restrict__ cols = S.cols + o0 * 32 + lane;
   const V* __restrict__ v = val + o0 * (32 * B * B) + lane;
   const int w = static_cast<int>(o1 - o0);
-#pragma unroll 2
-  for (int k = 0; k < w; ++k) {
+  // slots in batches of U: the U column loads, then the U x gathers, are independent of
+  // one another, so a lane has U (not one) dependent load chains in flight; the slice's
+  // time is then a few L2 round trips instead of two per slot
+  constexpr int U = B <= 2 ? 4 : 2;
+  int k = 0;
+  for (; k + U <= w; k += U) {
+    int c[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) c[u] = __ldg(cols + (k + u) * 32);
+    V xv[U][B];
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int j = 0; j < B; ++j) {
+        const T* xp = x + static_cast<int64_t>(c[u]) * B + j;
+        xv[u][j] = static_cast<V>(kCoherent ? __ldcg(xp) : *xp);
+      }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const V* __restrict__ vk = v + static_cast<int64_t>(k + u) * (32 * B * B);
+#pragma unroll
+      for (int i = 0; i < B; ++i)
+#pragma unroll
+        for (int j = 0; j < B; ++j) acc[i] += __ldg(vk + (i * B + j) * 32) * xv[u][j];
+    }
+  }
+  for (; k < w; ++k) {
     const int c = __ldg(cols + k * 32);
     V xv[B];
 #pragma unroll
-    for (int j = 0; j < B; ++j) xv[j] = static_cast<V>(x[static_cast<int64_t>(c) * B + j]);
+    for (int j = 0; j < B; ++j) {
+      const T* xp = x + static_cast<int64_t>(c) * B + j;
+      xv[j] = static_cast<V>(kCoherent ? __ldcg(xp) : *xp);
+    }
     const V* __restrict__ vk = v + static_cast<int64_t>(k) * (32 * B * B);
 #pragma unroll
     for (int i = 0; i < B; ++i)

@@ -4,6 +4,8 @@
 #include <cfloat>
 #include <cmath>
 #include <limits>
+#include <condition_variable>
+#include <mutex>
 #include <type_traits>
 
 #include "assemble.cuh"
@@ -81,6 +83,9 @@ Solver::Solver(Model& m, cudaStream_t s) : model(m), stream(s) {
   kphat_.resize(n_); kshat_.resize(n_); kx_.resize(n_);
   dinv_.resize(static_cast<size_t>(m.nnodes) * m.bs * m.bs);
   partial_.resize(kReduceBlocks * 4);
+  // single-launch BiCGSTAB partial sums: room for two blocks on each of up to 256 SMs, so a
+  // solve allocates nothing
+  fpart_.resize(fused_bicgstab_partials(2 * 256));
   scal_.resize(32);
   counter_.resize(1);
   status_.resize(1);
@@ -175,6 +180,9 @@ Solver::Solver(Model& m, cudaStream_t s) : model(m), stream(s) {
   else if (fmt == "sell") spmv_request_ = kSpmvSell;
   else throw ConfigError("linear_solver.spmv must be auto, bsr or sell, not '" + fmt + "'");
   spmv_format = spmv_request_;
+  // BiCGSTAB with block Jacobi: the whole solve in one cooperative launch (default), or one
+  // launch per phase replayed from a CUDA graph (false)
+  fused_ = ls.get_bool("single_launch", true);
   dec_ = tso.get_double("time_step_decrease_factor", 0.5);
   inc_ = tso.get_double("time_step_increase_factor", 1.1);
   has_min_ = tso.has_key("time_step_min");
@@ -193,6 +201,7 @@ void Solver::enable_mixed(bool on) {
   if (on && fr_.size() != static_cast<size_t>(n_)) {
     fr_.resize(n_); frhat_.resize(n_); fp_.resize(n_); fv_.resize(n_); fs_.resize(n_); ft_.resize(n_);
     fphat_.resize(n_); fshat_.resize(n_); fx_.resize(n_); fb_.resize(n_);
+    fp2_.resize(n_); fv2_.resize(n_);
     fdinv_.resize(static_cast<size_t>(model.nnodes) * model.bs * model.bs);
     if (spmv_request_ != kSpmvSell || use_amg_) J32_.resize(static_cast<size_t>(model.nnzb()) * model.bs * model.bs);
     if (spmv_request_ != kSpmvBsr) Js32_.resize(static_cast<size_t>(model.sell_slots) * 32 * model.bs * model.bs);
@@ -240,6 +249,8 @@ Solver::~Solver() {
   for (auto& g : graphs_)
     if (g) cudaGraphExecDestroy(g);
   for (cudaEvent_t e : graph_events_) cudaEventDestroy(e);
+  for (cudaEvent_t e : fused_ev_)
+    if (e) cudaEventDestroy(e);
 }
 
 void Solver::set_state(const std::vector<double>& ref, double t) {
@@ -527,11 +538,106 @@ int Solver::gmres_t(double rel, int max_it, int* iters) {
   return beta <= target ? DC_OK : DC_ERR_TIMEOUT;
 }
 
+namespace {
+// Device share held by the single-launch solves in flight (all models of the process): a
+// solve reserves its grid's slots before launching and returns them once its result has
+// been read, waiting while they are taken.  Cooperative grids in flight together then
+// always fit on the device at once, so no grid's barrier waits for blocks that cannot be
+// scheduled; and every solve takes the single-launch path whatever else runs, so a
+// simulation's results do not depend on the others.
+class SlotBudget {
+ public:
+  void acquire(int slots, int capacity) {
+    std::unique_lock<std::mutex> lk(m_);
+    cv_.wait(lk, [&] { return used_ + slots <= capacity; });
+    used_ += slots;
+  }
+  void release(int slots) {
+    {
+      std::lock_guard<std::mutex> lk(m_);
+      used_ -= slots;
+    }
+    cv_.notify_all();
+  }
+
+ private:
+  std::mutex m_;
+  std::condition_variable cv_;
+  long long used_ = 0;
+};
+SlotBudget g_slots;
+
+struct SlotGuard {
+  int slots;
+  SlotGuard(int s, int capacity) : slots(s) { g_slots.acquire(s, capacity); }
+  ~SlotGuard() { g_slots.release(slots); }
+};
+}  // namespace
+
+// BiCGSTAB + block Jacobi as one cooperative launch (krylov_fused.cu).  Returns false, with
+// nothing launched, when the device cannot run it; the caller then replays the graph of
+// per-phase launches.
+template <class T>
+bool Solver::krylov_fused(double rel, int max_it, int* iters, int* status) {
+  constexpr bool f32 = std::is_same_v<T, float>;
+  const bool sell = f32 && spmv_format == kSpmvSell;
+  const Bsr A = model.bsr(J_.get(), J32_.get());
+  int blocks = 0, slots = 0, capacity = 0;
+  if (!fused_bicgstab_plan<T, T>(model.bs, sell, A.nrows, &blocks, &slots, &capacity)) return false;
+  SlotGuard guard(slots, capacity);
+  const int64_t np = fused_bicgstab_partials(blocks);
+  if (static_cast<int64_t>(fpart_.size()) < np) fpart_.resize(np);
+  FusedBicgArgs<T, T> a;
+  a.nrows = A.nrows;
+  a.rowptr = A.rowptr;
+  a.colidx = A.colidx;
+  if constexpr (f32) {
+    a.vals = sell ? Js32_.get() : J32_.get();
+    a.dinv = fdinv_.get();
+    a.x = fx_.get(); a.r = fr_.get(); a.rhat = frhat_.get(); a.p = fp_.get(); a.v = fv_.get();
+    a.s = fs_.get(); a.t = ft_.get(); a.phat = fphat_.get(); a.shat = fshat_.get();
+    a.p2 = fp2_.get(); a.v2 = fv2_.get();
+  } else {
+    a.vals = J_.get();
+    a.dinv = dinv_.get();
+    a.x = kx_.get(); a.r = kr_.get(); a.rhat = krhat_.get(); a.p = kp_.get(); a.v = kv_.get();
+    a.s = ks_.get(); a.t = kt_.get(); a.phat = kphat_.get(); a.shat = kshat_.get();
+    a.p2 = nullptr; a.v2 = nullptr;  // the fp64 operator is BSR: five phases, one p and v
+  }
+  if (sell) a.S = model.sell();
+  a.partial = fpart_.get();
+  a.sc = scal_.get();
+  a.rel = rel;
+  a.max_it = max_it;
+  if (profiling_ && !fused_ev_[0])
+    for (auto& e : fused_ev_) cuda_check(cudaEventCreate(&e), "cudaEventCreate");
+  if (profiling_) cuda_check(cudaEventRecord(fused_ev_[0], stream), "cudaEventRecord");
+  fused_bicgstab<T, T>(model.bs, sell, blocks, a, stream);
+  if (profiling_) cuda_check(cudaEventRecord(fused_ev_[1], stream), "cudaEventRecord");
+  double h[KS_COUNT];
+  read_scalars(h, 0, KS_COUNT);
+  if (h[KS_FAULT] != 0.0) throw std::runtime_error("single-launch BiCGSTAB: a grid-barrier wait timed out");
+  *iters = static_cast<int>(h[KS_ITER]);
+  if (profiling_) {
+    float ms = 0.0f;
+    cuda_check(cudaEventElapsedTime(&ms, fused_ev_[0], fused_ev_[1]), "cudaEventElapsedTime");
+    kernel_times.ms[3] += ms;
+    kernel_times.calls[3] += *iters;
+  }
+  *status = h[KS_DONE] == kDoneConverged ? DC_OK : (h[KS_DONE] == 0.0 ? DC_ERR_TIMEOUT : DC_ERR_DIVERGED);
+  return true;
+}
+
 // Replays chunks of Krylov (BiCGSTAB or CG) iterations until the device flag reports
 // convergence, breakdown or a non-finite value, or max_it iterations have run.  r (kr_ /
 // fr_) holds the right-hand side on entry; the solution is left in the Krylov x vector.
 int Solver::krylov_run(bool fp32, double rel, int max_it, int* iters) {
   if (krylov_gmres_) return fp32 ? gmres_t<float>(rel, max_it, iters) : gmres_t<double>(rel, max_it, iters);
+  if (fused_ && !krylov_cg_ && !use_amg_) {
+    int st = DC_OK;
+    if (fp32 ? krylov_fused<float>(rel, max_it, iters, &st) : krylov_fused<double>(rel, max_it, iters, &st))
+      return st;
+  }
   double* sc = scal_.get();
   const int64_t n = n_;
   const Bsr A = model.bsr(J_.get(), J32_.get());

@@ -88,11 +88,12 @@ class Solver {
 
   // per-category device time of the hot launches, measured with CUDA events on the
   // solver's stream: 0 = assembly (all colour launches of one operator evaluation),
-  // 1 = SpMV (fp64 and fp32), 2 = preconditioner apply
-  static constexpr int kTimerCategories = 3;
+  // 1 = SpMV (fp64 and fp32), 2 = preconditioner apply,
+  // 3 = single-launch BiCGSTAB solves, whose `calls` count the Krylov ITERATIONS they ran
+  static constexpr int kTimerCategories = 4;
   struct KernelTimes {
-    double ms[kTimerCategories] = {0, 0, 0};
-    long long calls[kTimerCategories] = {0, 0, 0};
+    double ms[kTimerCategories] = {0, 0, 0, 0};
+    long long calls[kTimerCategories] = {0, 0, 0, 0};
   };
   void enable_profiling(bool on);
   KernelTimes kernel_times;
@@ -139,6 +140,7 @@ class Solver {
   // Krylov workspace
   DeviceBuffer<double> kr_, krhat_, kp_, kv_, ks_, kt_, kphat_, kshat_, kx_, dinv_;
   DeviceBuffer<float> fr_, frhat_, fp_, fv_, fs_, ft_, fphat_, fshat_, fx_, fdinv_, fb_;
+  DeviceBuffer<float> fp2_, fv2_;  // second p / v of the three-phase single-launch solve
   DeviceBuffer<float> J32_;
   DeviceBuffer<float> Js32_;  // fp32 operator in the SELL-32 layout
   DeviceBuffer<double> partial_, scal_;
@@ -163,6 +165,13 @@ class Solver {
   template <class T>
   int gmres_t(double rel, int max_it, int* iters);
   int launches_per_iter_ = 5;     // kernels of one captured Krylov iteration
+  // single-launch BiCGSTAB (cooperative kernel) whenever the device supports it; the
+  // graph-replayed per-phase iteration otherwise, or with linear_solver.single_launch = false
+  bool fused_ = true;
+  DeviceBuffer<double> fpart_;
+  cudaEvent_t fused_ev_[2] = {nullptr, nullptr};
+  template <class T>
+  bool krylov_fused(double rel, int max_it, int* iters, int* status);
   double direct_tol_ = 1e-10;
   int lin_max_it_ = 500;
   std::string precond_ = "Jacobi";

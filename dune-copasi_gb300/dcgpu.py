@@ -433,11 +433,13 @@ class Model:
         _check(self._lib.dc_profile_enable(self._h, 1 if enabled else 0))
 
     def kernel_times(self):
-        """{category: (total ms, launches)} for assembly, spmv, precond."""
-        ms = np.zeros(3)
-        calls = np.zeros(3, np.int64)
-        _check(self._lib.dc_profile_get(self._h, _ptr(ms), _ptr(calls, ctypes.c_int64), 3))
-        return {k: (float(ms[i]), int(calls[i])) for i, k in enumerate(("assembly", "spmv", "precond"))}
+        """{category: (total ms, launches)} for assembly, spmv, precond and krylov_iteration
+        (single-launch BiCGSTAB solves; its count is the Krylov iterations they ran)."""
+        names = ("assembly", "spmv", "precond", "krylov_iteration")
+        ms = np.zeros(len(names))
+        calls = np.zeros(len(names), np.int64)
+        _check(self._lib.dc_profile_get(self._h, _ptr(ms), _ptr(calls, ctypes.c_int64), len(names)))
+        return {k: (float(ms[i]), int(calls[i])) for i, k in enumerate(names)}
 
     def spmv_format(self):
         """Layout of the fp32 Krylov operator and the tuner's SpMV times:

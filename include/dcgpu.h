@@ -149,7 +149,8 @@ int dc_expr_eval(const char* expression, const char* context_ini, const char* co
  * counters of LinearSolver / TimeStep, model/make_step_operator.hh:104-139):
  * the CUDA stream the model launches on (cudaStream_t as void*), the number of kernels
  * this library has launched, and per-category device times measured with CUDA events
- * (0 = assembly, 1 = SpMV, 2 = preconditioner apply) while profiling is enabled. */
+ * (0 = assembly, 1 = SpMV, 2 = preconditioner apply, 3 = single-launch BiCGSTAB solves,
+ * whose call count is the number of Krylov iterations they ran) while profiling is enabled. */
 int dc_stream_handle(const dc_model* model, void** stream);
 int64_t dc_launch_count(void);
 int dc_profile_enable(dc_model* model, int enabled);

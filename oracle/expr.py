@@ -24,6 +24,8 @@ import re
 
 import numpy as np
 
+from .tiff import TiffError, TiffImage
+
 
 class ExprError(ValueError):
     pass
@@ -241,15 +243,73 @@ class UserFunction:
         self.body = body
 
 
+def lerp_exact(a, b, t):
+    """std::lerp, the algorithm of C++ proposal P0811R3: exact when a and b straddle zero,
+    b at t == 1, monotonic and never past b."""
+    a, b, t = np.broadcast_arrays(np.asarray(a, float), np.asarray(b, float), np.asarray(t, float))
+    with np.errstate(invalid="ignore"):
+        straddle = ((a <= 0) & (b >= 0)) | ((a >= 0) & (b <= 0))
+        r1 = t * b + (1.0 - t) * a
+        x = a + t * (b - a)
+        r2 = np.where((t > 1) == (b > a), np.where(b < x, x, b), np.where(b > x, x, b))
+        r2 = np.where(t == 1, b, r2)
+    return np.where(straddle, r1, r2)
+
+
 class Interpolation:
     def __init__(self, domain, rng):
         self.domain = np.asarray(domain, float)
         self.range = np.asarray(rng, float)
 
     def __call__(self, x):
+        """context.cc:77-90: std::lower_bound over the domain; the first range value up to
+        the first domain point (and for NaN), the last one past the end, std::lerp between."""
+        X, Y = self.domain, self.range
         x = np.asarray(x, float)
-        # context.cc:77-90: lower_bound, clamp to first/last value, std::lerp in between
-        return np.interp(x, self.domain, self.range)
+        d = np.clip(np.searchsorted(X, np.where(np.isnan(x), X[0], x), side="left"), 1, len(X) - 1)
+        with np.errstate(invalid="ignore", divide="ignore"):
+            t = (x - X[d - 1]) / (X[d] - X[d - 1])
+        mid = lerp_exact(Y[d - 1], Y[d], t)
+        out = np.where(X[len(X) - 1] < x, Y[-1], mid)
+        return np.where(~(X[0] < x), Y[0], out)
+
+
+class FunctionTable:
+    """A 1-argument parser-context function with ``interpolate = true`` (context.cc:237-280):
+    its values g on intervals + 1 uniform points of the domain.  The reference's lookup
+    blends g[i] with g[j] where both are the integer part of (x - d0) * intervals /
+    (d1 - d0), so its result is g at that index exactly: a left-endpoint step function.
+    out_of_bounds = clamp clamps x into the domain (NaN to d0); out_of_bounds = error
+    raises MathError in the reference, and gives NaN here (the GPU path then fails the
+    Newton step)."""
+
+    def __init__(self, name, fn, intervals, d0, d1, clamp, constants, indep):
+        self.name = name
+        self.d0, self.d1, self.clamp = float(d0), float(d1), bool(clamp)
+        self.n = int(intervals)
+        nf = float(self.n)
+        width = (self.d1 - self.d0) / nf
+        self.ctn = nf / (self.d1 - self.d0)
+        xs = self.d0 + np.arange(self.n + 1, dtype=float) * width
+        env = dict(constants)
+        env[fn.args[0]] = xs
+        self.g = np.broadcast_to(np.asarray(evaluate(fn.body, env, indep), float), xs.shape).copy()
+
+    def __call__(self, x):
+        x = np.asarray(x, float)
+        if self.clamp:
+            x = np.where(x > self.d0, x, self.d0)
+            x = np.where(self.d1 < x, self.d1, x)
+            bad = np.zeros(x.shape, bool)
+        else:
+            bad = ~((x >= self.d0) & (x <= self.d1))
+            x = np.where(bad, self.d0, x)
+        i = np.minimum(((x - self.d0) * self.ctn).astype(np.int64), self.n)
+        return np.where(bad, np.nan, self.g[i])
+
+
+def _independent(functions):
+    return {k: v for k, v in (functions or {}).items() if isinstance(v, (Interpolation, TiffImage))}
 
 
 def parse_function_definition(text):
@@ -332,17 +392,23 @@ def evaluate(node, env, functions=None):
         args = [np.asarray(evaluate(a, env, functions), dtype=float) for a in node[2]]
         if name in functions:
             f = functions[name]
-            if isinstance(f, Interpolation):
+            if isinstance(f, (Interpolation, FunctionTable)):
                 if len(args) != 1:
                     raise ExprError("interpolation %r takes one argument" % name)
                 return f(args[0])
+            if isinstance(f, TiffImage):
+                if len(args) != 2:
+                    raise ExprError("tiff function %r takes two arguments" % name)
+                return f(args[0], args[1])
             if len(args) != len(f.args):
                 raise ExprError("function %r takes %d arguments" % (name, len(f.args)))
             inner = dict(env)
             for an, av in zip(f.args, args):
                 inner[an] = av
-            # user functions may not call other user functions (math_expr.mdx:325-347)
-            return evaluate(f.body, inner, None)
+            # a user function's body sees the context-independent functions (interpolation
+            # tables, images) but no other expression function (context.cc:283-330,
+            # math_expr.mdx:325-347)
+            return evaluate(f.body, inner, _independent(functions))
         if name not in FUNCTIONS:
             raise ExprError("unknown function %r" % name)
         lo, hi = FUNCTIONS[name]
@@ -428,14 +494,26 @@ class Context:
         self.functions = {}
         if cfg is None:
             return
+        tabulate = []
         for name in cfg.sub_keys():
             sub = cfg.sub(name)
             typ = sub.get("type")
             if typ == "constant":
                 self.constants[name] = float(sub["value"])
+            elif typ == "tiff":
+                try:
+                    self.functions[name] = TiffImage(sub["path"])
+                except TiffError as e:
+                    raise ExprError(str(e))
+            elif typ == "random_field":
+                # context.cc:93-160 needs the optional parafields library
+                raise ExprError("Library was compiled without random fields support")
+            elif typ == "cell_data":
+                raise ExprError("cell data is not implemented")
             elif typ == "function":
                 if sub.get_bool("interpolate", False):
-                    raise ExprError("parser_context.%s.interpolate = true is not supported" % name)
+                    tabulate.append((name, sub))
+                    continue
                 self.functions[name] = parse_function_definition(sub["expression"])
             elif typ == "interpolation":
                 dom = sub.get_floats("domain")
@@ -446,11 +524,36 @@ class Context:
                     raise ExprError("Interpolation range and domain must match (>= 2 points)")
                 self.functions[name] = Interpolation(dom, rng)
             else:
-                raise ExprError("unsupported parser_context type %r for %r" % (typ, name))
-        # user function bodies see the constants (context.cc add_independent_context)
+                raise ExprError("Unknown type %s" % typ)
+        # context.cc:237-280: 1-argument functions replaced by their values on a grid; the
+        # bodies see constants, interpolation tables and images only
+        indep = _independent(self.functions)
+        made = {}
+        for name, sub in tabulate:
+            fn = parse_function_definition(sub["expression"])
+            if len(fn.args) != 1:
+                raise ExprError("Cannot interpolate '%s' function with %d arguments" % (name, len(fn.args)))
+            nested = called_functions(fn.body) & (set(self.functions) - set(indep))
+            if nested:
+                raise ExprError("user functions may not call user functions: %s" % nested)
+            intervals = int(sub.get("interpolation.intervals", "1000"))
+            if intervals > 100000:
+                raise ExprError("Number of interpolation intervals is too big!")
+            if intervals < 1:
+                raise ExprError("At least one interval is required in function %s" % name)
+            dom = sub.get_floats("interpolation.domain." + fn.args[0]) if sub.has_key(
+                "interpolation.domain." + fn.args[0]) else [0.0, 1.0]
+            if dom[0] >= dom[1]:
+                raise ExprError("Domain arguments (%g, %g) of function %s are not ordered" % (dom[0], dom[1], name))
+            ooo = sub.get("interpolation.out_of_bounds", "error")
+            if ooo not in ("clamp", "error"):
+                raise ExprError("Not known '%s.interpolation.out_of_bounds = %s'" % (name, ooo))
+            made[name] = FunctionTable(name, fn, intervals, dom[0], dom[1], ooo == "clamp", self.constants, indep)
+        self.functions.update(made)
+        # user function bodies see the constants and the context-independent functions
         for f in self.functions.values():
             if isinstance(f, UserFunction):
-                nested = called_functions(f.body) & set(self.functions)
+                nested = called_functions(f.body) & (set(self.functions) - set(indep))
                 if nested:
                     raise ExprError("user functions may not call user functions: %s" % nested)
 

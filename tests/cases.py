@@ -353,3 +353,79 @@ time_step_max = 0.05
 [model.time_step_operator.nonlinear_solver]
 convergence_condition.relative_tolerance = 1e-16
 """ % (dim, path)
+
+
+def context_ini(tiff_a, tiff_b, n=20):
+    """Three species whose initial concentrations come from grayscale TIFF images (the
+    shape of the reference's test/time_snap.ini, on a structured square), with a function
+    tabulated over position (clamped), a function tabulated over the state, and an
+    interpolation table in the coefficients."""
+    return """
+[grid]
+dimension = 2
+cells = {n} {n}
+
+[compartments.domain]
+expression = 1
+
+[parser_context.A_initialConcentration]
+type = tiff
+path = {a}
+
+[parser_context.B_initialConcentration]
+type = tiff
+path = {b}
+
+[parser_context.dprofile]
+type = function
+expression = x: 0.2 + 0.1*sin(6*x)
+interpolate = true
+interpolation.intervals = 64
+interpolation.domain.x = 0 1
+interpolation.out_of_bounds = clamp
+
+[parser_context.sat]
+type = function
+expression = c: c/(50 + c)
+interpolate = true
+interpolation.intervals = 4000
+interpolation.domain.c = 0 2000
+interpolation.out_of_bounds = clamp
+
+[parser_context.ramp]
+type = interpolation
+domain = 0 0.3 0.7 1
+range = 1 1.5 0.5 1
+
+[model.scalar_field.A]
+compartment = domain
+cross_diffusion.A.expression = 0.4
+reaction.expression = A*B*1e-06*-100.0*ramp(position_y) - 0.01*sat(A)
+reaction.jacobian.A.expression = B*1e-06*-100.0*ramp(position_y)
+reaction.jacobian.B.expression = A*1e-06*-100.0*ramp(position_y)
+storage.expression = 1
+initial.expression = 1000*A_initialConcentration(position_x,position_y)
+
+[model.scalar_field.B]
+compartment = domain
+cross_diffusion.B.expression = 0.4
+reaction.expression = A*B*1e-06*-100.0*ramp(position_y)
+reaction.jacobian.A.expression = B*1e-06*-100.0*ramp(position_y)
+reaction.jacobian.B.expression = A*1e-06*-100.0*ramp(position_y)
+storage.expression = 1
+initial.expression = 1000*B_initialConcentration(position_x,position_y)
+
+[model.scalar_field.C]
+compartment = domain
+cross_diffusion.C.expression = 25*dprofile(position_x)
+reaction.expression = A*B*1e-06*100.0*ramp(position_y) + B_initialConcentration(position_x, position_y)
+reaction.jacobian.A.expression = B*1e-06*100.0*ramp(position_y)
+reaction.jacobian.B.expression = A*1e-06*100.0*ramp(position_y)
+storage.expression = 1
+initial.expression = 0
+
+[model.time_step_operator]
+type = ImplicitEuler
+time_step_initial = 0.1
+time_end = 0.2
+""".format(n=n, a=tiff_a, b=tiff_b)

@@ -504,3 +504,68 @@ def test_gmres_matches_oracle(dcgpu_lib, restart, precond, mixed):
     for t, errs, n_o, n_g, stages in records:
         for e in errs.values():
             assert e <= STEP_TOL, (restart, precond, mixed, t, e)
+
+
+@pytest.mark.parametrize("case,n", [("gray_scott", 24), ("gray_scott", 72), ("two_compartment", 40),
+                                    ("cross_diffusion_3d", 9)])
+@pytest.mark.parametrize("mixed", [False, True])
+@pytest.mark.parametrize("single", ["true", "false"])
+def test_single_launch_bicgstab_matches_oracle(dcgpu_lib, case, n, mixed, single):
+    """BiCGSTAB + block Jacobi as one cooperative launch per solve (single_launch = true,
+    the default) and as graph-replayed per-phase launches: both within the step tolerance of
+    the oracle.  The larger sizes run the single-launch kernel on many blocks (one block row
+    per thread), so its grid barriers and the block-order partial sums are exercised."""
+    builders = {"gray_scott": cases.small_gray_scott, "two_compartment": cases.small_two_compartment,
+                "cross_diffusion_3d": cases.small_3d}
+    ini, init = builders[case](n=n, steps=2)
+    ov = {"model.time_step_operator.linear_solver.single_launch": single}
+    records = _run_both(dcgpu_lib, ini, init, mixed=mixed, overrides=ov)
+    assert records
+    for t, errs, n_o, n_g, stages in records:
+        for name, e in errs.items():
+            assert e <= STEP_TOL, (case, n, t, name, e)
+        assert abs(n_o - n_g) <= max(1, stages)
+
+
+@pytest.mark.parametrize("mixed", [False, True])
+def test_single_launch_path_is_taken(dcgpu_lib, mixed):
+    """With single_launch on, the Krylov iterations run inside the cooperative kernel (the
+    per-phase SpMV timer sees no launch); with it off, no single-launch solve runs."""
+    ini, init = cases.small_gray_scott(n=48, steps=1)
+    om = OracleModel(ini)
+    x0 = _init_state(om, init)
+    seen = {}
+    for single in ("true", "false"):
+        gm = dcgpu_lib.Model(ini, {"model.time_step_operator.linear_solver.single_launch": single})
+        if mixed:
+            gm.set_mixed_precision(True)
+        gm.set_state(x0, 0.0)
+        gm.profile(True)
+        info = gm.step(1.0)
+        kt = gm.kernel_times()
+        gm.close()
+        seen[single] = (kt, info)
+    kt, info = seen["true"]
+    assert kt["krylov_iteration"][1] == info["linear_iterations"] > 0
+    assert kt["spmv"][1] == 0
+    kt, info = seen["false"]
+    assert kt["krylov_iteration"][1] == 0 and kt["spmv"][1] > 0
+
+
+def test_single_launch_matches_graph_path_at_full_size(dcgpu_lib):
+    """Gray-Scott 512^2 (526,338 DOF, more block rows than the cooperative grid has threads):
+    one mixed-precision Alexander2 step through the single-launch solve and through the
+    per-phase launches agree to far below the step tolerance, with the same Newton counts."""
+    import workloads as W
+    ini, init = W.gray_scott(n=512, steps=1, dt=1.0)
+    out = {}
+    for single in ("true", "false"):
+        gm = dcgpu_lib.Model(ini, {"model.time_step_operator.linear_solver.single_launch": single})
+        gm.set_mixed_precision(True)
+        gm.set_state(gm.seeded_state(init), 0.0)
+        info = gm.step(1.0)
+        out[single] = (gm.state(), info["newton_iterations"])
+        gm.close()
+    (xa, na), (xb, nb) = out["true"], out["false"]
+    assert na == nb
+    assert _rel(xa, xb) <= 1e-10

@@ -55,7 +55,22 @@ struct FusedBicgArgs {
   double* sc = nullptr;             // device scalars (KrylovSlot)
   double rel = 0.0;
   int max_it = 0;
+  // Mixed-precision iterative refinement around the solve (b64 null: a plain solve of r):
+  // solve J z = b64 in fp64 to the relative residual rel, each correction by the solve above
+  // in T on the scaled residual, to the relative reduction max(inner, rel / 2 / |r| * |b|).
+  // vals64 holds J in the BSR layout of rowptr / colidx; r64 is fp64 scratch.
+  const double* b64 = nullptr;
+  double* z64 = nullptr;
+  double* r64 = nullptr;
+  const double* vals64 = nullptr;
+  double inner = 1e-4;
+  int max_refinements = 50;
 };
+// results of a refined solve: sc[KS_ITER] all inner iterations, sc[KS_REFINEMENTS] the
+// corrections, sc[KS_RR] the final |r|^2 (fp64), sc[KS_DONE] 1 converged, 2 diverged (a
+// non-finite residual, or a correction that broke down in its first iteration), 0 not
+// converged within max_it iterations / max_refinements corrections
+constexpr int KS_REFINEMENTS = KS_SS;
 // Launch plan of the single-launch solve for block size bs: false when the device cannot
 // run it (no cooperative launch, unsupported block size).  blocks is bounded by what is
 // co-resident on the device and by the problem size; `slots` is the share of the device

@@ -317,16 +317,23 @@ __device__ __forceinline__ void sell_rows_jacobi(const Sell& S, int64_t sl, int 
   }
 }
 
-// The solve.  THREE (SELL-32 operator, block size <= 4): three phases per iteration, the
-// preconditioned vectors formed inside the SpMVs, p and v alternating between two buffers by
-// iteration parity (p[cur], v[cur] written, p[prv], v[prv] read).  Otherwise five phases:
-// p update with the Jacobi apply, SpMV, s update with the Jacobi apply, SpMV, x / r update.
+// A grid-wide barrier whose wait gave up: flag it; the caller's whole block returns.
+__device__ __forceinline__ bool barrier_or_fault(unsigned* bar, unsigned& gen, double* sc) {
+  if (grid_barrier(bar, gen)) return true;
+  if (threadIdx.x == 0) sc[KS_FAULT] = 1.0;
+  return false;
+}
+
+// One BiCGSTAB solve of A x = r to the relative reduction rel in at most max_it iterations.
+// With r64 set, r is first formed as r64 * scale (rounded to T), else read as it is.
+// THREE (SELL-32 operator, block size <= 4): three phases per iteration, the preconditioned
+// vectors formed inside the SpMVs, p and v alternating between two buffers by iteration
+// parity (p[cur], v[cur] written, p[prv], v[prv] read).  Otherwise five phases: p update
+// with the Jacobi apply, SpMV, s update with the Jacobi apply, SpMV, x / r update.
+// Returns false when a barrier wait gave up.
 template <int B, class T, class V, bool SELL, bool THREE>
-__global__ void __launch_bounds__(kFThreads, kFMinBlocksPerSm) k_bicgstab_single(FusedBicgArgs<T, V> a) {
-  static_assert(SELL || !THREE, "the three-phase iteration runs on the SELL operator");
-  __shared__ BicgScalars S;
-  unsigned* bar = reinterpret_cast<unsigned*>(a.sc + KS_BARRIER);
-  unsigned gen = 0;
+__device__ __forceinline__ bool bicg_solve(const FusedBicgArgs<T, V>& a, BicgScalars& S, unsigned* bar, unsigned& gen,
+                                           const double* r64, double scale, double rel, int max_it) {
   const int G = static_cast<int>(gridDim.x);
   double* part_rv = a.partial;
   double* part_ts = a.partial + G;
@@ -337,12 +344,6 @@ __global__ void __launch_bounds__(kFThreads, kFMinBlocksPerSm) k_bicgstab_single
   const int64_t nw = gstride >> 5;
   const int nrows = a.nrows;
   const int64_t n = static_cast<int64_t>(nrows) * B;
-  // a wait that gave up: flag it and leave (the whole block returns together)
-#define DC_BARRIER_OR_LEAVE                         \
-  if (!grid_barrier(bar, gen)) {                    \
-    if (threadIdx.x == 0) a.sc[KS_FAULT] = 1.0;     \
-    return;                                         \
-  }
 
   // x = 0, rhat = r, the p and v read by iteration 0 = 0, ||r||^2
   {
@@ -350,7 +351,13 @@ __global__ void __launch_bounds__(kFThreads, kFMinBlocksPerSm) k_bicgstab_single
     T* p0 = THREE ? a.p2 : a.p;
     T* v0 = THREE ? a.v2 : a.v;
     for (int64_t i = gtid; i < n; i += gstride) {
-      const T ri = __ldcg(a.r + i);
+      T ri;
+      if (r64) {
+        ri = static_cast<T>(__ldcg(r64 + i) * scale);
+        a.r[i] = ri;
+      } else {
+        ri = __ldcg(a.r + i);
+      }
       a.rhat[i] = ri;
       p0[i] = T(0);
       v0[i] = T(0);
@@ -359,16 +366,16 @@ __global__ void __launch_bounds__(kFThreads, kFMinBlocksPerSm) k_bicgstab_single
     }
     block_partials<1>(a1, part_rv);
   }
-  DC_BARRIER_OR_LEAVE
+  if (!barrier_or_fault(bar, gen, a.sc)) return false;
   {
     double t1[1];
     grid_totals0<1>(part_rv, t1);
-    if (threadIdx.x == 0) scalars_init(S, t1[0], a.rel);
+    if (threadIdx.x == 0) scalars_init(S, t1[0], rel);
   }
   __syncthreads();
 
   for (;;) {
-    if (S.done != 0.0 || S.it >= a.max_it) break;
+    if (S.done != 0.0 || S.it >= max_it) break;
     const int cur = S.it & 1;
     const V bv = static_cast<V>(S.beta), ov = static_cast<V>(S.omega);
     T* pc = (THREE && cur) ? a.p2 : a.p;
@@ -406,12 +413,12 @@ __global__ void __launch_bounds__(kFThreads, kFMinBlocksPerSm) k_bicgstab_single
         for (int i = 0; i < B; ++i) a.p[static_cast<int64_t>(nd) * B + i] = static_cast<T>(u[i]);
         jacobi_row<B, T, V>(a.dinv, nd, u, a.phat);
       }
-      DC_BARRIER_OR_LEAVE
+      if (!barrier_or_fault(bar, gen, a.sc)) return false;
       T acc[1] = {T(0)};
       spmv_dots<B, T, V, SELL, 1>(a, a.phat, a.v, a.rhat, acc, gtid, gstride);
       block_partials<1>(acc, part_rv);
     }
-    DC_BARRIER_OR_LEAVE
+    if (!barrier_or_fault(bar, gen, a.sc)) return false;
     {
       double t1[1];
       grid_totals0<1>(part_rv, t1);
@@ -456,12 +463,12 @@ __global__ void __launch_bounds__(kFThreads, kFMinBlocksPerSm) k_bicgstab_single
         for (int i = 0; i < B; ++i) a.s[static_cast<int64_t>(nd) * B + i] = static_cast<T>(u[i]);
         jacobi_row<B, T, V>(a.dinv, nd, u, a.shat);
       }
-      DC_BARRIER_OR_LEAVE
+      if (!barrier_or_fault(bar, gen, a.sc)) return false;
       T acc[2] = {T(0), T(0)};
       spmv_dots<B, T, V, SELL, 2>(a, a.shat, a.t, a.s, acc, gtid, gstride);
       block_partials<2>(acc, part_ts);
     }
-    DC_BARRIER_OR_LEAVE
+    if (!barrier_or_fault(bar, gen, a.sc)) return false;
     {
       double t2[2];
       grid_totals0<2>(part_ts, t2);
@@ -483,7 +490,7 @@ __global__ void __launch_bounds__(kFThreads, kFMinBlocksPerSm) k_bicgstab_single
       }
       block_partials<2>(acc, part_rr);
     }
-    DC_BARRIER_OR_LEAVE
+    if (!barrier_or_fault(bar, gen, a.sc)) return false;
     {
       double t2[2];
       grid_totals0<2>(part_rr, t2);
@@ -491,8 +498,132 @@ __global__ void __launch_bounds__(kFThreads, kFMinBlocksPerSm) k_bicgstab_single
     }
     __syncthreads();
   }
-#undef DC_BARRIER_OR_LEAVE
-  if (blockIdx.x == 0 && threadIdx.x == 0) scalars_store(S, a.sc);
+  return true;
+}
+
+// fp64 residual r64 = b64 - J z64 (one thread per scalar row, as the fp64 BSR SpMV) and
+// its squared norm into the block partials
+template <int B, class T, class V>
+__device__ __forceinline__ void residual64(const FusedBicgArgs<T, V>& a, double* part) {
+  const int gtid = blockIdx.x * kFThreads + threadIdx.x;
+  const int gstride = static_cast<int>(gridDim.x) * kFThreads;
+  const int64_t n = static_cast<int64_t>(a.nrows) * B;
+  double acc[1] = {0.0};
+  for (int64_t row = gtid; row < n; row += gstride) {
+    const int br = static_cast<int>(row / B), i = static_cast<int>(row % B);
+    double y = 0.0;
+    const int k0 = __ldg(a.rowptr + br), k1 = __ldg(a.rowptr + br + 1);
+    for (int k = k0; k < k1; ++k) {
+      const int c = __ldg(a.colidx + k);
+      const double* blk = a.vals64 + static_cast<int64_t>(k) * B * B + i * B;
+      const double* zc = a.z64 + static_cast<int64_t>(c) * B;
+#pragma unroll
+      for (int j = 0; j < B; ++j) y += __ldg(blk + j) * __ldcg(zc + j);
+    }
+    const double r = __ldg(a.b64 + row) - y;
+    a.r64[row] = r;
+    acc[0] += r * r;
+  }
+  block_partials<1>(acc, part);
+}
+
+// the refinement's state, kept in shared memory like the BiCGSTAB scalars
+struct RefineState {
+  double rn, target;
+  int total, refs, status;   // status: 0 running, 1 converged, 2 diverged, 3 out of iterations
+};
+
+template <int B, class T, class V, bool SELL, bool THREE>
+__global__ void __launch_bounds__(kFThreads, kFMinBlocksPerSm) k_bicgstab_single(FusedBicgArgs<T, V> a) {
+  static_assert(SELL || !THREE, "the three-phase iteration runs on the SELL operator");
+  __shared__ BicgScalars S;
+  __shared__ RefineState R;
+  unsigned* bar = reinterpret_cast<unsigned*>(a.sc + KS_BARRIER);
+  unsigned gen = 0;
+  if (!a.b64) {
+    if (!bicg_solve<B, T, V, SELL, THREE>(a, S, bar, gen, nullptr, 1.0, a.rel, a.max_it)) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) scalars_store(S, a.sc);
+    return;
+  }
+
+  // refined solve: z = 0, |b|
+  const int gtid = blockIdx.x * kFThreads + threadIdx.x;
+  const int gstride = static_cast<int>(gridDim.x) * kFThreads;
+  const int64_t n = static_cast<int64_t>(a.nrows) * B;
+  double* part = a.partial + 3 * static_cast<int64_t>(gridDim.x);   // the ||r||^2 partials
+  {
+    double acc[1] = {0.0};
+    for (int64_t i = gtid; i < n; i += gstride) {
+      a.z64[i] = 0.0;
+      const double bi = __ldg(a.b64 + i);
+      acc[0] += bi * bi;
+    }
+    block_partials<1>(acc, part);
+  }
+  if (!barrier_or_fault(bar, gen, a.sc)) return;
+  {
+    double t1[1];
+    grid_totals0<1>(part, t1);
+    if (threadIdx.x == 0) {
+      const double b0 = sqrt(t1[0]);
+      R.rn = b0;
+      R.target = a.rel * b0;
+      R.total = 0;
+      R.refs = 0;
+      R.status = b0 == 0.0 ? 1 : (!isfinite(b0) ? 2 : 0);
+    }
+  }
+  __syncthreads();
+
+  for (int ref = 0; R.status == 0 && ref < a.max_refinements && R.total < a.max_it; ++ref) {
+    if (ref > 0) {
+      // r = b - J z and its norm decide whether another correction is needed
+      residual64<B, T, V>(a, part);
+      if (!barrier_or_fault(bar, gen, a.sc)) return;
+      double t1[1];
+      grid_totals0<1>(part, t1);
+      if (threadIdx.x == 0) {
+        R.rn = sqrt(t1[0]);
+        if (!isfinite(R.rn)) R.status = 2;
+        else if (R.rn <= R.target) R.status = 1;
+      }
+      __syncthreads();
+      if (R.status != 0) break;
+    }
+    // the correction equation J d = r / |r| in T, then z += |r| d
+    const double rn = R.rn;
+    const double inner = fmax(a.inner, 0.5 * R.target / rn);
+    if (!bicg_solve<B, T, V, SELL, THREE>(a, S, bar, gen, ref == 0 ? a.b64 : a.r64, 1.0 / rn, inner,
+                                          a.max_it - R.total))
+      return;
+    if (threadIdx.x == 0) {
+      R.refs += 1;
+      R.total += S.it;
+      if (S.it == 0 && (S.done == kDoneBreakdown || S.done == kDoneNonFinite)) R.status = 2;
+    }
+    __syncthreads();
+    if (R.status != 0) break;
+    for (int64_t i = gtid; i < n; i += gstride) a.z64[i] += rn * static_cast<double>(__ldcg(a.x + i));
+    if (!barrier_or_fault(bar, gen, a.sc)) return;
+  }
+  if (R.status == 0) {
+    // out of corrections or iterations: the final residual decides
+    residual64<B, T, V>(a, part);
+    if (!barrier_or_fault(bar, gen, a.sc)) return;
+    double t1[1];
+    grid_totals0<1>(part, t1);
+    if (threadIdx.x == 0) {
+      R.rn = sqrt(t1[0]);
+      R.status = R.rn <= R.target ? 1 : 3;
+    }
+    __syncthreads();
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    a.sc[KS_ITER] = static_cast<double>(R.total);
+    a.sc[KS_REFINEMENTS] = static_cast<double>(R.refs);
+    a.sc[KS_RR] = R.rn * R.rn;
+    a.sc[KS_DONE] = R.status == 1 ? kDoneConverged : (R.status == 2 ? kDoneBreakdown : 0.0);
+  }
 }
 
 template <class T, class V>

@@ -578,7 +578,7 @@ struct SlotGuard {
 // nothing launched, when the device cannot run it; the caller then replays the graph of
 // per-phase launches.
 template <class T>
-bool Solver::krylov_fused(double rel, int max_it, int* iters, int* status) {
+bool Solver::krylov_fused(double rel, int max_it, int* iters, int* status, const double* b64, double* z64) {
   constexpr bool f32 = std::is_same_v<T, float>;
   const bool sell = f32 && spmv_format == kSpmvSell;
   const Bsr A = model.bsr(J_.get(), J32_.get());
@@ -609,6 +609,17 @@ bool Solver::krylov_fused(double rel, int max_it, int* iters, int* status) {
   a.sc = scal_.get();
   a.rel = rel;
   a.max_it = max_it;
+  if constexpr (f32) {
+    if (b64) {
+      // the fp64 iterative refinement of bicgstab_mixed, on the device
+      a.b64 = b64;
+      a.z64 = z64;
+      a.r64 = kr_.get();
+      a.vals64 = J_.get();
+      a.inner = kMixedInnerReduction;
+      a.max_refinements = kMixedMaxRefinements;
+    }
+  }
   if (profiling_ && !fused_ev_[0])
     for (auto& e : fused_ev_) cuda_check(cudaEventCreate(&e), "cudaEventCreate");
   if (profiling_) cuda_check(cudaEventRecord(fused_ev_[0], stream), "cudaEventRecord");
@@ -618,6 +629,7 @@ bool Solver::krylov_fused(double rel, int max_it, int* iters, int* status) {
   read_scalars(h, 0, KS_COUNT);
   if (h[KS_FAULT] != 0.0) throw std::runtime_error("single-launch BiCGSTAB: a grid-barrier wait timed out");
   *iters = static_cast<int>(h[KS_ITER]);
+  if (b64) stats.refinements += static_cast<long long>(h[KS_REFINEMENTS]);
   if (profiling_) {
     float ms = 0.0f;
     cuda_check(cudaEventElapsedTime(&ms, fused_ev_[0], fused_ev_[1]), "cudaEventElapsedTime");
@@ -694,6 +706,11 @@ int Solver::bicgstab(const double* b, double* z, double rel_tol, int max_it, int
 // fp32 BiCGSTAB on the correction equation inside fp64 iterative refinement:
 //   r = b - J z (fp64);  solve J d = r in fp32 to a modest reduction;  z += d
 int Solver::bicgstab_mixed(const double* b, double* z, double rel_tol, int max_it, int* iters) {
+  // BiCGSTAB + block Jacobi: the whole refinement loop below in one cooperative launch
+  if (fused_ && !krylov_cg_ && !krylov_gmres_ && !use_amg_) {
+    int st = DC_OK;
+    if (krylov_fused<float>(rel_tol, max_it, iters, &st, b, z)) return st;
+  }
   Bsr A = model.bsr(J_.get(), J32_.get());
   const int64_t n = n_;
   cuda_check(cudaMemsetAsync(z, 0, n * sizeof(double), stream), "memset");
@@ -702,10 +719,10 @@ int Solver::bicgstab_mixed(const double* b, double* z, double rel_tol, int max_i
   if (b0 == 0.0) return DC_OK;
   if (!std::isfinite(b0)) return DC_ERR_DIVERGED;
   const double target = rel_tol * b0;
-  const double inner_red = 1e-4;
+  const double inner_red = kMixedInnerReduction;
   double rn = b0;
   int total = 0;
-  for (int ref = 0; ref < 50 && total < max_it; ++ref) {
+  for (int ref = 0; ref < kMixedMaxRefinements && total < max_it; ++ref) {
     // fp64 refinement residual r = b - J z (skip the SpMV for z = 0)
     if (ref == 0) {
       cuda_check(cudaMemcpyAsync(kr_.get(), b, n * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");

@@ -170,8 +170,15 @@ class Solver {
   bool fused_ = true;
   DeviceBuffer<double> fpart_;
   cudaEvent_t fused_ev_[2] = {nullptr, nullptr};
+  // with b64 / z64 (fp32 only): the mixed-precision refinement loop solving J z = b64, in the
+  // same launch
   template <class T>
-  bool krylov_fused(double rel, int max_it, int* iters, int* status);
+  bool krylov_fused(double rel, int max_it, int* iters, int* status, const double* b64 = nullptr,
+                    double* z64 = nullptr);
+  // mixed precision: relative reduction asked of each fp32 correction, and the cap on
+  // corrections per solve
+  static constexpr double kMixedInnerReduction = 1e-4;
+  static constexpr int kMixedMaxRefinements = 50;
   double direct_tol_ = 1e-10;
   int lin_max_it_ = 500;
   std::string precond_ = "Jacobi";

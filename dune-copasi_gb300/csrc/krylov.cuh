@@ -35,7 +35,7 @@ constexpr double kDoneConverged = 1.0, kDoneBreakdown = 2.0, kDoneNonFinite = 3.
 // folds the per-block partial sums itself (same values, same order, so every block takes
 // the same convergence decision), and the loop runs on the device until convergence,
 // breakdown or max_it.  Same arithmetic per element as the five-kernel iteration below.
-// On the SELL-32 operator with block size <= 4 an iteration has three phases: each SpMV
+// On the SELL-32 operator with block size <= 2 an iteration has three phases: each SpMV
 // forms the preconditioned vector it multiplies (D^-1 (r + beta (p - omega v)), then
 // D^-1 (r - alpha v)) for every column it gathers, instead of reading it from a vector
 // written in a phase of its own; the BSR operator keeps five phases.

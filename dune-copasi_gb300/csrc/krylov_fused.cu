@@ -22,6 +22,13 @@ namespace {
 constexpr int kFThreads = 512;
 constexpr int kFWarps = kFThreads / 32;
 constexpr int kFMinBlocksPerSm = 2;
+// Largest block size for which the three-phase iteration (each SpMV forming the
+// preconditioned vector per gathered column) is used.  It trades two phases and their
+// barriers for 3B + B^2 values gathered per column instead of B: a gain while the operator
+// sits in L2 and the iteration is latency-bound (Gray-Scott 512^2, B = 2: 43 -> 38 us per
+// iteration), a loss once the gathers compete for HBM bandwidth (3D cross-diffusion 128^3,
+// B = 3: 55 % of the HBM peak against 73 % with five phases).
+constexpr int kThreePhaseMaxB = 2;
 constexpr unsigned long long kBarrierTimeoutNs = 2000000000ull;  // 2 s
 
 __device__ __forceinline__ unsigned long long global_ns() {
@@ -98,9 +105,23 @@ __device__ __forceinline__ void grid_totals0(const double* part, double (&out)[N
   double acc[N];
 #pragma unroll
   for (int k = 0; k < N; ++k) acc[k] = 0.0;
-  for (int b = threadIdx.x; b < static_cast<int>(gridDim.x); b += 32)
+  // a lane's partials (blocks lane, lane + 32, ...) are loaded 8 at a time before they are
+  // added, so their L2 latencies overlap
+  constexpr int U = 8;
+  const int G = static_cast<int>(gridDim.x);
+  for (int b0 = 0; b0 < G; b0 += 32 * U) {
+    double v[U][N];
 #pragma unroll
-    for (int k = 0; k < N; ++k) acc[k] += __ldcg(part + static_cast<int64_t>(b) * N + k);
+    for (int u = 0; u < U; ++u) {
+      const int b = b0 + u * 32 + static_cast<int>(threadIdx.x);
+#pragma unroll
+      for (int k = 0; k < N; ++k) v[u][k] = b < G ? __ldcg(part + static_cast<int64_t>(b) * N + k) : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int k = 0; k < N; ++k) acc[k] += v[u][k];
+  }
 #pragma unroll
   for (int k = 0; k < N; ++k) {
 #pragma unroll
@@ -247,25 +268,31 @@ __device__ __forceinline__ void jacobi_row(const V* __restrict__ dinv, int nd, c
 template <int B, class T, class V, bool PU>
 __device__ __forceinline__ void combine_row(int64_t c, const T* __restrict__ r, const T* __restrict__ p,
                                             const T* __restrict__ v, V c1, V c2, V (&u)[B]) {
+  T rv[B], vv[B];
+  load_block<B, true>(r + c * B, rv);
+  load_block<B, true>(v + c * B, vv);
+  if constexpr (PU) {
+    T pv[B];
+    load_block<B, true>(p + c * B, pv);
 #pragma unroll
-  for (int j = 0; j < B; ++j) {
-    const int64_t k = c * B + j;
-    if constexpr (PU)
-      u[j] = static_cast<V>(__ldcg(r + k)) + c1 * (static_cast<V>(__ldcg(p + k)) - c2 * static_cast<V>(__ldcg(v + k)));
-    else
-      u[j] = static_cast<V>(__ldcg(r + k)) - c1 * static_cast<V>(__ldcg(v + k));
+    for (int j = 0; j < B; ++j)
+      u[j] = static_cast<V>(rv[j]) + c1 * (static_cast<V>(pv[j]) - c2 * static_cast<V>(vv[j]));
+  } else {
+#pragma unroll
+    for (int j = 0; j < B; ++j) u[j] = static_cast<V>(rv[j]) - c1 * static_cast<V>(vv[j]);
   }
 }
 
 // D_c^-1 u rounded to T, as the stored preconditioned vector would hold it
 template <int B, class T, class V>
 __device__ __forceinline__ void jacobi_apply(const V* __restrict__ dinv, int64_t c, const V (&u)[B], V (&out)[B]) {
-  const V* d = dinv + c * B * B;
+  V d[B * B];
+  load_block<B * B, false>(dinv + c * B * B, d);
 #pragma unroll
   for (int i = 0; i < B; ++i) {
     V acc = V(0);
 #pragma unroll
-    for (int j = 0; j < B; ++j) acc += __ldg(d + i * B + j) * u[j];
+    for (int j = 0; j < B; ++j) acc += d[i * B + j] * u[j];
     out[i] = static_cast<V>(static_cast<T>(acc));
   }
 }
@@ -282,14 +309,23 @@ __device__ __forceinline__ void sell_rows_jacobi(const Sell& S, int64_t sl, int 
   for (int i = 0; i < B; ++i) acc[i] = V(0);
   const int64_t o0 = S.off[sl], o1 = S.off[sl + 1];
   const int32_t* __restrict__ cols = S.cols + o0 * 32 + lane;
-  const V* __restrict__ vbase = val + o0 * (32 * B * B) + lane;
+  const V* __restrict__ vbase = val + (o0 * 32 + lane) * (B * B);
   const int w = static_cast<int>(o1 - o0);
   constexpr int U = 2;
+  // the column indices of the next batch are loaded while the current batch's gathers are
+  // in flight, so a batch costs one L2 round trip, not two
+  int cn[U];
+#pragma unroll
+  for (int q = 0; q < U; ++q) cn[q] = q < w ? __ldg(cols + q * 32) : 0;
   int k = 0;
   for (; k + U <= w; k += U) {
     int c[U];
 #pragma unroll
-    for (int q = 0; q < U; ++q) c[q] = __ldg(cols + (k + q) * 32);
+    for (int q = 0; q < U; ++q) {
+      c[q] = cn[q];
+      const int kn = k + U + q;
+      cn[q] = kn < w ? __ldg(cols + kn * 32) : 0;
+    }
     V u[U][B], xh[U][B];
 #pragma unroll
     for (int q = 0; q < U; ++q) combine_row<B, T, V, PU>(c[q], r, p, v, c1, c2, u[q]);
@@ -297,23 +333,28 @@ __device__ __forceinline__ void sell_rows_jacobi(const Sell& S, int64_t sl, int 
     for (int q = 0; q < U; ++q) jacobi_apply<B, T, V>(dinv, c[q], u[q], xh[q]);
 #pragma unroll
     for (int q = 0; q < U; ++q) {
-      const V* __restrict__ vk = vbase + static_cast<int64_t>(k + q) * (32 * B * B);
+      V blk[B * B];
+      load_block<B * B, false>(vbase + static_cast<int64_t>(k + q) * (32 * B * B), blk);
 #pragma unroll
       for (int i = 0; i < B; ++i)
 #pragma unroll
-        for (int j = 0; j < B; ++j) acc[i] += __ldg(vk + (i * B + j) * 32) * xh[q][j];
+        for (int j = 0; j < B; ++j) acc[i] += blk[i * B + j] * xh[q][j];
     }
   }
-  for (; k < w; ++k) {
-    const int c = __ldg(cols + k * 32);
+  // the last w % U slots, whose columns are already in cn
+#pragma unroll
+  for (int q = 0; q < U - 1; ++q) {
+    if (k + q >= w) break;
+    const int c = cn[q];
     V u[B], xh[B];
     combine_row<B, T, V, PU>(c, r, p, v, c1, c2, u);
     jacobi_apply<B, T, V>(dinv, c, u, xh);
-    const V* __restrict__ vk = vbase + static_cast<int64_t>(k) * (32 * B * B);
+    V blk[B * B];
+    load_block<B * B, false>(vbase + static_cast<int64_t>(k + q) * (32 * B * B), blk);
 #pragma unroll
     for (int i = 0; i < B; ++i)
 #pragma unroll
-      for (int j = 0; j < B; ++j) acc[i] += __ldg(vk + (i * B + j) * 32) * xh[j];
+      for (int j = 0; j < B; ++j) acc[i] += blk[i * B + j] * xh[j];
   }
 }
 
@@ -326,7 +367,7 @@ __device__ __forceinline__ bool barrier_or_fault(unsigned* bar, unsigned& gen, d
 
 // One BiCGSTAB solve of A x = r to the relative reduction rel in at most max_it iterations.
 // With r64 set, r is first formed as r64 * scale (rounded to T), else read as it is.
-// THREE (SELL-32 operator, block size <= 4): three phases per iteration, the preconditioned
+// THREE (SELL-32 operator, block size <= kThreePhaseMaxB): three phases per iteration, the preconditioned
 // vectors formed inside the SpMVs, p and v alternating between two buffers by iteration
 // parity (p[cur], v[cur] written, p[prv], v[prv] read).  Otherwise five phases: p update
 // with the Jacobi apply, SpMV, s update with the Jacobi apply, SpMV, x / r update.
@@ -631,7 +672,7 @@ const void* fused_kernel(int bs, bool sell) {
 #define DC_FK(B)                                                                                   \
   case B:                                                                                          \
     if constexpr (std::is_same_v<V, float>) {                                                      \
-      if constexpr (B <= 4) {                                                                      \
+      if constexpr (B <= kThreePhaseMaxB) {                                                        \
         if (sell) return reinterpret_cast<const void*>(&k_bicgstab_single<B, T, V, true, true>);   \
       }                                                                                            \
       if (sell) return reinterpret_cast<const void*>(&k_bicgstab_single<B, T, V, true, false>);    \

@@ -2,15 +2,17 @@
 // Krylov operator.
 //
 // Block rows are taken in slices of 32 consecutive rows.  Slot k of a slice holds the k-th
-// stored block of each of its 32 rows, zero padded up to the slice's longest row.  Entry
-// (i, j) of slot k of lane r (row 32 s + r) sits at ((off[s] + k) * B*B + i*B + j) * 32 + r
-// and the slot's block column at (off[s] + k) * 32 + r.  A warp computes one slice, one lane
-// per block row: every value load of the warp is one contiguous 128-byte line, the column
-// load too, against (32 / B) scattered B-value segments per load of the thread-per-row BSR
-// kernel.  Padding slots point at the row itself and hold zeros.
+// stored block of each of its 32 rows, zero padded up to the slice's longest row.  The B x B
+// block of slot k of lane r (row 32 s + r) is contiguous, row-major, at
+// ((off[s] + k) * 32 + r) * B*B, and the slot's block column sits at (off[s] + k) * 32 + r.
+// A warp computes one slice, one lane per block row: a slot's 32 blocks are one contiguous
+// 32 * B*B-value stretch, which a lane reads with one 16-byte load for B = 2 (B*B / 4 loads
+// for B = 4), and the column load of the warp is one 128-byte line.  Padding slots point at
+// the row itself (row 0 past the last row) and hold zeros.
 #pragma once
 
 #include <cstdint>
+#include <type_traits>
 
 namespace dcgpu {
 
@@ -24,9 +26,35 @@ struct Sell {
 };
 
 #ifdef __CUDACC__
+// N consecutive values starting at p: 8- or 16-byte loads for fp32 runs of 2 or a multiple
+// of 4 values (the callers' offsets are multiples of 8 / 16 bytes), else N loads.
+// kCoherent reads through L2 only (ld.global.cg, for data that other blocks write inside
+// the same launch), otherwise through the read-only path.
+template <int N, bool kCoherent, class T>
+__device__ __forceinline__ void load_block(const T* __restrict__ p, T (&out)[N]) {
+  if constexpr (std::is_same_v<T, float> && N == 2) {
+    const float2 q = kCoherent ? __ldcg(reinterpret_cast<const float2*>(p)) : __ldg(reinterpret_cast<const float2*>(p));
+    out[0] = q.x;
+    out[1] = q.y;
+  } else if constexpr (std::is_same_v<T, float> && N % 4 == 0) {
+#pragma unroll
+    for (int j = 0; j < N; j += 4) {
+      const float4 q = kCoherent ? __ldcg(reinterpret_cast<const float4*>(p + j))
+                                 : __ldg(reinterpret_cast<const float4*>(p + j));
+      out[j] = q.x;
+      out[j + 1] = q.y;
+      out[j + 2] = q.z;
+      out[j + 3] = q.w;
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < N; ++j) out[j] = kCoherent ? __ldcg(p + j) : __ldg(p + j);
+  }
+}
+
 // y rows of slice `sl` for lane `lane`: acc[i] = sum over the lane's blocks of A(i, :) x.
-// kCoherent reads x through L2 only (ld.global.cg), for kernels in which other blocks write x
-// between grid-wide barriers; the operator itself is read-only and uses the read-only path.
+// kCoherent reads x through L2 only, for kernels in which other blocks write x between
+// grid-wide barriers; the operator itself is read-only and uses the read-only path.
 template <int B, class T, class V, bool kCoherent = false>
 __device__ __forceinline__ void sell_lane_rows(const Sell& S, int64_t sl, int lane, const V* __restrict__ val,
                                                const T* __restrict__ x, V (&acc)[B]) {
@@ -34,47 +62,49 @@ __device__ __forceinline__ void sell_lane_rows(const Sell& S, int64_t sl, int la
   for (int i = 0; i < B; ++i) acc[i] = V(0);
   const int64_t o0 = S.off[sl], o1 = S.off[sl + 1];
   const int32_t* __restrict__ cols = S.cols + o0 * 32 + lane;
-  const V* __restrict__ v = val + o0 * (32 * B * B) + lane;
+  const V* __restrict__ v = val + (o0 * 32 + lane) * (B * B);
   const int w = static_cast<int>(o1 - o0);
   // slots in batches of U: the U column loads, then the U x gathers, are independent of
-  // one another, so a lane has U (not one) dependent load chains in flight; the slice's
-  // time is then a few L2 round trips instead of two per slot
+  // one another, so a lane has U (not one) dependent load chains in flight, and the next
+  // batch's column indices load while this batch's gathers are in flight
   constexpr int U = B <= 2 ? 4 : 2;
+  int cn[U];
+#pragma unroll
+  for (int u = 0; u < U; ++u) cn[u] = u < w ? __ldg(cols + u * 32) : 0;
   int k = 0;
   for (; k + U <= w; k += U) {
     int c[U];
 #pragma unroll
-    for (int u = 0; u < U; ++u) c[u] = __ldg(cols + (k + u) * 32);
-    V xv[U][B];
+    for (int u = 0; u < U; ++u) {
+      c[u] = cn[u];
+      const int kn = k + U + u;
+      cn[u] = kn < w ? __ldg(cols + kn * 32) : 0;
+    }
+    T xv[U][B];
 #pragma unroll
-    for (int u = 0; u < U; ++u)
-#pragma unroll
-      for (int j = 0; j < B; ++j) {
-        const T* xp = x + static_cast<int64_t>(c[u]) * B + j;
-        xv[u][j] = static_cast<V>(kCoherent ? __ldcg(xp) : *xp);
-      }
+    for (int u = 0; u < U; ++u) load_block<B, kCoherent>(x + static_cast<int64_t>(c[u]) * B, xv[u]);
 #pragma unroll
     for (int u = 0; u < U; ++u) {
-      const V* __restrict__ vk = v + static_cast<int64_t>(k + u) * (32 * B * B);
+      V blk[B * B];
+      load_block<B * B, false>(v + static_cast<int64_t>(k + u) * (32 * B * B), blk);
 #pragma unroll
       for (int i = 0; i < B; ++i)
 #pragma unroll
-        for (int j = 0; j < B; ++j) acc[i] += __ldg(vk + (i * B + j) * 32) * xv[u][j];
+        for (int j = 0; j < B; ++j) acc[i] += blk[i * B + j] * static_cast<V>(xv[u][j]);
     }
   }
-  for (; k < w; ++k) {
-    const int c = __ldg(cols + k * 32);
-    V xv[B];
+  // the last w % U slots, whose columns are already in cn
 #pragma unroll
-    for (int j = 0; j < B; ++j) {
-      const T* xp = x + static_cast<int64_t>(c) * B + j;
-      xv[j] = static_cast<V>(kCoherent ? __ldcg(xp) : *xp);
-    }
-    const V* __restrict__ vk = v + static_cast<int64_t>(k) * (32 * B * B);
+  for (int u = 0; u < U - 1; ++u) {
+    if (k + u >= w) break;
+    T xv[B];
+    load_block<B, kCoherent>(x + static_cast<int64_t>(cn[u]) * B, xv);
+    V blk[B * B];
+    load_block<B * B, false>(v + static_cast<int64_t>(k + u) * (32 * B * B), blk);
 #pragma unroll
     for (int i = 0; i < B; ++i)
 #pragma unroll
-      for (int j = 0; j < B; ++j) acc[i] += __ldg(vk + (i * B + j) * 32) * xv[j];
+      for (int j = 0; j < B; ++j) acc[i] += blk[i * B + j] * static_cast<V>(xv[j]);
   }
 }
 #endif

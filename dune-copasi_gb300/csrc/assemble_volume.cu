@@ -3,6 +3,7 @@
 #include <cstdio>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
 
 #include "assemble.cuh"
 #include "interp.cuh"
@@ -62,13 +63,12 @@ template <> struct MassConst<3> {
   static constexpr double alpha = 0.5854101966249685, beta = 0.1381966011250105;
 };
 
-template <int DIM, int NS>
-__device__ __forceinline__ double volume_input(uint16_t id, const double (&u)[NS],
-                                               const double (&g)[NS][DIM], const double (&xq)[DIM],
-                                               double t, double vol, int soff) {
+template <int DIM, int NS, class F = double>
+__device__ __forceinline__ F volume_input(uint16_t id, const F (&u)[NS], const F (&g)[NS][DIM], const F (&xq)[DIM],
+                                          F t, F vol, int soff) {
   if (id < IN_GRAD) {
     const int s = static_cast<int>(id) - soff;
-    double v = 0.0;
+    F v = F(0);
 #pragma unroll
     for (int i = 0; i < NS; ++i)
       if (i == s) v = u[i];
@@ -77,7 +77,7 @@ __device__ __forceinline__ double volume_input(uint16_t id, const double (&u)[NS
   if (id < IN_POSITION) {
     const int gi = static_cast<int>(id) - IN_GRAD;
     const int s = gi / 3 - soff, ax = gi % 3;
-    double v = 0.0;
+    F v = F(0);
 #pragma unroll
     for (int i = 0; i < NS; ++i)
 #pragma unroll
@@ -87,7 +87,7 @@ __device__ __forceinline__ double volume_input(uint16_t id, const double (&u)[NS
   }
   if (id < IN_NORMAL) {
     const int ax = static_cast<int>(id) - IN_POSITION;
-    double v = 0.0;
+    F v = F(0);
 #pragma unroll
     for (int d = 0; d < DIM; ++d)
       if (d == ax) v = xq[d];
@@ -96,8 +96,8 @@ __device__ __forceinline__ double volume_input(uint16_t id, const double (&u)[NS
   switch (id) {
     case IN_TIME: return t;
     case IN_ENTITY_VOLUME: return vol;
-    case IN_IN_VOLUME: return 1.0;
-    default: return 0.0;
+    case IN_IN_VOLUME: return F(1);
+    default: return F(0);
   }
 }
 
@@ -173,7 +173,7 @@ __device__ __forceinline__ void element_jacobian(const VolumeParams& P, const JT
   }
 }
 
-template <int DIM, int NS>
+template <int DIM, int NS, class F>
 __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int begin, const int end,
                                                 const int mode) {
   constexpr int NL = DIM + 1;
@@ -182,7 +182,7 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
   if (k >= end) return;
 
   int nd[NL];
-  double X[NL][DIM];
+  F X[NL][DIM];
 #pragma unroll
   for (int a = 0; a < NL; ++a) {
     const int v = P.verts[static_cast<int64_t>(k) * NL + a];
@@ -191,24 +191,24 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
     for (int d = 0; d < DIM; ++d) X[a][d] = P.coords[static_cast<int64_t>(v) * DIM + d];
   }
   // affine map x = X0 + Bm xi ; gradients of the P1 basis: rows of B^{-1} (local_operator.hh:461-464)
-  double Bm[DIM][DIM];
+  F Bm[DIM][DIM];
 #pragma unroll
   for (int i = 0; i < DIM; ++i)
 #pragma unroll
     for (int j = 0; j < DIM; ++j) Bm[i][j] = X[j + 1][i] - X[0][i];
-  double Bi[DIM][DIM];
-  double det;
+  F Bi[DIM][DIM];
+  F det;
   if constexpr (DIM == 2) {
     det = Bm[0][0] * Bm[1][1] - Bm[0][1] * Bm[1][0];
-    const double id = 1.0 / det;
+    const F id = F(1) / det;
     Bi[0][0] = Bm[1][1] * id;  Bi[0][1] = -Bm[0][1] * id;
     Bi[1][0] = -Bm[1][0] * id; Bi[1][1] = Bm[0][0] * id;
   } else {
-    const double c00 = Bm[1][1] * Bm[2][2] - Bm[1][2] * Bm[2][1];
-    const double c01 = Bm[1][2] * Bm[2][0] - Bm[1][0] * Bm[2][2];
-    const double c02 = Bm[1][0] * Bm[2][1] - Bm[1][1] * Bm[2][0];
+    const F c00 = Bm[1][1] * Bm[2][2] - Bm[1][2] * Bm[2][1];
+    const F c01 = Bm[1][2] * Bm[2][0] - Bm[1][0] * Bm[2][2];
+    const F c02 = Bm[1][0] * Bm[2][1] - Bm[1][1] * Bm[2][0];
     det = Bm[0][0] * c00 + Bm[0][1] * c01 + Bm[0][2] * c02;
-    const double id = 1.0 / det;
+    const F id = F(1) / det;
     Bi[0][0] = c00 * id;
     Bi[1][0] = c01 * id;
     Bi[2][0] = c02 * id;
@@ -219,12 +219,12 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
     Bi[1][2] = (Bm[0][2] * Bm[1][0] - Bm[0][0] * Bm[1][2]) * id;
     Bi[2][2] = (Bm[0][0] * Bm[1][1] - Bm[0][1] * Bm[1][0]) * id;
   }
-  const double adet = fabs(det);
-  const double vol = adet / (DIM == 2 ? 2.0 : 6.0);
-  double G[NL][DIM];
+  const F adet = fabs(det);
+  const F vol = adet / F(DIM == 2 ? 2 : 6);
+  F G[NL][DIM];
 #pragma unroll
   for (int j = 0; j < DIM; ++j) {
-    double s = 0.0;
+    F s = 0.0;
 #pragma unroll
     for (int kk = 0; kk < DIM; ++kk) {
       G[kk + 1][j] = Bi[kk][j];
@@ -234,18 +234,18 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
   }
 
   const int bs = P.bs;
-  double c[NL][NS];
+  F c[NL][NS];
 #pragma unroll
   for (int a = 0; a < NL; ++a)
 #pragma unroll
     for (int s = 0; s < NS; ++s) c[a][s] = P.x ? P.x[static_cast<int64_t>(nd[a]) * bs + s] : 0.0;
   // state gradients only when a program reads them or a term takes one (uniform branch)
-  double g[NS][DIM];
+  F g[NS][DIM];
 #pragma unroll
   for (int s = 0; s < NS; ++s)
 #pragma unroll
     for (int j = 0; j < DIM; ++j) {
-      double acc = 0.0;
+      F acc = 0.0;
       if (P.need_grad) {
 #pragma unroll
         for (int a = 0; a < NL; ++a) acc += c[a][s] * G[a][j];
@@ -255,12 +255,12 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
 
   const bool do_res = (mode & 1) && P.r;
   const bool do_jac = (mode & 2) && P.J;
-  double rl[NL][NS];
+  F rl[NL][NS];
 #pragma unroll
   for (int a = 0; a < NL; ++a)
 #pragma unroll
     for (int s = 0; s < NS; ++s) rl[a][s] = 0.0;
-  double coef[kMaxCoefficients];
+  F coef[kMaxCoefficients];
   int ncoef = 0;
   if (do_jac) {
     for (int t = 0; t < P.n_jac_terms; ++t) {
@@ -274,36 +274,36 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
     }
     for (int i = 0; i < ncoef; ++i) coef[i] = 0.0;
   }
-  double R[kMaxDevRegisters];
+  F R[kMaxDevRegisters];
 
 #pragma unroll 1
   for (int q = 0; q < NQ; ++q) {
-    double u[NS];
+    F u[NS];
 #pragma unroll
     for (int s = 0; s < NS; ++s) {
-      double acc = 0.0;
+      F acc = 0.0;
 #pragma unroll
-      for (int a = 0; a < NL; ++a) acc += c[a][s] * phi<DIM>(q, a);
+      for (int a = 0; a < NL; ++a) acc += c[a][s] * F(phi<DIM>(q, a));
       u[s] = acc;
     }
-    double xq[DIM];
+    F xq[DIM];
 #pragma unroll
     for (int i = 0; i < DIM; ++i) {
-      double acc = X[0][i];
+      F acc = X[0][i];
       if (P.need_pos) {
 #pragma unroll
-        for (int j = 0; j < DIM; ++j) acc += Bm[i][j] * Rule<DIM>::xi(q, j);
+        for (int j = 0; j < DIM; ++j) acc += Bm[i][j] * F(Rule<DIM>::xi(q, j));
       }
       xq[i] = acc;
     }
-    const double fq = Rule<DIM>::w(q) * adet;
+    const F fq = F(Rule<DIM>::w(q)) * adet;
     for (int i = 0; i < P.prog.ninputs; ++i)
-      R[i] = volume_input<DIM, NS>(P.prog.inputs[i], u, g, xq, P.t, vol, P.species_offset);
+      R[i] = volume_input<DIM, NS, F>(P.prog.inputs[i], u, g, xq, F(P.t), vol, P.species_offset);
     run_program(P.prog, P.tables, R);
     const uint8_t* out = P.prog.outputs;
 
     if (do_res) {
-      double scal[NS], flux[NS][DIM];
+      F scal[NS], flux[NS][DIM];
 #pragma unroll
       for (int s = 0; s < NS; ++s) {
         scal[s] = 0.0;
@@ -312,16 +312,16 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
       }
       for (int t = 0; t < P.n_res_terms; ++t) {
         const Term T = P.res_terms[t];
-        const double sc = T.form ? P.ca : P.cm;
-        const double o = R[out[T.out]];
-        double ds = 0.0, df[DIM];
+        const F sc = F(T.form ? P.ca : P.cm);
+        const F o = R[out[T.out]];
+        F ds = 0.0, df[DIM];
 #pragma unroll
         for (int j = 0; j < DIM; ++j) df[j] = 0.0;
-        double ut = 0.0;
+        F ut = 0.0;
 #pragma unroll
         for (int s = 0; s < NS; ++s)
           if (s == T.test) ut = u[s];
-        double gw[DIM];
+        F gw[DIM];
 #pragma unroll
         for (int j = 0; j < DIM; ++j) {
           gw[j] = 0.0;
@@ -343,7 +343,7 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
           case R_DIFF_TENSOR:
 #pragma unroll
             for (int i = 0; i < DIM; ++i) {
-              double acc = 0.0;
+              F acc = 0.0;
 #pragma unroll
               for (int j = 0; j < DIM; ++j) acc += R[out[T.out + i * DIM + j]] * gw[j];
               df[i] = -acc;
@@ -362,24 +362,24 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
       }
       // rl[a][s] += (scal[s] phi_a - flux[s] . G_a) fq, with the factor fq applied once per
       // species rather than per entry (one FMA per entry for the scalar part)
-      double ts[NS];
+      F ts[NS];
 #pragma unroll
       for (int s = 0; s < NS; ++s) ts[s] = scal[s] * fq;
 #pragma unroll
       for (int a = 0; a < NL; ++a) {
-        const double pa = phi<DIM>(q, a);
+        const F pa = F(phi<DIM>(q, a));
 #pragma unroll
         for (int s = 0; s < NS; ++s) rl[a][s] = fma(ts[s], pa, rl[a][s]);
       }
       if (P.has_flux) {
 #pragma unroll
         for (int s = 0; s < NS; ++s) {
-          double tf[DIM];
+          F tf[DIM];
 #pragma unroll
           for (int j = 0; j < DIM; ++j) tf[j] = flux[s][j] * fq;
 #pragma unroll
           for (int a = 0; a < NL; ++a) {
-            double fg = 0.0;
+            F fg = 0.0;
 #pragma unroll
             for (int j = 0; j < DIM; ++j) fg = fma(tf[j], G[a][j], fg);
             rl[a][s] -= fg;
@@ -389,12 +389,12 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
     }
 
     if (do_jac) {
-      const double scm = P.cm * fq, sca = P.ca * fq;
+      const F scm = F(P.cm) * fq, sca = F(P.ca) * fq;
       for (int t = 0; t < P.n_jac_terms; ++t) {
         const Term T = P.jac_terms[t];
-        const double sc = T.form ? sca : scm;
-        const double o = R[out[T.out]];
-        double ut = 0.0;
+        const F sc = T.form ? sca : scm;
+        const F o = R[out[T.out]];
+        F ut = 0.0;
 #pragma unroll
         for (int s = 0; s < NS; ++s)
           if (s == T.test) ut = u[s];
@@ -411,7 +411,7 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
           case J_VELOCITY_JAC:
           case J_DIFFJAC_SCALAR:
           case J_DIFFJAC_TENSOR: {
-            double vec[DIM];
+            F vec[DIM];
             if (T.kind == J_VELOCITY) {
 #pragma unroll
               for (int j = 0; j < DIM; ++j) vec[j] = -R[out[T.out + j]];
@@ -419,7 +419,7 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
 #pragma unroll
               for (int j = 0; j < DIM; ++j) vec[j] = -R[out[T.out + j]] * ut;
             } else {
-              double gw[DIM];
+              F gw[DIM];
 #pragma unroll
               for (int j = 0; j < DIM; ++j) {
                 gw[j] = 0.0;
@@ -433,7 +433,7 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
               } else {
 #pragma unroll
                 for (int i = 0; i < DIM; ++i) {
-                  double acc = 0.0;
+                  F acc = 0.0;
 #pragma unroll
                   for (int j = 0; j < DIM; ++j) acc += R[out[T.out + i * DIM + j]] * gw[j];
                   vec[i] = acc;
@@ -442,7 +442,7 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
             }
 #pragma unroll
             for (int a = 0; a < NL; ++a) {
-              const double pa = phi<DIM>(q, a) * sc;
+              const F pa = F(phi<DIM>(q, a)) * sc;
 #pragma unroll
               for (int j = 0; j < DIM; ++j) coef[T.coef + a * DIM + j] += pa * vec[j];
             }
@@ -461,7 +461,7 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
 #pragma unroll
     for (int a = 0; a < NL; ++a)
 #pragma unroll
-      for (int s = 0; s < NS; ++s) er[a * NS + s] = rl[a][s];
+      for (int s = 0; s < NS; ++s) er[a * NS + s] = static_cast<double>(rl[a][s]);
   }
   if (do_jac) {
     constexpr double be = MassConst<DIM>::beta;
@@ -469,16 +469,19 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
     for (int t = 0; t < P.n_jac_terms; ++t) {
       const Term T = P.jac_terms[t];
       if (T.kind == J_MASS || T.kind == J_MASS_U || T.kind == J_STORAGE_SELF) {
-        double S = 0.0;
+        F S = 0.0;
 #pragma unroll
         for (int q = 0; q < NQ; ++q) S += coef[T.coef + q];
-        coef[T.coef + NQ] = (be * be) * S;
+        coef[T.coef + NQ] = F(be * be) * S;
       }
     }
     const int64_t off = static_cast<int64_t>(k) * NL * NL * P.n_slots;
-    if (P.jac_f32) {
-      // mixed precision: the element Jacobian in fp32 (the fp32 Krylov operator is built
-      // from it; the residual stays fp64)
+    if constexpr (std::is_same_v<F, float>) {
+      // the FP32 Jacobian-only pass of the mixed-precision path
+      element_jacobian<DIM, float>(P, coef, G, reinterpret_cast<float*>(P.ej) + off);
+    } else if (P.jac_f32) {
+      // mixed precision, computed alongside the fp64 residual: the element Jacobian in fp32
+      // (the fp32 Krylov operator is built from it; the residual stays fp64)
       float cf[kMaxCoefficients];
       for (int i = 0; i < ncoef; ++i) cf[i] = static_cast<float>(coef[i]);
       float Gf[NL][DIM];
@@ -734,8 +737,10 @@ void launch_t(const VolumeParams& p, int begin, int end, int mode, cudaStream_t 
   count_launches(1);
   if (mode == kVolumeNumericalJacobian)
     k_volume_fd<DIM, NS><<<(n + threads - 1) / threads, threads, 0, stream>>>(p, begin, end);
+  else if (mode == 2 && p.jac_f32)
+    k_volume<DIM, NS, float><<<(n + threads - 1) / threads, threads, 0, stream>>>(p, begin, end, mode);
   else
-    k_volume<DIM, NS><<<(n + threads - 1) / threads, threads, 0, stream>>>(p, begin, end, mode);
+    k_volume<DIM, NS, double><<<(n + threads - 1) / threads, threads, 0, stream>>>(p, begin, end, mode);
 }
 
 }  // namespace

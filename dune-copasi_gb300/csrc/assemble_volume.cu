@@ -198,9 +198,13 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
     for (int j = 0; j < DIM; ++j) Bm[i][j] = X[j + 1][i] - X[0][i];
   F Bi[DIM][DIM];
   F det;
+  // the inverse (basis gradients) only when a gradient, a flux or the Jacobian needs it: a
+  // reaction-only residual pass needs |det| alone, and the FP64 division is the dearest
+  // operation of the geometry (uniform branch)
+  const bool need_inv = P.need_grad || P.has_flux || ((mode & 2) && P.J);
   if constexpr (DIM == 2) {
     det = Bm[0][0] * Bm[1][1] - Bm[0][1] * Bm[1][0];
-    const F id = F(1) / det;
+    const F id = need_inv ? F(1) / det : F(0);
     Bi[0][0] = Bm[1][1] * id;  Bi[0][1] = -Bm[0][1] * id;
     Bi[1][0] = -Bm[1][0] * id; Bi[1][1] = Bm[0][0] * id;
   } else {
@@ -208,7 +212,7 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
     const F c01 = Bm[1][2] * Bm[2][0] - Bm[1][0] * Bm[2][2];
     const F c02 = Bm[1][0] * Bm[2][1] - Bm[1][1] * Bm[2][0];
     det = Bm[0][0] * c00 + Bm[0][1] * c01 + Bm[0][2] * c02;
-    const F id = F(1) / det;
+    const F id = need_inv ? F(1) / det : F(0);
     Bi[0][0] = c00 * id;
     Bi[1][0] = c01 * id;
     Bi[2][0] = c02 * id;

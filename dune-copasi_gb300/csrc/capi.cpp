@@ -455,6 +455,15 @@ int dc_stream_handle(const dc_model* model, void** stream) {
 
 int64_t dc_launch_count(void) { return dcgpu::launch_count(); }
 
+int dc_selftest_barrier_timeout(double* gave_up_blocks, double* elapsed_ms) {
+  return guarded([&] {
+    if (!gave_up_blocks || !elapsed_ms) throw std::invalid_argument("null argument");
+    if (dcgpu::barrier_selftest(gave_up_blocks, elapsed_ms) != 0)
+      throw std::runtime_error("barrier self-test: CUDA error");
+    return DC_OK;
+  });
+}
+
 int dc_profile_enable(dc_model* model, int enabled) {
   return guarded([&] {
     if (!model) throw std::invalid_argument("null argument");

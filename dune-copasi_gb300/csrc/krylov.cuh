@@ -83,6 +83,10 @@ inline int64_t fused_bicgstab_partials(int blocks) { return 5 * static_cast<int6
 // resets the barrier words and the fault flag, then launches the solve on `s`
 template <class T, class V>
 void fused_bicgstab(int bs, bool sell, int blocks, const FusedBicgArgs<T, V>& a, cudaStream_t s);
+// Runs one grid-wide barrier that cannot complete (4 blocks, 50 ms limit): every block's wait
+// must give up and flag it.  Returns non-zero on a CUDA error; gave_up_blocks receives the
+// number of blocks that flagged, elapsed_ms the kernel's duration.
+int barrier_selftest(double* gave_up_blocks, double* elapsed_ms);
 
 template <class T>
 struct KrylovVectors {

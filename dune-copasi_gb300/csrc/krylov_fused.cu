@@ -41,7 +41,8 @@ __device__ __forceinline__ unsigned long long global_ns() {
 // arrivals, bar[1] holds the generation.  The last block to arrive resets the counter and
 // publishes the next generation; the others poll it, for at most kBarrierTimeoutNs.
 // Returns false in every thread of the block when the wait gave up.
-__device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned& gen) {
+__device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned& gen,
+                                             unsigned long long timeout_ns = kBarrierTimeoutNs) {
   __shared__ int ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -55,7 +56,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned& gen) {
     } else {
       const unsigned long long t0 = global_ns();
       while (*reinterpret_cast<volatile unsigned*>(&bar[1]) != next) {
-        if (global_ns() - t0 > kBarrierTimeoutNs) {
+        if (global_ns() - t0 > timeout_ns) {
           good = 0;
           break;
         }
@@ -667,6 +668,14 @@ __global__ void __launch_bounds__(kFThreads, kFMinBlocksPerSm) k_bicgstab_single
   }
 }
 
+// Self-test of the bounded wait: one barrier whose arrival counter starts past the value
+// its last arrival would reach, so it can never complete; every block must give up after
+// timeout_ns, flag the fault and return.
+__global__ void k_barrier_selftest(unsigned* bar, double* flag, unsigned long long timeout_ns) {
+  unsigned gen = 0;
+  if (!grid_barrier(bar, gen, timeout_ns) && threadIdx.x == 0) atomicAdd(flag, 1.0);
+}
+
 template <class T, class V>
 const void* fused_kernel(int bs, bool sell) {
 #define DC_FK(B)                                                                                   \
@@ -725,6 +734,45 @@ void fused_bicgstab(int bs, bool sell, int blocks, const FusedBicgArgs<T, V>& a,
   if (e != cudaSuccess)
     throw std::runtime_error(std::string("fused BiCGSTAB launch failed: ") + cudaGetErrorString(e));
   count_launches(1);
+}
+
+int barrier_selftest(double* gave_up_blocks, double* elapsed_ms) {
+  constexpr int kBlocks = 4;
+  constexpr unsigned long long kTimeoutNs = 50000000ull;  // 50 ms
+  unsigned* bar = nullptr;
+  double* flag = nullptr;
+  if (cudaMalloc(&bar, 2 * sizeof(unsigned)) != cudaSuccess) return 1;
+  if (cudaMalloc(&flag, sizeof(double)) != cudaSuccess) {
+    cudaFree(bar);
+    return 1;
+  }
+  // counter far past kBlocks - 1: no arrival ever sees the last-arrival value
+  const unsigned init[2] = {1000u, 0u};
+  cudaMemcpy(bar, init, sizeof init, cudaMemcpyHostToDevice);
+  cudaMemset(flag, 0, sizeof(double));
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  unsigned long long t = kTimeoutNs;
+  void* args[] = {&bar, &flag, &t};
+  cudaEventRecord(a);
+  cudaError_t e = cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(&k_barrier_selftest), dim3(kBlocks),
+                                              dim3(32), args, 0, nullptr);
+  cudaEventRecord(b);
+  if (e == cudaSuccess) e = cudaEventSynchronize(b);
+  float ms = 0.0f;
+  if (e == cudaSuccess) cudaEventElapsedTime(&ms, a, b);
+  double h = 0.0;
+  if (e == cudaSuccess) e = cudaMemcpy(&h, flag, sizeof(double), cudaMemcpyDeviceToHost);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(bar);
+  cudaFree(flag);
+  if (e != cudaSuccess) return 1;
+  count_launches(1);
+  *gave_up_blocks = h;
+  *elapsed_ms = ms;
+  return 0;
 }
 
 template bool fused_bicgstab_plan<float, float>(int, bool, int, int*, int*, int*);

@@ -35,6 +35,7 @@ EXPORTED = [
     "dc_assemble_residual_noalloc", "dc_server_create", "dc_server_submit", "dc_server_poll",
     "dc_server_take_state", "dc_server_estimate", "dc_server_destroy", "dc_last_error",
     "dc_spmv_format", "dc_vertex_coords", "dc_constraints", "dc_reduce", "dc_write_vtk", "dc_config_get",
+    "dc_selftest_barrier_timeout",
 ]
 
 
@@ -130,6 +131,7 @@ def load_library(path=LIB_PATH):
     lib.dc_reduce.argtypes = [vp, ctypes.c_char_p, P(ReduceValue), sz, P(sz)]
     lib.dc_write_vtk.argtypes = [vp, ctypes.c_char_p, ctypes.c_int]
     lib.dc_config_get.argtypes = [vp, ctypes.c_char_p, ctypes.c_char_p, sz]
+    lib.dc_selftest_barrier_timeout.argtypes = [pd, pd]
     lib.dc_last_error.argtypes = []
     lib.dc_last_error.restype = ctypes.c_char_p
     for name in EXPORTED:
@@ -453,6 +455,16 @@ class Model:
 
 def launch_count():
     return int(load_library().dc_launch_count())
+
+
+def selftest_barrier_timeout():
+    """Runs one grid-wide barrier that cannot complete (4 cooperative blocks, 50 ms limit)
+    and returns (blocks whose wait gave up, kernel milliseconds)."""
+    lib = load_library()
+    gave = ctypes.c_double(0.0)
+    ms = ctypes.c_double(0.0)
+    _check(lib.dc_selftest_barrier_timeout(ctypes.byref(gave), ctypes.byref(ms)))
+    return gave.value, ms.value
 
 
 def estimate_bytes(ini, overrides=None):

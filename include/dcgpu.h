@@ -153,6 +153,12 @@ int dc_expr_eval(const char* expression, const char* context_ini, const char* co
  * whose call count is the number of Krylov iterations they ran) while profiling is enabled. */
 int dc_stream_handle(const dc_model* model, void** stream);
 int64_t dc_launch_count(void);
+
+/* Self-test of the bounded device waits (no reference counterpart): runs one grid-wide
+ * barrier of the single-launch solve's kind that cannot complete (4 cooperative blocks, 50 ms
+ * limit).  Every block's wait must give up and flag it; *gave_up_blocks receives how many did
+ * and *elapsed_ms the kernel's duration.  The CUDA context stays usable afterwards. */
+int dc_selftest_barrier_timeout(double* gave_up_blocks, double* elapsed_ms);
 int dc_profile_enable(dc_model* model, int enabled);
 int dc_profile_get(const dc_model* model, double* ms, int64_t* calls, int32_t n_categories);
 

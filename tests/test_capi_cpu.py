@@ -95,3 +95,112 @@ def test_nested_user_function_rejected(dcgpu_lib):
     ctx = "[parser_context.f]\ntype=function\nexpression=x: x\n[parser_context.g]\ntype=function\nexpression=x: f(x)\n"
     with pytest.raises(dcgpu_lib.DcError):
         dcgpu_lib.expr_eval("g(1)", {}, ctx)
+
+
+# ------------------------------------------------------------------ parser-context extras
+
+def _tiff_context(path, name="img"):
+    return "[parser_context.%s]\ntype = tiff\npath = %s\n" % (name, path)
+
+
+@pytest.mark.parametrize("bits,photometric,big_endian,compression,predictor", [
+    (8, 1, False, "none", False), (16, 0, True, "lzw", True), (32, 1, True, "packbits", False),
+    (16, 1, False, "lzw", False), (8, 0, False, "lzw", True)])
+def test_engine_tiff_matches_oracle(dcgpu_lib, tmp_path, bits, photometric, big_endian, compression, predictor):
+    """The engine's TIFF reader and position lookup against the oracle's, bit for bit, over
+    positions inside, on the edges of and outside the image."""
+    import tiff_files as TF
+    from oracle.tiff import TiffImage
+    path = str(tmp_path / "im.tif")
+    v = TF.seeded_image(23, 37, bits, seed=bits)
+    TF.write_tiff(path, v, bits=bits, photometric=photometric, big_endian=big_endian, compression=compression,
+                  predictor=predictor, resolution=(37, 1), position=(1, 8), rows_per_strip=6)
+    im = TiffImage(path)
+    ctx = _tiff_context(path)
+    rng = np.random.default_rng(bits)
+    pts = list(rng.uniform(-0.3, 1.5, size=(60, 2))) + [(0.125, 0.125), (1.125, 0.75), (0.5, 1.0 / 37 + 0.125)]
+    for x, y in pts:
+        got = dcgpu_lib.expr_eval("img(x, y)", {"x": x, "y": y}, ctx)
+        assert got == float(im(x, y)), (x, y)
+
+
+def test_engine_tiff_errors(dcgpu_lib, tmp_path):
+    import tiff_files as TF
+    p4 = str(tmp_path / "four.tif")
+    TF.write_tiff(p4, np.full((3, 4), 5, dtype=np.uint64), bits=4)
+    rgb = str(tmp_path / "rgb.tif")
+    TF.write_tiff(rgb, np.ones((3, 3), dtype=np.uint64), photometric=2)
+    nores = str(tmp_path / "nores.tif")
+    TF.write_tiff(nores, np.ones((3, 3), dtype=np.uint64), res_tags=False)
+    for path, msg in [(p4, "Encoding with 4 bits not implemented"), (rgb, "must be in grayscale"),
+                      (nores, "negative resolution"), (str(tmp_path / "none.tif"), "does not exists")]:
+        with pytest.raises(dcgpu_lib.DcError) as ei:
+            dcgpu_lib.expr_eval("img(0.5, 0.5)", {}, _tiff_context(path))
+        assert ei.value.status == 4 and msg in str(ei.value)
+
+
+TABULATED = """
+[parser_context.k]
+type = constant
+value = 3
+[parser_context.ramp]
+type = interpolation
+domain = 0 0.5 2
+range = 1 2 0
+[parser_context.f]
+type = function
+expression = s: k*sin(s) + ramp(s)
+interpolate = true
+interpolation.intervals = 37
+interpolation.domain.s = -0.5 2
+interpolation.out_of_bounds = %s
+"""
+
+
+@pytest.mark.parametrize("mode", ["clamp", "error"])
+def test_engine_tabulated_function_matches_oracle(dcgpu_lib, mode):
+    """interpolate = true: the grid values agree with the oracle's to rounding, and the
+    lookup picks the same grid value (the reference's left-endpoint step) everywhere."""
+    text = TABULATED % mode
+    ctx = E.Context(ParameterTree.from_text(text).sub("parser_context"))
+    f = ctx.functions["f"]
+    xs = list(np.linspace(-0.5, 2.0, 38)) + list(np.random.default_rng(3).uniform(-1.0, 2.5, 80)) + [float("nan")]
+    for x in xs:
+        ref = float(E.Expression("f(x)", ctx)({"x": np.array(x)}))
+        got = dcgpu_lib.expr_eval("f(x)", {"x": x}, text)
+        if math.isnan(ref):
+            assert math.isnan(got), x
+        else:
+            assert got == pytest.approx(ref, rel=1e-14, abs=1e-15), x
+    assert f.n == 37
+
+
+@pytest.mark.parametrize("edit,msg", [
+    (("interpolation.intervals = 37", "interpolation.intervals = 100001"), "too big"),
+    (("interpolation.intervals = 37", "interpolation.intervals = 0"), "At least one interval"),
+    (("interpolation.domain.s = -0.5 2", "interpolation.domain.s = 2 -0.5"), "not ordered"),
+    (("expression = s: k*sin(s) + ramp(s)", "expression = s, t: s*t"), "Cannot interpolate"),
+])
+def test_engine_tabulated_function_config_errors(dcgpu_lib, edit, msg):
+    with pytest.raises(dcgpu_lib.DcError) as ei:
+        dcgpu_lib.expr_eval("f(0.5)", {}, (TABULATED % "clamp").replace(*edit))
+    assert ei.value.status == 4 and msg in str(ei.value)
+
+
+def test_engine_interpolation_is_exact_lerp(dcgpu_lib):
+    """Interpolation tables: std::lower_bound and std::lerp, the same bits as the oracle's
+    restatement, at the nodes, between them, outside and for NaN."""
+    text = "[parser_context.tab]\ntype = interpolation\ndomain = -1 0 0 0.5 2\nrange = 3 -1 2 4 -2\n"
+    ctx = E.Context(ParameterTree.from_text(text).sub("parser_context"))
+    for x in [-2.0, -1.0, -0.3, 0.0, 1e-17, 0.25, 0.5, 0.9999, 2.0, 7.0, float("nan")]:
+        ref = float(ctx.functions["tab"](np.array(x)))
+        got = dcgpu_lib.expr_eval("tab(x)", {"x": x}, text)
+        assert got == ref, x
+
+
+@pytest.mark.parametrize("typ,msg", [("random_field", "random fields"), ("cell_data", "cell data"),
+                                     ("wavelet", "Unknown type")])
+def test_engine_unsupported_context_types(dcgpu_lib, typ, msg):
+    with pytest.raises(dcgpu_lib.DcError) as ei:
+        dcgpu_lib.expr_eval("1", {}, "[parser_context.q]\ntype = %s\n" % typ)
+    assert ei.value.status == 4 and msg in str(ei.value)

@@ -17,31 +17,69 @@ namespace {
 template <int DIM> struct Rule;
 template <> struct Rule<2> {
   static constexpr int NQ = 3;
-  __device__ static constexpr double xi(int q, int k) {
+  __host__ __device__ static constexpr double xi(int q, int k) {
     return (q == 0) ? (k == 0 ? 2.0 / 3.0 : 1.0 / 6.0)
          : (q == 1) ? (k == 0 ? 1.0 / 6.0 : 2.0 / 3.0)
                     : 1.0 / 6.0;
   }
-  __device__ static constexpr double w(int) { return 1.0 / 6.0; }
+  __host__ __device__ static constexpr double w(int) { return 1.0 / 6.0; }
 };
 template <> struct Rule<3> {
   static constexpr int NQ = 4;
-  __device__ static constexpr double xi(int q, int k) {
+  __host__ __device__ static constexpr double xi(int q, int k) {
     // q = 0: (b,b,b); q = 1..3: a in coordinate q-1
     return (q == k + 1) ? 0.5854101966249685 : 0.1381966011250105;
   }
-  __device__ static constexpr double w(int) { return 1.0 / 24.0; }
+  __host__ __device__ static constexpr double w(int) { return 1.0 / 24.0; }
 };
 
+template <int DIM> struct MassConst;
+
+// P1 basis function a at point q: 1 - (xi_0 + ... ) for a = 0 and xi_{a-1} otherwise, the
+// sum formed left to right as the oracle's numpy sum does, so the partition of unity has the
+// same bits on both sides (a table of a step function of the state, evaluated at a
+// quadrature point on a step, then picks the same step).  The point loop is not unrolled,
+// so the values come from constant tables formed at compile time rather than from FP64
+// arithmetic per point.
+template <int DIM>
+__host__ __device__ constexpr double phi_value(int q, int a) {
+  if (a > 0) return Rule<DIM>::xi(q, a - 1);
+  double s = 0.0;
+  for (int k = 0; k < DIM; ++k) s += Rule<DIM>::xi(q, k);
+  return 1.0 - s;
+}
+template <int DIM, class F>
+struct PhiTable {
+  F v[Rule<DIM>::NQ][DIM + 1];
+};
+template <int DIM, class F>
+constexpr PhiTable<DIM, F> make_phi_table() {
+  PhiTable<DIM, F> t{};
+  for (int q = 0; q < Rule<DIM>::NQ; ++q)
+    for (int a = 0; a <= DIM; ++a) t.v[q][a] = static_cast<F>(phi_value<DIM>(q, a));
+  return t;
+}
+__constant__ PhiTable<2, double> c_phi2d = make_phi_table<2, double>();
+__constant__ PhiTable<3, double> c_phi3d = make_phi_table<3, double>();
+__constant__ PhiTable<2, float> c_phi2f = make_phi_table<2, float>();
+__constant__ PhiTable<3, float> c_phi3f = make_phi_table<3, float>();
+
+template <int DIM, class F>
+__device__ __forceinline__ F phi_t(int q, int a) {
+  if constexpr (std::is_same_v<F, double>) return DIM == 2 ? c_phi2d.v[q][a] : c_phi3d.v[q][a];
+  else return DIM == 2 ? c_phi2f.v[q][a] : c_phi3f.v[q][a];
+}
 template <int DIM>
 __device__ __forceinline__ double phi(int q, int a) {
-  if (a == 0) {
-    double s = 1.0;
-#pragma unroll
-    for (int k = 0; k < DIM; ++k) s -= Rule<DIM>::xi(q, k);
-    return s;
-  }
-  return Rule<DIM>::xi(q, a - 1);
+  return phi_t<DIM, double>(q, a);
+}
+// reference coordinate k of point q in the arithmetic type F
+template <int DIM, class F>
+__device__ __forceinline__ F xi_t(int q, int k) {
+  constexpr F al = static_cast<F>(MassConst<DIM>::alpha), be = static_cast<F>(MassConst<DIM>::beta);
+  // the point's vertex in 0..DIM; reference coordinate k belongs to vertex k + 1
+  const int vq = DIM == 2 ? (q == 2 ? 0 : q + 1) : q;
+  return vq == k + 1 ? al : be;
 }
 
 // Both rules have one point per vertex: point q carries the large barycentric weight
@@ -287,7 +325,7 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
     for (int s = 0; s < NS; ++s) {
       F acc = 0.0;
 #pragma unroll
-      for (int a = 0; a < NL; ++a) acc += c[a][s] * F(phi<DIM>(q, a));
+      for (int a = 0; a < NL; ++a) acc += c[a][s] * phi_t<DIM, F>(q, a);
       u[s] = acc;
     }
     F xq[DIM];
@@ -296,11 +334,11 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
       F acc = X[0][i];
       if (P.need_pos) {
 #pragma unroll
-        for (int j = 0; j < DIM; ++j) acc += Bm[i][j] * F(Rule<DIM>::xi(q, j));
+        for (int j = 0; j < DIM; ++j) acc += Bm[i][j] * xi_t<DIM, F>(q, j);
       }
       xq[i] = acc;
     }
-    const F fq = F(Rule<DIM>::w(q)) * adet;
+    const F fq = static_cast<F>(Rule<DIM>::w(0)) * adet;
     for (int i = 0; i < P.prog.ninputs; ++i)
       R[i] = volume_input<DIM, NS, F>(P.prog.inputs[i], u, g, xq, F(P.t), vol, P.species_offset);
     run_program(P.prog, P.tables, R);
@@ -371,7 +409,7 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
       for (int s = 0; s < NS; ++s) ts[s] = scal[s] * fq;
 #pragma unroll
       for (int a = 0; a < NL; ++a) {
-        const F pa = F(phi<DIM>(q, a));
+        const F pa = phi_t<DIM, F>(q, a);
 #pragma unroll
         for (int s = 0; s < NS; ++s) rl[a][s] = fma(ts[s], pa, rl[a][s]);
       }
@@ -446,7 +484,7 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
             }
 #pragma unroll
             for (int a = 0; a < NL; ++a) {
-              const F pa = F(phi<DIM>(q, a)) * sc;
+              const F pa = phi_t<DIM, F>(q, a) * sc;
 #pragma unroll
               for (int j = 0; j < DIM; ++j) coef[T.coef + a * DIM + j] += pa * vec[j];
             }

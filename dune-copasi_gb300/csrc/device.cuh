@@ -12,6 +12,7 @@ namespace dcgpu {
 struct DevProgram {
   const Instr* code = nullptr;
   const double* consts = nullptr;
+  const float* consts32 = nullptr;  // the same constants rounded to FP32 (FP32 interpreter)
   const uint16_t* inputs = nullptr;
   const uint8_t* outputs = nullptr;
   int ncode = 0, ninputs = 0, noutputs = 0, nregs = 0;

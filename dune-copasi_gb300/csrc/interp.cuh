@@ -7,6 +7,8 @@
 
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "device.cuh"
 
 namespace dcgpu {
@@ -96,7 +98,10 @@ __device__ __forceinline__ void run_program(const DevProgram& P, const DevTables
     const Instr ins = P.code[pc];
     F v;
     if (ins.op == OP_CONST) {
-      v = static_cast<F>(P.consts[ins.a | (ins.b << 8)]);
+      // FP32 programs read the constants pre-rounded: a double-to-float conversion per use
+      // runs on the FP64 pipe
+      if constexpr (std::is_same_v<F, float>) v = P.consts32[ins.a | (ins.b << 8)];
+      else v = P.consts[ins.a | (ins.b << 8)];
     } else {
       const F a = R[ins.a];
       const bool table = ins.op == OP_INTERP || ins.op == OP_FTAB || ins.op == OP_TIFF;

@@ -19,6 +19,7 @@ DevProgram ProgramBundle::view() const {
   DevProgram p;
   p.code = code.get();
   p.consts = consts.get();
+  p.consts32 = consts32.get();
   p.inputs = inputs.get();
   p.outputs = outputs.get();
   p.ncode = static_cast<int>(host.code.size());
@@ -32,6 +33,7 @@ void ProgramBundle::upload() {
   if (host.nregs > kMaxDevRegisters) throw ConfigError("expression program needs too many registers");
   code.upload(host.code);
   consts.upload(host.consts);
+  consts32.upload(std::vector<float>(host.consts.begin(), host.consts.end()));
   inputs.upload(host.inputs);
   outputs.upload(host.outputs);
 }

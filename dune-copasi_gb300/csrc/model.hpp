@@ -93,6 +93,7 @@ struct ProgramBundle {
   Program host;
   DeviceBuffer<Instr> code;
   DeviceBuffer<double> consts;
+  DeviceBuffer<float> consts32;
   DeviceBuffer<uint16_t> inputs;
   DeviceBuffer<uint8_t> outputs;
   DevProgram view() const;

@@ -144,6 +144,14 @@ void Server::worker() {
     try {
       cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
       Model model(req.ini, req.overrides);
+      // Concurrent simulations solve with graph-replayed per-phase launches unless their
+      // configuration asks otherwise: a single-launch solve holds whole SMs (its blocks use
+      // the full register file) through its barrier waits, which starves the kernels of the
+      // other simulations' streams (32-request serving mix: 21.3 M against 29.3 M
+      // DOF·Newton-steps/s).  Every request of a server takes the same path, so results do
+      // not depend on what else runs.
+      const std::string sl_key = "model.time_step_operator.linear_solver.single_launch";
+      if (!model.cfg.has_key(sl_key)) model.cfg.set(sl_key, "false");
       Solver solver(model, stream);
       Ini tso = model.cfg.sub("model").sub("time_step_operator");
       const double t0 = tso.get_double("time_begin", 0.0);

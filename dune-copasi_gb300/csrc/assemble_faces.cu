@@ -187,7 +187,7 @@ __global__ void __launch_bounds__(128) k_faces(const FaceParams P, const int beg
         }
         R[i] = v;
       }
-      run_program(P.prog[side], P.tables, R);
+      run_program<double>(P.prog[side], P.tables, R);
       const uint8_t* out = P.prog[side].outputs;
       for (int t = 0; t < nt; ++t) {
         const Term T = terms[t];

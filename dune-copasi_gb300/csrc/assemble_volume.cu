@@ -143,8 +143,8 @@ __device__ __forceinline__ F volume_input(uint16_t id, const F (&u)[NS], const F
 // the terms (sorted by slot) are summed per slot and each slot stored once.  With only
 // mass-type terms the element matrix is symmetric and only a <= b is evaluated.  JT is the
 // arithmetic and storage type (fp64, or fp32 for the mixed-precision path).
-template <int DIM, class JT>
-__device__ __forceinline__ void element_jacobian(const VolumeParams& P, const JT* coef, const JT (&G)[DIM + 1][DIM],
+template <int DIM, class JT, class Coef>
+__device__ __forceinline__ void element_jacobian(const VolumeParams& P, Coef coef, const JT (&G)[DIM + 1][DIM],
                                                  JT* ej) {
   constexpr int NL = DIM + 1;
   constexpr int NQ = Rule<DIM>::NQ;
@@ -243,14 +243,17 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
   if constexpr (DIM == 2) {
     det = Bm[0][0] * Bm[1][1] - Bm[0][1] * Bm[1][0];
     const F id = need_inv ? F(1) / det : F(0);
-    Bi[0][0] = Bm[1][1] * id;  Bi[0][1] = -Bm[0][1] * id;
-    Bi[1][0] = -Bm[1][0] * id; Bi[1][1] = Bm[0][0] * id;
+    if (need_inv) {
+      Bi[0][0] = Bm[1][1] * id;  Bi[0][1] = -Bm[0][1] * id;
+      Bi[1][0] = -Bm[1][0] * id; Bi[1][1] = Bm[0][0] * id;
+    }
   } else {
     const F c00 = Bm[1][1] * Bm[2][2] - Bm[1][2] * Bm[2][1];
     const F c01 = Bm[1][2] * Bm[2][0] - Bm[1][0] * Bm[2][2];
     const F c02 = Bm[1][0] * Bm[2][1] - Bm[1][1] * Bm[2][0];
     det = Bm[0][0] * c00 + Bm[0][1] * c01 + Bm[0][2] * c02;
     const F id = need_inv ? F(1) / det : F(0);
+    if (need_inv) {
     Bi[0][0] = c00 * id;
     Bi[1][0] = c01 * id;
     Bi[2][0] = c02 * id;
@@ -260,17 +263,19 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
     Bi[0][2] = (Bm[0][1] * Bm[1][2] - Bm[0][2] * Bm[1][1]) * id;
     Bi[1][2] = (Bm[0][2] * Bm[1][0] - Bm[0][0] * Bm[1][2]) * id;
     Bi[2][2] = (Bm[0][0] * Bm[1][1] - Bm[0][1] * Bm[1][0]) * id;
+    }
   }
   const F adet = fabs(det);
-  const F vol = adet / F(DIM == 2 ? 2 : 6);
+  // the element volume only for programs that read entity_volume (an FP64 division)
+  const F vol = P.need_vol ? adet / F(DIM == 2 ? 2 : 6) : F(0);
   F G[NL][DIM];
 #pragma unroll
   for (int j = 0; j < DIM; ++j) {
     F s = 0.0;
 #pragma unroll
     for (int kk = 0; kk < DIM; ++kk) {
-      G[kk + 1][j] = Bi[kk][j];
-      s += Bi[kk][j];
+      G[kk + 1][j] = need_inv ? Bi[kk][j] : F(0);
+      s += G[kk + 1][j];
     }
     G[0][j] = -s;
   }
@@ -302,7 +307,13 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
   for (int a = 0; a < NL; ++a)
 #pragma unroll
     for (int s = 0; s < NS; ++s) rl[a][s] = 0.0;
-  F coef[kMaxCoefficients];
+  // interpreter registers and Jacobian coefficients: per-thread slices of dynamic shared
+  // memory (sized by the launcher from the program's registers and the term list)
+  extern __shared__ __align__(16) unsigned char volume_smem[];
+  F* const smem = reinterpret_cast<F*>(volume_smem);
+  const Strided<F> R{smem + threadIdx.x, static_cast<int>(blockDim.x)};
+  const Strided<F> coef{smem + static_cast<int64_t>(P.prog.nregs) * blockDim.x + threadIdx.x,
+                        static_cast<int>(blockDim.x)};
   int ncoef = 0;
   if (do_jac) {
     for (int t = 0; t < P.n_jac_terms; ++t) {
@@ -316,8 +327,6 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
     }
     for (int i = 0; i < ncoef; ++i) coef[i] = 0.0;
   }
-  F R[kMaxDevRegisters];
-
 #pragma unroll 1
   for (int q = 0; q < NQ; ++q) {
     F u[NS];
@@ -341,7 +350,7 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
     const F fq = static_cast<F>(Rule<DIM>::w(0)) * adet;
     for (int i = 0; i < P.prog.ninputs; ++i)
       R[i] = volume_input<DIM, NS, F>(P.prog.inputs[i], u, g, xq, F(P.t), vol, P.species_offset);
-    run_program(P.prog, P.tables, R);
+    run_program<F>(P.prog, P.tables, R);
     const uint8_t* out = P.prog.outputs;
 
     if (do_res) {
@@ -397,8 +406,10 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
         for (int s = 0; s < NS; ++s) {
           if (s == T.test) {
             scal[s] += sc * ds;
+            if (P.has_flux) {
 #pragma unroll
-            for (int j = 0; j < DIM; ++j) flux[s][j] += sc * df[j];
+              for (int j = 0; j < DIM; ++j) flux[s][j] += sc * df[j];
+            }
           }
         }
       }
@@ -524,8 +535,7 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
     } else if (P.jac_f32) {
       // mixed precision, computed alongside the fp64 residual: the element Jacobian in fp32
       // (the fp32 Krylov operator is built from it; the residual stays fp64)
-      float cf[kMaxCoefficients];
-      for (int i = 0; i < ncoef; ++i) cf[i] = static_cast<float>(coef[i]);
+      const StridedCast<F, float> cf{coef.p, coef.stride};
       float Gf[NL][DIM];
 #pragma unroll
       for (int a = 0; a < NL; ++a)
@@ -609,7 +619,7 @@ __device__ void fd_local_residual(const VolumeParams& P, const double (&c)[DIM +
     const double fq = Rule<DIM>::w(q) * adet;
     for (int i = 0; i < P.prog.ninputs; ++i)
       R[i] = volume_input<DIM, NS>(P.prog.inputs[i], u, g, xq, P.t, vol, P.species_offset);
-    run_program(P.prog, P.tables, R);
+    run_program<double>(P.prog, P.tables, R);
     const uint8_t* out = P.prog.outputs;
     double scal[NS], flux[NS][DIM];
 #pragma unroll
@@ -771,6 +781,27 @@ __global__ void __launch_bounds__(128) k_volume_fd(const VolumeParams P, const i
   }
 }
 
+// k_volume with its shared-memory register file and coefficients: 128 threads per block,
+// fewer when a large program would need more than kVolumeSmemCap bytes per block
+constexpr int kVolumeSmemCap = 160 * 1024;
+template <int DIM, int NS, class F>
+void launch_volume_kernel(const VolumeParams& p, int begin, int end, int mode, cudaStream_t stream) {
+  const int n = end - begin;
+  const int64_t per_thread = static_cast<int64_t>(p.prog.nregs + p.ncoef) * static_cast<int64_t>(sizeof(F));
+  int threads = 128;
+  while (threads > 32 && per_thread * threads > kVolumeSmemCap) threads /= 2;
+  const size_t smem = static_cast<size_t>(per_thread * threads);
+  // once per instantiation (thread-safe static initialisation)
+  static const bool attr_set = [] {
+    if (cudaFuncSetAttribute(k_volume<DIM, NS, F>, cudaFuncAttributeMaxDynamicSharedMemorySize, kVolumeSmemCap) !=
+        cudaSuccess)
+      throw std::runtime_error("k_volume: cannot raise the shared-memory limit");
+    return true;
+  }();
+  (void)attr_set;
+  k_volume<DIM, NS, F><<<(n + threads - 1) / threads, threads, smem, stream>>>(p, begin, end, mode);
+}
+
 template <int DIM, int NS>
 void launch_t(const VolumeParams& p, int begin, int end, int mode, cudaStream_t stream) {
   const int n = end - begin;
@@ -780,9 +811,9 @@ void launch_t(const VolumeParams& p, int begin, int end, int mode, cudaStream_t 
   if (mode == kVolumeNumericalJacobian)
     k_volume_fd<DIM, NS><<<(n + threads - 1) / threads, threads, 0, stream>>>(p, begin, end);
   else if (mode == 2 && p.jac_f32)
-    k_volume<DIM, NS, float><<<(n + threads - 1) / threads, threads, 0, stream>>>(p, begin, end, mode);
+    launch_volume_kernel<DIM, NS, float>(p, begin, end, mode, stream);
   else
-    k_volume<DIM, NS, double><<<(n + threads - 1) / threads, threads, 0, stream>>>(p, begin, end, mode);
+    launch_volume_kernel<DIM, NS, double>(p, begin, end, mode, stream);
 }
 
 }  // namespace

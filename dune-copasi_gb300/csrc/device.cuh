@@ -97,6 +97,26 @@ struct VolumeParams {
   int need_pos;              // a program reads position_*
   int need_grad;             // a program reads a gradient or a term takes one
   int has_flux;              // a residual term contributes a flux (velocity / diffusion)
+  int need_vol;              // a program reads entity_volume
+  int ncoef;                 // Jacobian coefficients per element of the jac_terms (0 without)
+};
+
+// A thread's slice of a block-wide shared-memory array: element i at p[i * stride] (stride =
+// block size, so the threads of a warp touch consecutive words).  The volume kernel keeps
+// the interpreter's register file and the element's Jacobian coefficients there: indexed
+// at run time, as local arrays they lived in local memory and spilled to L2 and DRAM.
+template <class F>
+struct Strided {
+  F* p;
+  int stride;
+  __device__ __forceinline__ F& operator[](int i) const { return p[i * stride]; }
+};
+// the same array read through a conversion to U (fp64 coefficients of an fp32 element matrix)
+template <class F, class U>
+struct StridedCast {
+  const F* p;
+  int stride;
+  __device__ __forceinline__ U operator[](int i) const { return static_cast<U>(p[i * stride]); }
 };
 
 struct FaceParams {

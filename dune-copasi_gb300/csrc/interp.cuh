@@ -92,8 +92,8 @@ __device__ __forceinline__ F apply_op(const Instr ins, F a, F b, F c, const DevT
 
 // Run a program; inputs must already be in R[0..ninputs).  All threads of a warp run the
 // same instruction stream, so the dispatch is uniform.
-template <class F>
-__device__ __forceinline__ void run_program(const DevProgram& P, const DevTables& T, F* R) {
+template <class F, class Regs>
+__device__ __forceinline__ void run_program(const DevProgram& P, const DevTables& T, Regs R) {
   for (int pc = 0; pc < P.ncode; ++pc) {
     const Instr ins = P.code[pc];
     F v;

@@ -122,11 +122,24 @@ Model::Model(const std::string& ini_text, const std::string& overrides) {
   build_constraints();
 }
 
-// uniform skip flags of the volume kernel for one program and its term lists
+// uniform skip flags of the volume kernel for one program and its term lists, and the
+// number of per-element Jacobian coefficients of the terms (k_volume's shared-memory size:
+// NQ point weights + one for mass-type terms, 1 for scalar diffusion, dim^2 for tensor
+// diffusion, (dim + 1) dim for the vector terms)
 static void set_volume_flags(VolumeParams& p, const Program& prog, const std::vector<Term>& res,
-                             const std::vector<Term>& jac) {
-  p.need_pos = p.need_grad = p.has_flux = 0;
+                             const std::vector<Term>& jac, int dim) {
+  const int nq = dim == 2 ? 3 : 4;
+  p.ncoef = 0;
+  for (const Term& T : jac) {
+    const int sz = (T.kind == J_MASS || T.kind == J_MASS_U || T.kind == J_STORAGE_SELF) ? nq + 1
+                   : T.kind == J_DIFF_SCALAR                                             ? 1
+                   : T.kind == J_DIFF_TENSOR                                             ? dim * dim
+                                                                                         : (dim + 1) * dim;
+    p.ncoef = std::max(p.ncoef, static_cast<int>(T.coef) + sz);
+  }
+  p.need_pos = p.need_grad = p.has_flux = p.need_vol = 0;
   for (uint16_t id : prog.inputs) {
+    if (id == IN_ENTITY_VOLUME) p.need_vol = 1;
     if (id >= IN_POSITION && id < IN_NORMAL) p.need_pos = 1;
     if (id >= IN_GRAD && id < IN_POSITION) p.need_grad = 1;
   }
@@ -175,7 +188,7 @@ void Model::build_static_matrices() {
     p.ej = d_ej.get();
     p.n_slots = g.slots_static;
     p.all_mass = g.static_all_mass ? 1 : 0;
-    set_volume_flags(p, g.prog_static.host, {}, g.static_terms);
+    set_volume_flags(p, g.prog_static.host, {}, g.static_terms, dim);
     for (int form = 0; form < 2; ++form) {
       if ((form == 0 && !g.static_mass) || (form == 1 && !g.static_stiffness)) continue;
       double* target = form == 0 ? d_Ms.get() : d_Ks.get();
@@ -1172,8 +1185,8 @@ void Model::assemble(const double* x, double t, double cm, double ca, double* r,
     p.n_slots = g.slots_dyn;
     p.all_mass = g.dyn_all_mass ? 1 : 0;
     p.jac_f32 = jac_f32 ? 1 : 0;
-    if (jac) set_volume_flags(p, g.prog_all.host, g.res_terms_a, g.jac_terms);
-    else set_volume_flags(p, g.prog_res.host, g.res_terms_r, {});
+    if (jac) set_volume_flags(p, g.prog_all.host, g.res_terms_a, g.jac_terms, dim);
+    else set_volume_flags(p, g.prog_res.host, g.res_terms_r, {}, dim);
     const int ne = static_cast<int>(g.ne);
     if (numerical_jacobian && (mode & 2)) {
       // jacobian.type = numerical: residual pass (if asked) + finite-difference Jacobian pass
@@ -1181,7 +1194,7 @@ void Model::assemble(const double* x, double t, double cm, double ca, double* r,
       p.prog = g.prog_res.view();
       p.res_terms = g.d_res_r.get();
       p.n_res_terms = static_cast<int>(g.res_terms_r.size());
-      set_volume_flags(p, g.prog_res.host, g.res_terms_r, {});
+      set_volume_flags(p, g.prog_res.host, g.res_terms_r, {}, dim);
       if ((mode & 1) && r) {
         launch_volume(dim, g.ns, p, 0, ne, 1, s);
         launch_gather_residual(r, bs, g.ns, g.node_begin, g.nnodes, g.rlist_ptr.get(), g.rlist.get(), d_er.get(), s);

@@ -150,7 +150,7 @@ __global__ void __launch_bounds__(128) k_reduce_eval(const ReduceParams P) {
       }
       R[i] = v;
     }
-    run_program(P.prog, P.tables, R);
+    run_program<double>(P.prog, P.tables, R);
     for (int k = 0; k < P.nkeys; ++k) P.out[k * npts + e * NQ + q] = R[P.prog.outputs[k]];
   }
 }

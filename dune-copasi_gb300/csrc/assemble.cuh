@@ -25,10 +25,19 @@ void launch_faces(int dim, const FaceParams& p, int begin, int end, int mode, cu
 // VolumeParams), these gathers add them into r / J per node / block in list order
 void launch_gather_residual(double* r, int bs, int ns, int64_t node_begin, int64_t nnodes, const int64_t* ptr,
                             const int32_t* list, const double* er, cudaStream_t stream);
-// (f32: the element values are floats, summed in fp32)
+// (f32: the element values are floats, summed in fp32).  Optional fused outputs of a gather
+// that covers every entry of J: `overwrite` takes `base` (the static operator, or zero when
+// null) in place of J's old value, and `sell` receives each final value rounded to fp32 at
+// SELL-32 slot sell_bpos[block] (the mixed-precision operator copy, without a conversion pass).
+struct JacobianGatherOut {
+  int overwrite = 0;
+  const double* base = nullptr;
+  float* sell = nullptr;
+  const int64_t* sell_bpos = nullptr;
+};
 void launch_gather_jacobian(double* J, int bs, int nslot, const int32_t* slot_pos, int64_t block_begin,
                             int64_t nblocks, const int64_t* ptr, const int32_t* list, const double* ej, bool f32,
-                            cudaStream_t stream);
+                            cudaStream_t stream, const JacobianGatherOut& out = JacobianGatherOut{});
 // J[diag[i]] block gets identity in the padded slots s >= ns_of_row (rows of compartments
 // with fewer species than the block size)
 void launch_pad_identity(const int32_t* diag, const int8_t* row_ns, int nrows, int bs, double* J,

@@ -568,13 +568,19 @@ __global__ void k_gather_residual(double* __restrict__ r, int bs, unsigned ns, i
 template <class E>
 __global__ void k_gather_jacobian(double* __restrict__ J, int bs2, unsigned nslot, const int32_t* __restrict__ slot_pos,
                                   int64_t block_begin, unsigned ntotal, const int64_t* __restrict__ ptr,
-                                  const int32_t* __restrict__ list, const E* __restrict__ ej) {
+                                  const int32_t* __restrict__ list, const E* __restrict__ ej, const JacobianGatherOut o) {
   const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ntotal) return;
   const unsigned b = t / nslot, m = t - b * nslot;
   E acc = E(0);
   for (int64_t i = ptr[b]; i < ptr[b + 1]; ++i) acc += ej[static_cast<int64_t>(list[i]) * nslot + m];
-  J[(block_begin + b) * bs2 + slot_pos[m]] += static_cast<double>(acc);
+  const int64_t blk = block_begin + b;
+  const int64_t at = blk * bs2 + slot_pos[m];
+  // overwrite: this gather covers every entry of J, so the static operator (or zero) is its
+  // base and no separate copy of it into J runs
+  const double v = (o.overwrite ? (o.base ? o.base[at] : 0.0) : J[at]) + static_cast<double>(acc);
+  J[at] = v;
+  if (o.sell) o.sell[o.sell_bpos[blk] * bs2 + slot_pos[m]] = static_cast<float>(v);
 }
 
 // Local residual of one element for coefficients c (residual terms only, both forms).
@@ -830,7 +836,7 @@ void launch_gather_residual(double* r, int bs, int ns, int64_t node_begin, int64
 
 void launch_gather_jacobian(double* J, int bs, int nslot, const int32_t* slot_pos, int64_t block_begin,
                             int64_t nblocks, const int64_t* ptr, const int32_t* list, const double* ej, bool f32,
-                            cudaStream_t stream) {
+                            cudaStream_t stream, const JacobianGatherOut& out) {
   if (nblocks <= 0 || nslot <= 0) return;
   const int64_t total = nblocks * nslot;
   if (total >= (int64_t{1} << 32) - 256) throw std::runtime_error("gather: more than 2^32 block entries");
@@ -839,10 +845,10 @@ void launch_gather_jacobian(double* J, int bs, int nslot, const int32_t* slot_po
   if (f32)
     k_gather_jacobian<float><<<grid, 256, 0, stream>>>(J, bs * bs, static_cast<unsigned>(nslot), slot_pos, block_begin,
                                                        static_cast<unsigned>(total), ptr, list,
-                                                       reinterpret_cast<const float*>(ej));
+                                                       reinterpret_cast<const float*>(ej), out);
   else
     k_gather_jacobian<double><<<grid, 256, 0, stream>>>(J, bs * bs, static_cast<unsigned>(nslot), slot_pos,
-                                                        block_begin, static_cast<unsigned>(total), ptr, list, ej);
+                                                        block_begin, static_cast<unsigned>(total), ptr, list, ej, out);
 }
 
 void launch_volume(int dim, int ns, const VolumeParams& p, int begin, int end, int mode,

@@ -491,9 +491,14 @@ void Model::build_pattern() {
             k < len ? colidx[rowptr[br] + k] : static_cast<int32_t>(br < nnodes ? br : 0);
     }
   }
+  std::vector<int64_t> sbpos(colidx.size());
+  for (int64_t br = 0; br < nnodes; ++br)
+    for (int k = 0; k < rowptr[br + 1] - rowptr[br]; ++k)
+      sbpos[rowptr[br] + k] = (soff[br / 32] + k) * 32 + (br % 32);
   sell_slots = soff[nsl];
   d_sell_off.upload(soff);
   d_sell_cols.upload(scols);
+  d_sell_bpos.upload(sbpos);
   d_row_ns.upload(row_ns);
 }
 
@@ -1120,8 +1125,8 @@ Sell Model::sell() const {
   return S;
 }
 
-void Model::assemble(const double* x, double t, double cm, double ca, double* r, double* J, int mode,
-                     cudaStream_t s) const {
+bool Model::assemble(const double* x, double t, double cm, double ca, double* r, double* J, int mode,
+                     cudaStream_t s, float* jac_sell32) const {
   // static part: r += (cm Ms + ca Ks) x, J (+)= cm Ms + ca Ks
   const Bsr A0 = bsr(nullptr, nullptr);
   const int64_t nvals = nnzb() * bs * bs;
@@ -1147,7 +1152,25 @@ void Model::assemble(const double* x, double t, double cm, double ca, double* r,
       if (use_k) spmv_acc(A0, d_Ks.get(), x, r, ca, s);
     }
   }
-  if ((mode & 2) && J) {
+  // one compartment whose state-dependent gather covers every Jacobian entry: that gather
+  // takes the static operator as its base (no copy of it into J first) and, with nothing
+  // added to J after it, also writes the fp32 SELL-32 copy
+  const VolumeGroup* cover = nullptr;
+  if ((mode & 2) && J && (mode & kAssembleOverwriteJacobian) && !numerical_jacobian && vgroups.size() == 1) {
+    const VolumeGroup& g = vgroups[0];
+    const bool active = (cm != 0.0 && g.has_mass) || (ca != 0.0 && g.has_stiffness);
+    if (active && g.slots_dyn == bs * bs && g.block_begin == 0 && g.nblocks == nnzb()) cover = &g;
+  }
+  JacobianGatherOut gout;
+  if (cover) {
+    gout.overwrite = 1;
+    gout.base = C;
+    if (jac_sell32 && (fgroups.empty() || ca == 0.0) && !padded && n_constraints == 0) {
+      gout.sell = jac_sell32;
+      gout.sell_bpos = d_sell_bpos.get();
+    }
+  }
+  if ((mode & 2) && J && !cover) {
     if (mode & kAssembleOverwriteJacobian) {
       if (C) cuda_check(cudaMemcpyAsync(J, C, nvals * sizeof(double), cudaMemcpyDeviceToDevice, s), "copy");
       else cuda_check(cudaMemsetAsync(J, 0, nvals * sizeof(double), s), "memset");
@@ -1211,7 +1234,7 @@ void Model::assemble(const double* x, double t, double cm, double ca, double* r,
       launch_gather_residual(r, bs, g.ns, g.node_begin, g.nnodes, g.rlist_ptr.get(), g.rlist.get(), d_er.get(), s);
     if ((mode & 2) && J && g.slots_dyn > 0)
       launch_gather_jacobian(J, bs, g.slots_dyn, g.slot_pos_dyn.get(), g.block_begin, g.nblocks, g.blist_ptr.get(),
-                             g.blist.get(), d_ej.get(), jac_f32, s);
+                             g.blist.get(), d_ej.get(), jac_f32, s, &g == cover ? gout : JacobianGatherOut{});
   }
   if (ca != 0.0) {
     for (const auto& g : fgroups) {
@@ -1247,6 +1270,7 @@ void Model::assemble(const double* x, double t, double cm, double ca, double* r,
         launch_faces(dim, p, g.color_offsets[k], g.color_offsets[k + 1], mode, s);
     }
   }
+  return gout.sell != nullptr;
 }
 
 }  // namespace dcgpu

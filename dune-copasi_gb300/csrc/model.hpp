@@ -227,13 +227,18 @@ class Model {
   // kAssembleJacobianF32: the per-element Jacobian values of the state-dependent terms are
   // computed and gathered in fp32 (mixed precision; the residual and the static part stay fp64)
   static constexpr int kAssembleJacobianF32 = 16;
-  void assemble(const double* x, double t, double cm, double ca, double* r, double* J, int mode,
-                cudaStream_t s) const;
+  // jac_sell32 (optional, sell_slots * 32 * bs * bs floats with zero padding slots): when one
+  // volume gather produces every final Jacobian entry (one compartment, every slot
+  // state-dependent, no membrane, padding or constraint rows), that gather also writes the
+  // fp32 SELL-32 copy of J there; the return value says whether it did.
+  bool assemble(const double* x, double t, double cm, double ca, double* r, double* J, int mode, cudaStream_t s,
+                float* jac_sell32 = nullptr) const;
   Bsr bsr(double* val, float* val32) const;
   Sell sell() const;  // SELL-32 layout of the pattern (values sized sell_slots * 32 * bs * bs)
   int64_t sell_slots = 0;
   DeviceBuffer<int64_t> d_sell_off;
   DeviceBuffer<int32_t> d_sell_cols;
+  DeviceBuffer<int64_t> d_sell_bpos;  // per BSR block: its SELL-32 value slot ((off + k) * 32 + lane)
   int64_t nnzb() const { return static_cast<int64_t>(colidx.size()); }
 
  private:

@@ -91,7 +91,8 @@ Solver::Solver(Model& m, cudaStream_t s) : model(m), stream(s) {
   status_.resize(1);
   cuda_check(cudaMemsetAsync(counter_.get(), 0, sizeof(unsigned int), stream), "memset");
   cuda_check(cudaMemsetAsync(scal_.get(), 0, 32 * sizeof(double), stream), "memset");
-  cuda_check(cudaMallocHost(&pinned_, 32 * sizeof(double)), "cudaMallocHost");
+  // 32 scalar slots + one for the deferred preconditioner status
+  cuda_check(cudaMallocHost(&pinned_, 33 * sizeof(double)), "cudaMallocHost");
   rs_.partial = partial_.get();
   rs_.counter = counter_.get();
   rs_.result = scal_.get() + 16;
@@ -204,7 +205,11 @@ void Solver::enable_mixed(bool on) {
     fp2_.resize(n_); fv2_.resize(n_);
     fdinv_.resize(static_cast<size_t>(model.nnodes) * model.bs * model.bs);
     if (spmv_request_ != kSpmvSell || use_amg_) J32_.resize(static_cast<size_t>(model.nnzb()) * model.bs * model.bs);
-    if (spmv_request_ != kSpmvBsr) Js32_.resize(static_cast<size_t>(model.sell_slots) * 32 * model.bs * model.bs);
+    if (spmv_request_ != kSpmvBsr) {
+      // the padding slots stay zero: the fused gather of Model::assemble writes real blocks only
+      Js32_.resize(static_cast<size_t>(model.sell_slots) * 32 * model.bs * model.bs);
+      cuda_check(cudaMemset(Js32_.get(), 0, Js32_.size() * sizeof(float)), "memset");
+    }
   }
 }
 
@@ -272,6 +277,13 @@ std::vector<double> Solver::get_state() const {
   return ref;
 }
 
+void Solver::check_setup_status() {
+  if (!setup_status_pending_) return;
+  setup_status_pending_ = false;
+  cuda_check(cudaStreamSynchronize(stream), "status");  // normally already idle: the solve read its result
+  if (*pinned_status()) throw StepFailure("singular diagonal block in the Jacobian");
+}
+
 double Solver::read_scalar(int slot) {
   double v;
   read_scalars(&v, slot, 1);
@@ -334,16 +346,24 @@ void Solver::setup_preconditioner() {
   Bsr A = model.bsr(J_.get(), nullptr);
   block_jacobi_setup(A, model.d_diag.get(), dinv_.get(), status_.get(), stream);
   int st = 0;
-  cuda_check(cudaMemcpyAsync(&st, status_.get(), sizeof(int), cudaMemcpyDeviceToHost, stream), "status");
-  cuda_check(cudaStreamSynchronize(stream), "status");
-  if (st) throw StepFailure("singular diagonal block in the Jacobian");
+  if (!use_amg_) {
+    // read with the solve's own result instead of a stream synchronisation of its own
+    // (check_setup_status); a singular block only makes that solve's values meaningless
+    cuda_check(cudaMemcpyAsync(pinned_status(), status_.get(), sizeof(int), cudaMemcpyDeviceToHost, stream),
+               "status");
+    setup_status_pending_ = true;
+  } else {
+    cuda_check(cudaMemcpyAsync(&st, status_.get(), sizeof(int), cudaMemcpyDeviceToHost, stream), "status");
+    cuda_check(cudaStreamSynchronize(stream), "status");
+    if (st) throw StepFailure("singular diagonal block in the Jacobian");
+  }
   if (mixed_precision) {
     // the BSR copy feeds the BSR SpMV, the tuner and the multigrid fine level; the SELL-32
     // copy feeds the SELL SpMV
     const bool need_bsr = spmv_format != kSpmvSell || use_amg_;
     const bool need_sell = spmv_format != kSpmvBsr;
     if (need_bsr) to_float(static_cast<int64_t>(model.nnzb()) * model.bs * model.bs, J_.get(), J32_.get(), stream);
-    if (need_sell) bsr_to_sell(A, J_.get(), model.sell(), Js32_.get(), stream);
+    if (need_sell && !jac_sell_fresh_) bsr_to_sell(A, J_.get(), model.sell(), Js32_.get(), stream);
     to_float(static_cast<int64_t>(model.nnodes) * model.bs * model.bs, dinv_.get(), fdinv_.get(), stream);
     if (spmv_format == kSpmvAuto) tune_spmv();
   }
@@ -754,6 +774,7 @@ int Solver::linear_solve(const double* b, double* z, double rel_tol, int* iters)
   setup_preconditioner();
   int it = 0;
   int st = mixed_precision ? bicgstab_mixed(b, z, rel_tol, lin_max_it_, &it) : bicgstab(b, z, rel_tol, lin_max_it_, &it);
+  check_setup_status();
   if (iters) *iters = it;
   stats.linear_iterations += it;
   ++stats.linear_solves;
@@ -872,7 +893,7 @@ void Solver::one_step(double dt) {
     };
     auto jac = [&](const double* y) {
       tbegin(0);
-      model.assemble(y, ti, ai, bi, nullptr, J_.get(), 2 | jmode, stream);
+      jac_sell_fresh_ = model.assemble(y, ti, ai, bi, nullptr, J_.get(), 2 | jmode, stream, jac_sell_target());
       tend();
       finish_jac();
       ++stats.assemblies;
@@ -880,7 +901,7 @@ void Solver::one_step(double dt) {
     auto resjac = [&](const double* y, double* r) {
       cuda_check(cudaMemcpyAsync(r, const_.get(), n_ * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");
       tbegin(0);
-      model.assemble(y, ti, ai, bi, r, J_.get(), 3 | jmode, stream);
+      jac_sell_fresh_ = model.assemble(y, ti, ai, bi, r, J_.get(), 3 | jmode, stream, jac_sell_target());
       tend();
       model.constrain_residual(r, stream);
       finish_jac();

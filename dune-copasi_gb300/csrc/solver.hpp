@@ -143,10 +143,17 @@ class Solver {
   DeviceBuffer<float> fp2_, fv2_;  // second p / v of the three-phase single-launch solve
   DeviceBuffer<float> J32_;
   DeviceBuffer<float> Js32_;  // fp32 operator in the SELL-32 layout
+  bool jac_sell_fresh_ = false;  // the last Jacobian assembly also wrote Js32_
+  float* jac_sell_target() {
+    return mixed_precision && spmv_format != kSpmvBsr && Js32_.size() > 0 ? Js32_.get() : nullptr;
+  }
   DeviceBuffer<double> partial_, scal_;
   DeviceBuffer<unsigned int> counter_;
   DeviceBuffer<int> status_;
   double* pinned_ = nullptr;
+  int* pinned_status() { return reinterpret_cast<int*>(pinned_ + 32); }
+  bool setup_status_pending_ = false;  // a block-Jacobi status copy awaits check_setup_status
+  void check_setup_status();
   ReduceScratch rs_{};
 
   // configuration

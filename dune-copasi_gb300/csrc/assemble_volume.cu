@@ -548,6 +548,31 @@ __global__ void __launch_bounds__(128) k_volume(const VolumeParams P, const int 
   }
 }
 
+// sum of v[list[i] * stride + col] for i in [i0, i1), added in ascending i.  The list
+// entries and the values are fetched eight at a time as independent loads (the plain loop
+// is a chain of dependent list -> value loads, latency-bound); the sum order is unchanged.
+// Used by the block gather (nine-entry element matrices, long lists); the node gather's
+// short lists measured faster with the plain loop.
+template <class E>
+__device__ __forceinline__ E gather_sum(int64_t i0, int64_t i1, const int32_t* __restrict__ list,
+                                        const E* __restrict__ v, unsigned stride, unsigned col) {
+  constexpr int kBatch = 8;
+  E acc = E(0);
+  for (int64_t i = i0; i < i1; i += kBatch) {
+    int32_t idx[kBatch];
+    E val[kBatch];
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) idx[u] = i + u < i1 ? list[i + u] : 0;
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u)
+      val[u] = i + u < i1 ? v[static_cast<int64_t>(idx[u]) * stride + col] : E(0);
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u)
+      if (i + u < i1) acc += val[u];
+  }
+  return acc;
+}
+
 // r[node, s] += sum of the element residual entries of the node's (element, vertex) list;
 // a thread per (node, species), species fastest, 32-bit index arithmetic
 __global__ void k_gather_residual(double* __restrict__ r, int bs, unsigned ns, int64_t node_begin, unsigned ntotal,
@@ -572,8 +597,7 @@ __global__ void k_gather_jacobian(double* __restrict__ J, int bs2, unsigned nslo
   const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ntotal) return;
   const unsigned b = t / nslot, m = t - b * nslot;
-  E acc = E(0);
-  for (int64_t i = ptr[b]; i < ptr[b + 1]; ++i) acc += ej[static_cast<int64_t>(list[i]) * nslot + m];
+  const E acc = gather_sum<E>(ptr[b], ptr[b + 1], list, ej, nslot, m);
   const int64_t blk = block_begin + b;
   const int64_t at = blk * bs2 + slot_pos[m];
   // overwrite: this gather covers every entry of J, so the static operator (or zero) is its

@@ -65,6 +65,9 @@ def parse():
     ap.add_argument("--single-launch", default="on", choices=["on", "off"],
                     help="BiCGSTAB as one cooperative launch per solve (on) or one launch per "
                          "phase from a CUDA graph (off) (linear_solver.single_launch)")
+    ap.add_argument("--inner-reduction", type=float, default=None,
+                    help="mixed precision: residual reduction of each fp32 correction solve "
+                         "(linear_solver.inner_reduction; engine default 1e-4)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--large-n", type=int, default=128,
                     help="cube edge of the HBM-resident SpMV measurement (0 disables it)")
@@ -354,9 +357,12 @@ def main():
 
     ini, init, dt0, wdesc = make_workload(args.n, args.workload)
     single = "true" if args.single_launch == "on" else "false"
-    model = dcgpu.Model(ini, {"model.time_step_operator.linear_solver.spmv": args.spmv,
-                              "model.time_step_operator.linear_solver.preconditioner.type": args.precond,
-                              "model.time_step_operator.linear_solver.single_launch": single})
+    ov = {"model.time_step_operator.linear_solver.spmv": args.spmv,
+          "model.time_step_operator.linear_solver.preconditioner.type": args.precond,
+          "model.time_step_operator.linear_solver.single_launch": single}
+    if args.inner_reduction is not None:
+        ov["model.time_step_operator.linear_solver.inner_reduction"] = repr(args.inner_reduction)
+    model = dcgpu.Model(ini, ov)
     if args.precision == "mixed":
         model.set_mixed_precision(True)
     x0 = model.seeded_state(init)

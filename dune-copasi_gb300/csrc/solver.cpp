@@ -175,6 +175,11 @@ Solver::Solver(Model& m, cudaStream_t s) : model(m), stream(s) {
   if (jp != "single" && jp != "double")
     throw ConfigError("linear_solver.jacobian_precision must be single or double, not '" + jp + "'");
   jac_f32_ = jp == "single";
+  // mixed precision only: residual reduction of each fp32 correction solve inside the fp64
+  // iterative refinement (fewer refinements against more fp32 iterations each)
+  mixed_inner_ = ls.get_double("inner_reduction", kMixedInnerReduction);
+  if (!(mixed_inner_ >= 1e-7 && mixed_inner_ < 1.0))
+    throw ConfigError("linear_solver.inner_reduction must be in [1e-7, 1)");
   const std::string fmt = ls.get("spmv", "auto");
   if (fmt == "auto") spmv_request_ = kSpmvAuto;
   else if (fmt == "bsr") spmv_request_ = kSpmvBsr;
@@ -636,7 +641,7 @@ bool Solver::krylov_fused(double rel, int max_it, int* iters, int* status, const
       a.z64 = z64;
       a.r64 = kr_.get();
       a.vals64 = J_.get();
-      a.inner = kMixedInnerReduction;
+      a.inner = mixed_inner_;
       a.max_refinements = kMixedMaxRefinements;
     }
   }
@@ -739,7 +744,7 @@ int Solver::bicgstab_mixed(const double* b, double* z, double rel_tol, int max_i
   if (b0 == 0.0) return DC_OK;
   if (!std::isfinite(b0)) return DC_ERR_DIVERGED;
   const double target = rel_tol * b0;
-  const double inner_red = kMixedInnerReduction;
+  const double inner_red = mixed_inner_;
   double rn = b0;
   int total = 0;
   for (int ref = 0; ref < kMixedMaxRefinements && total < max_it; ++ref) {

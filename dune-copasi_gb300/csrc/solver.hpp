@@ -185,6 +185,7 @@ class Solver {
   // mixed precision: relative reduction asked of each fp32 correction, and the cap on
   // corrections per solve
   static constexpr double kMixedInnerReduction = 1e-4;
+  double mixed_inner_ = kMixedInnerReduction;  // linear_solver.inner_reduction
   static constexpr int kMixedMaxRefinements = 50;
   double direct_tol_ = 1e-10;
   int lin_max_it_ = 500;

@@ -133,7 +133,8 @@ void spmv_dispatch(const Bsr& A, const V* val, const X* x, X* y, const X* b, cud
 // ---------------------------------------------------------------- block Jacobi
 
 template <int B>
-__global__ void k_bj_setup(int nrows, const int32_t* diag, const double* val, double* dinv, int* status) {
+__global__ void k_bj_setup(int nrows, const int32_t* diag, const double* val, double* dinv, int* status,
+                           float* dinv32) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= nrows) return;
   double a[B][B], inv[B][B];
@@ -177,6 +178,14 @@ __global__ void k_bj_setup(int nrows, const int32_t* diag, const double* val, do
   for (int i = 0; i < B; ++i)
 #pragma unroll
     for (int j = 0; j < B; ++j) o[i * B + j] = inv[i][j];
+  // the fp32 copy of the mixed-precision solve, without a conversion pass
+  if (dinv32) {
+    float* o32 = dinv32 + static_cast<int64_t>(r) * B * B;
+#pragma unroll
+    for (int i = 0; i < B; ++i)
+#pragma unroll
+      for (int j = 0; j < B; ++j) o32[i * B + j] = static_cast<float>(inv[i][j]);
+  }
 }
 
 template <int B, class V, class X>
@@ -359,12 +368,13 @@ void dot(const double* x, const double* y, int64_t n, ReduceScratch rs, int slot
   reduce<1>(n, DotBody{x, y}, StoreFin{rs.result + slot}, rs, s);
 }
 
-void block_jacobi_setup(const Bsr& A, const int32_t* diag, double* dinv, int* status, cudaStream_t s) {
+void block_jacobi_setup(const Bsr& A, const int32_t* diag, double* dinv, int* status, cudaStream_t s,
+                        float* dinv32) {
   if (A.nrows == 0) return;
   const int threads = 128, blocks = (A.nrows + threads - 1) / threads;
   count_launches(1);
 #define DC_BJS(B) \
-  case B: k_bj_setup<B><<<blocks, threads, 0, s>>>(A.nrows, diag, A.val, dinv, status); return;
+  case B: k_bj_setup<B><<<blocks, threads, 0, s>>>(A.nrows, diag, A.val, dinv, status, dinv32); return;
   switch (A.bs) {
     DC_BJS(1) DC_BJS(2) DC_BJS(3) DC_BJS(4) DC_BJS(5) DC_BJS(6) DC_BJS(7) DC_BJS(8)
     default: throw std::runtime_error("block Jacobi: block size unsupported");

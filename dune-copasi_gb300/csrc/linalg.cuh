@@ -52,7 +52,9 @@ void dot(const double* x, const double* y, int64_t n, ReduceScratch rs, int slot
 
 // block Jacobi: dinv = inverse of the diagonal blocks; returns via status[0] != 0 on a
 // singular block
-void block_jacobi_setup(const Bsr& A, const int32_t* diag, double* dinv, int* status, cudaStream_t s);
+// (dinv32, optional: the same inverses rounded to fp32)
+void block_jacobi_setup(const Bsr& A, const int32_t* diag, double* dinv, int* status, cudaStream_t s,
+                        float* dinv32 = nullptr);
 void block_jacobi_apply(int nrows, int bs, const double* dinv, const double* x, double* y, cudaStream_t s);
 void block_jacobi_apply32(int nrows, int bs, const float* dinv, const float* x, float* y, cudaStream_t s);
 

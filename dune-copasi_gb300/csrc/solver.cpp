@@ -349,7 +349,8 @@ double Solver::norm2(const double* v) {
 void Solver::setup_preconditioner() {
   cuda_check(cudaMemsetAsync(status_.get(), 0, sizeof(int), stream), "memset");
   Bsr A = model.bsr(J_.get(), nullptr);
-  block_jacobi_setup(A, model.d_diag.get(), dinv_.get(), status_.get(), stream);
+  block_jacobi_setup(A, model.d_diag.get(), dinv_.get(), status_.get(), stream,
+                     mixed_precision ? fdinv_.get() : nullptr);
   int st = 0;
   if (!use_amg_) {
     // read with the solve's own result instead of a stream synchronisation of its own
@@ -369,7 +370,6 @@ void Solver::setup_preconditioner() {
     const bool need_sell = spmv_format != kSpmvBsr;
     if (need_bsr) to_float(static_cast<int64_t>(model.nnzb()) * model.bs * model.bs, J_.get(), J32_.get(), stream);
     if (need_sell && !jac_sell_fresh_) bsr_to_sell(A, J_.get(), model.sell(), Js32_.get(), stream);
-    to_float(static_cast<int64_t>(model.nnodes) * model.bs * model.bs, dinv_.get(), fdinv_.get(), stream);
     if (spmv_format == kSpmvAuto) tune_spmv();
   }
   if (use_amg_) {

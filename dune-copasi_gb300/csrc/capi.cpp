@@ -177,8 +177,7 @@ int dc_state_get(const dc_model* model, double* host_out, size_t n) {
   return guarded([&] {
     if (!model || !host_out) throw std::invalid_argument("null argument");
     if (static_cast<int64_t>(n) != model->model->ndof) throw std::invalid_argument("size mismatch");
-    auto v = model->solver->get_state();
-    std::memcpy(host_out, v.data(), n * sizeof(double));
+    model->solver->get_state(host_out, static_cast<int64_t>(n));
     return DC_OK;
   });
 }
@@ -195,7 +194,7 @@ int dc_state_set(dc_model* model, const double* host_in, size_t n, double time) 
   return guarded([&] {
     if (!model || !host_in) throw std::invalid_argument("null argument");
     if (static_cast<int64_t>(n) != model->model->ndof) throw std::invalid_argument("size mismatch");
-    model->solver->set_state(std::vector<double>(host_in, host_in + n), time);
+    model->solver->set_state(host_in, static_cast<int64_t>(n), time);
     return DC_OK;
   });
 }

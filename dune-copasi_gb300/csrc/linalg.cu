@@ -400,6 +400,30 @@ void scale_copy(int64_t n, double a, const double* x, double* y, cudaStream_t s)
 void combine(int64_t n, double a, const double* x, double b, const double* y, double* out, cudaStream_t s) {
   if (n > 0) k_combine<<<ew_blocks(n), 256, 0, s>>>(n, a, x, b, y, out);
 }
+namespace {
+__global__ void k_scatter_idx(int64_t n, const int64_t* __restrict__ idx, const double* __restrict__ src,
+                              double* __restrict__ dst) {
+  const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) dst[idx[i]] = src[i];
+}
+__global__ void k_gather_idx(int64_t n, const int64_t* __restrict__ idx, const double* __restrict__ src,
+                             double* __restrict__ dst) {
+  const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = src[idx[i]];
+}
+}  // namespace
+
+void scatter_idx(int64_t n, const int64_t* idx, const double* src, double* dst, cudaStream_t s) {
+  if (n <= 0) return;
+  count_launches(1);
+  k_scatter_idx<<<static_cast<unsigned>((n + 255) / 256), 256, 0, s>>>(n, idx, src, dst);
+}
+void gather_idx(int64_t n, const int64_t* idx, const double* src, double* dst, cudaStream_t s) {
+  if (n <= 0) return;
+  count_launches(1);
+  k_gather_idx<<<static_cast<unsigned>((n + 255) / 256), 256, 0, s>>>(n, idx, src, dst);
+}
+
 void to_float(int64_t n, const double* x, float* y, cudaStream_t s) {
   if (n > 0) k_to_float<<<ew_blocks(n), 256, 0, s>>>(n, x, 1.0, y);
 }

@@ -70,6 +70,9 @@ void scale_copy(int64_t n, double a, const double* x, double* y, cudaStream_t s)
 // out = a x + b y; x or y may be null (its term is left out)
 void combine(int64_t n, double a, const double* x, double b, const double* y, double* out, cudaStream_t s);
 void to_float(int64_t n, const double* x, float* y, cudaStream_t s);
+// dst[idx[i]] = src[i] / dst[i] = src[idx[i]] for i < n (reference <-> blocked state layout)
+void scatter_idx(int64_t n, const int64_t* idx, const double* src, double* dst, cudaStream_t s);
+void gather_idx(int64_t n, const int64_t* idx, const double* src, double* dst, cudaStream_t s);
 void add_float(int64_t n, const float* x, double* y, cudaStream_t s);                 // y += x
 void to_float_scaled(int64_t n, const double* x, double scale, float* y, cudaStream_t s);
 void add_float_scaled(int64_t n, const float* x, double scale, double* y, cudaStream_t s);

@@ -500,6 +500,15 @@ void Model::build_pattern() {
   d_sell_cols.upload(scols);
   d_sell_bpos.upload(sbpos);
   d_row_ns.upload(row_ns);
+  // reference DOF -> blocked index (the layout map of to_blocked / from_blocked, on the device)
+  {
+    std::vector<int64_t> r2b;
+    r2b.reserve(ndof);
+    for (size_t c = 0; c < comp_names.size(); ++c)
+      for (int64_t k = 0; k < static_cast<int64_t>(comp_vertices[c].size()); ++k)
+        for (int s = 0; s < ns[c]; ++s) r2b.push_back((comp_node_offset[c] + k) * bs + s);
+    d_ref2blk.upload(r2b);
+  }
 }
 
 static int32_t find_block(const std::vector<int32_t>& rowptr, const std::vector<int32_t>& colidx, int32_t r,

@@ -165,6 +165,7 @@ class Model {
   std::vector<int32_t> rowptr, colidx, diag;
   DeviceBuffer<int32_t> d_rowptr, d_colidx, d_diag;
   DeviceBuffer<int8_t> d_row_ns;
+  DeviceBuffer<int64_t> d_ref2blk;  // reference DOF index -> blocked state index
   bool padded = false;
 
   // geometry on the device

@@ -264,21 +264,32 @@ Solver::~Solver() {
 }
 
 void Solver::set_state(const std::vector<double>& ref, double t) {
-  if (static_cast<int64_t>(ref.size()) != model.ndof) throw std::invalid_argument("state size mismatch");
-  std::vector<double> blk;
-  model.to_blocked(ref, blk);
-  cuda_check(cudaMemcpyAsync(x_.get(), blk.data(), blk.size() * sizeof(double), cudaMemcpyHostToDevice, stream),
-             "set_state");
+  set_state(ref.data(), static_cast<int64_t>(ref.size()), t);
+}
+
+// one copy of the caller's reference-layout vector to the device and a scatter kernel into
+// the blocked layout (padded slots zero); no host-side reordering or temporary vectors
+void Solver::set_state(const double* ref, int64_t n, double t) {
+  if (n != model.ndof) throw std::invalid_argument("state size mismatch");
+  if (ref_stage_.size() != static_cast<size_t>(n)) ref_stage_.resize(n);
+  cuda_check(cudaMemcpyAsync(ref_stage_.get(), ref, n * sizeof(double), cudaMemcpyHostToDevice, stream), "set_state");
+  if (model.padded) cuda_check(cudaMemsetAsync(x_.get(), 0, n_ * sizeof(double), stream), "set_state");
+  scatter_idx(n, model.d_ref2blk.get(), ref_stage_.get(), x_.get(), stream);
   cuda_check(cudaStreamSynchronize(stream), "set_state");
   t_ = t;
 }
 
-std::vector<double> Solver::get_state() const {
-  std::vector<double> blk(n_);
-  cuda_check(cudaMemcpyAsync(blk.data(), x_.get(), n_ * sizeof(double), cudaMemcpyDeviceToHost, stream), "get_state");
+void Solver::get_state(double* out, int64_t n) const {
+  if (n != model.ndof) throw std::invalid_argument("state size mismatch");
+  if (ref_stage_.size() != static_cast<size_t>(n)) ref_stage_.resize(n);
+  gather_idx(n, model.d_ref2blk.get(), x_.get(), ref_stage_.get(), stream);
+  cuda_check(cudaMemcpyAsync(out, ref_stage_.get(), n * sizeof(double), cudaMemcpyDeviceToHost, stream), "get_state");
   cuda_check(cudaStreamSynchronize(stream), "get_state");
-  std::vector<double> ref;
-  model.from_blocked(blk, ref);
+}
+
+std::vector<double> Solver::get_state() const {
+  std::vector<double> ref(model.ndof);
+  get_state(ref.data(), model.ndof);
   return ref;
 }
 

@@ -66,7 +66,10 @@ class Solver {
 
   // state (reference DOF order on the host)
   void set_state(const std::vector<double>& ref, double t);
+  void set_state(const double* ref, int64_t n, double t);  // reference DOF layout, host memory
   std::vector<double> get_state() const;
+  void get_state(double* out, int64_t n) const;             // reference DOF layout, host memory
+  mutable DeviceBuffer<double> ref_stage_;                   // reference-layout staging vector
   double time() const { return t_; }
   const double* state_device() const { return x_.get(); }  // blocked state
   const double* device_state() const { return x_.get(); }

@@ -214,8 +214,13 @@ class Model:
     def ndof(self):
         return self.info["n_dof"]
 
-    def state(self):
-        out = np.empty(self.ndof)
+    def state(self, out=None):
+        """The state in the reference DOF layout; `out` (float64, ndof, contiguous) is filled
+        in place when given (e.g. a pinned host array)."""
+        if out is None:
+            out = np.empty(self.ndof)
+        elif out.dtype != np.float64 or out.size != self.ndof or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError("out must be a contiguous float64 array of ndof values")
         _check(self._lib.dc_state_get(self._h, _ptr(out), out.size))
         return out
 

@@ -491,6 +491,21 @@ def test_fp32_and_fp64_jacobian_in_mixed_precision(dcgpu_lib):
         dcgpu_lib.Model(ini, {"model.time_step_operator.linear_solver.type": "QMR"})
 
 
+@pytest.mark.parametrize("inner", ["1e-5", "1e-6"])
+def test_mixed_inner_reduction(dcgpu_lib, inner):
+    """linear_solver.inner_reduction: a deeper fp32 correction solve per refinement still
+    meets the oracle tolerance on every step; values outside [1e-7, 1) are rejected."""
+    ini, init = ALL_CASES["features_2d"]()
+    ov = {"model.time_step_operator.linear_solver.inner_reduction": inner}
+    records = _run_both(dcgpu_lib, ini, init, mixed=True, overrides=ov)
+    for t, errs, n_o, n_g, stages in records:
+        for e in errs.values():
+            assert e <= STEP_TOL, (inner, t, e)
+    for bad in ("0", "1", "1e-9"):
+        with pytest.raises(dcgpu_lib.DcError):
+            dcgpu_lib.Model(ini, {"model.time_step_operator.linear_solver.inner_reduction": bad})
+
+
 @pytest.mark.parametrize("restart,precond,mixed", [(40, "Jacobi", False), (5, "Jacobi", False),
                                                    (10, "AMG", False), (10, "Jacobi", True)])
 def test_gmres_matches_oracle(dcgpu_lib, restart, precond, mixed):

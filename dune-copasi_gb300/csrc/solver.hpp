@@ -69,7 +69,6 @@ class Solver {
   void set_state(const double* ref, int64_t n, double t);  // reference DOF layout, host memory
   std::vector<double> get_state() const;
   void get_state(double* out, int64_t n) const;             // reference DOF layout, host memory
-  mutable DeviceBuffer<double> ref_stage_;                   // reference-layout staging vector
   double time() const { return t_; }
   const double* state_device() const { return x_.get(); }  // blocked state
   const double* device_state() const { return x_.get(); }
@@ -139,6 +138,7 @@ class Solver {
   int64_t n_ = 0;          // padded vector length
   double t_ = 0.0;
   DeviceBuffer<double> x_, r_, J_, stage_, const_, z_;
+  mutable DeviceBuffer<double> ref_stage_;  // reference-layout staging vector of set/get_state
   std::vector<DeviceBuffer<double>> us_;
   // Krylov workspace
   DeviceBuffer<double> kr_, krhat_, kp_, kv_, ks_, kt_, kphat_, kshat_, kx_, dinv_;

@@ -51,9 +51,11 @@ int dc_model_create(const char* ini_text, const char* overrides, dc_model** out)
     dcgpu::cuda_check(cudaGetDeviceCount(&dev_count), "cudaGetDeviceCount");
     if (dev_count == 0) throw dcgpu::CudaError("no CUDA device");
     auto m = std::make_unique<dc_model>();
+    dcgpu::cuda_check(cudaGetDevice(&m->device), "cudaGetDevice");
     dcgpu::cuda_check(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking), "cudaStreamCreate");
     m->model = std::make_unique<dcgpu::Model>(ini_text, overrides ? overrides : "");
     m->solver = std::make_unique<dcgpu::Solver>(*m->model, m->stream);
+    dc_noalloc_prepare(m->device);
     *out = m.release();
     return DC_OK;
   });

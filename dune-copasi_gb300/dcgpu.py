@@ -373,8 +373,26 @@ class Model:
         return d.value
 
     # -- operator access
-    def assemble(self, x, t, cm, ca, residual=True, jacobian=True):
+    def _state_arg(self, x):
+        """x as a C-contiguous float64 vector of n_dof values (the C ABI copies n_dof values
+        from it and takes no length)."""
         x = np.ascontiguousarray(x, dtype=np.float64)
+        if x.ndim != 1 or x.size != self.ndof:
+            raise ValueError("state vector must hold %d values, got shape %s" % (self.ndof, x.shape))
+        return x
+
+    def _out_arg(self, out):
+        """A caller's output vector: it must be a writable C-contiguous float64 array of n_dof
+        values, since the C ABI writes n_dof values into it."""
+        if out is None:
+            return np.empty(self.ndof)
+        if (not isinstance(out, np.ndarray) or out.dtype != np.float64 or not out.flags.c_contiguous
+                or not out.flags.writeable or out.size != self.ndof):
+            raise ValueError("out must be a writable C-contiguous float64 array of %d values" % self.ndof)
+        return out
+
+    def assemble(self, x, t, cm, ca, residual=True, jacobian=True):
+        x = self._state_arg(x)
         r = np.empty(self.ndof) if residual else None
         bs = self.info["block_size"]
         nj = self.info["n_blocks"] * bs * bs
@@ -387,8 +405,8 @@ class Model:
     def residual_noalloc(self, x, t, cm, ca, out=None):
         """Residual through the allocation-free entry point (staging in the library's fixed
         device array; see include/dcgpu.h).  Returns the residual, or raises DcError."""
-        x = np.ascontiguousarray(x, dtype=np.float64)
-        r = np.empty(self.ndof) if out is None else out
+        x = self._state_arg(x)
+        r = self._out_arg(out)
         st = self._lib.dc_assemble_residual_noalloc(self._h, _ptr(x), float(t), float(cm), float(ca), _ptr(r))
         if st != DC_OK:
             raise DcError(st, "dc_assemble_residual_noalloc failed")

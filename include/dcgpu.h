@@ -120,8 +120,11 @@ int dc_assemble(dc_model* model, const double* x, double t, double cm, double ca
  * fixed 16 MiB device array compiled into the library, held by every GPU that loads it:
  * models with more than 2^20 DOF, or whose compartments carry different species counts,
  * return DC_ERR_ARGUMENT.  All calls on a device share the array; calls that overlap on
- * the GPU race.  The first call on each device (with that device current) looks up the
- * array's address: make it before any stream capture.  Returns a status code only;
+ * the GPU race.  The call runs on the model's device whatever device is current.
+ * dc_model_create looks up the array's address on the model's device, which loads the
+ * module holding the array and commits it there; should that lookup fail, the first call
+ * retries it, so create the model (or make one call) before any stream capture.  x and r
+ * hold n_dof doubles each.  Returns a status code only (DC_ERR_CUDA for a CUDA failure);
  * dc_last_error() is not updated. */
 int dc_assemble_residual_noalloc(dc_model* model, const double* x, double t, double cm, double ca, double* r);
 

@@ -326,6 +326,19 @@ int dc_dof_map(const dc_model* model, int64_t* ref_to_dev, size_t n) {
   });
 }
 
+int dc_step_stage_newton(const dc_model* model, int32_t* counts, size_t n, size_t* n_out) {
+  return guarded([&] {
+    if (!model || !n_out) throw std::invalid_argument("null argument");
+    const auto& v = model->solver->stats.step_stage_newton;
+    *n_out = v.size();
+    if (counts) {
+      if (n < v.size()) throw std::invalid_argument("counts holds fewer entries than stage solves");
+      for (size_t i = 0; i < v.size(); ++i) counts[i] = v[i];
+    }
+    return DC_OK;
+  });
+}
+
 int dc_stats(const dc_model* model, int64_t* newton_iterations, int64_t* linear_iterations, int64_t* assemblies,
              int64_t* failed_steps) {
   return guarded([&] {

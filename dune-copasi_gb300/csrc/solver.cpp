@@ -860,6 +860,7 @@ void Solver::newton(double* x, const ResFn& res, const JacFn& jac, const ResFn& 
   }
   stats.newton_iterations += it;
   stats.last_newton = it;
+  stats.step_stage_newton.push_back(it);
 }
 
 void Solver::one_step(double dt) {
@@ -941,6 +942,7 @@ int Solver::do_step(double& dt, double* dt_used) {
     if (has_max_ && f_gt(std::fabs(d), std::fabs(dt_max_))) return false;
     return true;
   };
+  stats.step_stage_newton.clear();
   if (!check(dt)) return DC_ERR_DT_MIN;
   // Without time_step_min the reference keeps halving until dt underflows; here a step
   // gives up after kMaxRejections consecutive rejections (dt reduced by dec^60 ~ 1e-18).

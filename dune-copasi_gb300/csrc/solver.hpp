@@ -49,6 +49,9 @@ struct SolverStats {
   long steps = 0;
   long refinements = 0;
   int last_newton = 0;
+  // Newton iterations of every stage solve of the last do_step, in order (stages of
+  // rejected attempts included; a stage whose Newton failed adds nothing)
+  std::vector<int> step_stage_newton;
 };
 
 class StepFailure : public std::runtime_error {

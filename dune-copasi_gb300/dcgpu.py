@@ -35,7 +35,7 @@ EXPORTED = [
     "dc_assemble_residual_noalloc", "dc_server_create", "dc_server_submit", "dc_server_poll",
     "dc_server_take_state", "dc_server_estimate", "dc_server_destroy", "dc_last_error",
     "dc_spmv_format", "dc_vertex_coords", "dc_constraints", "dc_reduce", "dc_write_vtk", "dc_config_get",
-    "dc_selftest_barrier_timeout",
+    "dc_selftest_barrier_timeout", "dc_step_stage_newton",
 ]
 
 
@@ -97,6 +97,7 @@ def load_library(path=LIB_PATH):
     pd = P(ctypes.c_double)
     lib.dc_model_create.argtypes = [ctypes.c_char_p, ctypes.c_char_p, P(vp)]
     lib.dc_model_destroy.argtypes = [vp]
+    lib.dc_step_stage_newton.argtypes = [vp, P(ctypes.c_int32), sz, P(sz)]
     lib.dc_model_info_get.argtypes = [vp, P(ModelInfo)]
     lib.dc_species_name.argtypes = [vp, i32, ctypes.c_char_p, sz]
     lib.dc_species_size.argtypes = [vp, i32, P(ctypes.c_int64)]
@@ -359,7 +360,16 @@ class Model:
         _check(st)
         out = {f: getattr(info, f) for f, _ in StepInfo._fields_}
         out["dt_next"] = d.value
+        out["newton_per_stage"] = self.stage_newton()
         return out
+
+    def stage_newton(self):
+        """Newton iterations of every stage solve of the last step (dc_step_stage_newton)."""
+        n = ctypes.c_size_t()
+        _check(self._lib.dc_step_stage_newton(self._h, None, 0, ctypes.byref(n)))
+        buf = (ctypes.c_int32 * max(n.value, 1))()
+        _check(self._lib.dc_step_stage_newton(self._h, buf, n.value, ctypes.byref(n)))
+        return [int(buf[i]) for i in range(n.value)]
 
     def evolve(self, t_end, dt, callback=None):
         d = ctypes.c_double(dt)

@@ -133,6 +133,14 @@ int dc_pattern(const dc_model* model, int32_t* rowptr, size_t n_rowptr, int32_t*
 /* map from reference DOF index to padded device index (node * block_size + species) */
 int dc_dof_map(const dc_model* model, int64_t* ref_to_dev, size_t n);
 
+/* Newton iterations of every stage solve of the last dc_step, in stage order (stages of
+ * attempts that the stepper rejected first, then the accepted attempt's stages; a stage
+ * whose Newton solve failed adds no entry; linear models add none).  Replaces reading
+ * PDELab's NewtonOperator result per stage (the Newton of model/make_step_operator.hh:
+ * 246-288, run by the RungeKutta one-step method once per stage, :408-443).  *n_out
+ * receives the count; with counts non-null (n >= *n_out) the values are copied. */
+int dc_step_stage_newton(const dc_model* model, int32_t* counts, size_t n, size_t* n_out);
+
 /* solver statistics accumulated since creation */
 int dc_stats(const dc_model* model, int64_t* newton_iterations, int64_t* linear_iterations, int64_t* assemblies,
              int64_t* failed_steps);

@@ -17,7 +17,11 @@ Restates, on top of oracle.fem:
     (dune/copasi/common/stepper.hh:95-239,337-368) with the CLI defaults of
     src/dune_copasi.cc:384-402 (decrease 0.5, increase 1.1).
 The linear solve is direct (scipy SuperLU), standing in for the reference's default
-UMFPack (dune/copasi/solver/istl/factory/direct.hh:9-12).
+UMFPack (dune/copasi/solver/istl/factory/direct.hh:9-12).  For meshes whose factorisation
+does not fit in memory (3D and 1024^2 multi-species systems) ``linear="iterative"`` replaces
+it with BiCGSTAB + Jacobi inside iterative refinement to a relative true residual of 1e-13
+(the direct solve's role in Newton: an essentially exact correction).  Assembly runs over at
+most ``chunk`` cells at a time, so the element arrays of large meshes stay bounded.
 """
 
 import math
@@ -119,7 +123,17 @@ class StepFailed(Exception):
 class OracleModel:
     """Everything between an ini text and a time-evolved state, on the CPU."""
 
-    def __init__(self, ini_text, overrides=None):
+    #: cells assembled at once (bounds the memory of the element arrays on big meshes)
+    chunk = 1 << 19
+    #: matrix entries collected before they are summed into the global matrix
+    flush_entries = 1 << 26
+    #: relative true-residual target of the iterative solve
+    iterative_rtol = 1e-13
+
+    def __init__(self, ini_text, overrides=None, linear="direct"):
+        if linear not in ("direct", "iterative"):
+            raise ValueError("linear must be 'direct' or 'iterative'")
+        self.linear = linear
         self.cfg = ParameterTree.from_text(ini_text, overrides)
         cfg = self.cfg
         self.ctx = E.Context(cfg.sub("parser_context") if cfg.has_sub("parser_context") else None)
@@ -754,10 +768,15 @@ class OracleModel:
                                 vals.append(loc.ravel())
 
     # ---------------------------------------------------------------- global operators
+    def _chunks(self, els):
+        for i in range(0, els.shape[0], self.chunk):
+            yield els[i:i + self.chunk]
+
     def residual(self, x, t, form):
         r = np.zeros(self.ndof)
         for els, sps in self.groups:
-            self._volume_residual(x, t, form, els, sps, r)
+            for part in self._chunks(els):
+                self._volume_residual(x, t, form, part, sps, r)
         if form == "stiffness" and self.has_outflow:
             self._skeleton(x, t, r, None, None, None)
         return r
@@ -766,11 +785,23 @@ class OracleModel:
         if self.numerical_jacobian:
             return self._numerical_jacobian(x, t, form)
         rows, cols, vals = [], [], []
+        J = None
+
+        def flush(J):
+            part = self._to_csr(rows, cols, vals)
+            rows.clear()
+            cols.clear()
+            vals.clear()
+            return part if J is None else J + part
+
         for els, sps in self.groups:
-            self._volume_jacobian(x, t, form, els, sps, rows, cols, vals)
+            for part in self._chunks(els):
+                self._volume_jacobian(x, t, form, part, sps, rows, cols, vals)
+                if sum(v.size for v in vals) >= self.flush_entries:
+                    J = flush(J)
         if form == "stiffness" and self.has_outflow:
             self._skeleton(x, t, None, rows, cols, vals)
-        return self._to_csr(rows, cols, vals)
+        return flush(J) if (rows or J is None) else J
 
     def _to_csr(self, rows, cols, vals):
         n = self.ndof
@@ -855,11 +886,41 @@ class OracleModel:
     def _solve(self, J, r):
         if J.nnz == 0:
             raise StepFailed("singular stage Jacobian")
+        if self.linear == "iterative":
+            return self._solve_iterative(J, r)
         # minimum-degree ordering on A^T + A: the matrix pattern is structurally symmetric
         lu = spla.splu(J.tocsc(), permc_spec="MMD_AT_PLUS_A")
         z = lu.solve(r)
         if not np.all(np.isfinite(z)):
             raise StepFailed("linear solve produced non-finite values")
+        return z
+
+    def _solve_iterative(self, J, r):
+        """BiCGSTAB + Jacobi (scipy) inside iterative refinement: corrections are added
+        until the true residual |r - J z| is below iterative_rtol |r|."""
+        J = J.tocsr()
+        d = J.diagonal()
+        if np.any(d == 0.0):
+            raise StepFailed("zero diagonal entry in the stage Jacobian")
+        dinv = 1.0 / d
+        M = spla.LinearOperator(J.shape, matvec=lambda v: dinv * v, dtype=float)
+        bn = float(np.linalg.norm(r))
+        z = np.zeros_like(r)
+        if bn == 0.0:
+            return z
+        res = r.copy()
+        for _sweep in range(8):
+            rn = float(np.linalg.norm(res))
+            if rn <= self.iterative_rtol * bn:
+                return z
+            dz, info = spla.bicgstab(J, res, rtol=max(1e-10, 0.1 * self.iterative_rtol * bn / rn), atol=0.0,
+                                     maxiter=20000, M=M)
+            if not np.all(np.isfinite(dz)):
+                raise StepFailed("iterative linear solve produced non-finite values")
+            z += dz
+            res = r - J @ z
+        if float(np.linalg.norm(res)) > self.iterative_rtol * bn:
+            raise StepFailed("iterative linear solve did not reach %g" % self.iterative_rtol)
         return z
 
     def _linear_solve_step(self, res, jac, x, stats):

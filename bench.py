@@ -1,24 +1,28 @@
 """Benchmark: DOF x Newton-steps per second of the implicit time step on one GB300.
 
-Workload (the configuration the headline metric is quoted on): seeded Gray-Scott,
-2 species, unit square 512 x 512 P1 triangles (526,338 DOF), Alexander2 DIRK dt = 1,
-Newton relative tolerance 1e-10 (squared l2, as the reference), direct-solve semantics
-(the reference's default UMFPack is replaced by BiCGSTAB converged to a relative
-residual of 1e-10).
+Headline workload (the largest configuration that fits one GPU): seeded 3D
+cross-diffusion, unit cube 128^3 cubes x 6 P1 tetrahedra (12,582,912 cells, 2,146,689
+vertices, 3 species, 6,440,067 DOF), Michaelis-Menten reactions and a full 3 x 3
+cross-diffusion matrix, Alexander2 DIRK dt = 0.01, Newton relative tolerance 1e-10 on the
+squared l2 norm (as the reference), direct-solve semantics (the reference's default
+UMFPack is replaced by BiCGSTAB + block Jacobi converged to a relative residual of 1e-10).
+`--workload gray_scott | two_compartment | heat` selects the other configurations.
 
 A "step" is one Alexander2 time step (2 stages x Newton iterations).  Timed per step with
-CUDA events on the engine's stream (dc_step_info.device_ms); the L2 cache is flushed
-between timed steps (a 256 MiB write).  value = DOF x Newton iterations of all timed
-steps / sum of device step times, for the mixed-precision path (fp32 Krylov in fp64
-refinement) by default; "plain_fp64" is the plain FP64 path on the same workload and steps,
-with the per-species relative L2 deviation of the mixed state from it.  e2e = the same
-through the public C ABI with host buffers: state upload (pinned->device), step, state
-download, host-timed.  "serving" runs a Poisson stream of random requests through the
-request server: served concurrently with mixed precision, and one at a time in plain FP64.
+CUDA events on the engine's stream (dc_step_info.device_ms); the operator (1.36 GB fp32,
+3.6 GB fp64) and the element buffers are far larger than L2, and a 256 MiB write flushes L2
+between timed steps as well.  value = DOF x Newton iterations of all timed steps / sum of
+device step times, for the mixed-precision path (fp32 Krylov in fp64 refinement);
+"plain_fp64" is the plain FP64 path on the same workload and steps, with the per-species
+relative L2 deviation of the mixed state from it.  e2e = the same metric through the public
+C ABI with host buffers: state upload from pinned host memory, step, state download,
+host-timed.  "secondary" holds the Gray-Scott 512^2 and two-compartment 1024^2
+configurations, "serving" a Poisson stream of random requests through the request server.
 
---impl reference times the CPU restatement of the reference algorithm (numpy assembly +
-SuperLU direct solve, the oracle) on the host cores, one Newton iteration of the full
-workload per step.
+--impl reference times the CPU restatement of the reference algorithm (C++, std::thread
+colour-parallel assembly, BiCGSTAB + block Jacobi, or + SSOR as the reference's iterative
+default with --cpu-precond ssor; built from oracle/cpu_newton.cpp) on all host cores: each
+bench step is one Newton iteration of the same time-stepping sequence on the same workload.
 
 Multi-GPU: independent replicas (one model per rank), no collective; scaling "weak".
 """
@@ -39,7 +43,14 @@ for p in (ROOT, PKG):
         sys.path.insert(0, p)
 
 METRIC = "DOF·Newton-steps/s"
-WORKLOAD = "gray_scott_512x512_p1_alexander2_dt1"
+
+# name -> (generator, default size, dt, scheme, local vertices per cell)
+WORKLOADS = {
+    "cross_diffusion_3d": ("cross_diffusion_3d", 128, 0.01, "Alexander2", 4),
+    "gray_scott": ("gray_scott", 512, 1.0, "Alexander2", 3),
+    "two_compartment": ("two_compartment", 1024, 0.05, "ImplicitEuler", 3),
+    "heat": ("heat", 128, 0.01, "ImplicitEuler", 3),
+}
 
 
 def parse():
@@ -48,11 +59,11 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="cross_diffusion_3d", choices=sorted(WORKLOADS))
     # "--grid" is the spelling to use after a torchrun launcher, whose own parser reads
     # "--n" as an ambiguous abbreviation of its options
-    ap.add_argument("--n", "--grid", dest="n", type=int, default=512)
-    ap.add_argument("--workload", default="gray_scott", choices=["gray_scott", "cross_diffusion_3d"],
-                    help="gray_scott (headline, n = grid edge) or cross_diffusion_3d (n = cube edge)")
+    ap.add_argument("--n", "--grid", dest="n", type=int, default=0,
+                    help="mesh size (grid edge in 2D, cube edge in 3D); 0 = the configuration's own")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"],
                     help="mixed (default): fp32 Krylov in fp64 refinement, measured against the plain "
                          "FP64 path on the same workload; fp64: the plain path alone")
@@ -68,9 +79,18 @@ def parse():
     ap.add_argument("--inner-reduction", type=float, default=None,
                     help="mixed precision: residual reduction of each fp32 correction solve "
                          "(linear_solver.inner_reduction; engine default 1e-4)")
+    ap.add_argument("--override", action="append", default=[],
+                    help="extra engine configuration key=value (repeatable)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--large-n", type=int, default=128,
-                    help="cube edge of the HBM-resident SpMV measurement (0 disables it)")
+    ap.add_argument("--cpu-iterations", type=int, default=2,
+                    help="Newton iterations of the CPU baseline leg")
+    ap.add_argument("--cpu-precond", default="bjacobi", choices=["bjacobi", "ssor"],
+                    help="preconditioner of the CPU restatement's BiCGSTAB: block Jacobi (the GPU path's) "
+                         "or SSOR (the reference's iterative default)")
+    ap.add_argument("--no-spmv-phase", action="store_true",
+                    help="skip the per-phase SpMV measurement on the headline operator")
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="skip the Gray-Scott 512^2 and two-compartment 1024^2 measurements")
     ap.add_argument("--serve-active", type=int, default=16,
                     help="simulations the request server runs at once (each on its own stream)")
     ap.add_argument("--serve-requests", type=int, default=32,
@@ -99,35 +119,35 @@ def dist_setup(args):
     return rank, world
 
 
-def make_workload(n, kind="gray_scott"):
-    """(ini, init, dt, description) of the bench workload; gray_scott is the headline one."""
-    import workloads as W
+def workload_desc(kind, n):
+    """Static description of a workload (no GPU needed): the `config` both arms print."""
+    gen, n0, dt, scheme, nl = WORKLOADS[kind]
+    n = n or n0
     if kind == "cross_diffusion_3d":
-        ini, init = W.cross_diffusion_3d(n=n, steps=100000, dt=0.01)
-        return ini, init, 0.01, {"workload": "cross_diffusion_3d_%d^3x6_p1_tets_alexander2_dt0.01" % n,
-                                 "mesh": "%d^3 cubes x 6 P1 tetrahedra" % n, "species": 3, "nl": 4}
-    ini, init = W.gray_scott(n=n, steps=100000, dt=1.0)
-    name = WORKLOAD if n == 512 else "gray_scott_%dx%d_p1_alexander2_dt1" % (n, n)
-    return ini, init, 1.0, {"workload": name, "mesh": "%dx%d P1 triangles" % (n, n), "species": 2, "nl": 3}
+        desc = {"workload": "cross_diffusion_3d_%d^3x6_p1_tets_alexander2_dt0.01" % n,
+                "mesh": "%d^3 cubes x 6 P1 tetrahedra" % n, "cells": 6 * n ** 3, "dof": 3 * (n + 1) ** 3,
+                "species": 3}
+    elif kind == "gray_scott":
+        desc = {"workload": "gray_scott_%dx%d_p1_alexander2_dt1" % (n, n), "mesh": "%dx%d P1 triangles" % (n, n),
+                "cells": 2 * n * n, "dof": 2 * (n + 1) ** 2, "species": 2}
+    elif kind == "two_compartment":
+        desc = {"workload": "two_compartment_%dx%d_p1_5+5_species_implicit_euler_dt0.05" % (n, n),
+                "mesh": "%dx%d P1 triangles, disk r=0.3 + annulus" % (n, n), "cells": 2 * n * n, "species": 10}
+    else:
+        desc = {"workload": "heat_%dx%d_p1_implicit_euler_dt0.01" % (n, n), "mesh": "%dx%d P1 triangles" % (n, n),
+                "cells": 2 * n * n, "dof": (n + 1) ** 2, "species": 1}
+    desc.update({"scheme": scheme, "dt": dt, "newton_rel_tol_sq": 1e-10})
+    return desc
 
 
-def initial_vector(om, init):
-    """Seeded initial state in the reference DOF order for the CPU legs, from the oracle
-    model `om` (the GPU arm builds the same vector from its own model, Model.seeded_state)."""
-    x = om.initial_state()
-    for sp in (om.species if init is not None else []):
-        verts = om.comp_vertices[sp.comp]
-        x[om.dof(sp, verts)] = init(sp.name, om.mesh.coords[verts])
-    return x
-
-
-def oracle_newton_iteration(om, x, dt):
-    """The work of one Newton iteration of an Alexander2 stage on the CPU oracle:
-    residual and Jacobian of M + gamma dt A at x, direct (SuperLU) solve, update."""
-    a = (1.0 - 0.5 * 2 ** 0.5) * dt
-    r = om.residual(x, 0.0, "mass") + a * om.residual(x, 0.0, "stiffness")
-    J = om.jacobian(x, 0.0, "mass") + a * om.jacobian(x, 0.0, "stiffness")
-    return x - om._solve(J, r)
+def make_workload(kind, n):
+    """(ini, init, dt, nl, description) of a workload."""
+    import workloads as W
+    gen, n0, dt, _scheme, nl = WORKLOADS[kind]
+    n = n or n0
+    kw = {"n": n, "steps": 100000, "dt": dt}
+    ini, init = getattr(W, gen)(**kw)
+    return ini, init, dt, nl, workload_desc(kind, n)
 
 
 class ClockSampler:
@@ -183,50 +203,57 @@ class ClockSampler:
         return out
 
 
-def cpu_baseline(ini, init, dt, wdesc, newton_steps=1):
-    """Oracle (numpy assembly + SuperLU) on the host: one Newton iteration of the full workload."""
-    from oracle.model import OracleModel
-    om = OracleModel(ini)
-    x0 = initial_vector(om, init)
-    t0 = time.perf_counter()
-    for _ in range(newton_steps):
-        x0 = oracle_newton_iteration(om, x0, dt)
-    dt = time.perf_counter() - t0
-    return {"value": om.ndof * newton_steps / dt, "unit": METRIC, "cores": 1, "kind": "port",
-            "sample": "%d Newton iteration(s) (residual + Jacobian assembly + SuperLU solve) of the "
-                      "%d-DOF %s stage system, first Alexander2 stage"
-                      % (newton_steps, om.ndof, wdesc["workload"]),
-            "seconds": dt}
+# ----------------------------------------------------------------------------- CPU legs
+def cpu_newton_run(kind, n, iterations, warmup, threads, precond):
+    """The C++ CPU restatement (oracle/cpu_newton.cpp) on the same workload: `warmup` +
+    `iterations` Newton iterations of the time-stepping sequence; returns its JSON report."""
+    from oracle import cpu_newton
+    ini, init, dt, _nl, _desc = make_workload(kind, n)
+    return cpu_newton.run(ini, init, iterations=iterations, warmup=warmup, threads=threads, precond=precond)
+
+
+def cpu_baseline(kind, n, iterations, precond):
+    """CPU baseline leg of the GPU arm: a bounded sample (a few Newton iterations of the same
+    time-stepping sequence) on all host cores, and one iteration on one core."""
+    threads = os.cpu_count() or 1
+    rep = cpu_newton_run(kind, n, iterations, 1, threads, precond)
+    one = cpu_newton_run(kind, n, 1, 0, 1, precond)
+    return {"value": rep["value"], "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": "%d Newton iteration(s) (residual + Jacobian assembly on %d threads, BiCGSTAB + %s to "
+                      "1e-10) of the %d-DOF stage systems of the first time step, after one untimed iteration"
+                      % (iterations, threads, rep["precond"], rep["ndof"]),
+            "value_1core": one["value"], "seconds": rep["seconds"], "assembly_seconds": rep["assembly_seconds"],
+            "solve_seconds": rep["solve_seconds"], "krylov_iterations": rep["krylov_iterations"],
+            "cpu": rep.get("cpu", "")}
 
 
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    ini, init, dt0, wdesc = make_workload(args.n, args.workload)
-    from oracle.model import OracleModel
-    om = OracleModel(ini)
-    x = initial_vector(om, init)
-    times = []
-    for k in range(args.warmup + args.steps):
-        t0 = time.perf_counter()
-        x = oracle_newton_iteration(om, x, dt0)
-        t1 = time.perf_counter()
-        if k >= args.warmup:
-            times.append(t1 - t0)
-    total = sum(times)
-    value = om.ndof * len(times) / total
+    desc = workload_desc(args.workload, args.n)
+    threads = os.cpu_count() or 1
+    try:
+        rep = cpu_newton_run(args.workload, args.n, args.steps, args.warmup, threads, args.cpu_precond)
+    except Exception as e:  # the restatement covers one-compartment models only
+        print(json.dumps({"impl": "reference", "unavailable": "CPU restatement: %s" % e}), flush=True)
+        return
+    value = rep["value"]
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / len(times),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * rep["seconds"] / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded initial state)",
-            "config": {"workload": wdesc["workload"], "dof": om.ndof,
-                       "step": "one Newton iteration (assembly + SuperLU)"},
-            "cpu_baseline": {"value": value, "unit": METRIC, "cores": 1, "kind": "port",
-                             "sample": "one Newton iteration of the full workload per step"},
-            "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "data": "synthetic (seeded initial state, no dataset)",
+            "config": desc,
+            "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
+                             "sample": "one Newton iteration of the time-stepping sequence per step (assembly on "
+                                       "%d threads, BiCGSTAB + %s to 1e-10)" % (threads, rep["precond"]),
+                             "cpu": rep.get("cpu", "")},
+            "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "detail": {"assembly_seconds": rep["assembly_seconds"], "solve_seconds": rep["solve_seconds"],
+                       "krylov_iterations": rep["krylov_iterations"]}}
     print(json.dumps(line), flush=True)
 
 
+# ----------------------------------------------------------------------------- serving
 def run_serving(dcgpu, n_requests, lam, max_active, precision, seed=20261203, budget=64 << 30):
     """Poisson stream of random requests through the request server; returns latency
     percentiles and the aggregate DOF x Newton-step throughput."""
@@ -261,56 +288,7 @@ def run_serving(dcgpu, n_requests, lam, max_active, precision, seed=20261203, bu
             "mix": "2D N log-U[32,160] / 3D N log-U[12,32], 1-2 compartments, 1-8 species, 10-40 IE steps"}
 
 
-def large_spmv(dcgpu, precision, peak_gbs, n=128, spmv="auto"):
-    """SpMV roofline on an operator far larger than L2: the 3D cross-diffusion workload
-    (n^3 cubes x 6 tetrahedra, 3 species, ~6.4 M DOF at n = 128), one Alexander2 step with
-    per-kernel events; returns the fused-SpMV achieved bandwidth against the HBM peak."""
-    import workloads as W
-    ini, init = W.cross_diffusion_3d(n=n, steps=1, dt=0.01)
-    vb = 4 if precision == "mixed" else 8
-
-    def one(single):
-        m = dcgpu.Model(ini, {"model.time_step_operator.linear_solver.spmv": spmv,
-                              "model.time_step_operator.linear_solver.single_launch": single})
-        if precision == "mixed":
-            m.set_mixed_precision(True)
-        m.set_state(m.seeded_state(init), 0.0)
-        m.step(0.01)  # first step: tuner, graphs
-        m.profile(True)
-        info = m.step(0.01)
-        kt = m.kernel_times()
-        m.profile(False)
-        fmt = m.spmv_format()
-        mi = m.info
-        m.close()
-        return info, kt, fmt, mi
-
-    # per-phase launches: the fused SpMV kernel timed on its own
-    info, kt, fmt, mi = one("false")
-    ms, calls = kt["spmv"]
-    alg = spmv_bytes(mi["n_dof"], mi["n_blocks"], mi["block_size"], mi["n_block_rows"], vb)
-    avg = ms * 1e-3 / max(calls, 1)
-    ach = alg / avg / 1e9 if avg > 0 else 0.0
-    out = {"workload": "cross_diffusion_3d_%d^3x6_tets_3_species" % n, "dof": mi["n_dof"],
-           "blocks": mi["n_blocks"], "block_size": mi["block_size"], "precision": precision,
-           "spmv_layout": fmt["format"], "tuner_us": {"bsr": fmt["bsr_us"], "sell": fmt["sell_us"]},
-           "algorithmic_bytes_per_launch": alg, "avg_launch_us": avg * 1e6, "launches": calls,
-           "achieved": ach, "peak": peak_gbs, "unit": "GB/s", "frac": ach / peak_gbs,
-           "newton_iterations": info["newton_iterations"], "krylov_iterations": info["linear_iterations"]}
-    # single-launch solve: whole BiCGSTAB iterations on the same operator
-    info, kt, fmt, mi = one("true")
-    ms, iters = kt["krylov_iteration"]
-    if iters:
-        alg = krylov_iteration_bytes(mi["n_dof"], mi["n_blocks"], mi["block_size"], mi["n_block_rows"], vb)
-        avg = ms * 1e-3 / iters
-        ach = alg / avg / 1e9 if avg > 0 else 0.0
-        out["single_launch_iteration"] = {
-            "algorithmic_bytes_per_iteration": alg, "avg_iteration_us": avg * 1e6, "iterations": iters,
-            "achieved": ach, "peak": peak_gbs, "unit": "GB/s", "frac": ach / peak_gbs,
-            "spmv_layout": fmt["format"]}
-    return out
-
-
+# ----------------------------------------------------------------------------- roofline
 def spmv_bytes(ndof, nnzb, bs, nrows, vbytes):
     """Algorithmic bytes of one fused BiCGSTAB SpMV launch: BSR values + block column
     indices + row pointers + x read once + y written once + the dot-product partner
@@ -328,14 +306,119 @@ def krylov_iteration_bytes(ndof, nnzb, bs, nrows, vbytes):
             + 2 * nrows * bs * bs * vbytes)
 
 
-def assembly_bytes(ne, nl, ns, ndof, nnz, jac):
-    """Algorithmic bytes of one residual (+ Jacobian) assembly pass: cell vertex and node
-    indices, vertex coordinates and coefficients gathered once per cell, residual written
-    once, Jacobian values written once (colour-ordered, no read-back)."""
-    b = ne * (nl * 4 * 2 + nl * ns * 8) + ndof * 8
-    if jac:
-        b += nnz * 8 + ne * nl * nl * 4
-    return b
+def load_counters(workload):
+    """ncu counters per unit of work, committed as profiles/counters_<workload>.txt: lines
+    `<category> <counter> <value per unit> <unit>` (comment lines start with '#')."""
+    out = {}
+    path = os.path.join(ROOT, "profiles", "counters_%s.txt" % workload)
+    if not os.path.exists(path):
+        return out
+    for line in open(path):
+        line = line.strip()
+        if not line or line.startswith("#"):
+            continue
+        parts = line.split()
+        if len(parts) >= 4:
+            out.setdefault(parts[0], {})[parts[1]] = (float(parts[2]), parts[3])
+    return out
+
+
+def roofline_for(name, ms, calls, geo, peaks, counters):
+    """Roofline object of one kernel category.  Assembly passes are bound by the FP64 pipe
+    (their arithmetic intensity far exceeds GB300's FP64 flop/byte balance): achieved = FP64
+    flops per launch (ncu's executed DFMA x 2 + DADD + DMUL per cell, from the committed
+    counters) / average launch time, against the FP64 FMA rate measured in this run.  Krylov
+    and SpMV are bound by HBM: achieved = algorithmic bytes per launch / average launch
+    time, against the measured HBM copy bandwidth."""
+    avg_s = ms * 1e-3 / max(calls, 1)
+    c = counters.get(name, {})
+    if name.startswith("assembly"):
+        per_cell = c.get("fp64_flops", (None, None))[0]
+        flops = per_cell * geo["cells"] if per_cell is not None else None
+        achieved = flops / avg_s / 1e12 if (flops and avg_s > 0) else None
+        dram = c.get("dram_bytes", (None, None))[0]
+        r = {"kernel": name, "bound": "fp64", "achieved": achieved, "peak": peaks["fp64_tflops"],
+             "unit": "TFLOP/s", "frac": achieved / peaks["fp64_tflops"] if achieved else None,
+             "peak_source": "measured in this run (FMA chains, dc_selftest_fma_peaks)",
+             "traffic": dram * geo["cells"] if dram is not None else None,
+             "work_per_launch": flops, "avg_launch_us": avg_s * 1e6, "launches": calls,
+             "per": "volume assembly pass over all cells (element kernel + gathers)"}
+        return r
+    if name == "krylov_iteration":
+        alg = krylov_iteration_bytes(geo["ndof"], geo["nnzb"], geo["bs"], geo["nrows"], geo["vbytes"])
+        per = "BiCGSTAB iteration inside the single-launch solve"
+    else:
+        alg = spmv_bytes(geo["ndof"], geo["nnzb"], geo["bs"], geo["nrows"], geo["vbytes"])
+        per = "fused SpMV launch"
+    achieved = alg / avg_s / 1e9 if avg_s > 0 else 0.0
+    dram = c.get("dram_bytes", (None, None))[0]
+    return {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+            "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["hbm_source"],
+            "traffic": dram * geo["nnzb"] if dram is not None else None,
+            "algorithmic_bytes_per_launch": alg, "avg_launch_us": avg_s * 1e6, "launches": calls, "per": per}
+
+
+def spmv_phase(dcgpu, ini, init, dt, precision, spmv, peaks, counters, warm_steps=1):
+    """The fused SpMV kernel timed on its own on the headline operator: per-phase launches
+    (linear_solver.single_launch = false), one step after a warm-up step."""
+    m = dcgpu.Model(ini, {"model.time_step_operator.linear_solver.spmv": spmv,
+                          "model.time_step_operator.linear_solver.single_launch": "false"})
+    if precision == "mixed":
+        m.set_mixed_precision(True)
+    m.set_state(m.seeded_state(init), 0.0)
+    d = dt
+    for _ in range(warm_steps):
+        d = m.step(d)["dt_next"]
+    m.profile(True)
+    m.step(d)
+    kt = m.kernel_times()
+    m.profile(False)
+    mi = m.info
+    fmt = m.spmv_format()
+    m.close()
+    geo = {"ndof": mi["n_dof"], "nnzb": mi["n_blocks"], "bs": mi["block_size"], "nrows": mi["n_block_rows"],
+           "vbytes": 4 if precision == "mixed" else 8}
+    ms, calls = kt["spmv"]
+    r = roofline_for("spmv", ms, calls, geo, peaks, counters)
+    r["spmv_layout"] = fmt["format"]
+    r["tuner_us"] = {"bsr": fmt["bsr_us"], "sell": fmt["sell_us"]}
+    return r
+
+
+def secondary(dcgpu, kind, steps, warmup, flush):
+    """Mixed and plain FP64 DOF x Newton-steps/s of another configuration (device-timed
+    steps after warm-up steps, L2 flushed before each)."""
+    import torch
+    ini, init, dt0, _nl, desc = make_workload(kind, 0)
+    out = {"config": desc, "steps": steps, "warmup": warmup}
+    states = {}
+    for prec in ("mixed", "fp64"):
+        m = dcgpu.Model(ini)
+        if prec == "mixed":
+            m.set_mixed_precision(True)
+        m.set_state(m.seeded_state(init), 0.0)
+        d = dt0
+        for _ in range(warmup):
+            d = m.step(d)["dt_next"]
+        tot, newton = 0.0, 0
+        for _ in range(steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            inf = m.step(d)
+            d = inf["dt_next"]
+            tot += inf["device_ms"]
+            newton += inf["newton_iterations"]
+        out[prec] = {"value": m.ndof * newton / (tot * 1e-3), "ms_per_step": tot / steps, "newton_iterations": newton}
+        states[prec] = (m.state(), {nm: m.species_dofs(nm) for nm in m.species})
+        out["config"]["dof"] = m.ndof
+        m.close()
+    import numpy as np
+    xm, idx = states["mixed"]
+    xf, _ = states["fp64"]
+    out["max_species_rel_l2_mixed_vs_fp64"] = max(
+        float(np.linalg.norm(xm[i] - xf[i]) / max(np.linalg.norm(xf[i]), 1e-300)) for i in idx.values())
+    out["speedup_mixed_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    return out
 
 
 def main():
@@ -355,18 +438,35 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("gloo")
 
-    ini, init, dt0, wdesc = make_workload(args.n, args.workload)
+    ini, init, dt0, nl, desc = make_workload(args.workload, args.n)
     single = "true" if args.single_launch == "on" else "false"
     ov = {"model.time_step_operator.linear_solver.spmv": args.spmv,
           "model.time_step_operator.linear_solver.preconditioner.type": args.precond,
           "model.time_step_operator.linear_solver.single_launch": single}
     if args.inner_reduction is not None:
         ov["model.time_step_operator.linear_solver.inner_reduction"] = repr(args.inner_reduction)
+    for kv in args.override:
+        k, v = kv.split("=", 1)
+        ov[k.strip()] = v.strip()
+
+    # measured peaks: FP64 / FP32 FMA rates of this GPU now, HBM copy bandwidth from the
+    # pool's measurement file
+    fp64_tf, fp32_tf = dcgpu.fma_peaks()
+    peaks = {"fp64_tflops": fp64_tf, "fp32_tflops": fp32_tf}
+    try:
+        peaks["hbm_gbs"] = float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"])
+        peaks["hbm_source"] = "measured (MEASURED_PEAKS.json)"
+    except Exception:
+        peaks["hbm_gbs"] = 6800.0
+        peaks["hbm_source"] = "fallback"
+    counters = load_counters(args.workload)
+
     model = dcgpu.Model(ini, ov)
     if args.precision == "mixed":
         model.set_mixed_precision(True)
     x0 = model.seeded_state(init)
     ndof = model.ndof
+    desc["dof"] = ndof
     model.set_state(x0, 0.0)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
 
@@ -456,80 +556,57 @@ def main():
     e2e = {"value": world * ndof * e2e_newton / e2e_t, "unit": METRIC,
            "h2d_bytes_per_step": ndof * 8, "d2h_bytes_per_step": ndof * 8}
 
-    # roofline of the dominant kernel category
-    import json as _j
-    peaks = {}
-    try:
-        peaks = _j.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-        peak_gbs = float(peaks["hbm_gbs"])
-        peak_src = "measured"
-    except Exception:
-        peak_gbs = 6800.0
-        peak_src = "fallback"
+    # roofline of every kernel category; the headline object is the category with the
+    # largest device time
     info_m = model.info
-    bs = info_m["block_size"]
-    nrows = info_m["n_block_rows"]
-    nnzb = info_m["n_blocks"]
-    ne = info_m["n_elements"]
-    vbytes = 4 if args.precision == "mixed" else 8
-    cats = {}
-    for name, (ms, calls) in kt.items():
-        if calls:
-            cats[name] = (ms, calls)
-    def cat_roof(name):
-        ms, calls = cats.get(name, (0.0, 1))
-        avg_s = ms * 1e-3 / max(calls, 1)
-        if name == "spmv":
-            alg = spmv_bytes(ndof, nnzb, bs, nrows, vbytes)
-        elif name == "krylov_iteration":
-            alg = krylov_iteration_bytes(ndof, nnzb, bs, nrows, vbytes)
-        elif name == "assembly":
-            alg = assembly_bytes(ne, wdesc["nl"], wdesc["species"], ndof, nnzb * bs * bs, jac=True)
-        else:
-            alg = nrows * bs * bs * vbytes + 2 * ndof * vbytes
-        achieved = alg / avg_s / 1e9 if avg_s > 0 else 0.0
-        r = {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": peak_gbs, "unit": "GB/s",
-             "frac": achieved / peak_gbs, "peak_source": peak_src, "traffic": None,
-             "algorithmic_bytes_per_launch": alg, "avg_launch_us": avg_s * 1e6, "launches": calls}
-        if name == "krylov_iteration":
-            # one cooperative launch runs a whole solve: bytes and time are per iteration
-            r["per"] = "BiCGSTAB iteration inside k_bicgstab_fused"
-        return r
-
-    dom = max(cats, key=lambda k: cats[k][0]) if cats else "spmv"
-    roof = cat_roof(dom)
-    roof["category_ms"] = {k: v[0] for k, v in cats.items()}
-    roof["category_launches"] = {k: v[1] for k, v in cats.items()}
-    roof["by_category"] = {k: cat_roof(k) for k in cats}
+    geo = {"ndof": ndof, "nnzb": info_m["n_blocks"], "bs": info_m["block_size"], "nrows": info_m["n_block_rows"],
+           "cells": info_m["n_elements"], "vbytes": 4 if args.precision == "mixed" else 8}
+    cats = {k: v for k, v in kt.items() if v[1] and k != "assembly"}
+    by_cat = {k: roofline_for(k, v[0], v[1], geo, peaks, counters) for k, v in cats.items()}
+    dom = max(cats, key=lambda k: cats[k][0]) if cats else "krylov_iteration"
+    roof = dict(by_cat.get(dom, {}))
+    roof["category_ms"] = {k: v[0] for k, v in kt.items()}
+    roof["category_launches"] = {k: v[1] for k, v in kt.items()}
+    roof["by_category"] = by_cat
+    if not args.no_spmv_phase:
+        roof["spmv_fused_kernel"] = spmv_phase(dcgpu, ini, init, dt0, args.precision, args.spmv, peaks, counters)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(ini, init, dt0, wdesc)
-    roof["spmv_layout"] = model.spmv_format()
-    if args.large_n > 0:
-        roof["spmv_hbm_resident"] = large_spmv(dcgpu, args.precision, peak_gbs, args.large_n, args.spmv)
+        try:
+            cpu = cpu_baseline(args.workload, args.n, args.cpu_iterations, args.cpu_precond)
+        except Exception as e:
+            cpu = {"unavailable": str(e)}
+    sec = None
+    if not args.no_secondary and args.workload == "cross_diffusion_3d":
+        sec = {"gray_scott_512": secondary(dcgpu, "gray_scott", 10, 3, flush),
+               "two_compartment_1024": secondary(dcgpu, "two_compartment", 3, 2, flush)}
     serving = None
     if args.serve_requests > 0:
         served = run_serving(dcgpu, args.serve_requests, 50.0, args.serve_active, args.precision)
         alone = run_serving(dcgpu, args.serve_requests, 50.0, 1, "fp64")
         serving = {"served_concurrent": served, "plain_fp64_one_at_a_time": alone,
                    "speedup": served["value"] / alone["value"] if alone["value"] > 0 else None}
+    # `config` names the workload only (the reference arm prints the same dict); how this
+    # arm ran it is under "run"
+    config = workload_desc(args.workload, args.n)
+    config["dof"] = ndof
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f64+f32",
             "data": "synthetic (seeded initial state, no dataset)",
-            "config": {"workload": wdesc["workload"], "mesh": wdesc["mesh"], "dof": ndof,
-                       "species": wdesc["species"], "scheme": "Alexander2", "dt": dt0, "precision": args.precision,
-                       "linear_solver": "BiCGSTAB+%s to 1e-10 (direct-solve semantics)"
-                                        % ("block-Jacobi" if args.precond == "Jacobi" else "aggregation-AMG"),
-                       "spmv_layout": model.spmv_format()["format"],
-                       "krylov_launch": "single cooperative launch per solve" if single == "true"
-                                        else "one launch per phase, CUDA graph of 8 iterations",
-                       "newton_rel_tol_sq": 1e-10, "l2_flush": "256 MiB write between timed steps",
-                       "newton_iterations": newton, "krylov_iterations": linear},
+            "config": config,
+            "run": {"precision": args.precision,
+                    "linear_solver": "BiCGSTAB+%s to 1e-10 (direct-solve semantics)"
+                                     % ("block-Jacobi" if args.precond == "Jacobi" else "aggregation-AMG"),
+                    "l2_flush": "inputs larger than L2, and a 256 MiB write between timed steps",
+                    "newton_iterations": newton, "krylov_iterations": linear,
+                    "spmv_layout": model.spmv_format()["format"],
+                    "krylov_launch": "single cooperative launch per solve" if single == "true"
+                                     else "one launch per phase, CUDA graph of 8 iterations"},
             "plain_fp64": plain,
             "speedup_vs_plain_fp64": (value / plain["value"]) if plain else None,
-            "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
-            "serving": serving}
+            "e2e": e2e, "roofline": roof, "peaks": peaks, "cpu_baseline": cpu, "clocks": clk,
+            "gpu_launches": launches, "secondary": sec, "serving": serving}
     if rank == 0:
         print(json.dumps(line), flush=True)
     model.close()

@@ -478,6 +478,17 @@ int dc_selftest_barrier_timeout(double* gave_up_blocks, double* elapsed_ms) {
   });
 }
 
+int dc_selftest_fma_peaks(double* fp64_tflops, double* fp32_tflops) {
+  return guarded([&] {
+    if (!fp64_tflops || !fp32_tflops) throw std::invalid_argument("null argument");
+    int dev_count = 0;
+    dcgpu::cuda_check(cudaGetDeviceCount(&dev_count), "cudaGetDeviceCount");
+    if (dev_count == 0) throw dcgpu::CudaError("no CUDA device");
+    if (dcgpu::fma_peaks(fp64_tflops, fp32_tflops) != 0) throw dcgpu::CudaError("FMA throughput probe failed");
+    return DC_OK;
+  });
+}
+
 int dc_profile_enable(dc_model* model, int enabled) {
   return guarded([&] {
     if (!model) throw std::invalid_argument("null argument");

@@ -87,6 +87,9 @@ void fused_bicgstab(int bs, bool sell, int blocks, const FusedBicgArgs<T, V>& a,
 // must give up and flag it.  Returns non-zero on a CUDA error; gave_up_blocks receives the
 // number of blocks that flagged, elapsed_ms the kernel's duration.
 int barrier_selftest(double* gave_up_blocks, double* elapsed_ms);
+// FP64 / FP32 fused multiply-add throughput of the current device in TFLOP/s (peaks.cu);
+// returns non-zero on a CUDA failure
+int fma_peaks(double* fp64_tflops, double* fp32_tflops);
 
 template <class T>
 struct KrylovVectors {

@@ -909,7 +909,7 @@ void Solver::one_step(double dt) {
       model.constrain_jacobian(J_.get(), stream);
     };
     auto jac = [&](const double* y) {
-      tbegin(0);
+      tbegin(4);
       jac_sell_fresh_ = model.assemble(y, ti, ai, bi, nullptr, J_.get(), 2 | jmode, stream, jac_sell_target());
       tend();
       finish_jac();
@@ -917,7 +917,7 @@ void Solver::one_step(double dt) {
     };
     auto resjac = [&](const double* y, double* r) {
       cuda_check(cudaMemcpyAsync(r, const_.get(), n_ * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");
-      tbegin(0);
+      tbegin(5);
       jac_sell_fresh_ = model.assemble(y, ti, ai, bi, r, J_.get(), 3 | jmode, stream, jac_sell_target());
       tend();
       model.constrain_residual(r, stream);

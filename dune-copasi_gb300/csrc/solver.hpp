@@ -95,10 +95,13 @@ class Solver {
   // solver's stream: 0 = assembly (all colour launches of one operator evaluation),
   // 1 = SpMV (fp64 and fp32), 2 = preconditioner apply,
   // 3 = single-launch BiCGSTAB solves, whose `calls` count the Krylov ITERATIONS they ran
-  static constexpr int kTimerCategories = 4;
+  // 0 = residual-only assembly passes, 1 = SpMV, 2 = preconditioner, 3 = single-launch
+  // BiCGSTAB iterations, 4 = Jacobian-only assembly passes, 5 = combined residual + Jacobian
+  // assembly passes
+  static constexpr int kTimerCategories = 6;
   struct KernelTimes {
-    double ms[kTimerCategories] = {0, 0, 0, 0};
-    long long calls[kTimerCategories] = {0, 0, 0, 0};
+    double ms[kTimerCategories] = {};
+    long long calls[kTimerCategories] = {};
   };
   void enable_profiling(bool on);
   KernelTimes kernel_times;

@@ -35,7 +35,7 @@ EXPORTED = [
     "dc_assemble_residual_noalloc", "dc_server_create", "dc_server_submit", "dc_server_poll",
     "dc_server_take_state", "dc_server_estimate", "dc_server_destroy", "dc_last_error",
     "dc_spmv_format", "dc_vertex_coords", "dc_constraints", "dc_reduce", "dc_write_vtk", "dc_config_get",
-    "dc_selftest_barrier_timeout", "dc_step_stage_newton",
+    "dc_selftest_barrier_timeout", "dc_step_stage_newton", "dc_selftest_fma_peaks",
 ]
 
 
@@ -98,6 +98,7 @@ def load_library(path=LIB_PATH):
     lib.dc_model_create.argtypes = [ctypes.c_char_p, ctypes.c_char_p, P(vp)]
     lib.dc_model_destroy.argtypes = [vp]
     lib.dc_step_stage_newton.argtypes = [vp, P(ctypes.c_int32), sz, P(sz)]
+    lib.dc_selftest_fma_peaks.argtypes = [pd, pd]
     lib.dc_model_info_get.argtypes = [vp, P(ModelInfo)]
     lib.dc_species_name.argtypes = [vp, i32, ctypes.c_char_p, sz]
     lib.dc_species_size.argtypes = [vp, i32, P(ctypes.c_int64)]
@@ -468,13 +469,19 @@ class Model:
         _check(self._lib.dc_profile_enable(self._h, 1 if enabled else 0))
 
     def kernel_times(self):
-        """{category: (total ms, launches)} for assembly, spmv, precond and krylov_iteration
-        (single-launch BiCGSTAB solves; its count is the Krylov iterations they ran)."""
-        names = ("assembly", "spmv", "precond", "krylov_iteration")
+        """{category: (total ms, launches)} for assembly (all passes), spmv, precond,
+        krylov_iteration (single-launch BiCGSTAB solves; its count is the Krylov iterations
+        they ran) and the assembly passes by kind: assembly_residual, assembly_jacobian,
+        assembly_combined."""
+        names = ("assembly_residual", "spmv", "precond", "krylov_iteration", "assembly_jacobian",
+                 "assembly_combined")
         ms = np.zeros(len(names))
         calls = np.zeros(len(names), np.int64)
         _check(self._lib.dc_profile_get(self._h, _ptr(ms), _ptr(calls, ctypes.c_int64), len(names)))
-        return {k: (float(ms[i]), int(calls[i])) for i, k in enumerate(names)}
+        out = {k: (float(ms[i]), int(calls[i])) for i, k in enumerate(names)}
+        parts = ("assembly_residual", "assembly_jacobian", "assembly_combined")
+        out["assembly"] = (sum(out[k][0] for k in parts), sum(out[k][1] for k in parts))
+        return out
 
     def spmv_format(self):
         """Layout of the fp32 Krylov operator and the tuner's SpMV times:
@@ -488,6 +495,15 @@ class Model:
 
 def launch_count():
     return int(load_library().dc_launch_count())
+
+
+def fma_peaks():
+    """(FP64, FP32) fused multiply-add throughput of the current device in TFLOP/s."""
+    lib = load_library()
+    d = ctypes.c_double(0.0)
+    f = ctypes.c_double(0.0)
+    _check(lib.dc_selftest_fma_peaks(ctypes.byref(d), ctypes.byref(f)))
+    return d.value, f.value
 
 
 def selftest_barrier_timeout():

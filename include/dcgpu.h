@@ -160,8 +160,10 @@ int dc_expr_eval(const char* expression, const char* context_ini, const char* co
  * counters of LinearSolver / TimeStep, model/make_step_operator.hh:104-139):
  * the CUDA stream the model launches on (cudaStream_t as void*), the number of kernels
  * this library has launched, and per-category device times measured with CUDA events
- * (0 = assembly, 1 = SpMV, 2 = preconditioner apply, 3 = single-launch BiCGSTAB solves,
- * whose call count is the number of Krylov iterations they ran) while profiling is enabled. */
+ * (0 = residual-only assembly passes, 1 = SpMV, 2 = preconditioner apply, 3 = single-launch
+ * BiCGSTAB solves, whose call count is the number of Krylov iterations they ran,
+ * 4 = Jacobian-only assembly passes, 5 = combined residual + Jacobian assembly passes)
+ * while profiling is enabled. */
 int dc_stream_handle(const dc_model* model, void** stream);
 int64_t dc_launch_count(void);
 
@@ -170,6 +172,10 @@ int64_t dc_launch_count(void);
  * limit).  Every block's wait must give up and flag it; *gave_up_blocks receives how many did
  * and *elapsed_ms the kernel's duration.  The CUDA context stays usable afterwards. */
 int dc_selftest_barrier_timeout(double* gave_up_blocks, double* elapsed_ms);
+/* Arithmetic throughput of the current device (no reference counterpart; instrumentation
+ * for the roofline of the FP64-bound assembly): FP64 and FP32 fused multiply-add rates in
+ * TFLOP/s (2 flops per FMA), measured with independent FMA chains on every SM (~20 ms). */
+int dc_selftest_fma_peaks(double* fp64_tflops, double* fp32_tflops);
 int dc_profile_enable(dc_model* model, int enabled);
 int dc_profile_get(const dc_model* model, double* ms, int64_t* calls, int32_t n_categories);
 

@@ -601,6 +601,7 @@ def main():
                     "l2_flush": "inputs larger than L2, and a 256 MiB write between timed steps",
                     "newton_iterations": newton, "krylov_iterations": linear,
                     "spmv_layout": model.spmv_format()["format"],
+                    "volume_kernels": model.jit_status(),
                     "krylov_launch": "single cooperative launch per solve" if single == "true"
                                      else "one launch per phase, CUDA graph of 8 iterations"},
             "plain_fp64": plain,

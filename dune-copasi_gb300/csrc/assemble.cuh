@@ -11,6 +11,8 @@
 
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "device.cuh"
 
 namespace dcgpu {
@@ -38,6 +40,13 @@ struct JacobianGatherOut {
 void launch_gather_jacobian(double* J, int bs, int nslot, const int32_t* slot_pos, int64_t block_begin,
                             int64_t nblocks, const int64_t* ptr, const int32_t* list, const double* ej, bool f32,
                             cudaStream_t stream, const JacobianGatherOut& out = JacobianGatherOut{});
+// The covering gather for a compartment whose dynamic slots are only some of the bs x bs
+// entries of each block: every entry of every block of [block_begin, block_begin + nblocks)
+// becomes base (out.overwrite's base, or zero) plus its dynamic slot's element values (slot m
+// sits at entry slot_pos_host[m]); out.sell, when set, receives the fp32 copy.
+void launch_gather_jacobian_full(double* J, int bs, int nslot, const std::vector<int32_t>& slot_pos_host,
+                                 int64_t block_begin, int64_t nblocks, const int64_t* ptr, const int32_t* list,
+                                 const double* ej, bool f32, cudaStream_t stream, const JacobianGatherOut& out);
 // J[diag[i]] block gets identity in the padded slots s >= ns_of_row (rows of compartments
 // with fewer species than the block size)
 void launch_pad_identity(const int32_t* diag, const int8_t* row_ns, int nrows, int bs, double* J,

@@ -478,6 +478,15 @@ int dc_selftest_barrier_timeout(double* gave_up_blocks, double* elapsed_ms) {
   });
 }
 
+int dc_model_jit_status(const dc_model* model, char* buf, size_t len) {
+  return guarded([&] {
+    if (!model || !buf || len == 0) throw std::invalid_argument("null argument");
+    std::strncpy(buf, model->model->jit_status.c_str(), len - 1);
+    buf[len - 1] = '\0';
+    return DC_OK;
+  });
+}
+
 int dc_selftest_fma_peaks(double* fp64_tflops, double* fp32_tflops) {
   return guarded([&] {
     if (!fp64_tflops || !fp32_tflops) throw std::invalid_argument("null argument");

@@ -120,14 +120,52 @@ Model::Model(const std::string& ini_text, const std::string& overrides) {
   build_face_groups();
   build_static_matrices();
   build_constraints();
+  setup_volume_jit();
+}
+
+// model.assembly.jit = auto | true | false: the compartments' volume kernels compiled at
+// set-up for their own programs (volume_jit.hpp); auto compiles them for compartments of at
+// least kJitAutoCells cells, where the compilation (about a second) is small against the
+// assembly time it saves.  Without NVRTC, or when a compilation fails, the interpreter
+// kernels stay in use (jit_status says why); `true` makes that a configuration error.
+void Model::setup_volume_jit() {
+  constexpr int64_t kJitAutoCells = int64_t{1} << 18;
+  const std::string mode = cfg.get("model.assembly.jit", "auto");
+  if (mode != "auto" && mode != "true" && mode != "false")
+    throw ConfigError("model.assembly.jit must be auto, true or false");
+  jit_status = "off";
+  if (mode == "false" || numerical_jacobian) return;
+  for (auto& g : vgroups) {
+    if (mode == "auto" && g.ne < kJitAutoCells) continue;
+    JitVolumeInput in;
+    in.dim = dim;
+    in.ns = g.ns;
+    in.species_offset = species_offset[g.comp];
+    in.n_slots = g.slots_dyn;
+    in.all_mass = g.dyn_all_mass;
+    in.prog_res = &g.prog_res.host;
+    in.prog_all = &g.prog_all.host;
+    in.res_terms_r = &g.res_terms_r;
+    in.res_terms_a = &g.res_terms_a;
+    in.jac_terms = &g.jac_terms;
+    std::string why;
+    g.jit = build_volume_jit(in, &why);
+    if (!g.jit) {
+      if (mode == "true") throw ConfigError("model.assembly.jit = true: " + why);
+      jit_status = "interpreter (" + why + ")";
+      for (auto& h : vgroups) h.jit.reset();
+      return;
+    }
+    jit_status = "compiled";
+  }
 }
 
 // uniform skip flags of the volume kernel for one program and its term lists, and the
 // number of per-element Jacobian coefficients of the terms (k_volume's shared-memory size:
 // NQ point weights + one for mass-type terms, 1 for scalar diffusion, dim^2 for tensor
 // diffusion, (dim + 1) dim for the vector terms)
-static void set_volume_flags(VolumeParams& p, const Program& prog, const std::vector<Term>& res,
-                             const std::vector<Term>& jac, int dim) {
+void set_volume_flags(VolumeParams& p, const Program& prog, const std::vector<Term>& res, const std::vector<Term>& jac,
+                      int dim) {
   const int nq = dim == 2 ? 3 : 4;
   p.ncoef = 0;
   for (const Term& T : jac) {
@@ -855,7 +893,8 @@ void Model::build_volume_groups() {
       if (coef > kMaxCoefficients) throw ConfigError("too many Jacobian terms in one compartment");
       // Jacobian slots: one per distinct (test, trial) pair, terms sorted by slot so the
       // volume kernel writes each slot of each local pair once
-      auto assign_slots = [&](std::vector<Term>& terms, int& nslot, bool& all_mass, DeviceBuffer<int32_t>& pos) {
+      auto assign_slots = [&](std::vector<Term>& terms, int& nslot, bool& all_mass, DeviceBuffer<int32_t>& pos,
+                              std::vector<int32_t>* host_pos) {
         std::map<std::pair<int, int>, int> idx;
         std::vector<int32_t> p;
         all_mass = true;
@@ -873,9 +912,10 @@ void Model::build_volume_groups() {
         std::stable_sort(terms.begin(), terms.end(), [](const Term& a, const Term& b) { return a.slot < b.slot; });
         nslot = static_cast<int>(p.size());
         pos.upload(p);
+        if (host_pos) *host_pos = p;
       };
-      if (pass == 0) assign_slots(jterms, g.slots_static, g.static_all_mass, g.slot_pos_static);
-      if (pass == 2) assign_slots(jterms, g.slots_dyn, g.dyn_all_mass, g.slot_pos_dyn);
+      if (pass == 0) assign_slots(jterms, g.slots_static, g.static_all_mass, g.slot_pos_static, nullptr);
+      if (pass == 2) assign_slots(jterms, g.slots_dyn, g.dyn_all_mass, g.slot_pos_dyn, &g.slot_pos_dyn_host);
       if (pass == 0) {
         g.prog_static.host = pb.finish();
         g.static_terms = jterms;
@@ -1161,14 +1201,15 @@ bool Model::assemble(const double* x, double t, double cm, double ca, double* r,
       if (use_k) spmv_acc(A0, d_Ks.get(), x, r, ca, s);
     }
   }
-  // one compartment whose state-dependent gather covers every Jacobian entry: that gather
-  // takes the static operator as its base (no copy of it into J first) and, with nothing
-  // added to J after it, also writes the fp32 SELL-32 copy
+  // one compartment whose state-dependent gather covers every block of J: that gather takes
+  // the static operator as its base (no copy of it into J first) and, with nothing added to J
+  // after it, also writes the fp32 SELL-32 copy; when only some species pairs have dynamic
+  // terms, a gather over every entry of every block (launch_gather_jacobian_full) does it
   const VolumeGroup* cover = nullptr;
   if ((mode & 2) && J && (mode & kAssembleOverwriteJacobian) && !numerical_jacobian && vgroups.size() == 1) {
     const VolumeGroup& g = vgroups[0];
     const bool active = (cm != 0.0 && g.has_mass) || (ca != 0.0 && g.has_stiffness);
-    if (active && g.slots_dyn == bs * bs && g.block_begin == 0 && g.nblocks == nnzb()) cover = &g;
+    if (active && g.slots_dyn > 0 && g.block_begin == 0 && g.nblocks == nnzb()) cover = &g;
   }
   JacobianGatherOut gout;
   if (cover) {
@@ -1238,12 +1279,18 @@ bool Model::assemble(const double* x, double t, double cm, double ca, double* r,
     }
     // two-phase: element outputs for all cells of the compartment in one launch, then the
     // per-node / per-block gathers (fixed order, no atomics, no colouring)
-    launch_volume(dim, g.ns, p, 0, ne, mode, s);
+    if (g.jit) launch_volume_jit(*g.jit, p, 0, ne, mode, s);
+    else launch_volume(dim, g.ns, p, 0, ne, mode, s);
     if ((mode & 1) && r)
       launch_gather_residual(r, bs, g.ns, g.node_begin, g.nnodes, g.rlist_ptr.get(), g.rlist.get(), d_er.get(), s);
-    if ((mode & 2) && J && g.slots_dyn > 0)
-      launch_gather_jacobian(J, bs, g.slots_dyn, g.slot_pos_dyn.get(), g.block_begin, g.nblocks, g.blist_ptr.get(),
-                             g.blist.get(), d_ej.get(), jac_f32, s, &g == cover ? gout : JacobianGatherOut{});
+    if ((mode & 2) && J && g.slots_dyn > 0) {
+      if (&g == cover && g.slots_dyn < bs * bs)
+        launch_gather_jacobian_full(J, bs, g.slots_dyn, g.slot_pos_dyn_host, g.block_begin, g.nblocks,
+                                    g.blist_ptr.get(), g.blist.get(), d_ej.get(), jac_f32, s, gout);
+      else
+        launch_gather_jacobian(J, bs, g.slots_dyn, g.slot_pos_dyn.get(), g.block_begin, g.nblocks, g.blist_ptr.get(),
+                               g.blist.get(), d_ej.get(), jac_f32, s, &g == cover ? gout : JacobianGatherOut{});
+    }
   }
   if (ca != 0.0) {
     for (const auto& g : fgroups) {

@@ -25,6 +25,7 @@
 #include "ini.hpp"
 #include "linalg.cuh"
 #include "mesh.hpp"
+#include "volume_jit.hpp"
 
 namespace dcgpu {
 
@@ -116,9 +117,11 @@ struct VolumeGroup {
   int slots_static = 0, slots_dyn = 0;
   bool static_all_mass = false, dyn_all_mass = false;
   DeviceBuffer<int32_t> slot_pos_static, slot_pos_dyn;     // test * bs + trial per slot
+  std::vector<int32_t> slot_pos_dyn_host;
   int64_t node_begin = 0, nnodes = 0, block_begin = 0, nblocks = 0;
   DeviceBuffer<int64_t> rlist_ptr, blist_ptr;
   DeviceBuffer<int32_t> rlist, blist;                     // k * nl + a ; (k * nl + a) * nl + b
+  std::shared_ptr<const JitVolume> jit;                   // run-time compiled kernels, or null
 };
 
 struct FaceGroup {
@@ -132,6 +135,11 @@ struct FaceGroup {
   std::vector<Term> terms[2];
   DeviceBuffer<Term> d_terms[2];
 };
+
+// uniform skip flags of the volume kernel for one program and its term lists, and the
+// number of per-element Jacobian coefficients of the terms
+void set_volume_flags(VolumeParams& p, const Program& prog, const std::vector<Term>& res, const std::vector<Term>& jac,
+                      int dim);
 
 class Model {
  public:
@@ -150,6 +158,9 @@ class Model {
   std::vector<int> species_offset;              // global index of the first species of each compartment
   bool is_linear = false;
   bool numerical_jacobian = false;
+  // volume kernels: "compiled" (run-time compiled for the model's programs), "off", or
+  // "interpreter (<reason>)" when the compilation was asked for and could not be had
+  std::string jit_status = "off";
   double fd_eps = 1e-7;
   int bs = 1;
 
@@ -251,6 +262,7 @@ class Model {
   void upload_geometry();
   void build_static_matrices();
   void build_constraints();
+  void setup_volume_jit();
 };
 
 }  // namespace dcgpu

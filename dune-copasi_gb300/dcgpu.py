@@ -35,7 +35,8 @@ EXPORTED = [
     "dc_assemble_residual_noalloc", "dc_server_create", "dc_server_submit", "dc_server_poll",
     "dc_server_take_state", "dc_server_estimate", "dc_server_destroy", "dc_last_error",
     "dc_spmv_format", "dc_vertex_coords", "dc_constraints", "dc_reduce", "dc_write_vtk", "dc_config_get",
-    "dc_selftest_barrier_timeout", "dc_step_stage_newton", "dc_selftest_fma_peaks",
+    "dc_selftest_barrier_timeout", "dc_step_stage_newton", "dc_selftest_fma_peaks", "dc_jit_selftest",
+    "dc_model_jit_status",
 ]
 
 
@@ -99,6 +100,8 @@ def load_library(path=LIB_PATH):
     lib.dc_model_destroy.argtypes = [vp]
     lib.dc_step_stage_newton.argtypes = [vp, P(ctypes.c_int32), sz, P(sz)]
     lib.dc_selftest_fma_peaks.argtypes = [pd, pd]
+    lib.dc_jit_selftest.argtypes = [ctypes.c_char_p, sz]
+    lib.dc_model_jit_status.argtypes = [vp, ctypes.c_char_p, sz]
     lib.dc_model_info_get.argtypes = [vp, P(ModelInfo)]
     lib.dc_species_name.argtypes = [vp, i32, ctypes.c_char_p, sz]
     lib.dc_species_size.argtypes = [vp, i32, P(ctypes.c_int64)]
@@ -364,6 +367,12 @@ class Model:
         out["newton_per_stage"] = self.stage_newton()
         return out
 
+    def jit_status(self):
+        """"compiled", "off" or "interpreter (<reason>)": the model's volume kernels."""
+        buf = ctypes.create_string_buffer(4096)
+        _check(self._lib.dc_model_jit_status(self._h, buf, len(buf)))
+        return buf.value.decode()
+
     def stage_newton(self):
         """Newton iterations of every stage solve of the last step (dc_step_stage_newton)."""
         n = ctypes.c_size_t()
@@ -495,6 +504,14 @@ class Model:
 
 def launch_count():
     return int(load_library().dc_launch_count())
+
+
+def jit_selftest():
+    """(ok, message) of the run-time compilation self-test (NVRTC, no GPU needed)."""
+    lib = load_library()
+    buf = ctypes.create_string_buffer(8192)
+    st = lib.dc_jit_selftest(buf, len(buf))
+    return st == DC_OK, buf.value.decode()
 
 
 def fma_peaks():

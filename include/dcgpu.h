@@ -172,6 +172,16 @@ int64_t dc_launch_count(void);
  * limit).  Every block's wait must give up and flag it; *gave_up_blocks receives how many did
  * and *elapsed_ms the kernel's duration.  The CUDA context stays usable afterwards. */
 int dc_selftest_barrier_timeout(double* gave_up_blocks, double* elapsed_ms);
+/* Run-time compilation self-test (no reference counterpart; needs no GPU): generates the
+ * volume kernels of a synthetic two-species compartment whose terms cover every volume term
+ * kind, in 2D and 3D, and compiles them with NVRTC for sm_103a.  Returns DC_OK, or
+ * DC_ERR_CONFIG with the reason in `message` (NVRTC missing, compilation log). */
+int dc_jit_selftest(char* message, size_t len);
+/* Volume kernels of the model (no reference counterpart): copies "compiled" (kernels
+ * compiled at set-up for the model's expression programs), "off" (the bytecode
+ * interpreter kernels) or "interpreter (<reason>)" into buf.  Set by model.assembly.jit =
+ * auto | true | false (auto: compiled for compartments of at least 2^18 cells). */
+int dc_model_jit_status(const dc_model* model, char* buf, size_t len);
 /* Arithmetic throughput of the current device (no reference counterpart; instrumentation
  * for the roofline of the FP64-bound assembly): FP64 and FP32 fused multiply-add rates in
  * TFLOP/s (2 flops per FMA), measured with independent FMA chains on every SM (~20 ms). */

@@ -204,3 +204,10 @@ def test_engine_unsupported_context_types(dcgpu_lib, typ, msg):
     with pytest.raises(dcgpu_lib.DcError) as ei:
         dcgpu_lib.expr_eval("1", {}, "[parser_context.q]\ntype = %s\n" % typ)
     assert ei.value.status == 4 and msg in str(ei.value)
+
+
+def test_run_time_compilation_selftest(dcgpu_lib):
+    """NVRTC compiles the generated volume kernels of a synthetic compartment that covers
+    every volume term kind, in 2D and 3D (no GPU needed)."""
+    ok, msg = dcgpu_lib.jit_selftest()
+    assert ok, msg

@@ -8,7 +8,7 @@ import pytest
 import cases
 import tiff_files as TF
 from oracle.model import OracleModel
-from test_gpu_parity import STEP_TOL, _run_both
+from test_gpu_parity import STEP_TOL, _run_both, assert_newton_per_stage
 
 pytestmark = pytest.mark.gpu
 
@@ -37,10 +37,10 @@ def test_context_extras_time_stepping_matches_oracle(dcgpu_lib, tmp_path, compre
     ini = cases.context_ini(*_images(tmp_path, compression))
     records = _run_both(dcgpu_lib, ini, None)
     assert records
-    for t, errs, n_o, n_g, stages in records:
+    for t, errs, n_o, n_g in records:
         for name, e in errs.items():
             assert e <= STEP_TOL, (t, name, e)
-        assert abs(n_o - n_g) <= max(1, stages)
+        assert_newton_per_stage(n_o, n_g, (t,))
 
 
 @pytest.mark.parametrize("section,msg", [

@@ -90,15 +90,22 @@ def test_layout_matches_oracle(dcgpu_lib, case):
     gm.close()
 
 
+# model.assembly.jit: "false" runs the bytecode-interpreter volume kernels, "true" the
+# kernels compiled at set-up for each model's programs (NVRTC)
+JIT = ["false", "true"]
+
+
+@pytest.mark.parametrize("jit", JIT)
 @pytest.mark.parametrize("case", sorted(ALL_CASES))
 @pytest.mark.parametrize("form", ["mass", "stiffness"])
-def test_assembly_matches_oracle(dcgpu_lib, case, form):
+def test_assembly_matches_oracle(dcgpu_lib, case, form, jit):
     ini, init = ALL_CASES[case]()
     om = OracleModel(ini)
     rng = np.random.default_rng(11)
     x = _init_state(om, init) + 0.05 * rng.uniform(-1, 1, om.ndof)
     t = 0.0375
-    gm = dcgpu_lib.Model(ini)
+    gm = dcgpu_lib.Model(ini, {"model.assembly.jit": jit})
+    assert gm.jit_status() == ("compiled" if jit == "true" else "off")
     cm, ca = (1.0, 0.0) if form == "mass" else (0.0, 1.0)
     r, J = gm.assemble(x, t, cm, ca)
     r_ref = om.residual(x, t, form)
@@ -151,10 +158,11 @@ def _run_both(dcgpu_lib, ini, init, mixed=False, overrides=None):
     return records
 
 
+@pytest.mark.parametrize("jit", JIT)
 @pytest.mark.parametrize("case", sorted(ALL_CASES))
-def test_time_stepping_matches_oracle(dcgpu_lib, case):
+def test_time_stepping_matches_oracle(dcgpu_lib, case, jit):
     ini, init = ALL_CASES[case]()
-    records = _run_both(dcgpu_lib, ini, init)
+    records = _run_both(dcgpu_lib, ini, init, overrides={"model.assembly.jit": jit})
     assert records
     for t, errs, n_o, n_g in records:
         for name, e in errs.items():
@@ -163,12 +171,13 @@ def test_time_stepping_matches_oracle(dcgpu_lib, case):
 
 
 @pytest.mark.parametrize("case", ["gray_scott", "two_compartment", "cross_diffusion_3d", "features_3d_padded"])
-@pytest.mark.parametrize("fmt", ["auto", "bsr", "sell"])
-def test_mixed_precision_matches_oracle(dcgpu_lib, case, fmt):
+@pytest.mark.parametrize("fmt,jit", [("auto", "false"), ("bsr", "false"), ("sell", "false"), ("auto", "true")])
+def test_mixed_precision_matches_oracle(dcgpu_lib, case, fmt, jit):
     """fp32 BiCGSTAB inside fp64 iterative refinement, with the fp32 operator in BSR or
-    SELL-32 layout or the tuner's choice: same tolerance against the fp64 oracle."""
+    SELL-32 layout or the tuner's choice: same tolerance against the fp64 oracle (and with
+    the run-time compiled volume kernels, whose fp32 Jacobian-only pass this exercises)."""
     ini, init = ALL_CASES[case]()
-    ov = {"model.time_step_operator.linear_solver.spmv": fmt}
+    ov = {"model.time_step_operator.linear_solver.spmv": fmt, "model.assembly.jit": jit}
     records = _run_both(dcgpu_lib, ini, init, mixed=True, overrides=ov)
     for t, errs, n_o, n_g in records:
         for name, e in errs.items():
@@ -249,7 +258,7 @@ def test_iterative_solver_configuration(dcgpu_lib):
     ov = {"model.time_step_operator.linear_solver.type": "BiCGSTAB",
           "model.time_step_operator.nonlinear_solver.convergence_condition.relative_tolerance": "1e-24"}
     records = _run_both(dcgpu_lib, ini, init, overrides=ov)
-    for t, errs, n_o, n_g, stages in records:
+    for t, errs, n_o, n_g in records:
         for e in errs.values():
             assert e <= STEP_TOL
 
@@ -441,10 +450,10 @@ def test_gmsh_grid_matches_oracle(dcgpu_lib, tmp_path, dim):
         assert np.array_equal(gm.species_vertices(sp.name), om.comp_vertices[sp.comp])
     gm.close()
     records = _run_both(dcgpu_lib, ini, None)
-    for t, errs, n_o, n_g, stages in records:
+    for t, errs, n_o, n_g in records:
         for name, e in errs.items():
             assert e <= STEP_TOL, (dim, t, name, e)
-        assert abs(n_o - n_g) <= max(1, stages)
+        assert_newton_per_stage(n_o, n_g, (t,))
 
 
 def test_matrix_free_configuration(dcgpu_lib):
@@ -454,10 +463,10 @@ def test_matrix_free_configuration(dcgpu_lib):
     ini, init = ALL_CASES["features_2d"]()
     ov = {"model.time_step_operator.linear_solver.matrix_free": "true"}
     records = _run_both(dcgpu_lib, ini, init, overrides=ov)
-    for t, errs, n_o, n_g, stages in records:
+    for t, errs, n_o, n_g in records:
         for name, e in errs.items():
             assert e <= STEP_TOL, (t, name, e)
-        assert abs(n_o - n_g) <= max(1, stages)
+        assert_newton_per_stage(n_o, n_g, (t,))
     with pytest.raises(dcgpu_lib.DcError):
         dcgpu_lib.Model(ini, {"model.time_step_operator.linear_solver.matrix_free": "maybe"})
 
@@ -474,7 +483,7 @@ def test_cg_matches_oracle(dcgpu_lib, precond, mixed):
           "model.time_step_operator.linear_solver.preconditioner.coarsen_target": "16",
           "model.time_step_operator.nonlinear_solver.convergence_condition.relative_tolerance": "1e-24"}
     records = _run_both(dcgpu_lib, ini, init, mixed=mixed, overrides=ov)
-    for t, errs, n_o, n_g, stages in records:
+    for t, errs, n_o, n_g in records:
         for e in errs.values():
             assert e <= STEP_TOL, (precond, mixed, t, e)
 
@@ -487,7 +496,7 @@ def test_fp32_and_fp64_jacobian_in_mixed_precision(dcgpu_lib):
     for jp in ("single", "double"):
         ov = {"model.time_step_operator.linear_solver.jacobian_precision": jp}
         records = _run_both(dcgpu_lib, ini, init, mixed=True, overrides=ov)
-        for t, errs, n_o, n_g, stages in records:
+        for t, errs, n_o, n_g in records:
             for e in errs.values():
                 assert e <= STEP_TOL, (jp, t, e)
         finals.append(records[-1][1])
@@ -504,7 +513,7 @@ def test_mixed_inner_reduction(dcgpu_lib, inner):
     ini, init = ALL_CASES["features_2d"]()
     ov = {"model.time_step_operator.linear_solver.inner_reduction": inner}
     records = _run_both(dcgpu_lib, ini, init, mixed=True, overrides=ov)
-    for t, errs, n_o, n_g, stages in records:
+    for t, errs, n_o, n_g in records:
         for e in errs.values():
             assert e <= STEP_TOL, (inner, t, e)
     for bad in ("0", "1", "1e-9"):
@@ -526,7 +535,7 @@ def test_gmres_matches_oracle(dcgpu_lib, restart, precond, mixed):
           "model.time_step_operator.linear_solver.convergence_condition.relative_tolerance": "1e-12",
           "model.time_step_operator.nonlinear_solver.convergence_condition.relative_tolerance": "1e-24"}
     records = _run_both(dcgpu_lib, ini, init, mixed=mixed, overrides=ov)
-    for t, errs, n_o, n_g, stages in records:
+    for t, errs, n_o, n_g in records:
         for e in errs.values():
             assert e <= STEP_TOL, (restart, precond, mixed, t, e)
 
@@ -546,10 +555,10 @@ def test_single_launch_bicgstab_matches_oracle(dcgpu_lib, case, n, mixed, single
     ov = {"model.time_step_operator.linear_solver.single_launch": single}
     records = _run_both(dcgpu_lib, ini, init, mixed=mixed, overrides=ov)
     assert records
-    for t, errs, n_o, n_g, stages in records:
+    for t, errs, n_o, n_g in records:
         for name, e in errs.items():
             assert e <= STEP_TOL, (case, n, t, name, e)
-        assert abs(n_o - n_g) <= max(1, stages)
+        assert_newton_per_stage(n_o, n_g, (t,))
 
 
 @pytest.mark.parametrize("mixed", [False, True])

@@ -147,6 +147,71 @@ __global__ void k_gather_jacobian_full(double* __restrict__ J, unsigned bs2, uns
   if (o.sell) o.sell[o.sell_bpos[blk] * bs2 + e] = static_cast<float>(v);
 }
 
+// The covering gather with a thread per block of J: the block's (cell, local pair) list is
+// read once and each entry's slot values (contiguous in the element record) summed per slot
+// in list order, the same order and so the same bits as the per-entry gathers.  The block
+// values start from the base (static operator) read through shared memory and go back
+// through it, so J's loads and stores are contiguous across the thread block; the fp32
+// SELL-32 copy is written from the same values.  BS2 = bs * bs (at most 25 here).
+constexpr int kBlockGatherThreads = 128;
+template <class E, int BS2>
+__global__ void __launch_bounds__(kBlockGatherThreads)
+    k_gather_jacobian_blocks(double* __restrict__ J, int nslot, const EntrySlots es, int64_t block_begin,
+                             unsigned nblocks, const int64_t* __restrict__ ptr, const int32_t* __restrict__ list,
+                             const E* __restrict__ ej, const JacobianGatherOut o) {
+  constexpr int SB = BS2 | 1;  // odd stride: the threads' own blocks sit in distinct banks
+  __shared__ double stage[kBlockGatherThreads * SB];
+  const unsigned b0 = blockIdx.x * kBlockGatherThreads;
+  const int nb = static_cast<int>(min(static_cast<unsigned>(kBlockGatherThreads), nblocks - b0));
+  const int64_t g0 = (block_begin + b0) * BS2;
+  for (int i = threadIdx.x; i < nb * BS2; i += kBlockGatherThreads) {
+    const int t = i / BS2, e = i - t * BS2;
+    stage[t * SB + e] = o.base ? o.base[g0 + i] : 0.0;
+  }
+  __syncthreads();
+  if (static_cast<int>(threadIdx.x) < nb) {
+    const unsigned b = b0 + threadIdx.x;
+    E acc[BS2];
+#pragma unroll
+    for (int m = 0; m < BS2; ++m) acc[m] = E(0);
+    const int64_t i0 = ptr[b], i1 = ptr[b + 1];
+    constexpr int kBatch = 4;
+    for (int64_t i = i0; i < i1; i += kBatch) {
+      int32_t idx[kBatch];
+#pragma unroll
+      for (int u = 0; u < kBatch; ++u) idx[u] = i + u < i1 ? list[i + u] : 0;
+      E val[kBatch][BS2];
+#pragma unroll
+      for (int u = 0; u < kBatch; ++u)
+#pragma unroll
+        for (int m = 0; m < BS2; ++m)
+          val[u][m] = (m < nslot && i + u < i1) ? ej[static_cast<int64_t>(idx[u]) * nslot + m] : E(0);
+#pragma unroll
+      for (int u = 0; u < kBatch; ++u)
+        if (i + u < i1) {
+#pragma unroll
+          for (int m = 0; m < BS2; ++m)
+            if (m < nslot) acc[m] += val[u][m];
+        }
+    }
+    double* mine = stage + threadIdx.x * SB;
+#pragma unroll
+    for (int e = 0; e < BS2; ++e) {
+      const int m = es.slot[e];
+#pragma unroll
+      for (int mm = 0; mm < BS2; ++mm)
+        if (mm == m) mine[e] += static_cast<double>(acc[mm]);
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nb * BS2; i += kBlockGatherThreads) {
+    const int t = i / BS2, e = i - t * BS2;
+    const double v = stage[t * SB + e];
+    J[g0 + i] = v;
+    if (o.sell) o.sell[o.sell_bpos[block_begin + b0 + t] * BS2 + e] = static_cast<float>(v);
+  }
+}
+
 // Local residual of one element for coefficients c (residual terms only, both forms).
 template <int DIM, int NS>
 __device__ void fd_local_residual(const VolumeParams& P, const double (&c)[DIM + 1][NS], const double (&X)[DIM + 1][DIM],
@@ -424,6 +489,22 @@ void launch_gather_jacobian_full(double* J, int bs, int nslot, const std::vector
   EntrySlots es;
   for (int e = 0; e < 64; ++e) es.slot[e] = -1;
   for (size_t m = 0; m < slot_pos_host.size(); ++m) es.slot[slot_pos_host[m]] = static_cast<int8_t>(m);
+  if (nblocks >= (int64_t{1} << 32) - 256) throw std::runtime_error("gather: more than 2^32 blocks");
+  const unsigned nb = static_cast<unsigned>(nblocks);
+  const unsigned bgrid = (nb + kBlockGatherThreads - 1) / kBlockGatherThreads;
+#define DC_BLOCKS(B2)                                                                                           \
+  if (bs2 == B2) {                                                                                              \
+    count_launches(1);                                                                                          \
+    if (f32)                                                                                                    \
+      k_gather_jacobian_blocks<float, B2><<<bgrid, kBlockGatherThreads, 0, stream>>>(                           \
+          J, nslot, es, block_begin, nb, ptr, list, reinterpret_cast<const float*>(ej), out);                   \
+    else                                                                                                        \
+      k_gather_jacobian_blocks<double, B2><<<bgrid, kBlockGatherThreads, 0, stream>>>(J, nslot, es, block_begin, \
+                                                                                       nb, ptr, list, ej, out); \
+    return;                                                                                                     \
+  }
+  DC_BLOCKS(1) DC_BLOCKS(4) DC_BLOCKS(9) DC_BLOCKS(16) DC_BLOCKS(25)
+#undef DC_BLOCKS
   const int64_t total = nblocks * bs2;
   if (total >= (int64_t{1} << 32) - 256) throw std::runtime_error("gather: more than 2^32 block entries");
   count_launches(1);

@@ -459,6 +459,11 @@ int ProgramBuilder::fold_or_make(uint8_t op, int a, int b, int c, int8_t imm) {
   bool cc = c < 0 || is_constant(c, &vc);
   if (ca && cb && cc && op != OP_INTERP) return constant(eval_op(op, va, vb, vc, imm, nullptr));
   if (op == OP_SEL && is_constant(a, &va)) return va != 0.0 ? b : c;
+  // identities that hold bit for bit in IEEE arithmetic (x * 1, 1 * x, x / 1, x - 0 are x
+  // for every x, signed zeros, infinities and NaN included)
+  if (op == OP_MUL && ca && va == 1.0) return b;
+  if ((op == OP_MUL || op == OP_DIV) && cb && vb == 1.0) return a;
+  if (op == OP_SUB && cb && vb == 0.0 && !std::signbit(vb)) return a;
   Node n; n.op = op; n.a = a; n.b = b; n.c = c; n.imm = imm;
   return intern(n);
 }

@@ -1284,7 +1284,7 @@ bool Model::assemble(const double* x, double t, double cm, double ca, double* r,
     if ((mode & 1) && r)
       launch_gather_residual(r, bs, g.ns, g.node_begin, g.nnodes, g.rlist_ptr.get(), g.rlist.get(), d_er.get(), s);
     if ((mode & 2) && J && g.slots_dyn > 0) {
-      if (&g == cover && g.slots_dyn < bs * bs)
+      if (&g == cover)
         launch_gather_jacobian_full(J, bs, g.slots_dyn, g.slot_pos_dyn_host, g.block_begin, g.nblocks,
                                     g.blist_ptr.get(), g.blist.get(), d_ej.get(), jac_f32, s, gout);
       else

@@ -19,6 +19,7 @@
 
 #include "linalg.cuh"
 #include "model.hpp"
+#include "volume_kernel.cuh"
 
 // kJitHeaderNames / kJitHeaderSources: the text of device.cuh, bytecode.hpp, lookup.hpp and
 // volume_kernel.cuh, embedded at build time
@@ -250,6 +251,11 @@ int coef_count(const std::vector<Term>& jac, int dim) {
 }
 
 // one generated Spec: a program with its residual and Jacobian term lists
+// whether the kernels stage their element records in shared memory (all four variants)
+bool jit_stages(const JitVolumeInput& in) {
+  return vk::jit_stage_bytes(in.dim, in.ns, in.n_slots, 3, 8) <= vk::kJitStageMax;
+}
+
 std::string spec_code(const char* name, const Program& prog, const std::vector<Term>& res,
                       const std::vector<Term>& jac, const JitVolumeInput& in) {
   VolumeParams flags{};
@@ -260,6 +266,8 @@ std::string spec_code(const char* name, const Program& prog, const std::vector<T
     << "  static constexpr bool kUnrollPoints = true;\n"
     << "  static constexpr int kRegs = " << std::max(prog.nregs, 1) << ";\n"
     << "  static constexpr int kCoefs = " << std::max(ncoef, 1) << ";\n"
+    << "  static constexpr int kSlots = " << in.n_slots << ";\n"
+    << "  static constexpr bool kStage = " << (jit_stages(in) ? "true" : "false") << ";\n"
     << "  __device__ __forceinline__ static constexpr int n_res(const VolumeParams&, bool) { return " << res.size()
     << "; }\n"
     << "  __device__ __forceinline__ static constexpr Term res(const VolumeParams&, bool, int t) {\n"
@@ -422,7 +430,17 @@ std::shared_ptr<const JitVolume> build_volume_jit(const JitVolumeInput& in, std:
       return nullptr;
     }
     *slots[v] = reinterpret_cast<const void*>(k);
+    // the staging area of the largest variant (fp64 residual and Jacobian records)
+    const int need = jit_stages(in) ? vk::jit_stage_bytes(in.dim, in.ns, in.n_slots, 3, 8) : 0;
+    if (need > 48 * 1024 &&
+        cudaFuncSetAttribute(*slots[v], cudaFuncAttributeMaxDynamicSharedMemorySize, need) != cudaSuccess) {
+      (void)cudaGetLastError();
+      if (why) *why = "cannot raise the shared-memory limit of the compiled volume kernels";
+      return nullptr;
+    }
   }
+  jit->n_slots = in.n_slots;
+  jit->staged = jit_stages(in);
   jit->compile_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   e.jit = jit;
   g_cache.emplace(src, e);
@@ -433,17 +451,29 @@ void launch_volume_jit(const JitVolume& jit, const VolumeParams& p, int begin, i
                        cudaStream_t stream) {
   const int n = end - begin;
   if (n <= 0) return;
+  if (mode == 3 && p.jac_f32) {
+    // residual in fp64 and the element Jacobian in fp32 (mixed precision): two passes, the
+    // second entirely in fp32, cost less than one pass that forms the Jacobian coefficients
+    // in fp64 on GB300's narrow FP64 pipe
+    launch_volume_jit(jit, p, begin, end, 1, stream);
+    launch_volume_jit(jit, p, begin, end, 2, stream);
+    return;
+  }
   const void* k = nullptr;
   if (mode == 1) k = jit.k_res;
   else if (mode == 3) k = jit.k_both;
   else if (mode == 2) k = p.jac_f32 ? jit.k_jac32 : jit.k_jac64;
   if (!k) throw std::runtime_error("run-time compiled volume kernel: unsupported mode " + std::to_string(mode));
-  constexpr int kThreads = 128;
+  // element values of the staged Jacobian records: fp64 unless the pass runs in fp32 or rounds to it
+  const bool ej64 = (mode == 2 && k == jit.k_jac64) || (mode == 3 && !p.jac_f32);
+  const int smem = jit.staged ? vk::jit_stage_bytes(jit.dim, jit.ns, jit.n_slots, mode, ej64 ? 8 : 4) : 0;
   VolumeParams pp = p;
   int b = begin, e = end;
   void* args[] = {&pp, &b, &e};
   count_launches(1);
-  const cudaError_t err = cudaLaunchKernel(k, dim3((n + kThreads - 1) / kThreads), dim3(kThreads), args, 0, stream);
+  constexpr int kThreads = vk::kJitThreads;
+  const cudaError_t err =
+      cudaLaunchKernel(k, dim3((n + kThreads - 1) / kThreads), dim3(kThreads), args, smem, stream);
   if (err != cudaSuccess) throw CudaError(std::string("run-time compiled volume kernel: ") + cudaGetErrorString(err));
 }
 

@@ -31,6 +31,8 @@ struct JitVolume {
   const void* k_jac64 = nullptr;
   const void* k_jac32 = nullptr;
   double compile_seconds = 0.0;
+  int n_slots = 0;      // Jacobian slots of the element records (sizes the shared-memory staging)
+  bool staged = false;  // element records staged in shared memory (vk::k_volume_jit)
 };
 
 // What the generator needs of one volume group (a compartment's cells).

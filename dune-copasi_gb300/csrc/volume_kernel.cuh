@@ -111,6 +111,10 @@ __device__ __forceinline__ constexpr int point_of_vertex(int a) {
   // 2D: points 0, 1, 2 sit at vertices 1, 2, 0; 3D: point q at vertex q
   return DIM == 2 ? (a == 0 ? 2 : a - 1) : a;
 }
+template <int DIM>
+__device__ __forceinline__ constexpr int vertex_of_point(int q) {
+  return DIM == 2 ? (q == 2 ? 0 : q + 1) : q;
+}
 
 // value of program input `id` at a point (species values / gradients relative to the
 // compartment's first species, positions, time, entity volume)
@@ -229,10 +233,12 @@ __device__ __forceinline__ void element_jacobian(const VolumeParams& P, Coef coe
 // The element kernel body for cell k.  R: the program's register file, coef: the
 // element's Jacobian coefficients (shared-memory slices for the interpreter, local arrays
 // indexed by constants for generated Specs).  MODE: 1 residual, 2 Jacobian, 3 both, or 0
-// for the run-time `mode` argument.
+// for the run-time `mode` argument.  er_dst / ej_dst: where the cell's residual vector and
+// Jacobian slot values go (a staging record in shared memory), or null for their places in
+// P.er / P.ej.
 template <int DIM, int NS, class F, class Spec, int MODE, class Regs, class Coef>
 __device__ __forceinline__ void volume_element(const VolumeParams& P, const int k, const int mode_rt, Regs R,
-                                               Coef coef) {
+                                               Coef coef, double* er_dst = nullptr, void* ej_dst = nullptr) {
   constexpr int NL = DIM + 1;
   constexpr int NQ = Rule<DIM>::NQ;
   const int mode = MODE ? MODE : mode_rt;
@@ -321,11 +327,31 @@ __device__ __forceinline__ void volume_element(const VolumeParams& P, const int 
   const bool do_res = (mode & 1) && P.r;
   const bool do_jac = (mode & 2) && P.J;
   const bool jac_prog = (mode & 2) != 0;  // which program and residual term list the pass runs
-  F rl[NL][NS];
+  // Every point of the rule sits at one vertex: phi_a(q) = beta + (alpha - beta) [a = v(q)].
+  // So the value of species s at point q is beta sum_a c_a + (alpha - beta) c_v(q), and the
+  // scalar residual part sum_q w_q phi_a(q) = beta sum_q w_q + (alpha - beta) w_q(a): one
+  // FMA per value instead of NL, and the point sums folded once per cell.
+  constexpr F kBe = static_cast<F>(MassConst<DIM>::beta);
+  constexpr F kAmB = static_cast<F>(MassConst<DIM>::alpha - MassConst<DIM>::beta);
+  F bsum[NS];
 #pragma unroll
-  for (int a = 0; a < NL; ++a)
+  for (int s = 0; s < NS; ++s) {
+    F acc = c[0][s];
 #pragma unroll
-    for (int s = 0; s < NS; ++s) rl[a][s] = 0.0;
+    for (int a = 1; a < NL; ++a) acc += c[a][s];
+    bsum[s] = kBe * acc;
+  }
+  // residual accumulators: the scalar part of the point at each vertex, its sum over the
+  // points, and the flux summed over the points (the basis gradients are constant on a cell)
+  F rl[NL][NS], tsum[NS], fsum[NS][DIM];
+#pragma unroll
+  for (int s = 0; s < NS; ++s) {
+    tsum[s] = 0.0;
+#pragma unroll
+    for (int a = 0; a < NL; ++a) rl[a][s] = 0.0;
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) fsum[s][j] = 0.0;
+  }
   int ncoef = 0;
   if (do_jac) {
 #pragma unroll
@@ -342,13 +368,15 @@ __device__ __forceinline__ void volume_element(const VolumeParams& P, const int 
     for (int i = 0; i < Spec::coef_bound(P, ncoef); ++i) coef[i] = 0.0;
   }
   auto point = [&](const int q) {
+    const int vq = vertex_of_point<DIM>(q);
     F u[NS];
 #pragma unroll
     for (int s = 0; s < NS; ++s) {
-      F acc = 0.0;
+      F cv = c[0][s];
 #pragma unroll
-      for (int a = 0; a < NL; ++a) acc += c[a][s] * phi_t<DIM, F>(q, a);
-      u[s] = acc;
+      for (int a = 1; a < NL; ++a)
+        if (a == vq) cv = c[a][s];
+      u[s] = fma(kAmB, cv, bsum[s]);
     }
     F xq[DIM];
 #pragma unroll
@@ -424,31 +452,20 @@ __device__ __forceinline__ void volume_element(const VolumeParams& P, const int 
           }
         }
       }
-      // rl[a][s] += (scal[s] phi_a - flux[s] . G_a) fq, with the factor fq applied once per
-      // species rather than per entry (one FMA per entry for the scalar part)
-      F ts[NS];
+      // per point only sums: the point's scalar part goes to its vertex, its total and the
+      // flux total accumulate (the weights and gradients are applied after the last point)
 #pragma unroll
-      for (int s = 0; s < NS; ++s) ts[s] = scal[s] * fq;
+      for (int s = 0; s < NS; ++s) {
+        tsum[s] += scal[s];
 #pragma unroll
-      for (int a = 0; a < NL; ++a) {
-        const F pa = phi_t<DIM, F>(q, a);
-#pragma unroll
-        for (int s = 0; s < NS; ++s) rl[a][s] = fma(ts[s], pa, rl[a][s]);
+        for (int a = 0; a < NL; ++a)
+          if (a == vq) rl[a][s] = scal[s];
       }
       if (Spec::has_flux(P)) {
 #pragma unroll
-        for (int s = 0; s < NS; ++s) {
-          F tf[DIM];
+        for (int s = 0; s < NS; ++s)
 #pragma unroll
-          for (int j = 0; j < DIM; ++j) tf[j] = flux[s][j] * fq;
-#pragma unroll
-          for (int a = 0; a < NL; ++a) {
-            F fg = 0.0;
-#pragma unroll
-            for (int j = 0; j < DIM; ++j) fg = fma(tf[j], G[a][j], fg);
-            rl[a][s] -= fg;
-          }
-        }
+          for (int j = 0; j < DIM; ++j) fsum[s][j] += flux[s][j];
       }
     }
 
@@ -528,10 +545,34 @@ __device__ __forceinline__ void volume_element(const VolumeParams& P, const int 
     for (int q = 0; q < NQ; ++q) point(q);
   }
 
+  // rl[a][s] = fq (sum_q scal_q phi_a(q) - fsum . G_a), all points having the weight fq
+  if (do_res) {
+    const F fq = static_cast<F>(Rule<DIM>::w(0)) * adet;
+    const F fb = fq * kBe, fab = fq * kAmB;
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+      const F base = fb * tsum[s];
+#pragma unroll
+      for (int a = 0; a < NL; ++a) rl[a][s] = fma(fab, rl[a][s], base);
+      if (Spec::has_flux(P)) {
+        F tf[DIM];
+#pragma unroll
+        for (int j = 0; j < DIM; ++j) tf[j] = fsum[s][j] * fq;
+#pragma unroll
+        for (int a = 0; a < NL; ++a) {
+          F fg = 0.0;
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) fg = fma(tf[j], G[a][j], fg);
+          rl[a][s] -= fg;
+        }
+      }
+    }
+  }
+
   // element outputs: residual vector and Jacobian slot values, each written exactly once
   // (the gather kernels add them into r and J in a fixed order)
   if (do_res) {
-    double* er = P.er + static_cast<int64_t>(k) * NL * NS;
+    double* er = er_dst ? er_dst : P.er + static_cast<int64_t>(k) * NL * NS;
 #pragma unroll
     for (int a = 0; a < NL; ++a)
 #pragma unroll
@@ -550,10 +591,11 @@ __device__ __forceinline__ void volume_element(const VolumeParams& P, const int 
         coef[T.coef + NQ] = F(be * be) * S;
       }
     }
-    const int64_t off = static_cast<int64_t>(k) * NL * NL * Spec::n_slots(P);
+    const int64_t off = ej_dst ? 0 : static_cast<int64_t>(k) * NL * NL * Spec::n_slots(P);
+    void* const ejb = ej_dst ? ej_dst : static_cast<void*>(P.ej);
     if constexpr (same_type<F, float>::value) {
       // the FP32 Jacobian-only pass of the mixed-precision path
-      element_jacobian<DIM, float, Spec>(P, coef, G, reinterpret_cast<float*>(P.ej) + off);
+      element_jacobian<DIM, float, Spec>(P, coef, G, static_cast<float*>(ejb) + off);
     } else if (P.jac_f32) {
       // mixed precision, computed alongside the fp64 residual: the element Jacobian in fp32
       // (the fp32 Krylov operator is built from it; the residual stays fp64)
@@ -563,9 +605,9 @@ __device__ __forceinline__ void volume_element(const VolumeParams& P, const int 
       for (int a = 0; a < NL; ++a)
 #pragma unroll
         for (int j = 0; j < DIM; ++j) Gf[a][j] = static_cast<float>(G[a][j]);
-      element_jacobian<DIM, float, Spec>(P, cf, Gf, reinterpret_cast<float*>(P.ej) + off);
+      element_jacobian<DIM, float, Spec>(P, cf, Gf, static_cast<float*>(ejb) + off);
     } else {
-      element_jacobian<DIM, double, Spec>(P, coef, G, P.ej + off);
+      element_jacobian<DIM, double, Spec>(P, coef, G, static_cast<double*>(ejb) + off);
     }
   }
 }
@@ -589,15 +631,70 @@ struct ArrCast {
   __device__ __forceinline__ float operator[](int i) const { return static_cast<float>(p[i]); }
 };
 
+// copy n elements of T from a shared-memory staging area of per-thread records (record
+// length REC, stride REC + 1) to consecutive global memory: each global store of a warp
+// covers consecutive addresses
+template <class T, int REC>
+__device__ __forceinline__ void stage_out(const T* __restrict__ stage, T* __restrict__ dst, int n) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int t = i / REC, e = i - t * REC;
+    dst[i] = stage[t * (REC + 1) + e];
+  }
+}
+
+constexpr int kJitThreads = 128;
+// largest staging area the compiled volume kernels use (larger records are not staged)
+constexpr int kJitStageMax = 160 * 1024;
+
+// bytes of dynamic shared memory of a k_volume_jit launch: the staged residual records
+// (NL * NS doubles per thread) and Jacobian records (NL * NL * nslot values of esize bytes)
+__host__ __device__ constexpr int jit_stage_bytes(int dim, int ns, int nslot, int mode, int esize) {
+  return ((mode & 1) ? kJitThreads * ((dim + 1) * ns + 1) * 8 : 0) +
+         ((mode & 2) ? kJitThreads * ((dim + 1) * (dim + 1) * nslot + 1) * esize : 0);
+}
+
 // Kernel of a generated Spec S (instantiated only by the run-time compiled sources): one
-// thread per cell, MODE fixed at compile time
+// thread per cell, MODE fixed at compile time.  The cells' element outputs are staged in
+// shared memory and written out as one contiguous range per block: a thread's own record
+// is contiguous but records are strided across the warp, so direct stores would each touch
+// 32 sectors and throttle the store pipe.
 template <int DIM, int NS, class F, class S, int MODE>
-__global__ void __launch_bounds__(128) k_volume_jit(const VolumeParams P, const int begin, const int end) {
-  const int k = begin + blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= end) return;
-  F R[S::kRegs];
-  F C[S::kCoefs];
-  volume_element<DIM, NS, F, S, MODE>(P, k, MODE, Arr<F>{R}, Arr<F>{C});
+__global__ void __launch_bounds__(kJitThreads) k_volume_jit(const VolumeParams P, const int begin, const int end) {
+  constexpr int NL = DIM + 1;
+  constexpr int RE = NL * NS;
+  constexpr int RJ = NL * NL * S::kSlots;
+  const int k0 = begin + blockIdx.x * kJitThreads;
+  const int k = k0 + threadIdx.x;
+  if constexpr (!S::kStage) {
+    // records too large to stage: each thread writes its own
+    if (k < end) {
+      F R[S::kRegs];
+      F C[S::kCoefs];
+      volume_element<DIM, NS, F, S, MODE>(P, k, MODE, Arr<F>{R}, Arr<F>{C});
+    }
+  } else {
+    extern __shared__ __align__(16) unsigned char jit_stage[];
+    double* const ser = reinterpret_cast<double*>(jit_stage);
+    unsigned char* const sej = jit_stage + ((MODE & 1) ? kJitThreads * (RE + 1) * 8 : 0);
+    const bool ej32 = same_type<F, float>::value || P.jac_f32;
+    if (k < end) {
+      F R[S::kRegs];
+      F C[S::kCoefs];
+      volume_element<DIM, NS, F, S, MODE>(
+          P, k, MODE, Arr<F>{R}, Arr<F>{C}, (MODE & 1) ? ser + threadIdx.x * (RE + 1) : nullptr,
+          (MODE & 2) ? static_cast<void*>(sej + threadIdx.x * (RJ + 1) * (ej32 ? 4 : 8)) : nullptr);
+    }
+    __syncthreads();
+    const int nv = min(kJitThreads, end - k0);
+    if ((MODE & 1) && P.r) stage_out<double, RE>(ser, P.er + static_cast<int64_t>(k0) * RE, nv * RE);
+    if ((MODE & 2) && P.J) {
+      if (ej32)
+        stage_out<float, RJ>(reinterpret_cast<const float*>(sej),
+                             reinterpret_cast<float*>(P.ej) + static_cast<int64_t>(k0) * RJ, nv * RJ);
+      else
+        stage_out<double, RJ>(reinterpret_cast<const double*>(sej), P.ej + static_cast<int64_t>(k0) * RJ, nv * RJ);
+    }
+  }
 }
 
 }  // namespace vk

@@ -121,6 +121,14 @@ Model::Model(const std::string& ini_text, const std::string& overrides) {
   build_static_matrices();
   build_constraints();
   setup_volume_jit();
+  for (const auto& g : vgroups) {
+    dynamic_mass = dynamic_mass || g.has_mass;
+    for (const Program* pr : {&g.prog_res.host, &g.prog_all.host})
+      for (uint16_t id : pr->inputs) dynamic_time = dynamic_time || id == IN_TIME;
+  }
+  for (const auto& f : fgroups)
+    for (int side = 0; side < 2; ++side)
+      for (uint16_t id : f.prog[side].host.inputs) dynamic_time = dynamic_time || id == IN_TIME;
 }
 
 // model.assembly.jit = auto | true | false: the compartments' volume kernels compiled at
@@ -1193,7 +1201,11 @@ bool Model::assemble(const double* x, double t, double cm, double ca, double* r,
   } else if ((use_m || use_k) && cs_valid && cs_cm == cm && cs_ca == ca) {
     C = d_Cs.get();
   }
-  if ((mode & 1) && r) {
+  // residual-only passes may take the static part alone or the state-dependent part alone
+  const bool skip_static = (mode & kAssembleDynamicOnly) != 0, skip_dynamic = (mode & kAssembleStaticOnly) != 0;
+  if ((skip_static || skip_dynamic) && (mode & 2))
+    throw std::logic_error("assemble: static-only / dynamic-only passes are residual passes");
+  if ((mode & 1) && r && !skip_static) {
     if (C) {
       spmv_acc(A0, C, x, r, 1.0, s);
     } else {
@@ -1230,6 +1242,7 @@ bool Model::assemble(const double* x, double t, double cm, double ca, double* r,
   }
   const bool jac_f32 = (mode & kAssembleJacobianF32) != 0;
   mode &= 3;
+  if (skip_dynamic) return false;
   for (const auto& g : vgroups) {
     if (!(cm != 0.0 && g.has_mass) && !(ca != 0.0 && g.has_stiffness)) continue;
     VolumeParams p{};

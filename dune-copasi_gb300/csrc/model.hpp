@@ -161,6 +161,8 @@ class Model {
   // volume kernels: "compiled" (run-time compiled for the model's programs), "off", or
   // "interpreter (<reason>)" when the compilation was asked for and could not be had
   std::string jit_status = "off";
+  // state-dependent (dynamic) terms: any in the mass form; any reading the time
+  bool dynamic_mass = false, dynamic_time = false;
   double fd_eps = 1e-7;
   int bs = 1;
 
@@ -239,6 +241,10 @@ class Model {
   // kAssembleJacobianF32: the per-element Jacobian values of the state-dependent terms are
   // computed and gathered in fp32 (mixed precision; the residual and the static part stay fp64)
   static constexpr int kAssembleJacobianF32 = 16;
+  // residual passes only: kAssembleStaticOnly adds the static part (cm Ms + ca Ks) x alone,
+  // kAssembleDynamicOnly the state-dependent volume and face terms alone
+  static constexpr int kAssembleStaticOnly = 32;
+  static constexpr int kAssembleDynamicOnly = 64;
   // jac_sell32 (optional, sell_slots * 32 * bs * bs floats with zero padding slots): when one
   // volume gather produces every final Jacobian entry (one compartment, every slot
   // state-dependent, no membrane, padding or constraint rows), that gather also writes the

@@ -79,6 +79,18 @@ Solver::Solver(Model& m, cudaStream_t s) : model(m), stream(s) {
   const_.resize(n_);
   z_.resize(n_);
   J_.resize(static_cast<size_t>(m.nnzb()) * m.bs * m.bs);
+  // model.assembly.split_residual = true (default) | false: the split stage residual of
+  // one_step, for models whose mass form is static and that carry state-dependent
+  // stiffness terms (Newton path, no constraints)
+  {
+    const std::string sr = m.cfg.get("model.assembly.split_residual", "true");
+    if (sr != "true" && sr != "false") throw ConfigError("model.assembly.split_residual must be true or false");
+    bool dyn_stiffness = !m.fgroups.empty();
+    for (const auto& g : m.vgroups) dyn_stiffness = dyn_stiffness || g.has_stiffness;
+    split_residual_ = sr == "true" && !m.dynamic_mass && dyn_stiffness && !m.is_linear && !m.numerical_jacobian &&
+                      m.n_constraints == 0;
+    if (split_residual_) dyn_.resize(n_);
+  }
   kr_.resize(n_); krhat_.resize(n_); kp_.resize(n_); kv_.resize(n_); ks_.resize(n_); kt_.resize(n_);
   kphat_.resize(n_); kshat_.resize(n_); kx_.resize(n_);
   dinv_.resize(static_cast<size_t>(m.nnodes) * m.bs * m.bs);
@@ -277,6 +289,7 @@ void Solver::set_state(const double* ref, int64_t n, double t) {
   scatter_idx(n, model.d_ref2blk.get(), ref_stage_.get(), x_.get(), stream);
   cuda_check(cudaStreamSynchronize(stream), "set_state");
   t_ = t;
+  dyn_valid_ = false;
 }
 
 void Solver::get_state(double* out, int64_t n) const {
@@ -875,6 +888,15 @@ void Solver::one_step(double dt) {
   for (int j = 0; j <= s; ++j) ts[j] = t + tab.D[j] * dt;
   cuda_check(cudaMemcpyAsync(us_[0].get(), x_.get(), n_ * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");
   cuda_check(cudaMemcpyAsync(stage_.get(), x_.get(), n_ * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");
+  // Split residual: with a purely static mass form, the stage residual is
+  // const + (a Ms + b dt Ks) y + b dt D(y), D the state-dependent stiffness terms.  D of the
+  // last evaluated state is kept (dyn_): a stage's Newton ends with a residual at its
+  // solution, so the next stage's explicit term and its first residual (the stage starts
+  // from that solution) take D from there instead of another volume pass, and so does the
+  // first residual of the next step.  D depends on the time only through programs that
+  // read it; those models reuse it at the same time only.
+  const bool split = split_residual_;
+  auto dyn_reusable = [&](double at) { return dyn_valid_ && (!model.dynamic_time || dyn_t_ == at); };
   for (int i = 1; i <= s; ++i) {
     const auto& a = tab.A[i - 1];
     const auto& b = tab.B[i - 1];
@@ -882,19 +904,44 @@ void Solver::one_step(double dt) {
     cuda_check(cudaMemsetAsync(const_.get(), 0, n_ * sizeof(double), stream), "memset");
     for (int j = 0; j < i; ++j) {
       if (a[j] == 0.0 && b[j] == 0.0) continue;
+      if (split && j == i - 1 && dyn_reusable(ts[j])) {
+        // the previous stage's solution: its D is the one kept from that stage's last residual
+        model.assemble(us_[j].get(), ts[j], a[j], b[j] * dt, const_.get(), nullptr, 1 | Model::kAssembleStaticOnly,
+                       stream);
+        if (b[j] != 0.0) axpy(n_, b[j] * dt, dyn_.get(), const_.get(), stream);
+        continue;
+      }
       tbegin(0);
       model.assemble(us_[j].get(), ts[j], a[j], b[j] * dt, const_.get(), nullptr, 1, stream);
       tend();
       ++stats.assemblies;
     }
     const double ai = a[i], bi = b[i] * dt, ti = ts[i];
+    // the stage starts from the previous stage's solution (or the step's start state), whose
+    // D may be kept
+    bool reuse_first = split && dyn_reusable(ti);
     auto res = [&](const double* y, double* r) {
       cuda_check(cudaMemcpyAsync(r, const_.get(), n_ * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");
-      tbegin(0);
-      model.assemble(y, ti, ai, bi, r, nullptr, 1, stream);
-      tend();
+      if (split) {
+        model.assemble(y, ti, ai, bi, r, nullptr, 1 | Model::kAssembleStaticOnly, stream);
+        if (!reuse_first) {
+          cuda_check(cudaMemsetAsync(dyn_.get(), 0, n_ * sizeof(double), stream), "memset");
+          tbegin(0);
+          model.assemble(y, ti, 0.0, 1.0, dyn_.get(), nullptr, 1 | Model::kAssembleDynamicOnly, stream);
+          tend();
+          ++stats.assemblies;
+          dyn_t_ = ti;
+        }
+        reuse_first = false;
+        dyn_valid_ = true;
+        if (bi != 0.0) axpy(n_, bi, dyn_.get(), r, stream);
+      } else {
+        tbegin(0);
+        model.assemble(y, ti, ai, bi, r, nullptr, 1, stream);
+        tend();
+        ++stats.assemblies;
+      }
       model.constrain_residual(r, stream);
-      ++stats.assemblies;
     };
     // mixed precision inside Newton: the state-dependent Jacobian terms in fp32 (the
     // Jacobian only steers the Newton correction; the residual, the static part and the
@@ -916,6 +963,12 @@ void Solver::one_step(double dt) {
       ++stats.assemblies;
     };
     auto resjac = [&](const double* y, double* r) {
+      if (split) {
+        // the residual (possibly from the kept D) and the Jacobian as separate passes
+        res(y, r);
+        jac(y);
+        return;
+      }
       cuda_check(cudaMemcpyAsync(r, const_.get(), n_ * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");
       tbegin(5);
       jac_sell_fresh_ = model.assemble(y, ti, ai, bi, r, J_.get(), 3 | jmode, stream, jac_sell_target());
@@ -953,6 +1006,8 @@ int Solver::do_step(double& dt, double* dt_used) {
       one_step(dt);
       break;
     } catch (const StepFailure&) {
+      // the kept state-dependent residual belongs to a state of the failed attempt
+      dyn_valid_ = false;
       ++stats.failed_steps;
       // the state of the step's start is kept (x_ is only overwritten on success)
       dt = dt * dec_;

@@ -144,6 +144,12 @@ class Solver {
   int64_t n_ = 0;          // padded vector length
   double t_ = 0.0;
   DeviceBuffer<double> x_, r_, J_, stage_, const_, z_;
+  // split stage residual (see one_step): the state-dependent stiffness residual D of the
+  // last evaluated state, the time it was evaluated at, and whether it belongs to stage_
+  bool split_residual_ = false;
+  DeviceBuffer<double> dyn_;
+  bool dyn_valid_ = false;
+  double dyn_t_ = 0.0;
   mutable DeviceBuffer<double> ref_stage_;  // reference-layout staging vector of set/get_state
   std::vector<DeviceBuffer<double>> us_;
   // Krylov workspace

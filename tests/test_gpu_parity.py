@@ -603,3 +603,33 @@ def test_single_launch_matches_graph_path_at_full_size(dcgpu_lib):
     (xa, na), (xb, nb) = out["true"], out["false"]
     assert na == nb
     assert _rel(xa, xb) <= 1e-10
+
+
+@pytest.mark.parametrize("case", ["gray_scott", "two_compartment", "cross_diffusion_3d"])
+@pytest.mark.parametrize("mixed", [False, True])
+def test_unsplit_stage_residual_matches_oracle(dcgpu_lib, case, mixed):
+    """model.assembly.split_residual = false: every stage residual is one combined pass over
+    the static and state-dependent terms (the default keeps the state-dependent part of the
+    last evaluated state and reuses it at stage boundaries); both meet the oracle tolerance."""
+    ini, init = ALL_CASES[case]()
+    records = _run_both(dcgpu_lib, ini, init, mixed=mixed, overrides={"model.assembly.split_residual": "false"})
+    for t, errs, n_o, n_g in records:
+        for name, e in errs.items():
+            assert e <= STEP_TOL, (case, t, name, e)
+        assert_newton_per_stage(n_o, n_g, (case, t))
+
+
+def test_split_residual_saves_assembly_passes(dcgpu_lib):
+    """With the split stage residual an Alexander2 step of a model with a static mass form
+    runs fewer assembly passes than the combined form, for the same state."""
+    ini, init = ALL_CASES["cross_diffusion_3d"]()
+    out = {}
+    for split in ("true", "false"):
+        gm = dcgpu_lib.Model(ini, {"model.assembly.split_residual": split})
+        for _ in range(3):
+            gm.step(0.01)
+        out[split] = (gm.stats()["assemblies"], gm.state())
+        gm.close()
+    assert out["true"][0] < out["false"][0]
+    x1, x0 = out["true"][1], out["false"][1]
+    assert np.linalg.norm(x1 - x0) <= 1e-12 * np.linalg.norm(x0)

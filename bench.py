@@ -82,8 +82,13 @@ def parse():
     ap.add_argument("--override", action="append", default=[],
                     help="extra engine configuration key=value (repeatable)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-iterations", type=int, default=2,
-                    help="Newton iterations of the CPU baseline leg")
+    ap.add_argument("--cpu-iterations", type=int, default=1,
+                    help="timed Newton iterations of the CPU baseline leg (after one untimed)")
+    ap.add_argument("--cpu-1core-iterations", type=int, default=0,
+                    help="timed Newton iterations of the CPU baseline on one core (0: not run)")
+    ap.add_argument("--minimal", action="store_true",
+                    help="the timed steps only (no plain FP64, profile, end-to-end, SpMV, CPU, secondary or "
+                         "serving runs): for profiling a step under ncu")
     ap.add_argument("--cpu-precond", default="bjacobi", choices=["bjacobi", "ssor"],
                     help="preconditioner of the CPU restatement's BiCGSTAB: block Jacobi (the GPU path's) "
                          "or SSOR (the reference's iterative default)")
@@ -204,27 +209,39 @@ class ClockSampler:
 
 
 # ----------------------------------------------------------------------------- CPU legs
-def cpu_newton_run(kind, n, iterations, warmup, threads, precond):
+def cpu_newton_run(kind, n, iterations, warmup, threads, precond, time_budget=None):
     """The C++ CPU restatement (oracle/cpu_newton.cpp) on the same workload: `warmup` +
-    `iterations` Newton iterations of the time-stepping sequence; returns its JSON report."""
+    `iterations` Newton iterations of the time-stepping sequence (fewer timed ones when
+    `time_budget` seconds run out first); returns its JSON report."""
     from oracle import cpu_newton
     ini, init, dt, _nl, _desc = make_workload(kind, n)
-    return cpu_newton.run(ini, init, iterations=iterations, warmup=warmup, threads=threads, precond=precond)
+    return cpu_newton.run(ini, init, iterations=iterations, warmup=warmup, threads=threads, precond=precond,
+                          time_budget=time_budget)
 
 
-def cpu_baseline(kind, n, iterations, precond):
-    """CPU baseline leg of the GPU arm: a bounded sample (a few Newton iterations of the same
-    time-stepping sequence) on all host cores, and one iteration on one core."""
+def cpu_baseline(kind, n, iterations, precond, one_core_iterations=0):
+    """CPU baseline leg of the GPU arm: a bounded sample (Newton iterations of the same
+    time-stepping sequence, after one untimed iteration) on all host cores; optionally the
+    same on one core."""
     threads = os.cpu_count() or 1
     rep = cpu_newton_run(kind, n, iterations, 1, threads, precond)
-    one = cpu_newton_run(kind, n, 1, 0, 1, precond)
-    return {"value": rep["value"], "unit": METRIC, "cores": threads, "kind": "port",
-            "sample": "%d Newton iteration(s) (residual + Jacobian assembly on %d threads, BiCGSTAB + %s to "
-                      "1e-10) of the %d-DOF stage systems of the first time step, after one untimed iteration"
-                      % (iterations, threads, rep["precond"], rep["ndof"]),
-            "value_1core": one["value"], "seconds": rep["seconds"], "assembly_seconds": rep["assembly_seconds"],
-            "solve_seconds": rep["solve_seconds"], "krylov_iterations": rep["krylov_iterations"],
-            "cpu": rep.get("cpu", "")}
+    out = {"value": rep["value"], "unit": METRIC, "cores": threads, "kind": "port",
+           "sample": "%d Newton iteration(s) (residual + Jacobian assembly on %d threads, BiCGSTAB + %s to "
+                     "1e-10) of the %d-DOF stage systems of the first time step, after one untimed iteration"
+                     % (iterations, threads, rep["precond"], rep["ndof"]),
+           "seconds": rep["seconds"], "assembly_seconds": rep["assembly_seconds"],
+           "solve_seconds": rep["solve_seconds"], "krylov_iterations": rep["krylov_iterations"],
+           "cpu": rep.get("cpu", "")}
+    if one_core_iterations > 0:
+        one = cpu_newton_run(kind, n, one_core_iterations, 0, 1, precond)
+        out["value_1core"] = one["value"]
+    return out
+
+
+# the reference arm's timed Newton iterations stop once they have taken this long, and it
+# runs at most one untimed iteration first (a Newton iteration of the 128^3 workload takes
+# tens of seconds on a host CPU): the whole arm then ends within a few minutes
+REFERENCE_TIME_BUDGET_S = 120.0
 
 
 def run_reference(args, rank, world):
@@ -232,24 +249,30 @@ def run_reference(args, rank, world):
         return
     desc = workload_desc(args.workload, args.n)
     threads = os.cpu_count() or 1
+    warm = min(args.warmup, 1)
     try:
-        rep = cpu_newton_run(args.workload, args.n, args.steps, args.warmup, threads, args.cpu_precond)
+        rep = cpu_newton_run(args.workload, args.n, args.steps, warm, threads, args.cpu_precond,
+                             time_budget=REFERENCE_TIME_BUDGET_S)
     except Exception as e:  # the restatement covers one-compartment models only
         print(json.dumps({"impl": "reference", "unavailable": "CPU restatement: %s" % e}), flush=True)
         return
     value = rep["value"]
+    done = int(rep["timed_newton_iterations"])
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * rep["seconds"] / args.steps,
+            "steps": done, "warmup": warm, "requested_steps": args.steps, "requested_warmup": args.warmup,
+            "ms_per_step": 1e3 * rep["seconds"] / max(done, 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded initial state, no dataset)",
             "config": desc,
             "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
                              "sample": "one Newton iteration of the time-stepping sequence per step (assembly on "
-                                       "%d threads, BiCGSTAB + %s to 1e-10)" % (threads, rep["precond"]),
+                                       "%d threads, BiCGSTAB + %s to 1e-10); at most %d warm-up iteration and "
+                                       "%.0f s of timed iterations" % (threads, rep["precond"], warm,
+                                                                      REFERENCE_TIME_BUDGET_S),
                              "cpu": rep.get("cpu", "")},
             "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "detail": {"assembly_seconds": rep["assembly_seconds"], "solve_seconds": rep["solve_seconds"],
-                       "krylov_iterations": rep["krylov_iterations"]}}
+                       "krylov_iterations": rep["krylov_iterations"], "setup_seconds": rep["setup_seconds"]}}
     print(json.dumps(line), flush=True)
 
 
@@ -323,35 +346,55 @@ def load_counters(workload):
     return out
 
 
+def assembly_jacobian_bytes(geo, record_bytes):
+    """Algorithmic bytes of one mixed-precision Jacobian pass (element kernel + covering
+    gather): cell vertex and block-row indices, coordinates and state read once, the fp32
+    element records written once and read once, the gather lists read once, the static
+    operator read once, J (fp64) and its SELL-32 copy (fp32) written once."""
+    cells, nnzb, bs, ndof = geo["cells"], geo["nnzb"], geo["bs"], geo["ndof"]
+    nl = geo["nl"]
+    return (cells * nl * 4 * 2 + geo["nv"] * geo["dim"] * 8 + ndof * 8 + 2 * cells * record_bytes
+            + cells * nl * nl * 4 + nnzb * 8 + nnzb * bs * bs * (8 + 8 + 4))
+
+
 def roofline_for(name, ms, calls, geo, peaks, counters):
-    """Roofline object of one kernel category.  Assembly passes are bound by the FP64 pipe
-    (their arithmetic intensity far exceeds GB300's FP64 flop/byte balance): achieved = FP64
-    flops per launch (ncu's executed DFMA x 2 + DADD + DMUL per cell, from the committed
-    counters) / average launch time, against the FP64 FMA rate measured in this run.  Krylov
-    and SpMV are bound by HBM: achieved = algorithmic bytes per launch / average launch
-    time, against the measured HBM copy bandwidth."""
+    """Roofline object of one kernel category.  Residual assembly passes are bound by the FP64
+    pipe (their arithmetic intensity far exceeds GB300's FP64 flop/byte balance): achieved =
+    FP64 flops per launch (ncu's executed DFMA x 2 + DADD + DMUL per cell, from the committed
+    counters) / average launch time, against the FP64 FMA rate measured in this run.  The
+    mixed-precision Jacobian pass (fp32 element kernel + gather), the Krylov iteration and
+    the SpMV are bound by HBM: achieved = algorithmic bytes per launch / average launch time,
+    against the measured HBM copy bandwidth.  traffic = ncu DRAM bytes per unit x units."""
     avg_s = ms * 1e-3 / max(calls, 1)
     c = counters.get(name, {})
-    if name.startswith("assembly"):
+    dram = c.get("dram_bytes", (None, None))[0]
+    if name in ("assembly_residual", "assembly_combined") or (name == "assembly_jacobian" and geo["vbytes"] == 8):
         per_cell = c.get("fp64_flops", (None, None))[0]
         flops = per_cell * geo["cells"] if per_cell is not None else None
         achieved = flops / avg_s / 1e12 if (flops and avg_s > 0) else None
-        dram = c.get("dram_bytes", (None, None))[0]
-        r = {"kernel": name, "bound": "fp64", "achieved": achieved, "peak": peaks["fp64_tflops"],
-             "unit": "TFLOP/s", "frac": achieved / peaks["fp64_tflops"] if achieved else None,
-             "peak_source": "measured in this run (FMA chains, dc_selftest_fma_peaks)",
-             "traffic": dram * geo["cells"] if dram is not None else None,
-             "work_per_launch": flops, "avg_launch_us": avg_s * 1e6, "launches": calls,
-             "per": "volume assembly pass over all cells (element kernel + gathers)"}
-        return r
+        return {"kernel": name, "bound": "fp64", "achieved": achieved, "peak": peaks["fp64_tflops"],
+                "unit": "TFLOP/s", "frac": achieved / peaks["fp64_tflops"] if achieved else None,
+                "peak_source": "measured in this run (FMA chains, dc_selftest_fma_peaks)",
+                "traffic": dram * geo["cells"] if dram is not None else None,
+                "work_per_launch": flops, "avg_launch_us": avg_s * 1e6, "launches": calls,
+                "per": "volume assembly pass over all cells (element kernel + gathers)"}
+    if name == "assembly_jacobian":
+        rec = c.get("record_bytes", (None, None))[0]
+        alg = assembly_jacobian_bytes(geo, rec) if rec is not None else None
+        achieved = alg / avg_s / 1e9 if (alg and avg_s > 0) else None
+        return {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / peaks["hbm_gbs"] if achieved else None, "peak_source": peaks["hbm_source"],
+                "traffic": dram * geo["cells"] if dram is not None else None,
+                "algorithmic_bytes_per_launch": alg, "avg_launch_us": avg_s * 1e6, "launches": calls,
+                "per": "fp32 element Jacobian pass + covering gather into J and its SELL-32 copy"}
     if name == "krylov_iteration":
         alg = krylov_iteration_bytes(geo["ndof"], geo["nnzb"], geo["bs"], geo["nrows"], geo["vbytes"])
-        per = "BiCGSTAB iteration inside the single-launch solve"
+        per = ("BiCGSTAB iteration inside the single-launch solve (its time includes the solve's share of "
+               "the fp64 refinement residuals, which the algorithmic bytes leave out)")
     else:
         alg = spmv_bytes(geo["ndof"], geo["nnzb"], geo["bs"], geo["nrows"], geo["vbytes"])
         per = "fused SpMV launch"
     achieved = alg / avg_s / 1e9 if avg_s > 0 else 0.0
-    dram = c.get("dram_bytes", (None, None))[0]
     return {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
             "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["hbm_source"],
             "traffic": dram * geo["nnzb"] if dram is not None else None,
@@ -497,6 +540,16 @@ def main():
     total_ms, newton, linear, dt = timed_steps(model, dt)
     launches = dcgpu.launch_count() - launches0
     clk = clocks.stop()
+    if args.minimal:
+        total_ms = max_over_ranks(total_ms, dist)
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": world * ndof * newton / (total_ms * 1e-3), "unit": METRIC,
+                              "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                              "ms_per_step": total_ms / args.steps, "config": workload_desc(args.workload, args.n),
+                              "run": {"minimal": True, "newton_iterations": newton, "krylov_iterations": linear,
+                                      "volume_kernels": model.jit_status()}}), flush=True)
+        model.close()
+        return
 
     # the plain FP64 path on the same workload and steps, for the metric's comparison, and
     # the mixed path's deviation from it (per-species relative L2 after W + K steps)
@@ -560,7 +613,8 @@ def main():
     # largest device time
     info_m = model.info
     geo = {"ndof": ndof, "nnzb": info_m["n_blocks"], "bs": info_m["block_size"], "nrows": info_m["n_block_rows"],
-           "cells": info_m["n_elements"], "vbytes": 4 if args.precision == "mixed" else 8}
+           "cells": info_m["n_elements"], "vbytes": 4 if args.precision == "mixed" else 8, "nl": nl,
+           "nv": info_m["n_vertices"], "dim": info_m["dim"]}
     cats = {k: v for k, v in kt.items() if v[1] and k != "assembly"}
     by_cat = {k: roofline_for(k, v[0], v[1], geo, peaks, counters) for k, v in cats.items()}
     dom = max(cats, key=lambda k: cats[k][0]) if cats else "krylov_iteration"
@@ -573,7 +627,8 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         try:
-            cpu = cpu_baseline(args.workload, args.n, args.cpu_iterations, args.cpu_precond)
+            cpu = cpu_baseline(args.workload, args.n, args.cpu_iterations, args.cpu_precond,
+                               args.cpu_1core_iterations)
         except Exception as e:
             cpu = {"unavailable": str(e)}
     sec = None

@@ -27,9 +27,10 @@
 //
 // Usage:
 //   cpu_newton --ini FILE [--state FILE] [--threads T] [--iterations K] [--warmup W]
-//              [--steps S] [--out FILE] [--precond ssor|bjacobi]
+//              [--steps S] [--out FILE] [--precond ssor|bjacobi] [--time-budget SECONDS]
 // With --iterations, the time-stepping sequence runs until W + K Newton iterations are done
-// and the last K are timed; with --steps, S whole time steps run and --out receives the
+// and the last K are timed (with --time-budget, no further timed iteration starts once the
+// timed ones have taken that long); with --steps, S whole time steps run and --out receives the
 // final state (float64, reference DOF order).  A JSON report goes to stdout.
 
 #include <algorithm>
@@ -1026,7 +1027,14 @@ struct Stepper {
     for (int64_t i = 0; i < m.ndof; ++i) diag[i] = find_col(m, i, i);
   }
 
-  bool done() const { return budget >= 0 && rep.newton >= warmup + budget; }
+  double time_budget = -1.0;  // seconds of timed iterations after which no new one starts (-1: none)
+
+  bool done() const {
+    if (budget >= 0 && rep.newton >= warmup + budget) return true;
+    // a time budget ends the timed region after at least one timed iteration
+    return time_budget > 0.0 && rep.timed_newton > 0 &&
+           std::chrono::duration<double>(last - mark).count() >= time_budget;
+  }
 
   // iteration boundary: the Newton iteration just finished counts as timed once the
   // warm-up iterations are done
@@ -1116,6 +1124,7 @@ std::string cpu_name() {
 int main(int argc, char** argv) {
   std::string ini_path, state_path, out_path;
   int64_t iterations = -1, warmup = 0, steps = -1;
+  double time_budget = -1.0;
   for (int i = 1; i < argc; ++i) {
     const std::string a = argv[i];
     auto next = [&]() -> std::string {
@@ -1129,6 +1138,7 @@ int main(int argc, char** argv) {
     else if (a == "--iterations") iterations = std::stoll(next());
     else if (a == "--warmup") warmup = std::stoll(next());
     else if (a == "--steps") steps = std::stoll(next());
+    else if (a == "--time-budget") time_budget = std::stod(next());
     else if (a == "--precond") {
       const std::string v = next();
       if (v == "ssor") g_precond = Precond::SSOR;
@@ -1195,6 +1205,7 @@ int main(int argc, char** argv) {
     Stepper st(m);
     st.rel = std::stod(get(tso + "nonlinear_solver.convergence_condition.relative_tolerance", "1e-4"));
     st.budget = iterations;
+    st.time_budget = time_budget;
     st.warmup = warmup;
     int64_t nsteps = 0;
     while (true) {

@@ -65,10 +65,11 @@ def initial_state(ini, init):
 
 
 def run(ini, init=None, iterations=None, warmup=0, threads=1, steps=None, want_state=False, timeout=3600,
-        precond="ssor"):
+        precond="ssor", time_budget=None):
     """Runs the restatement: `warmup` + `iterations` Newton iterations of the time-stepping
     sequence (the last `iterations` timed), or `steps` whole time steps; `precond` is "ssor"
-    (the reference's iterative default) or "bjacobi".  Returns the report dict; with
+    (the reference's iterative default) or "bjacobi"; with `time_budget` (seconds) no further
+    timed iteration starts once the timed ones have taken that long.  Returns the report dict; with
     want_state the final state is under "state"."""
     exe = build()
     with tempfile.TemporaryDirectory() as tmp:
@@ -83,6 +84,8 @@ def run(ini, init=None, iterations=None, warmup=0, threads=1, steps=None, want_s
             cmd += ["--state", sp]
         if iterations is not None:
             cmd += ["--iterations", str(int(iterations)), "--warmup", str(int(warmup))]
+            if time_budget is not None:
+                cmd += ["--time-budget", repr(float(time_budget))]
         if steps is not None:
             cmd += ["--steps", str(int(steps))]
         out = os.path.join(tmp, "out.bin")

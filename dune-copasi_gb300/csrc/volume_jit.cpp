@@ -41,9 +41,10 @@ typedef unsigned char uint8_t;
 typedef unsigned short uint16_t;
 typedef unsigned int uint32_t;
 typedef unsigned long long uint64_t;
+typedef unsigned long long uintptr_t;
 namespace std {
 using ::int8_t; using ::int16_t; using ::int32_t; using ::int64_t;
-using ::uint8_t; using ::uint16_t; using ::uint32_t; using ::uint64_t;
+using ::uint8_t; using ::uint16_t; using ::uint32_t; using ::uint64_t; using ::uintptr_t;
 }
 )DCSTUB";
 

@@ -235,10 +235,13 @@ __device__ __forceinline__ void element_jacobian(const VolumeParams& P, Coef coe
 // indexed by constants for generated Specs).  MODE: 1 residual, 2 Jacobian, 3 both, or 0
 // for the run-time `mode` argument.  er_dst / ej_dst: where the cell's residual vector and
 // Jacobian slot values go (a staging record in shared memory), or null for their places in
-// P.er / P.ej.
+// P.er / P.ej.  verts_src / nodes_src: the cell's vertex and block-row indices already staged
+// in shared memory, or null to read them from P.verts / P.nodes.
 template <int DIM, int NS, class F, class Spec, int MODE, class Regs, class Coef>
 __device__ __forceinline__ void volume_element(const VolumeParams& P, const int k, const int mode_rt, Regs R,
-                                               Coef coef, double* er_dst = nullptr, void* ej_dst = nullptr) {
+                                               Coef coef, double* er_dst = nullptr, void* ej_dst = nullptr,
+                                               const int32_t* verts_src = nullptr,
+                                               const int32_t* nodes_src = nullptr) {
   constexpr int NL = DIM + 1;
   constexpr int NQ = Rule<DIM>::NQ;
   const int mode = MODE ? MODE : mode_rt;
@@ -247,8 +250,8 @@ __device__ __forceinline__ void volume_element(const VolumeParams& P, const int 
   F X[NL][DIM];
 #pragma unroll
   for (int a = 0; a < NL; ++a) {
-    const int v = P.verts[static_cast<int64_t>(k) * NL + a];
-    nd[a] = P.nodes[static_cast<int64_t>(k) * NL + a];
+    const int v = verts_src ? verts_src[a] : P.verts[static_cast<int64_t>(k) * NL + a];
+    nd[a] = nodes_src ? nodes_src[a] : P.nodes[static_cast<int64_t>(k) * NL + a];
 #pragma unroll
     for (int d = 0; d < DIM; ++d) X[a][d] = P.coords[static_cast<int64_t>(v) * DIM + d];
   }
@@ -643,6 +646,45 @@ __device__ __forceinline__ void stage_out(const T* __restrict__ stage, T* __rest
 }
 
 constexpr int kJitThreads = 128;
+
+// ---- bulk asynchronous copies (the TMA engine) of the block's element index data
+// One thread of the block arms an mbarrier with the expected byte count and issues
+// cp.async.bulk copies global -> shared; every thread then waits on the barrier's phase.
+// The wait is bounded: after kBulkWaitPolls unsuccessful polls the block reports failure and
+// its threads read the indices from global memory instead (the result is the same).
+constexpr int kBulkWaitPolls = 1 << 20;
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+// bytes (a multiple of 16) from 16-byte aligned global src to 16-byte aligned shared dst
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+// true once phase `parity` of the barrier has completed, false after kBulkWaitPolls polls
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+  for (int i = 0; i < kBulkWaitPolls; ++i) {
+    unsigned done = 0;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
 // largest staging area the compiled volume kernels use (larger records are not staged)
 constexpr int kJitStageMax = 160 * 1024;
 
@@ -677,15 +719,47 @@ __global__ void __launch_bounds__(kJitThreads) k_volume_jit(const VolumeParams P
     double* const ser = reinterpret_cast<double*>(jit_stage);
     unsigned char* const sej = jit_stage + ((MODE & 1) ? kJitThreads * (RE + 1) * 8 : 0);
     const bool ej32 = same_type<F, float>::value || P.jac_f32;
+    // the block's cells are consecutive: their vertex and block-row indices are two
+    // contiguous ranges, brought into shared memory by the bulk-copy engine
+    __shared__ __align__(16) int32_t s_verts[kJitThreads * NL];
+    __shared__ __align__(16) int32_t s_nodes[kJitThreads * NL];
+    __shared__ __align__(8) uint64_t s_bar;
+    __shared__ int s_bulk;
+    const int nv = min(kJitThreads, end - k0);
+    const int32_t* gv = P.verts + static_cast<int64_t>(k0) * NL;
+    const int32_t* gn = P.nodes + static_cast<int64_t>(k0) * NL;
+    const unsigned bytes = static_cast<unsigned>(nv * NL * 4);
+    const bool bulk = bytes % 16 == 0 && (reinterpret_cast<uintptr_t>(gv) & 15) == 0 &&
+                      (reinterpret_cast<uintptr_t>(gn) & 15) == 0;
+    if (threadIdx.x == 0) {
+      s_bulk = 0;
+      if (bulk) {
+        mbar_init(&s_bar, 1);
+        mbar_expect_tx(&s_bar, 2 * bytes);
+        bulk_load(s_verts, gv, bytes, &s_bar);
+        bulk_load(s_nodes, gn, bytes, &s_bar);
+      }
+    }
+    __syncthreads();
+    bool staged = false;
+    if (bulk) {
+      staged = mbar_wait(&s_bar, 0);
+      if (!staged) atomicExch(&s_bulk, 1);
+    }
+    __syncthreads();
+    // a wait that gave up in any thread: every thread reads its indices from global memory
+    // (the copies still land in the block's own shared memory before it exits below)
+    if (s_bulk) staged = false;
     if (k < end) {
       F R[S::kRegs];
       F C[S::kCoefs];
       volume_element<DIM, NS, F, S, MODE>(
           P, k, MODE, Arr<F>{R}, Arr<F>{C}, (MODE & 1) ? ser + threadIdx.x * (RE + 1) : nullptr,
-          (MODE & 2) ? static_cast<void*>(sej + threadIdx.x * (RJ + 1) * (ej32 ? 4 : 8)) : nullptr);
+          (MODE & 2) ? static_cast<void*>(sej + threadIdx.x * (RJ + 1) * (ej32 ? 4 : 8)) : nullptr,
+          staged ? s_verts + threadIdx.x * NL : nullptr, staged ? s_nodes + threadIdx.x * NL : nullptr);
     }
+    if (bulk && s_bulk && threadIdx.x == 0) mbar_wait(&s_bar, 0);  // the copies in flight, bounded
     __syncthreads();
-    const int nv = min(kJitThreads, end - k0);
     if ((MODE & 1) && P.r) stage_out<double, RE>(ser, P.er + static_cast<int64_t>(k0) * RE, nv * RE);
     if ((MODE & 2) && P.J) {
       if (ej32)

@@ -633,3 +633,18 @@ def test_split_residual_saves_assembly_passes(dcgpu_lib):
     assert out["true"][0] < out["false"][0]
     x1, x0 = out["true"][1], out["false"][1]
     assert np.linalg.norm(x1 - x0) <= 1e-12 * np.linalg.norm(x0)
+
+
+@pytest.mark.parametrize("scheme", ["ExplicitEuler", "ImplicitEuler", "Heun", "Shu3", "RungeKutta4", "Alexander2",
+                                    "FractionalStepTheta", "Alexander3"])
+def test_runge_kutta_schemes_match_oracle(dcgpu_lib, scheme):
+    """Every one-step scheme of the reference's registry (make_step_operator.hh:408-443) on the
+    engine against the oracle: the stage states after each step and the Newton iterations of
+    every stage (explicit schemes solve their mass-form stage systems by Newton too)."""
+    ini, init = cases.small_gray_scott(n=20, steps=3)
+    records = _run_both(dcgpu_lib, ini, init, overrides={"model.time_step_operator.type": scheme})
+    assert len(records) == 3
+    for t, errs, n_o, n_g in records:
+        for name, e in errs.items():
+            assert e <= STEP_TOL, (scheme, t, name, e)
+        assert_newton_per_stage(n_o, n_g, (scheme, t))

@@ -19,8 +19,9 @@ Restates, on top of oracle.fem:
 The linear solve is direct (scipy SuperLU), standing in for the reference's default
 UMFPack (dune/copasi/solver/istl/factory/direct.hh:9-12).  For meshes whose factorisation
 does not fit in memory (3D and 1024^2 multi-species systems) ``linear="iterative"`` replaces
-it with BiCGSTAB + Jacobi inside iterative refinement to a relative true residual of 1e-13
-(the direct solve's role in Newton: an essentially exact correction).  Assembly runs over at
+it with BiCGSTAB + Jacobi inside iterative refinement to a relative true residual of 1e-13,
+or of the rounding floor of the fp64 residual r - J z where that lies above (accepted up to
+1e-10; the direct solve's role in Newton: an essentially exact correction).  Assembly runs over at
 most ``chunk`` cells at a time, so the element arrays of large meshes stay bounded.
 """
 
@@ -127,8 +128,10 @@ class OracleModel:
     chunk = 1 << 19
     #: matrix entries collected before they are summed into the global matrix
     flush_entries = 1 << 26
-    #: relative true-residual target of the iterative solve
+    #: relative true-residual target of the iterative solve, and the largest relative residual
+    #: it accepts once refinement sweeps stop reducing it (the rounding floor of r - J z)
     iterative_rtol = 1e-13
+    iterative_floor = 1e-10
 
     def __init__(self, ini_text, overrides=None, linear="direct"):
         if linear not in ("direct", "iterative"):
@@ -909,18 +912,25 @@ class OracleModel:
         if bn == 0.0:
             return z
         res = r.copy()
+        rn = float(np.linalg.norm(res))
         for _sweep in range(8):
-            rn = float(np.linalg.norm(res))
             if rn <= self.iterative_rtol * bn:
                 return z
             dz, info = spla.bicgstab(J, res, rtol=max(1e-10, 0.1 * self.iterative_rtol * bn / rn), atol=0.0,
                                      maxiter=20000, M=M)
             if not np.all(np.isfinite(dz)):
                 raise StepFailed("iterative linear solve produced non-finite values")
-            z += dz
-            res = r - J @ z
-        if float(np.linalg.norm(res)) > self.iterative_rtol * bn:
-            raise StepFailed("iterative linear solve did not reach %g" % self.iterative_rtol)
+            z_new = z + dz
+            res_new = r - J @ z_new
+            rn_new = float(np.linalg.norm(res_new))
+            if rn_new > 0.5 * rn and rn <= self.iterative_floor * bn:
+                # no longer reduced: the fp64 evaluation of r - J z has reached its rounding
+                # floor (a small right-hand side against an operator of large norm), as a
+                # direct solve's backward error would
+                return z if rn <= rn_new else z_new
+            z, res, rn = z_new, res_new, rn_new
+        if rn > self.iterative_floor * bn:
+            raise StepFailed("iterative linear solve did not reach %g" % self.iterative_floor)
         return z
 
     def _linear_solve_step(self, res, jac, x, stats):

@@ -14,7 +14,8 @@ Names (the configurations at the sizes the benchmark quotes them on):
 
 SuperLU cannot factor the last two stage systems in this machine's memory (5.26 M and
 6.44 M unknowns), so the oracle solves them with BiCGSTAB + Jacobi inside iterative
-refinement to a relative true residual of 1e-13 (OracleModel(linear="iterative")); Newton
+refinement to a relative true residual of 1e-13, or of the rounding floor of the fp64
+residual where that lies above (at most 1e-10) (OracleModel(linear="iterative")); Newton
 then takes the same iterates as with an exact solve up to that residual.
 
 Each fixture holds the configuration text, the workload generator and its arguments (so

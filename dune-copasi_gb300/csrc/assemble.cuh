@@ -23,6 +23,8 @@ constexpr int kVolumeNumericalJacobian = 4;
 void launch_volume(int dim, int ns, const VolumeParams& p, int begin, int end, int mode,
                    cudaStream_t stream);
 void launch_faces(int dim, const FaceParams& p, int begin, int end, int mode, cudaStream_t stream);
+// numerical Jacobian of the outflow terms (forward differences of the face residuals) added to p.J
+void launch_faces_fd(int dim, const FaceParams& p, int begin, int end, double eps, cudaStream_t stream);
 // volume assembly is two-phase: k_volume writes per-element outputs (er / ej of
 // VolumeParams), these gathers add them into r / J per node / block in list order
 void launch_gather_residual(double* r, int bs, int ns, int64_t node_begin, int64_t nnodes, const int64_t* ptr,

@@ -118,6 +118,13 @@ Model::Model(const std::string& ini_text, const std::string& overrides) {
   upload_geometry();
   build_volume_groups();
   build_face_groups();
+  if (numerical_jacobian)
+    for (const auto& g : fgroups)
+      for (int side = 0; side < 2; ++side)
+        for (uint16_t id : g.prog[side].host.inputs)
+          if (id >= IN_GRAD && id < IN_POSITION)
+            throw ConfigError("model.jacobian.type = numerical: outflow expressions that read a gradient are not "
+                              "supported");
   build_static_matrices();
   build_constraints();
   setup_volume_jit();
@@ -974,8 +981,6 @@ void Model::build_face_groups() {
         }
   }
   if (!any) return;
-  if (numerical_jacobian)
-    throw ConfigError("model.jacobian.type = numerical together with outflow terms is not supported");
   Faces F = compute_faces(mesh);
   const int nl = dim + 1;
   // group key: (c_in, c_out, boundary)
@@ -1335,8 +1340,15 @@ bool Model::assemble(const double* x, double t, double cm, double ca, double* r,
       p.bs = bs;
       p.t = t;
       p.ca = ca;
-      for (size_t k = 0; k + 1 < g.color_offsets.size(); ++k)
-        launch_faces(dim, p, g.color_offsets[k], g.color_offsets[k + 1], mode, s);
+      for (size_t k = 0; k + 1 < g.color_offsets.size(); ++k) {
+        if (numerical_jacobian && (mode & 2)) {
+          // jacobian.type = numerical: the residual as usual, the Jacobian by forward differences
+          if ((mode & 1) && r) launch_faces(dim, p, g.color_offsets[k], g.color_offsets[k + 1], 1, s);
+          if (J) launch_faces_fd(dim, p, g.color_offsets[k], g.color_offsets[k + 1], fd_eps, s);
+        } else {
+          launch_faces(dim, p, g.color_offsets[k], g.color_offsets[k + 1], mode, s);
+        }
+      }
     }
   }
   return gout.sell != nullptr;

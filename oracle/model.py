@@ -663,7 +663,15 @@ class OracleModel:
         Binv = np.linalg.inv(self.B[els])
         return np.einsum("nij,nqj->nqi", Binv, xq - v0[:, None, :])
 
-    def _skeleton(self, x, t, residual, rows, cols, vals):
+    def _skeleton(self, x, t, residual, rows, cols, vals, perturb=None, local=None):
+        """Skeleton / boundary outflow terms (local_operator.hh:777-1203, 1398-1436).
+
+        ``perturb`` = (cell role 0 | 1 (the face's first / second cell), species name, cell-local
+        vertex, delta[nf]) adds delta to one local coefficient of that cell on every face
+        (face-local finite differences); ``local`` (a dict) receives the residual contributions
+        per face instead of summing them into ``residual``: local[(role, species)] = [nf, d+1]
+        over the test functions of the cell with that role.
+        """
         if self.face_e0.shape[0] == 0:
             return
         m = self.mesh
@@ -713,11 +721,17 @@ class OracleModel:
                 if use_in.any():
                     idx = np.nonzero(use_in)[0]
                     c = x[self.dof(s, cin[idx])]
+                    if perturb is not None and perturb[1] == s.name and perturb[0] == side:
+                        c = c.copy()
+                        c[:, perturb[2]] += perturb[3][idx]
                     u[idx] = np.einsum("na,nqa->nq", c, phin[idx])
                     g[idx] = np.einsum("na,naj->nj", c, self.G[ein[idx]])[:, None, :]
                 if use_out.any():
                     idx = np.nonzero(use_out)[0]
                     c = x[self.dof(s, cout[idx])]
+                    if perturb is not None and perturb[1] == s.name and perturb[0] == 1 - side:
+                        c = c.copy()
+                        c[:, perturb[2]] += perturb[3][idx]
                     u[idx] = np.einsum("na,nqa->nq", c, phout[idx])
                     g[idx] = np.einsum("na,naj->nj", c, self.G[eout[idx]])[:, None, :]
                 env[s.name] = u
@@ -745,10 +759,14 @@ class OracleModel:
                     shape = (idx.shape[0], nq)
                     fq_ = fac[idx]
                     rows_test = self.dof(s, cin[idx])                          # [k, d+1]
-                    if residual is not None:
+                    if residual is not None or local is not None:
                         T = F._ev(fn.value, sub, shape)
                         loc = np.einsum("kq,kqa->ka", T * fq_, phin[idx])
-                        np.add.at(residual, rows_test, loc)
+                        if local is not None:
+                            acc = local.setdefault((side, s.name), np.zeros((nf, self.dim + 1)))
+                            np.add.at(acc, idx, loc)
+                        else:
+                            np.add.at(residual, rows_test, loc)
                     if rows is not None:
                         for (w, jex) in fn.jac:
                             sw = next(sp_ for sp_ in self.species if sp_.name == w)
@@ -815,10 +833,53 @@ class OracleModel:
         v = np.concatenate(vals)
         return sp.csr_matrix((v, (r, c)), shape=(n, n))
 
+    def _numerical_skeleton_jacobian(self, x, t, rows, cols, vals):
+        """Face-local forward differences of the outflow terms (local_operator.hh:1205-1344):
+        every local coefficient of the face's first cell, then of its second cell, is moved by
+        delta and the change of both cells' face residuals divided by it.  The reference sizes
+        the delta of a second-cell coefficient from the first cell's container at the same node
+        and index (line 1305), which on an interface between compartments names a coefficient
+        the first cell does not carry; here delta = eps (1 + |c|) of the coefficient moved."""
+        nf = self.face_e0.shape[0]
+        if nf == 0:
+            return
+        m = self.mesh
+        e0 = self.face_e0
+        has_nb = self.face_e1 >= 0
+        e1s = np.where(has_nb, self.face_e1, e0)
+        role_cells = (m.cells[e0], m.cells[e1s])
+        role_elems = (e0, e1s)
+        role_valid = (np.ones(nf, bool), has_nb)
+        sig = self.elem_sig
+        down = {}
+        self._skeleton(x, t, None, None, None, None, local=down)
+        for role in (0, 1):
+            for sw in self.species:
+                ex_w = ((sig[role_elems[role]] >> sw.comp) & 1).astype(bool) & role_valid[role]
+                if not ex_w.any():
+                    continue
+                for b in range(self.dim + 1):
+                    vtx = np.where(ex_w, role_cells[role][:, b], self.comp_vertices[sw.comp][0])
+                    delta = np.where(ex_w, self.fd_eps * (1.0 + np.abs(x[self.dof(sw, vtx)])), 0.0)
+                    up = {}
+                    self._skeleton(x, t, None, None, None, None, perturb=(role, sw.name, b, delta), local=up)
+                    for (rho, sname), arr in up.items():
+                        sp_t = next(sp_ for sp_ in self.species if sp_.name == sname)
+                        ex_s = ((sig[role_elems[rho]] >> sp_t.comp) & 1).astype(bool) & role_valid[rho]
+                        sel = ex_w & ex_s
+                        if not sel.any():
+                            continue
+                        dn = down.get((rho, sname), np.zeros_like(arr))
+                        d = (arr[sel] - dn[sel]) / delta[sel][:, None]               # [k, d+1]
+                        rr = self.dof(sp_t, role_cells[rho][sel])
+                        cc = np.repeat(self.dof(sw, role_cells[role][sel, b])[:, None], self.dim + 1, axis=1)
+                        rows.append(rr.ravel())
+                        cols.append(cc.ravel())
+                        vals.append(d.ravel())
+
     def _numerical_jacobian(self, x, t, form):
-        """Element-local forward differences, delta = eps (1 + |c|) (local_operator.hh:713-765)."""
-        if form == "stiffness" and self.has_outflow:
-            raise NotImplementedError("numerical Jacobian with outflow terms")
+        """Element-local forward differences, delta = eps (1 + |c|) (local_operator.hh:713-765),
+        and face-local ones for the outflow terms of the stiffness form."""
         rows, cols, vals = [], [], []
         cells_all = self.mesh.cells
         nl = self.dim + 1
@@ -835,6 +896,8 @@ class OracleModel:
                         rows.append(self.dof(s_te, cells).ravel())
                         cols.append(np.repeat(dofs_b[:, None], nl, axis=1).ravel())
                         vals.append(col.ravel())
+        if form == "stiffness" and self.has_outflow:
+            self._numerical_skeleton_jacobian(x, t, rows, cols, vals)
         return self._to_csr(rows, cols, vals)
 
     # ---------------------------------------------------------------- time stepping

@@ -227,10 +227,11 @@ def test_multigrid_preconditioner_matches_oracle(dcgpu_lib, case, mixed):
         assert_newton_per_stage(n_o, n_g, (case, t))
 
 
-@pytest.mark.parametrize("case", ["gray_scott", "cross_diffusion_3d"])
+@pytest.mark.parametrize("case", ["gray_scott", "cross_diffusion_3d", "two_compartment"])
 def test_numerical_jacobian_matches_oracle(dcgpu_lib, case):
     """model.jacobian.type = numerical: element-local forward differences with
-    delta = eps (1 + |c|) (local_operator.hh:713-765) on both sides."""
+    delta = eps (1 + |c|) (local_operator.hh:713-765) on both sides, and face-local ones for
+    the interface outflow terms of the two-compartment case (local_operator.hh:1205-1344)."""
     ini, init = ALL_CASES[case]()
     ov = {"model.jacobian.type": "numerical",
           "model.time_step_operator.nonlinear_solver.convergence_condition.relative_tolerance": "1e-20"}
@@ -648,3 +649,27 @@ def test_runge_kutta_schemes_match_oracle(dcgpu_lib, scheme):
         for name, e in errs.items():
             assert e <= STEP_TOL, (scheme, t, name, e)
         assert_newton_per_stage(n_o, n_g, (scheme, t))
+
+
+@pytest.mark.parametrize("case", ["two_compartment", "features_2d"])
+def test_numerical_skeleton_jacobian_matches_oracle(dcgpu_lib, case):
+    """The numerical Jacobian of a model with outflow terms: the engine's forward differences of
+    the face residuals against the oracle's (same delta rule), and, where the configured
+    jacobian expressions are the exact derivatives (the two-compartment case), close to the
+    analytic Jacobian (forward-difference truncation, delta ~ 1e-7)."""
+    ini, init = ALL_CASES[case]()
+    ov = {"model.jacobian.type": "numerical"}
+    om = OracleModel(ini, ov)
+    om_a = OracleModel(ini)
+    rng = np.random.default_rng(5)
+    x = _init_state(om, init) + 0.05 * rng.uniform(0, 1, om.ndof)
+    gm = dcgpu_lib.Model(ini, ov)
+    _r, J = gm.assemble(x, 0.0125, 0.0, 1.0)
+    Jg = gm.jacobian_csr(J)
+    Jo = om.jacobian(x, 0.0125, "stiffness")
+    Ja = om_a.jacobian(x, 0.0125, "stiffness")
+    jscale = abs(Ja).max()
+    assert abs(Jg - Jo).max() <= 1e-9 * jscale
+    if case == "two_compartment":
+        assert abs(Jg - Ja).max() <= 1e-6 * jscale
+    gm.close()

@@ -1,9 +1,11 @@
 #include "amg.hpp"
 
 #include <algorithm>
-#include <numeric>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
+
+#include "blockops.cuh"
 
 namespace dcgpu {
 
@@ -32,275 +34,431 @@ __global__ void k_galerkin(int64_t n_entries, int bs2, const int32_t* __restrict
   }
 }
 
-// x = omega D^-1 r
-template <int B, class T, class V>
-__global__ void k_bj_scale(int nrows, const V* __restrict__ dinv, const T* __restrict__ r, T* __restrict__ x,
-                           V omega, const double* sc, int slot) {
-  if (skip(sc, slot)) return;
-  const int stride = gridDim.x * blockDim.x;
-  for (int nd = blockIdx.x * blockDim.x + threadIdx.x; nd < nrows; nd += stride) {
-    const int64_t o = static_cast<int64_t>(nd) * B;
-    const V* d = dinv + static_cast<int64_t>(nd) * B * B;
-    V rv[B];
-#pragma unroll
-    for (int j = 0; j < B; ++j) rv[j] = static_cast<V>(r[o + j]);
-#pragma unroll
-    for (int i = 0; i < B; ++i) {
-      V acc = V(0);
-#pragma unroll
-      for (int j = 0; j < B; ++j) acc += d[i * B + j] * rv[j];
-      x[o + i] = static_cast<T>(omega * acc);
-    }
-  }
-}
-
-// x += omega D^-1 t
-template <int B, class T, class V>
-__global__ void k_bj_axpy(int nrows, const V* __restrict__ dinv, const T* __restrict__ t, T* __restrict__ x,
-                          V omega, const double* sc, int slot) {
-  if (skip(sc, slot)) return;
-  const int stride = gridDim.x * blockDim.x;
-  for (int nd = blockIdx.x * blockDim.x + threadIdx.x; nd < nrows; nd += stride) {
-    const int64_t o = static_cast<int64_t>(nd) * B;
-    const V* d = dinv + static_cast<int64_t>(nd) * B * B;
-    V tv[B];
-#pragma unroll
-    for (int j = 0; j < B; ++j) tv[j] = static_cast<V>(t[o + j]);
-#pragma unroll
-    for (int i = 0; i < B; ++i) {
-      V acc = V(0);
-#pragma unroll
-      for (int j = 0; j < B; ++j) acc += d[i * B + j] * tv[j];
-      x[o + i] = static_cast<T>(static_cast<V>(x[o + i]) + omega * acc);
-    }
-  }
-}
-
-// t = r - A x   (one thread per scalar row)
-template <int B, class T, class V>
-__global__ void k_residual(int nrows, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ colidx,
-                           const V* __restrict__ val, const T* __restrict__ x, const T* __restrict__ r,
-                           T* __restrict__ t, const double* sc, int slot) {
-  if (skip(sc, slot)) return;
-  const int64_t n = static_cast<int64_t>(nrows) * B;
+// L1-Jacobi inverse: (A_ii + diag(sum over j != i of |A_ij| by row))^-1
+template <int B>
+__global__ void k_l1_setup(int64_t nrows, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ diag,
+                           const double* __restrict__ val, double* __restrict__ sinv, float* __restrict__ sinv32,
+                           int* status) {
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-  for (int64_t row = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; row < n; row += stride) {
-    const int br = static_cast<int>(row / B), i = static_cast<int>(row % B);
-    V acc = V(0);
-    for (int k = rowptr[br]; k < rowptr[br + 1]; ++k) {
-      const V* blk = val + static_cast<int64_t>(k) * B * B + i * B;
-      const T* xc = x + static_cast<int64_t>(colidx[k]) * B;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < nrows; i += stride) {
+    double a[B][B], inv[B][B];
+    load_block<B>(val + static_cast<int64_t>(diag[i]) * B * B, a);
+    for (int32_t e = rowptr[i]; e < rowptr[i + 1]; ++e) {
+      if (e == diag[i]) continue;
+      const double* blk = val + static_cast<int64_t>(e) * B * B;
 #pragma unroll
-      for (int j = 0; j < B; ++j) acc += blk[j] * static_cast<V>(xc[j]);
+      for (int s = 0; s < B; ++s) {
+        double m = 0.0;
+#pragma unroll
+        for (int q = 0; q < B; ++q) m += fabs(blk[s * B + q]);
+        a[s][s] += a[s][s] < 0.0 ? -m : m;
+      }
     }
-    t[row] = static_cast<T>(static_cast<V>(r[row]) - acc);
+    if (!invert_block<B>(a, inv)) {
+      atomicExch(status, 1);
+      continue;
+    }
+    store_block<B>(sinv + i * B * B, inv);
+    if (sinv32) {
+#pragma unroll
+      for (int s = 0; s < B; ++s)
+#pragma unroll
+        for (int q = 0; q < B; ++q) sinv32[i * B * B + s * B + q] = static_cast<float>(inv[s][q]);
+    }
   }
 }
 
-// rc[I] = sum of t over the rows of aggregate I
+// x = omega S r   (S: the smoother's inverse blocks)
 template <int B, class T>
-__global__ void k_restrict(int ncoarse, const int32_t* __restrict__ agg_ptr, const int32_t* __restrict__ agg_rows,
-                           const T* __restrict__ t, T* __restrict__ rc, const double* sc, int slot) {
+__global__ void k_smooth_first(int64_t nrows, const T* __restrict__ sinv, const T* __restrict__ r, T* __restrict__ x,
+                               T omega, const double* sc, int slot) {
   if (skip(sc, slot)) return;
-  const int stride = gridDim.x * blockDim.x;
-  for (int I = blockIdx.x * blockDim.x + threadIdx.x; I < ncoarse; I += stride) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < nrows; i += stride) {
+    const T* d = sinv + i * B * B;
+    T rv[B];
+#pragma unroll
+    for (int q = 0; q < B; ++q) rv[q] = r[i * B + q];
+#pragma unroll
+    for (int s = 0; s < B; ++s) {
+      T acc = T(0);
+#pragma unroll
+      for (int q = 0; q < B; ++q) acc += d[s * B + q] * rv[q];
+      x[i * B + s] = omega * acc;
+    }
+  }
+}
+
+// x += omega S (r - A x)
+template <int B, class T>
+__global__ void k_smooth_more(int64_t nrows, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ colidx,
+                              const T* __restrict__ val, const T* __restrict__ sinv, const T* __restrict__ r,
+                              const T* __restrict__ xin, T* __restrict__ xout, T omega, const double* sc, int slot) {
+  if (skip(sc, slot)) return;
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < nrows; i += stride) {
+    T t[B];
+#pragma unroll
+    for (int s = 0; s < B; ++s) t[s] = r[i * B + s];
+    for (int32_t e = rowptr[i]; e < rowptr[i + 1]; ++e) {
+      const T* blk = val + static_cast<int64_t>(e) * B * B;
+      const T* xj = xin + static_cast<int64_t>(colidx[e]) * B;
+      T v[B];
+#pragma unroll
+      for (int q = 0; q < B; ++q) v[q] = xj[q];
+#pragma unroll
+      for (int s = 0; s < B; ++s) {
+        T acc = T(0);
+#pragma unroll
+        for (int q = 0; q < B; ++q) acc += blk[s * B + q] * v[q];
+        t[s] -= acc;
+      }
+    }
+    const T* d = sinv + i * B * B;
+#pragma unroll
+    for (int s = 0; s < B; ++s) {
+      T acc = T(0);
+#pragma unroll
+      for (int q = 0; q < B; ++q) acc += d[s * B + q] * t[q];
+      xout[i * B + s] = xin[i * B + s] + omega * acc;
+    }
+  }
+}
+
+// u = r - A x   (thread per block row)
+template <int B, class T>
+__global__ void k_residual(int64_t nrows, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ colidx,
+                           const T* __restrict__ val, const T* __restrict__ x, const T* __restrict__ r,
+                           T* __restrict__ u, const double* sc, int slot) {
+  if (skip(sc, slot)) return;
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < nrows; i += stride) {
+    T t[B];
+#pragma unroll
+    for (int s = 0; s < B; ++s) t[s] = r[i * B + s];
+    for (int32_t e = rowptr[i]; e < rowptr[i + 1]; ++e) {
+      const T* blk = val + static_cast<int64_t>(e) * B * B;
+      const T* xj = x + static_cast<int64_t>(colidx[e]) * B;
+      T v[B];
+#pragma unroll
+      for (int q = 0; q < B; ++q) v[q] = xj[q];
+#pragma unroll
+      for (int s = 0; s < B; ++s) {
+        T acc = T(0);
+#pragma unroll
+        for (int q = 0; q < B; ++q) acc += blk[s * B + q] * v[q];
+        t[s] -= acc;
+      }
+    }
+#pragma unroll
+    for (int s = 0; s < B; ++s) u[i * B + s] = t[s];
+  }
+}
+
+// rc[I] = sum of u over the rows of aggregate I (ascending row order)
+template <int B, class T>
+__global__ void k_restrict(int64_t ncoarse, const int32_t* __restrict__ agg_ptr, const int32_t* __restrict__ agg_rows,
+                           const T* __restrict__ u, T* __restrict__ rc, const double* sc, int slot) {
+  if (skip(sc, slot)) return;
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t I = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; I < ncoarse; I += stride) {
     T acc[B];
 #pragma unroll
     for (int s = 0; s < B; ++s) acc[s] = T(0);
-    for (int q = agg_ptr[I]; q < agg_ptr[I + 1]; ++q) {
-      const T* ti = t + static_cast<int64_t>(agg_rows[q]) * B;
+    for (int32_t q = agg_ptr[I]; q < agg_ptr[I + 1]; ++q) {
+      const T* ui = u + static_cast<int64_t>(agg_rows[q]) * B;
 #pragma unroll
-      for (int s = 0; s < B; ++s) acc[s] += ti[s];
+      for (int s = 0; s < B; ++s) acc[s] += ui[s];
     }
 #pragma unroll
-    for (int s = 0; s < B; ++s) rc[static_cast<int64_t>(I) * B + s] = acc[s];
+    for (int s = 0; s < B; ++s) rc[I * B + s] = acc[s];
   }
 }
 
-// x[i] += xc[agg[i]]
+// x = y + omega S (r - A y) with y = t + P xc, formed on the fly (coarse correction and
+// post-smoothing in one pass over A)
 template <int B, class T>
-__global__ void k_prolong(int nrows, const int32_t* __restrict__ agg, const T* __restrict__ xc, T* __restrict__ x,
+__global__ void k_prolong_smooth(int64_t nrows, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ colidx,
+                                 const T* __restrict__ val, const T* __restrict__ sinv, const int32_t* __restrict__ agg,
+                                 const T* __restrict__ xc, const T* __restrict__ t, const T* __restrict__ r,
+                                 T* __restrict__ x, T omega, const double* sc, int slot) {
+  if (skip(sc, slot)) return;
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < nrows; i += stride) {
+    T res[B];
+#pragma unroll
+    for (int s = 0; s < B; ++s) res[s] = r[i * B + s];
+    for (int32_t e = rowptr[i]; e < rowptr[i + 1]; ++e) {
+      const int32_t j = colidx[e];
+      const T* blk = val + static_cast<int64_t>(e) * B * B;
+      const T* tj = t + static_cast<int64_t>(j) * B;
+      const T* cj = xc + static_cast<int64_t>(agg[j]) * B;
+      T v[B];
+#pragma unroll
+      for (int q = 0; q < B; ++q) v[q] = tj[q] + cj[q];
+#pragma unroll
+      for (int s = 0; s < B; ++s) {
+        T acc = T(0);
+#pragma unroll
+        for (int q = 0; q < B; ++q) acc += blk[s * B + q] * v[q];
+        res[s] -= acc;
+      }
+    }
+    const T* d = sinv + i * B * B;
+    const T* ci = xc + static_cast<int64_t>(agg[i]) * B;
+#pragma unroll
+    for (int s = 0; s < B; ++s) {
+      T acc = T(0);
+#pragma unroll
+      for (int q = 0; q < B; ++q) acc += d[s * B + q] * res[q];
+      x[i * B + s] = t[i * B + s] + ci[s] + omega * acc;
+    }
+  }
+}
+
+// x += P xc
+template <int B, class T>
+__global__ void k_prolong(int64_t nrows, const int32_t* __restrict__ agg, const T* __restrict__ xc, T* __restrict__ x,
                           const double* sc, int slot) {
   if (skip(sc, slot)) return;
-  const int64_t n = static_cast<int64_t>(nrows) * B;
+  const int64_t n = nrows * B;
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-  for (int64_t row = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; row < n; row += stride) {
-    const int64_t i = row / B;
-    const int s = static_cast<int>(row % B);
-    x[row] += xc[static_cast<int64_t>(agg[i]) * B + s];
+  for (int64_t row = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; row < n; row += stride)
+    x[row] += xc[static_cast<int64_t>(agg[row / B]) * B + row % B];
+}
+
+// ---------------------------------------------------------------- dense coarsest solve
+template <int B>
+__global__ void k_dense_fill(int64_t nrows, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ colidx,
+                             const double* __restrict__ val, int n, double* __restrict__ dense) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t I = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; I < nrows; I += stride)
+    for (int32_t e = rowptr[I]; e < rowptr[I + 1]; ++e)
+      for (int s = 0; s < B; ++s)
+        for (int q = 0; q < B; ++q)
+          dense[(I * B + s) * n + static_cast<int64_t>(colidx[e]) * B + q] = val[static_cast<int64_t>(e) * B * B + s * B + q];
+}
+
+constexpr int kLuThreads = 256;
+
+// LU = P A with partial pivoting (row-major, unit lower triangle implicit), one block, the
+// matrix in shared memory; perm[i] = the row of A at position i.  status[0] = 1 on a zero
+// or non-finite pivot.
+__global__ void __launch_bounds__(kLuThreads) k_dense_lu(int n, const double* A, double* LU,
+                                                         int32_t* __restrict__ perm_out, int* status) {
+  extern __shared__ double a[];
+  __shared__ int32_t perm[Amg::kDenseMax];
+  __shared__ int s_piv, s_fail;
+  for (int q = threadIdx.x; q < n * n; q += kLuThreads) a[q] = A[q];
+  for (int q = threadIdx.x; q < n; q += kLuThreads) perm[q] = q;
+  if (threadIdx.x == 0) s_fail = 0;
+  __syncthreads();
+  for (int k = 0; k < n; ++k) {
+    if (threadIdx.x < 32) {  // pivot: largest |a[i][k]| for i >= k, lowest index on ties
+      double best = -1.0;
+      int bi = k;
+      for (int i = k + threadIdx.x; i < n; i += 32) {
+        const double v = fabs(a[i * n + k]);
+        if (v > best) {
+          best = v;
+          bi = i;
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_down_sync(0xffffffffu, best, o);
+        const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+        if (ob > best || (ob == best && oi < bi)) {
+          best = ob;
+          bi = oi;
+        }
+      }
+      if (threadIdx.x == 0) {
+        s_piv = bi;
+        if (!(best > 0.0) || !isfinite(best)) s_fail = 1;
+        const int32_t t = perm[k];
+        perm[k] = perm[bi];
+        perm[bi] = t;
+      }
+    }
+    __syncthreads();
+    if (s_fail) break;
+    const int p = s_piv;
+    if (p != k)
+      for (int j = threadIdx.x; j < n; j += kLuThreads) {
+        const double t = a[k * n + j];
+        a[k * n + j] = a[p * n + j];
+        a[p * n + j] = t;
+      }
+    __syncthreads();
+    const double piv = a[k * n + k];
+    for (int i = k + 1 + threadIdx.x; i < n; i += kLuThreads) a[i * n + k] /= piv;
+    __syncthreads();
+    const int m = n - k - 1;
+    for (int q = threadIdx.x; q < m * m; q += kLuThreads) {
+      const int i = k + 1 + q / m, j = k + 1 + q % m;
+      a[i * n + j] -= a[i * n + k] * a[k * n + j];
+    }
+    __syncthreads();
+  }
+  if (s_fail) {
+    if (threadIdx.x == 0) atomicExch(status, 1);
+    return;
+  }
+  for (int q = threadIdx.x; q < n * n; q += kLuThreads) LU[q] = a[q];
+  for (int q = threadIdx.x; q < n; q += kLuThreads) perm_out[q] = perm[q];
+}
+
+// column j (block j) of A^-1 from LU = P A: solve L U y = P e_j; written column-major
+// (inv_cm[j * n + i] = (A^-1)_ij), fp64 and fp32
+__global__ void __launch_bounds__(Amg::kDenseMax) k_dense_inverse(int n, const double* __restrict__ LU,
+                                                                  const int32_t* __restrict__ perm,
+                                                                  double* __restrict__ inv_cm,
+                                                                  float* __restrict__ inv_cm32) {
+  __shared__ double y[Amg::kDenseMax];
+  const int j = blockIdx.x, i = threadIdx.x;
+  if (i < n) y[i] = perm[i] == j ? 1.0 : 0.0;
+  __syncthreads();
+  for (int k = 0; k < n; ++k) {  // unit lower triangle
+    if (i > k && i < n) y[i] -= LU[i * n + k] * y[k];
+    __syncthreads();
+  }
+  for (int k = n - 1; k >= 0; --k) {
+    if (i == k) y[k] /= LU[k * n + k];
+    __syncthreads();
+    if (i < k) y[i] -= LU[i * n + k] * y[k];
+    __syncthreads();
+  }
+  if (i < n) {
+    inv_cm[static_cast<int64_t>(j) * n + i] = y[i];
+    inv_cm32[static_cast<int64_t>(j) * n + i] = static_cast<float>(y[i]);
   }
 }
 
-template <int B, class T, class V>
-struct Cycle {
-  struct L {
-    int64_t nrows;
-    const int32_t *rowptr, *colidx, *agg, *agg_ptr, *agg_rows;
-    const V *val, *dinv;
-    T *x, *t, *rc;
-    int64_t ncoarse;
-  };
-  static void run(const std::vector<L>& lv, int l, const T* r, T* x, V omega, int sweeps, const double* sc,
-                  int slot, cudaStream_t s) {
-    const L& a = lv[l];
-    const int n = static_cast<int>(a.nrows);
-    const int gb = blocks_for(a.nrows), gr = blocks_for(a.nrows * B);
-    count_launches(1);
-    k_bj_scale<B, T, V><<<gb, kT, 0, s>>>(n, a.dinv, r, x, omega, sc, slot);
-    if (l + 1 == static_cast<int>(lv.size())) {
-      for (int k = 1; k < sweeps; ++k) {
-        count_launches(2);
-        k_residual<B, T, V><<<gr, kT, 0, s>>>(n, a.rowptr, a.colidx, a.val, x, r, a.t, sc, slot);
-        k_bj_axpy<B, T, V><<<gb, kT, 0, s>>>(n, a.dinv, a.t, x, omega, sc, slot);
-      }
-      return;
-    }
-    const L& c = lv[l + 1];
-    count_launches(2);
-    k_residual<B, T, V><<<gr, kT, 0, s>>>(n, a.rowptr, a.colidx, a.val, x, r, a.t, sc, slot);
-    k_restrict<B, T><<<blocks_for(a.ncoarse), kT, 0, s>>>(static_cast<int>(a.ncoarse), a.agg_ptr, a.agg_rows, a.t,
-                                                          c.rc, sc, slot);
-    run(lv, l + 1, c.rc, c.x, omega, sweeps, sc, slot, s);
-    count_launches(3);
-    k_prolong<B, T><<<gr, kT, 0, s>>>(n, a.agg, c.x, x, sc, slot);
-    k_residual<B, T, V><<<gr, kT, 0, s>>>(n, a.rowptr, a.colidx, a.val, x, r, a.t, sc, slot);
-    k_bj_axpy<B, T, V><<<gb, kT, 0, s>>>(n, a.dinv, a.t, x, omega, sc, slot);
-  }
-};
+// x = A^-1 r with the column-major inverse
+template <class T>
+__global__ void k_dense_apply(int n, const T* __restrict__ inv_cm, const T* __restrict__ r, T* __restrict__ x,
+                              const double* sc, int slot) {
+  if (skip(sc, slot)) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  T acc = T(0);
+  for (int j = 0; j < n; ++j) acc += inv_cm[static_cast<int64_t>(j) * n + i] * r[j];
+  x[i] = acc;
+}
+
+template <class T>
+T* pick(const DeviceBuffer<double>& d, const DeviceBuffer<float>& f) {
+  if constexpr (std::is_same<T, float>::value) return f.get();
+  else return d.get();
+}
+template <class T>
+const T* pickc(const double* d, const float* f) {
+  if constexpr (std::is_same<T, float>::value) return f;
+  else return d;
+}
 
 }  // namespace
 
-void Amg::build(const std::vector<int32_t>& rowptr, const std::vector<int32_t>& colidx,
-                const std::vector<int32_t>& diag, const std::vector<int32_t>& group, int bs, int max_levels,
-                int min_rows) {
+void Amg::build(int64_t nrows, int bs, int64_t nnzb, const int32_t* rowptr, const int32_t* colidx,
+                const int32_t* diag, const int32_t* group, cudaStream_t s) {
+  if (bs < 1 || bs > 8) throw std::runtime_error("multigrid: block size " + std::to_string(bs) + " unsupported");
   levels_.clear();
   bs_ = bs;
-  std::vector<int32_t> rp = rowptr, ci = colidx, dg = diag, grp = group;
-  int64_t n = static_cast<int64_t>(rp.size()) - 1;
-  for (int l = 0; l < max_levels; ++l) {
-    Level L;
-    L.nrows = n;
-    L.nnzb = static_cast<int64_t>(ci.size());
-    L.rowptr_o.upload(rp);
-    L.colidx_o.upload(ci);
-    L.diag_o.upload(dg);
-    L.rowptr = L.rowptr_o.get();
-    L.colidx = L.colidx_o.get();
-    L.diag = L.diag_o.get();
-    const bool last = (l + 1 == max_levels) || n <= min_rows;
-    if (last) {
-      levels_.push_back(std::move(L));
-      break;
-    }
-    // greedy aggregation within groups
-    std::vector<int32_t> agg(n, -1);
-    int32_t na = 0;
-    for (int64_t i = 0; i < n; ++i) {
-      if (agg[i] != -1) continue;
-      bool free_nb = true;
-      for (int32_t k = rp[i]; k < rp[i + 1] && free_nb; ++k) {
-        const int32_t j = ci[k];
-        if (j != i && grp[j] == grp[i] && agg[j] != -1) free_nb = false;
-      }
-      if (!free_nb) continue;
-      agg[i] = na;
-      for (int32_t k = rp[i]; k < rp[i + 1]; ++k) {
-        const int32_t j = ci[k];
-        if (grp[j] == grp[i]) agg[j] = na;
-      }
-      ++na;
-    }
-    const std::vector<int32_t> agg1 = agg;
-    for (int64_t i = 0; i < n; ++i) {
-      if (agg[i] != -1) continue;
-      for (int32_t k = rp[i]; k < rp[i + 1]; ++k) {
-        const int32_t j = ci[k];
-        if (j != i && grp[j] == grp[i] && agg1[j] != -1) {
-          agg[i] = agg1[j];
-          break;
-        }
-      }
-    }
-    for (int64_t i = 0; i < n; ++i)
-      if (agg[i] == -1) agg[i] = na++;
-    if (na >= 0.9 * n) {  // coarsening stalled: this level is the coarsest
-      levels_.push_back(std::move(L));
-      break;
-    }
-    // aggregate members (CSR)
-    std::vector<int32_t> aptr(na + 1, 0), arows(n);
-    for (int64_t i = 0; i < n; ++i) aptr[agg[i] + 1]++;
-    for (int32_t a = 0; a < na; ++a) aptr[a + 1] += aptr[a];
-    {
-      std::vector<int32_t> fill(aptr.begin(), aptr.end() - 1);
-      for (int64_t i = 0; i < n; ++i) arows[fill[agg[i]]++] = static_cast<int32_t>(i);
-    }
-    // coarse pattern
-    std::vector<int32_t> crp(na + 1, 0), cci, cdg(na, -1), cgrp(na, 0);
-    std::vector<int32_t> cols;
-    for (int32_t a = 0; a < na; ++a) {
-      cols.clear();
-      for (int32_t q = aptr[a]; q < aptr[a + 1]; ++q) {
-        const int32_t i = arows[q];
-        for (int32_t k = rp[i]; k < rp[i + 1]; ++k) cols.push_back(agg[ci[k]]);
-      }
-      std::sort(cols.begin(), cols.end());
-      cols.erase(std::unique(cols.begin(), cols.end()), cols.end());
-      for (int32_t c : cols) {
-        if (c == a) cdg[a] = static_cast<int32_t>(cci.size());
-        cci.push_back(c);
-      }
-      crp[a + 1] = static_cast<int32_t>(cci.size());
-      cgrp[a] = grp[arows[aptr[a]]];
-    }
-    // fine block -> coarse block, grouped per coarse block in increasing fine order
-    std::vector<int32_t> target(ci.size());
-    for (int64_t i = 0; i < n; ++i) {
-      const int32_t I = agg[i];
-      for (int32_t k = rp[i]; k < rp[i + 1]; ++k) {
-        const int32_t J = agg[ci[k]];
-        auto b = cci.begin() + crp[I], e = cci.begin() + crp[I + 1];
-        target[k] = static_cast<int32_t>(std::lower_bound(b, e, J) - cci.begin());
-      }
-    }
-    std::vector<int32_t> gptr(cci.size() + 1, 0), gsrc(ci.size());
-    for (size_t k = 0; k < ci.size(); ++k) gptr[target[k] + 1]++;
-    for (size_t c = 0; c < cci.size(); ++c) gptr[c + 1] += gptr[c];
-    {
-      std::vector<int32_t> fill(gptr.begin(), gptr.end() - 1);
-      for (size_t k = 0; k < ci.size(); ++k) gsrc[fill[target[k]]++] = static_cast<int32_t>(k);
-    }
-    L.agg.upload(agg);
-    L.agg_ptr.upload(aptr);
-    L.agg_rows.upload(arows);
-    L.gal_ptr.upload(gptr);
-    L.gal_src.upload(gsrc);
-    levels_.push_back(std::move(L));
-    rp = std::move(crp);
-    ci = std::move(cci);
-    dg = std::move(cdg);
-    grp = std::move(cgrp);
-    n = na;
+  dense_n_ = 0;
+  const int64_t target = coarsen_target > 0 ? coarsen_target : std::max<int64_t>(1, kDenseMax / bs);
+  {
+    Level L0;
+    L0.nrows = nrows;
+    L0.nnzb = nnzb;
+    L0.rowptr = rowptr;
+    L0.colidx = colidx;
+    L0.diag = diag;
+    L0.group = group;
+    levels_.push_back(std::move(L0));
   }
-  // values and work vectors
+  while (static_cast<int>(levels_.size()) < max_levels && levels_.back().nrows > target) {
+    Level& f = levels_.back();
+    DeviceGraph g;
+    g.n = f.nrows;
+    g.rowptr = f.rowptr;
+    g.colidx = f.colidx;
+    g.group = f.group;
+    f.agg.resize(static_cast<size_t>(f.nrows));
+    const int64_t na = aggregate_mis(g, mis_distance, f.agg.get(), s);
+    if (na >= 0.9 * static_cast<double>(f.nrows)) {  // coarsening stalled: this level is the coarsest
+      f.agg.resize(0);
+      break;
+    }
+    Level c;
+    coarse_structure(g, f.agg.get(), na, &c.own, s);
+    c.nrows = na;
+    c.nnzb = c.own.nnzb;
+    c.rowptr = c.own.rowptr.get();
+    c.colidx = c.own.colidx.get();
+    c.diag = c.own.diag.get();
+    c.group = c.own.group.get();
+    levels_.push_back(std::move(c));
+  }
+  const int64_t last_n = levels_.back().nrows * bs;
+  if (last_n <= kDenseMax) {
+    dense_n_ = static_cast<int>(last_n);
+    const size_t n2 = static_cast<size_t>(dense_n_) * dense_n_;
+    dense_.resize(n2);
+    dinvd_.resize(n2);
+    dinvf_.resize(n2);
+    dense_piv_.resize(static_cast<size_t>(dense_n_));
+    const size_t smem = n2 * sizeof(double);
+    cuda_check(cudaFuncSetAttribute(k_dense_lu, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)),
+               "multigrid dense solve");
+  }
+  const size_t b2 = static_cast<size_t>(bs) * bs;
   for (size_t l = 0; l < levels_.size(); ++l) {
     Level& L = levels_[l];
-    const int64_t nv = L.nrows * bs_;
+    const size_t nv = static_cast<size_t>(L.nrows) * bs;
     if (l > 0) {
-      L.val_o.resize(L.nnzb * bs_ * bs_);
-      L.dinv_o.resize(L.nrows * bs_ * bs_);
+      L.val_o.resize(static_cast<size_t>(L.nnzb) * b2);
+      L.dinv_o.resize(static_cast<size_t>(L.nrows) * b2);
       L.val = L.val_o.get();
       L.dinv = L.dinv_o.get();
     }
     L.x.resize(nv);
     L.t.resize(nv);
     L.rc.resize(nv);
+    const bool smoothed = !(l + 1 == levels_.size() && dense_n_ > 0);
+    if (smoothed && smoother == Smoother::L1Jacobi) L.sinv_o.resize(static_cast<size_t>(L.nrows) * b2);
+    if (smoothed && smoother == Smoother::GaussSeidel) {
+      L.gs = std::make_unique<ColorPrecond>();
+      L.gs->build(ColorPrecond::Kind::Sor, L.nrows, bs, L.nnzb, L.rowptr, L.colidx, L.diag, s);
+      L.gs->omega = omega;
+    }
   }
-  cuda_check(cudaStreamSynchronize(cudaStreamLegacy), "multigrid set-up");
+  cuda_check(cudaStreamSynchronize(s), "multigrid set-up");
 }
 
-void Amg::setup(const double* fine_vals, const double* fine_dinv, const float* fine_vals32,
-                const float* fine_dinv32, bool fp32, int* status, cudaStream_t s) {
+std::vector<double> Amg::values_host(int l) const {
+  const Level& L = levels_[l];
+  std::vector<double> h(static_cast<size_t>(L.nnzb) * bs_ * bs_);
+  if (!h.empty())
+    cuda_check(cudaMemcpy(h.data(), L.val, h.size() * sizeof(double), cudaMemcpyDeviceToHost), "multigrid values");
+  return h;
+}
+std::vector<int32_t> Amg::rowptr_host(int l) const {
+  const Level& L = levels_[l];
+  std::vector<int32_t> h(static_cast<size_t>(L.nrows) + 1);
+  cuda_check(cudaMemcpy(h.data(), L.rowptr, h.size() * sizeof(int32_t), cudaMemcpyDeviceToHost), "multigrid pattern");
+  return h;
+}
+std::vector<int32_t> Amg::colidx_host(int l) const {
+  const Level& L = levels_[l];
+  std::vector<int32_t> h(static_cast<size_t>(L.nnzb));
+  if (!h.empty())
+    cuda_check(cudaMemcpy(h.data(), L.colidx, h.size() * sizeof(int32_t), cudaMemcpyDeviceToHost), "multigrid pattern");
+  return h;
+}
+
+void Amg::setup(const double* fine_vals, const double* fine_dinv, const float* fine_vals32, const float* fine_dinv32,
+                bool fp32, int* status, cudaStream_t s) {
   if (levels_.empty()) return;
   levels_[0].val = fine_vals;
   levels_[0].dinv = fine_dinv;
@@ -312,7 +470,7 @@ void Amg::setup(const double* fine_vals, const double* fine_dinv, const float* f
     Level& c = levels_[l];
     const int64_t ne = c.nnzb * bs2;
     count_launches(1);
-    k_galerkin<<<blocks_for(ne), kT, 0, s>>>(ne, bs2, f.gal_ptr.get(), f.gal_src.get(), f.val, c.val_o.get());
+    k_galerkin<<<blocks_for(ne), kT, 0, s>>>(ne, bs2, c.own.gal_ptr.get(), c.own.gal_src.get(), f.val, c.val_o.get());
     Bsr A;
     A.nrows = static_cast<int>(c.nrows);
     A.bs = bs_;
@@ -341,50 +499,121 @@ void Amg::setup(const double* fine_vals, const double* fine_dinv, const float* f
         L.rc32.resize(L.rc.size());
       }
   }
+  // smoothers
+  for (size_t l = 0; l < levels_.size(); ++l) {
+    Level& L = levels_[l];
+    if (L.sinv_o.size()) {
+      if (fp32 && L.sinv32_o.size() != L.sinv_o.size()) L.sinv32_o.resize(L.sinv_o.size());
+      count_launches(1);
+#define DC_L1(B)                                                                                             \
+  case B:                                                                                                    \
+    k_l1_setup<B><<<blocks_for(L.nrows), kT, 0, s>>>(L.nrows, L.rowptr, L.diag, L.val, L.sinv_o.get(),      \
+                                                     fp32 ? L.sinv32_o.get() : nullptr, status);             \
+    break;
+      switch (bs_) { DC_L1(1) DC_L1(2) DC_L1(3) DC_L1(4) DC_L1(5) DC_L1(6) DC_L1(7) DC_L1(8) }
+#undef DC_L1
+    }
+    if (L.gs) L.gs->setup(L.val, L.dinv, L.val32, L.dinv32, fp32, status, s);
+  }
+  // dense coarsest solve
+  if (dense_n_ > 0) {
+    const Level& c = levels_.back();
+    const int n = dense_n_;
+    cuda_check(cudaMemsetAsync(dense_.get(), 0, static_cast<size_t>(n) * n * sizeof(double), s), "multigrid");
+    count_launches(3);
+#define DC_DF(B) \
+  case B: k_dense_fill<B><<<blocks_for(c.nrows), kT, 0, s>>>(c.nrows, c.rowptr, c.colidx, c.val, n, dense_.get()); break;
+    switch (bs_) { DC_DF(1) DC_DF(2) DC_DF(3) DC_DF(4) DC_DF(5) DC_DF(6) DC_DF(7) DC_DF(8) }
+#undef DC_DF
+    // factor in place: the LU overwrites the assembled matrix
+    k_dense_lu<<<1, kLuThreads, static_cast<size_t>(n) * n * sizeof(double), s>>>(n, dense_.get(), dense_.get(),
+                                                                                 dense_piv_.get(), status);
+    k_dense_inverse<<<n, kDenseMax, 0, s>>>(n, dense_.get(), dense_piv_.get(), dinvd_.get(), dinvf_.get());
+  }
 }
 
 template <class T>
-void Amg::apply(const T* r, T* z, const double* sc, int done_slot, cudaStream_t s) const {
-  constexpr bool f32 = std::is_same<T, float>::value;
-  using V = T;
-#define DC_AMG(B)                                                                                        \
-  case B: {                                                                                              \
-    std::vector<typename Cycle<B, T, V>::L> lv(levels_.size());                                          \
-    for (size_t l = 0; l < levels_.size(); ++l) {                                                        \
-      const Level& L = levels_[l];                                                                       \
-      auto& o = lv[l];                                                                                   \
-      o.nrows = L.nrows;                                                                                 \
-      o.rowptr = L.rowptr;                                                                               \
-      o.colidx = L.colidx;                                                                               \
-      o.agg = L.agg.get();                                                                               \
-      o.agg_ptr = L.agg_ptr.get();                                                                       \
-      o.agg_rows = L.agg_rows.get();                                                                     \
-      o.ncoarse = (l + 1 < levels_.size()) ? levels_[l + 1].nrows : 0;                                   \
-      if constexpr (f32) {                                                                               \
-        o.val = reinterpret_cast<const V*>(L.val32);                                                     \
-        o.dinv = reinterpret_cast<const V*>(L.dinv32);                                                   \
-        o.x = reinterpret_cast<T*>(L.x32.get());                                                         \
-        o.t = reinterpret_cast<T*>(L.t32.get());                                                         \
-        o.rc = reinterpret_cast<T*>(L.rc32.get());                                                       \
-      } else {                                                                                           \
-        o.val = reinterpret_cast<const V*>(L.val);                                                       \
-        o.dinv = reinterpret_cast<const V*>(L.dinv);                                                     \
-        o.x = reinterpret_cast<T*>(L.x.get());                                                           \
-        o.t = reinterpret_cast<T*>(L.t.get());                                                           \
-        o.rc = reinterpret_cast<T*>(L.rc.get());                                                         \
-      }                                                                                                  \
-    }                                                                                                    \
-    Cycle<B, T, V>::run(lv, 0, r, z, static_cast<V>(omega), coarse_sweeps, sc, done_slot, s);            \
-    break;                                                                                               \
+void Amg::cycle(int l, const T* r, T* x, const double* sc, int slot, cudaStream_t s) const {
+  const Level& a = levels_[l];
+  const int64_t n = a.nrows;
+  const T* A = pickc<T>(a.val, a.val32);
+  const T* D = pickc<T>(a.dinv, a.dinv32);
+  const T w = static_cast<T>(omega);
+  T* t = pick<T>(a.t, a.t32);
+  const bool last = l + 1 == static_cast<int>(levels_.size());
+#define DC_BS(KERNEL_CALL)                                                                                    \
+  switch (bs_) {                                                                                              \
+    case 1: { constexpr int B = 1; KERNEL_CALL; } break;                                                      \
+    case 2: { constexpr int B = 2; KERNEL_CALL; } break;                                                      \
+    case 3: { constexpr int B = 3; KERNEL_CALL; } break;                                                      \
+    case 4: { constexpr int B = 4; KERNEL_CALL; } break;                                                      \
+    case 5: { constexpr int B = 5; KERNEL_CALL; } break;                                                      \
+    case 6: { constexpr int B = 6; KERNEL_CALL; } break;                                                      \
+    case 7: { constexpr int B = 7; KERNEL_CALL; } break;                                                      \
+    default: { constexpr int B = 8; KERNEL_CALL; } break;                                                     \
   }
-  switch (bs_) {
-    DC_AMG(1) DC_AMG(2) DC_AMG(3) DC_AMG(4) DC_AMG(5) DC_AMG(6) DC_AMG(7) DC_AMG(8)
-    default: throw std::runtime_error("multigrid: block size " + std::to_string(bs_) + " unsupported");
+  if (last) {
+    if (dense_n_ > 0) {
+      count_launches(1);
+      k_dense_apply<T><<<(dense_n_ + 31) / 32, 32, 0, s>>>(dense_n_, pick<T>(dinvd_, dinvf_), r, x, sc, slot);
+      return;
+    }
+    // coarsening stalled above the dense limit: damped block-Jacobi sweeps
+    count_launches(1);
+    DC_BS((k_smooth_first<B, T><<<blocks_for(n), kT, 0, s>>>(n, D, r, x, w, sc, slot)));
+    for (int k = 1; k < coarse_sweeps; ++k) {
+      count_launches(2);
+      DC_BS((k_smooth_more<B, T><<<blocks_for(n), kT, 0, s>>>(n, a.rowptr, a.colidx, A, D, r, x, t, w, sc, slot)));
+      cuda_check(cudaMemcpyAsync(x, t, static_cast<size_t>(n) * bs_ * sizeof(T), cudaMemcpyDeviceToDevice, s),
+                 "multigrid");
+    }
+    return;
   }
-#undef DC_AMG
+  const Level& c = levels_[l + 1];
+  T* u = t;  // residual scratch (Gauss-Seidel) / smoothed iterate (Jacobi)
+  T* xc = pick<T>(c.x, c.x32);
+  T* rc = pick<T>(c.rc, c.rc32);
+  if (smoother == Smoother::GaussSeidel) {
+    a.gs->template sor_sweep<T>(r, x, true, true, sc, slot, s);
+    count_launches(2);
+    DC_BS((k_residual<B, T><<<blocks_for(n), kT, 0, s>>>(n, a.rowptr, a.colidx, A, x, r, u, sc, slot)));
+    DC_BS((k_restrict<B, T><<<blocks_for(c.nrows), kT, 0, s>>>(c.nrows, c.own.agg_ptr.get(), c.own.agg_rows.get(), u,
+                                                               rc, sc, slot)));
+    cycle<T>(l + 1, rc, xc, sc, slot, s);
+    count_launches(1);
+    DC_BS((k_prolong<B, T><<<blocks_for(n * bs_), kT, 0, s>>>(n, a.agg.get(), xc, x, sc, slot)));
+    a.gs->template sor_sweep<T>(r, x, false, false, sc, slot, s);
+    return;
+  }
+  // (L1-)Jacobi: t = omega S r; u = r - A t (into x as scratch); coarse correction; x = y +
+  // omega S (r - A y) with y = t + P xc
+  const T* S = smoother == Smoother::L1Jacobi ? pick<T>(a.sinv_o, a.sinv32_o) : D;
+  count_launches(3);
+  DC_BS((k_smooth_first<B, T><<<blocks_for(n), kT, 0, s>>>(n, S, r, t, w, sc, slot)));
+  DC_BS((k_residual<B, T><<<blocks_for(n), kT, 0, s>>>(n, a.rowptr, a.colidx, A, t, r, x, sc, slot)));
+  DC_BS((k_restrict<B, T><<<blocks_for(c.nrows), kT, 0, s>>>(c.nrows, c.own.agg_ptr.get(), c.own.agg_rows.get(), x,
+                                                             rc, sc, slot)));
+  cycle<T>(l + 1, rc, xc, sc, slot, s);
+  count_launches(1);
+  DC_BS((k_prolong_smooth<B, T><<<blocks_for(n), kT, 0, s>>>(n, a.rowptr, a.colidx, A, S, a.agg.get(), xc, t, r, x, w,
+                                                             sc, slot)));
+#undef DC_BS
 }
 
-template void Amg::apply<double>(const double*, double*, const double*, int, cudaStream_t) const;
-template void Amg::apply<float>(const float*, float*, const double*, int, cudaStream_t) const;
+template <class T>
+void Amg::apply_t(const T* r, T* z, const double* sc, int done_slot, cudaStream_t s) const {
+  if (levels_.empty()) throw std::runtime_error("multigrid: not built");
+  if constexpr (std::is_same<T, float>::value) {
+    if (levels_[0].val32 == nullptr) throw std::runtime_error("multigrid: fp32 values not set up");
+  }
+  cycle<T>(0, r, z, sc, done_slot, s);
+}
+
+void Amg::apply(const double* r, double* z, const double* sc, int done_slot, cudaStream_t s) const {
+  apply_t<double>(r, z, sc, done_slot, s);
+}
+void Amg::apply(const float* r, float* z, const double* sc, int done_slot, cudaStream_t s) const {
+  apply_t<float>(r, z, sc, done_slot, s);
+}
 
 }  // namespace dcgpu

@@ -1,67 +1,96 @@
-// Aggregation algebraic multigrid on the block (BSR) Jacobian, applied as a V(1,1) cycle
-// with damped block-Jacobi smoothing.
+// Aggregation algebraic multigrid on the block (BSR) Jacobian, applied as one V(1,1) cycle
+// per preconditioner application.
 //
 // The reference offers no multigrid (its preconditioners are dune-istl's Richardson,
 // Jacobi, SSOR, SOR, Gauss-Seidel, ILU variants and BlockJacobi,
-// dune/copasi/solver/istl/factory/preconditioner.hh:226-256); this is the GPU engine's
+// dune/copasi/solver/istl/factory/preconditioner.hh:88-112); this is the GPU engine's
 // preconditioner for stiff, diffusion-dominated stage systems (large D dt / h^2), where
 // block Jacobi needs hundreds of Krylov iterations.
 //
-// Structure (once per model, on the host): the block-row graph is coarsened by greedy
-// aggregation restricted to rows of the same compartment (a row and its not yet aggregated
-// neighbours form an aggregate; leftovers join a neighbouring aggregate), level after level,
-// until a level has at most `min_rows` rows.  Prolongation is piecewise constant per
-// aggregate, so the Galerkin operator A_c = P^T A P is a sum of fine blocks; for every
-// coarse block the list of fine blocks that add into it is precomputed.
-// Values (every Newton iteration, on the device): coarse blocks are summed in a fixed
-// order (deterministic), each level's block-Jacobi inverse is formed, and fp32 copies are
-// kept for the mixed-precision Krylov path.
+// Structure (once per pattern, on the device): each level's block-row graph, restricted to
+// edges between rows of the same compartment, is coarsened around a distance-k maximal
+// independent set (graph.hpp): roots and the rows that join them form the aggregates.
+// Coarsening stops at a level small enough for the dense direct solve (at most
+// kDenseMax unknowns), at `max_levels`, or when it stalls.  Prolongation is piecewise
+// constant per aggregate, so the Galerkin operator A_c = P^T A P is a sum of fine blocks:
+// for every coarse block the list of the fine blocks that add into it is precomputed.
+// Values (every Newton iteration, on the device): coarse blocks are summed in a fixed order
+// (deterministic), every level's smoother is set up, and the coarsest operator is factored
+// by a dense FP64 LU with partial pivoting and inverted; fp32 copies of everything are kept
+// for the mixed-precision Krylov path.
+// Smoothers: damped block Jacobi, block L1-Jacobi (the diagonal block plus the absolute row
+// sums of the off-diagonal blocks on its diagonal), or multicolour block Gauss-Seidel
+// (forward sweep before the coarse correction, backward sweep after it: a symmetric cycle).
 #pragma once
 
 #include <cstdint>
+#include <memory>
 #include <vector>
 
 #include <cuda_runtime.h>
 
+#include "graph.hpp"
 #include "linalg.cuh"
+#include "mcolor.hpp"
 #include "model.hpp"
+#include "precond.hpp"
 
 namespace dcgpu {
 
-class Amg {
+class Amg : public Preconditioner {
  public:
+  enum class Smoother { Jacobi, L1Jacobi, GaussSeidel };
+  // largest coarsest level (unknowns) solved by the dense LU
+  static constexpr int kDenseMax = 128;
+
   Amg() = default;
   Amg(const Amg&) = delete;
   Amg& operator=(const Amg&) = delete;
 
-  // rows of different `group` are never aggregated together
-  void build(const std::vector<int32_t>& rowptr, const std::vector<int32_t>& colidx,
-             const std::vector<int32_t>& diag, const std::vector<int32_t>& group, int bs, int max_levels = 10,
-             int min_rows = 256);
-  // Galerkin values and smoother inverses of every coarse level from the fine values
+  // hierarchy of the pattern (device arrays, borrowed for level 0); rows of different
+  // `group` (device, null: one group) are never aggregated together
+  void build(int64_t nrows, int bs, int64_t nnzb, const int32_t* rowptr, const int32_t* colidx, const int32_t* diag,
+             const int32_t* group, cudaStream_t s);
+  // Galerkin values, smoothers and the coarse factorisation from the fine values
   // (fine_dinv: the fine block-Jacobi inverses already computed by the solver); with fp32,
   // float copies of every level as well (fine_vals32 / fine_dinv32 already converted)
   void setup(const double* fine_vals, const double* fine_dinv, const float* fine_vals32, const float* fine_dinv32,
              bool fp32, int* status, cudaStream_t s);
   // z = M^-1 r, one V(1,1)-cycle; no work when sc != nullptr and sc[done] != 0
-  template <class T>
-  void apply(const T* r, T* z, const double* sc, int done_slot, cudaStream_t s) const;
+  void apply(const double* r, double* z, const double* sc, int done_slot, cudaStream_t s) const override;
+  void apply(const float* r, float* z, const double* sc, int done_slot, cudaStream_t s) const override;
 
   int levels() const { return static_cast<int>(levels_.size()); }
   int64_t rows(int l) const { return levels_[l].nrows; }
+  int64_t blocks(int l) const { return levels_[l].nnzb; }
   bool built() const { return !levels_.empty(); }
+  bool dense_coarse() const { return dense_n_ > 0; }
+  int colors(int l) const { return levels_[l].gs ? levels_[l].gs->colors() : 0; }
+  // aggregate of every row of level l (l + 1 < levels()), the values of level l (fp64), the
+  // inverse of the coarsest operator (row-major, dense_coarse() only): for tests
+  std::vector<int32_t> aggregates_host(int l) const { return levels_[l].agg.download(); }
+  std::vector<double> values_host(int l) const;
+  std::vector<int32_t> rowptr_host(int l) const;
+  std::vector<int32_t> colidx_host(int l) const;
+  std::vector<double> coarse_inverse_host() const { return dinvd_.download(); }
 
-  double omega = 0.8;      // block-Jacobi damping
-  int coarse_sweeps = 6;   // block-Jacobi sweeps on the coarsest level
+  // parameters (read before build)
+  Smoother smoother = Smoother::Jacobi;
+  double omega = 0.8;        // smoother relaxation
+  int coarse_sweeps = 6;     // smoother sweeps on a coarsest level too large for the dense solve
+  int max_levels = 10;
+  int64_t coarsen_target = 0;  // stop coarsening at this many rows (0: the dense solve's limit)
+  int mis_distance = 2;      // aggregation around a distance-1 or distance-2 independent set
 
  private:
   struct Level {
     int64_t nrows = 0, nnzb = 0;
     // pattern of this level (level 0: borrowed from the model)
-    DeviceBuffer<int32_t> rowptr_o, colidx_o, diag_o;
     const int32_t* rowptr = nullptr;
     const int32_t* colidx = nullptr;
     const int32_t* diag = nullptr;
+    const int32_t* group = nullptr;
+    CoarseStructure own;  // this level's pattern when it is a coarse level
     // values of this level (level 0: borrowed from the solver)
     DeviceBuffer<double> val_o, dinv_o;
     DeviceBuffer<float> val32_o, dinv32_o;
@@ -69,14 +98,28 @@ class Amg {
     const double* dinv = nullptr;
     const float* val32 = nullptr;
     const float* dinv32 = nullptr;
-    // aggregation to the next level
-    DeviceBuffer<int32_t> agg, agg_ptr, agg_rows, gal_ptr, gal_src;
-    // work vectors (x: correction, t: residual), fp64 and fp32
+    // smoother inverses (L1-Jacobi: own; else the block-Jacobi inverses above)
+    DeviceBuffer<double> sinv_o;
+    DeviceBuffer<float> sinv32_o;
+    std::unique_ptr<ColorPrecond> gs;  // Gauss-Seidel smoother: colouring of this level
+    // aggregation to the next level (agg_ptr / agg_rows / gal_* live in the next level's own)
+    DeviceBuffer<int32_t> agg;
+    // work vectors: x the correction, t the smoothed iterate / residual, rc the right-hand side
     DeviceBuffer<double> x, t, rc;
     DeviceBuffer<float> x32, t32, rc32;
   };
+  template <class T>
+  void cycle(int l, const T* r, T* x, const double* sc, int slot, cudaStream_t s) const;
+  template <class T>
+  void apply_t(const T* r, T* z, const double* sc, int done_slot, cudaStream_t s) const;
+
   std::vector<Level> levels_;
   int bs_ = 1;
+  // dense coarsest solve: n unknowns, the operator's inverse (row-major) in fp64 / fp32
+  int dense_n_ = 0;
+  DeviceBuffer<double> dense_, dinvd_;
+  DeviceBuffer<float> dinvf_;
+  DeviceBuffer<int32_t> dense_piv_;
 };
 
 }  // namespace dcgpu

@@ -5,7 +5,10 @@
 #include <string>
 
 #include "../../include/dcgpu.h"
+#include "amg.hpp"
+#include "graph.hpp"
 #include "handle.hpp"
+#include "mcolor.hpp"
 
 namespace {
 
@@ -474,6 +477,171 @@ int dc_selftest_barrier_timeout(double* gave_up_blocks, double* elapsed_ms) {
     if (!gave_up_blocks || !elapsed_ms) throw std::invalid_argument("null argument");
     if (dcgpu::barrier_selftest(gave_up_blocks, elapsed_ms) != 0)
       throw std::runtime_error("barrier self-test: CUDA error");
+    return DC_OK;
+  });
+}
+
+namespace {
+
+void require_device() {
+  int dev_count = 0;
+  dcgpu::cuda_check(cudaGetDeviceCount(&dev_count), "cudaGetDeviceCount");
+  if (dev_count == 0) throw dcgpu::CudaError("no CUDA device");
+}
+
+// host CSR graph -> device copies (validated)
+struct HostGraph {
+  dcgpu::DeviceBuffer<int32_t> rowptr, colidx, group;
+  HostGraph(int64_t n, const int32_t* rp, const int32_t* ci, const int32_t* grp) {
+    if (n <= 0 || n >= (int64_t(1) << 31) || !rp || !ci) throw std::invalid_argument("bad graph");
+    std::vector<int32_t> r(rp, rp + n + 1);
+    if (r[0] != 0) throw std::invalid_argument("rowptr[0] must be 0");
+    for (int64_t i = 0; i < n; ++i)
+      if (r[i + 1] < r[i]) throw std::invalid_argument("rowptr must not decrease");
+    std::vector<int32_t> c(ci, ci + r[n]);
+    for (int32_t v : c)
+      if (v < 0 || v >= n) throw std::invalid_argument("column index out of range");
+    rowptr.upload(r);
+    colidx.upload(c);
+    if (grp) group.upload(std::vector<int32_t>(grp, grp + n));
+  }
+};
+
+double param(const std::string& params, const std::string& key, double dflt) {
+  size_t pos = 0;
+  while (pos < params.size()) {
+    size_t end = params.find(';', pos);
+    if (end == std::string::npos) end = params.size();
+    const std::string item = params.substr(pos, end - pos);
+    const size_t eq = item.find('=');
+    if (eq != std::string::npos && item.substr(0, eq) == key) return std::stod(item.substr(eq + 1));
+    pos = end + 1;
+  }
+  return dflt;
+}
+
+}  // namespace
+
+int dc_selftest_color(int64_t nrows, const int32_t* rowptr, const int32_t* colidx, int32_t* colour_out,
+                      int32_t* ncolours) {
+  return guarded([&] {
+    if (!colour_out || !ncolours) throw std::invalid_argument("null argument");
+    require_device();
+    HostGraph g(nrows, rowptr, colidx, nullptr);
+    dcgpu::DeviceGraph dg;
+    dg.n = nrows;
+    dg.rowptr = g.rowptr.get();
+    dg.colidx = g.colidx.get();
+    dcgpu::DeviceBuffer<int32_t> colour(static_cast<size_t>(nrows));
+    *ncolours = dcgpu::color_rows(dg, colour.get(), cudaStreamLegacy);
+    dcgpu::cuda_check(cudaMemcpy(colour_out, colour.get(), nrows * sizeof(int32_t), cudaMemcpyDeviceToHost), "colour");
+    return DC_OK;
+  });
+}
+
+int dc_selftest_aggregate(int64_t nrows, const int32_t* rowptr, const int32_t* colidx, const int32_t* group,
+                          int32_t distance, int32_t* agg_out, int64_t* naggregates) {
+  return guarded([&] {
+    if (!agg_out || !naggregates) throw std::invalid_argument("null argument");
+    if (distance != 1 && distance != 2) throw std::invalid_argument("distance must be 1 or 2");
+    require_device();
+    HostGraph g(nrows, rowptr, colidx, group);
+    dcgpu::DeviceGraph dg;
+    dg.n = nrows;
+    dg.rowptr = g.rowptr.get();
+    dg.colidx = g.colidx.get();
+    dg.group = group ? g.group.get() : nullptr;
+    dcgpu::DeviceBuffer<int32_t> agg(static_cast<size_t>(nrows));
+    *naggregates = dcgpu::aggregate_mis(dg, distance, agg.get(), cudaStreamLegacy);
+    dcgpu::cuda_check(cudaMemcpy(agg_out, agg.get(), nrows * sizeof(int32_t), cudaMemcpyDeviceToHost), "aggregate");
+    return DC_OK;
+  });
+}
+
+int dc_selftest_precond(const char* kind, const char* params, int64_t nrows, int32_t bs, const int32_t* rowptr,
+                        const int32_t* colidx, const double* vals, const int32_t* group, const double* r, double* z,
+                        int32_t fp32, double* info) {
+  return guarded([&] {
+    if (!kind || !vals || !r || !z) throw std::invalid_argument("null argument");
+    if (bs < 1 || bs > 8) throw std::invalid_argument("block size must be in [1, 8]");
+    require_device();
+    const std::string k = kind, prm = params ? params : "";
+    HostGraph g(nrows, rowptr, colidx, group);
+    const int64_t nnzb = rowptr[nrows];
+    std::vector<int32_t> diag(static_cast<size_t>(nrows), -1);
+    for (int64_t i = 0; i < nrows; ++i)
+      for (int32_t e = rowptr[i]; e < rowptr[i + 1]; ++e)
+        if (colidx[e] == i) diag[i] = e;
+    for (int32_t d : diag)
+      if (d < 0) throw std::invalid_argument("a row without its diagonal block");
+    const size_t b2 = static_cast<size_t>(bs) * bs, nv = static_cast<size_t>(nrows) * bs;
+    dcgpu::DeviceBuffer<int32_t> ddiag, status(1);
+    ddiag.upload(diag);
+    dcgpu::DeviceBuffer<double> dval, dinv(static_cast<size_t>(nrows) * b2), dr, dz(nv);
+    dval.upload(std::vector<double>(vals, vals + nnzb * b2));
+    dr.upload(std::vector<double>(r, r + nv));
+    dcgpu::DeviceBuffer<float> fval(static_cast<size_t>(nnzb) * b2), fdinv(static_cast<size_t>(nrows) * b2),
+        fr(nv), fz(nv);
+    cudaStream_t s = cudaStreamLegacy;
+    dcgpu::cuda_check(cudaMemset(status.get(), 0, sizeof(int)), "memset");
+    dcgpu::Bsr A;
+    A.nrows = static_cast<int>(nrows);
+    A.bs = bs;
+    A.nnzb = nnzb;
+    A.rowptr = g.rowptr.get();
+    A.colidx = g.colidx.get();
+    A.val = dval.get();
+    dcgpu::block_jacobi_setup(A, ddiag.get(), dinv.get(), status.get(), s, fdinv.get());
+    dcgpu::to_float(static_cast<int64_t>(nnzb * b2), dval.get(), fval.get(), s);
+    dcgpu::to_float(static_cast<int64_t>(nv), dr.get(), fr.get(), s);
+    std::unique_ptr<dcgpu::Preconditioner> pc;
+    double inf[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (k == "AMG") {
+      auto amg = std::make_unique<dcgpu::Amg>();
+      const int smi = static_cast<int>(param(prm, "smoother", 0));
+      amg->smoother = smi == 0 ? dcgpu::Amg::Smoother::Jacobi
+                               : smi == 1 ? dcgpu::Amg::Smoother::L1Jacobi : dcgpu::Amg::Smoother::GaussSeidel;
+      amg->omega = param(prm, "relaxation", smi == 0 ? 0.8 : 1.0);
+      amg->coarse_sweeps = static_cast<int>(param(prm, "coarse_sweeps", 6));
+      amg->max_levels = static_cast<int>(param(prm, "max_level", 10));
+      amg->coarsen_target = static_cast<int64_t>(param(prm, "coarsen_target", 0));
+      amg->mis_distance = static_cast<int>(param(prm, "aggregation_distance", 2));
+      amg->build(nrows, bs, nnzb, g.rowptr.get(), g.colidx.get(), ddiag.get(), group ? g.group.get() : nullptr, s);
+      amg->setup(dval.get(), dinv.get(), fval.get(), fdinv.get(), fp32 != 0, status.get(), s);
+      inf[0] = amg->levels();
+      inf[1] = amg->dense_coarse() ? static_cast<double>(amg->rows(amg->levels() - 1) * bs) : 0.0;
+      for (int l = 0; l < amg->levels() && l < 6; ++l) inf[2 + l] = static_cast<double>(amg->rows(l));
+      pc = std::move(amg);
+    } else {
+      dcgpu::ColorPrecond::Kind kd;
+      if (k == "SSOR") kd = dcgpu::ColorPrecond::Kind::Ssor;
+      else if (k == "SOR") kd = dcgpu::ColorPrecond::Kind::Sor;
+      else if (k == "ILU") kd = dcgpu::ColorPrecond::Kind::Ilu0;
+      else if (k == "DILU") kd = dcgpu::ColorPrecond::Kind::Dilu;
+      else throw std::invalid_argument("unknown preconditioner kind " + k);
+      auto mc = std::make_unique<dcgpu::ColorPrecond>();
+      mc->omega = param(prm, "relaxation", 1.0);
+      mc->iterations = static_cast<int>(param(prm, "iterations", 1));
+      mc->build(kd, nrows, bs, nnzb, g.rowptr.get(), g.colidx.get(), ddiag.get(), s);
+      mc->setup(dval.get(), dinv.get(), fval.get(), fdinv.get(), fp32 != 0, status.get(), s);
+      inf[0] = mc->colors();
+      pc = std::move(mc);
+    }
+    int st = 0;
+    dcgpu::cuda_check(cudaMemcpy(&st, status.get(), sizeof(int), cudaMemcpyDeviceToHost), "status");
+    if (st) throw dcgpu::StepFailure("singular block in the preconditioner set-up");
+    std::vector<double> out(nv);
+    if (fp32) {
+      pc->apply(fr.get(), fz.get(), nullptr, 0, s);
+      std::vector<float> o(nv);
+      dcgpu::cuda_check(cudaMemcpy(o.data(), fz.get(), nv * sizeof(float), cudaMemcpyDeviceToHost), "result");
+      for (size_t q = 0; q < nv; ++q) out[q] = o[q];
+    } else {
+      pc->apply(dr.get(), dz.get(), nullptr, 0, s);
+      dcgpu::cuda_check(cudaMemcpy(out.data(), dz.get(), nv * sizeof(double), cudaMemcpyDeviceToHost), "result");
+    }
+    std::memcpy(z, out.data(), nv * sizeof(double));
+    if (info) std::memcpy(info, inf, sizeof(inf));
     return DC_OK;
   });
 }

@@ -1,6 +1,6 @@
 #include "krylov.cuh"
 
-#include "amg.hpp"
+#include "precond.hpp"
 
 #include <stdexcept>
 #include <string>
@@ -537,11 +537,11 @@ __global__ void __launch_bounds__(kThreads) k_cg_rz(int64_t n, const T* __restri
 
 template <class T, class V>
 void cg_init(const Bsr& A, const V* dinv, const KrylovVectors<T>& k, double rel, ReduceScratch rs, double* sc,
-             cudaStream_t s, const Amg* amg) {
-  count_launches(amg ? 2 : 1);
+             cudaStream_t s, const Preconditioner* pc) {
+  count_launches(pc ? 2 : 1);
 #define DC_CGI(B)                                                                                              \
   case B:                                                                                                      \
-    if (amg)                                                                                                   \
+    if (pc)                                                                                                   \
       k_cg_init<B, T, V, false><<<kReduceBlocks, kThreads, 0, s>>>(A.nrows, k.x, k.r, k.p, k.s, dinv, rel, rs, \
                                                                    sc);                                        \
     else                                                                                                       \
@@ -553,17 +553,17 @@ void cg_init(const Bsr& A, const V* dinv, const KrylovVectors<T>& k, double rel,
     default: throw std::runtime_error("cg: block size " + std::to_string(A.bs) + " unsupported");
   }
 #undef DC_CGI
-  if (amg) {
-    amg->apply<T>(k.r, k.s, sc, KS_DONE, s);
+  if (pc) {
+    pc->apply(k.r, k.s, sc, KS_DONE, s);
     k_cg_rz<T><<<kReduceBlocks, kThreads, 0, s>>>(static_cast<int64_t>(A.nrows) * A.bs, k.r, k.s, rs, sc);
   }
 }
 
 template <class T, class V>
 void cg_iteration(const Bsr& A, const V* vals, const V* dinv, const KrylovVectors<T>& k, ReduceScratch rs,
-                  double* sc, cudaStream_t s, const Amg* amg, const Sell* sell) {
+                  double* sc, cudaStream_t s, const Preconditioner* pc, const Sell* sell) {
   const int64_t n = static_cast<int64_t>(A.nrows) * A.bs;
-  count_launches(amg ? 4 : 3);
+  count_launches(pc ? 4 : 3);
   k_cg_p<T><<<grid_for(n), kThreads, 0, s>>>(n, k.p, k.s, sc);
 #define DC_CG(B)                                                                                                  \
   case B:                                                                                                         \
@@ -573,7 +573,7 @@ void cg_iteration(const Bsr& A, const V* vals, const V* dinv, const KrylovVector
     else                                                                                                          \
       k_spmv_rv<B, T, V><<<kReduceBlocks, kThreads, 0, s>>>(A.nrows, A.rowptr, A.colidx, vals, k.p, k.v, k.p, rs, \
                                                             sc);                                                  \
-    if (amg)                                                                                                      \
+    if (pc)                                                                                                      \
       k_cg_update<B, T, V, false><<<kReduceBlocks, kThreads, 0, s>>>(A.nrows, k.x, k.r, k.s, k.p, k.v, dinv, rs, \
                                                                      sc);                                         \
     else                                                                                                          \
@@ -585,20 +585,20 @@ void cg_iteration(const Bsr& A, const V* vals, const V* dinv, const KrylovVector
     default: throw std::runtime_error("cg: block size " + std::to_string(A.bs) + " unsupported");
   }
 #undef DC_CG
-  if (amg) {
-    amg->apply<T>(k.r, k.s, sc, KS_DONE, s);
+  if (pc) {
+    pc->apply(k.r, k.s, sc, KS_DONE, s);
     k_cg_rz<T><<<kReduceBlocks, kThreads, 0, s>>>(n, k.r, k.s, rs, sc);
   }
 }
 
 template void cg_init<double, double>(const Bsr&, const double*, const KrylovVectors<double>&, double, ReduceScratch,
-                                      double*, cudaStream_t, const Amg*);
+                                      double*, cudaStream_t, const Preconditioner*);
 template void cg_init<float, float>(const Bsr&, const float*, const KrylovVectors<float>&, double, ReduceScratch,
-                                    double*, cudaStream_t, const Amg*);
+                                    double*, cudaStream_t, const Preconditioner*);
 template void cg_iteration<double, double>(const Bsr&, const double*, const double*, const KrylovVectors<double>&,
-                                           ReduceScratch, double*, cudaStream_t, const Amg*, const Sell*);
+                                           ReduceScratch, double*, cudaStream_t, const Preconditioner*, const Sell*);
 template void cg_iteration<float, float>(const Bsr&, const float*, const float*, const KrylovVectors<float>&,
-                                         ReduceScratch, double*, cudaStream_t, const Amg*, const Sell*);
+                                         ReduceScratch, double*, cudaStream_t, const Preconditioner*, const Sell*);
 
 template <class T>
 void krylov_init(const KrylovVectors<T>& k, int64_t n, double rel, ReduceScratch rs, double* sc, cudaStream_t s) {
@@ -608,7 +608,7 @@ void krylov_init(const KrylovVectors<T>& k, int64_t n, double rel, ReduceScratch
 
 template <class T, class V>
 void krylov_iteration(const Bsr& A, const V* vals, const V* dinv, const KrylovVectors<T>& k, ReduceScratch rs,
-                      double* sc, cudaStream_t s, cudaEvent_t* ev, const Amg* amg, const Sell* sell) {
+                      double* sc, cudaStream_t s, cudaEvent_t* ev, const Preconditioner* pc, const Sell* sell) {
   const int64_t n = static_cast<int64_t>(A.nrows) * A.bs;
   const int gn = grid_for(A.nrows);
   count_launches(5);
@@ -619,9 +619,9 @@ void krylov_iteration(const Bsr& A, const V* vals, const V* dinv, const KrylovVe
   };
 #define DC_KR(B)                                                                                                 \
   case B:                                                                                                        \
-    if (amg) {                                                                                                   \
+    if (pc) {                                                                                                   \
       k_update_p<B, T, V, false><<<gn, kThreads, 0, s>>>(A.nrows, k.p, k.r, k.v, dinv, k.phat, sc);              \
-      amg->apply<T>(k.p, k.phat, sc, KS_DONE, s);                                                                \
+      pc->apply(k.p, k.phat, sc, KS_DONE, s);                                                                \
     } else {                                                                                                     \
       k_update_p<B, T, V, true><<<gn, kThreads, 0, s>>>(A.nrows, k.p, k.r, k.v, dinv, k.phat, sc);               \
     }                                                                                                            \
@@ -632,10 +632,10 @@ void krylov_iteration(const Bsr& A, const V* vals, const V* dinv, const KrylovVe
       k_spmv_rv<B, T, V><<<kReduceBlocks, kThreads, 0, s>>>(A.nrows, A.rowptr, A.colidx, vals, k.phat, k.v,      \
                                                             k.rhat, rs, sc);                                     \
     mark(1);                                                                                                     \
-    if (amg) {                                                                                                   \
+    if (pc) {                                                                                                   \
       k_update_s<B, T, V, false><<<kReduceBlocks, kThreads, 0, s>>>(A.nrows, k.s, k.r, k.v, dinv, k.shat, rs,    \
                                                                     sc);                                         \
-      amg->apply<T>(k.s, k.shat, sc, KS_DONE, s);                                                                \
+      pc->apply(k.s, k.shat, sc, KS_DONE, s);                                                                \
     } else {                                                                                                     \
       k_update_s<B, T, V, true><<<kReduceBlocks, kThreads, 0, s>>>(A.nrows, k.s, k.r, k.v, dinv, k.shat, rs, sc); \
     }                                                                                                            \
@@ -658,10 +658,10 @@ void krylov_iteration(const Bsr& A, const V* vals, const V* dinv, const KrylovVe
 template void krylov_init<double>(const KrylovVectors<double>&, int64_t, double, ReduceScratch, double*, cudaStream_t);
 template void krylov_init<float>(const KrylovVectors<float>&, int64_t, double, ReduceScratch, double*, cudaStream_t);
 template void krylov_iteration<double, double>(const Bsr&, const double*, const double*, const KrylovVectors<double>&,
-                                               ReduceScratch, double*, cudaStream_t, cudaEvent_t*, const Amg*,
+                                               ReduceScratch, double*, cudaStream_t, cudaEvent_t*, const Preconditioner*,
                                                const Sell*);
 template void krylov_iteration<float, float>(const Bsr&, const float*, const float*, const KrylovVectors<float>&,
-                                             ReduceScratch, double*, cudaStream_t, cudaEvent_t*, const Amg*,
+                                             ReduceScratch, double*, cudaStream_t, cudaEvent_t*, const Preconditioner*,
                                              const Sell*);
 
 }  // namespace dcgpu

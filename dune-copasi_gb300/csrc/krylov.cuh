@@ -103,9 +103,10 @@ void krylov_init(const KrylovVectors<T>& k, int64_t n, double rel, ReduceScratch
 
 // one iteration (five launches); V is the matrix / preconditioner value type.  When `ev`
 // is given, ev[0..1] bracket the first SpMV kernel and ev[2..3] the second.
-// With `amg`, the preconditioner is one multigrid V-cycle instead of block Jacobi.  With
-// `sell`, the two SpMVs read `vals` in that SELL-32 layout instead of A's BSR layout.
-class Amg;
+// With `pc`, the preconditioner is pc->apply (a separate launch sequence) instead of the
+// block-Jacobi inverse `dinv` fused into the update kernels.  With `sell`, the two SpMVs
+// read `vals` in that SELL-32 layout instead of A's BSR layout.
+class Preconditioner;
 
 // Preconditioned CG (dune-istl CGSolver; also used for GeneralizedPCG / RestartedFCG /
 // CompleteFCG, which coincide with CG for a fixed preconditioner).  cg_init: x = 0, z =
@@ -114,14 +115,14 @@ class Amg;
 // z in `s`, q in `v`.  Same device scalars, done flag and graph capture as BiCGSTAB.
 template <class T, class V>
 void cg_init(const Bsr& A, const V* dinv, const KrylovVectors<T>& k, double rel, ReduceScratch rs, double* sc,
-             cudaStream_t s, const Amg* amg = nullptr);
+             cudaStream_t s, const Preconditioner* pc = nullptr);
 template <class T, class V>
 void cg_iteration(const Bsr& A, const V* vals, const V* dinv, const KrylovVectors<T>& k, ReduceScratch rs,
-                  double* sc, cudaStream_t s, const Amg* amg = nullptr, const Sell* sell = nullptr);
+                  double* sc, cudaStream_t s, const Preconditioner* pc = nullptr, const Sell* sell = nullptr);
 
 template <class T, class V>
 void krylov_iteration(const Bsr& A, const V* vals, const V* dinv, const KrylovVectors<T>& k, ReduceScratch rs,
-                      double* sc, cudaStream_t s, cudaEvent_t* ev = nullptr, const Amg* amg = nullptr,
+                      double* sc, cudaStream_t s, cudaEvent_t* ev = nullptr, const Preconditioner* pc = nullptr,
                       const Sell* sell = nullptr);
 
 }  // namespace dcgpu

@@ -159,20 +159,7 @@ Solver::Solver(Model& m, cudaStream_t s) : model(m), stream(s) {
   // the last correction of the direct-solve one
   direct_tol_ = ls.get_double("direct_tolerance", 1e-10);
   if (!(direct_tol_ > 0.0 && direct_tol_ < 1.0)) throw ConfigError("linear_solver.direct_tolerance must be in (0, 1)");
-  precond_ = ls.get("preconditioner.type", "Jacobi");
-  // every dune-istl preconditioner of the reference's registry (Richardson, Jacobi, SSOR,
-  // SOR, GaussSeidel, BlockJacobi, ILU variants) maps to block Jacobi on the device; "AMG"
-  // selects the aggregation multigrid V-cycle
-  use_amg_ = (precond_ == "AMG");
-  if (use_amg_) {
-    std::vector<int32_t> group(m.nnodes, 0);
-    for (size_t c = 0; c < m.comp_names.size(); ++c)
-      for (int64_t k = m.comp_node_offset[c]; k < m.comp_node_offset[c + 1]; ++k) group[k] = static_cast<int32_t>(c);
-    amg_.omega = ls.get_double("preconditioner.relaxation", 0.8);
-    amg_.coarse_sweeps = static_cast<int>(ls.get_long("preconditioner.coarse_sweeps", 6));
-    amg_.build(m.rowptr, m.colidx, m.diag, group, m.bs, static_cast<int>(ls.get_long("preconditioner.max_level", 10)),
-               static_cast<int>(ls.get_long("preconditioner.coarsen_target", 256)));
-  }
+  configure_preconditioner(ls);
   const bool want_mixed = ls.get("precision", "double") == "mixed";
   // linear_solver.matrix_free (make_step_operator.hh:201,289-293): the reference then applies
   // the stage Jacobian through the local operators' jacobian_apply without a matrix.  The
@@ -214,6 +201,80 @@ Solver::Solver(Model& m, cudaStream_t s) : model(m), stream(s) {
   set_state(init, tso.get_double("time_begin", 0.0));
 }
 
+// linear_solver.preconditioner (the reference's registry,
+// dune/copasi/solver/istl/factory/preconditioner.hh:88-118; dune-istl parameter names):
+//   Jacobi, BlockJacobi (default)  block Jacobi on the node blocks, fused into the Krylov
+//                                  kernels; the reference's default SSOR is the key's
+//                                  default only for its iterative solvers, whose
+//                                  convergence (not their result) depends on it
+//   SSOR, SOR, GaussSeidel         multicolour block SSOR / forward SOR (iterations,
+//                                  relaxation; Gauss-Seidel: SOR with relaxation 1)
+//   ILU (any fill level n), ILDL   multicolour block ILU(0) (relaxation)
+//   DILU                           multicolour block DILU (relaxation)
+//   Richardson                     z = relaxation * r
+//   AMG                            the aggregation multigrid V-cycle (engine addition)
+// InverseOperator (an inner solver as preconditioner) runs as block Jacobi: the outer
+// solve converges to the same tolerance.
+void Solver::configure_preconditioner(const Ini& ls) {
+  const Model& m = model;
+  precond_ = ls.get("preconditioner.type", "Jacobi");
+  const std::string& p = precond_;
+  auto mc = [&](ColorPrecond::Kind kind, double omega_default) {
+    mc_ = std::make_unique<ColorPrecond>();
+    mc_->omega = ls.get_double("preconditioner.relaxation", omega_default);
+    mc_->iterations = static_cast<int>(ls.get_long("preconditioner.iterations", 1));
+    if (mc_->iterations < 1 || mc_->iterations > 100)
+      throw ConfigError("linear_solver.preconditioner.iterations must be in [1, 100]");
+    if (!(mc_->omega > 0.0 && mc_->omega < 2.0))
+      throw ConfigError("linear_solver.preconditioner.relaxation must be in (0, 2)");
+    mc_->build(kind, m.nnodes, m.bs, m.nnzb(), m.d_rowptr.get(), m.d_colidx.get(), m.d_diag.get(), stream);
+    pc_ = mc_.get();
+  };
+  if (p == "Jacobi" || p == "BlockJacobi" || p == "InverseOperator") {
+    pc_ = nullptr;
+  } else if (p == "SSOR") {
+    mc(ColorPrecond::Kind::Ssor, 1.0);
+  } else if (p == "SOR") {
+    mc(ColorPrecond::Kind::Sor, 1.0);
+  } else if (p == "GaussSeidel") {
+    mc(ColorPrecond::Kind::Sor, 1.0);
+    mc_->omega = 1.0;
+  } else if (p == "ILU" || p == "ILDL") {
+    mc(ColorPrecond::Kind::Ilu0, 1.0);
+  } else if (p == "DILU") {
+    mc(ColorPrecond::Kind::Dilu, 1.0);
+  } else if (p == "Richardson") {
+    rich_.omega = ls.get_double("preconditioner.relaxation", 1.0);
+    rich_.n = n_;
+    pc_ = &rich_;
+  } else if (p == "AMG") {
+    amg_ = std::make_unique<Amg>();
+    const std::string sm = ls.get("preconditioner.smoother", "jacobi");
+    if (sm == "jacobi") amg_->smoother = Amg::Smoother::Jacobi;
+    else if (sm == "l1jacobi") amg_->smoother = Amg::Smoother::L1Jacobi;
+    else if (sm == "gauss_seidel") amg_->smoother = Amg::Smoother::GaussSeidel;
+    else throw ConfigError("linear_solver.preconditioner.smoother must be jacobi, l1jacobi or gauss_seidel, not '" +
+                           sm + "'");
+    amg_->omega = ls.get_double("preconditioner.relaxation", sm == "jacobi" ? 0.8 : 1.0);
+    amg_->coarse_sweeps = static_cast<int>(ls.get_long("preconditioner.coarse_sweeps", 6));
+    amg_->max_levels = static_cast<int>(ls.get_long("preconditioner.max_level", 10));
+    amg_->coarsen_target = ls.get_long("preconditioner.coarsen_target", 0);
+    amg_->mis_distance = static_cast<int>(ls.get_long("preconditioner.aggregation_distance", 2));
+    if (amg_->mis_distance != 1 && amg_->mis_distance != 2)
+      throw ConfigError("linear_solver.preconditioner.aggregation_distance must be 1 or 2");
+    if (amg_->max_levels < 1) throw ConfigError("linear_solver.preconditioner.max_level must be >= 1");
+    std::vector<int32_t> group(m.nnodes, 0);
+    for (size_t c = 0; c < m.comp_names.size(); ++c)
+      for (int64_t k = m.comp_node_offset[c]; k < m.comp_node_offset[c + 1]; ++k) group[k] = static_cast<int32_t>(c);
+    row_group_.upload(group);
+    amg_->build(m.nnodes, m.bs, m.nnzb(), m.d_rowptr.get(), m.d_colidx.get(), m.d_diag.get(), row_group_.get(),
+                stream);
+    pc_ = amg_.get();
+  } else {
+    throw ConfigError("The key '" + p + "' is not a known preconditioner type");
+  }
+}
+
 void Solver::enable_mixed(bool on) {
   mixed_precision = on;
   if (on && fr_.size() != static_cast<size_t>(n_)) {
@@ -221,7 +282,7 @@ void Solver::enable_mixed(bool on) {
     fphat_.resize(n_); fshat_.resize(n_); fx_.resize(n_); fb_.resize(n_);
     fp2_.resize(n_); fv2_.resize(n_);
     fdinv_.resize(static_cast<size_t>(model.nnodes) * model.bs * model.bs);
-    if (spmv_request_ != kSpmvSell || use_amg_) J32_.resize(static_cast<size_t>(model.nnzb()) * model.bs * model.bs);
+    if (spmv_request_ != kSpmvSell || pc_) J32_.resize(static_cast<size_t>(model.nnzb()) * model.bs * model.bs);
     if (spmv_request_ != kSpmvBsr) {
       // the padding slots stay zero: the fused gather of Model::assemble writes real blocks only
       Js32_.resize(static_cast<size_t>(model.sell_slots) * 32 * model.bs * model.bs);
@@ -258,7 +319,7 @@ void Solver::tune_spmv() {
   cudaEventDestroy(e1);
   spmv_format = spmv_tune_us[1] < spmv_tune_us[0] ? kSpmvSell : kSpmvBsr;
   if (spmv_format == kSpmvBsr) Js32_.resize(0);
-  else if (!use_amg_) J32_.resize(0);
+  else if (!pc_) J32_.resize(0);
 }
 
 Solver::~Solver() {
@@ -376,7 +437,7 @@ void Solver::setup_preconditioner() {
   block_jacobi_setup(A, model.d_diag.get(), dinv_.get(), status_.get(), stream,
                      mixed_precision ? fdinv_.get() : nullptr);
   int st = 0;
-  if (!use_amg_) {
+  if (!pc_) {
     // read with the solve's own result instead of a stream synchronisation of its own
     // (check_setup_status); a singular block only makes that solve's values meaningless
     cuda_check(cudaMemcpyAsync(pinned_status(), status_.get(), sizeof(int), cudaMemcpyDeviceToHost, stream),
@@ -388,19 +449,21 @@ void Solver::setup_preconditioner() {
     if (st) throw StepFailure("singular diagonal block in the Jacobian");
   }
   if (mixed_precision) {
-    // the BSR copy feeds the BSR SpMV, the tuner and the multigrid fine level; the SELL-32
-    // copy feeds the SELL SpMV
-    const bool need_bsr = spmv_format != kSpmvSell || use_amg_;
+    // the BSR copy feeds the BSR SpMV, the tuner and the separately launched
+    // preconditioners; the SELL-32 copy feeds the SELL SpMV
+    const bool need_bsr = spmv_format != kSpmvSell || pc_;
     const bool need_sell = spmv_format != kSpmvBsr;
     if (need_bsr) to_float(static_cast<int64_t>(model.nnzb()) * model.bs * model.bs, J_.get(), J32_.get(), stream);
     if (need_sell && !jac_sell_fresh_) bsr_to_sell(A, J_.get(), model.sell(), Js32_.get(), stream);
     if (spmv_format == kSpmvAuto) tune_spmv();
   }
-  if (use_amg_) {
-    amg_.setup(J_.get(), dinv_.get(), J32_.get(), fdinv_.get(), mixed_precision, status_.get(), stream);
+  if (amg_ || mc_) {
+    if (amg_) amg_->setup(J_.get(), dinv_.get(), J32_.get(), fdinv_.get(), mixed_precision, status_.get(), stream);
+    else mc_->setup(J_.get(), dinv_.get(), J32_.get(), fdinv_.get(), mixed_precision, status_.get(), stream);
     cuda_check(cudaMemcpyAsync(&st, status_.get(), sizeof(int), cudaMemcpyDeviceToHost, stream), "status");
     cuda_check(cudaStreamSynchronize(stream), "status");
-    if (st) throw StepFailure("singular diagonal block in a coarse multigrid level");
+    if (st) throw StepFailure(amg_ ? "singular diagonal block in a coarse multigrid level"
+                                   : "singular pivot block in the preconditioner factorisation");
   }
 }
 
@@ -425,20 +488,20 @@ cudaGraphExec_t Solver::krylov_graph(bool fp32) {
   cuda_check(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
   for (int k = 0; k < kKrylovChunk; ++k) {
     cudaEvent_t* e = ev ? ev + 4 * k : nullptr;
-    const Amg* amg = use_amg_ ? &amg_ : nullptr;
+    const Preconditioner* pc = pc_;
     if (fp32) {
       KrylovVectors<float> kv{fx_.get(), fr_.get(), frhat_.get(), fp_.get(), fv_.get(), fs_.get(), ft_.get(),
                               fphat_.get(), fshat_.get()};
       const bool sell = spmv_format == kSpmvSell;
       const Sell S = model.sell();
       const float* vals = sell ? Js32_.get() : J32_.get();
-      if (krylov_cg_) cg_iteration<float, float>(A, vals, fdinv_.get(), kv, rs_, sc, stream, amg, sell ? &S : nullptr);
-      else krylov_iteration<float, float>(A, vals, fdinv_.get(), kv, rs_, sc, stream, e, amg, sell ? &S : nullptr);
+      if (krylov_cg_) cg_iteration<float, float>(A, vals, fdinv_.get(), kv, rs_, sc, stream, pc, sell ? &S : nullptr);
+      else krylov_iteration<float, float>(A, vals, fdinv_.get(), kv, rs_, sc, stream, e, pc, sell ? &S : nullptr);
     } else {
       KrylovVectors<double> kv{kx_.get(), kr_.get(), krhat_.get(), kp_.get(), kv_.get(), ks_.get(), kt_.get(),
                                kphat_.get(), kshat_.get()};
-      if (krylov_cg_) cg_iteration<double, double>(A, J_.get(), dinv_.get(), kv, rs_, sc, stream, amg);
-      else krylov_iteration<double, double>(A, J_.get(), dinv_.get(), kv, rs_, sc, stream, e, amg);
+      if (krylov_cg_) cg_iteration<double, double>(A, J_.get(), dinv_.get(), kv, rs_, sc, stream, pc);
+      else krylov_iteration<double, double>(A, J_.get(), dinv_.get(), kv, rs_, sc, stream, e, pc);
     }
   }
   cuda_check(cudaStreamEndCapture(stream, &g), "cudaStreamEndCapture");
@@ -478,11 +541,11 @@ int Solver::gmres_t(double rel, int max_it, int* iters) {
   double* hn = gh_.get() + 2 * (m + 2);
   const Bsr A = model.bsr(J_.get(), J32_.get());
   const Sell S = model.sell();
-  // the multigrid cycle checks a device "done" flag: keep it cleared
+  // the preconditioner launches check a device "done" flag: keep it cleared
   cuda_check(cudaMemsetAsync(scal_.get(), 0, KS_COUNT * sizeof(double), stream), "memset");
   auto precond = [&](const T* in, T* out) {
-    if (use_amg_) {
-      amg_.apply<T>(in, out, scal_.get(), KS_DONE, stream);
+    if (pc_) {
+      pc_->apply(in, out, scal_.get(), KS_DONE, stream);
     } else if constexpr (f32) {
       block_jacobi_apply32(static_cast<int>(model.nnodes), model.bs, fdinv_.get(), in, out, stream);
     } else {
@@ -694,7 +757,7 @@ bool Solver::krylov_fused(double rel, int max_it, int* iters, int* status, const
 // fr_) holds the right-hand side on entry; the solution is left in the Krylov x vector.
 int Solver::krylov_run(bool fp32, double rel, int max_it, int* iters) {
   if (krylov_gmres_) return fp32 ? gmres_t<float>(rel, max_it, iters) : gmres_t<double>(rel, max_it, iters);
-  if (fused_ && !krylov_cg_ && !use_amg_) {
+  if (fused_ && !krylov_cg_ && !pc_) {
     int st = DC_OK;
     if (fp32 ? krylov_fused<float>(rel, max_it, iters, &st) : krylov_fused<double>(rel, max_it, iters, &st))
       return st;
@@ -702,16 +765,16 @@ int Solver::krylov_run(bool fp32, double rel, int max_it, int* iters) {
   double* sc = scal_.get();
   const int64_t n = n_;
   const Bsr A = model.bsr(J_.get(), J32_.get());
-  const Amg* amg = use_amg_ ? &amg_ : nullptr;
+  const Preconditioner* pc = pc_;
   if (fp32) {
     KrylovVectors<float> kv{fx_.get(), fr_.get(), frhat_.get(), fp_.get(), fv_.get(), fs_.get(), ft_.get(),
                             fphat_.get(), fshat_.get()};
-    if (krylov_cg_) cg_init<float, float>(A, fdinv_.get(), kv, rel, rs_, sc, stream, amg);
+    if (krylov_cg_) cg_init<float, float>(A, fdinv_.get(), kv, rel, rs_, sc, stream, pc);
     else krylov_init<float>(kv, n, rel, rs_, sc, stream);
   } else {
     KrylovVectors<double> kv{kx_.get(), kr_.get(), krhat_.get(), kp_.get(), kv_.get(), ks_.get(), kt_.get(),
                              kphat_.get(), kshat_.get()};
-    if (krylov_cg_) cg_init<double, double>(A, dinv_.get(), kv, rel, rs_, sc, stream, amg);
+    if (krylov_cg_) cg_init<double, double>(A, dinv_.get(), kv, rel, rs_, sc, stream, pc);
     else krylov_init<double>(kv, n, rel, rs_, sc, stream);
   }
   cudaGraphExec_t exec = krylov_graph(fp32);
@@ -756,7 +819,7 @@ int Solver::bicgstab(const double* b, double* z, double rel_tol, int max_it, int
 //   r = b - J z (fp64);  solve J d = r in fp32 to a modest reduction;  z += d
 int Solver::bicgstab_mixed(const double* b, double* z, double rel_tol, int max_it, int* iters) {
   // BiCGSTAB + block Jacobi: the whole refinement loop below in one cooperative launch
-  if (fused_ && !krylov_cg_ && !krylov_gmres_ && !use_amg_) {
+  if (fused_ && !krylov_cg_ && !krylov_gmres_ && !pc_) {
     int st = DC_OK;
     if (krylov_fused<float>(rel_tol, max_it, iters, &st, b, z)) return st;
   }

@@ -14,10 +14,13 @@
 #pragma once
 
 #include <functional>
+#include <memory>
 #include <string>
 #include <vector>
 
 #include "amg.hpp"
+#include "mcolor.hpp"
+#include "precond.hpp"
 #include "krylov.cuh"
 #include "model.hpp"
 
@@ -205,8 +208,14 @@ class Solver {
   double direct_tol_ = 1e-10;
   int lin_max_it_ = 500;
   std::string precond_ = "Jacobi";
-  bool use_amg_ = false;
-  Amg amg_;
+  // a preconditioner applied by its own launches (null: block Jacobi, fused into the
+  // Krylov kernels); it reads the BSR operator, in fp32 as well with mixed precision
+  const Preconditioner* pc_ = nullptr;
+  std::unique_ptr<Amg> amg_;
+  std::unique_ptr<ColorPrecond> mc_;
+  RichardsonPrecond rich_;
+  DeviceBuffer<int32_t> row_group_;  // compartment of every block row (multigrid)
+  void configure_preconditioner(const Ini& ls);
   // fp32 SpMV layout: kSpmvAuto times both on the first fp32 operator and keeps the faster
   int spmv_request_ = kSpmvAuto;
   void tune_spmv();

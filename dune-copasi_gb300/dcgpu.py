@@ -36,7 +36,7 @@ EXPORTED = [
     "dc_server_take_state", "dc_server_estimate", "dc_server_destroy", "dc_last_error",
     "dc_spmv_format", "dc_vertex_coords", "dc_constraints", "dc_reduce", "dc_write_vtk", "dc_config_get",
     "dc_selftest_barrier_timeout", "dc_step_stage_newton", "dc_selftest_fma_peaks", "dc_jit_selftest",
-    "dc_model_jit_status",
+    "dc_model_jit_status", "dc_selftest_color", "dc_selftest_aggregate", "dc_selftest_precond",
 ]
 
 
@@ -101,6 +101,12 @@ def load_library(path=LIB_PATH):
     lib.dc_step_stage_newton.argtypes = [vp, P(ctypes.c_int32), sz, P(sz)]
     lib.dc_selftest_fma_peaks.argtypes = [pd, pd]
     lib.dc_jit_selftest.argtypes = [ctypes.c_char_p, sz]
+    pi32 = ctypes.POINTER(ctypes.c_int32)
+    lib.dc_selftest_color.argtypes = [ctypes.c_int64, pi32, pi32, pi32, pi32]
+    lib.dc_selftest_aggregate.argtypes = [ctypes.c_int64, pi32, pi32, pi32, ctypes.c_int32, pi32,
+                                          ctypes.POINTER(ctypes.c_int64)]
+    lib.dc_selftest_precond.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int64, ctypes.c_int32, pi32, pi32,
+                                        pd, pi32, pd, pd, ctypes.c_int32, pd]
     lib.dc_model_jit_status.argtypes = [vp, ctypes.c_char_p, sz]
     lib.dc_model_info_get.argtypes = [vp, P(ModelInfo)]
     lib.dc_species_name.argtypes = [vp, i32, ctypes.c_char_p, sz]
@@ -521,6 +527,66 @@ def fma_peaks():
     f = ctypes.c_double(0.0)
     _check(lib.dc_selftest_fma_peaks(ctypes.byref(d), ctypes.byref(f)))
     return d.value, f.value
+
+
+def _i32(a):
+    a = np.ascontiguousarray(a, dtype=np.int32)
+    return a, a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+
+
+def _f64(a):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a, a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def color_graph(rowptr, colidx):
+    """(colour per row, number of colours) of the multicolour preconditioners' colouring."""
+    lib = load_library()
+    n = len(rowptr) - 1
+    rp, prp = _i32(rowptr)
+    ci, pci = _i32(colidx)
+    out = np.zeros(n, np.int32)
+    nc = ctypes.c_int32(0)
+    _check(lib.dc_selftest_color(n, prp, pci, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), ctypes.byref(nc)))
+    return out, nc.value
+
+
+def aggregate_graph(rowptr, colidx, group=None, distance=2):
+    """(aggregate per row, number of aggregates) of one multigrid coarsening."""
+    lib = load_library()
+    n = len(rowptr) - 1
+    rp, prp = _i32(rowptr)
+    ci, pci = _i32(colidx)
+    if group is not None:
+        g, pg = _i32(group)
+    else:
+        pg = None
+    out = np.zeros(n, np.int32)
+    na = ctypes.c_int64(0)
+    _check(lib.dc_selftest_aggregate(n, prp, pci, pg, int(distance), out.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                     ctypes.byref(na)))
+    return out, int(na.value)
+
+
+def precond_apply(kind, rowptr, colidx, vals, r, bs, params="", group=None, fp32=False):
+    """z = M^-1 r for preconditioner `kind` built on the BSR matrix (vals: nnzb x bs x bs);
+    returns (z, info) with info as dc_selftest_precond describes."""
+    lib = load_library()
+    n = len(rowptr) - 1
+    rp, prp = _i32(rowptr)
+    ci, pci = _i32(colidx)
+    v, pv = _f64(np.asarray(vals).reshape(-1))
+    rr, pr = _f64(r)
+    if group is not None:
+        g, pg = _i32(group)
+    else:
+        pg = None
+    z = np.zeros(n * bs)
+    info = np.zeros(8)
+    _check(lib.dc_selftest_precond(kind.encode(), params.encode(), n, int(bs), prp, pci, pv, pg, pr,
+                                   z.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), 1 if fp32 else 0,
+                                   info.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+    return z, info
 
 
 def selftest_barrier_timeout():

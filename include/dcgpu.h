@@ -186,6 +186,29 @@ int dc_model_jit_status(const dc_model* model, char* buf, size_t len);
  * for the roofline of the FP64-bound assembly): FP64 and FP32 fused multiply-add rates in
  * TFLOP/s (2 flops per FMA), measured with independent FMA chains on every SM (~20 ms). */
 int dc_selftest_fma_peaks(double* fp64_tflops, double* fp32_tflops);
+/* Preconditioner building blocks on a caller-given block matrix (no reference counterpart;
+ * test instrumentation of the preconditioners that replace dune-istl's SeqSSOR / SeqSOR /
+ * SeqILU / SeqDILU, dune/copasi/solver/istl/factory/preconditioner.hh:94-112, and of the
+ * engine's multigrid).  Graphs are CSR on the host (nrows rows, rowptr[nrows] entries,
+ * self-loops allowed).
+ * dc_selftest_color: the colouring the multicolour preconditioners use (colour_out[nrows],
+ * *ncolours).  dc_selftest_aggregate: the multigrid's aggregation of one level (rows of
+ * different group, NULL: one group, never share an aggregate; distance 1 or 2) into
+ * agg_out[nrows], *naggregates.  dc_selftest_precond: builds preconditioner `kind` ("SSOR",
+ * "SOR", "ILU", "DILU" or "AMG") for the BSR matrix (block size bs, row-major blocks in
+ * vals, every row holding its diagonal block), with `params` "key=value;..." (relaxation,
+ * iterations; AMG: smoother 0 Jacobi / 1 L1-Jacobi / 2 Gauss-Seidel, relaxation,
+ * coarse_sweeps, max_level, coarsen_target, aggregation_distance), applies it once to r
+ * (in fp64, or in fp32 when fp32 != 0) and writes z (nrows * bs).  info (8 doubles, may be
+ * NULL): colours, or for AMG the levels, the dense coarse solve's unknowns (0: none) and
+ * the rows of levels 0 to 5. */
+int dc_selftest_color(int64_t nrows, const int32_t* rowptr, const int32_t* colidx, int32_t* colour_out,
+                      int32_t* ncolours);
+int dc_selftest_aggregate(int64_t nrows, const int32_t* rowptr, const int32_t* colidx, const int32_t* group,
+                          int32_t distance, int32_t* agg_out, int64_t* naggregates);
+int dc_selftest_precond(const char* kind, const char* params, int64_t nrows, int32_t bs, const int32_t* rowptr,
+                        const int32_t* colidx, const double* vals, const int32_t* group, const double* r, double* z,
+                        int32_t fp32, double* info);
 int dc_profile_enable(dc_model* model, int enabled);
 int dc_profile_get(const dc_model* model, double* ms, int64_t* calls, int32_t n_categories);
 

@@ -17,7 +17,9 @@ device step times, for the mixed-precision path (fp32 Krylov in fp64 refinement)
 relative L2 deviation of the mixed state from it.  e2e = the same metric through the public
 C ABI with host buffers: state upload from pinned host memory, step, state download,
 host-timed.  "secondary" holds the Gray-Scott 512^2 and two-compartment 1024^2
-configurations, "serving" a Poisson stream of random requests through the request server.
+configurations, "preconditioners" block Jacobi, the multigrid, multicolour SSOR / ILU(0) and
+the engine's adaptive default side by side on heat 128^2 and two compartments 1024^2, and
+"serving" a Poisson stream of random requests through the request server.
 
 --impl reference times the CPU restatement of the reference algorithm (C++, std::thread
 colour-parallel assembly, BiCGSTAB + block Jacobi, or + SSOR as the reference's iterative
@@ -71,8 +73,12 @@ def parse():
                     help="skip the plain FP64 comparison run of the mixed path")
     ap.add_argument("--spmv", default="auto", choices=["auto", "bsr", "sell"],
                     help="layout of the fp32 Krylov operator (linear_solver.spmv)")
-    ap.add_argument("--precond", default="Jacobi", choices=["Jacobi", "AMG"],
-                    help="BiCGSTAB preconditioner (linear_solver.preconditioner.type)")
+    ap.add_argument("--precond", default="auto", choices=["auto", "Jacobi", "AMG", "SSOR", "ILU", "DILU"],
+                    help="BiCGSTAB preconditioner (linear_solver.preconditioner.type; auto, the engine's "
+                         "default: block Jacobi, the multigrid once a solve needs more than 100 iterations)")
+    ap.add_argument("--no-precond-comparison", action="store_true",
+                    help="skip the block-Jacobi / multigrid / SSOR comparison on heat 128^2 and two "
+                         "compartments 1024^2")
     ap.add_argument("--single-launch", default="on", choices=["on", "off"],
                     help="BiCGSTAB as one cooperative launch per solve (on) or one launch per "
                          "phase from a CUDA graph (off) (linear_solver.single_launch)")
@@ -464,6 +470,40 @@ def secondary(dcgpu, kind, steps, warmup, flush):
     return out
 
 
+def precond_comparison(dcgpu, kind, precs, steps, warmup, flush, precision="mixed"):
+    """Per preconditioner on one configuration: device ms per step, Newton and Krylov
+    iterations, ms per Newton iteration (per linear solve for a linear model), and the
+    preconditioner's structure; steps after warm-up steps, L2 flushed before each."""
+    import torch
+    ini, init, dt0, _nl, desc = make_workload(kind, 0)
+    out = {"config": desc, "steps": steps, "warmup": warmup, "precision": precision}
+    for pc in precs:
+        m = dcgpu.Model(ini, {"model.time_step_operator.linear_solver.preconditioner.type": pc})
+        if precision == "mixed":
+            m.set_mixed_precision(True)
+        m.set_state(m.seeded_state(init), 0.0)
+        d = dt0
+        for _ in range(warmup):
+            d = m.step(d)["dt_next"]
+        s0 = m.stats()
+        tot, newton = 0.0, 0
+        for _ in range(steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            inf = m.step(d)
+            d = inf["dt_next"]
+            tot += inf["device_ms"]
+            newton += inf["newton_iterations"]
+        s1 = m.stats()
+        lin = s1["linear_iterations"] - s0["linear_iterations"]
+        solves = max(newton, 1)
+        out[pc] = {"ms_per_step": tot / steps, "newton_iterations": newton, "krylov_iterations": lin,
+                   "krylov_iterations_per_solve": lin / solves, "ms_per_newton_iteration": tot / solves,
+                   "preconditioner": m.precond_info()}
+        m.close()
+    return out
+
+
 def main():
     args = parse()
     rank, world = dist_setup(args)
@@ -635,6 +675,12 @@ def main():
     if not args.no_secondary and args.workload == "cross_diffusion_3d":
         sec = {"gray_scott_512": secondary(dcgpu, "gray_scott", 10, 3, flush),
                "two_compartment_1024": secondary(dcgpu, "two_compartment", 3, 2, flush)}
+    pcmp = None
+    if not args.no_precond_comparison and args.workload == "cross_diffusion_3d":
+        pcmp = {"heat_128": precond_comparison(dcgpu, "heat", ["Jacobi", "AMG", "SSOR", "auto"], 5, 2, flush,
+                                               "fp64"),
+                "two_compartment_1024": precond_comparison(dcgpu, "two_compartment",
+                                                           ["Jacobi", "AMG", "SSOR", "ILU", "auto"], 2, 1, flush)}
     serving = None
     if args.serve_requests > 0:
         served = run_serving(dcgpu, args.serve_requests, 50.0, args.serve_active, args.precision)
@@ -651,8 +697,8 @@ def main():
             "data": "synthetic (seeded initial state, no dataset)",
             "config": config,
             "run": {"precision": args.precision,
-                    "linear_solver": "BiCGSTAB+%s to 1e-10 (direct-solve semantics)"
-                                     % ("block-Jacobi" if args.precond == "Jacobi" else "aggregation-AMG"),
+                    "linear_solver": "BiCGSTAB to 1e-10 (direct-solve semantics)",
+                    "preconditioner": model.precond_info(),
                     "l2_flush": "inputs larger than L2, and a 256 MiB write between timed steps",
                     "newton_iterations": newton, "krylov_iterations": linear,
                     "spmv_layout": model.spmv_format()["format"],
@@ -662,7 +708,7 @@ def main():
             "plain_fp64": plain,
             "speedup_vs_plain_fp64": (value / plain["value"]) if plain else None,
             "e2e": e2e, "roofline": roof, "peaks": peaks, "cpu_baseline": cpu, "clocks": clk,
-            "gpu_launches": launches, "secondary": sec, "serving": serving}
+            "gpu_launches": launches, "secondary": sec, "preconditioners": pcmp, "serving": serving}
     if rank == 0:
         print(json.dumps(line), flush=True)
     model.close()

@@ -6,6 +6,7 @@
 #include <type_traits>
 
 #include "blockops.cuh"
+#include "sellrow.cuh"
 
 namespace dcgpu {
 
@@ -17,6 +18,8 @@ inline int blocks_for(int64_t n) {
   int64_t b = (n + kT - 1) / kT;
   return static_cast<int>(b < 1 ? 1 : (b > 152 * 64 ? 152 * 64 : b));
 }
+// blocks of kT threads for a warp per slice
+inline int blocks_for_slices(int64_t nslices) { return blocks_for(nslices * 32); }
 
 __device__ __forceinline__ bool skip(const double* sc, int slot) { return sc && sc[slot] != 0.0; }
 
@@ -89,142 +92,189 @@ __global__ void k_smooth_first(int64_t nrows, const T* __restrict__ sinv, const 
   }
 }
 
-// x += omega S (r - A x)
+// x_out = x_in + omega S (r - A x_in)   (SELL-32, lane per row)
 template <int B, class T>
-__global__ void k_smooth_more(int64_t nrows, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ colidx,
-                              const T* __restrict__ val, const T* __restrict__ sinv, const T* __restrict__ r,
+__global__ void k_smooth_more(Sell S, const T* __restrict__ val, const T* __restrict__ sinv, const T* __restrict__ r,
                               const T* __restrict__ xin, T* __restrict__ xout, T omega, const double* sc, int slot) {
   if (skip(sc, slot)) return;
-  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < nrows; i += stride) {
+  const SliceLoop L;
+  for (int64_t sl = L.first; sl < S.nslices; sl += L.stride) {
+    const int64_t i = sl * 32 + L.lane;
+    if (i >= S.nrows) continue;
+    T acc[B];
+#pragma unroll
+    for (int s = 0; s < B; ++s) acc[s] = T(0);
+    sell_row_apply<B, T>(S, sl, L.lane, val, [](int32_t) { return true; },
+                         [&](int32_t c, T (&xv)[B]) {
+#pragma unroll
+                           for (int q = 0; q < B; ++q) xv[q] = xin[static_cast<int64_t>(c) * B + q];
+                         },
+                         acc);
     T t[B];
 #pragma unroll
-    for (int s = 0; s < B; ++s) t[s] = r[i * B + s];
-    for (int32_t e = rowptr[i]; e < rowptr[i + 1]; ++e) {
-      const T* blk = val + static_cast<int64_t>(e) * B * B;
-      const T* xj = xin + static_cast<int64_t>(colidx[e]) * B;
-      T v[B];
+    for (int s = 0; s < B; ++s) t[s] = r[i * B + s] - acc[s];
+    const T* d = sinv + i * B * B;
 #pragma unroll
-      for (int q = 0; q < B; ++q) v[q] = xj[q];
+    for (int s = 0; s < B; ++s) {
+      T a = T(0);
 #pragma unroll
-      for (int s = 0; s < B; ++s) {
-        T acc = T(0);
+      for (int q = 0; q < B; ++q) a += d[s * B + q] * t[q];
+      xout[i * B + s] = xin[i * B + s] + omega * a;
+    }
+  }
+}
+
+// u = r - A x   (SELL-32, lane per row)
+template <int B, class T>
+__global__ void k_residual(Sell S, const T* __restrict__ val, const T* __restrict__ x, const T* __restrict__ r,
+                           T* __restrict__ u, const double* sc, int slot) {
+  if (skip(sc, slot)) return;
+  const SliceLoop L;
+  for (int64_t sl = L.first; sl < S.nslices; sl += L.stride) {
+    const int64_t i = sl * 32 + L.lane;
+    if (i >= S.nrows) continue;
+    T acc[B];
 #pragma unroll
-        for (int q = 0; q < B; ++q) acc += blk[s * B + q] * v[q];
-        t[s] -= acc;
+    for (int s = 0; s < B; ++s) acc[s] = T(0);
+    sell_row_apply<B, T>(S, sl, L.lane, val, [](int32_t) { return true; },
+                         [&](int32_t c, T (&xv)[B]) {
+#pragma unroll
+                           for (int q = 0; q < B; ++q) xv[q] = x[static_cast<int64_t>(c) * B + q];
+                         },
+                         acc);
+#pragma unroll
+    for (int s = 0; s < B; ++s) u[i * B + s] = r[i * B + s] - acc[s];
+  }
+}
+
+// x = y + omega S (r - A y) with y = t + P xc, formed on the fly (coarse correction and
+// post-smoothing in one pass over A; SELL-32, lane per row)
+template <int B, class T>
+__global__ void k_prolong_smooth(Sell S, const T* __restrict__ val, const T* __restrict__ sinv,
+                                 const int32_t* __restrict__ agg, const T* __restrict__ xc, const T* __restrict__ t,
+                                 const T* __restrict__ r, T* __restrict__ x, T omega, T cs, const double* sc,
+                                 int slot) {
+  if (skip(sc, slot)) return;
+  const SliceLoop L;
+  for (int64_t sl = L.first; sl < S.nslices; sl += L.stride) {
+    const int64_t i = sl * 32 + L.lane;
+    if (i >= S.nrows) continue;
+    T acc[B];
+#pragma unroll
+    for (int s = 0; s < B; ++s) acc[s] = T(0);
+    sell_row_apply<B, T>(S, sl, L.lane, val, [](int32_t) { return true; },
+                         [&](int32_t c, T (&xv)[B]) {
+                           const T* tj = t + static_cast<int64_t>(c) * B;
+                           const T* cj = xc + static_cast<int64_t>(agg[c]) * B;
+#pragma unroll
+                           for (int q = 0; q < B; ++q) xv[q] = tj[q] + cs * cj[q];
+                         },
+                         acc);
+    const T* ci = xc + static_cast<int64_t>(agg[i]) * B;
+    T res[B];
+#pragma unroll
+    for (int s = 0; s < B; ++s) res[s] = r[i * B + s] - acc[s];
+    const T* d = sinv + i * B * B;
+#pragma unroll
+    for (int s = 0; s < B; ++s) {
+      T a = T(0);
+#pragma unroll
+      for (int q = 0; q < B; ++q) a += d[s * B + q] * res[q];
+      x[i * B + s] = t[i * B + s] + cs * ci[s] + omega * a;
+    }
+  }
+}
+
+// Warp per row on the BSR values (small levels): lanes take the row's blocks in turn, the
+// partial products are summed over the warp (fixed butterfly order), and lane 0 finishes
+// the row.  MODE 0: out = r - A x.  MODE 1: out = y + omega S (r - A y) with y = x + cs P xc
+// (x: the pre-smoothed iterate).  MODE 2: out = x + omega S (r - A x).
+template <int B, class T, int MODE>
+__global__ void k_rows_warp(int64_t nrows, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ colidx,
+                            const T* __restrict__ val, const T* __restrict__ sinv, const int32_t* __restrict__ agg,
+                            const T* __restrict__ xc, const T* __restrict__ x, const T* __restrict__ r,
+                            T* __restrict__ out, T omega, T cs, const double* sc, int slot) {
+  if (skip(sc, slot)) return;
+  const SliceLoop L;  // here: one row per warp
+  for (int64_t i = L.first; i < nrows; i += L.stride) {
+    T acc[B];
+#pragma unroll
+    for (int s = 0; s < B; ++s) acc[s] = T(0);
+    for (int32_t e = rowptr[i] + L.lane; e < rowptr[i + 1]; e += 32) {
+      const int32_t c = colidx[e];
+      T xv[B];
+#pragma unroll
+      for (int q = 0; q < B; ++q) {
+        xv[q] = x[static_cast<int64_t>(c) * B + q];
+        if (MODE == 1) xv[q] += cs * xc[static_cast<int64_t>(agg[c]) * B + q];
       }
+      const T* blk = val + static_cast<int64_t>(e) * B * B;
+#pragma unroll
+      for (int s = 0; s < B; ++s)
+#pragma unroll
+        for (int q = 0; q < B; ++q) acc[s] += blk[s * B + q] * xv[q];
+    }
+#pragma unroll
+    for (int s = 0; s < B; ++s)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc[s] += __shfl_xor_sync(0xffffffffu, acc[s], o);
+    if (L.lane != 0) continue;
+    T res[B];
+#pragma unroll
+    for (int s = 0; s < B; ++s) res[s] = r[i * B + s] - acc[s];
+    if (MODE == 0) {
+#pragma unroll
+      for (int s = 0; s < B; ++s) out[i * B + s] = res[s];
+      continue;
     }
     const T* d = sinv + i * B * B;
 #pragma unroll
     for (int s = 0; s < B; ++s) {
-      T acc = T(0);
+      T a = T(0);
 #pragma unroll
-      for (int q = 0; q < B; ++q) acc += d[s * B + q] * t[q];
-      xout[i * B + s] = xin[i * B + s] + omega * acc;
+      for (int q = 0; q < B; ++q) a += d[s * B + q] * res[q];
+      T y = x[i * B + s];
+      if (MODE == 1) y += cs * xc[static_cast<int64_t>(agg[i]) * B + s];
+      out[i * B + s] = y + omega * a;
     }
   }
 }
 
-// u = r - A x   (thread per block row)
+// rc[I] = sum of u over the rows of aggregate I: warp per aggregate, fixed butterfly order
 template <int B, class T>
-__global__ void k_residual(int64_t nrows, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ colidx,
-                           const T* __restrict__ val, const T* __restrict__ x, const T* __restrict__ r,
-                           T* __restrict__ u, const double* sc, int slot) {
+__global__ void k_restrict_warp(int64_t ncoarse, const int32_t* __restrict__ agg_ptr,
+                                const int32_t* __restrict__ agg_rows, const T* __restrict__ u, T* __restrict__ rc,
+                                const double* sc, int slot) {
   if (skip(sc, slot)) return;
-  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < nrows; i += stride) {
-    T t[B];
-#pragma unroll
-    for (int s = 0; s < B; ++s) t[s] = r[i * B + s];
-    for (int32_t e = rowptr[i]; e < rowptr[i + 1]; ++e) {
-      const T* blk = val + static_cast<int64_t>(e) * B * B;
-      const T* xj = x + static_cast<int64_t>(colidx[e]) * B;
-      T v[B];
-#pragma unroll
-      for (int q = 0; q < B; ++q) v[q] = xj[q];
-#pragma unroll
-      for (int s = 0; s < B; ++s) {
-        T acc = T(0);
-#pragma unroll
-        for (int q = 0; q < B; ++q) acc += blk[s * B + q] * v[q];
-        t[s] -= acc;
-      }
-    }
-#pragma unroll
-    for (int s = 0; s < B; ++s) u[i * B + s] = t[s];
-  }
-}
-
-// rc[I] = sum of u over the rows of aggregate I (ascending row order)
-template <int B, class T>
-__global__ void k_restrict(int64_t ncoarse, const int32_t* __restrict__ agg_ptr, const int32_t* __restrict__ agg_rows,
-                           const T* __restrict__ u, T* __restrict__ rc, const double* sc, int slot) {
-  if (skip(sc, slot)) return;
-  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-  for (int64_t I = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; I < ncoarse; I += stride) {
+  const SliceLoop L;
+  for (int64_t I = L.first; I < ncoarse; I += L.stride) {
     T acc[B];
 #pragma unroll
     for (int s = 0; s < B; ++s) acc[s] = T(0);
-    for (int32_t q = agg_ptr[I]; q < agg_ptr[I + 1]; ++q) {
+    for (int32_t q = agg_ptr[I] + L.lane; q < agg_ptr[I + 1]; q += 32) {
       const T* ui = u + static_cast<int64_t>(agg_rows[q]) * B;
 #pragma unroll
       for (int s = 0; s < B; ++s) acc[s] += ui[s];
     }
 #pragma unroll
-    for (int s = 0; s < B; ++s) rc[I * B + s] = acc[s];
+    for (int s = 0; s < B; ++s)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc[s] += __shfl_xor_sync(0xffffffffu, acc[s], o);
+    if (L.lane == 0)
+#pragma unroll
+      for (int s = 0; s < B; ++s) rc[I * B + s] = acc[s];
   }
 }
 
-// x = y + omega S (r - A y) with y = t + P xc, formed on the fly (coarse correction and
-// post-smoothing in one pass over A)
-template <int B, class T>
-__global__ void k_prolong_smooth(int64_t nrows, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ colidx,
-                                 const T* __restrict__ val, const T* __restrict__ sinv, const int32_t* __restrict__ agg,
-                                 const T* __restrict__ xc, const T* __restrict__ t, const T* __restrict__ r,
-                                 T* __restrict__ x, T omega, const double* sc, int slot) {
-  if (skip(sc, slot)) return;
-  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < nrows; i += stride) {
-    T res[B];
-#pragma unroll
-    for (int s = 0; s < B; ++s) res[s] = r[i * B + s];
-    for (int32_t e = rowptr[i]; e < rowptr[i + 1]; ++e) {
-      const int32_t j = colidx[e];
-      const T* blk = val + static_cast<int64_t>(e) * B * B;
-      const T* tj = t + static_cast<int64_t>(j) * B;
-      const T* cj = xc + static_cast<int64_t>(agg[j]) * B;
-      T v[B];
-#pragma unroll
-      for (int q = 0; q < B; ++q) v[q] = tj[q] + cj[q];
-#pragma unroll
-      for (int s = 0; s < B; ++s) {
-        T acc = T(0);
-#pragma unroll
-        for (int q = 0; q < B; ++q) acc += blk[s * B + q] * v[q];
-        res[s] -= acc;
-      }
-    }
-    const T* d = sinv + i * B * B;
-    const T* ci = xc + static_cast<int64_t>(agg[i]) * B;
-#pragma unroll
-    for (int s = 0; s < B; ++s) {
-      T acc = T(0);
-#pragma unroll
-      for (int q = 0; q < B; ++q) acc += d[s * B + q] * res[q];
-      x[i * B + s] = t[i * B + s] + ci[s] + omega * acc;
-    }
-  }
-}
-
-// x += P xc
+// x += cs P xc
 template <int B, class T>
 __global__ void k_prolong(int64_t nrows, const int32_t* __restrict__ agg, const T* __restrict__ xc, T* __restrict__ x,
-                          const double* sc, int slot) {
+                          T cs, const double* sc, int slot) {
   if (skip(sc, slot)) return;
   const int64_t n = nrows * B;
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
   for (int64_t row = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; row < n; row += stride)
-    x[row] += xc[static_cast<int64_t>(agg[row / B]) * B + row % B];
+    x[row] += cs * xc[static_cast<int64_t>(agg[row / B]) * B + row % B];
 }
 
 // ---------------------------------------------------------------- dense coarsest solve
@@ -426,6 +476,8 @@ void Amg::build(int64_t nrows, int bs, int64_t nnzb, const int32_t* rowptr, cons
     L.t.resize(nv);
     L.rc.resize(nv);
     const bool smoothed = !(l + 1 == levels_.size() && dense_n_ > 0);
+    L.warp_rows = smoothed && L.nrows < warp_rows_below;
+    if (smoothed && !L.warp_rows) sell_structure(L.nrows, L.rowptr, L.colidx, &L.sell, s);
     if (smoothed && smoother == Smoother::L1Jacobi) L.sinv_o.resize(static_cast<size_t>(L.nrows) * b2);
     if (smoothed && smoother == Smoother::GaussSeidel) {
       L.gs = std::make_unique<ColorPrecond>();
@@ -434,6 +486,20 @@ void Amg::build(int64_t nrows, int bs, int64_t nnzb, const int32_t* rowptr, cons
     }
   }
   cuda_check(cudaStreamSynchronize(s), "multigrid set-up");
+}
+
+std::string Amg::describe() const {
+  static const char* names[] = {"jacobi", "l1jacobi", "gauss_seidel"};
+  std::string o = "{\"type\": \"AMG\", \"smoother\": \"" + std::string(names[static_cast<int>(smoother)]) +
+                  "\", \"aggregation_distance\": " + std::to_string(mis_distance) + ", \"levels\": [";
+  for (size_t l = 0; l < levels_.size(); ++l) {
+    const Level& L = levels_[l];
+    const bool dense = l + 1 == levels_.size() && dense_n_ > 0;
+    o += (l ? ", " : "") + std::string("{\"rows\": ") + std::to_string(L.nrows) + ", \"blocks\": " +
+         std::to_string(L.nnzb) + ", \"kernels\": \"" + (dense ? "dense" : L.warp_rows ? "warp_per_row" : "sell32") +
+         "\"}";
+  }
+  return o + "]}";
 }
 
 std::vector<double> Amg::values_host(int l) const {
@@ -457,12 +523,11 @@ std::vector<int32_t> Amg::colidx_host(int l) const {
   return h;
 }
 
-void Amg::setup(const double* fine_vals, const double* fine_dinv, const float* fine_vals32, const float* fine_dinv32,
-                bool fp32, int* status, cudaStream_t s) {
+void Amg::setup(const double* fine_vals, const double* fine_dinv, const float* fine_dinv32, bool fp32, int* status,
+                cudaStream_t s) {
   if (levels_.empty()) return;
   levels_[0].val = fine_vals;
   levels_[0].dinv = fine_dinv;
-  levels_[0].val32 = fine_vals32;
   levels_[0].dinv32 = fine_dinv32;
   const int bs2 = bs_ * bs_;
   for (size_t l = 1; l < levels_.size(); ++l) {
@@ -478,27 +543,35 @@ void Amg::setup(const double* fine_vals, const double* fine_dinv, const float* f
     A.rowptr = c.rowptr;
     A.colidx = c.colidx;
     A.val = c.val_o.get();
-    block_jacobi_setup(A, c.diag, c.dinv_o.get(), status, s);
+    if (fp32 && c.dinv32_o.size() != c.dinv_o.size()) c.dinv32_o.resize(c.dinv_o.size());
+    block_jacobi_setup(A, c.diag, c.dinv_o.get(), status, s, fp32 ? c.dinv32_o.get() : nullptr);
+    c.dinv32 = fp32 ? c.dinv32_o.get() : nullptr;
   }
-  if (fp32) {
-    for (size_t l = 1; l < levels_.size(); ++l) {
-      Level& c = levels_[l];
-      if (c.val32_o.size() != c.val_o.size()) {
-        c.val32_o.resize(c.val_o.size());
-        c.dinv32_o.resize(c.dinv_o.size());
-      }
-      to_float(static_cast<int64_t>(c.val_o.size()), c.val_o.get(), c.val32_o.get(), s);
-      to_float(static_cast<int64_t>(c.dinv_o.size()), c.dinv_o.get(), c.dinv32_o.get(), s);
-      c.val32 = c.val32_o.get();
-      c.dinv32 = c.dinv32_o.get();
+  // SELL-32 copies of the values in the precision the cycle runs in
+  for (auto& L : levels_) {
+    if (L.warp_rows && fp32) {
+      const size_t nb = static_cast<size_t>(L.nnzb) * bs2;
+      if (L.val32_o.size() != nb) L.val32_o.resize(nb);
+      to_float(static_cast<int64_t>(nb), L.val, L.val32_o.get(), s);
     }
+    if (L.sell.nslices == 0) continue;
+    const size_t nv = static_cast<size_t>(L.sell.nslots) * 32 * bs2;
+    if (fp32) {
+      if (L.sv32.size() != nv) L.sv32.resize(nv);
+      sell_values(L.sell, bs_, L.val, L.sv32.get(), s);
+    } else {
+      if (L.sv64.size() != nv) L.sv64.resize(nv);
+      sell_values(L.sell, bs_, L.val, L.sv64.get(), s);
+    }
+  }
+  if (fp32)
     for (auto& L : levels_)
       if (L.x32.size() != L.x.size()) {
         L.x32.resize(L.x.size());
         L.t32.resize(L.t.size());
         L.rc32.resize(L.rc.size());
       }
-  }
+  fp32_ = fp32;
   // smoothers
   for (size_t l = 0; l < levels_.size(); ++l) {
     Level& L = levels_[l];
@@ -513,7 +586,7 @@ void Amg::setup(const double* fine_vals, const double* fine_dinv, const float* f
       switch (bs_) { DC_L1(1) DC_L1(2) DC_L1(3) DC_L1(4) DC_L1(5) DC_L1(6) DC_L1(7) DC_L1(8) }
 #undef DC_L1
     }
-    if (L.gs) L.gs->setup(L.val, L.dinv, L.val32, L.dinv32, fp32, status, s);
+    if (L.gs) L.gs->setup(L.val, L.dinv, L.dinv32, fp32, status, s);
   }
   // dense coarsest solve
   if (dense_n_ > 0) {
@@ -536,9 +609,12 @@ template <class T>
 void Amg::cycle(int l, const T* r, T* x, const double* sc, int slot, cudaStream_t s) const {
   const Level& a = levels_[l];
   const int64_t n = a.nrows;
-  const T* A = pickc<T>(a.val, a.val32);
+  const T* A = a.warp_rows ? pickc<T>(a.val, a.val32_o.get()) : pick<T>(a.sv64, a.sv32);
   const T* D = pickc<T>(a.dinv, a.dinv32);
+  const Sell SA = a.sell.view(bs_);
+  const int gw = blocks_for(n * 32);  // warp per row
   const T w = static_cast<T>(omega);
+  const T cs = static_cast<T>(correction);
   T* t = pick<T>(a.t, a.t32);
   const bool last = l + 1 == static_cast<int>(levels_.size());
 #define DC_BS(KERNEL_CALL)                                                                                    \
@@ -552,6 +628,14 @@ void Amg::cycle(int l, const T* r, T* x, const double* sc, int slot, cudaStream_
     case 7: { constexpr int B = 7; KERNEL_CALL; } break;                                                      \
     default: { constexpr int B = 8; KERNEL_CALL; } break;                                                     \
   }
+  // u = r - A v
+  auto residual = [&](const T* v, T* u) {
+    if (a.warp_rows)
+      DC_BS((k_rows_warp<B, T, 0><<<gw, kT, 0, s>>>(n, a.rowptr, a.colidx, A, nullptr, nullptr, nullptr, v, r, u, w,
+                                                     cs, sc, slot)))
+    else
+      DC_BS((k_residual<B, T><<<blocks_for_slices(SA.nslices), kT, 0, s>>>(SA, A, v, r, u, sc, slot)))
+  };
   if (last) {
     if (dense_n_ > 0) {
       count_launches(1);
@@ -563,7 +647,11 @@ void Amg::cycle(int l, const T* r, T* x, const double* sc, int slot, cudaStream_
     DC_BS((k_smooth_first<B, T><<<blocks_for(n), kT, 0, s>>>(n, D, r, x, w, sc, slot)));
     for (int k = 1; k < coarse_sweeps; ++k) {
       count_launches(2);
-      DC_BS((k_smooth_more<B, T><<<blocks_for(n), kT, 0, s>>>(n, a.rowptr, a.colidx, A, D, r, x, t, w, sc, slot)));
+      if (a.warp_rows)
+        DC_BS((k_rows_warp<B, T, 2><<<gw, kT, 0, s>>>(n, a.rowptr, a.colidx, A, D, nullptr, nullptr, x, r, t, w, cs,
+                                                       sc, slot)))
+      else
+        DC_BS((k_smooth_more<B, T><<<blocks_for_slices(SA.nslices), kT, 0, s>>>(SA, A, D, r, x, t, w, sc, slot)))
       cuda_check(cudaMemcpyAsync(x, t, static_cast<size_t>(n) * bs_ * sizeof(T), cudaMemcpyDeviceToDevice, s),
                  "multigrid");
     }
@@ -576,12 +664,12 @@ void Amg::cycle(int l, const T* r, T* x, const double* sc, int slot, cudaStream_
   if (smoother == Smoother::GaussSeidel) {
     a.gs->template sor_sweep<T>(r, x, true, true, sc, slot, s);
     count_launches(2);
-    DC_BS((k_residual<B, T><<<blocks_for(n), kT, 0, s>>>(n, a.rowptr, a.colidx, A, x, r, u, sc, slot)));
-    DC_BS((k_restrict<B, T><<<blocks_for(c.nrows), kT, 0, s>>>(c.nrows, c.own.agg_ptr.get(), c.own.agg_rows.get(), u,
-                                                               rc, sc, slot)));
+    residual(x, u);
+    DC_BS((k_restrict_warp<B, T><<<blocks_for(c.nrows * 32), kT, 0, s>>>(c.nrows, c.own.agg_ptr.get(),
+                                                                         c.own.agg_rows.get(), u, rc, sc, slot)));
     cycle<T>(l + 1, rc, xc, sc, slot, s);
     count_launches(1);
-    DC_BS((k_prolong<B, T><<<blocks_for(n * bs_), kT, 0, s>>>(n, a.agg.get(), xc, x, sc, slot)));
+    DC_BS((k_prolong<B, T><<<blocks_for(n * bs_), kT, 0, s>>>(n, a.agg.get(), xc, x, cs, sc, slot)));
     a.gs->template sor_sweep<T>(r, x, false, false, sc, slot, s);
     return;
   }
@@ -590,22 +678,25 @@ void Amg::cycle(int l, const T* r, T* x, const double* sc, int slot, cudaStream_
   const T* S = smoother == Smoother::L1Jacobi ? pick<T>(a.sinv_o, a.sinv32_o) : D;
   count_launches(3);
   DC_BS((k_smooth_first<B, T><<<blocks_for(n), kT, 0, s>>>(n, S, r, t, w, sc, slot)));
-  DC_BS((k_residual<B, T><<<blocks_for(n), kT, 0, s>>>(n, a.rowptr, a.colidx, A, t, r, x, sc, slot)));
-  DC_BS((k_restrict<B, T><<<blocks_for(c.nrows), kT, 0, s>>>(c.nrows, c.own.agg_ptr.get(), c.own.agg_rows.get(), x,
-                                                             rc, sc, slot)));
+  residual(t, x);
+  DC_BS((k_restrict_warp<B, T><<<blocks_for(c.nrows * 32), kT, 0, s>>>(c.nrows, c.own.agg_ptr.get(),
+                                                                       c.own.agg_rows.get(), x, rc, sc, slot)));
   cycle<T>(l + 1, rc, xc, sc, slot, s);
   count_launches(1);
-  DC_BS((k_prolong_smooth<B, T><<<blocks_for(n), kT, 0, s>>>(n, a.rowptr, a.colidx, A, S, a.agg.get(), xc, t, r, x, w,
-                                                             sc, slot)));
+  if (a.warp_rows)
+    DC_BS((k_rows_warp<B, T, 1><<<gw, kT, 0, s>>>(n, a.rowptr, a.colidx, A, S, a.agg.get(), xc, t, r, x, w, cs, sc,
+                                                   slot)))
+  else
+    DC_BS((k_prolong_smooth<B, T><<<blocks_for_slices(SA.nslices), kT, 0, s>>>(SA, A, S, a.agg.get(), xc, t, r, x, w,
+                                                                                cs, sc, slot)))
 #undef DC_BS
 }
 
 template <class T>
 void Amg::apply_t(const T* r, T* z, const double* sc, int done_slot, cudaStream_t s) const {
   if (levels_.empty()) throw std::runtime_error("multigrid: not built");
-  if constexpr (std::is_same<T, float>::value) {
-    if (levels_[0].val32 == nullptr) throw std::runtime_error("multigrid: fp32 values not set up");
-  }
+  if ((std::is_same<T, float>::value) != fp32_)
+    throw std::runtime_error("multigrid: applied in another precision than it was set up for");
   cycle<T>(0, r, z, sc, done_slot, s);
 }
 

@@ -16,8 +16,9 @@
 // for every coarse block the list of the fine blocks that add into it is precomputed.
 // Values (every Newton iteration, on the device): coarse blocks are summed in a fixed order
 // (deterministic), every level's smoother is set up, and the coarsest operator is factored
-// by a dense FP64 LU with partial pivoting and inverted; fp32 copies of everything are kept
-// for the mixed-precision Krylov path.
+// by a dense FP64 LU with partial pivoting and inverted.  The cycle reads SELL-32 copies of
+// the level operators (sell.cuh) in the precision of the Krylov solve (fp32 in the
+// mixed-precision path).
 // Smoothers: damped block Jacobi, block L1-Jacobi (the diagonal block plus the absolute row
 // sums of the off-diagonal blocks on its diagonal), or multicolour block Gauss-Seidel
 // (forward sweep before the coarse correction, backward sweep after it: a symmetric cycle).
@@ -25,6 +26,7 @@
 
 #include <cstdint>
 #include <memory>
+#include <string>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -42,6 +44,8 @@ class Amg : public Preconditioner {
   enum class Smoother { Jacobi, L1Jacobi, GaussSeidel };
   // largest coarsest level (unknowns) solved by the dense LU
   static constexpr int kDenseMax = 128;
+  // levels with fewer rows use the warp-per-row kernels (default of warp_rows_below)
+  static constexpr int64_t kWarpRowsBelow = 65536;
 
   Amg() = default;
   Amg(const Amg&) = delete;
@@ -52,15 +56,17 @@ class Amg : public Preconditioner {
   void build(int64_t nrows, int bs, int64_t nnzb, const int32_t* rowptr, const int32_t* colidx, const int32_t* diag,
              const int32_t* group, cudaStream_t s);
   // Galerkin values, smoothers and the coarse factorisation from the fine values
-  // (fine_dinv: the fine block-Jacobi inverses already computed by the solver); with fp32,
-  // float copies of every level as well (fine_vals32 / fine_dinv32 already converted)
-  void setup(const double* fine_vals, const double* fine_dinv, const float* fine_vals32, const float* fine_dinv32,
-             bool fp32, int* status, cudaStream_t s);
+  // (fine_dinv: the fine block-Jacobi inverses already computed by the solver).  The cycle
+  // then runs in fp32 (fp32 true; fine_dinv32: the inverses already rounded) or in fp64.
+  void setup(const double* fine_vals, const double* fine_dinv, const float* fine_dinv32, bool fp32, int* status,
+             cudaStream_t s);
   // z = M^-1 r, one V(1,1)-cycle; no work when sc != nullptr and sc[done] != 0
   void apply(const double* r, double* z, const double* sc, int done_slot, cudaStream_t s) const override;
   void apply(const float* r, float* z, const double* sc, int done_slot, cudaStream_t s) const override;
 
   int levels() const { return static_cast<int>(levels_.size()); }
+  // the hierarchy as a JSON object: smoother, rows / blocks / kernel kind per level
+  std::string describe() const;
   int64_t rows(int l) const { return levels_[l].nrows; }
   int64_t blocks(int l) const { return levels_[l].nnzb; }
   bool built() const { return !levels_.empty(); }
@@ -81,6 +87,8 @@ class Amg : public Preconditioner {
   int max_levels = 10;
   int64_t coarsen_target = 0;  // stop coarsening at this many rows (0: the dense solve's limit)
   int mis_distance = 2;      // aggregation around a distance-1 or distance-2 independent set
+  double correction = 1.0;   // scale of the coarse-grid correction x += correction * P xc
+  int64_t warp_rows_below = kWarpRowsBelow;
 
  private:
   struct Level {
@@ -91,13 +99,20 @@ class Amg : public Preconditioner {
     const int32_t* diag = nullptr;
     const int32_t* group = nullptr;
     CoarseStructure own;  // this level's pattern when it is a coarse level
-    // values of this level (level 0: borrowed from the solver)
+    // BSR values of this level and their block-Jacobi inverses (level 0: borrowed from the
+    // solver); the cycle's products read the SELL-32 copy in the precision of the last setup
     DeviceBuffer<double> val_o, dinv_o;
-    DeviceBuffer<float> val32_o, dinv32_o;
+    DeviceBuffer<float> dinv32_o;
     const double* val = nullptr;
     const double* dinv = nullptr;
-    const float* val32 = nullptr;
     const float* dinv32 = nullptr;
+    // products: lane per row on a SELL-32 copy (large levels), or warp per row on the BSR
+    // values (levels below warp_rows_below rows, where a lane per row leaves the GPU idle
+    // and each lane would walk a long coarse row alone)
+    bool warp_rows = false;
+    SellStructure sell;
+    DeviceBuffer<double> sv64;
+    DeviceBuffer<float> sv32, val32_o;
     // smoother inverses (L1-Jacobi: own; else the block-Jacobi inverses above)
     DeviceBuffer<double> sinv_o;
     DeviceBuffer<float> sinv32_o;
@@ -115,6 +130,7 @@ class Amg : public Preconditioner {
 
   std::vector<Level> levels_;
   int bs_ = 1;
+  bool fp32_ = false;  // precision of the last setup
   // dense coarsest solve: n unknowns, the operator's inverse (row-major) in fp64 / fp32
   int dense_n_ = 0;
   DeviceBuffer<double> dense_, dinvd_;

@@ -606,8 +606,10 @@ int dc_selftest_precond(const char* kind, const char* params, int64_t nrows, int
       amg->max_levels = static_cast<int>(param(prm, "max_level", 10));
       amg->coarsen_target = static_cast<int64_t>(param(prm, "coarsen_target", 0));
       amg->mis_distance = static_cast<int>(param(prm, "aggregation_distance", 2));
+      amg->correction = param(prm, "coarse_correction", 1.0);
+      amg->warp_rows_below = static_cast<int64_t>(param(prm, "warp_rows_below", dcgpu::Amg::kWarpRowsBelow));
       amg->build(nrows, bs, nnzb, g.rowptr.get(), g.colidx.get(), ddiag.get(), group ? g.group.get() : nullptr, s);
-      amg->setup(dval.get(), dinv.get(), fval.get(), fdinv.get(), fp32 != 0, status.get(), s);
+      amg->setup(dval.get(), dinv.get(), fdinv.get(), fp32 != 0, status.get(), s);
       inf[0] = amg->levels();
       inf[1] = amg->dense_coarse() ? static_cast<double>(amg->rows(amg->levels() - 1) * bs) : 0.0;
       for (int l = 0; l < amg->levels() && l < 6; ++l) inf[2 + l] = static_cast<double>(amg->rows(l));
@@ -623,7 +625,7 @@ int dc_selftest_precond(const char* kind, const char* params, int64_t nrows, int
       mc->omega = param(prm, "relaxation", 1.0);
       mc->iterations = static_cast<int>(param(prm, "iterations", 1));
       mc->build(kd, nrows, bs, nnzb, g.rowptr.get(), g.colidx.get(), ddiag.get(), s);
-      mc->setup(dval.get(), dinv.get(), fval.get(), fdinv.get(), fp32 != 0, status.get(), s);
+      mc->setup(dval.get(), dinv.get(), fdinv.get(), fp32 != 0, status.get(), s);
       inf[0] = mc->colors();
       pc = std::move(mc);
     }
@@ -642,6 +644,16 @@ int dc_selftest_precond(const char* kind, const char* params, int64_t nrows, int
     }
     std::memcpy(z, out.data(), nv * sizeof(double));
     if (info) std::memcpy(info, inf, sizeof(inf));
+    return DC_OK;
+  });
+}
+
+int dc_precond_info(const dc_model* model, char* buf, size_t len) {
+  return guarded([&] {
+    if (!model || !buf || len == 0) throw std::invalid_argument("null argument");
+    const std::string info = model->solver->precond_info();
+    std::strncpy(buf, info.c_str(), len - 1);
+    buf[len - 1] = '\0';
     return DC_OK;
   });
 }

@@ -367,6 +367,59 @@ __global__ void k_galerkin_lists(int64_t na, const int32_t* __restrict__ ptr, co
   }
 }
 
+// ---------------------------------------------------------------- SELL-32 layout
+__global__ void k_slice_width(int64_t nslices, int64_t nrows, const int32_t* __restrict__ rowptr,
+                              int32_t* __restrict__ width) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t sl = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; sl < nslices; sl += stride) {
+    int32_t w = 0;
+    for (int64_t i = sl * 32; i < sl * 32 + 32 && i < nrows; ++i) w = max(w, rowptr[i + 1] - rowptr[i]);
+    width[sl] = w;
+  }
+}
+
+__global__ void k_widen(int64_t n, const int32_t* __restrict__ in, int64_t* __restrict__ out) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i <= n; i += stride) out[i] = in[i];
+}
+
+// thread per (slice, lane): the lane's slots, padding pointing at the row itself (row 0
+// past the last row)
+__global__ void k_sell_fill(int64_t nslices, int64_t nrows, const int32_t* __restrict__ rowptr,
+                            const int32_t* __restrict__ colidx, const int64_t* __restrict__ off,
+                            int32_t* __restrict__ cols, int32_t* __restrict__ bpos) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < nslices * 32; t += stride) {
+    const int64_t sl = t / 32, i = t;
+    const int lane = static_cast<int>(t % 32);
+    const int32_t len = i < nrows ? rowptr[i + 1] - rowptr[i] : 0;
+    for (int64_t k = 0; k < off[sl + 1] - off[sl]; ++k) {
+      const int64_t p = (off[sl] + k) * 32 + lane;
+      if (k < len) {
+        cols[p] = colidx[rowptr[i] + k];
+        bpos[p] = static_cast<int32_t>(rowptr[i] + k);
+      } else {
+        cols[p] = i < nrows ? static_cast<int32_t>(i) : 0;
+        bpos[p] = -1;
+      }
+    }
+  }
+}
+
+// entry-interleaved values: out[(slot * bs2 + e) * 32 + lane] (sellrow.cuh)
+template <class V>
+__global__ void k_sell_values(int64_t nvals, int bs2, const int32_t* __restrict__ bpos, const double* __restrict__ bsr,
+                              V* __restrict__ out) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < nvals; t += stride) {
+    const int64_t lane = t % 32, q = t / 32;
+    const int64_t slot = q / bs2;
+    const int e = static_cast<int>(q % bs2);
+    const int32_t b = bpos[slot * 32 + lane];
+    out[t] = b >= 0 ? static_cast<V>(bsr[static_cast<int64_t>(b) * bs2 + e]) : V(0);
+  }
+}
+
 int32_t read_int(const int32_t* d, cudaStream_t s) {
   int32_t h = 0;
   cuda_check(cudaMemcpyAsync(&h, d, sizeof(int32_t), cudaMemcpyDeviceToHost, s), "graph set-up read");
@@ -375,6 +428,37 @@ int32_t read_int(const int32_t* d, cudaStream_t s) {
 }
 
 }  // namespace
+
+void sell_structure(int64_t nrows, const int32_t* rowptr, const int32_t* colidx, SellStructure* out, cudaStream_t s) {
+  SellStructure& S = *out;
+  S.nrows = nrows;
+  S.nslices = (nrows + 31) / 32;
+  DeviceBuffer<int32_t> width(static_cast<size_t>(S.nslices)), off32(static_cast<size_t>(S.nslices) + 1);
+  count_launches(1);
+  k_slice_width<<<grid_for_rows(S.nslices), kT, 0, s>>>(S.nslices, nrows, rowptr, width.get());
+  S.nslots = exclusive_scan(width.get(), off32.get(), S.nslices, s);
+  S.off.resize(static_cast<size_t>(S.nslices) + 1);
+  S.cols.resize(static_cast<size_t>(S.nslots) * 32);
+  S.bpos.resize(static_cast<size_t>(S.nslots) * 32);
+  count_launches(2);
+  k_widen<<<grid_for_rows(S.nslices + 1), kT, 0, s>>>(S.nslices, off32.get(), S.off.get());
+  k_sell_fill<<<grid_for_rows(S.nslices * 32), kT, 0, s>>>(S.nslices, nrows, rowptr, colidx, S.off.get(), S.cols.get(),
+                                                           S.bpos.get());
+  cuda_check(cudaStreamSynchronize(s), "SELL layout");
+}
+
+void sell_values(const SellStructure& S, int bs, const double* bsr, double* out, cudaStream_t s) {
+  const int64_t nv = S.nslots * 32 * bs * bs;
+  if (nv == 0) return;
+  count_launches(1);
+  k_sell_values<double><<<grid_for_rows(nv), kT, 0, s>>>(nv, bs * bs, S.bpos.get(), bsr, out);
+}
+void sell_values(const SellStructure& S, int bs, const double* bsr, float* out, cudaStream_t s) {
+  const int64_t nv = S.nslots * 32 * bs * bs;
+  if (nv == 0) return;
+  count_launches(1);
+  k_sell_values<float><<<grid_for_rows(nv), kT, 0, s>>>(nv, bs * bs, S.bpos.get(), bsr, out);
+}
 
 int64_t exclusive_scan(const int32_t* in, int32_t* out, int64_t n, cudaStream_t s) {
   if (n <= 0) {

@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include "model.hpp"
+#include "sell.cuh"
 
 namespace dcgpu {
 
@@ -60,5 +61,28 @@ struct CoarseStructure {
 };
 void coarse_structure(const DeviceGraph& fine, const int32_t* agg, int64_t na, CoarseStructure* out,
                       cudaStream_t s);
+
+// SELL-32 layout (sell.cuh) of a BSR pattern, built on the device: slot offsets per slice of
+// 32 rows, the padded block columns, and for every slot the BSR block it holds (-1: padding).
+struct SellStructure {
+  int64_t nrows = 0, nslices = 0, nslots = 0;
+  DeviceBuffer<int64_t> off;
+  DeviceBuffer<int32_t> cols, bpos;
+  Sell view(int bs) const {
+    Sell S;
+    S.nrows = static_cast<int>(nrows);
+    S.bs = bs;
+    S.nslices = nslices;
+    S.nslots = nslots;
+    S.off = off.get();
+    S.cols = cols.get();
+    return S;
+  }
+};
+void sell_structure(int64_t nrows, const int32_t* rowptr, const int32_t* colidx, SellStructure* out, cudaStream_t s);
+// out (nslots * 32 * bs * bs values) = the BSR blocks `bsr` in the layout S with the
+// entries interleaved by lane (sellrow.cuh), padding zero
+void sell_values(const SellStructure& S, int bs, const double* bsr, double* out, cudaStream_t s);
+void sell_values(const SellStructure& S, int bs, const double* bsr, float* out, cudaStream_t s);
 
 }  // namespace dcgpu

@@ -7,6 +7,7 @@
 #include "blockops.cuh"
 #include "graph.hpp"
 #include "linalg.cuh"
+#include "sellrow.cuh"
 
 namespace dcgpu {
 
@@ -39,65 +40,62 @@ __global__ void k_inverse_positions(int64_t n, const int32_t* __restrict__ perm,
 // row of colour c in row i).  dmat holds the inverse pivot blocks of the mode.
 enum SweepMode : int { kSorFirst = 0, kSorFull = 1, kLowerSolve = 2, kUpperSolve = 3, kDiluLower = 4, kDiluUpper = 5 };
 
-template <int B, class T, class V, int MODE>
-__global__ void __launch_bounds__(kT) k_sweep(int64_t begin, int64_t end, const int32_t* __restrict__ perm,
-                                              const int32_t* __restrict__ rowptr, const int32_t* __restrict__ colidx,
-                                              const int32_t* __restrict__ colour, int c, const V* __restrict__ vals,
-                                              const V* __restrict__ dmat, const T* __restrict__ r, T* __restrict__ z,
-                                              V omega, const double* sc, int slot) {
+template <int B, class T, int MODE>
+__global__ void __launch_bounds__(kT) k_sweep(Sell S, const int32_t* __restrict__ colour, int c,
+                                              const T* __restrict__ vals, const T* __restrict__ dmat,
+                                              const T* __restrict__ r, T* __restrict__ z, T omega, const double* sc,
+                                              int slot) {
   if (skip(sc, slot)) return;
-  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-  for (int64_t p = begin + static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; p < end; p += stride) {
-    const int32_t i = perm[p];
-    const int64_t oi = static_cast<int64_t>(i) * B;
-    V t[B];
+  const SliceLoop L;
+  for (int64_t sl = L.first; sl < S.nslices; sl += L.stride) {
+    const int64_t i = sl * 32 + L.lane;
+    if (i >= S.nrows || colour[i] != c) continue;
+    const int64_t oi = i * B;
+    T t[B];
 #pragma unroll
     for (int s = 0; s < B; ++s) {
-      if (MODE == kSorFirst || MODE == kSorFull) t[s] = static_cast<V>(r[oi + s]);
-      else if (MODE == kLowerSolve || MODE == kDiluLower) t[s] = omega * static_cast<V>(r[oi + s]);
-      else if (MODE == kUpperSolve) t[s] = static_cast<V>(z[oi + s]);
-      else t[s] = V(0);
+      if (MODE == kSorFirst || MODE == kSorFull) t[s] = r[oi + s];
+      else if (MODE == kLowerSolve || MODE == kDiluLower) t[s] = omega * r[oi + s];
+      else if (MODE == kUpperSolve) t[s] = z[oi + s];
+      else t[s] = T(0);
     }
-    for (int32_t e = rowptr[i]; e < rowptr[i + 1]; ++e) {
-      const int32_t j = colidx[e];
-      if (MODE != kSorFull) {
-        const int cj = colour[j];
-        const bool lower = cj < c;
-        const bool upper = cj > c;
-        if ((MODE == kSorFirst || MODE == kLowerSolve || MODE == kDiluLower) ? !lower : !upper) continue;
-      }
-      const V* blk = vals + static_cast<int64_t>(e) * B * B;
-      V zj[B];
+    T acc[B];
 #pragma unroll
-      for (int q = 0; q < B; ++q) zj[q] = static_cast<V>(z[static_cast<int64_t>(j) * B + q]);
+    for (int s = 0; s < B; ++s) acc[s] = T(0);
+    sell_row_apply<B, T>(
+        S, sl, L.lane, vals,
+        [&](int32_t j) {
+          if (MODE == kSorFull) return true;
+          const int cj = colour[j];
+          return (MODE == kSorFirst || MODE == kLowerSolve || MODE == kDiluLower) ? cj < c : cj > c;
+        },
+        [&](int32_t j, T (&xv)[B]) {
 #pragma unroll
-      for (int s = 0; s < B; ++s) {
-        V acc = V(0);
+          for (int q = 0; q < B; ++q) xv[q] = z[static_cast<int64_t>(j) * B + q];
+        },
+        acc);
 #pragma unroll
-        for (int q = 0; q < B; ++q) acc += blk[s * B + q] * zj[q];
-        t[s] -= acc;
-      }
-    }
+    for (int s = 0; s < B; ++s) t[s] -= acc[s];
     if (MODE == kLowerSolve) {
 #pragma unroll
-      for (int s = 0; s < B; ++s) z[oi + s] = static_cast<T>(t[s]);
+      for (int s = 0; s < B; ++s) z[oi + s] = t[s];
       continue;
     }
-    const V* d = dmat + static_cast<int64_t>(i) * B * B;
-    V out[B];
+    const T* d = dmat + i * B * B;
+    T out[B];
 #pragma unroll
     for (int s = 0; s < B; ++s) {
-      V acc = V(0);
+      T a = T(0);
 #pragma unroll
-      for (int q = 0; q < B; ++q) acc += d[s * B + q] * t[q];
-      out[s] = acc;
+      for (int q = 0; q < B; ++q) a += d[s * B + q] * t[q];
+      out[s] = a;
     }
 #pragma unroll
     for (int s = 0; s < B; ++s) {
-      if (MODE == kSorFirst) z[oi + s] = static_cast<T>(omega * out[s]);
-      else if (MODE == kSorFull) z[oi + s] = static_cast<T>(static_cast<V>(z[oi + s]) + omega * out[s]);
-      else if (MODE == kDiluUpper) z[oi + s] = static_cast<T>(static_cast<V>(z[oi + s]) + out[s]);
-      else z[oi + s] = static_cast<T>(out[s]);
+      if (MODE == kSorFirst) z[oi + s] = omega * out[s];
+      else if (MODE == kSorFull) z[oi + s] = z[oi + s] + omega * out[s];
+      else if (MODE == kDiluUpper) z[oi + s] = z[oi + s] + out[s];
+      else z[oi + s] = out[s];
     }
   }
 }
@@ -224,6 +222,7 @@ void ColorPrecond::build(Kind kind, int64_t nrows, int bs, int64_t nnzb, const i
   order_by_color(nrows, colour_.get(), nc, perm_.get(), &offsets_, s);
   count_launches(1);
   k_inverse_positions<<<grid_for(nrows), kT, 0, s>>>(nrows, perm_.get(), ipos_.get());
+  sell_structure(nrows, rowptr, colidx, &sell_, s);
   const size_t nb2 = static_cast<size_t>(bs) * bs;
   if (kind == Kind::Ilu0) {
     lu_.resize(static_cast<size_t>(nnzb) * nb2);
@@ -234,12 +233,11 @@ void ColorPrecond::build(Kind kind, int64_t nrows, int bs, int64_t nnzb, const i
   cuda_check(cudaStreamSynchronize(s), "multicolour set-up");
 }
 
-void ColorPrecond::setup(const double* vals, const double* dinv, const float* vals32, const float* dinv32, bool fp32,
-                         int* status, cudaStream_t s) {
-  vals_ = vals;
+void ColorPrecond::setup(const double* vals, const double* dinv, const float* dinv32, bool fp32, int* status,
+                         cudaStream_t s) {
   dinv_ = dinv;
-  vals32_ = vals32;
   dinv32_ = dinv32;
+  fp32_ = fp32;
   const int nc = colors();
   const size_t nb2 = static_cast<size_t>(bs_) * bs_;
   if (kind_ == Kind::Ilu0) {
@@ -270,15 +268,19 @@ void ColorPrecond::setup(const double* vals, const double* dinv, const float* va
 #undef DC_DILU
     }
   }
+  // the SELL-32 copy the sweeps read: the ILU(0) factors, else the operator
+  const double* src = kind_ == Kind::Ilu0 ? lu_.get() : vals;
+  const size_t nv = static_cast<size_t>(sell_.nslots) * 32 * nb2;
   if (fp32) {
-    if (kind_ == Kind::Ilu0) {
-      if (lu32_.size() != lu_.size()) lu32_.resize(lu_.size());
-      to_float(static_cast<int64_t>(lu_.size()), lu_.get(), lu32_.get(), s);
-    }
+    if (sv32_.size() != nv) sv32_.resize(nv);
+    sell_values(sell_, bs_, src, sv32_.get(), s);
     if (kind_ == Kind::Ilu0 || kind_ == Kind::Dilu) {
       if (dfac32_.size() != dfac_.size()) dfac32_.resize(dfac_.size());
       to_float(static_cast<int64_t>(dfac_.size()), dfac_.get(), dfac32_.get(), s);
     }
+  } else {
+    if (sv64_.size() != nv) sv64_.resize(nv);
+    sell_values(sell_, bs_, src, sv64_.get(), s);
   }
 }
 
@@ -286,13 +288,13 @@ template <class T>
 void ColorPrecond::sweep_color(int mode, int c, const T* vals, const T* dmat, const T* r, T* z, const double* sc,
                                int done_slot, cudaStream_t s) const {
   using V = T;
-  const int64_t b = offsets_[c], e = offsets_[c + 1];
-  if (e == b) return;
+  if (offsets_[c + 1] == offsets_[c]) return;
   count_launches(1);
-  const int gb = grid_for(e - b);
+  const Sell S = sell_.view(bs_);
+  const int gb = grid_for(S.nslices * 32);
   const V w = static_cast<V>(omega);
 #define DC_SW(B, M) \
-  k_sweep<B, T, V, M><<<gb, kT, 0, s>>>(b, e, perm_.get(), rowptr_, colidx_, colour_.get(), c, vals, dmat, r, z, w, sc, done_slot)
+  k_sweep<B, T, M><<<gb, kT, 0, s>>>(S, colour_.get(), c, vals, dmat, r, z, w, sc, done_slot)
 #define DC_SWB(B)                                          \
   case B:                                                  \
     switch (mode) {                                        \
@@ -316,9 +318,16 @@ static const T* pick(const double* d, const float* f) {
 }
 
 template <class T>
+static void check_precision(bool fp32) {
+  if ((std::is_same<T, float>::value) != fp32)
+    throw std::runtime_error("multicolour preconditioner: applied in another precision than it was set up for");
+}
+
+template <class T>
 void ColorPrecond::sor_sweep(const T* r, T* z, bool forward, bool from_zero, const double* sc, int done_slot,
                              cudaStream_t s) const {
-  const T* A = pick<T>(vals_, vals32_);
+  check_precision<T>(fp32_);
+  const T* A = pick<T>(sv64_.get(), sv32_.get());
   const T* D = pick<T>(dinv_, dinv32_);
   if (A == nullptr || D == nullptr) throw std::runtime_error("multicolour sweep: values not set up");
   const int nc = colors();
@@ -335,8 +344,8 @@ template void ColorPrecond::sor_sweep<float>(const float*, float*, bool, bool, c
 
 template <class T>
 void ColorPrecond::apply_t(const T* r, T* z, const double* sc, int done_slot, cudaStream_t s) const {
-  const T* A = pick<T>(vals_, vals32_);
-  const T* LU = pick<T>(lu_.get(), lu32_.get());
+  check_precision<T>(fp32_);
+  const T* A = pick<T>(sv64_.get(), sv32_.get());  // operator, or the ILU(0) factors
   const T* DF = pick<T>(dfac_.get(), dfac32_.get());
   if (A == nullptr) throw std::runtime_error("multicolour preconditioner: values not set up");
   const int nc = colors();
@@ -349,14 +358,21 @@ void ColorPrecond::apply_t(const T* r, T* z, const double* sc, int done_slot, cu
       }
       break;
     case Kind::Ilu0:
-      for (int c = 0; c < nc; ++c) sweep_color<T>(kLowerSolve, c, LU, DF, r, z, sc, done_slot, s);
-      for (int c = nc - 1; c >= 0; --c) sweep_color<T>(kUpperSolve, c, LU, DF, r, z, sc, done_slot, s);
+      for (int c = 0; c < nc; ++c) sweep_color<T>(kLowerSolve, c, A, DF, r, z, sc, done_slot, s);
+      for (int c = nc - 1; c >= 0; --c) sweep_color<T>(kUpperSolve, c, A, DF, r, z, sc, done_slot, s);
       break;
     case Kind::Dilu:
       for (int c = 0; c < nc; ++c) sweep_color<T>(kDiluLower, c, A, DF, r, z, sc, done_slot, s);
       for (int c = nc - 1; c >= 0; --c) sweep_color<T>(kDiluUpper, c, A, DF, r, z, sc, done_slot, s);
       break;
   }
+}
+
+std::string ColorPrecond::describe() const {
+  static const char* names[] = {"SSOR", "SOR", "ILU0", "DILU"};
+  return "{\"type\": \"" + std::string(names[static_cast<int>(kind_)]) + "\", \"colours\": " +
+         std::to_string(colors()) + ", \"relaxation\": " + std::to_string(omega) +
+         ", \"iterations\": " + std::to_string(iterations) + "}";
 }
 
 void ColorPrecond::apply(const double* r, double* z, const double* sc, int done_slot, cudaStream_t s) const {

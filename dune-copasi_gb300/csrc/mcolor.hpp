@@ -14,10 +14,12 @@
 #pragma once
 
 #include <cstdint>
+#include <string>
 #include <vector>
 
 #include <cuda_runtime.h>
 
+#include "graph.hpp"
 #include "model.hpp"
 #include "precond.hpp"
 
@@ -36,10 +38,11 @@ class ColorPrecond : public Preconditioner {
   void build(Kind kind, int64_t nrows, int bs, int64_t nnzb, const int32_t* rowptr, const int32_t* colidx,
              const int32_t* diag, cudaStream_t s);
   // numeric set-up for new values: vals / dinv are the operator and its block-Jacobi
-  // inverses (fp64), vals32 / dinv32 their fp32 copies (needed with fp32; borrowed until the
-  // next setup).  ILU(0) and DILU factor here; status[0] != 0 on a singular pivot block.
-  void setup(const double* vals, const double* dinv, const float* vals32, const float* dinv32, bool fp32,
-             int* status, cudaStream_t s);
+  // inverses (fp64; dinv32 the inverses rounded to fp32, needed with fp32; borrowed until the
+  // next setup).  The sweeps then run in fp32 (fp32 true) or fp64 and read SELL-32 copies
+  // (sell.cuh) of the operator or factors made here.  ILU(0) and DILU factor here (in fp64);
+  // status[0] != 0 on a singular pivot block.
+  void setup(const double* vals, const double* dinv, const float* dinv32, bool fp32, int* status, cudaStream_t s);
   void apply(const double* r, double* z, const double* sc, int done_slot, cudaStream_t s) const override;
   void apply(const float* r, float* z, const double* sc, int done_slot, cudaStream_t s) const override;
 
@@ -51,6 +54,8 @@ class ColorPrecond : public Preconditioner {
                  cudaStream_t s) const;
 
   Kind kind() const { return kind_; }
+  // JSON object: kind, colours, relaxation, iterations
+  std::string describe() const;
   int colors() const { return static_cast<int>(offsets_.size()) - 1; }
   bool built() const { return !offsets_.empty(); }
   // colour of every block row and the rows in colour order (tests)
@@ -75,15 +80,15 @@ class ColorPrecond : public Preconditioner {
   const int32_t* diag_ = nullptr;
   DeviceBuffer<int32_t> colour_, perm_, ipos_;
   std::vector<int64_t> offsets_;  // colour c: perm[offsets_[c] .. offsets_[c + 1])
-  // borrowed operator values
-  const double* vals_ = nullptr;
+  SellStructure sell_;
+  bool fp32_ = false;  // precision of the last setup
+  // borrowed block-Jacobi inverses
   const double* dinv_ = nullptr;
-  const float* vals32_ = nullptr;
   const float* dinv32_ = nullptr;
-  // owned factors: ILU(0) L / U blocks in the pattern and the inverse pivot blocks; DILU
-  // inverse pivot blocks
-  DeviceBuffer<double> lu_, dfac_;
-  DeviceBuffer<float> lu32_, dfac32_;
+  // owned: the operator (SSOR / SOR / DILU) or the ILU(0) factors (L / U blocks in the
+  // pattern) in the SELL-32 layout; ILU(0) / DILU inverse pivot blocks per row
+  DeviceBuffer<double> lu_, dfac_, sv64_;
+  DeviceBuffer<float> dfac32_, sv32_;
 };
 
 // Richardson: z = omega r (dune-istl Richardson, the registry's matrix-free entry)

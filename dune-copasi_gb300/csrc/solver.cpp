@@ -213,11 +213,33 @@ Solver::Solver(Model& m, cudaStream_t s) : model(m), stream(s) {
 //   DILU                           multicolour block DILU (relaxation)
 //   Richardson                     z = relaxation * r
 //   AMG                            the aggregation multigrid V-cycle (engine addition)
+//   auto (the engine's default)    block Jacobi, until a solve needs more than
+//                                  preconditioner.auto_threshold (100) Krylov iterations or
+//                                  fails: the multigrid from then on (stiff systems)
 // InverseOperator (an inner solver as preconditioner) runs as block Jacobi: the outer
 // solve converges to the same tolerance.
+// the captured Krylov graphs hold the preconditioner's launches: drop them when it changes
+void Solver::graphs_invalidate() {
+  for (auto& g : graphs_) {
+    if (g) cudaGraphExecDestroy(g);
+    g = nullptr;
+  }
+}
+
+void Solver::build_multigrid() {
+  const Model& m = model;
+  std::vector<int32_t> group(m.nnodes, 0);
+  for (size_t c = 0; c < m.comp_names.size(); ++c)
+    for (int64_t k = m.comp_node_offset[c]; k < m.comp_node_offset[c + 1]; ++k) group[k] = static_cast<int32_t>(c);
+  row_group_.upload(group);
+  amg_->build(m.nnodes, m.bs, m.nnzb(), m.d_rowptr.get(), m.d_colidx.get(), m.d_diag.get(), row_group_.get(), stream);
+  pc_ = amg_.get();
+  graphs_invalidate();
+}
+
 void Solver::configure_preconditioner(const Ini& ls) {
   const Model& m = model;
-  precond_ = ls.get("preconditioner.type", "Jacobi");
+  precond_ = ls.get("preconditioner.type", "auto");
   const std::string& p = precond_;
   auto mc = [&](ColorPrecond::Kind kind, double omega_default) {
     mc_ = std::make_unique<ColorPrecond>();
@@ -247,7 +269,7 @@ void Solver::configure_preconditioner(const Ini& ls) {
     rich_.omega = ls.get_double("preconditioner.relaxation", 1.0);
     rich_.n = n_;
     pc_ = &rich_;
-  } else if (p == "AMG") {
+  } else if (p == "AMG" || p == "auto") {
     amg_ = std::make_unique<Amg>();
     const std::string sm = ls.get("preconditioner.smoother", "jacobi");
     if (sm == "jacobi") amg_->smoother = Amg::Smoother::Jacobi;
@@ -260,19 +282,32 @@ void Solver::configure_preconditioner(const Ini& ls) {
     amg_->max_levels = static_cast<int>(ls.get_long("preconditioner.max_level", 10));
     amg_->coarsen_target = ls.get_long("preconditioner.coarsen_target", 0);
     amg_->mis_distance = static_cast<int>(ls.get_long("preconditioner.aggregation_distance", 2));
+    amg_->correction = ls.get_double("preconditioner.coarse_correction", 1.0);
+    amg_->warp_rows_below = ls.get_long("preconditioner.warp_rows_below", Amg::kWarpRowsBelow);
+    if (!(amg_->correction > 0.0 && amg_->correction < 4.0))
+      throw ConfigError("linear_solver.preconditioner.coarse_correction must be in (0, 4)");
     if (amg_->mis_distance != 1 && amg_->mis_distance != 2)
       throw ConfigError("linear_solver.preconditioner.aggregation_distance must be 1 or 2");
     if (amg_->max_levels < 1) throw ConfigError("linear_solver.preconditioner.max_level must be >= 1");
-    std::vector<int32_t> group(m.nnodes, 0);
-    for (size_t c = 0; c < m.comp_names.size(); ++c)
-      for (int64_t k = m.comp_node_offset[c]; k < m.comp_node_offset[c + 1]; ++k) group[k] = static_cast<int32_t>(c);
-    row_group_.upload(group);
-    amg_->build(m.nnodes, m.bs, m.nnzb(), m.d_rowptr.get(), m.d_colidx.get(), m.d_diag.get(), row_group_.get(),
-                stream);
-    pc_ = amg_.get();
+    if (!(amg_->omega > 0.0 && amg_->omega < 2.0))
+      throw ConfigError("linear_solver.preconditioner.relaxation must be in (0, 2)");
+    auto_threshold_ = static_cast<int>(ls.get_long("preconditioner.auto_threshold", kAutoMultigridIterations));
+    if (auto_threshold_ < 1) throw ConfigError("linear_solver.preconditioner.auto_threshold must be >= 1");
+    auto_pc_ = p == "auto";
+    if (!auto_pc_) build_multigrid();
   } else {
     throw ConfigError("The key '" + p + "' is not a known preconditioner type");
   }
+}
+
+std::string Solver::precond_info() const {
+  if (auto_pc_)
+    return std::string("{\"type\": \"auto\", \"active\": ") +
+           (amg_->built() ? amg_->describe() : std::string("{\"type\": \"block_jacobi\"}")) + "}";
+  if (amg_) return amg_->describe();
+  if (mc_) return mc_->describe();
+  if (pc_ == &rich_) return "{\"type\": \"Richardson\", \"relaxation\": " + std::to_string(rich_.omega) + "}";
+  return "{\"type\": \"block_jacobi\", \"requested\": \"" + precond_ + "\"}";
 }
 
 void Solver::enable_mixed(bool on) {
@@ -282,7 +317,7 @@ void Solver::enable_mixed(bool on) {
     fphat_.resize(n_); fshat_.resize(n_); fx_.resize(n_); fb_.resize(n_);
     fp2_.resize(n_); fv2_.resize(n_);
     fdinv_.resize(static_cast<size_t>(model.nnodes) * model.bs * model.bs);
-    if (spmv_request_ != kSpmvSell || pc_) J32_.resize(static_cast<size_t>(model.nnzb()) * model.bs * model.bs);
+    if (spmv_request_ != kSpmvSell) J32_.resize(static_cast<size_t>(model.nnzb()) * model.bs * model.bs);
     if (spmv_request_ != kSpmvBsr) {
       // the padding slots stay zero: the fused gather of Model::assemble writes real blocks only
       Js32_.resize(static_cast<size_t>(model.sell_slots) * 32 * model.bs * model.bs);
@@ -319,7 +354,7 @@ void Solver::tune_spmv() {
   cudaEventDestroy(e1);
   spmv_format = spmv_tune_us[1] < spmv_tune_us[0] ? kSpmvSell : kSpmvBsr;
   if (spmv_format == kSpmvBsr) Js32_.resize(0);
-  else if (!pc_) J32_.resize(0);
+  else J32_.resize(0);
 }
 
 Solver::~Solver() {
@@ -449,17 +484,17 @@ void Solver::setup_preconditioner() {
     if (st) throw StepFailure("singular diagonal block in the Jacobian");
   }
   if (mixed_precision) {
-    // the BSR copy feeds the BSR SpMV, the tuner and the separately launched
-    // preconditioners; the SELL-32 copy feeds the SELL SpMV
-    const bool need_bsr = spmv_format != kSpmvSell || pc_;
+    // the BSR copy feeds the BSR SpMV and the tuner; the SELL-32 copy feeds the SELL SpMV
+    // (the separately launched preconditioners keep their own copies)
+    const bool need_bsr = spmv_format != kSpmvSell;
     const bool need_sell = spmv_format != kSpmvBsr;
     if (need_bsr) to_float(static_cast<int64_t>(model.nnzb()) * model.bs * model.bs, J_.get(), J32_.get(), stream);
     if (need_sell && !jac_sell_fresh_) bsr_to_sell(A, J_.get(), model.sell(), Js32_.get(), stream);
     if (spmv_format == kSpmvAuto) tune_spmv();
   }
   if (amg_ || mc_) {
-    if (amg_) amg_->setup(J_.get(), dinv_.get(), J32_.get(), fdinv_.get(), mixed_precision, status_.get(), stream);
-    else mc_->setup(J_.get(), dinv_.get(), J32_.get(), fdinv_.get(), mixed_precision, status_.get(), stream);
+    if (amg_) amg_->setup(J_.get(), dinv_.get(), fdinv_.get(), mixed_precision, status_.get(), stream);
+    else mc_->setup(J_.get(), dinv_.get(), fdinv_.get(), mixed_precision, status_.get(), stream);
     cuda_check(cudaMemcpyAsync(&st, status_.get(), sizeof(int), cudaMemcpyDeviceToHost, stream), "status");
     cuda_check(cudaStreamSynchronize(stream), "status");
     if (st) throw StepFailure(amg_ ? "singular diagonal block in a coarse multigrid level"
@@ -867,9 +902,21 @@ int Solver::linear_solve(const double* b, double* z, double rel_tol, int* iters)
   int it = 0;
   int st = mixed_precision ? bicgstab_mixed(b, z, rel_tol, lin_max_it_, &it) : bicgstab(b, z, rel_tol, lin_max_it_, &it);
   check_setup_status();
-  if (iters) *iters = it;
   stats.linear_iterations += it;
   ++stats.linear_solves;
+  // preconditioner "auto": a stiff system (many block-Jacobi iterations, or none enough)
+  // switches this model to the multigrid; a failed solve is repeated with it
+  if (auto_pc_ && !amg_->built() && (st != DC_OK || it > auto_threshold_)) {
+    build_multigrid();
+    if (st != DC_OK) {
+      int it2 = 0;
+      st = linear_solve(b, z, rel_tol, &it2);
+      it += it2;
+      if (iters) *iters = it;
+      return st;
+    }
+  }
+  if (iters) *iters = it;
   return st;
 }
 

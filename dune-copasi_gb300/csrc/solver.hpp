@@ -216,6 +216,19 @@ class Solver {
   RichardsonPrecond rich_;
   DeviceBuffer<int32_t> row_group_;  // compartment of every block row (multigrid)
   void configure_preconditioner(const Ini& ls);
+  void build_multigrid();
+  void graphs_invalidate();
+  // preconditioner "auto": block Jacobi until a solve needs more than auto_threshold_
+  // iterations, then the multigrid
+  static constexpr int kAutoMultigridIterations = 100;
+  bool auto_pc_ = false;
+  int auto_threshold_ = kAutoMultigridIterations;
+
+ public:
+  // the preconditioner in use as a JSON object
+  std::string precond_info() const;
+
+ private:
   // fp32 SpMV layout: kSpmvAuto times both on the first fp32 operator and keeps the faster
   int spmv_request_ = kSpmvAuto;
   void tune_spmv();

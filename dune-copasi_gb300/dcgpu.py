@@ -36,7 +36,7 @@ EXPORTED = [
     "dc_server_take_state", "dc_server_estimate", "dc_server_destroy", "dc_last_error",
     "dc_spmv_format", "dc_vertex_coords", "dc_constraints", "dc_reduce", "dc_write_vtk", "dc_config_get",
     "dc_selftest_barrier_timeout", "dc_step_stage_newton", "dc_selftest_fma_peaks", "dc_jit_selftest",
-    "dc_model_jit_status", "dc_selftest_color", "dc_selftest_aggregate", "dc_selftest_precond",
+    "dc_model_jit_status", "dc_precond_info", "dc_selftest_color", "dc_selftest_aggregate", "dc_selftest_precond",
 ]
 
 
@@ -108,6 +108,7 @@ def load_library(path=LIB_PATH):
     lib.dc_selftest_precond.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int64, ctypes.c_int32, pi32, pi32,
                                         pd, pi32, pd, pd, ctypes.c_int32, pd]
     lib.dc_model_jit_status.argtypes = [vp, ctypes.c_char_p, sz]
+    lib.dc_precond_info.argtypes = [vp, ctypes.c_char_p, sz]
     lib.dc_model_info_get.argtypes = [vp, P(ModelInfo)]
     lib.dc_species_name.argtypes = [vp, i32, ctypes.c_char_p, sz]
     lib.dc_species_size.argtypes = [vp, i32, P(ctypes.c_int64)]
@@ -378,6 +379,14 @@ class Model:
         buf = ctypes.create_string_buffer(4096)
         _check(self._lib.dc_model_jit_status(self._h, buf, len(buf)))
         return buf.value.decode()
+
+    def precond_info(self):
+        """The preconditioner of the linear solves (dict): type and structure (colours, or
+        rows / blocks / kernel kind of every multigrid level)."""
+        import json
+        buf = ctypes.create_string_buffer(16384)
+        _check(self._lib.dc_precond_info(self._h, buf, len(buf)))
+        return json.loads(buf.value.decode())
 
     def stage_newton(self):
         """Newton iterations of every stage solve of the last step (dc_step_stage_newton)."""

@@ -182,6 +182,11 @@ int dc_jit_selftest(char* message, size_t len);
  * interpreter kernels) or "interpreter (<reason>)" into buf.  Set by model.assembly.jit =
  * auto | true | false (auto: compiled for compartments of at least 2^18 cells). */
 int dc_model_jit_status(const dc_model* model, char* buf, size_t len);
+/* Preconditioner of the model's linear solves (no reference counterpart; the reference logs
+ * "Creating preconditioner with type ...", preconditioner.hh:127-128): a JSON object with the
+ * type and its structure (colours of the multicolour sweeps; rows, blocks and kernel kind per
+ * multigrid level), copied into buf. */
+int dc_precond_info(const dc_model* model, char* buf, size_t len);
 /* Arithmetic throughput of the current device (no reference counterpart; instrumentation
  * for the roofline of the FP64-bound assembly): FP64 and FP32 fused multiply-add rates in
  * TFLOP/s (2 flops per FMA), measured with independent FMA chains on every SM (~20 ms). */
@@ -198,7 +203,8 @@ int dc_selftest_fma_peaks(double* fp64_tflops, double* fp32_tflops);
  * "SOR", "ILU", "DILU" or "AMG") for the BSR matrix (block size bs, row-major blocks in
  * vals, every row holding its diagonal block), with `params` "key=value;..." (relaxation,
  * iterations; AMG: smoother 0 Jacobi / 1 L1-Jacobi / 2 Gauss-Seidel, relaxation,
- * coarse_sweeps, max_level, coarsen_target, aggregation_distance), applies it once to r
+ * coarse_sweeps, max_level, coarsen_target, aggregation_distance, coarse_correction,
+ * warp_rows_below), applies it once to r
  * (in fp64, or in fp32 when fp32 != 0) and writes z (nrows * bs).  info (8 doubles, may be
  * NULL): colours, or for AMG the levels, the dense coarse solve's unknowns (0: none) and
  * the rows of levels 0 to 5. */

@@ -212,9 +212,10 @@ def amg_hierarchy(rowptr, colidx, vals, bs, group, aggregate, distance=2, coarse
     return levels
 
 
-def amg_apply(levels, bs, r, smoother="jacobi", omega=0.8, coarse_sweeps=6, colour=None):
-    """One V(1,1) cycle z = M^-1 r.  colour(rowptr, colidx) -> colours (Gauss-Seidel only:
-    the engine's colouring of the level's graph)."""
+def amg_apply(levels, bs, r, smoother="jacobi", omega=0.8, coarse_sweeps=6, colour=None, correction=1.0):
+    """One V(1,1) cycle z = M^-1 r with the coarse-grid correction scaled by `correction`.
+    colour(rowptr, colidx) -> colours (Gauss-Seidel only: the engine's colouring of the
+    level's graph)."""
 
     def smoother_inverse(rp, ci, v):
         n = len(rp) - 1
@@ -269,7 +270,7 @@ def amg_apply(levels, bs, r, smoother="jacobi", omega=0.8, coarse_sweeps=6, colo
             order = color_order(colour(rp, ci))
             x = sor_apply(rp, ci, v, bs, order, rl, omega, 1, symmetric=False)
             xc = cycle(l + 1, restrict(rl - matvec(rp, ci, v, x)))
-            x = x + prolong(xc)
+            x = x + correction * prolong(xc)
             # backward sweep from the corrected iterate
             xs = x.reshape(n, bs).copy()
             d = diag_index(rp, ci)
@@ -283,7 +284,7 @@ def amg_apply(levels, bs, r, smoother="jacobi", omega=0.8, coarse_sweeps=6, colo
         S = smoother_inverse(rp, ci, v)
         t = omega * bdiag(S, rl)
         xc = cycle(l + 1, restrict(rl - matvec(rp, ci, v, t)))
-        y = t + prolong(xc)
+        y = t + correction * prolong(xc)
         return y + omega * bdiag(S, rl - matvec(rp, ci, v, y))
 
     return cycle(0, np.asarray(r, dtype=np.float64))

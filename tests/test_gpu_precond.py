@@ -144,7 +144,10 @@ def test_ilu0_is_exact_on_a_full_pattern(dcgpu_lib):
 
 
 AMG_CASES = [("jacobi", 2, 1, ""), ("jacobi", 1, 2, ""), ("l1jacobi", 2, 3, ""), ("gauss_seidel", 2, 2, ""),
-             ("gauss_seidel", 1, 1, ""), ("jacobi", 2, 2, "max_level=2"), ("gauss_seidel", 2, 4, "coarsen_target=3")]
+             ("gauss_seidel", 1, 1, ""), ("jacobi", 2, 2, "max_level=2"), ("gauss_seidel", 2, 4, "coarsen_target=3"),
+             ("jacobi", 2, 5, "coarse_correction=1.6;warp_rows_below=0"),
+             ("l1jacobi", 1, 3, "coarse_correction=1.3;warp_rows_below=100000"),
+             ("gauss_seidel", 2, 2, "coarse_correction=1.5;warp_rows_below=200")]
 SMOOTHER_ID = {"jacobi": 0, "l1jacobi": 1, "gauss_seidel": 2}
 
 
@@ -176,7 +179,8 @@ def test_multigrid_matches_restatement(dcgpu_lib, smoother, distance, bs, extra,
     assert int(info[1]) == (last_n if last_n <= P.DENSE_MAX else 0)
     if "max_level" in extra:
         assert info[1] == 0  # the coarsest level is above the dense limit: smoother sweeps
-    want = P.amg_apply(levels, bs, r, smoother, omega, colour=colour)
+    want = P.amg_apply(levels, bs, r, smoother, omega, colour=colour,
+                       correction=float(kv.get("coarse_correction", 1.0)))
     assert rel(z, want) <= (1e-4 if fp32 else 1e-11), (smoother, distance, bs, extra, rel(z, want))
 
 

@@ -524,7 +524,7 @@ std::vector<int32_t> Amg::colidx_host(int l) const {
 }
 
 void Amg::setup(const double* fine_vals, const double* fine_dinv, const float* fine_dinv32, bool fp32, int* status,
-                cudaStream_t s) {
+                cudaStream_t s, const Sell* fine_sell, const float* fine_sell32) {
   if (levels_.empty()) return;
   levels_[0].val = fine_vals;
   levels_[0].dinv = fine_dinv;
@@ -547,14 +547,25 @@ void Amg::setup(const double* fine_vals, const double* fine_dinv, const float* f
     block_jacobi_setup(A, c.diag, c.dinv_o.get(), status, s, fp32 ? c.dinv32_o.get() : nullptr);
     c.dinv32 = fp32 ? c.dinv32_o.get() : nullptr;
   }
-  // SELL-32 copies of the values in the precision the cycle runs in
+  // SELL-32 copies of the values in the precision the cycle runs in (level 0 may borrow the
+  // caller's)
+  {
+    Level& L0 = levels_[0];
+    L0.ext = fp32 && fine_sell && fine_sell32 && !L0.warp_rows && L0.sell.nslices > 0 &&
+             fine_sell->nrows == L0.nrows && fine_sell->bs == bs_;
+    if (L0.ext) {
+      L0.ext_view = *fine_sell;
+      L0.ext_sv32 = fine_sell32;
+      L0.sv32.resize(0);
+    }
+  }
   for (auto& L : levels_) {
     if (L.warp_rows && fp32) {
       const size_t nb = static_cast<size_t>(L.nnzb) * bs2;
       if (L.val32_o.size() != nb) L.val32_o.resize(nb);
       to_float(static_cast<int64_t>(nb), L.val, L.val32_o.get(), s);
     }
-    if (L.sell.nslices == 0) continue;
+    if (L.sell.nslices == 0 || L.ext) continue;
     const size_t nv = static_cast<size_t>(L.sell.nslots) * 32 * bs2;
     if (fp32) {
       if (L.sv32.size() != nv) L.sv32.resize(nv);
@@ -586,7 +597,7 @@ void Amg::setup(const double* fine_vals, const double* fine_dinv, const float* f
       switch (bs_) { DC_L1(1) DC_L1(2) DC_L1(3) DC_L1(4) DC_L1(5) DC_L1(6) DC_L1(7) DC_L1(8) }
 #undef DC_L1
     }
-    if (L.gs) L.gs->setup(L.val, L.dinv, L.dinv32, fp32, status, s);
+    if (L.gs) L.gs->setup(L.val, L.dinv, L.dinv32, fp32, status, s, L.ext ? &L.ext_view : nullptr, L.ext_sv32);
   }
   // dense coarsest solve
   if (dense_n_ > 0) {
@@ -609,9 +620,10 @@ template <class T>
 void Amg::cycle(int l, const T* r, T* x, const double* sc, int slot, cudaStream_t s) const {
   const Level& a = levels_[l];
   const int64_t n = a.nrows;
-  const T* A = a.warp_rows ? pickc<T>(a.val, a.val32_o.get()) : pick<T>(a.sv64, a.sv32);
+  const T* A = a.warp_rows ? pickc<T>(a.val, a.val32_o.get())
+                           : a.ext ? pickc<T>(nullptr, a.ext_sv32) : pick<T>(a.sv64, a.sv32);
   const T* D = pickc<T>(a.dinv, a.dinv32);
-  const Sell SA = a.sell.view(bs_);
+  const Sell SA = a.ext ? a.ext_view : a.sell.view(bs_);
   const int gw = blocks_for(n * 32);  // warp per row
   const T w = static_cast<T>(omega);
   const T cs = static_cast<T>(correction);

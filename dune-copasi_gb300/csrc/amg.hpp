@@ -58,8 +58,10 @@ class Amg : public Preconditioner {
   // Galerkin values, smoothers and the coarse factorisation from the fine values
   // (fine_dinv: the fine block-Jacobi inverses already computed by the solver).  The cycle
   // then runs in fp32 (fp32 true; fine_dinv32: the inverses already rounded) or in fp64.
+  // With fine_sell / fine_sell32 (fp32 only), the finest level's products read that SELL-32
+  // copy of the fine operator (the Krylov solve's own) instead of a copy of their own.
   void setup(const double* fine_vals, const double* fine_dinv, const float* fine_dinv32, bool fp32, int* status,
-             cudaStream_t s);
+             cudaStream_t s, const Sell* fine_sell = nullptr, const float* fine_sell32 = nullptr);
   // z = M^-1 r, one V(1,1)-cycle; no work when sc != nullptr and sc[done] != 0
   void apply(const double* r, double* z, const double* sc, int done_slot, cudaStream_t s) const override;
   void apply(const float* r, float* z, const double* sc, int done_slot, cudaStream_t s) const override;
@@ -111,6 +113,9 @@ class Amg : public Preconditioner {
     // and each lane would walk a long coarse row alone)
     bool warp_rows = false;
     SellStructure sell;
+    bool ext = false;  // level 0 reading the caller's SELL-32 copy (ext_view, ext_sv32)
+    Sell ext_view{};
+    const float* ext_sv32 = nullptr;
     DeviceBuffer<double> sv64;
     DeviceBuffer<float> sv32, val32_o;
     // smoother inverses (L1-Jacobi: own; else the block-Jacobi inverses above)

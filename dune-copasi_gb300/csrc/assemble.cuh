@@ -20,9 +20,18 @@ namespace dcgpu {
 // mode bit 1: residual, bit 2: Jacobian; kVolumeNumericalJacobian: Jacobian by forward
 // differences of the residual terms (params.prog / res_terms must be the residual program)
 constexpr int kVolumeNumericalJacobian = 4;
+// matrix-free Jacobian products: mode kVolumeJacobianApply | 2 evaluates each element's
+// Jacobian and writes J_e v_e into the residual records (params.v, params.slot_pos);
+// launch_faces with kFaceJacobianApply adds the face Jacobians times params.v to params.y
+constexpr int kVolumeJacobianApply = 8;
+constexpr int kFaceJacobianApply = 8;
 void launch_volume(int dim, int ns, const VolumeParams& p, int begin, int end, int mode,
                    cudaStream_t stream);
 void launch_faces(int dim, const FaceParams& p, int begin, int end, int mode, cudaStream_t stream);
+// y = v on the unit rows of the Jacobian: the padded species slots of every block row
+// (row_ns may be null: no padding) and the constrained DOFs
+void launch_unit_rows_apply(const int8_t* row_ns, int64_t nrows, int bs, const int64_t* cons, int64_t ncons,
+                            const double* v, double* y, cudaStream_t stream);
 // numerical Jacobian of the outflow terms (forward differences of the face residuals) added to p.J
 void launch_faces_fd(int dim, const FaceParams& p, int begin, int end, double eps, cudaStream_t stream);
 // volume assembly is two-phase: k_volume writes per-element outputs (er / ej of

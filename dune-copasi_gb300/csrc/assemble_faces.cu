@@ -7,6 +7,7 @@
 // face quadrature points; gradients (only loaded when a program reads them) come from
 // the full neighbouring cells.  Values of species living on the other side are taken at
 // the same physical point through the other side's own cell.
+#include <algorithm>
 #include <stdexcept>
 
 #include "assemble.cuh"
@@ -209,7 +210,8 @@ __global__ void __launch_bounds__(128) k_faces(const FaceParams P, const int beg
   const double ielem = P.ielem[f];
   const double fvol = P.fvolume[f];
   const bool do_res = (mode & 1) && P.r;
-  const bool do_jac = (mode & 2) && P.J;
+  const bool do_apply = (mode & kFaceJacobianApply) != 0;  // matrix-free: y += J_face v
+  const bool do_jac = ((mode & 2) && P.J) || do_apply;
 
   double R[kMaxDevRegisters];
   for (int side = 0; side < 2; ++side) {
@@ -237,7 +239,11 @@ __global__ void __launch_bounds__(128) k_faces(const FaceParams P, const int beg
             double v = 0.0;
             for (int q = 0; q < NQ; ++q)
               v += coef[T.coef + q] * FaceRule<DIM>::lam(q, k) * FaceRule<DIM>::lam(q, l);
-            P.J[static_cast<int64_t>(bp[k * NF + l]) * bs2 + T.test * bs + T.trial] += v;
+            if (do_apply)
+              P.y[static_cast<int64_t>(node[side][k]) * bs + T.test] +=
+                  v * P.v[static_cast<int64_t>(node[col_side][l]) * bs + T.trial];
+            else
+              P.J[static_cast<int64_t>(bp[k * NF + l]) * bs2 + T.test * bs + T.trial] += v;
           }
       }
     }
@@ -326,7 +332,25 @@ __global__ void k_constraint_rows(double* J, ConstraintRows cr, const int64_t* _
   J[static_cast<int64_t>(cr.diag[br]) * bs2 + i * bs + i] = 1.0;
 }
 
+// y = v on the rows whose Jacobian row is a unit row: padded species slots (row_ns[i] <= s
+// < bs) and constrained DOFs
+__global__ void k_unit_rows_apply(const int8_t* __restrict__ row_ns, int64_t nrows, int bs, const int64_t* __restrict__ cons,
+                                  int64_t ncons, const double* __restrict__ v, double* __restrict__ y) {
+  const int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (row_ns && t < nrows)
+    for (int s = row_ns[t]; s < bs; ++s) y[t * bs + s] = v[t * bs + s];
+  if (t < ncons) y[cons[t]] = v[cons[t]];
+}
+
 }  // namespace
+
+void launch_unit_rows_apply(const int8_t* row_ns, int64_t nrows, int bs, const int64_t* cons, int64_t ncons,
+                            const double* v, double* y, cudaStream_t stream) {
+  const int64_t n = std::max<int64_t>(row_ns ? nrows : 0, ncons);
+  if (n <= 0) return;
+  count_launches(1);
+  k_unit_rows_apply<<<static_cast<int>((n + 255) / 256), 256, 0, stream>>>(row_ns, nrows, bs, cons, ncons, v, y);
+}
 
 void launch_constraints(double* v, const int64_t* idx, const double* val, int64_t n, int op, cudaStream_t stream) {
   if (n <= 0) return;

@@ -119,7 +119,7 @@ __global__ void k_gather_jacobian(double* __restrict__ J, int bs2, unsigned nslo
   // base and no separate copy of it into J runs
   const double v = (o.overwrite ? (o.base ? o.base[at] : 0.0) : J[at]) + static_cast<double>(acc);
   J[at] = v;
-  if (o.sell) o.sell[o.sell_bpos[blk] * bs2 + slot_pos[m]] = static_cast<float>(v);
+  if (o.sell) o.sell[sell_value_index(o.sell_bpos[blk], slot_pos[m], bs2)] = static_cast<float>(v);
 }
 
 // A gather that covers every block of J when only some entries of a block have dynamic
@@ -144,7 +144,7 @@ __global__ void k_gather_jacobian_full(double* __restrict__ J, unsigned bs2, uns
   double v = o.base ? o.base[at] : 0.0;
   if (m >= 0) v += static_cast<double>(gather_sum<E>(ptr[b], ptr[b + 1], list, ej, nslot, static_cast<unsigned>(m)));
   J[at] = v;
-  if (o.sell) o.sell[o.sell_bpos[blk] * bs2 + e] = static_cast<float>(v);
+  if (o.sell) o.sell[sell_value_index(o.sell_bpos[blk], e, bs2)] = static_cast<float>(v);
 }
 
 // The covering gather with a thread per block of J: the block's (cell, local pair) list is
@@ -208,7 +208,7 @@ __global__ void __launch_bounds__(kBlockGatherThreads)
     const int t = i / BS2, e = i - t * BS2;
     const double v = stage[t * SB + e];
     J[g0 + i] = v;
-    if (o.sell) o.sell[o.sell_bpos[block_begin + b0 + t] * BS2 + e] = static_cast<float>(v);
+    if (o.sell) o.sell[sell_value_index(o.sell_bpos[block_begin + b0 + t], e, BS2)] = static_cast<float>(v);
   }
 }
 

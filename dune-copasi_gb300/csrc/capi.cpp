@@ -302,6 +302,27 @@ int dc_assemble(dc_model* model, const double* x, double t, double cm, double ca
   });
 }
 
+int dc_jacobian_apply(dc_model* model, const double* x, double t, double cm, double ca, const double* v, double* y) {
+  return guarded([&] {
+    if (!model || !x || !v || !y) throw std::invalid_argument("null argument");
+    auto& m = *model->model;
+    const int64_t n = m.nnodes * m.bs;
+    std::vector<double> bx, bv;
+    m.to_blocked(std::vector<double>(x, x + m.ndof), bx);
+    m.to_blocked(std::vector<double>(v, v + m.ndof), bv);
+    dcgpu::DeviceBuffer<double> dx, dv, dy(static_cast<size_t>(n));
+    dx.upload(bx);
+    dv.upload(bv);
+    cudaStream_t s = model->stream;
+    m.jacobian_apply(dx.get(), t, cm, ca, dv.get(), dy.get(), s);
+    dcgpu::cuda_check(cudaStreamSynchronize(s), "jacobian apply");
+    std::vector<double> yb = dy.download(), yr;
+    m.from_blocked(yb, yr);
+    std::memcpy(y, yr.data(), m.ndof * sizeof(double));
+    return DC_OK;
+  });
+}
+
 int dc_pattern(const dc_model* model, int32_t* rowptr, size_t n_rowptr, int32_t* colidx, size_t n_colidx) {
   return guarded([&] {
     if (!model || !rowptr || !colidx) throw std::invalid_argument("null argument");

@@ -92,6 +92,11 @@ struct VolumeParams {
   double* ej;                // Jacobian: ((k * nl + a) * nl + b) * n_slots + slot
   int n_slots;               // distinct (test, trial) pairs of the Jacobian terms
   int all_mass;              // every Jacobian term is mass-type: symmetric element matrix
+  // matrix-free Jacobian products (mode kVolumeJacobianApply): the direction v (node-major,
+  // block size bs) and the block position test * bs + trial of every Jacobian slot; the
+  // element's J v goes to er like a residual
+  const double* v;
+  const int32_t* slot_pos;
   int jac_f32;               // element Jacobian in fp32 (ej then holds floats)
   // work the kernel may skip (uniform flags set from the program inputs and term kinds)
   int need_pos;              // a program reads position_*
@@ -139,6 +144,9 @@ struct FaceParams {
   const double* x;
   double* r;
   double* J;
+  // matrix-free Jacobian products (mode kFaceJacobianApply): y += J_face v
+  const double* v;
+  double* y;
   int bs;
   int species_offset[2];     // model-global species index of local species 0, per side
   int ns[2];

@@ -310,7 +310,7 @@ __device__ __forceinline__ void sell_rows_jacobi(const Sell& S, int64_t sl, int 
   for (int i = 0; i < B; ++i) acc[i] = V(0);
   const int64_t o0 = S.off[sl], o1 = S.off[sl + 1];
   const int32_t* __restrict__ cols = S.cols + o0 * 32 + lane;
-  const V* __restrict__ vbase = val + (o0 * 32 + lane) * (B * B);
+  const V* __restrict__ vbase = val + o0 * 32 * (B * B) + lane;
   const int w = static_cast<int>(o1 - o0);
   constexpr int U = 2;
   // the column indices of the next batch are loaded while the current batch's gathers are
@@ -335,7 +335,7 @@ __device__ __forceinline__ void sell_rows_jacobi(const Sell& S, int64_t sl, int 
 #pragma unroll
     for (int q = 0; q < U; ++q) {
       V blk[B * B];
-      load_block<B * B, false>(vbase + static_cast<int64_t>(k + q) * (32 * B * B), blk);
+      load_block_interleaved<B * B>(vbase + static_cast<int64_t>(k + q) * (32 * B * B), blk);
 #pragma unroll
       for (int i = 0; i < B; ++i)
 #pragma unroll
@@ -351,7 +351,7 @@ __device__ __forceinline__ void sell_rows_jacobi(const Sell& S, int64_t sl, int 
     combine_row<B, T, V, PU>(c, r, p, v, c1, c2, u);
     jacobi_apply<B, T, V>(dinv, c, u, xh);
     V blk[B * B];
-    load_block<B * B, false>(vbase + static_cast<int64_t>(k + q) * (32 * B * B), blk);
+    load_block_interleaved<B * B>(vbase + static_cast<int64_t>(k + q) * (32 * B * B), blk);
 #pragma unroll
     for (int i = 0; i < B; ++i)
 #pragma unroll

@@ -303,10 +303,10 @@ __global__ void __launch_bounds__(256) k_bsr_to_sell(Sell S, const int32_t* __re
     len = rowptr[t + 1] - k0;
   }
   for (int k = 0; k < w; ++k) {
-    float* dst = out + ((o0 + k) * 32 + lane) * (B * B);
+    float* dst = out + (o0 + k) * 32 * (B * B) + lane;
     const double* src = val + static_cast<int64_t>(k0 + k) * (B * B);
 #pragma unroll
-    for (int e = 0; e < B * B; ++e) dst[e] = k < len ? static_cast<float>(src[e]) : 0.0f;
+    for (int e = 0; e < B * B; ++e) dst[e * 32] = k < len ? static_cast<float>(src[e]) : 0.0f;
   }
 }
 

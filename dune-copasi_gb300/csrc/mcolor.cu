@@ -234,7 +234,7 @@ void ColorPrecond::build(Kind kind, int64_t nrows, int bs, int64_t nnzb, const i
 }
 
 void ColorPrecond::setup(const double* vals, const double* dinv, const float* dinv32, bool fp32, int* status,
-                         cudaStream_t s) {
+                         cudaStream_t s, const Sell* sell_ext, const float* sv32_ext) {
   dinv_ = dinv;
   dinv32_ = dinv32;
   fp32_ = fp32;
@@ -268,10 +268,20 @@ void ColorPrecond::setup(const double* vals, const double* dinv, const float* di
 #undef DC_DILU
     }
   }
-  // the SELL-32 copy the sweeps read: the ILU(0) factors, else the operator
+  // the SELL-32 copy the sweeps read: the ILU(0) factors, else the operator (possibly the
+  // caller's)
   const double* src = kind_ == Kind::Ilu0 ? lu_.get() : vals;
   const size_t nv = static_cast<size_t>(sell_.nslots) * 32 * nb2;
-  if (fp32) {
+  ext_sv32_ = (fp32 && kind_ != Kind::Ilu0 && sell_ext && sv32_ext && sell_ext->nrows == n_ && sell_ext->bs == bs_)
+                  ? sv32_ext : nullptr;
+  if (ext_sv32_) {
+    ext_view_ = *sell_ext;
+    sv32_.resize(0);
+    if (kind_ == Kind::Dilu) {
+      if (dfac32_.size() != dfac_.size()) dfac32_.resize(dfac_.size());
+      to_float(static_cast<int64_t>(dfac_.size()), dfac_.get(), dfac32_.get(), s);
+    }
+  } else if (fp32) {
     if (sv32_.size() != nv) sv32_.resize(nv);
     sell_values(sell_, bs_, src, sv32_.get(), s);
     if (kind_ == Kind::Ilu0 || kind_ == Kind::Dilu) {
@@ -290,7 +300,7 @@ void ColorPrecond::sweep_color(int mode, int c, const T* vals, const T* dmat, co
   using V = T;
   if (offsets_[c + 1] == offsets_[c]) return;
   count_launches(1);
-  const Sell S = sell_.view(bs_);
+  const Sell S = (ext_sv32_ && std::is_same<T, float>::value) ? ext_view_ : sell_.view(bs_);
   const int gb = grid_for(S.nslices * 32);
   const V w = static_cast<V>(omega);
 #define DC_SW(B, M) \
@@ -327,7 +337,7 @@ template <class T>
 void ColorPrecond::sor_sweep(const T* r, T* z, bool forward, bool from_zero, const double* sc, int done_slot,
                              cudaStream_t s) const {
   check_precision<T>(fp32_);
-  const T* A = pick<T>(sv64_.get(), sv32_.get());
+  const T* A = pick<T>(sv64_.get(), ext_sv32_ ? ext_sv32_ : sv32_.get());
   const T* D = pick<T>(dinv_, dinv32_);
   if (A == nullptr || D == nullptr) throw std::runtime_error("multicolour sweep: values not set up");
   const int nc = colors();
@@ -345,7 +355,7 @@ template void ColorPrecond::sor_sweep<float>(const float*, float*, bool, bool, c
 template <class T>
 void ColorPrecond::apply_t(const T* r, T* z, const double* sc, int done_slot, cudaStream_t s) const {
   check_precision<T>(fp32_);
-  const T* A = pick<T>(sv64_.get(), sv32_.get());  // operator, or the ILU(0) factors
+  const T* A = pick<T>(sv64_.get(), ext_sv32_ ? ext_sv32_ : sv32_.get());  // operator, or the ILU(0) factors
   const T* DF = pick<T>(dfac_.get(), dfac32_.get());
   if (A == nullptr) throw std::runtime_error("multicolour preconditioner: values not set up");
   const int nc = colors();

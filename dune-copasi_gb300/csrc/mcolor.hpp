@@ -42,7 +42,10 @@ class ColorPrecond : public Preconditioner {
   // next setup).  The sweeps then run in fp32 (fp32 true) or fp64 and read SELL-32 copies
   // (sell.cuh) of the operator or factors made here.  ILU(0) and DILU factor here (in fp64);
   // status[0] != 0 on a singular pivot block.
-  void setup(const double* vals, const double* dinv, const float* dinv32, bool fp32, int* status, cudaStream_t s);
+  // With sell_ext / sv32_ext (fp32, SSOR / SOR / DILU), the sweeps read that SELL-32 copy
+  // of the operator (the Krylov solve's own) instead of a copy of their own.
+  void setup(const double* vals, const double* dinv, const float* dinv32, bool fp32, int* status, cudaStream_t s,
+             const Sell* sell_ext = nullptr, const float* sv32_ext = nullptr);
   void apply(const double* r, double* z, const double* sc, int done_slot, cudaStream_t s) const override;
   void apply(const float* r, float* z, const double* sc, int done_slot, cudaStream_t s) const override;
 
@@ -82,6 +85,8 @@ class ColorPrecond : public Preconditioner {
   std::vector<int64_t> offsets_;  // colour c: perm[offsets_[c] .. offsets_[c + 1])
   SellStructure sell_;
   bool fp32_ = false;  // precision of the last setup
+  Sell ext_view_{};
+  const float* ext_sv32_ = nullptr;  // borrowed operator copy (null: own)
   // borrowed block-Jacobi inverses
   const double* dinv_ = nullptr;
   const float* dinv32_ = nullptr;

@@ -1354,4 +1354,77 @@ bool Model::assemble(const double* x, double t, double cm, double ca, double* r,
   return gout.sell != nullptr;
 }
 
+void Model::jacobian_apply(const double* x, double t, double cm, double ca, const double* v, double* y,
+                           cudaStream_t s) const {
+  cuda_check(cudaMemsetAsync(y, 0, static_cast<size_t>(nnodes) * bs * sizeof(double), s), "memset");
+  const Bsr A0 = bsr(nullptr, nullptr);
+  if (has_Ms && cm != 0.0) spmv_acc(A0, d_Ms.get(), v, y, cm, s);
+  if (has_Ks && ca != 0.0) spmv_acc(A0, d_Ks.get(), v, y, ca, s);
+  for (const auto& g : vgroups) {
+    if (!(cm != 0.0 && g.has_mass) && !(ca != 0.0 && g.has_stiffness)) continue;
+    if (g.slots_dyn == 0) continue;
+    VolumeParams p{};
+    p.coords = d_coords.get();
+    p.verts = g.verts.get();
+    p.nodes = g.nodes.get();
+    p.bpos = g.bpos.get();
+    p.prog = g.prog_all.view();
+    p.res_terms = g.d_res_a.get();
+    p.n_res_terms = static_cast<int>(g.res_terms_a.size());
+    p.jac_terms = g.d_jac.get();
+    p.n_jac_terms = static_cast<int>(g.jac_terms.size());
+    p.tables = tables;
+    p.x = x;
+    p.bs = bs;
+    p.species_offset = species_offset[g.comp];
+    p.t = t;
+    p.cm = cm;
+    p.ca = ca;
+    p.fd_eps = fd_eps;
+    p.er = d_er.get();
+    p.n_slots = g.slots_dyn;
+    p.all_mass = g.dyn_all_mass ? 1 : 0;
+    p.v = v;
+    p.slot_pos = g.slot_pos_dyn.get();
+    set_volume_flags(p, g.prog_all.host, g.res_terms_a, g.jac_terms, dim);
+    launch_volume(dim, g.ns, p, 0, static_cast<int>(g.ne), 2 | kVolumeJacobianApply, s);
+    launch_gather_residual(y, bs, g.ns, g.node_begin, g.nnodes, g.rlist_ptr.get(), g.rlist.get(), d_er.get(), s);
+  }
+  if (ca != 0.0) {
+    for (const auto& g : fgroups) {
+      FaceParams p{};
+      p.coords = d_coords.get();
+      p.fverts = g.fverts.get();
+      p.node_in = g.node_in.get();
+      p.node_out = g.node_out.get();
+      p.bpos = g.bpos.get();
+      p.normal = g.normal.get();
+      p.ielem = g.ielem.get();
+      p.fvolume = g.fvolume.get();
+      p.elem_in = g.elem_in.get();
+      p.elem_out = g.elem_out.get();
+      p.cells = d_cells.get();
+      for (int side = 0; side < 2; ++side) {
+        const int c = g.comp[side];
+        p.vnode[side] = c >= 0 ? d_comp_vnode[c].get() : nullptr;
+        p.terms[side] = g.d_terms[side].get();
+        p.n_terms[side] = static_cast<int>(g.terms[side].size());
+        p.prog[side] = g.prog[side].view();
+        p.species_offset[side] = c >= 0 ? species_offset[c] : 0;
+        p.ns[side] = c >= 0 ? ns[c] : 0;
+      }
+      p.tables = tables;
+      p.x = x;
+      p.v = v;
+      p.y = y;
+      p.bs = bs;
+      p.t = t;
+      p.ca = ca;
+      for (size_t k = 0; k + 1 < g.color_offsets.size(); ++k)
+        launch_faces(dim, p, g.color_offsets[k], g.color_offsets[k + 1], kFaceJacobianApply, s);
+    }
+  }
+  launch_unit_rows_apply(padded ? d_row_ns.get() : nullptr, nnodes, bs, d_cons_idx.get(), n_constraints, v, y, s);
+}
+
 }  // namespace dcgpu

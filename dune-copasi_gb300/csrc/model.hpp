@@ -251,6 +251,12 @@ class Model {
   // fp32 SELL-32 copy of J there; the return value says whether it did.
   bool assemble(const double* x, double t, double cm, double ca, double* r, double* J, int mode, cudaStream_t s,
                 float* jac_sell32 = nullptr) const;
+  // matrix-free Jacobian product y = (cm dM/dx + ca dA/dx)(x, t) v: the state-dependent
+  // volume and face terms evaluated per element / face (mode kVolumeJacobianApply /
+  // kFaceJacobianApply) and gathered like a residual, the constant terms from their matrices
+  // assembled at set-up, unit rows for padded species slots and constrained DOFs
+  void jacobian_apply(const double* x, double t, double cm, double ca, const double* v, double* y,
+                      cudaStream_t s) const;
   Bsr bsr(double* val, float* val32) const;
   Sell sell() const;  // SELL-32 layout of the pattern (values sized sell_slots * 32 * bs * bs)
   int64_t sell_slots = 0;

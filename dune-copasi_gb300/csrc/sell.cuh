@@ -2,19 +2,25 @@
 // Krylov operator.
 //
 // Block rows are taken in slices of 32 consecutive rows.  Slot k of a slice holds the k-th
-// stored block of each of its 32 rows, zero padded up to the slice's longest row.  The B x B
-// block of slot k of lane r (row 32 s + r) is contiguous, row-major, at
-// ((off[s] + k) * 32 + r) * B*B, and the slot's block column sits at (off[s] + k) * 32 + r.
-// A warp computes one slice, one lane per block row: a slot's 32 blocks are one contiguous
-// 32 * B*B-value stretch, which a lane reads with one 16-byte load for B = 2 (B*B / 4 loads
-// for B = 4), and the column load of the warp is one 128-byte line.  Padding slots point at
-// the row itself (row 0 past the last row) and hold zeros.
+// stored block of each of its 32 rows, zero padded up to the slice's longest row.  Slot
+// position p = (off[s] + k) * 32 + r belongs to lane r (row 32 s + r); the slot's block
+// column sits at cols[p], and entry e (row-major) of its B x B block at
+// sell_value_index(p, e, B*B) = (off[s] + k) * 32 * B*B + e * 32 + r: the values are
+// interleaved by entry, so when a warp (one slice, one lane per block row) reads entry e of
+// its 32 blocks it reads one contiguous line (128 bytes in fp32) for every block size, and
+// the column load of the warp is one 128-byte line as well.  Padding slots point at the row
+// itself (row 0 past the last row) and hold zeros.
 #pragma once
 
 #include <cstdint>
 #include <type_traits>
 
 namespace dcgpu {
+
+// index of entry e of the block at slot position p (bs2 = B*B values per block)
+__host__ __device__ inline int64_t sell_value_index(int64_t p, int e, int bs2) {
+  return (p >> 5) * 32 * bs2 + static_cast<int64_t>(e) * 32 + (p & 31);
+}
 
 struct Sell {
   int nrows = 0;                  // block rows
@@ -26,6 +32,13 @@ struct Sell {
 };
 
 #ifdef __CUDACC__
+// the N = B*B entries of one lane's block in the entry-interleaved layout (p: entry 0)
+template <int N, class V>
+__device__ __forceinline__ void load_block_interleaved(const V* __restrict__ p, V (&out)[N]) {
+#pragma unroll
+  for (int e = 0; e < N; ++e) out[e] = __ldg(p + e * 32);
+}
+
 // N consecutive values starting at p: 8- or 16-byte loads for fp32 runs of 2 or a multiple
 // of 4 values (the callers' offsets are multiples of 8 / 16 bytes), else N loads.
 // kCoherent reads through L2 only (ld.global.cg, for data that other blocks write inside
@@ -62,7 +75,7 @@ __device__ __forceinline__ void sell_lane_rows(const Sell& S, int64_t sl, int la
   for (int i = 0; i < B; ++i) acc[i] = V(0);
   const int64_t o0 = S.off[sl], o1 = S.off[sl + 1];
   const int32_t* __restrict__ cols = S.cols + o0 * 32 + lane;
-  const V* __restrict__ v = val + (o0 * 32 + lane) * (B * B);
+  const V* __restrict__ v = val + o0 * 32 * (B * B) + lane;
   const int w = static_cast<int>(o1 - o0);
   // slots in batches of U: the U column loads, then the U x gathers, are independent of
   // one another, so a lane has U (not one) dependent load chains in flight, and the next
@@ -86,7 +99,7 @@ __device__ __forceinline__ void sell_lane_rows(const Sell& S, int64_t sl, int la
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       V blk[B * B];
-      load_block<B * B, false>(v + static_cast<int64_t>(k + u) * (32 * B * B), blk);
+      load_block_interleaved<B * B>(v + static_cast<int64_t>(k + u) * (32 * B * B), blk);
 #pragma unroll
       for (int i = 0; i < B; ++i)
 #pragma unroll
@@ -100,7 +113,7 @@ __device__ __forceinline__ void sell_lane_rows(const Sell& S, int64_t sl, int la
     T xv[B];
     load_block<B, kCoherent>(x + static_cast<int64_t>(cn[u]) * B, xv);
     V blk[B * B];
-    load_block<B * B, false>(v + static_cast<int64_t>(k + u) * (32 * B * B), blk);
+    load_block_interleaved<B * B>(v + static_cast<int64_t>(k + u) * (32 * B * B), blk);
 #pragma unroll
     for (int i = 0; i < B; ++i)
 #pragma unroll

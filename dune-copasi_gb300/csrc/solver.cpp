@@ -159,15 +159,23 @@ Solver::Solver(Model& m, cudaStream_t s) : model(m), stream(s) {
   // the last correction of the direct-solve one
   direct_tol_ = ls.get_double("direct_tolerance", 1e-10);
   if (!(direct_tol_ > 0.0 && direct_tol_ < 1.0)) throw ConfigError("linear_solver.direct_tolerance must be in (0, 1)");
+  // linear_solver.matrix_free (make_step_operator.hh:201,289-293): the stage Jacobian is
+  // never assembled; each Krylov product J v is evaluated element by element (and face by
+  // face) at the Newton iterate, Model::jacobian_apply.  The reference then offers only its
+  // iterative solvers (inverse.hh:31-58) and the matrix-free preconditioners Richardson and
+  // InverseOperator (preconditioner.hh:94-95); the Krylov solve runs in fp64.
+  matrix_free_ = ls.get_bool("matrix_free", false);
+  if (matrix_free_) {
+    if (lin_direct_)
+      throw ConfigError("The key '" + lt + "' is not a known inverse operator type (linear_solver.matrix_free = true "
+                        "takes an iterative solver)");
+    if (m.numerical_jacobian)
+      throw ConfigError("linear_solver.matrix_free = true with model.jacobian.type = numerical is not supported");
+    mf_x_.resize(n_);
+    J_.resize(0);
+  }
   configure_preconditioner(ls);
   const bool want_mixed = ls.get("precision", "double") == "mixed";
-  // linear_solver.matrix_free (make_step_operator.hh:201,289-293): the reference then applies
-  // the stage Jacobian through the local operators' jacobian_apply without a matrix.  The
-  // products are the same; here they always come from the assembled matrix, because an
-  // element-wise re-evaluation of the FP64 term programs per Krylov iteration costs a full
-  // assembly per SpMV on GB300's FP64 pipe, while the assembled fp32/fp64 SpMV streams at
-  // the HBM rate.  The key is read (and validated) for drop-in compatibility.
-  (void)ls.get_bool("matrix_free", false);
   // mixed precision only: precision of the state-dependent Jacobian terms (single, default,
   // or double)
   const std::string jp = ls.get("jacobian_precision", "single");
@@ -239,8 +247,18 @@ void Solver::build_multigrid() {
 
 void Solver::configure_preconditioner(const Ini& ls) {
   const Model& m = model;
-  precond_ = ls.get("preconditioner.type", "auto");
+  precond_ = ls.get("preconditioner.type", matrix_free_ ? "Richardson" : "auto");
   const std::string& p = precond_;
+  if (matrix_free_) {
+    // InverseOperator (an inner solve as preconditioner) runs as Richardson with relaxation 1
+    if (p != "Richardson" && p != "InverseOperator")
+      throw ConfigError("The key '" + p + "' is not a known preconditioner type (linear_solver.matrix_free = true: "
+                        "Richardson, InverseOperator)");
+    rich_.omega = p == "Richardson" ? ls.get_double("preconditioner.relaxation", 1.0) : 1.0;
+    rich_.n = n_;
+    pc_ = &rich_;
+    return;
+  }
   auto mc = [&](ColorPrecond::Kind kind, double omega_default) {
     mc_ = std::make_unique<ColorPrecond>();
     mc_->omega = ls.get_double("preconditioner.relaxation", omega_default);
@@ -312,6 +330,7 @@ std::string Solver::precond_info() const {
 
 void Solver::enable_mixed(bool on) {
   mixed_precision = on;
+  if (matrix_free_) return;  // the matrix-free Krylov solve runs in fp64
   if (on && fr_.size() != static_cast<size_t>(n_)) {
     fr_.resize(n_); frhat_.resize(n_); fp_.resize(n_); fv_.resize(n_); fs_.resize(n_); ft_.resize(n_);
     fphat_.resize(n_); fshat_.resize(n_); fx_.resize(n_); fb_.resize(n_);
@@ -492,9 +511,14 @@ void Solver::setup_preconditioner() {
     if (need_sell && !jac_sell_fresh_) bsr_to_sell(A, J_.get(), model.sell(), Js32_.get(), stream);
     if (spmv_format == kSpmvAuto) tune_spmv();
   }
-  if (amg_ || mc_) {
-    if (amg_) amg_->setup(J_.get(), dinv_.get(), fdinv_.get(), mixed_precision, status_.get(), stream);
-    else mc_->setup(J_.get(), dinv_.get(), fdinv_.get(), mixed_precision, status_.get(), stream);
+  if ((amg_ && amg_->built()) || mc_) {
+    // in the mixed path the fine level reads the Krylov solve's own SELL-32 operator copy
+    const Sell S = model.sell();
+    const bool share = mixed_precision && spmv_format == kSpmvSell && Js32_.size() > 0;
+    const Sell* sp = share ? &S : nullptr;
+    const float* sv = share ? Js32_.get() : nullptr;
+    if (amg_) amg_->setup(J_.get(), dinv_.get(), fdinv_.get(), mixed_precision, status_.get(), stream, sp, sv);
+    else mc_->setup(J_.get(), dinv_.get(), fdinv_.get(), mixed_precision, status_.get(), stream, sp, sv);
     cuda_check(cudaMemcpyAsync(&st, status_.get(), sizeof(int), cudaMemcpyDeviceToHost, stream), "status");
     cuda_check(cudaStreamSynchronize(stream), "status");
     if (st) throw StepFailure(amg_ ? "singular diagonal block in a coarse multigrid level"
@@ -592,7 +616,8 @@ int Solver::gmres_t(double rel, int max_it, int* iters) {
       if (spmv_format == kSpmvSell) spmv_sell32(S, Js32_.get(), in, out, stream);
       else spmv32_vals(A, J32_.get(), in, out, stream);
     } else {
-      spmv(A, in, out, stream);
+      if (matrix_free_) jacobian_apply_mf(in, out);
+      else spmv(A, in, out, stream);
     }
   };
   auto norm = [&](const T* v) {
@@ -897,7 +922,123 @@ int Solver::bicgstab_mixed(const double* b, double* z, double rel_tol, int max_i
   return rn <= target ? DC_OK : DC_ERR_TIMEOUT;
 }
 
+// J v at the stored linearisation point, element by element (matrix-free mode)
+void Solver::jacobian_apply_mf(const double* v, double* y) {
+  tbegin(1);
+  model.jacobian_apply(mf_x_.get(), mf_t_, mf_cm_, mf_ca_, v, y, stream);
+  tend();
+}
+
+// Krylov solve without a matrix (linear_solver.matrix_free = true): every product is
+// jacobian_apply_mf, the preconditioner is Richardson (the only matrix-free entries of the
+// reference's registry are Richardson and InverseOperator, preconditioner.hh:94-95).  BiCGSTAB
+// (and the aliases that run as it) or CG, in fp64, the scalars read back each iteration;
+// GMRES runs gmres_t with the same product.  Right-hand side b, solution z.
+int Solver::krylov_mf(const double* b, double* z, double rel, int max_it, int* iters) {
+  const int64_t n = n_;
+  *iters = 0;
+  if (krylov_gmres_) {
+    cuda_check(cudaMemcpyAsync(kr_.get(), b, n * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");
+    const int st = gmres_t<double>(rel, max_it, iters);
+    cuda_check(cudaMemcpyAsync(z, kx_.get(), n * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");
+    return st;
+  }
+  if (gh_.size() < 8) gh_.resize(8);
+  if (gpart_.size() < static_cast<size_t>(kGmresBlocks) * 2) gpart_.resize(static_cast<size_t>(kGmresBlocks) * 2);
+  double* hd = gh_.get();
+  auto dotp = [&](const double* a, const double* c) {
+    gmres_mdot<double>(a, n, 1, c, hd, gpart_.get(), false, stream);
+    double h = 0.0;
+    cuda_check(cudaMemcpyAsync(&h, hd, sizeof(double), cudaMemcpyDeviceToHost, stream), "krylov");
+    cuda_check(cudaStreamSynchronize(stream), "krylov");
+    return h;
+  };
+  auto precond = [&](const double* in, double* out) { pc_->apply(in, out, nullptr, 0, stream); };
+  double* x = z;
+  double* r = kr_.get();
+  double* rt = krhat_.get();
+  double* p = kp_.get();
+  double* v = kv_.get();
+  double* y = kphat_.get();
+  double* zz = kshat_.get();
+  double* t = kt_.get();
+  cuda_check(cudaMemsetAsync(x, 0, n * sizeof(double), stream), "memset");
+  cuda_check(cudaMemcpyAsync(r, b, n * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");
+  const double r0 = std::sqrt(dotp(r, r));
+  if (r0 == 0.0) return DC_OK;
+  if (!std::isfinite(r0)) return DC_ERR_DIVERGED;
+  const double target = rel * r0;
+  if (krylov_cg_) {
+    // preconditioned CG: p = y = M^-1 r, q = A p in v
+    precond(r, y);
+    cuda_check(cudaMemcpyAsync(p, y, n * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");
+    double rho = dotp(r, y);
+    for (int it = 1; it <= max_it; ++it) {
+      jacobian_apply_mf(p, v);
+      const double pq = dotp(p, v);
+      if (pq == 0.0 || !std::isfinite(pq)) return DC_ERR_DIVERGED;
+      const double alpha = rho / pq;
+      axpy(n, alpha, p, x, stream);
+      axpy(n, -alpha, v, r, stream);
+      *iters = it;
+      const double rn = std::sqrt(dotp(r, r));
+      if (!std::isfinite(rn)) return DC_ERR_DIVERGED;
+      if (rn <= target) return DC_OK;
+      precond(r, y);
+      const double rho_new = dotp(r, y);
+      axpby(n, 1.0, y, rho_new / rho, p, stream);
+      rho = rho_new;
+    }
+    return DC_ERR_TIMEOUT;
+  }
+  // BiCGSTAB (dune-istl BiCGSTABSolver's recurrences)
+  cuda_check(cudaMemcpyAsync(rt, r, n * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");
+  cuda_check(cudaMemsetAsync(p, 0, n * sizeof(double), stream), "memset");
+  cuda_check(cudaMemsetAsync(v, 0, n * sizeof(double), stream), "memset");
+  double rho = 1.0, alpha = 1.0, omega = 1.0;
+  for (int it = 1; it <= max_it; ++it) {
+    const double rho_new = dotp(rt, r);
+    if (rho_new == 0.0 || !std::isfinite(rho_new)) return DC_ERR_DIVERGED;
+    const double beta = (rho_new / rho) * (alpha / omega);
+    // p = r + beta (p - omega v)
+    axpy(n, -omega, v, p, stream);
+    axpby(n, 1.0, r, beta, p, stream);
+    precond(p, y);
+    jacobian_apply_mf(y, v);
+    const double rtv = dotp(rt, v);
+    if (rtv == 0.0 || !std::isfinite(rtv)) return DC_ERR_DIVERGED;
+    alpha = rho_new / rtv;
+    axpy(n, -alpha, v, r, stream);  // r = s
+    axpy(n, alpha, y, x, stream);
+    *iters = it;
+    double rn = std::sqrt(dotp(r, r));
+    if (!std::isfinite(rn)) return DC_ERR_DIVERGED;
+    if (rn <= target) return DC_OK;
+    precond(r, zz);
+    jacobian_apply_mf(zz, t);
+    const double tt = dotp(t, t);
+    if (tt == 0.0 || !std::isfinite(tt)) return DC_ERR_DIVERGED;
+    omega = dotp(t, r) / tt;
+    axpy(n, omega, zz, x, stream);
+    axpy(n, -omega, t, r, stream);
+    rn = std::sqrt(dotp(r, r));
+    if (!std::isfinite(rn)) return DC_ERR_DIVERGED;
+    if (rn <= target) return DC_OK;
+    if (omega == 0.0) return DC_ERR_DIVERGED;
+    rho = rho_new;
+  }
+  return DC_ERR_TIMEOUT;
+}
+
 int Solver::linear_solve(const double* b, double* z, double rel_tol, int* iters) {
+  if (matrix_free_) {
+    int it = 0;
+    const int st = krylov_mf(b, z, rel_tol, lin_max_it_, &it);
+    stats.linear_iterations += it;
+    ++stats.linear_solves;
+    if (iters) *iters = it;
+    return st;
+  }
   setup_preconditioner();
   int it = 0;
   int st = mixed_precision ? bicgstab_mixed(b, z, rel_tol, lin_max_it_, &it) : bicgstab(b, z, rel_tol, lin_max_it_, &it);
@@ -1066,6 +1207,15 @@ void Solver::one_step(double dt) {
       model.constrain_jacobian(J_.get(), stream);
     };
     auto jac = [&](const double* y) {
+      if (matrix_free_) {
+        // linear_solver.matrix_free: no matrix; the Krylov solve's products J v are evaluated
+        // element by element at this linearisation point
+        cuda_check(cudaMemcpyAsync(mf_x_.get(), y, n_ * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");
+        mf_t_ = ti;
+        mf_cm_ = ai;
+        mf_ca_ = bi;
+        return;
+      }
       tbegin(4);
       jac_sell_fresh_ = model.assemble(y, ti, ai, bi, nullptr, J_.get(), 2 | jmode, stream, jac_sell_target());
       tend();
@@ -1073,7 +1223,7 @@ void Solver::one_step(double dt) {
       ++stats.assemblies;
     };
     auto resjac = [&](const double* y, double* r) {
-      if (split) {
+      if (split || matrix_free_) {
         // the residual (possibly from the kept D) and the Jacobian as separate passes
         res(y, r);
         jac(y);

@@ -218,6 +218,13 @@ class Solver {
   void configure_preconditioner(const Ini& ls);
   void build_multigrid();
   void graphs_invalidate();
+  // matrix-free mode: linearisation point of the last Jacobian request (state, time, mass
+  // and stiffness scales) and the products at it
+  bool matrix_free_ = false;
+  DeviceBuffer<double> mf_x_;
+  double mf_t_ = 0.0, mf_cm_ = 0.0, mf_ca_ = 0.0;
+  void jacobian_apply_mf(const double* v, double* y);
+  int krylov_mf(const double* b, double* z, double rel, int max_it, int* iters);
   // preconditioner "auto": block Jacobi until a solve needs more than auto_threshold_
   // iterations, then the multigrid
   static constexpr int kAutoMultigridIterations = 100;

@@ -160,9 +160,9 @@ __device__ __forceinline__ F volume_input(uint16_t id, const F (&u)[NS], const F
 // the terms (sorted by slot) are summed per slot and each slot stored once.  With only
 // mass-type terms the element matrix is symmetric and only a <= b is evaluated.  JT is the
 // arithmetic and storage type (fp64, or fp32 for the mixed-precision path).
-template <int DIM, class JT, class Spec, class Coef>
-__device__ __forceinline__ void element_jacobian(const VolumeParams& P, Coef coef, const JT (&G)[DIM + 1][DIM],
-                                                 JT* ej) {
+template <int DIM, class JT, class Spec, class Coef, class Sink>
+__device__ __forceinline__ void element_jacobian_to(const VolumeParams& P, Coef coef, const JT (&G)[DIM + 1][DIM],
+                                                    Sink sink) {
   constexpr int NL = DIM + 1;
   constexpr int NQ = Rule<DIM>::NQ;
   constexpr double al = MassConst<DIM>::alpha, be = MassConst<DIM>::beta;
@@ -213,21 +213,49 @@ __device__ __forceinline__ void element_jacobian(const VolumeParams& P, Coef coe
             break;
         }
         if (T.slot != cur) {
-          if (cur >= 0) {
-            ej[(a * NL + b) * nslot + cur] = acc;
-            if (all_mass && a != b) ej[(b * NL + a) * nslot + cur] = acc;
-          }
+          if (cur >= 0) sink(a, b, cur, acc, all_mass && a != b);
           cur = T.slot;
           acc = JT(0);
         }
         acc += v;
       }
-      if (cur >= 0) {
-        ej[(a * NL + b) * nslot + cur] = acc;
-        if (all_mass && a != b) ej[(b * NL + a) * nslot + cur] = acc;
-      }
+      if (cur >= 0) sink(a, b, cur, acc, all_mass && a != b);
     }
   }
+  (void)nslot;
+}
+
+// the element matrix stored per slot: ej[(a * NL + b) * n_slots + slot] (and the mirrored
+// pair of a symmetric all-mass matrix)
+template <int DIM, class JT, class Spec, class Coef>
+__device__ __forceinline__ void element_jacobian(const VolumeParams& P, Coef coef, const JT (&G)[DIM + 1][DIM],
+                                                 JT* ej) {
+  constexpr int NL = DIM + 1;
+  const int nslot = Spec::n_slots(P);
+  element_jacobian_to<DIM, JT, Spec>(P, coef, G, [&](int a, int b, int slot, JT acc, bool mirror) {
+    ej[(a * NL + b) * nslot + slot] = acc;
+    if (mirror) ej[(b * NL + a) * nslot + slot] = acc;
+  });
+}
+
+// the element matrix applied to the direction v at the element's block rows nd:
+// out[a][test] += J_e(a test, b trial) v(nd[b] trial) (matrix-free Jacobian products)
+template <int DIM, int NS, class JT, class Spec, class Coef>
+__device__ __forceinline__ void element_jacobian_apply(const VolumeParams& P, Coef coef, const JT (&G)[DIM + 1][DIM],
+                                                       const int (&nd)[DIM + 1], JT (&out)[DIM + 1][NS]) {
+  const int bs = P.bs;
+  element_jacobian_to<DIM, JT, Spec>(P, coef, G, [&](int a, int b, int slot, JT acc, bool mirror) {
+    const int pos = P.slot_pos[slot];
+    const int te = pos / bs, tr = pos - te * bs;
+    const JT vb = static_cast<JT>(P.v[static_cast<int64_t>(nd[b]) * bs + tr]);
+    const JT va = mirror ? static_cast<JT>(P.v[static_cast<int64_t>(nd[a]) * bs + tr]) : JT(0);
+#pragma unroll
+    for (int s = 0; s < NS; ++s)
+      if (s == te) {
+        out[a][s] += acc * vb;
+        if (mirror) out[b][s] += acc * va;
+      }
+  });
 }
 
 // The element kernel body for cell k.  R: the program's register file, coef: the
@@ -266,7 +294,8 @@ __device__ __forceinline__ void volume_element(const VolumeParams& P, const int 
   // the inverse (basis gradients) only when a gradient, a flux or the Jacobian needs it: a
   // reaction-only residual pass needs |det| alone, and the FP64 division is the dearest
   // operation of the geometry (uniform branch)
-  const bool need_inv = Spec::need_grad(P) || Spec::has_flux(P) || ((mode & 2) && P.J);
+  const bool do_apply = (mode & 8) != 0;  // matrix-free J v (kVolumeJacobianApply)
+  const bool need_inv = Spec::need_grad(P) || Spec::has_flux(P) || ((mode & 2) && P.J) || do_apply;
   if constexpr (DIM == 2) {
     det = Bm[0][0] * Bm[1][1] - Bm[0][1] * Bm[1][0];
     const F id = need_inv ? F(1) / det : F(0);
@@ -328,7 +357,7 @@ __device__ __forceinline__ void volume_element(const VolumeParams& P, const int 
     }
 
   const bool do_res = (mode & 1) && P.r;
-  const bool do_jac = (mode & 2) && P.J;
+  const bool do_jac = ((mode & 2) && P.J) || do_apply;
   const bool jac_prog = (mode & 2) != 0;  // which program and residual term list the pass runs
   // Every point of the rule sits at one vertex: phi_a(q) = beta + (alpha - beta) [a = v(q)].
   // So the value of species s at point q is beta sum_a c_a + (alpha - beta) c_v(q), and the
@@ -596,7 +625,19 @@ __device__ __forceinline__ void volume_element(const VolumeParams& P, const int 
     }
     const int64_t off = ej_dst ? 0 : static_cast<int64_t>(k) * NL * NL * Spec::n_slots(P);
     void* const ejb = ej_dst ? ej_dst : static_cast<void*>(P.ej);
-    if constexpr (same_type<F, float>::value) {
+    if (do_apply) {
+      F out[NL][NS];
+#pragma unroll
+      for (int a = 0; a < NL; ++a)
+#pragma unroll
+        for (int s = 0; s < NS; ++s) out[a][s] = F(0);
+      element_jacobian_apply<DIM, NS, F, Spec>(P, coef, G, nd, out);
+      double* er = er_dst ? er_dst : P.er + static_cast<int64_t>(k) * NL * NS;
+#pragma unroll
+      for (int a = 0; a < NL; ++a)
+#pragma unroll
+        for (int s = 0; s < NS; ++s) er[a * NS + s] = static_cast<double>(out[a][s]);
+    } else if constexpr (same_type<F, float>::value) {
       // the FP32 Jacobian-only pass of the mixed-precision path
       element_jacobian<DIM, float, Spec>(P, coef, G, static_cast<float*>(ejb) + off);
     } else if (P.jac_f32) {

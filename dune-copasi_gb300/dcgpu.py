@@ -36,7 +36,7 @@ EXPORTED = [
     "dc_server_take_state", "dc_server_estimate", "dc_server_destroy", "dc_last_error",
     "dc_spmv_format", "dc_vertex_coords", "dc_constraints", "dc_reduce", "dc_write_vtk", "dc_config_get",
     "dc_selftest_barrier_timeout", "dc_step_stage_newton", "dc_selftest_fma_peaks", "dc_jit_selftest",
-    "dc_model_jit_status", "dc_precond_info", "dc_selftest_color", "dc_selftest_aggregate", "dc_selftest_precond",
+    "dc_model_jit_status", "dc_precond_info", "dc_jacobian_apply", "dc_selftest_color", "dc_selftest_aggregate", "dc_selftest_precond",
 ]
 
 
@@ -109,6 +109,7 @@ def load_library(path=LIB_PATH):
                                         pd, pi32, pd, pd, ctypes.c_int32, pd]
     lib.dc_model_jit_status.argtypes = [vp, ctypes.c_char_p, sz]
     lib.dc_precond_info.argtypes = [vp, ctypes.c_char_p, sz]
+    lib.dc_jacobian_apply.argtypes = [vp, pd, ctypes.c_double, ctypes.c_double, ctypes.c_double, pd, pd]
     lib.dc_model_info_get.argtypes = [vp, P(ModelInfo)]
     lib.dc_species_name.argtypes = [vp, i32, ctypes.c_char_p, sz]
     lib.dc_species_size.argtypes = [vp, i32, P(ctypes.c_int64)]
@@ -436,6 +437,16 @@ class Model:
                                      _ptr(r) if r is not None else None,
                                      _ptr(J) if J is not None else None, nj if J is not None else 0))
         return r, J
+
+    def jacobian_apply(self, x, t, cm, ca, v):
+        """Matrix-free product (cm dM/dx + ca dA/dx)(x, t) v, reference order (dc_jacobian_apply)."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        y = np.zeros(self.ndof)
+        P = ctypes.POINTER(ctypes.c_double)
+        _check(self._lib.dc_jacobian_apply(self._h, x.ctypes.data_as(P), float(t), float(cm), float(ca),
+                                           v.ctypes.data_as(P), y.ctypes.data_as(P)))
+        return y
 
     def residual_noalloc(self, x, t, cm, ca, out=None):
         """Residual through the allocation-free entry point (staging in the library's fixed

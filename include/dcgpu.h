@@ -112,6 +112,13 @@ int dc_evolve(dc_model* model, double t_end, double* dt, dc_callback cb, void* u
  * cm * dM/dx + ca * dA/dx.  r and jac_values may be NULL. */
 int dc_assemble(dc_model* model, const double* x, double t, double cm, double ca, double* r, double* jac_values,
                 size_t n_jac_values);
+/* Matrix-free Jacobian product (replaces the local operators' jacobian_apply,
+ * local_operator.hh:510-524, 1354-1396, 1438-1455, as driven by
+ * PDELab::makeInstationaryMatrixFreeAssembler, make_step_operator.hh:289-293): at state x and
+ * time t, y = (cm * dM/dx + ca * dA/dx) v with every state-dependent volume and face term
+ * evaluated per element / face (vectors in reference order, ndof entries).  The Newton
+ * solve uses the same product under linear_solver.matrix_free = true. */
+int dc_jacobian_apply(dc_model* model, const double* x, double t, double cm, double ca, const double* v, double* y);
 /* No counterpart in the reference.  Residual assembly that allocates nothing, for callers
  * that cannot allocate device memory when they need a residual (their device memory is
  * owned by another allocator, or cudaMalloc/cudaFree would synchronise the device inside a

@@ -457,19 +457,77 @@ def test_gmsh_grid_matches_oracle(dcgpu_lib, tmp_path, dim):
         assert_newton_per_stage(n_o, n_g, (t,))
 
 
-def test_matrix_free_configuration(dcgpu_lib):
-    """linear_solver.matrix_free = true (make_step_operator.hh:289-293) is accepted and gives
-    the reference's Jacobian products (applied from the assembled matrix); a non-boolean
-    value is a configuration error."""
-    ini, init = ALL_CASES["features_2d"]()
-    ov = {"model.time_step_operator.linear_solver.matrix_free": "true"}
-    records = _run_both(dcgpu_lib, ini, init, overrides=ov)
+MF = {"model.time_step_operator.linear_solver.matrix_free": "true",
+      "model.time_step_operator.linear_solver.type": "BiCGSTAB",
+      "model.time_step_operator.linear_solver.preconditioner.type": "Richardson",
+      "model.time_step_operator.linear_solver.convergence_condition.relative_tolerance": "1e-12",
+      "model.time_step_operator.nonlinear_solver.convergence_condition.relative_tolerance": "1e-24"}
+
+
+@pytest.mark.parametrize("case", ["features_2d", "two_compartment", "features_3d_padded", "gray_scott",
+                                  "cross_diffusion_3d", "two_compartment_constrained"])
+def test_jacobian_apply_matches_assembled_product(dcgpu_lib, case):
+    """dc_jacobian_apply (per-element and per-face evaluation of the state-dependent terms,
+    the constant terms from their matrices) equals the assembled Jacobian times v, on the
+    rows that are not constrained (the assembled values carry no unit rows)."""
+    ini, init = ALL_CASES[case]()
+    gm = dcgpu_lib.Model(ini)
+    x = gm.seeded_state(init) if init is not None else gm.state()
+    rng = np.random.default_rng(11)
+    x = x * (1.0 + 0.1 * rng.standard_normal(x.size))
+    v = rng.standard_normal(x.size)
+    for cm, ca in ((1.0, 0.0), (0.0, 1.0), (1.0, 0.37)):
+        _r, J = gm.assemble(x, 0.25, cm, ca, residual=False)
+        want = gm.jacobian_csr(J) @ v
+        got = gm.jacobian_apply(x, 0.25, cm, ca, v)
+        free = np.ones(x.size, bool)
+        cons = gm.constraints()
+        if cons is not None and len(cons[0]):
+            free[np.asarray(cons[0])] = False
+            assert np.array_equal(got[~free], v[~free])
+        err = np.linalg.norm(got[free] - want[free]) / max(np.linalg.norm(want[free]), 1e-300)
+        assert err <= 1e-13, (case, cm, ca, err)
+    gm.close()
+
+
+@pytest.mark.parametrize("case", ["features_2d", "two_compartment", "features_3d_padded", "poisson_constrained"])
+def test_matrix_free_matches_oracle(dcgpu_lib, case):
+    """linear_solver.matrix_free = true (make_step_operator.hh:289-293): no matrix; BiCGSTAB +
+    Richardson with every product evaluated per element / face; the oracle's solution within
+    the Newton tolerance."""
+    ini, init = ALL_CASES[case]()
+    records = _run_both(dcgpu_lib, ini, init, overrides=MF)
     for t, errs, n_o, n_g in records:
         for name, e in errs.items():
-            assert e <= STEP_TOL, (t, name, e)
-        assert_newton_per_stage(n_o, n_g, (t,))
-    with pytest.raises(dcgpu_lib.DcError):
-        dcgpu_lib.Model(ini, {"model.time_step_operator.linear_solver.matrix_free": "maybe"})
+            assert e <= STEP_TOL, (case, t, name, e)
+
+
+@pytest.mark.parametrize("solver", ["CG", "RestartedGMRes"])
+def test_matrix_free_other_krylov(dcgpu_lib, solver):
+    ini, init = ALL_CASES["heat" if solver == "CG" else "features_2d"]()
+    ov = dict(MF)
+    ov["model.time_step_operator.linear_solver.type"] = solver
+    records = _run_both(dcgpu_lib, ini, init, overrides=ov)
+    for t, errs, n_o, n_g in records:
+        for e in errs.values():
+            assert e <= STEP_TOL, (solver, t, e)
+
+
+def test_matrix_free_configuration(dcgpu_lib):
+    """Matrix-free takes what the reference's matrix-free registries hold: iterative solvers
+    and Richardson / InverseOperator; a direct solver, a matrix-based preconditioner or a
+    non-boolean value is a configuration error."""
+    ini, _init = ALL_CASES["features_2d"]()
+    L = "model.time_step_operator.linear_solver."
+    gm = dcgpu_lib.Model(ini, {L + "matrix_free": "true", L + "type": "BiCGSTAB"})
+    assert gm.precond_info()["type"] == "Richardson"
+    gm.close()
+    for bad in ({L + "matrix_free": "maybe"},
+                {L + "matrix_free": "true"},  # UMFPack: a direct solver needs the matrix
+                {L + "matrix_free": "true", L + "type": "BiCGSTAB", L + "preconditioner.type": "SSOR"},
+                {L + "matrix_free": "true", L + "type": "BiCGSTAB", L + "preconditioner.type": "AMG"}):
+        with pytest.raises(dcgpu_lib.DcError):
+            dcgpu_lib.Model(ini, bad)
 
 
 @pytest.mark.parametrize("precond", ["Jacobi", "AMG"])

@@ -266,6 +266,17 @@ __global__ void k_restrict_warp(int64_t ncoarse, const int32_t* __restrict__ agg
   }
 }
 
+// x = t + cs P xc (the coarse correction without post-smoothing)
+template <int B, class T>
+__global__ void k_prolong_to(int64_t nrows, const int32_t* __restrict__ agg, const T* __restrict__ xc,
+                             const T* __restrict__ t, T* __restrict__ x, T cs, const double* sc, int slot) {
+  if (skip(sc, slot)) return;
+  const int64_t n = nrows * B;
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t row = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; row < n; row += stride)
+    x[row] = t[row] + cs * xc[static_cast<int64_t>(agg[row / B]) * B + row % B];
+}
+
 // x += cs P xc
 template <int B, class T>
 __global__ void k_prolong(int64_t nrows, const int32_t* __restrict__ agg, const T* __restrict__ xc, T* __restrict__ x,
@@ -695,7 +706,9 @@ void Amg::cycle(int l, const T* r, T* x, const double* sc, int slot, cudaStream_
                                                                        c.own.agg_rows.get(), x, rc, sc, slot)));
   cycle<T>(l + 1, rc, xc, sc, slot, s);
   count_launches(1);
-  if (a.warp_rows)
+  if (l == 0 && !finest_post_smoothing)
+    DC_BS((k_prolong_to<B, T><<<blocks_for(n * bs_), kT, 0, s>>>(n, a.agg.get(), xc, t, x, cs, sc, slot)))
+  else if (a.warp_rows)
     DC_BS((k_rows_warp<B, T, 1><<<gw, kT, 0, s>>>(n, a.rowptr, a.colidx, A, S, a.agg.get(), xc, t, r, x, w, cs, sc,
                                                    slot)))
   else

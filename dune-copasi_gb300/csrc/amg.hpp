@@ -84,12 +84,15 @@ class Amg : public Preconditioner {
 
   // parameters (read before build)
   Smoother smoother = Smoother::Jacobi;
-  double omega = 0.8;        // smoother relaxation
+  double omega = 0.85;       // smoother relaxation
   int coarse_sweeps = 6;     // smoother sweeps on a coarsest level too large for the dense solve
   int max_levels = 10;
   int64_t coarsen_target = 0;  // stop coarsening at this many rows (0: the dense solve's limit)
   int mis_distance = 2;      // aggregation around a distance-1 or distance-2 independent set
   double correction = 1.0;   // scale of the coarse-grid correction x += correction * P xc
+  // (L1-)Jacobi smoothing: post-smoothing on the finest level too (false: V(1,0) there, one
+  // pass over the finest operator less per cycle)
+  bool finest_post_smoothing = true;
   int64_t warp_rows_below = kWarpRowsBelow;
 
  private:

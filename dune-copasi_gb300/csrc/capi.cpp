@@ -450,6 +450,7 @@ int dc_server_poll(dc_server* server, int32_t wait, dc_result* results, int32_t 
       o.linear_iterations = r.linear_iterations;
       o.steps = r.steps;
       o.bytes_estimate = r.bytes_estimate;
+      o.bytes_measured = r.bytes_measured;
       if (r.status != DC_OK && !r.error.empty()) g_last_error = r.error;
     }
     *n_out = static_cast<int32_t>(done.size());
@@ -622,12 +623,13 @@ int dc_selftest_precond(const char* kind, const char* params, int64_t nrows, int
       const int smi = static_cast<int>(param(prm, "smoother", 0));
       amg->smoother = smi == 0 ? dcgpu::Amg::Smoother::Jacobi
                                : smi == 1 ? dcgpu::Amg::Smoother::L1Jacobi : dcgpu::Amg::Smoother::GaussSeidel;
-      amg->omega = param(prm, "relaxation", smi == 0 ? 0.8 : 1.0);
+      amg->omega = param(prm, "relaxation", smi == 0 ? 0.85 : 1.0);
       amg->coarse_sweeps = static_cast<int>(param(prm, "coarse_sweeps", 6));
       amg->max_levels = static_cast<int>(param(prm, "max_level", 10));
       amg->coarsen_target = static_cast<int64_t>(param(prm, "coarsen_target", 0));
       amg->mis_distance = static_cast<int>(param(prm, "aggregation_distance", 2));
       amg->correction = param(prm, "coarse_correction", 1.0);
+      amg->finest_post_smoothing = param(prm, "finest_post_smoothing", 1.0) != 0.0;
       amg->warp_rows_below = static_cast<int64_t>(param(prm, "warp_rows_below", dcgpu::Amg::kWarpRowsBelow));
       amg->build(nrows, bs, nnzb, g.rowptr.get(), g.colidx.get(), ddiag.get(), group ? g.group.get() : nullptr, s);
       amg->setup(dval.get(), dinv.get(), fdinv.get(), fp32 != 0, status.get(), s);

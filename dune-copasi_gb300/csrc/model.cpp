@@ -11,6 +11,11 @@
 
 namespace dcgpu {
 
+int64_t& device_bytes_this_thread() {
+  static thread_local int64_t bytes = 0;
+  return bytes;
+}
+
 void cuda_check(cudaError_t e, const char* what) {
   if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
 }

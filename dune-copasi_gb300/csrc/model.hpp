@@ -35,6 +35,10 @@ class CudaError : public std::runtime_error {
 };
 void cuda_check(cudaError_t e, const char* what);
 
+// Device bytes held by the DeviceBuffers the calling host thread allocated (the request
+// server measures a simulation's footprint with it: each runs on its own thread)
+int64_t& device_bytes_this_thread();
+
 template <class T>
 class DeviceBuffer {
  public:
@@ -50,7 +54,10 @@ class DeviceBuffer {
   ~DeviceBuffer() { release(); }
   void resize(size_t n) {
     release();
-    if (n) cuda_check(cudaMalloc(&p_, n * sizeof(T)), "cudaMalloc");
+    if (n) {
+      cuda_check(cudaMalloc(&p_, n * sizeof(T)), "cudaMalloc");
+      device_bytes_this_thread() += static_cast<int64_t>(n * sizeof(T));
+    }
     n_ = n;
   }
   void upload(const std::vector<T>& h) {
@@ -67,7 +74,10 @@ class DeviceBuffer {
 
  private:
   void release() {
-    if (p_) cudaFree(p_);
+    if (p_) {
+      cudaFree(p_);
+      device_bytes_this_thread() -= static_cast<int64_t>(n_ * sizeof(T));
+    }
     p_ = nullptr;
     n_ = 0;
   }

@@ -124,6 +124,16 @@ void Server::worker() {
                             [&](const Request& r) { return in_use_ + r.bytes <= budget_; });
       };
       cv_work_.wait(lk, [&] { return stop_ || admissible() != queue_.end(); });
+      // the device itself must have the room too (other processes, allocator slack):
+      // admission waits, re-checking when a simulation finishes or shrinks its charge
+      if (!stop_ && admissible() != queue_.end()) {
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess &&
+            static_cast<int64_t>(free_b) < admissible()->bytes + kDeviceReserve && active_ > 0) {
+          cv_work_.wait_for(lk, std::chrono::milliseconds(5));
+          continue;
+        }
+      }
       auto it = admissible();
       if (it == queue_.end()) {
         if (stop_) return;
@@ -137,6 +147,16 @@ void Server::worker() {
     ServerResult res;
     res.id = req.id;
     res.bytes_estimate = req.bytes;
+    int64_t held = req.bytes;                          // bytes charged against the budget
+    const int64_t base = device_bytes_this_thread();   // this worker's buffers before the request
+    int64_t peak = 0;
+    auto measure = [&]() {
+      const int64_t m = device_bytes_this_thread() - base;
+      if (m > peak) {
+        peak = m;
+        recharge(held, peak);
+      }
+    };
     const double t_admit = now();
     res.queue_s = t_admit - req.submit_t;
     std::vector<double> state;
@@ -153,13 +173,15 @@ void Server::worker() {
       const std::string sl_key = "model.time_step_operator.linear_solver.single_launch";
       if (!model.cfg.has_key(sl_key)) model.cfg.set(sl_key, "false");
       Solver solver(model, stream);
+      measure();
       Ini tso = model.cfg.sub("model").sub("time_step_operator");
       const double t0 = tso.get_double("time_begin", 0.0);
       const double t1 = tso.get_double("time_end", 1.0);
       const double dt_max = tso.get_double("time_step_max", 0.1);
       double dt = tso.get_double("time_step_initial", tso.has_key("time_step_max") ? dt_max : 0.1);
       if (!req.init.empty()) solver.set_state(req.init, t0);
-      res.status = solver.evolve(t1, dt, nullptr);
+      // buffers made during the run (graphs' work vectors, a multigrid built on the way)
+      res.status = solver.evolve(t1, dt, [&](double) { measure(); });
       res.ndof = model.ndof;
       res.newton_iterations = solver.stats.newton_iterations;
       res.linear_iterations = solver.stats.linear_iterations;
@@ -183,9 +205,10 @@ void Server::worker() {
     const double t_end = now();
     res.run_s = t_end - t_admit;
     res.latency_s = t_end - req.submit_t;
+    res.bytes_measured = peak;
     {
       std::lock_guard<std::mutex> lk(mu_);
-      in_use_ -= req.bytes;
+      in_use_ -= held;
       --active_;
       states_[res.id] = std::move(state);
       done_.push_back(std::move(res));
@@ -193,6 +216,16 @@ void Server::worker() {
     cv_done_.notify_all();
     cv_work_.notify_all();
   }
+}
+
+void Server::recharge(int64_t& held, int64_t measured) {
+  {
+    std::lock_guard<std::mutex> lk(mu_);
+    in_use_ += measured - held;
+    held = measured;
+  }
+  // a smaller charge than the estimate may let a waiting request in
+  cv_work_.notify_all();
 }
 
 std::vector<ServerResult> Server::poll(bool wait, int max) {

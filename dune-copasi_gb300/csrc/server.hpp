@@ -32,6 +32,7 @@ struct ServerResult {
   int64_t linear_iterations = 0;
   int64_t steps = 0;
   int64_t bytes_estimate = 0;
+  int64_t bytes_measured = 0;  // peak device bytes the simulation's buffers held
   std::string error;
 };
 
@@ -51,6 +52,8 @@ class Server {
   int pending() ;
 
   static int64_t estimate_bytes(const std::string& ini, const std::string& overrides);
+  // device memory kept free beyond an admitted request's estimate
+  static constexpr int64_t kDeviceReserve = int64_t{256} << 20;
 
  private:
   struct Request {
@@ -61,6 +64,9 @@ class Server {
     int64_t bytes;
   };
   void worker();
+  // charge a running simulation its measured footprint instead of what it was admitted
+  // with (held: the bytes currently charged for it, updated)
+  void recharge(int64_t& held, int64_t measured);
   double now() const;
 
   std::mutex mu_;

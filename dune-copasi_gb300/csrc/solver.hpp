@@ -203,7 +203,9 @@ class Solver {
   // mixed precision: relative reduction asked of each fp32 correction, and the cap on
   // corrections per solve
   static constexpr double kMixedInnerReduction = 1e-4;
+  static constexpr double kMixedInnerReductionMultigrid = 1e-2;  // default with the multigrid
   double mixed_inner_ = kMixedInnerReduction;  // linear_solver.inner_reduction
+  bool inner_set_ = false;                     // the key was given
   static constexpr int kMixedMaxRefinements = 50;
   double direct_tol_ = 1e-10;
   int lin_max_it_ = 500;

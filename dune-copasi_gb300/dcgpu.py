@@ -71,7 +71,7 @@ class Result(ctypes.Structure):
                 ("queue_s", ctypes.c_double), ("run_s", ctypes.c_double), ("latency_s", ctypes.c_double),
                 ("n_dof", ctypes.c_int64), ("newton_iterations", ctypes.c_int64),
                 ("linear_iterations", ctypes.c_int64), ("steps", ctypes.c_int64),
-                ("bytes_estimate", ctypes.c_int64)]
+                ("bytes_estimate", ctypes.c_int64), ("bytes_measured", ctypes.c_int64)]
 
 
 CALLBACK = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p)

@@ -265,7 +265,9 @@ typedef struct dc_result {
   int64_t newton_iterations;
   int64_t linear_iterations;
   int64_t steps;
-  int64_t bytes_estimate;
+  int64_t bytes_estimate;  /* footprint estimated at submission (admission charge) */
+  int64_t bytes_measured;  /* peak device bytes the simulation's buffers held; the server
+                              charges a running simulation this instead of the estimate */
 } dc_result;
 
 int dc_server_create(int64_t budget_bytes, int32_t max_active, dc_server** out);

@@ -212,7 +212,8 @@ def amg_hierarchy(rowptr, colidx, vals, bs, group, aggregate, distance=2, coarse
     return levels
 
 
-def amg_apply(levels, bs, r, smoother="jacobi", omega=0.8, coarse_sweeps=6, colour=None, correction=1.0):
+def amg_apply(levels, bs, r, smoother="jacobi", omega=0.8, coarse_sweeps=6, colour=None, correction=1.0,
+              finest_post_smoothing=True):
     """One V(1,1) cycle z = M^-1 r with the coarse-grid correction scaled by `correction`.
     colour(rowptr, colidx) -> colours (Gauss-Seidel only: the engine's colouring of the
     level's graph)."""
@@ -285,6 +286,8 @@ def amg_apply(levels, bs, r, smoother="jacobi", omega=0.8, coarse_sweeps=6, colo
         t = omega * bdiag(S, rl)
         xc = cycle(l + 1, restrict(rl - matvec(rp, ci, v, t)))
         y = t + correction * prolong(xc)
+        if l == 0 and not finest_post_smoothing:
+            return y
         return y + omega * bdiag(S, rl - matvec(rp, ci, v, y))
 
     return cycle(0, np.asarray(r, dtype=np.float64))

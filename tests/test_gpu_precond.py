@@ -147,7 +147,8 @@ AMG_CASES = [("jacobi", 2, 1, ""), ("jacobi", 1, 2, ""), ("l1jacobi", 2, 3, ""),
              ("gauss_seidel", 1, 1, ""), ("jacobi", 2, 2, "max_level=2"), ("gauss_seidel", 2, 4, "coarsen_target=3"),
              ("jacobi", 2, 5, "coarse_correction=1.6;warp_rows_below=0"),
              ("l1jacobi", 1, 3, "coarse_correction=1.3;warp_rows_below=100000"),
-             ("gauss_seidel", 2, 2, "coarse_correction=1.5;warp_rows_below=200")]
+             ("gauss_seidel", 2, 2, "coarse_correction=1.5;warp_rows_below=200"),
+             ("jacobi", 2, 3, "finest_post_smoothing=0"), ("l1jacobi", 2, 2, "finest_post_smoothing=0;warp_rows_below=0")]
 SMOOTHER_ID = {"jacobi": 0, "l1jacobi": 1, "gauss_seidel": 2}
 
 
@@ -158,7 +159,7 @@ def test_multigrid_matches_restatement(dcgpu_lib, smoother, distance, bs, extra,
     rowptr, colidx, vals, group = grid_matrix(nx, ny, bs, 20 + bs)
     n = len(rowptr) - 1
     r = np.random.default_rng(5).standard_normal(n * bs)
-    omega = 0.8 if smoother == "jacobi" else 1.0
+    omega = 0.85 if smoother == "jacobi" else 1.0
     params = "smoother=%d;aggregation_distance=%d;%s" % (SMOOTHER_ID[smoother], distance, extra)
     z, info = dcgpu_lib.precond_apply("AMG", rowptr, colidx, vals, r, bs, params, group=group, fp32=fp32)
     kv = dict(kv.split("=") for kv in extra.split(";") if kv)
@@ -180,7 +181,8 @@ def test_multigrid_matches_restatement(dcgpu_lib, smoother, distance, bs, extra,
     if "max_level" in extra:
         assert info[1] == 0  # the coarsest level is above the dense limit: smoother sweeps
     want = P.amg_apply(levels, bs, r, smoother, omega, colour=colour,
-                       correction=float(kv.get("coarse_correction", 1.0)))
+                       correction=float(kv.get("coarse_correction", 1.0)),
+                       finest_post_smoothing=kv.get("finest_post_smoothing", "1") != "0")
     assert rel(z, want) <= (1e-4 if fp32 else 1e-11), (smoother, distance, bs, extra, rel(z, want))
 
 

@@ -85,7 +85,9 @@ def test_results_identical_alone_and_in_the_mix(dcgpu_lib):
 def test_admission_respects_budget(dcgpu_lib):
     ini, _ = cases.small_heat(n=32, steps=6)
     est = dcgpu_lib.estimate_bytes(ini)
-    srv = dcgpu_lib.Server(budget_bytes=int(1.5 * est), max_active=4)
+    # a budget of one estimate: a running simulation is charged its measured footprint
+    # (> 0), so the next one (charged its estimate at admission) never fits beside it
+    srv = dcgpu_lib.Server(budget_bytes=est, max_active=4)
     ids = [srv.submit(ini) for _ in range(3)]
     res = _drain(srv, 3)
     spans = []
@@ -97,6 +99,22 @@ def test_admission_respects_budget(dcgpu_lib):
     spans.sort()
     for (a0, a1), (b0, b1) in zip(spans, spans[1:]):
         assert b0 >= a1 - 1e-3
+    srv.close()
+
+
+@pytest.mark.gpu
+def test_measured_footprint_is_reported_and_within_the_estimate(dcgpu_lib):
+    """Every result carries the peak device bytes of the simulation's buffers, which the
+    server charges instead of the admission estimate; the estimate bounds it."""
+    srv = dcgpu_lib.Server(budget_bytes=8 << 30, max_active=3)
+    reqs = [cases.small_heat(n=24, steps=4)[0], cases.small_gray_scott(n=32, steps=3)[0],
+            cases.small_two_compartment(n=24, steps=3)[0]]
+    ids = [srv.submit(ini) for ini in reqs]
+    res = _drain(srv, len(ids))
+    for rid in ids:
+        r = res[rid]
+        assert r["status"] == 0
+        assert 0 < r["bytes_measured"] <= r["bytes_estimate"], r
     srv.close()
 
 

@@ -102,6 +102,10 @@ def parse():
                     help="skip the per-phase SpMV measurement on the headline operator")
     ap.add_argument("--no-secondary", action="store_true",
                     help="skip the Gray-Scott 512^2 and two-compartment 1024^2 measurements")
+    ap.add_argument("--serve-spec", action="store_true",
+                    help="serving requests drawn at their specified sizes (2D N 32..512, 3D N 16..64, 20-500 "
+                         "steps; mixed and FP64 both with the server's concurrency) instead of the reduced mix; "
+                         "--serve-requests of them (the specification's 512 take about a GPU-hour per precision)")
     ap.add_argument("--serve-active", type=int, default=16,
                     help="simulations the request server runs at once (each on its own stream)")
     ap.add_argument("--serve-requests", type=int, default=32,
@@ -283,11 +287,18 @@ def run_reference(args, rank, world):
 
 
 # ----------------------------------------------------------------------------- serving
-def run_serving(dcgpu, n_requests, lam, max_active, precision, seed=20261203, budget=64 << 30):
+SERVE_REDUCED = {"n2d": (32, 160), "n3d": (12, 32), "steps": (10, 40)}
+# the serving stream at the size its specification names: 2D N log-uniform 32..512, 3D
+# N log-uniform 16..64, 20-500 implicit-Euler steps (--serve-spec)
+SERVE_SPEC = {"n2d": (32, 512), "n3d": (16, 64), "steps": (20, 500)}
+
+
+def run_serving(dcgpu, n_requests, lam, max_active, precision, seed=20261203, budget=64 << 30, mix=None):
     """Poisson stream of random requests through the request server; returns latency
     percentiles and the aggregate DOF x Newton-step throughput."""
     import workloads as W
-    stream = W.serving_stream(n_requests, lam, seed, n2d=(32, 160), n3d=(12, 32), steps=(10, 40))
+    mix = mix or SERVE_REDUCED
+    stream = W.serving_stream(n_requests, lam, seed, n2d=mix["n2d"], n3d=mix["n3d"], steps=mix["steps"])
     ov = {"model.time_step_operator.linear_solver.precision": "mixed"} if precision == "mixed" else None
     srv = dcgpu.Server(budget, max_active)
     t0 = time.perf_counter()
@@ -314,7 +325,9 @@ def run_serving(dcgpu, n_requests, lam, max_active, precision, seed=20261203, bu
             "precision": precision, "p50_latency_s": float(np.percentile(lat, 50)),
             "p99_latency_s": float(np.percentile(lat, 99)), "wall_s": wall,
             "value": work / wall, "unit": METRIC,
-            "mix": "2D N log-U[32,160] / 3D N log-U[12,32], 1-2 compartments, 1-8 species, 10-40 IE steps"}
+            "bytes_measured_max": max((r.get("bytes_measured", 0) for r in done.values()), default=0),
+            "mix": "2D N log-U[%d,%d] / 3D N log-U[%d,%d], 1-2 compartments, 1-8 species, %d-%d IE steps"
+                   % (mix["n2d"] + mix["n3d"] + mix["steps"])}
 
 
 # ----------------------------------------------------------------------------- roofline
@@ -682,7 +695,12 @@ def main():
                 "two_compartment_1024": precond_comparison(dcgpu, "two_compartment",
                                                            ["Jacobi", "AMG", "SSOR", "ILU", "auto"], 2, 1, flush)}
     serving = None
-    if args.serve_requests > 0:
+    if args.serve_spec and args.serve_requests > 0:
+        served = run_serving(dcgpu, args.serve_requests, 50.0, args.serve_active, "mixed", mix=SERVE_SPEC)
+        plain = run_serving(dcgpu, args.serve_requests, 50.0, args.serve_active, "fp64", mix=SERVE_SPEC)
+        serving = {"spec": True, "served_concurrent": served, "plain_fp64_concurrent": plain,
+                   "speedup": served["value"] / plain["value"] if plain["value"] > 0 else None}
+    elif args.serve_requests > 0:
         served = run_serving(dcgpu, args.serve_requests, 50.0, args.serve_active, args.precision)
         alone = run_serving(dcgpu, args.serve_requests, 50.0, 1, "fp64")
         serving = {"served_concurrent": served, "plain_fp64_one_at_a_time": alone,

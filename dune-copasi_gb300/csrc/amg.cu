@@ -266,6 +266,14 @@ __global__ void k_restrict_warp(int64_t ncoarse, const int32_t* __restrict__ agg
   }
 }
 
+// x += w
+template <class T>
+__global__ void k_add(int64_t n, const T* __restrict__ w, T* __restrict__ x, const double* sc, int slot) {
+  if (skip(sc, slot)) return;
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) x[i] += w[i];
+}
+
 // x = t + cs P xc (the coarse correction without post-smoothing)
 template <int B, class T>
 __global__ void k_prolong_to(int64_t nrows, const int32_t* __restrict__ agg, const T* __restrict__ xc,
@@ -490,17 +498,19 @@ void Amg::build(int64_t nrows, int bs, int64_t nnzb, const int32_t* rowptr, cons
     L.warp_rows = smoothed && L.nrows < warp_rows_below;
     if (smoothed && !L.warp_rows) sell_structure(L.nrows, L.rowptr, L.colidx, &L.sell, s);
     if (smoothed && smoother == Smoother::L1Jacobi) L.sinv_o.resize(static_cast<size_t>(L.nrows) * b2);
-    if (smoothed && smoother == Smoother::GaussSeidel) {
+    if (smoothed && (smoother == Smoother::GaussSeidel || smoother == Smoother::Ilu0)) {
       L.gs = std::make_unique<ColorPrecond>();
-      L.gs->build(ColorPrecond::Kind::Sor, L.nrows, bs, L.nnzb, L.rowptr, L.colidx, L.diag, s);
-      L.gs->omega = omega;
+      L.gs->build(smoother == Smoother::Ilu0 ? ColorPrecond::Kind::Ilu0 : ColorPrecond::Kind::Sor, L.nrows, bs, L.nnzb,
+                  L.rowptr, L.colidx, L.diag, s);
+      L.gs->omega = smoother == Smoother::Ilu0 ? 1.0 : omega;
+      if (smoother == Smoother::Ilu0) L.w.resize(nv);
     }
   }
   cuda_check(cudaStreamSynchronize(s), "multigrid set-up");
 }
 
 std::string Amg::describe() const {
-  static const char* names[] = {"jacobi", "l1jacobi", "gauss_seidel"};
+  static const char* names[] = {"jacobi", "l1jacobi", "gauss_seidel", "ilu0"};
   std::string o = "{\"type\": \"AMG\", \"smoother\": \"" + std::string(names[static_cast<int>(smoother)]) +
                   "\", \"aggregation_distance\": " + std::to_string(mis_distance) + ", \"levels\": [";
   for (size_t l = 0; l < levels_.size(); ++l) {
@@ -592,6 +602,7 @@ void Amg::setup(const double* fine_vals, const double* fine_dinv, const float* f
         L.x32.resize(L.x.size());
         L.t32.resize(L.t.size());
         L.rc32.resize(L.rc.size());
+        L.w32.resize(L.w.size());
       }
   fp32_ = fp32;
   // smoothers
@@ -684,6 +695,21 @@ void Amg::cycle(int l, const T* r, T* x, const double* sc, int slot, cudaStream_
   T* u = t;  // residual scratch (Gauss-Seidel) / smoothed iterate (Jacobi)
   T* xc = pick<T>(c.x, c.x32);
   T* rc = pick<T>(c.rc, c.rc32);
+  if (smoother == Smoother::Ilu0) {
+    T* w = pick<T>(a.w, a.w32);
+    a.gs->apply(r, x, sc, slot, s);
+    count_launches(2);
+    residual(x, u);
+    DC_BS((k_restrict_warp<B, T><<<blocks_for(c.nrows * 32), kT, 0, s>>>(c.nrows, c.own.agg_ptr.get(),
+                                                                         c.own.agg_rows.get(), u, rc, sc, slot)));
+    cycle<T>(l + 1, rc, xc, sc, slot, s);
+    count_launches(3);
+    DC_BS((k_prolong<B, T><<<blocks_for(n * bs_), kT, 0, s>>>(n, a.agg.get(), xc, x, cs, sc, slot)));
+    residual(x, u);
+    a.gs->apply(u, w, sc, slot, s);
+    k_add<T><<<blocks_for(n * bs_), kT, 0, s>>>(n * bs_, w, x, sc, slot);
+    return;
+  }
   if (smoother == Smoother::GaussSeidel) {
     a.gs->template sor_sweep<T>(r, x, true, true, sc, slot, s);
     count_launches(2);

@@ -20,8 +20,9 @@
 // the level operators (sell.cuh) in the precision of the Krylov solve (fp32 in the
 // mixed-precision path).
 // Smoothers: damped block Jacobi, block L1-Jacobi (the diagonal block plus the absolute row
-// sums of the off-diagonal blocks on its diagonal), or multicolour block Gauss-Seidel
-// (forward sweep before the coarse correction, backward sweep after it: a symmetric cycle).
+// sums of the off-diagonal blocks on its diagonal), multicolour block Gauss-Seidel (forward
+// sweep before the coarse correction, backward sweep after it: a symmetric cycle), or
+// multicolour block ILU(0) (x = M^-1 r before, x += M^-1 (r - A x) after).
 #pragma once
 
 #include <cstdint>
@@ -41,7 +42,7 @@ namespace dcgpu {
 
 class Amg : public Preconditioner {
  public:
-  enum class Smoother { Jacobi, L1Jacobi, GaussSeidel };
+  enum class Smoother { Jacobi, L1Jacobi, GaussSeidel, Ilu0 };
   // largest coarsest level (unknowns) solved by the dense LU
   static constexpr int kDenseMax = 128;
   // levels with fewer rows use the warp-per-row kernels (default of warp_rows_below)
@@ -124,12 +125,12 @@ class Amg : public Preconditioner {
     // smoother inverses (L1-Jacobi: own; else the block-Jacobi inverses above)
     DeviceBuffer<double> sinv_o;
     DeviceBuffer<float> sinv32_o;
-    std::unique_ptr<ColorPrecond> gs;  // Gauss-Seidel smoother: colouring of this level
+    std::unique_ptr<ColorPrecond> gs;  // Gauss-Seidel / ILU(0) smoother of this level (multicolour)
     // aggregation to the next level (agg_ptr / agg_rows / gal_* live in the next level's own)
     DeviceBuffer<int32_t> agg;
     // work vectors: x the correction, t the smoothed iterate / residual, rc the right-hand side
-    DeviceBuffer<double> x, t, rc;
-    DeviceBuffer<float> x32, t32, rc32;
+    DeviceBuffer<double> x, t, rc, w;  // w: the ILU(0) smoother's correction
+    DeviceBuffer<float> x32, t32, rc32, w32;
   };
   template <class T>
   void cycle(int l, const T* r, T* x, const double* sc, int slot, cudaStream_t s) const;

@@ -621,8 +621,10 @@ int dc_selftest_precond(const char* kind, const char* params, int64_t nrows, int
     if (k == "AMG") {
       auto amg = std::make_unique<dcgpu::Amg>();
       const int smi = static_cast<int>(param(prm, "smoother", 0));
-      amg->smoother = smi == 0 ? dcgpu::Amg::Smoother::Jacobi
-                               : smi == 1 ? dcgpu::Amg::Smoother::L1Jacobi : dcgpu::Amg::Smoother::GaussSeidel;
+      amg->smoother = smi == 0   ? dcgpu::Amg::Smoother::Jacobi
+                      : smi == 1 ? dcgpu::Amg::Smoother::L1Jacobi
+                      : smi == 2 ? dcgpu::Amg::Smoother::GaussSeidel
+                                 : dcgpu::Amg::Smoother::Ilu0;
       amg->omega = param(prm, "relaxation", smi == 0 ? 0.85 : 1.0);
       amg->coarse_sweeps = static_cast<int>(param(prm, "coarse_sweeps", 6));
       amg->max_levels = static_cast<int>(param(prm, "max_level", 10));

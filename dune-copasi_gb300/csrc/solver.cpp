@@ -295,7 +295,8 @@ void Solver::configure_preconditioner(const Ini& ls) {
     if (sm == "jacobi") amg_->smoother = Amg::Smoother::Jacobi;
     else if (sm == "l1jacobi") amg_->smoother = Amg::Smoother::L1Jacobi;
     else if (sm == "gauss_seidel") amg_->smoother = Amg::Smoother::GaussSeidel;
-    else throw ConfigError("linear_solver.preconditioner.smoother must be jacobi, l1jacobi or gauss_seidel, not '" +
+    else if (sm == "ilu0") amg_->smoother = Amg::Smoother::Ilu0;
+    else throw ConfigError("linear_solver.preconditioner.smoother must be jacobi, l1jacobi, gauss_seidel or ilu0, not '" +
                            sm + "'");
     amg_->omega = ls.get_double("preconditioner.relaxation", sm == "jacobi" ? 0.85 : 1.0);
     amg_->coarse_sweeps = static_cast<int>(ls.get_long("preconditioner.coarse_sweeps", 6));

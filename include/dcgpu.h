@@ -209,7 +209,7 @@ int dc_selftest_fma_peaks(double* fp64_tflops, double* fp32_tflops);
  * agg_out[nrows], *naggregates.  dc_selftest_precond: builds preconditioner `kind` ("SSOR",
  * "SOR", "ILU", "DILU" or "AMG") for the BSR matrix (block size bs, row-major blocks in
  * vals, every row holding its diagonal block), with `params` "key=value;..." (relaxation,
- * iterations; AMG: smoother 0 Jacobi / 1 L1-Jacobi / 2 Gauss-Seidel, relaxation,
+ * iterations; AMG: smoother 0 Jacobi / 1 L1-Jacobi / 2 Gauss-Seidel / 3 ILU(0), relaxation,
  * coarse_sweeps, max_level, coarsen_target, aggregation_distance, coarse_correction,
  * warp_rows_below), applies it once to r
  * (in fp64, or in fp32 when fp32 != 0) and writes z (nrows * bs).  info (8 doubles, may be

@@ -24,7 +24,7 @@ The multigrid restatement (no reference counterpart; the engine's addition) foll
 dune-copasi_gb300/csrc/amg.hpp: aggregation per level (taken as input: the engine's own
 deterministic aggregation of the same graph), piecewise-constant prolongation, Galerkin
 coarse operators, a V(1,1) cycle with damped block Jacobi, L1-Jacobi or Gauss-Seidel
-smoothing, and a dense direct solve on a coarsest level of at most 128 unknowns.
+or ILU(0) smoothing, and a dense direct solve on a coarsest level of at most 128 unknowns.
 """
 
 import numpy as np
@@ -267,6 +267,12 @@ def amg_apply(levels, bs, r, smoother="jacobi", omega=0.8, coarse_sweeps=6, colo
         def prolong(xc):
             return xc.reshape(na, bs)[agg].reshape(-1)
 
+        if smoother == "ilu0":
+            order = color_order(colour(rp, ci))
+            x = ilu0_apply(rp, ci, v, bs, order, rl)
+            xc = cycle(l + 1, restrict(rl - matvec(rp, ci, v, x)))
+            x = x + correction * prolong(xc)
+            return x + ilu0_apply(rp, ci, v, bs, order, rl - matvec(rp, ci, v, x))
         if smoother == "gauss_seidel":
             order = color_order(colour(rp, ci))
             x = sor_apply(rp, ci, v, bs, order, rl, omega, 1, symmetric=False)

@@ -13,6 +13,17 @@ for p in (ROOT, PKG):
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
     config.addinivalue_line("markers", "slow: longer CPU-only test")
+    config.addinivalue_line("markers", "timeout(seconds): per-test limit (pytest-timeout, when installed)")
+
+
+def pytest_collection_modifyitems(config, items):
+    # a per-test limit on the GPU tests (when pytest-timeout is installed): a solve that stops
+    # converging fails its test instead of holding the whole suite
+    if not config.pluginmanager.hasplugin("timeout"):
+        return
+    for item in items:
+        if item.get_closest_marker("gpu") and not item.get_closest_marker("timeout"):
+            item.add_marker(pytest.mark.timeout(900))
 
 
 @pytest.fixture(scope="session")

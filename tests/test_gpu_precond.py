@@ -148,8 +148,9 @@ AMG_CASES = [("jacobi", 2, 1, ""), ("jacobi", 1, 2, ""), ("l1jacobi", 2, 3, ""),
              ("jacobi", 2, 5, "coarse_correction=1.6;warp_rows_below=0"),
              ("l1jacobi", 1, 3, "coarse_correction=1.3;warp_rows_below=100000"),
              ("gauss_seidel", 2, 2, "coarse_correction=1.5;warp_rows_below=200"),
-             ("jacobi", 2, 3, "finest_post_smoothing=0"), ("l1jacobi", 2, 2, "finest_post_smoothing=0;warp_rows_below=0")]
-SMOOTHER_ID = {"jacobi": 0, "l1jacobi": 1, "gauss_seidel": 2}
+             ("jacobi", 2, 3, "finest_post_smoothing=0"), ("l1jacobi", 2, 2, "finest_post_smoothing=0;warp_rows_below=0"),
+             ("ilu0", 2, 2, ""), ("ilu0", 1, 3, "warp_rows_below=0")]
+SMOOTHER_ID = {"jacobi": 0, "l1jacobi": 1, "gauss_seidel": 2, "ilu0": 3}
 
 
 @pytest.mark.parametrize("smoother,distance,bs,extra", AMG_CASES)
@@ -228,9 +229,11 @@ def test_registry_preconditioners_with_solvers(dcgpu_lib, precond, solver):
         _steps_match(dcgpu_lib, "gray_scott", ov, mixed=True)
 
 
-@pytest.mark.parametrize("smoother", ["jacobi", "l1jacobi", "gauss_seidel"])
+@pytest.mark.timeout(300)
+@pytest.mark.parametrize("smoother,mixed", [("jacobi", False), ("l1jacobi", False), ("gauss_seidel", False),
+                                            ("ilu0", False), ("jacobi", True), ("l1jacobi", True),
+                                            ("gauss_seidel", True)])
 @pytest.mark.parametrize("distance", ["1", "2"])
-@pytest.mark.parametrize("mixed", [False, True])
 def test_multigrid_smoothers_match_oracle(dcgpu_lib, smoother, distance, mixed):
     ov = {LS + "preconditioner.type": "AMG", LS + "preconditioner.smoother": smoother,
           LS + "preconditioner.aggregation_distance": distance}

@@ -440,8 +440,8 @@ class Model:
 
     def jacobian_apply(self, x, t, cm, ca, v):
         """Matrix-free product (cm dM/dx + ca dA/dx)(x, t) v, reference order (dc_jacobian_apply)."""
-        x = np.ascontiguousarray(x, dtype=np.float64)
-        v = np.ascontiguousarray(v, dtype=np.float64)
+        x = self._state_arg(x)
+        v = self._state_arg(v)
         y = np.zeros(self.ndof)
         P = ctypes.POINTER(ctypes.c_double)
         _check(self._lib.dc_jacobian_apply(self._h, x.ctypes.data_as(P), float(t), float(cm), float(ca),
@@ -559,8 +559,21 @@ def _f64(a):
     return a, a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
 
 
+def _check_csr(rowptr, colidx, group=None):
+    """The C entry points read rowptr[n] column indices and n group entries and take no
+    lengths: check them here."""
+    rowptr = np.asarray(rowptr)
+    if rowptr.ndim != 1 or rowptr.size < 2:
+        raise ValueError("rowptr must hold n + 1 >= 2 offsets")
+    if len(colidx) != int(rowptr[-1]):
+        raise ValueError("colidx must hold rowptr[-1] = %d entries, got %d" % (int(rowptr[-1]), len(colidx)))
+    if group is not None and len(group) != rowptr.size - 1:
+        raise ValueError("group must hold one entry per row")
+
+
 def color_graph(rowptr, colidx):
     """(colour per row, number of colours) of the multicolour preconditioners' colouring."""
+    _check_csr(rowptr, colidx)
     lib = load_library()
     n = len(rowptr) - 1
     rp, prp = _i32(rowptr)
@@ -573,6 +586,7 @@ def color_graph(rowptr, colidx):
 
 def aggregate_graph(rowptr, colidx, group=None, distance=2):
     """(aggregate per row, number of aggregates) of one multigrid coarsening."""
+    _check_csr(rowptr, colidx, group)
     lib = load_library()
     n = len(rowptr) - 1
     rp, prp = _i32(rowptr)
@@ -591,8 +605,11 @@ def aggregate_graph(rowptr, colidx, group=None, distance=2):
 def precond_apply(kind, rowptr, colidx, vals, r, bs, params="", group=None, fp32=False):
     """z = M^-1 r for preconditioner `kind` built on the BSR matrix (vals: nnzb x bs x bs);
     returns (z, info) with info as dc_selftest_precond describes."""
-    lib = load_library()
+    _check_csr(rowptr, colidx, group)
     n = len(rowptr) - 1
+    if np.asarray(vals).size != len(colidx) * bs * bs or np.asarray(r).size != n * bs:
+        raise ValueError("vals must hold nnzb * bs * bs values and r n * bs values")
+    lib = load_library()
     rp, prp = _i32(rowptr)
     ci, pci = _i32(colidx)
     v, pv = _f64(np.asarray(vals).reshape(-1))

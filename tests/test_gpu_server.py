@@ -107,7 +107,8 @@ def test_measured_footprint_is_reported_and_within_the_estimate(dcgpu_lib):
     """Every result carries the peak device bytes of the simulation's buffers, which the
     server charges instead of the admission estimate; the estimate bounds it."""
     srv = dcgpu_lib.Server(budget_bytes=8 << 30, max_active=3)
-    reqs = [cases.small_heat(n=24, steps=4)[0], cases.small_gray_scott(n=32, steps=3)[0],
+    # configurations whose own initial state is a proper start (no seeded perturbation)
+    reqs = [cases.small_heat(n=24, steps=4)[0], cases.small_3d(n=5, steps=2)[0],
             cases.small_two_compartment(n=24, steps=3)[0]]
     ids = [srv.submit(ini) for ini in reqs]
     res = _drain(srv, len(ids))

@@ -18,12 +18,13 @@ def pytest_configure(config):
 
 def pytest_collection_modifyitems(config, items):
     # a per-test limit on the GPU tests (when pytest-timeout is installed): a solve that stops
-    # converging fails its test instead of holding the whole suite
+    # converging ends the run instead of holding it (the thread method also ends a test that
+    # waits inside the library, where no signal reaches the interpreter)
     if not config.pluginmanager.hasplugin("timeout"):
         return
     for item in items:
         if item.get_closest_marker("gpu") and not item.get_closest_marker("timeout"):
-            item.add_marker(pytest.mark.timeout(900))
+            item.add_marker(pytest.mark.timeout(900, method="thread"))
 
 
 @pytest.fixture(scope="session")

@@ -229,7 +229,7 @@ def test_registry_preconditioners_with_solvers(dcgpu_lib, precond, solver):
         _steps_match(dcgpu_lib, "gray_scott", ov, mixed=True)
 
 
-@pytest.mark.timeout(300)
+@pytest.mark.timeout(300, method="thread")
 @pytest.mark.parametrize("smoother,mixed", [("jacobi", False), ("l1jacobi", False), ("gauss_seidel", False),
                                             ("ilu0", False), ("jacobi", True), ("l1jacobi", True),
                                             ("gauss_seidel", True)])

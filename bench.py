@@ -702,8 +702,12 @@ def main():
                    "speedup": served["value"] / plain["value"] if plain["value"] > 0 else None}
     elif args.serve_requests > 0:
         served = run_serving(dcgpu, args.serve_requests, 50.0, args.serve_active, args.precision)
+        plain = run_serving(dcgpu, args.serve_requests, 50.0, args.serve_active, "fp64")
         alone = run_serving(dcgpu, args.serve_requests, 50.0, 1, "fp64")
-        serving = {"served_concurrent": served, "plain_fp64_one_at_a_time": alone,
+        serving = {"served_concurrent": served, "plain_fp64_concurrent": plain, "plain_fp64_one_at_a_time": alone,
+                   # mixed against FP64 at the same concurrency (the precision's effect alone),
+                   # and against FP64 one simulation at a time (precision and concurrency)
+                   "speedup_mixed_vs_fp64_concurrent": served["value"] / plain["value"] if plain["value"] > 0 else None,
                    "speedup": served["value"] / alone["value"] if alone["value"] > 0 else None}
     # `config` names the workload only (the reference arm prints the same dict); how this
     # arm ran it is under "run"

@@ -477,9 +477,15 @@ void Amg::build(int64_t nrows, int bs, int64_t nnzb, const int32_t* rowptr, cons
     dinvd_.resize(n2);
     dinvf_.resize(n2);
     dense_piv_.resize(static_cast<size_t>(dense_n_));
-    const size_t smem = n2 * sizeof(double);
-    cuda_check(cudaFuncSetAttribute(k_dense_lu, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)),
-               "multigrid dense solve");
+    // the attribute is the kernel's, shared by every multigrid of the process: set once to
+    // the largest dense level, so no instance lowers it under another's launch
+    static const bool attr_set = [] {
+      cuda_check(cudaFuncSetAttribute(k_dense_lu, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      static_cast<int>(sizeof(double) * kDenseMax * kDenseMax)),
+                 "multigrid dense solve");
+      return true;
+    }();
+    (void)attr_set;
   }
   const size_t b2 = static_cast<size_t>(bs) * bs;
   for (size_t l = 0; l < levels_.size(); ++l) {
@@ -731,6 +737,16 @@ void Amg::cycle(int l, const T* r, T* x, const double* sc, int slot, cudaStream_
   DC_BS((k_restrict_warp<B, T><<<blocks_for(c.nrows * 32), kT, 0, s>>>(c.nrows, c.own.agg_ptr.get(),
                                                                        c.own.agg_rows.get(), x, rc, sc, slot)));
   cycle<T>(l + 1, rc, xc, sc, slot, s);
+  if (l < w_levels) {
+    // a second coarse-grid correction (W-cycle on this level): t += cs P xc, then the
+    // restricted residual of t and another coarse solve
+    count_launches(2);
+    DC_BS((k_prolong<B, T><<<blocks_for(n * bs_), kT, 0, s>>>(n, a.agg.get(), xc, t, cs, sc, slot)));
+    residual(t, x);
+    DC_BS((k_restrict_warp<B, T><<<blocks_for(c.nrows * 32), kT, 0, s>>>(c.nrows, c.own.agg_ptr.get(),
+                                                                         c.own.agg_rows.get(), x, rc, sc, slot)));
+    cycle<T>(l + 1, rc, xc, sc, slot, s);
+  }
   count_launches(1);
   if (l == 0 && !finest_post_smoothing)
     DC_BS((k_prolong_to<B, T><<<blocks_for(n * bs_), kT, 0, s>>>(n, a.agg.get(), xc, t, x, cs, sc, slot)))

@@ -94,6 +94,9 @@ class Amg : public Preconditioner {
   // (L1-)Jacobi smoothing: post-smoothing on the finest level too (false: V(1,0) there, one
   // pass over the finest operator less per cycle)
   bool finest_post_smoothing = true;
+  // (L1-)Jacobi smoothing: the top w_levels levels take two coarse-grid corrections per visit
+  // (a W-cycle there; 0: V-cycle)
+  int w_levels = 0;
   int64_t warp_rows_below = kWarpRowsBelow;
 
  private:

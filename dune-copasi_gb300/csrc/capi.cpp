@@ -632,6 +632,7 @@ int dc_selftest_precond(const char* kind, const char* params, int64_t nrows, int
       amg->mis_distance = static_cast<int>(param(prm, "aggregation_distance", 2));
       amg->correction = param(prm, "coarse_correction", 1.0);
       amg->finest_post_smoothing = param(prm, "finest_post_smoothing", 1.0) != 0.0;
+      amg->w_levels = static_cast<int>(param(prm, "w_levels", 0));
       amg->warp_rows_below = static_cast<int64_t>(param(prm, "warp_rows_below", dcgpu::Amg::kWarpRowsBelow));
       amg->build(nrows, bs, nnzb, g.rowptr.get(), g.colidx.get(), ddiag.get(), group ? g.group.get() : nullptr, s);
       amg->setup(dval.get(), dinv.get(), fdinv.get(), fp32 != 0, status.get(), s);

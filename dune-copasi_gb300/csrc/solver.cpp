@@ -305,6 +305,9 @@ void Solver::configure_preconditioner(const Ini& ls) {
     amg_->mis_distance = static_cast<int>(ls.get_long("preconditioner.aggregation_distance", 2));
     amg_->correction = ls.get_double("preconditioner.coarse_correction", 1.0);
     amg_->finest_post_smoothing = ls.get_bool("preconditioner.finest_post_smoothing", true);
+    amg_->w_levels = static_cast<int>(ls.get_long("preconditioner.w_levels", 0));
+    if (amg_->w_levels < 0 || amg_->w_levels > 3)
+      throw ConfigError("linear_solver.preconditioner.w_levels must be in [0, 3]");
     amg_->warp_rows_below = ls.get_long("preconditioner.warp_rows_below", Amg::kWarpRowsBelow);
     if (!(amg_->correction > 0.0 && amg_->correction < 4.0))
       throw ConfigError("linear_solver.preconditioner.coarse_correction must be in (0, 4)");

@@ -211,7 +211,7 @@ int dc_selftest_fma_peaks(double* fp64_tflops, double* fp32_tflops);
  * vals, every row holding its diagonal block), with `params` "key=value;..." (relaxation,
  * iterations; AMG: smoother 0 Jacobi / 1 L1-Jacobi / 2 Gauss-Seidel / 3 ILU(0), relaxation,
  * coarse_sweeps, max_level, coarsen_target, aggregation_distance, coarse_correction,
- * warp_rows_below), applies it once to r
+ * warp_rows_below, finest_post_smoothing, w_levels), applies it once to r
  * (in fp64, or in fp32 when fp32 != 0) and writes z (nrows * bs).  info (8 doubles, may be
  * NULL): colours, or for AMG the levels, the dense coarse solve's unknowns (0: none) and
  * the rows of levels 0 to 5. */

@@ -213,7 +213,7 @@ def amg_hierarchy(rowptr, colidx, vals, bs, group, aggregate, distance=2, coarse
 
 
 def amg_apply(levels, bs, r, smoother="jacobi", omega=0.8, coarse_sweeps=6, colour=None, correction=1.0,
-              finest_post_smoothing=True):
+              finest_post_smoothing=True, w_levels=0):
     """One V(1,1) cycle z = M^-1 r with the coarse-grid correction scaled by `correction`.
     colour(rowptr, colidx) -> colours (Gauss-Seidel only: the engine's colouring of the
     level's graph)."""
@@ -291,6 +291,9 @@ def amg_apply(levels, bs, r, smoother="jacobi", omega=0.8, coarse_sweeps=6, colo
         S = smoother_inverse(rp, ci, v)
         t = omega * bdiag(S, rl)
         xc = cycle(l + 1, restrict(rl - matvec(rp, ci, v, t)))
+        if l < w_levels:  # W-cycle on this level: a second coarse-grid correction
+            t = t + correction * prolong(xc)
+            xc = cycle(l + 1, restrict(rl - matvec(rp, ci, v, t)))
         y = t + correction * prolong(xc)
         if l == 0 and not finest_post_smoothing:
             return y

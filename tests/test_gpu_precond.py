@@ -149,7 +149,8 @@ AMG_CASES = [("jacobi", 2, 1, ""), ("jacobi", 1, 2, ""), ("l1jacobi", 2, 3, ""),
              ("l1jacobi", 1, 3, "coarse_correction=1.3;warp_rows_below=100000"),
              ("gauss_seidel", 2, 2, "coarse_correction=1.5;warp_rows_below=200"),
              ("jacobi", 2, 3, "finest_post_smoothing=0"), ("l1jacobi", 2, 2, "finest_post_smoothing=0;warp_rows_below=0"),
-             ("ilu0", 2, 2, ""), ("ilu0", 1, 3, "warp_rows_below=0")]
+             ("ilu0", 2, 2, ""), ("ilu0", 1, 3, "warp_rows_below=0"),
+             ("jacobi", 2, 3, "w_levels=1"), ("l1jacobi", 1, 2, "w_levels=2;warp_rows_below=0")]
 SMOOTHER_ID = {"jacobi": 0, "l1jacobi": 1, "gauss_seidel": 2, "ilu0": 3}
 
 
@@ -183,7 +184,8 @@ def test_multigrid_matches_restatement(dcgpu_lib, smoother, distance, bs, extra,
         assert info[1] == 0  # the coarsest level is above the dense limit: smoother sweeps
     want = P.amg_apply(levels, bs, r, smoother, omega, colour=colour,
                        correction=float(kv.get("coarse_correction", 1.0)),
-                       finest_post_smoothing=kv.get("finest_post_smoothing", "1") != "0")
+                       finest_post_smoothing=kv.get("finest_post_smoothing", "1") != "0",
+                       w_levels=int(kv.get("w_levels", 0)))
     assert rel(z, want) <= (1e-4 if fp32 else 1e-11), (smoother, distance, bs, extra, rel(z, want))
 
 

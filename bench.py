@@ -293,14 +293,16 @@ SERVE_REDUCED = {"n2d": (32, 160), "n3d": (12, 32), "steps": (10, 40)}
 SERVE_SPEC = {"n2d": (32, 512), "n3d": (16, 64), "steps": (20, 500)}
 
 
-def run_serving(dcgpu, n_requests, lam, max_active, precision, seed=20261203, budget=64 << 30, mix=None):
+def run_serving(dcgpu, n_requests, lam, max_active, precision, seed=20261203, budget=64 << 30, mix=None,
+                batch=False):
     """Poisson stream of random requests through the request server; returns latency
-    percentiles and the aggregate DOF x Newton-step throughput."""
+    percentiles and the aggregate DOF x Newton-step throughput.  batch: the server packs
+    the running simulations' Krylov solves into one continuously batched solve."""
     import workloads as W
     mix = mix or SERVE_REDUCED
     stream = W.serving_stream(n_requests, lam, seed, n2d=mix["n2d"], n3d=mix["n3d"], steps=mix["steps"])
     ov = {"model.time_step_operator.linear_solver.precision": "mixed"} if precision == "mixed" else None
-    srv = dcgpu.Server(budget, max_active)
+    srv = dcgpu.Server(budget, max_active, batch_krylov=batch)
     t0 = time.perf_counter()
     done = {}
     for arrival, ini in stream:
@@ -316,13 +318,15 @@ def run_serving(dcgpu, n_requests, lam, max_active, precision, seed=20261203, bu
         for r in srv.poll(wait=True):
             done[r["request_id"]] = r
     wall = time.perf_counter() - t0
+    bstats = srv.batch_stats() if batch else None
     srv.close()
     lat = sorted(r["latency_s"] for r in done.values())
     ok = sum(1 for r in done.values() if r["status"] == 0)
     work = sum(r["n_dof"] * r["newton_iterations"] for r in done.values())
     import numpy as np
     return {"requests": len(stream), "ok": ok, "lambda_per_s": lam, "max_active": max_active,
-            "precision": precision, "p50_latency_s": float(np.percentile(lat, 50)),
+            "precision": precision, "krylov_batched": batch, "batch_stats": bstats,
+            "p50_latency_s": float(np.percentile(lat, 50)),
             "p99_latency_s": float(np.percentile(lat, 99)), "wall_s": wall,
             "value": work / wall, "unit": METRIC,
             "bytes_measured_max": max((r.get("bytes_measured", 0) for r in done.values()), default=0),
@@ -695,20 +699,25 @@ def main():
                 "two_compartment_1024": precond_comparison(dcgpu, "two_compartment",
                                                            ["Jacobi", "AMG", "SSOR", "ILU", "auto"], 2, 1, flush)}
     serving = None
-    if args.serve_spec and args.serve_requests > 0:
-        served = run_serving(dcgpu, args.serve_requests, 50.0, args.serve_active, "mixed", mix=SERVE_SPEC)
-        plain = run_serving(dcgpu, args.serve_requests, 50.0, args.serve_active, "fp64", mix=SERVE_SPEC)
-        serving = {"spec": True, "served_concurrent": served, "plain_fp64_concurrent": plain,
-                   "speedup": served["value"] / plain["value"] if plain["value"] > 0 else None}
-    elif args.serve_requests > 0:
-        served = run_serving(dcgpu, args.serve_requests, 50.0, args.serve_active, args.precision)
-        plain = run_serving(dcgpu, args.serve_requests, 50.0, args.serve_active, "fp64")
-        alone = run_serving(dcgpu, args.serve_requests, 50.0, 1, "fp64")
-        serving = {"served_concurrent": served, "plain_fp64_concurrent": plain, "plain_fp64_one_at_a_time": alone,
-                   # mixed against FP64 at the same concurrency (the precision's effect alone),
-                   # and against FP64 one simulation at a time (precision and concurrency)
-                   "speedup_mixed_vs_fp64_concurrent": served["value"] / plain["value"] if plain["value"] > 0 else None,
-                   "speedup": served["value"] / alone["value"] if alone["value"] > 0 else None}
+    if args.serve_requests > 0:
+        # the same seeded stream each time: batched mixed (the served path), batched FP64,
+        # the unbatched server (every simulation replays its own Krylov graphs on its own
+        # stream) in mixed precision, and FP64 one simulation at a time
+        mix = SERVE_SPEC if args.serve_spec else None
+        ratio = lambda a, b: a["value"] / b["value"] if b["value"] > 0 else None  # noqa: E731
+        batched = run_serving(dcgpu, args.serve_requests, 50.0, args.serve_active, "mixed", mix=mix, batch=True)
+        batched64 = run_serving(dcgpu, args.serve_requests, 50.0, args.serve_active, "fp64", mix=mix, batch=True)
+        unbatched = run_serving(dcgpu, args.serve_requests, 50.0, args.serve_active, "mixed", mix=mix)
+        serving = {"spec": bool(args.serve_spec), "served_batched_mixed": batched, "batched_fp64": batched64,
+                   "unbatched_mixed": unbatched,
+                   # the precision's effect at the same batching, and the batching's at the same
+                   # precision
+                   "speedup_mixed_vs_fp64_batched": ratio(batched, batched64),
+                   "speedup_batched_vs_unbatched_mixed": ratio(batched, unbatched)}
+        if not args.serve_spec:
+            alone = run_serving(dcgpu, args.serve_requests, 50.0, 1, "fp64")
+            serving["plain_fp64_one_at_a_time"] = alone
+            serving["speedup"] = ratio(batched, alone)
     # `config` names the workload only (the reference arm prints the same dict); how this
     # arm ran it is under "run"
     config = workload_desc(args.workload, args.n)

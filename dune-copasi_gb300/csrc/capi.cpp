@@ -411,12 +411,31 @@ int dc_expr_eval(const char* expression, const char* context_ini, const char* co
 }
 
 int dc_server_create(int64_t budget_bytes, int32_t max_active, dc_server** out) {
+  return dc_server_create_ex(budget_bytes, max_active, 0, out);
+}
+
+int dc_server_create_ex(int64_t budget_bytes, int32_t max_active, int32_t flags, dc_server** out) {
   return guarded([&] {
     if (!out) throw std::invalid_argument("null argument");
     *out = nullptr;
+    if (flags & ~DC_SERVER_BATCH_KRYLOV) throw std::invalid_argument("unknown server flags");
     auto s = std::make_unique<dc_server>();
-    s->server = std::make_unique<dcgpu::Server>(budget_bytes, max_active);
+    s->server = std::make_unique<dcgpu::Server>(budget_bytes, max_active, (flags & DC_SERVER_BATCH_KRYLOV) != 0);
     *out = s.release();
+    return DC_OK;
+  });
+}
+
+int dc_server_batch_stats(const dc_server* server, dc_batch_stats* out) {
+  return guarded([&] {
+    if (!server || !out) throw std::invalid_argument("null argument");
+    const dcgpu::BatchStats b = server->server->batch_stats();
+    out->solves = b.solves;
+    out->replays = b.replays;
+    out->slot_replays = b.slot_replays;
+    out->iterations = b.iterations;
+    out->max_active = b.max_active;
+    out->reserved = 0;
     return DC_OK;
   });
 }

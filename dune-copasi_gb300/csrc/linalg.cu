@@ -288,9 +288,9 @@ namespace {
 // one thread per (slice, lane): copies the lane's blocks into its SELL slots as fp32 and
 // zero-fills the slots past the end of its row; the 32 lanes of a slice write each slot
 // entry as one contiguous 128-byte line
-template <int B>
+template <int B, class O>
 __global__ void __launch_bounds__(256) k_bsr_to_sell(Sell S, const int32_t* __restrict__ rowptr,
-                                                     const double* __restrict__ val, float* __restrict__ out) {
+                                                     const double* __restrict__ val, O* __restrict__ out) {
   const int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (t >= S.nslices * 32) return;
   const int64_t sl = t >> 5;
@@ -303,10 +303,10 @@ __global__ void __launch_bounds__(256) k_bsr_to_sell(Sell S, const int32_t* __re
     len = rowptr[t + 1] - k0;
   }
   for (int k = 0; k < w; ++k) {
-    float* dst = out + (o0 + k) * 32 * (B * B) + lane;
+    O* dst = out + (o0 + k) * 32 * (B * B) + lane;
     const double* src = val + static_cast<int64_t>(k0 + k) * (B * B);
 #pragma unroll
-    for (int e = 0; e < B * B; ++e) dst[e * 32] = k < len ? static_cast<float>(src[e]) : 0.0f;
+    for (int e = 0; e < B * B; ++e) dst[e * 32] = k < len ? static_cast<O>(src[e]) : O(0);
   }
 }
 
@@ -326,18 +326,26 @@ __global__ void __launch_bounds__(256) k_sell_spmv(Sell S, const float* __restri
 
 }  // namespace
 
-void bsr_to_sell(const Bsr& A, const double* val, const Sell& S, float* out, cudaStream_t s) {
+template <class O>
+void bsr_to_sell_t(const Bsr& A, const double* val, const Sell& S, O* out, cudaStream_t s) {
   if (S.nslices == 0) return;
   const int threads = 256;
   const int blocks = static_cast<int>((S.nslices * 32 + threads - 1) / threads);
   count_launches(1);
 #define DC_B2S(B) \
-  case B: k_bsr_to_sell<B><<<blocks, threads, 0, s>>>(S, A.rowptr, val, out); return;
+  case B: k_bsr_to_sell<B, O><<<blocks, threads, 0, s>>>(S, A.rowptr, val, out); return;
   switch (S.bs) {
     DC_B2S(1) DC_B2S(2) DC_B2S(3) DC_B2S(4) DC_B2S(5) DC_B2S(6) DC_B2S(7) DC_B2S(8)
     default: throw std::runtime_error("sell: block size unsupported");
   }
 #undef DC_B2S
+}
+
+void bsr_to_sell(const Bsr& A, const double* val, const Sell& S, float* out, cudaStream_t s) {
+  bsr_to_sell_t<float>(A, val, S, out, s);
+}
+void bsr_to_sell64(const Bsr& A, const double* val, const Sell& S, double* out, cudaStream_t s) {
+  bsr_to_sell_t<double>(A, val, S, out, s);
 }
 
 void spmv_sell32(const Sell& S, const float* val, const float* x, float* y, cudaStream_t s) {

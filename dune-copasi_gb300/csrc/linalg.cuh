@@ -40,6 +40,8 @@ void spmv32(const Bsr& A, const float* x, float* y, cudaStream_t s);
 void spmv32_vals(const Bsr& A, const float* val, const float* x, float* y, cudaStream_t s);
 // fp32 SELL-32 copy of the fp64 BSR values `val` (pattern of A, layout S); padding zeroed
 void bsr_to_sell(const Bsr& A, const double* val, const Sell& S, float* out, cudaStream_t s);
+// the same copy in fp64 (the batched fp64 Krylov solve reads the operator in this layout)
+void bsr_to_sell64(const Bsr& A, const double* val, const Sell& S, double* out, cudaStream_t s);
 // y = A x on the SELL-32 layout (warp per slice, lane per block row)
 void spmv_sell32(const Sell& S, const float* val, const float* x, float* y, cudaStream_t s);
 // r = b - A x (fp64)

@@ -11,10 +11,11 @@
 
 namespace dcgpu {
 
-Server::Server(int64_t budget_bytes, int max_active) : budget_(budget_bytes) {
+Server::Server(int64_t budget_bytes, int max_active, bool batch_krylov) : budget_(budget_bytes) {
   if (budget_bytes <= 0) throw std::invalid_argument("memory budget must be positive");
   if (max_active <= 0 || max_active > 256) throw std::invalid_argument("max_active must be in [1, 256]");
   cuda_check(cudaGetDevice(&device_), "cudaGetDevice");
+  if (batch_krylov) batcher_ = std::make_unique<KrylovBatcher>(device_, max_active);
   for (int i = 0; i < max_active; ++i) workers_.emplace_back([this] { worker(); });
 }
 
@@ -172,7 +173,11 @@ void Server::worker() {
       // not depend on what else runs.
       const std::string sl_key = "model.time_step_operator.linear_solver.single_launch";
       if (!model.cfg.has_key(sl_key)) model.cfg.set(sl_key, "false");
+      // the batch reads the fp32 operator in the SELL-32 layout: no per-model layout tuning
+      const std::string spmv_key = "model.time_step_operator.linear_solver.spmv";
+      if (batcher_ && !model.cfg.has_key(spmv_key)) model.cfg.set(spmv_key, "sell");
       Solver solver(model, stream);
+      if (batcher_) solver.attach_batcher(batcher_.get());
       measure();
       Ini tso = model.cfg.sub("model").sub("time_step_operator");
       const double t0 = tso.get_double("time_begin", 0.0);
@@ -217,6 +222,8 @@ void Server::worker() {
     cv_work_.notify_all();
   }
 }
+
+BatchStats Server::batch_stats() const { return batcher_ ? batcher_->stats() : BatchStats{}; }
 
 void Server::recharge(int64_t& held, int64_t measured) {
   {

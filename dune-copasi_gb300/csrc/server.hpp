@@ -14,10 +14,13 @@
 #include <cstdint>
 #include <deque>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <thread>
 #include <vector>
+
+#include "batch.hpp"
 
 namespace dcgpu {
 
@@ -38,7 +41,10 @@ struct ServerResult {
 
 class Server {
  public:
-  Server(int64_t budget_bytes, int max_active);
+  // batch_krylov: the running simulations' block-Jacobi BiCGSTAB solves are packed into
+  // one batch (KrylovBatcher, one slot per active simulation) instead of each replaying
+  // its own graphs on its own stream
+  Server(int64_t budget_bytes, int max_active, bool batch_krylov = false);
   ~Server();
   Server(const Server&) = delete;
   Server& operator=(const Server&) = delete;
@@ -50,6 +56,8 @@ class Server {
   // final state of a completed request (reference DOF order); erases it
   bool take_state(int64_t id, std::vector<double>& out);
   int pending() ;
+  // counters of the Krylov batch (all zero without batch_krylov)
+  BatchStats batch_stats() const;
 
   static int64_t estimate_bytes(const std::string& ini, const std::string& overrides);
   // device memory kept free beyond an admitted request's estimate
@@ -77,6 +85,7 @@ class Server {
   int64_t budget_, in_use_ = 0, next_id_ = 1;
   int active_ = 0;
   bool stop_ = false;
+  std::unique_ptr<KrylovBatcher> batcher_;  // destroyed after the workers have joined
   std::vector<std::thread> workers_;
   int device_ = 0;
 };

@@ -1,5 +1,7 @@
 #include "solver.hpp"
 
+#include "batch.hpp"
+
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
@@ -824,6 +826,10 @@ bool Solver::krylov_fused(double rel, int max_it, int* iters, int* status, const
 // fr_) holds the right-hand side on entry; the solution is left in the Krylov x vector.
 int Solver::krylov_run(bool fp32, double rel, int max_it, int* iters) {
   if (krylov_gmres_) return fp32 ? gmres_t<float>(rel, max_it, iters) : gmres_t<double>(rel, max_it, iters);
+  if (batch_) {
+    int st = DC_OK;
+    if (batch_solve(fp32, rel, max_it, iters, &st)) return st;
+  }
   if (fused_ && !krylov_cg_ && !pc_) {
     int st = DC_OK;
     if (fp32 ? krylov_fused<float>(rel, max_it, iters, &st) : krylov_fused<double>(rel, max_it, iters, &st))
@@ -875,6 +881,43 @@ int Solver::krylov_run(bool fp32, double rel, int max_it, int* iters) {
   return DC_ERR_DIVERGED;
 }
 
+// BiCGSTAB + block Jacobi in the batch shared with the other simulations of a server: the
+// right-hand side in kr_ / fr_, the solution left in kx_ / fx_, as krylov_run.  The fp64
+// operator is copied into the SELL-32 layout first (the batch reads that layout only).
+bool Solver::batch_solve(bool fp32, double rel, int max_it, int* iters, int* status) {
+  if (krylov_cg_ || krylov_gmres_ || pc_ || model.bs > 8) return false;
+  const Sell S = model.sell();
+  if (fp32) {
+    if (Js32_.size() == 0 || spmv_format != kSpmvSell) return false;
+    BatchSystem<float> y;
+    y.nrows = static_cast<int>(model.nnodes);
+    y.bs = model.bs;
+    y.S = S;
+    y.vals = Js32_.get();
+    y.dinv = fdinv_.get();
+    y.x = fx_.get(); y.r = fr_.get(); y.rhat = frhat_.get(); y.p = fp_.get(); y.v = fv_.get();
+    y.s = fs_.get(); y.t = ft_.get(); y.phat = fphat_.get(); y.shat = fshat_.get();
+    *status = batch_->solve(y, stream, rel, max_it, iters);
+  } else {
+    const size_t nv = static_cast<size_t>(model.sell_slots) * 32 * model.bs * model.bs;
+    if (Js64_.size() != nv) Js64_.resize(nv);
+    bsr_to_sell64(model.bsr(J_.get(), nullptr), J_.get(), S, Js64_.get(), stream);
+    BatchSystem<double> y;
+    y.nrows = static_cast<int>(model.nnodes);
+    y.bs = model.bs;
+    y.S = S;
+    y.vals = Js64_.get();
+    y.dinv = dinv_.get();
+    y.x = kx_.get(); y.r = kr_.get(); y.rhat = krhat_.get(); y.p = kp_.get(); y.v = kv_.get();
+    y.s = ks_.get(); y.t = kt_.get(); y.phat = kphat_.get(); y.shat = kshat_.get();
+    *status = batch_->solve(y, stream, rel, max_it, iters);
+  }
+  // the codes of the batch are those of the replayed solve: 0 converged, 1 breakdown / not
+  // finite, 3 max_it
+  *status = *status == 0 ? DC_OK : (*status == 3 ? DC_ERR_TIMEOUT : DC_ERR_DIVERGED);
+  return true;
+}
+
 int Solver::bicgstab(const double* b, double* z, double rel_tol, int max_it, int* iters) {
   cuda_check(cudaMemcpyAsync(kr_.get(), b, n_ * sizeof(double), cudaMemcpyDeviceToDevice, stream), "copy");
   int st = krylov_run(false, rel_tol, max_it, iters);
@@ -886,7 +929,8 @@ int Solver::bicgstab(const double* b, double* z, double rel_tol, int max_it, int
 //   r = b - J z (fp64);  solve J d = r in fp32 to a modest reduction;  z += d
 int Solver::bicgstab_mixed(const double* b, double* z, double rel_tol, int max_it, int* iters) {
   // BiCGSTAB + block Jacobi: the whole refinement loop below in one cooperative launch
-  if (fused_ && !krylov_cg_ && !krylov_gmres_ && !pc_) {
+  // (batched solvers run the loop below, each correction solve in the batch)
+  if (fused_ && !batch_ && !krylov_cg_ && !krylov_gmres_ && !pc_) {
     int st = DC_OK;
     if (krylov_fused<float>(rel_tol, max_it, iters, &st, b, z)) return st;
   }

@@ -26,6 +26,8 @@
 
 namespace dcgpu {
 
+class KrylovBatcher;
+
 enum Status : int {
   DC_OK = 0,
   DC_ERR_DIVERGED = 1,     // Newton / linear solve did not converge
@@ -93,6 +95,11 @@ class Solver {
   double* residual_buffer() { return r_.get(); }
 
   void enable_mixed(bool on);
+  // Hands this solver's block-Jacobi BiCGSTAB solves (fp64, and the fp32 corrections of the
+  // mixed path) to a batcher shared with other simulations (batch.hpp).  Solves with
+  // another Krylov method or preconditioner, or with the fp32 operator in the BSR layout,
+  // stay on this solver's own stream.  Call before the first step; b outlives the solver.
+  void attach_batcher(KrylovBatcher* b) { batch_ = b; }
 
   // per-category device time of the hot launches, measured with CUDA events on the
   // solver's stream: 0 = assembly (all colour launches of one operator evaluation),
@@ -127,6 +134,10 @@ class Solver {
   std::vector<cudaEvent_t> graph_events_;
   cudaGraphExec_t krylov_graph(bool fp32);
   int krylov_run(bool fp32, double rel, int max_it, int* iters);
+  // the solve of krylov_run through the batcher; false (nothing done) when it does not apply
+  bool batch_solve(bool fp32, double rel, int max_it, int* iters, int* status);
+  KrylovBatcher* batch_ = nullptr;
+  DeviceBuffer<double> Js64_;  // fp64 SELL-32 copy of J for the batched fp64 solve
   int bicgstab(const double* b, double* z, double rel_tol, int max_it, int* iters);
   int bicgstab_mixed(const double* b, double* z, double rel_tol, int max_it, int* iters);
   double norm2(const double* v);

@@ -37,7 +37,15 @@ EXPORTED = [
     "dc_spmv_format", "dc_vertex_coords", "dc_constraints", "dc_reduce", "dc_write_vtk", "dc_config_get",
     "dc_selftest_barrier_timeout", "dc_step_stage_newton", "dc_selftest_fma_peaks", "dc_jit_selftest",
     "dc_model_jit_status", "dc_precond_info", "dc_jacobian_apply", "dc_selftest_color", "dc_selftest_aggregate", "dc_selftest_precond",
+    "dc_server_create_ex", "dc_server_batch_stats",
 ]
+
+SERVER_BATCH_KRYLOV = 1
+
+
+class BatchStats(ctypes.Structure):
+    _fields_ = [("solves", ctypes.c_int64), ("replays", ctypes.c_int64), ("slot_replays", ctypes.c_int64),
+                ("iterations", ctypes.c_int64), ("max_active", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 class ReduceValue(ctypes.Structure):
@@ -129,6 +137,8 @@ def load_library(path=LIB_PATH):
     lib.dc_expr_eval.argtypes = [ctypes.c_char_p, ctypes.c_char_p, P(ctypes.c_char_p), pd, i32, pd]
     lib.dc_assemble_residual_noalloc.argtypes = [vp, pd, d, d, d, pd]
     lib.dc_server_create.argtypes = [ctypes.c_int64, i32, P(vp)]
+    lib.dc_server_create_ex.argtypes = [ctypes.c_int64, i32, i32, P(vp)]
+    lib.dc_server_batch_stats.argtypes = [vp, P(BatchStats)]
     lib.dc_server_submit.argtypes = [vp, ctypes.c_char_p, ctypes.c_char_p, pd, sz, P(ctypes.c_int64)]
     lib.dc_server_poll.argtypes = [vp, i32, P(Result), i32, P(i32)]
     lib.dc_server_take_state.argtypes = [vp, ctypes.c_int64, pd, sz]
@@ -649,13 +659,16 @@ class Server:
     """Request server: admits simulations by device-memory budget and runs them concurrently.
 
     ``submit`` returns a request id; ``poll`` returns completed results as dicts;
-    ``take_state`` returns the final state of a completed request.
+    ``take_state`` returns the final state of a completed request.  With ``batch_krylov``
+    the running simulations' block-Jacobi BiCGSTAB solves are packed into one continuously
+    batched solve (``batch_stats`` reports its counters).
     """
 
-    def __init__(self, budget_bytes, max_active=4):
+    def __init__(self, budget_bytes, max_active=4, batch_krylov=False):
         self._lib = load_library()
         h = ctypes.c_void_p()
-        _check(self._lib.dc_server_create(int(budget_bytes), int(max_active), ctypes.byref(h)))
+        flags = SERVER_BATCH_KRYLOV if batch_krylov else 0
+        _check(self._lib.dc_server_create_ex(int(budget_bytes), int(max_active), flags, ctypes.byref(h)))
         self._h = h
         self._ndof = {}
 
@@ -687,6 +700,11 @@ class Server:
         out = np.empty(n)
         _check(self._lib.dc_server_take_state(self._h, int(request_id), _ptr(out), out.size))
         return out
+
+    def batch_stats(self):
+        st = BatchStats()
+        _check(self._lib.dc_server_batch_stats(self._h, ctypes.byref(st)))
+        return {f: getattr(st, f) for f, _ in BatchStats._fields_ if f != "reserved"}
 
     def close(self):
         if getattr(self, "_h", None):

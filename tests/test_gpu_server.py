@@ -147,3 +147,82 @@ def test_failure_is_isolated(dcgpu_lib):
     assert np.array_equal(srv.take_state(a), ref)
     assert np.array_equal(srv.take_state(c), ref)
     srv.close()
+
+
+MIXED = {"model.time_step_operator.linear_solver.precision": "mixed"}
+
+
+def _run_server(dcgpu_lib, reqs, max_active, batch_krylov, overrides=None):
+    srv = dcgpu_lib.Server(budget_bytes=8 << 30, max_active=max_active, batch_krylov=batch_krylov)
+    ids = [srv.submit(ini, overrides=overrides, init=x0) for ini, x0 in reqs]
+    res = _drain(srv, len(ids))
+    states = []
+    for rid in ids:
+        assert res[rid]["status"] == 0, res[rid]
+        states.append(srv.take_state(rid))
+    stats = srv.batch_stats()
+    srv.close()
+    return states, [res[rid] for rid in ids], stats
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batched_results_identical_alone_and_in_the_mix(dcgpu_lib, precision):
+    """Continuous batching of the Krylov solves: each request's result is bitwise the same
+    whether its solves ran alone in the batch or packed with other requests' solves (block
+    sizes 1, 2, 3 and 5 side by side), and within 1e-8 of the unbatched server's."""
+    ov = MIXED if precision == "mixed" else None
+    reqs = _requests()
+    alone = [_run_server(dcgpu_lib, [rq], 1, True, ov)[0][0] for rq in reqs]
+    mixed_states, results, stats = _run_server(dcgpu_lib, reqs, len(reqs), True, ov)
+    for k in range(len(reqs)):
+        assert np.array_equal(mixed_states[k], alone[k]), k
+    # the block-Jacobi BiCGSTAB solves went through the batch (a solve that switches to the
+    # multigrid runs on the simulation's own stream)
+    assert stats["solves"] > 0 and stats["replays"] > 0
+    assert 0 < stats["iterations"] <= sum(r["linear_iterations"] for r in results)
+    assert stats["slot_replays"] >= stats["replays"]
+    assert 1 <= stats["max_active"] <= len(reqs)
+    unbatched, _, ustats = _run_server(dcgpu_lib, reqs, len(reqs), False, ov)
+    assert ustats["solves"] == 0
+    for k in range(len(reqs)):
+        ref = unbatched[k]
+        err = np.linalg.norm(mixed_states[k] - ref) / np.linalg.norm(ref)
+        assert err <= 1e-8, (k, err)
+
+
+@pytest.mark.gpu
+def test_batched_server_matches_oracle(dcgpu_lib):
+    """A batched request's final state against the oracle's time stepping of the same
+    model (per-species relative L2 <= 1e-8), served next to three other requests."""
+    from oracle.model import OracleModel
+    reqs = _requests()
+    states, results, _ = _run_server(dcgpu_lib, reqs, len(reqs), True, MIXED)
+    for k in (1, 3):  # Gray-Scott 20^2 (bs 2) and the 3D cross-diffusion 4^3 (bs 3)
+        ini, x0 = reqs[k]
+        om = OracleModel(ini)
+        x = om.initial_state() if x0 is None else x0.copy()
+        _dec, _inc, t0, t1, _mn, _mx, dt0 = om.stepper_params()
+        x, _t, _dt = om.evolve(x, t0, dt0, t1)
+        for sp in om.species:
+            idx = om.dof(sp, om.comp_vertices[sp.comp])
+            ref = x[idx]
+            err = np.linalg.norm(states[k][idx] - ref) / max(np.linalg.norm(ref), 1e-300)
+            assert err <= 1e-8, (k, sp.name, err)
+
+
+@pytest.mark.gpu
+def test_batched_failure_is_isolated(dcgpu_lib):
+    """A request whose Newton fails leaves the batch and the others' results unchanged."""
+    good_ini, _ = cases.small_heat(n=16, steps=3)
+    ref = _run_server(dcgpu_lib, [(good_ini, None)], 1, True)[0][0]
+    srv = dcgpu_lib.Server(budget_bytes=4 << 30, max_active=3, batch_krylov=True)
+    a = srv.submit(good_ini)
+    b = srv.submit(FAILING_INI)
+    c = srv.submit(good_ini)
+    res = _drain(srv, 3)
+    assert res[b]["status"] == 2
+    assert res[a]["status"] == 0 and res[c]["status"] == 0
+    assert np.array_equal(srv.take_state(a), ref)
+    assert np.array_equal(srv.take_state(c), ref)
+    srv.close()

@@ -385,6 +385,7 @@ struct Request {
   int status = 0;
   int iters = 0;
   std::string error;
+  std::condition_variable cv;  // the caller waits on it (with the batcher's mutex)
 };
 
 template <class T>
@@ -399,85 +400,99 @@ void alloc_host(T*& p, size_t n) {
   cuda_check(cudaMallocHost(reinterpret_cast<void**>(&p), std::max<size_t>(n, 1) * sizeof(T)), "cudaMallocHost");
 }
 
-// One precision's slots, tables and captured graph.  Only the batch thread touches a lane
+inline size_t round_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// One precision's slots, table and captured graphs.  Only the batch thread touches a lane
 // after construction.
+//
+// The table is one device buffer, uploaded by one copy per replay: the header (BLane), the
+// slot descriptors, then the tiles of all active instances followed by the tiles of the
+// instances admitted for this replay.  Graphs are captured for a few grid sizes (the
+// kernels read the header at the table's start); a replay runs the smallest grid that
+// covers its tiles, so a small batch does not hold the device's blocks through its
+// chain of short kernels, while large batches use four blocks per SM.
 template <class T>
 struct Lane {
   int max_slots = 0;
-  int grid = 0;
+  int grid_full = 0;
+  cudaStream_t stream = nullptr;
   std::vector<Request*> slot;  // null: free
   std::vector<char> fresh;     // admitted since the last replay
-  DeviceBuffer<BInst<T>> inst;
-  DeviceBuffer<BLane<T>> hdr;
-  DeviceBuffer<int2> tiles, init_tiles;
+  DeviceBuffer<unsigned char> table;
+  unsigned char* h_table = nullptr;
+  size_t off_inst = 0, off_tiles = 0;
+  size_t tile_cap = 0;  // run + init tiles the table holds
   DeviceBuffer<double> sc, part;
   DeviceBuffer<unsigned int> cnt;
-  BInst<T>* h_inst = nullptr;
-  BLane<T>* h_hdr = nullptr;
-  int2* h_tiles = nullptr;
-  int2* h_init = nullptr;
   double* h_sc = nullptr;
-  size_t tile_cap = 0;
-  cudaGraphExec_t graph = nullptr;
+  std::vector<std::pair<int, cudaGraphExec_t>> graphs;  // (grid, graph), ascending grid
 
-  void create(int slots, int grid_blocks, cudaStream_t stream) {
+  const BLane<T>* dev_header() const { return reinterpret_cast<const BLane<T>*>(table.get()); }
+
+  void create(int slots, int full_grid, cudaStream_t s) {
     max_slots = slots;
-    grid = grid_blocks;
+    grid_full = full_grid;
+    stream = s;
     slot.assign(slots, nullptr);
     fresh.assign(slots, 0);
-    inst.resize(slots);
-    hdr.resize(1);
     sc.resize(static_cast<size_t>(slots) * KS_COUNT);
     cnt.resize(slots);
     cuda_check(cudaMemsetAsync(cnt.get(), 0, slots * sizeof(unsigned int), stream), "memset");
     cuda_check(cudaMemsetAsync(sc.get(), 0, static_cast<size_t>(slots) * KS_COUNT * sizeof(double), stream), "memset");
-    alloc_host(h_inst, slots);
-    alloc_host(h_hdr, 1);
     alloc_host(h_sc, static_cast<size_t>(slots) * KS_COUNT);
-    reserve(1024);
-    // an empty header until the first replay
-    *h_hdr = BLane<T>{0, 0, tiles.get(), init_tiles.get(), inst.get(), sc.get(), part.get(), cnt.get()};
-    cuda_check(cudaMemcpyAsync(hdr.get(), h_hdr, sizeof(BLane<T>), cudaMemcpyHostToDevice, stream), "upload");
-    // kChunk iterations of the five phases, captured once; the kernels read everything
-    // that changes between replays from the header
-    cudaGraph_t g = nullptr;
-    cuda_check(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
-    const BLane<T>* L = hdr.get();
-    for (int k = 0; k < kChunk; ++k) {
-      k_bt_p<T><<<grid, kTileRows, 0, stream>>>(L);
-      k_bt_rv<T><<<grid, kTileRows, 0, stream>>>(L);
-      k_bt_s<T><<<grid, kTileRows, 0, stream>>>(L);
-      k_bt_omega<T><<<grid, kTileRows, 0, stream>>>(L);
-      k_bt_xr<T><<<grid, kTileRows, 0, stream>>>(L);
-    }
-    const cudaError_t e = cudaStreamEndCapture(stream, &g);
-    cuda_check(e, "cudaStreamEndCapture");
-    cuda_check(cudaGetLastError(), "batched BiCGSTAB capture");
-    cuda_check(cudaGraphInstantiate(&graph, g, 0), "cudaGraphInstantiate");
-    cudaGraphDestroy(g);
+    off_inst = round_up(sizeof(BLane<T>), 256);
+    off_tiles = round_up(off_inst + static_cast<size_t>(slots) * sizeof(BInst<T>), 256);
+    reserve(2048);
+  }
+
+  void drop_graphs() {
+    for (auto& g : graphs) cudaGraphExecDestroy(g.second);
+    graphs.clear();
   }
 
   void destroy() {
-    if (graph) cudaGraphExecDestroy(graph);
-    graph = nullptr;
-    free_host(h_inst);
-    free_host(h_hdr);
-    free_host(h_tiles);
-    free_host(h_init);
+    drop_graphs();
+    free_host(h_table);
     free_host(h_sc);
   }
 
-  // room for n tiles in the tables (called with the stream idle)
+  // kChunk iterations of the five phases at each grid size (called with the stream idle)
+  void capture() {
+    drop_graphs();
+    const BLane<T>* L = dev_header();
+    for (int grid : {32, 128, grid_full}) {
+      if (grid > grid_full || (!graphs.empty() && graphs.back().first >= grid)) continue;
+      cudaGraph_t g = nullptr;
+      cuda_check(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+      for (int k = 0; k < kChunk; ++k) {
+        k_bt_p<T><<<grid, kTileRows, 0, stream>>>(L);
+        k_bt_rv<T><<<grid, kTileRows, 0, stream>>>(L);
+        k_bt_s<T><<<grid, kTileRows, 0, stream>>>(L);
+        k_bt_omega<T><<<grid, kTileRows, 0, stream>>>(L);
+        k_bt_xr<T><<<grid, kTileRows, 0, stream>>>(L);
+      }
+      cuda_check(cudaStreamEndCapture(stream, &g), "cudaStreamEndCapture");
+      cuda_check(cudaGetLastError(), "batched BiCGSTAB capture");
+      cudaGraphExec_t exec = nullptr;
+      const cudaError_t e = cudaGraphInstantiate(&exec, g, 0);
+      cudaGraphDestroy(g);
+      cuda_check(e, "cudaGraphInstantiate");
+      graphs.emplace_back(grid, exec);
+    }
+  }
+
+  // room for n tiles (run + init) in the table (called with the stream idle); the table
+  // moves, so the graphs are captured again
   void reserve(size_t n) {
     if (n <= tile_cap) return;
-    size_t cap = std::max<size_t>(tile_cap, 1024);
+    size_t cap = std::max<size_t>(tile_cap, 2048);
     while (cap < n) cap *= 2;
-    tiles.resize(cap);
-    init_tiles.resize(cap);
+    const size_t bytes = off_tiles + cap * sizeof(int2);
+    table.resize(bytes);
+    alloc_host(h_table, bytes);
     part.resize(cap * 2);
-    alloc_host(h_tiles, cap);
-    alloc_host(h_init, cap);
     tile_cap = cap;
+    capture();
   }
 
   int active() const {
@@ -501,23 +516,26 @@ struct Lane {
     else return q->s64;
   }
 
-  // enqueues one replay (uploads, the new instances' initialisation, the graph, the scalars'
-  // download) on `stream`; returns the kernels launched
-  long long enqueue(cudaStream_t stream) {
-    int nt = 0, top = 0;
+  // enqueues one replay (the table upload, the new instances' initialisation, the graph,
+  // the scalars' download) on the stream; returns the kernels launched
+  long long enqueue() {
+    int nt = 0, ni = 0, top = 0;
     for (int k = 0; k < max_slots; ++k) {
       if (!slot[k]) continue;
-      const BatchSystem<T>& y = system(slot[k]);
-      nt += (y.nrows + kTileRows - 1) / kTileRows;
+      const int tk = (system(slot[k]).nrows + kTileRows - 1) / kTileRows;
+      nt += tk;
+      if (fresh[k]) ni += tk;
       top = k + 1;
     }
-    reserve(static_cast<size_t>(nt));
-    int t = 0, ni = 0;
+    reserve(static_cast<size_t>(nt) + ni);
+    BInst<T>* hi = reinterpret_cast<BInst<T>*>(h_table + off_inst);
+    int2* ht = reinterpret_cast<int2*>(h_table + off_tiles);
+    int t = 0, it = nt;
     for (int k = 0; k < top; ++k) {
       Request* q = slot[k];
       if (!q) continue;
       const BatchSystem<T>& y = system(q);
-      BInst<T>& d = h_inst[k];
+      BInst<T>& d = hi[k];
       d.nrows = y.nrows;
       d.bs = y.bs;
       d.ntiles = (y.nrows + kTileRows - 1) / kTileRows;
@@ -530,31 +548,34 @@ struct Lane {
       d.dinv = y.dinv;
       d.x = y.x; d.r = y.r; d.rhat = y.rhat; d.p = y.p; d.v = y.v; d.s = y.s; d.t = y.t;
       d.phat = y.phat; d.shat = y.shat;
-      for (int j = 0; j < d.ntiles; ++j) h_tiles[t + j] = make_int2(k, j);
+      for (int j = 0; j < d.ntiles; ++j) ht[t + j] = make_int2(k, j);
       if (fresh[k]) {
-        for (int j = 0; j < d.ntiles; ++j) h_init[ni + j] = make_int2(k, j);
-        ni += d.ntiles;
+        for (int j = 0; j < d.ntiles; ++j) ht[it + j] = make_int2(k, j);
+        it += d.ntiles;
         cuda_check(cudaStreamWaitEvent(stream, q->ready, 0), "cudaStreamWaitEvent");
         fresh[k] = 0;
       }
       t += d.ntiles;
     }
-    *h_hdr = BLane<T>{nt, ni, tiles.get(), init_tiles.get(), inst.get(), sc.get(), part.get(), cnt.get()};
-    cuda_check(cudaMemcpyAsync(inst.get(), h_inst, static_cast<size_t>(top) * sizeof(BInst<T>), cudaMemcpyHostToDevice,
-                               stream), "upload");
-    cuda_check(cudaMemcpyAsync(tiles.get(), h_tiles, static_cast<size_t>(nt) * sizeof(int2), cudaMemcpyHostToDevice,
-                               stream), "upload");
-    if (ni)
-      cuda_check(cudaMemcpyAsync(init_tiles.get(), h_init, static_cast<size_t>(ni) * sizeof(int2),
-                                 cudaMemcpyHostToDevice, stream), "upload");
-    cuda_check(cudaMemcpyAsync(hdr.get(), h_hdr, sizeof(BLane<T>), cudaMemcpyHostToDevice, stream), "upload");
+    const int2* dt = reinterpret_cast<const int2*>(table.get() + off_tiles);
+    *reinterpret_cast<BLane<T>*>(h_table) =
+        BLane<T>{nt, ni, dt, dt + nt, reinterpret_cast<const BInst<T>*>(table.get() + off_inst), sc.get(), part.get(),
+                 cnt.get()};
+    cuda_check(cudaMemcpyAsync(table.get(), h_table, off_tiles + static_cast<size_t>(nt + ni) * sizeof(int2),
+                               cudaMemcpyHostToDevice, stream), "upload");
     long long launched = 0;
     if (ni) {
-      k_bt_init<T><<<grid, kTileRows, 0, stream>>>(hdr.get());
+      k_bt_init<T><<<std::min(ni, grid_full), kTileRows, 0, stream>>>(dev_header());
       cuda_check(cudaGetLastError(), "batched BiCGSTAB init");
       ++launched;
     }
-    cuda_check(cudaGraphLaunch(graph, stream), "cudaGraphLaunch");
+    cudaGraphExec_t g = graphs.back().second;
+    for (const auto& gg : graphs)
+      if (gg.first >= nt) {
+        g = gg.second;
+        break;
+      }
+    cuda_check(cudaGraphLaunch(g, stream), "cudaGraphLaunch");
     launched += static_cast<long long>(kChunk) * kPhases;
     cuda_check(cudaMemcpyAsync(h_sc, sc.get(), static_cast<size_t>(top) * KS_COUNT * sizeof(double),
                                cudaMemcpyDeviceToHost, stream), "download");
@@ -577,6 +598,17 @@ struct Lane {
       slot[k] = nullptr;
     }
   }
+
+  // a failure: every request the lane holds ends with `why`
+  void fail_all(const std::string& why) {
+    for (Request*& q : slot)
+      if (q) {
+        q->error = why;
+        q->done = true;
+        q->cv.notify_one();
+        q = nullptr;
+      }
+  }
 };
 
 }  // namespace
@@ -585,7 +617,7 @@ struct KrylovBatcher::Impl {
   int device = 0;
   cudaStream_t stream = nullptr;
   std::mutex mu;
-  std::condition_variable cv_work, cv_done;
+  std::condition_variable cv_work;
   std::deque<Request*> pending;
   bool stop = false;
   std::string fatal;  // a CUDA failure of the batch thread: later solves fail with it
@@ -606,9 +638,12 @@ KrylovBatcher::KrylovBatcher(int device, int max_slots) : impl_(std::make_unique
   cuda_check(cudaSetDevice(device), "cudaSetDevice");
   int sms = 0;
   cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "cudaDeviceGetAttribute");
-  cuda_check(cudaStreamCreateWithFlags(&m.stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  // the batch is on every served simulation's critical path: its blocks go first
+  int prio_low = 0, prio_high = 0;
+  cuda_check(cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high), "cudaDeviceGetStreamPriorityRange");
+  cuda_check(cudaStreamCreateWithPriority(&m.stream, cudaStreamNonBlocking, prio_high), "cudaStreamCreate");
   try {
-    // four 256-thread blocks per SM walk the tile table
+    // at most four 256-thread blocks per SM walk the tile table
     m.l32.create(max_slots, 4 * sms, m.stream);
     m.l64.create(max_slots, 4 * sms, m.stream);
     cuda_check(cudaStreamSynchronize(m.stream), "cudaStreamSynchronize");
@@ -681,7 +716,7 @@ int KrylovBatcher::Impl::submit(const BatchSystem<T>& sys, cudaStream_t caller, 
   if (!fatal.empty()) throw CudaError(fatal);
   pending.push_back(&q);
   cv_work.notify_one();
-  cv_done.wait(lk, [&] { return q.done; });
+  q.cv.wait(lk, [&] { return q.done; });
   if (!q.error.empty()) throw CudaError(q.error);
   *iters = q.iters;
   return q.status;
@@ -708,21 +743,22 @@ void KrylovBatcher::Impl::loop() {
       }
       const int a32 = l32.active(), a64 = l64.active();
       long long launched = 0;
-      if (a32) launched += l32.enqueue(stream);
-      if (a64) launched += l64.enqueue(stream);
+      if (a32) launched += l32.enqueue();
+      if (a64) launched += l64.enqueue();
       count_launches(launched);
       cuda_check(cudaStreamSynchronize(stream), "batched BiCGSTAB");
       finished.clear();
-      {
-        std::lock_guard<std::mutex> lk(mu);
-        st.replays += (a32 > 0) + (a64 > 0);
-        st.slot_replays += a32 + a64;
-        st.max_active = std::max<int32_t>(st.max_active, a32 + a64);
-        l32.retire(finished, st);
-        l64.retire(finished, st);
-        for (Request* q : finished) q->done = true;
+      std::lock_guard<std::mutex> lk(mu);
+      st.replays += (a32 > 0) + (a64 > 0);
+      st.slot_replays += a32 + a64;
+      st.max_active = std::max<int32_t>(st.max_active, a32 + a64);
+      l32.retire(finished, st);
+      l64.retire(finished, st);
+      // under the lock: a caller returns (and destroys its request) only after taking it
+      for (Request* q : finished) {
+        q->done = true;
+        q->cv.notify_one();
       }
-      if (!finished.empty()) cv_done.notify_all();
     }
   } catch (const std::exception& e) {
     // nothing of the batch may still run on the callers' buffers when they resume
@@ -732,21 +768,11 @@ void KrylovBatcher::Impl::loop() {
     for (Request* q : pending) {
       q->error = fatal;
       q->done = true;
+      q->cv.notify_one();
     }
     pending.clear();
-    for (Request*& q : l32.slot)
-      if (q) {
-        q->error = fatal;
-        q->done = true;
-        q = nullptr;
-      }
-    for (Request*& q : l64.slot)
-      if (q) {
-        q->error = fatal;
-        q->done = true;
-        q = nullptr;
-      }
-    cv_done.notify_all();
+    l32.fail_all(fatal);
+    l64.fail_all(fatal);
   }
 }
 

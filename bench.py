@@ -330,6 +330,8 @@ def run_serving(dcgpu, n_requests, lam, max_active, precision, seed=20261203, bu
             "p99_latency_s": float(np.percentile(lat, 99)), "wall_s": wall,
             "value": work / wall, "unit": METRIC,
             "bytes_measured_max": max((r.get("bytes_measured", 0) for r in done.values()), default=0),
+            "setup_s_sum": sum(r.get("setup_s", 0.0) for r in done.values()),
+            "run_s_sum": sum(r["run_s"] for r in done.values()),
             "mix": "2D N log-U[%d,%d] / 3D N log-U[%d,%d], 1-2 compartments, 1-8 species, %d-%d IE steps"
                    % (mix["n2d"] + mix["n3d"] + mix["steps"])}
 

@@ -12,6 +12,7 @@
 #include "batch.hpp"
 
 #include <algorithm>
+#include <chrono>
 #include <condition_variable>
 #include <deque>
 #include <mutex>
@@ -409,8 +410,8 @@ inline size_t round_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 // slot descriptors, then the tiles of all active instances followed by the tiles of the
 // instances admitted for this replay.  Graphs are captured for a few grid sizes (the
 // kernels read the header at the table's start); a replay runs the smallest grid that
-// covers its tiles, so a small batch does not hold the device's blocks through its
-// chain of short kernels, while large batches use four blocks per SM.
+// leaves at most four tiles to a block, so a small batch does not hold the device's blocks
+// through its chain of short kernels, while large batches use four blocks per SM.
 template <class T>
 struct Lane {
   int max_slots = 0;
@@ -569,9 +570,12 @@ struct Lane {
       cuda_check(cudaGetLastError(), "batched BiCGSTAB init");
       ++launched;
     }
+    // the smallest captured grid that leaves at most four tiles to a block: the batch shares
+    // the device with the other simulations' kernels, and a grid that asks for every SM's
+    // blocks waits for all of them to drain before its last block runs
     cudaGraphExec_t g = graphs.back().second;
     for (const auto& gg : graphs)
-      if (gg.first >= nt) {
+      if (4 * gg.first >= nt) {
         g = gg.second;
         break;
       }
@@ -712,11 +716,13 @@ int KrylovBatcher::Impl::submit(const BatchSystem<T>& sys, cudaStream_t caller, 
   q.ready = ev.e;
   q.rel = rel;
   q.max_it = std::max(max_it, 1);
+  const auto t0 = std::chrono::steady_clock::now();
   std::unique_lock<std::mutex> lk(mu);
   if (!fatal.empty()) throw CudaError(fatal);
   pending.push_back(&q);
   cv_work.notify_one();
   q.cv.wait(lk, [&] { return q.done; });
+  st.wait_s += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   if (!q.error.empty()) throw CudaError(q.error);
   *iters = q.iters;
   return q.status;
@@ -741,6 +747,7 @@ void KrylovBatcher::Impl::loop() {
           it = ok ? pending.erase(it) : std::next(it);
         }
       }
+      const auto t0 = std::chrono::steady_clock::now();
       const int a32 = l32.active(), a64 = l64.active();
       long long launched = 0;
       if (a32) launched += l32.enqueue();
@@ -749,6 +756,7 @@ void KrylovBatcher::Impl::loop() {
       cuda_check(cudaStreamSynchronize(stream), "batched BiCGSTAB");
       finished.clear();
       std::lock_guard<std::mutex> lk(mu);
+      st.replay_s += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
       st.replays += (a32 > 0) + (a64 > 0);
       st.slot_replays += a32 + a64;
       st.max_active = std::max<int32_t>(st.max_active, a32 + a64);

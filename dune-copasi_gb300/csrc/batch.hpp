@@ -50,6 +50,8 @@ struct BatchStats {
   int64_t slot_replays = 0;  // sum over replays of the instances active in them
   int64_t iterations = 0;    // BiCGSTAB iterations of all solved systems
   int32_t max_active = 0;    // most instances in one replay
+  double replay_s = 0.0;     // host time from the start of each replay's enqueue to its end
+  double wait_s = 0.0;       // time the callers spent blocked in solve(), summed over calls
 };
 
 class KrylovBatcher {

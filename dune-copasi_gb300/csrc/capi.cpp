@@ -436,6 +436,8 @@ int dc_server_batch_stats(const dc_server* server, dc_batch_stats* out) {
     out->iterations = b.iterations;
     out->max_active = b.max_active;
     out->reserved = 0;
+    out->replay_s = b.replay_s;
+    out->wait_s = b.wait_s;
     return DC_OK;
   });
 }
@@ -470,6 +472,7 @@ int dc_server_poll(dc_server* server, int32_t wait, dc_result* results, int32_t 
       o.steps = r.steps;
       o.bytes_estimate = r.bytes_estimate;
       o.bytes_measured = r.bytes_measured;
+      o.setup_s = r.setup_s;
       if (r.status != DC_OK && !r.error.empty()) g_last_error = r.error;
     }
     *n_out = static_cast<int32_t>(done.size());

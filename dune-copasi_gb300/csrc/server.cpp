@@ -179,6 +179,7 @@ void Server::worker() {
       Solver solver(model, stream);
       if (batcher_) solver.attach_batcher(batcher_.get());
       measure();
+      res.setup_s = now() - t_admit;
       Ini tso = model.cfg.sub("model").sub("time_step_operator");
       const double t0 = tso.get_double("time_begin", 0.0);
       const double t1 = tso.get_double("time_end", 1.0);

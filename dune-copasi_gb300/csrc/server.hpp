@@ -36,6 +36,7 @@ struct ServerResult {
   int64_t steps = 0;
   int64_t bytes_estimate = 0;
   int64_t bytes_measured = 0;  // peak device bytes the simulation's buffers held
+  double setup_s = 0.0;        // model and solver set-up (part of run_s)
   std::string error;
 };
 

@@ -45,7 +45,8 @@ SERVER_BATCH_KRYLOV = 1
 
 class BatchStats(ctypes.Structure):
     _fields_ = [("solves", ctypes.c_int64), ("replays", ctypes.c_int64), ("slot_replays", ctypes.c_int64),
-                ("iterations", ctypes.c_int64), ("max_active", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("iterations", ctypes.c_int64), ("max_active", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("replay_s", ctypes.c_double), ("wait_s", ctypes.c_double)]
 
 
 class ReduceValue(ctypes.Structure):
@@ -79,7 +80,7 @@ class Result(ctypes.Structure):
                 ("queue_s", ctypes.c_double), ("run_s", ctypes.c_double), ("latency_s", ctypes.c_double),
                 ("n_dof", ctypes.c_int64), ("newton_iterations", ctypes.c_int64),
                 ("linear_iterations", ctypes.c_int64), ("steps", ctypes.c_int64),
-                ("bytes_estimate", ctypes.c_int64), ("bytes_measured", ctypes.c_int64)]
+                ("bytes_estimate", ctypes.c_int64), ("bytes_measured", ctypes.c_int64), ("setup_s", ctypes.c_double)]
 
 
 CALLBACK = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p)

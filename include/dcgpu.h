@@ -268,6 +268,7 @@ typedef struct dc_result {
   int64_t bytes_estimate;  /* footprint estimated at submission (admission charge) */
   int64_t bytes_measured;  /* peak device bytes the simulation's buffers held; the server
                               charges a running simulation this instead of the estimate */
+  double setup_s;          /* model and solver set-up, part of run_s */
 } dc_result;
 
 int dc_server_create(int64_t budget_bytes, int32_t max_active, dc_server** out);
@@ -289,6 +290,8 @@ typedef struct dc_batch_stats {
   int64_t iterations;    /* BiCGSTAB iterations of all solved systems */
   int32_t max_active;    /* most instances in one replay */
   int32_t reserved;
+  double replay_s;       /* host time from the start of each replay to its end, summed */
+  double wait_s;         /* time the simulations spent waiting for their solves, summed */
 } dc_batch_stats;
 /* counters of the Krylov batch (all zero for a server created without the flag) */
 int dc_server_batch_stats(const dc_server* server, dc_batch_stats* out);

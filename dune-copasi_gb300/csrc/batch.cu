@@ -517,10 +517,12 @@ struct Lane {
     else return q->s64;
   }
 
-  // enqueues one replay (the table upload, the new instances' initialisation, the graph,
-  // the scalars' download) on the stream; returns the kernels launched
-  long long enqueue() {
-    int nt = 0, ni = 0, top = 0;
+  int nt = 0, ni = 0, top = 0;  // the next replay's run tiles, init tiles and slot bound
+
+  // sizes the next replay and makes room for it (with the stream idle: a larger table is a
+  // new allocation and new graphs)
+  void plan() {
+    nt = ni = top = 0;
     for (int k = 0; k < max_slots; ++k) {
       if (!slot[k]) continue;
       const int tk = (system(slot[k]).nrows + kTileRows - 1) / kTileRows;
@@ -529,6 +531,11 @@ struct Lane {
       top = k + 1;
     }
     reserve(static_cast<size_t>(nt) + ni);
+  }
+
+  // enqueues the planned replay (the table upload, the new instances' initialisation, the
+  // graph, the scalars' download) on the stream; returns the kernels launched
+  long long enqueue() {
     BInst<T>* hi = reinterpret_cast<BInst<T>*>(h_table + off_inst);
     int2* ht = reinterpret_cast<int2*>(h_table + off_tiles);
     int t = 0, it = nt;
@@ -750,6 +757,8 @@ void KrylovBatcher::Impl::loop() {
       const auto t0 = std::chrono::steady_clock::now();
       const int a32 = l32.active(), a64 = l64.active();
       long long launched = 0;
+      if (a32) l32.plan();
+      if (a64) l64.plan();
       if (a32) launched += l32.enqueue();
       if (a64) launched += l64.enqueue();
       count_launches(launched);

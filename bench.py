@@ -319,6 +319,8 @@ def run_serving(dcgpu, n_requests, lam, max_active, precision, seed=20261203, bu
             done[r["request_id"]] = r
     wall = time.perf_counter() - t0
     bstats = srv.batch_stats() if batch else None
+    if batch:
+        bstats["tuned_grids"] = srv.batch_tuning()
     srv.close()
     lat = sorted(r["latency_s"] for r in done.values())
     ok = sum(1 for r in done.values() if r["status"] == 0)
@@ -353,6 +355,8 @@ def run_burst(dcgpu, copies, n, steps, batch, budget=16 << 30):
             done[r["request_id"]] = r
     wall = time.perf_counter() - t0
     bstats = srv.batch_stats() if batch else None
+    if batch:
+        bstats["tuned_grids"] = srv.batch_tuning()
     srv.close()
     work = sum(r["n_dof"] * r["newton_iterations"] for r in done.values())
     return {"copies": copies, "model": "cross_diffusion_3d_%d^3x6_mixed_%d_steps" % (n, steps),

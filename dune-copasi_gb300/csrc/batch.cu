@@ -12,6 +12,7 @@
 #include "batch.hpp"
 
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
@@ -409,9 +410,12 @@ inline size_t round_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 // The table is one device buffer, uploaded by one copy per replay: the header (BLane), the
 // slot descriptors, then the tiles of all active instances followed by the tiles of the
 // instances admitted for this replay.  Graphs are captured for a few grid sizes (the
-// kernels read the header at the table's start); a replay runs the smallest grid that
-// leaves at most four tiles to a block, so a small batch does not hold the device's blocks
-// through its chain of short kernels, while large batches use four blocks per SM.
+// kernels read the header at the table's start), and an autotuner picks the grid per batch
+// size: a replay of t tiles falls in bucket floor(log2 t); a bucket first times each grid
+// that leaves at most 64 tiles to a block on kTuneSamples replays (CUDA events around the
+// graph launch), then runs the one with the least mean time.  The batch shares the device
+// with the other simulations' kernels, so the fastest grid depends on the load as well as
+// on the size; the results do not depend on the grid (the tile decomposition is fixed).
 template <class T>
 struct Lane {
   int max_slots = 0;
@@ -428,7 +432,69 @@ struct Lane {
   double* h_sc = nullptr;
   std::vector<std::pair<int, cudaGraphExec_t>> graphs;  // (grid, graph), ascending grid
 
+  static constexpr int kBuckets = 24, kTuneSamples = 3, kMaxGrids = 3;
+  struct Bucket {
+    double ms[kMaxGrids] = {};
+    int n[kMaxGrids] = {};
+    int chosen = -1;  // index into graphs once tuned
+  };
+  std::array<Bucket, kBuckets> tune{};
+  cudaEvent_t tev[2] = {nullptr, nullptr};
+  int timed_bucket = -1, timed_graph = -1;  // the timed replay in flight
+
   const BLane<T>* dev_header() const { return reinterpret_cast<const BLane<T>*>(table.get()); }
+
+  // graph index for a replay of nt tiles; sets timed_* when this replay is a tuning sample
+  int pick_graph(int tiles) {
+    int b = 0;
+    while (b + 1 < kBuckets && (2 << b) <= tiles) ++b;
+    Bucket& k = tune[b];
+    timed_bucket = timed_graph = -1;
+    if (k.chosen >= 0) return k.chosen;
+    const int ng = static_cast<int>(graphs.size());
+    int best = -1;
+    for (int i = 0; i < ng; ++i) {
+      const bool fits = 64 * static_cast<int64_t>(graphs[i].first) >= tiles || i == ng - 1;
+      if (fits && k.n[i] < kTuneSamples && (best < 0 || k.n[i] < k.n[best])) best = i;
+    }
+    if (best < 0) {
+      // every candidate has its samples: keep the fastest
+      double bm = 0.0;
+      for (int i = 0; i < ng; ++i)
+        if (k.n[i] > 0 && (k.chosen < 0 || k.ms[i] / k.n[i] < bm)) {
+          k.chosen = i;
+          bm = k.ms[i] / k.n[i];
+        }
+      return k.chosen;
+    }
+    timed_bucket = b;
+    timed_graph = best;
+    return best;
+  }
+
+  // after the stream has been synchronised: books the timed replay's duration
+  void book_timing() {
+    if (timed_bucket < 0) return;
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, tev[0], tev[1]) == cudaSuccess) {
+      tune[timed_bucket].ms[timed_graph] += ms;
+      tune[timed_bucket].n[timed_graph] += 1;
+    } else {
+      cudaGetLastError();  // an unreadable sample is dropped
+    }
+    timed_bucket = timed_graph = -1;
+  }
+
+  // the tuned grids as JSON: {"<first tile count of the bucket>": grid, ...}
+  std::string tuning_json() const {
+    std::string out = "{";
+    for (int b = 0; b < kBuckets; ++b)
+      if (tune[b].chosen >= 0) {
+        if (out.size() > 1) out += ", ";
+        out += "\"" + std::to_string(1 << b) + "\": " + std::to_string(graphs[tune[b].chosen].first);
+      }
+    return out + "}";
+  }
 
   void create(int slots, int full_grid, cudaStream_t s) {
     max_slots = slots;
@@ -441,6 +507,7 @@ struct Lane {
     cuda_check(cudaMemsetAsync(cnt.get(), 0, slots * sizeof(unsigned int), stream), "memset");
     cuda_check(cudaMemsetAsync(sc.get(), 0, static_cast<size_t>(slots) * KS_COUNT * sizeof(double), stream), "memset");
     alloc_host(h_sc, static_cast<size_t>(slots) * KS_COUNT);
+    for (auto& e : tev) cuda_check(cudaEventCreate(&e), "cudaEventCreate");
     off_inst = round_up(sizeof(BLane<T>), 256);
     off_tiles = round_up(off_inst + static_cast<size_t>(slots) * sizeof(BInst<T>), 256);
     reserve(2048);
@@ -453,6 +520,9 @@ struct Lane {
 
   void destroy() {
     drop_graphs();
+    for (auto& e : tev)
+      if (e) cudaEventDestroy(e);
+    tev[0] = tev[1] = nullptr;
     free_host(h_table);
     free_host(h_sc);
   }
@@ -577,16 +647,10 @@ struct Lane {
       cuda_check(cudaGetLastError(), "batched BiCGSTAB init");
       ++launched;
     }
-    // the smallest captured grid that leaves at most four tiles to a block: the batch shares
-    // the device with the other simulations' kernels, and a grid that asks for every SM's
-    // blocks waits for all of them to drain before its last block runs
-    cudaGraphExec_t g = graphs.back().second;
-    for (const auto& gg : graphs)
-      if (4 * gg.first >= nt) {
-        g = gg.second;
-        break;
-      }
-    cuda_check(cudaGraphLaunch(g, stream), "cudaGraphLaunch");
+    const int gi = pick_graph(nt);
+    if (timed_bucket >= 0) cuda_check(cudaEventRecord(tev[0], stream), "cudaEventRecord");
+    cuda_check(cudaGraphLaunch(graphs[gi].second, stream), "cudaGraphLaunch");
+    if (timed_bucket >= 0) cuda_check(cudaEventRecord(tev[1], stream), "cudaEventRecord");
     launched += static_cast<long long>(kChunk) * kPhases;
     cuda_check(cudaMemcpyAsync(h_sc, sc.get(), static_cast<size_t>(top) * KS_COUNT * sizeof(double),
                                cudaMemcpyDeviceToHost, stream), "download");
@@ -686,6 +750,11 @@ BatchStats KrylovBatcher::stats() const {
   return impl_->st;
 }
 
+std::string KrylovBatcher::tuning() const {
+  std::lock_guard<std::mutex> lk(impl_->mu);
+  return "{\"fp32\": " + impl_->l32.tuning_json() + ", \"fp64\": " + impl_->l64.tuning_json() + "}";
+}
+
 int KrylovBatcher::solve(const BatchSystem<float>& sys, cudaStream_t caller, double rel, int max_it, int* iters) {
   return impl_->submit(sys, caller, rel, max_it, iters);
 }
@@ -769,6 +838,8 @@ void KrylovBatcher::Impl::loop() {
       st.replays += (a32 > 0) + (a64 > 0);
       st.slot_replays += a32 + a64;
       st.max_active = std::max<int32_t>(st.max_active, a32 + a64);
+      l32.book_timing();
+      l64.book_timing();
       l32.retire(finished, st);
       l64.retire(finished, st);
       // under the lock: a caller returns (and destroys its request) only after taking it

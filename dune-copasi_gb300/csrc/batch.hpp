@@ -22,6 +22,7 @@
 
 #include <cstdint>
 #include <memory>
+#include <string>
 
 #include <cuda_runtime.h>
 
@@ -73,6 +74,8 @@ class KrylovBatcher {
   int solve(const BatchSystem<double>& sys, cudaStream_t caller, double rel, int max_it, int* iters);
 
   BatchStats stats() const;
+  // the replay grid the autotuner chose per batch size, per precision, as JSON
+  std::string tuning() const;
 
   struct Impl;
 

@@ -426,6 +426,16 @@ int dc_server_create_ex(int64_t budget_bytes, int32_t max_active, int32_t flags,
   });
 }
 
+int dc_server_batch_tuning(const dc_server* server, char* buf, size_t len) {
+  return guarded([&] {
+    if (!server || !buf || len == 0) throw std::invalid_argument("null argument");
+    const std::string info = server->server->batch_tuning();
+    std::strncpy(buf, info.c_str(), len - 1);
+    buf[len - 1] = '\0';
+    return DC_OK;
+  });
+}
+
 int dc_server_batch_stats(const dc_server* server, dc_batch_stats* out) {
   return guarded([&] {
     if (!server || !out) throw std::invalid_argument("null argument");

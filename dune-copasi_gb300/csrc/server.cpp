@@ -225,6 +225,7 @@ void Server::worker() {
 }
 
 BatchStats Server::batch_stats() const { return batcher_ ? batcher_->stats() : BatchStats{}; }
+std::string Server::batch_tuning() const { return batcher_ ? batcher_->tuning() : std::string("{}"); }
 
 void Server::recharge(int64_t& held, int64_t measured) {
   {

@@ -59,6 +59,8 @@ class Server {
   int pending() ;
   // counters of the Krylov batch (all zero without batch_krylov)
   BatchStats batch_stats() const;
+  // the Krylov batch's tuned replay grids as JSON ("{}" without batch_krylov)
+  std::string batch_tuning() const;
 
   static int64_t estimate_bytes(const std::string& ini, const std::string& overrides);
   // device memory kept free beyond an admitted request's estimate

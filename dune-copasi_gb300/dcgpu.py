@@ -37,7 +37,7 @@ EXPORTED = [
     "dc_spmv_format", "dc_vertex_coords", "dc_constraints", "dc_reduce", "dc_write_vtk", "dc_config_get",
     "dc_selftest_barrier_timeout", "dc_step_stage_newton", "dc_selftest_fma_peaks", "dc_jit_selftest",
     "dc_model_jit_status", "dc_precond_info", "dc_jacobian_apply", "dc_selftest_color", "dc_selftest_aggregate", "dc_selftest_precond",
-    "dc_server_create_ex", "dc_server_batch_stats",
+    "dc_server_create_ex", "dc_server_batch_stats", "dc_server_batch_tuning",
 ]
 
 SERVER_BATCH_KRYLOV = 1
@@ -140,6 +140,7 @@ def load_library(path=LIB_PATH):
     lib.dc_server_create.argtypes = [ctypes.c_int64, i32, P(vp)]
     lib.dc_server_create_ex.argtypes = [ctypes.c_int64, i32, i32, P(vp)]
     lib.dc_server_batch_stats.argtypes = [vp, P(BatchStats)]
+    lib.dc_server_batch_tuning.argtypes = [vp, ctypes.c_char_p, sz]
     lib.dc_server_submit.argtypes = [vp, ctypes.c_char_p, ctypes.c_char_p, pd, sz, P(ctypes.c_int64)]
     lib.dc_server_poll.argtypes = [vp, i32, P(Result), i32, P(i32)]
     lib.dc_server_take_state.argtypes = [vp, ctypes.c_int64, pd, sz]
@@ -706,6 +707,13 @@ class Server:
         st = BatchStats()
         _check(self._lib.dc_server_batch_stats(self._h, ctypes.byref(st)))
         return {f: getattr(st, f) for f, _ in BatchStats._fields_ if f != "reserved"}
+
+    def batch_tuning(self):
+        """Replay grid the batch's autotuner chose per batch-size bucket and precision."""
+        import json
+        buf = ctypes.create_string_buffer(4096)
+        _check(self._lib.dc_server_batch_tuning(self._h, buf, len(buf)))
+        return json.loads(buf.value.decode())
 
     def close(self):
         if getattr(self, "_h", None):

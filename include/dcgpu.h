@@ -295,6 +295,10 @@ typedef struct dc_batch_stats {
 } dc_batch_stats;
 /* counters of the Krylov batch (all zero for a server created without the flag) */
 int dc_server_batch_stats(const dc_server* server, dc_batch_stats* out);
+/* the batch's launch-shape autotuner: per precision, the replay grid (blocks) it settled on
+ * for each batch size bucket, as JSON {"fp32": {"<tiles>": blocks, ...}, "fp64": {...}}
+ * ("{}" for a server created without the flag) */
+int dc_server_batch_tuning(const dc_server* server, char* buf, size_t len);
 int dc_server_submit(dc_server* server, const char* ini_text, const char* overrides, const double* init_state,
                      size_t n_init, int64_t* request_id);
 /* completed results, up to max; wait != 0 blocks until one is available (or none pending) */

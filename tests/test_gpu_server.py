@@ -161,6 +161,7 @@ def _run_server(dcgpu_lib, reqs, max_active, batch_krylov, overrides=None):
         assert res[rid]["status"] == 0, res[rid]
         states.append(srv.take_state(rid))
     stats = srv.batch_stats()
+    stats["tuned_grids"] = srv.batch_tuning()
     srv.close()
     return states, [res[rid] for rid in ids], stats
 
@@ -183,6 +184,9 @@ def test_batched_results_identical_alone_and_in_the_mix(dcgpu_lib, precision):
     assert 0 < stats["iterations"] <= sum(r["linear_iterations"] for r in results)
     assert stats["slot_replays"] >= stats["replays"]
     assert 1 <= stats["max_active"] <= len(reqs)
+    # the launch-shape autotuner settles on one of the captured grids per bucket it timed
+    for lane in stats["tuned_grids"].values():
+        assert all(g in (32, 128) or g % 4 == 0 for g in lane.values())
     unbatched, _, ustats = _run_server(dcgpu_lib, reqs, len(reqs), False, ov)
     assert ustats["solves"] == 0
     for k in range(len(reqs)):

@@ -440,48 +440,53 @@ struct Lane {
   };
   std::array<Bucket, kBuckets> tune{};
   cudaEvent_t tev[2] = {nullptr, nullptr};
-  int timed_bucket = -1, timed_graph = -1;  // the timed replay in flight
+  int timed_bucket = -1, timed_graph = -1, timed_tiles = 0;  // the timed replay in flight
 
   const BLane<T>* dev_header() const { return reinterpret_cast<const BLane<T>*>(table.get()); }
 
-  // graph index for a replay of nt tiles; sets timed_* when this replay is a tuning sample
+  // a candidate grid for t tiles: at most 64 tiles to a block (the largest grid always)
+  bool candidate(int i, int tiles) const {
+    return 64 * static_cast<int64_t>(graphs[i].first) >= tiles || i + 1 == static_cast<int>(graphs.size());
+  }
+
+  // graph index for a replay of `tiles` tiles; sets timed_* when this replay is a tuning
+  // sample (the least-sampled candidate of an untuned bucket)
   int pick_graph(int tiles) {
     int b = 0;
     while (b + 1 < kBuckets && (2 << b) <= tiles) ++b;
-    Bucket& k = tune[b];
+    const Bucket& k = tune[b];
     timed_bucket = timed_graph = -1;
     if (k.chosen >= 0) return k.chosen;
-    const int ng = static_cast<int>(graphs.size());
     int best = -1;
-    for (int i = 0; i < ng; ++i) {
-      const bool fits = 64 * static_cast<int64_t>(graphs[i].first) >= tiles || i == ng - 1;
-      if (fits && k.n[i] < kTuneSamples && (best < 0 || k.n[i] < k.n[best])) best = i;
-    }
-    if (best < 0) {
-      // every candidate has its samples: keep the fastest
-      double bm = 0.0;
-      for (int i = 0; i < ng; ++i)
-        if (k.n[i] > 0 && (k.chosen < 0 || k.ms[i] / k.n[i] < bm)) {
-          k.chosen = i;
-          bm = k.ms[i] / k.n[i];
-        }
-      return k.chosen;
-    }
+    for (int i = 0; i < static_cast<int>(graphs.size()); ++i)
+      if (candidate(i, tiles) && (best < 0 || k.n[i] < k.n[best])) best = i;
     timed_bucket = b;
     timed_graph = best;
+    timed_tiles = tiles;
     return best;
   }
 
-  // after the stream has been synchronised: books the timed replay's duration
+  // after the stream has been synchronised (under the batcher's mutex): books the timed
+  // replay's duration, and settles the bucket on its fastest candidate once every candidate
+  // has kTuneSamples samples
   void book_timing() {
     if (timed_bucket < 0) return;
+    Bucket& k = tune[timed_bucket];
     float ms = 0.0f;
     if (cudaEventElapsedTime(&ms, tev[0], tev[1]) == cudaSuccess) {
-      tune[timed_bucket].ms[timed_graph] += ms;
-      tune[timed_bucket].n[timed_graph] += 1;
+      k.ms[timed_graph] += ms;
+      k.n[timed_graph] += 1;
     } else {
       cudaGetLastError();  // an unreadable sample is dropped
     }
+    bool complete = true;
+    int best = -1;
+    for (int i = 0; i < static_cast<int>(graphs.size()); ++i) {
+      if (!candidate(i, timed_tiles)) continue;
+      if (k.n[i] < kTuneSamples) complete = false;
+      else if (best < 0 || k.ms[i] / k.n[i] < k.ms[best] / k.n[best]) best = i;
+    }
+    if (complete && best >= 0) k.chosen = best;
     timed_bucket = timed_graph = -1;
   }
 

@@ -33,7 +33,10 @@ namespace {
 
 constexpr int kTileRows = 256;  // block rows per tile = threads per block
 constexpr int kTileWarps = kTileRows / 32;
-constexpr int kChunk = 8;       // BiCGSTAB iterations per graph replay
+// BiCGSTAB iterations of the captured replays: a replay runs the shortest that covers the
+// iterations the instance closest to convergence is expected to need
+constexpr int kChunks[] = {2, 4, 8};
+constexpr int kNumChunks = 3;
 constexpr int kPhases = 5;      // kernels per iteration
 constexpr double kDoneMaxIt = 4.0;  // KS_DONE: max_it iterations ran without convergence
 
@@ -430,7 +433,14 @@ struct Lane {
   DeviceBuffer<double> sc, part;
   DeviceBuffer<unsigned int> cnt;
   double* h_sc = nullptr;
-  std::vector<std::pair<int, cudaGraphExec_t>> graphs;  // (grid, graph), ascending grid
+  struct GridGraphs {
+    int grid;
+    cudaGraphExec_t exec[kNumChunks];  // kChunks[c] iterations
+  };
+  std::vector<GridGraphs> graphs;  // ascending grid
+  // chunk length: running mean of the lane's solve lengths, and each slot's iterations so far
+  double mean_iters = 8.0;
+  std::vector<int> slot_iters;
 
   static constexpr int kBuckets = 24, kTuneSamples = 3, kMaxGrids = 3;
   struct Bucket {
@@ -441,12 +451,13 @@ struct Lane {
   std::array<Bucket, kBuckets> tune{};
   cudaEvent_t tev[2] = {nullptr, nullptr};
   int timed_bucket = -1, timed_graph = -1, timed_tiles = 0;  // the timed replay in flight
+  int timed_chunk = kChunks[kNumChunks - 1];                   // its iterations (times are per iteration)
 
   const BLane<T>* dev_header() const { return reinterpret_cast<const BLane<T>*>(table.get()); }
 
   // a candidate grid for t tiles: at most 64 tiles to a block (the largest grid always)
   bool candidate(int i, int tiles) const {
-    return 64 * static_cast<int64_t>(graphs[i].first) >= tiles || i + 1 == static_cast<int>(graphs.size());
+    return 64 * static_cast<int64_t>(graphs[i].grid) >= tiles || i + 1 == static_cast<int>(graphs.size());
   }
 
   // graph index for a replay of `tiles` tiles; sets timed_* when this replay is a tuning
@@ -474,7 +485,7 @@ struct Lane {
     Bucket& k = tune[timed_bucket];
     float ms = 0.0f;
     if (cudaEventElapsedTime(&ms, tev[0], tev[1]) == cudaSuccess) {
-      k.ms[timed_graph] += ms;
+      k.ms[timed_graph] += ms / timed_chunk;
       k.n[timed_graph] += 1;
     } else {
       cudaGetLastError();  // an unreadable sample is dropped
@@ -496,7 +507,7 @@ struct Lane {
     for (int b = 0; b < kBuckets; ++b)
       if (tune[b].chosen >= 0) {
         if (out.size() > 1) out += ", ";
-        out += "\"" + std::to_string(1 << b) + "\": " + std::to_string(graphs[tune[b].chosen].first);
+        out += "\"" + std::to_string(1 << b) + "\": " + std::to_string(graphs[tune[b].chosen].grid);
       }
     return out + "}";
   }
@@ -507,6 +518,7 @@ struct Lane {
     stream = s;
     slot.assign(slots, nullptr);
     fresh.assign(slots, 0);
+    slot_iters.assign(slots, 0);
     sc.resize(static_cast<size_t>(slots) * KS_COUNT);
     cnt.resize(slots);
     cuda_check(cudaMemsetAsync(cnt.get(), 0, slots * sizeof(unsigned int), stream), "memset");
@@ -519,7 +531,9 @@ struct Lane {
   }
 
   void drop_graphs() {
-    for (auto& g : graphs) cudaGraphExecDestroy(g.second);
+    for (auto& g : graphs)
+      for (auto& e : g.exec)
+        if (e) cudaGraphExecDestroy(e);
     graphs.clear();
   }
 
@@ -532,29 +546,43 @@ struct Lane {
     free_host(h_sc);
   }
 
-  // kChunk iterations of the five phases at each grid size (called with the stream idle)
+  // kChunks[c] iterations of the five phases at each grid size (called with the stream idle)
   void capture() {
     drop_graphs();
     const BLane<T>* L = dev_header();
     for (int grid : {32, 128, grid_full}) {
-      if (grid > grid_full || (!graphs.empty() && graphs.back().first >= grid)) continue;
-      cudaGraph_t g = nullptr;
-      cuda_check(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
-      for (int k = 0; k < kChunk; ++k) {
-        k_bt_p<T><<<grid, kTileRows, 0, stream>>>(L);
-        k_bt_rv<T><<<grid, kTileRows, 0, stream>>>(L);
-        k_bt_s<T><<<grid, kTileRows, 0, stream>>>(L);
-        k_bt_omega<T><<<grid, kTileRows, 0, stream>>>(L);
-        k_bt_xr<T><<<grid, kTileRows, 0, stream>>>(L);
+      if (grid > grid_full || (!graphs.empty() && graphs.back().grid >= grid)) continue;
+      GridGraphs gg{grid, {}};
+      graphs.push_back(gg);
+      for (int c = 0; c < kNumChunks; ++c) {
+        cudaGraph_t g = nullptr;
+        cuda_check(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+        for (int k = 0; k < kChunks[c]; ++k) {
+          k_bt_p<T><<<grid, kTileRows, 0, stream>>>(L);
+          k_bt_rv<T><<<grid, kTileRows, 0, stream>>>(L);
+          k_bt_s<T><<<grid, kTileRows, 0, stream>>>(L);
+          k_bt_omega<T><<<grid, kTileRows, 0, stream>>>(L);
+          k_bt_xr<T><<<grid, kTileRows, 0, stream>>>(L);
+        }
+        cuda_check(cudaStreamEndCapture(stream, &g), "cudaStreamEndCapture");
+        cuda_check(cudaGetLastError(), "batched BiCGSTAB capture");
+        const cudaError_t e = cudaGraphInstantiate(&graphs.back().exec[c], g, 0);
+        cudaGraphDestroy(g);
+        cuda_check(e, "cudaGraphInstantiate");
       }
-      cuda_check(cudaStreamEndCapture(stream, &g), "cudaStreamEndCapture");
-      cuda_check(cudaGetLastError(), "batched BiCGSTAB capture");
-      cudaGraphExec_t exec = nullptr;
-      const cudaError_t e = cudaGraphInstantiate(&exec, g, 0);
-      cudaGraphDestroy(g);
-      cuda_check(e, "cudaGraphInstantiate");
-      graphs.emplace_back(grid, exec);
     }
+  }
+
+  // chunk index of the next replay: the shortest captured length that covers the iterations
+  // the active instance closest to convergence is expected to need (the lane's mean solve
+  // length less the iterations it has run, at least one)
+  int pick_chunk() const {
+    double need = 1e30;
+    for (int k = 0; k < max_slots; ++k)
+      if (slot[k]) need = std::min(need, std::max(1.0, mean_iters - slot_iters[k]));
+    for (int c = 0; c < kNumChunks; ++c)
+      if (kChunks[c] >= need) return c;
+    return kNumChunks - 1;
   }
 
   // room for n tiles (run + init) in the table (called with the stream idle); the table
@@ -582,6 +610,7 @@ struct Lane {
       if (!slot[k]) {
         slot[k] = q;
         fresh[k] = 1;
+        slot_iters[k] = 0;
         return true;
       }
     return false;
@@ -652,11 +681,13 @@ struct Lane {
       cuda_check(cudaGetLastError(), "batched BiCGSTAB init");
       ++launched;
     }
+    const int ci = pick_chunk();
     const int gi = pick_graph(nt);
+    timed_chunk = kChunks[ci];
     if (timed_bucket >= 0) cuda_check(cudaEventRecord(tev[0], stream), "cudaEventRecord");
-    cuda_check(cudaGraphLaunch(graphs[gi].second, stream), "cudaGraphLaunch");
+    cuda_check(cudaGraphLaunch(graphs[gi].exec[ci], stream), "cudaGraphLaunch");
     if (timed_bucket >= 0) cuda_check(cudaEventRecord(tev[1], stream), "cudaEventRecord");
-    launched += static_cast<long long>(kChunk) * kPhases;
+    launched += static_cast<long long>(kChunks[ci]) * kPhases;
     cuda_check(cudaMemcpyAsync(h_sc, sc.get(), static_cast<size_t>(top) * KS_COUNT * sizeof(double),
                                cudaMemcpyDeviceToHost, stream), "download");
     return launched;
@@ -669,8 +700,10 @@ struct Lane {
       if (!q) continue;
       const double* s = h_sc + static_cast<int64_t>(k) * KS_COUNT;
       const double d = s[KS_DONE];
+      slot_iters[k] = static_cast<int>(s[KS_ITER]);
       if (d == 0.0) continue;
       q->iters = static_cast<int>(s[KS_ITER]);
+      mean_iters = 0.8 * mean_iters + 0.2 * q->iters;
       q->status = d == kDoneConverged ? 0 : (d == kDoneMaxIt ? 3 : 1);
       st.solves += 1;
       st.iterations += q->iters;

@@ -8,8 +8,8 @@
 // system it holds -- different meshes, block sizes and lengths -- into one set of tile
 // kernels: an instance is cut into tiles of 256 block rows, the tile table lists the tiles
 // of all instances, and each of the five phase kernels of a BiCGSTAB iteration walks that
-// table with a fixed grid.  Eight iterations are captured once as a CUDA graph whose
-// kernels read the table from device memory, so the same graph serves every batch
+// table with a fixed grid.  Runs of 2, 4 and 8 iterations are captured once as CUDA graphs
+// whose kernels read the table from device memory, so the same graphs serve every batch
 // composition.  Between replays the batcher retires the instances that converged (their
 // callers resume at once) and admits the systems that arrived meanwhile; new instances
 // join the running batch instead of waiting for it to drain.
@@ -47,7 +47,7 @@ struct BatchSystem {
 
 struct BatchStats {
   int64_t solves = 0;        // systems solved
-  int64_t replays = 0;       // graph replays (each 8 iterations of every active instance)
+  int64_t replays = 0;       // graph replays (2, 4 or 8 iterations of every active instance)
   int64_t slot_replays = 0;  // sum over replays of the instances active in them
   int64_t iterations = 0;    // BiCGSTAB iterations of all solved systems
   int32_t max_active = 0;    // most instances in one replay

@@ -275,8 +275,8 @@ int dc_server_create(int64_t budget_bytes, int32_t max_active, dc_server** out);
 /* dc_server_create with flags.  DC_SERVER_BATCH_KRYLOV: continuous batching of the running
  * simulations' block-Jacobi BiCGSTAB solves (fp64 solves and the fp32 corrections of the
  * mixed path): every such solve joins one batch whose five phase kernels walk a table of
- * 256-row tiles of all instances, replayed from one captured CUDA graph; instances join and
- * leave between replays of eight iterations.  Results do not depend on the mix (per-instance
+ * 256-row tiles of all instances, replayed from captured CUDA graphs of 2, 4 or 8
+ * iterations; instances join and leave between replays.  Results do not depend on the mix (per-instance
  * sums in a fixed order), but differ in rounding from the unbatched server's.  Other Krylov
  * methods and preconditioners stay on the simulation's own stream.  No counterpart in the
  * reference (one simulation per process; its LinearSolver solves one system at a time,
@@ -285,7 +285,7 @@ int dc_server_create(int64_t budget_bytes, int32_t max_active, dc_server** out);
 int dc_server_create_ex(int64_t budget_bytes, int32_t max_active, int32_t flags, dc_server** out);
 typedef struct dc_batch_stats {
   int64_t solves;        /* systems the batch solved */
-  int64_t replays;       /* graph replays (eight iterations of every active instance each) */
+  int64_t replays;       /* graph replays (2, 4 or 8 iterations of every active instance each) */
   int64_t slot_replays;  /* sum over replays of the instances active in them */
   int64_t iterations;    /* BiCGSTAB iterations of all solved systems */
   int32_t max_active;    /* most instances in one replay */

@@ -979,8 +979,12 @@ class OracleModel:
         for _sweep in range(8):
             if rn <= self.iterative_rtol * bn:
                 return z
-            dz, info = spla.bicgstab(J, res, rtol=max(1e-10, 0.1 * self.iterative_rtol * bn / rn), atol=0.0,
+            # the correction equation scaled to a unit right-hand side: scipy's breakdown test
+            # on rho = <rhat, r> is absolute (eps^2), and rho scales with |r|^2, so Newton's
+            # small late right-hand sides would otherwise break down before any progress
+            dz, info = spla.bicgstab(J, res / rn, rtol=max(1e-10, 0.1 * self.iterative_rtol * bn / rn), atol=0.0,
                                      maxiter=20000, M=M)
+            dz *= rn
             if not np.all(np.isfinite(dz)):
                 raise StepFailed("iterative linear solve produced non-finite values")
             z_new = z + dz

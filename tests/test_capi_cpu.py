@@ -211,3 +211,18 @@ def test_run_time_compilation_selftest(dcgpu_lib):
     every volume term kind, in 2D and 3D (no GPU needed)."""
     ok, msg = dcgpu_lib.jit_selftest()
     assert ok, msg
+
+
+def test_server_entry_points_check_arguments(dcgpu_lib):
+    """The batched-server entry points reject bad arguments before touching a device."""
+    lib = ctypes.CDLL(dcgpu_lib.LIB_PATH)
+    out = ctypes.c_void_p()
+    # unknown flag bits
+    assert lib.dc_server_create_ex(ctypes.c_int64(1 << 30), 4, 1 << 5, ctypes.byref(out)) == 6
+    assert out.value is None
+    # null handles and outputs
+    stats = dcgpu_lib.BatchStats()
+    assert lib.dc_server_batch_stats(None, ctypes.byref(stats)) == 6
+    buf = ctypes.create_string_buffer(64)
+    assert lib.dc_server_batch_tuning(None, buf, ctypes.c_size_t(len(buf))) == 6
+    assert lib.dc_server_create_ex(ctypes.c_int64(1 << 30), 4, 0, None) == 6

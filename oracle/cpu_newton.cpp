@@ -1109,14 +1109,21 @@ struct Stepper {
   }
 };
 
+// the host CPU: x86 "model name", or on Arm the implementer and part numbers (Neoverse V2,
+// the Grace core, is implementer 0x41 part 0xd4f)
 std::string cpu_name() {
   std::ifstream in("/proc/cpuinfo");
-  std::string line;
+  std::string line, implementer, part;
+  auto value = [&]() { return trim(line.substr(line.find(':') + 1)); };
   while (std::getline(in, line)) {
-    if (line.compare(0, 10, "model name") == 0 || line.compare(0, 9, "CPU part") == 0)
-      return trim(line.substr(line.find(':') + 1));
+    if (line.compare(0, 10, "model name") == 0) return value();
+    if (implementer.empty() && line.compare(0, 15, "CPU implementer") == 0) implementer = value();
+    if (part.empty() && line.compare(0, 8, "CPU part") == 0) part = value();
   }
-  return "";
+  if (part.empty()) return "";
+  std::string name = "CPU implementer " + implementer + " part " + part;
+  if (implementer == "0x41" && part == "0xd4f") name += " (Arm Neoverse V2)";
+  return name;
 }
 
 }  // namespace

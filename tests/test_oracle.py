@@ -401,3 +401,22 @@ def test_gmsh_grid_and_physical_compartments(tmp_path, dim):
     assert np.array_equal(om.comp_mask[0], phys == 1) and np.array_equal(om.comp_mask[1], phys == 2)
     x, t, *_ = om.run()
     assert t == pytest.approx(0.2) and np.all(np.isfinite(x))
+
+
+@pytest.mark.parametrize("scale", [1.0, 1e-10, 1e-14])
+def test_iterative_solve_scale_invariant(scale):
+    """The oracle's iterative stand-in for the direct solve reaches a relative residual of
+    1e-13 whatever the size of the right-hand side: Newton's late right-hand sides are tiny,
+    and an unscaled solve broke down in scipy's absolute test on rho = <rhat, r>."""
+    import scipy.sparse as sp
+    ini = ("[grid]\ncells = 4 4\n[compartments.d]\nexpression = 1\n"
+           "[model.scalar_field.u]\ncompartment = d\ncross_diffusion.u.expression = 0.01\n")
+    om = OracleModel(ini, linear="iterative")
+    rng = np.random.default_rng(7)
+    n = 400
+    A = sp.random(n, n, density=0.02, random_state=11, format="csr")
+    J = (A + A.T) * 0.1 + sp.diags(2.0 + rng.random(n))
+    r = rng.standard_normal(n) * scale
+    z = om._solve_iterative(J.tocsr(), r)
+    assert np.linalg.norm(r - J @ z) <= 1e-13 * np.linalg.norm(r)
+    assert np.allclose(z / scale, om._solve_iterative(J.tocsr(), r / scale), rtol=1e-10, atol=1e-14)
